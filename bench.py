@@ -1,0 +1,394 @@
+#!/usr/bin/env python3
+"""Headline benchmark of tdbem-gb300: DOF*steps/s of a full transient solve.
+
+A bench step is one pass of the hot path over the workload: assembly of every
+G^k/H^k level (collocation node x element x level quadrature) followed by the
+whole time march (history convolution + H^0 solve for every step).  Default
+workload: spherical cavity of radius 1 in a full space, 6x16x16 cubed-sphere
+quads (1536 elements, 1538 nodes, 4614 DOF), uniform step pressure, mu = 1,
+nu = 0.25, rho = 1, dt = 0.6 h / c_p, 400 steps, alpha = (0.25, 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+    python bench.py --impl reference ...   (the reference's algorithm on the host cores)
+
+Multi-GPU runs (torchrun, one process per GPU) are independent replicas of the
+workload (the path does not shard): value = total DOF*steps of all ranks / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "td-bem_gb300"))
+
+import numpy as np  # noqa: E402
+
+ALPHA = (0.25, 0.0)
+WORKLOADS = {
+    "sphere_6x16x16": dict(kind="sphere", n=16, numstep=400),
+    "sphere_6x24x24": dict(kind="sphere", n=24, numstep=500),
+    "sphere_6x8x8": dict(kind="sphere", n=8, numstep=200),
+    "bar_1x1x4_q2": dict(kind="bar", numstep=200),
+}
+METRIC = "DOF*steps/s"
+
+
+def make_model(name):
+    from tdbem import meshes
+    w = WORKLOADS[name]
+    if w["kind"] == "sphere":
+        return meshes.cubed_sphere(w["n"], numstep=w["numstep"])
+    return meshes.bar(1, 1, 4, per_unit=2, numstep=w["numstep"])
+
+
+# --------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# --------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        loaded = [x for x in sm if smax and x > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the reference's algorithm (the oracle restatement) on a sample
+# --------------------------------------------------------------------------
+def cpu_sample(model, M, numstep, a1, a2, nthreads):
+    """Estimate the reference CPU path's time for the whole workload from a bounded sample.
+
+    assembly: ElastoDynamicsT::G_H_Driver on the first R collocation rows at a mid step
+      (its cost does not depend on the step), scaled to all rows and M steps;
+    marching: Solve_Averaging steps at full size D on a synthetic level store (dense
+      random levels, diagonal level 0/1 so the LHS factorisation is cheap) with 2 and 5
+      levels, giving the per-step cost c0 + c1 * (level terms); summed over the
+      workload's steps with the reference's level-term count;
+    LU: the KSPSolve stand-in's dense LU timed at n = 2000 and scaled by (D/2000)^3,
+      once per distinct LHS."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    D = model.ndof
+    o = oracle.Oracle(model, nthreads=nthreads)
+    R = min(model.nnd, 4 * nthreads)
+    t0 = time.perf_counter()
+    o.gh_driver(max(1, M // 2) * model.dt, model.dt, 0, R - 1)
+    t_rows = time.perf_counter() - t0
+    t_asm = t_rows * (model.nnd / R) * M
+
+    rng = np.random.default_rng(0)
+
+    def march_cost(m_s, steps):
+        G = rng.standard_normal((m_s + 1, D, D)) * 1e-3
+        H = rng.standard_normal((m_s + 1, D, D)) * 1e-3
+        for k in (0, 1):
+            H[k] = np.diag(1.0 + rng.random(D))
+        u = np.zeros((steps + 2, D))
+        t = np.zeros((steps + 2, D))
+        ubc = np.zeros(0, np.int32)
+        fbc = np.arange(D, dtype=np.int32)
+        fv = np.ones(D)
+        t0 = time.perf_counter()
+        oracle.march_range(D, m_s, G, H, ubc, np.zeros(0), fbc, fv, a1, a2, 2, steps, u, t,
+                           nthreads=nthreads)
+        return time.perf_counter() - t0
+
+    def terms(s, m):
+        """Level-term pairs of Solve_Averaging at solve step s (SolverStepLinearT.cpp:408-482)."""
+        if s < 2:
+            return 0
+        return 1 + max(0, min(s + 1, m) - 2) + max(0, min(s - 1, m)) + max(0, min(s - 2, m) + 1)
+
+    m_a, m_b, n_a, n_b = 2, 5, 9, 13
+    ta = march_cost(m_a, n_a)
+    tb = march_cost(m_a, n_b)
+    tc = march_cost(m_b, n_a)
+    td = march_cost(m_b, n_b)
+    per_a = (tb - ta) / (n_b - n_a)  # saturated steps: 3*m term pairs
+    per_b = (td - tc) / (n_b - n_a)
+    c1 = max(0.0, (per_b - per_a) / (terms(40, m_b) - terms(40, m_a)))
+    c0 = max(0.0, per_a - c1 * terms(40, m_a))
+    t_march = sum(c0 + c1 * terms(s, M) for s in range(1, numstep))
+    n_lu = 2 if a1 != 0 or a2 != 0 else 1
+    A = rng.standard_normal((2000, 2000))
+    t0 = time.perf_counter()
+    oracle.lu_factor(A, nthreads)
+    t_lu = (time.perf_counter() - t0) * (D / 2000.0) ** 3 * n_lu
+    total = t_asm + t_march + t_lu
+    return {"seconds": total, "assembly_s": t_asm, "march_s": t_march, "lu_s": t_lu,
+            "value": D * numstep / total,
+            "sample": (f"G_H_Driver on {R} of {model.nnd} rows at one step scaled to all rows "
+                       f"x {M} steps; Solve_Averaging steps at D={D} on synthetic {m_a}- and "
+                       f"{m_b}-level stores fitted to c0+c1*terms and summed over {numstep} "
+                       f"steps; dense LU timed at n=2000 scaled by (D/2000)^3 x {n_lu}")}
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return 0
+    model = make_model(args.workload)
+    M = model.max_step()
+    nthreads = os.cpu_count() or 1
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(model, M, model.numstep, *ALPHA, nthreads)
+        if i >= args.warmup:
+            vals.append(r["value"])
+            last = r
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * model.ndof * model.numstep / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "dof": model.ndof, "steps": model.numstep,
+                       "max_step": M, "alpha": list(ALPHA), "precision": "fp64"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
+                             "sample": last["sample"]},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "estimate_seconds": {k: last[k] for k in ("assembly_s", "march_s", "lu_s")}}
+    print(json.dumps(line))
+    return 0
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def run_ours(args, dist):
+    import torch
+    from tdbem import lib
+
+    dev = dist.local if dist.world > 1 else 0
+    torch.cuda.set_device(dev)
+    torch.cuda.init()
+    lib.load()
+    prec = lib.FP64 if args.precision == "fp64" else lib.MIXED
+    model = make_model(args.workload)
+    D, nsteps = model.ndof, model.numstep
+    ctx = lib.Context(model)
+    ctx.set_alpha(*ALPHA)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def job():
+        ctx.assemble(precision=prec)
+        ctx.march(to_host=False)
+
+    for _ in range(args.warmup):
+        job()
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    n0 = ctx.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        job()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - n0
+    ms_total = dist.max(e0.elapsed_time(e1))
+    ms_step = ms_total / args.steps
+    value = D * nsteps * args.steps * dist.world / (ms_total / 1000.0)
+
+    # untimed profiling pass: per-kernel-class device time and algorithmic units
+    ctx.set_profiling(True)
+    job()
+    stats = ctx.kernel_stats()
+    ctx.set_profiling(False)
+    phase = ctx.timings()
+
+    # end to end through the C ABI with host buffers (create/copy in, solve, copy out)
+    e2e_times = []
+    h2d = model.coords.nbytes + model.ien.astype(np.int32).nbytes + \
+        model.fbc_dofs.nbytes + model.fbc_vals.nbytes + model.ubc_dofs.nbytes + \
+        model.ubc_vals.nbytes
+    d2h = 2 * (nsteps + 1) * D * 8
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with lib.Context(model) as c2:
+            c2.set_alpha(*ALPHA)
+            c2.assemble(precision=prec)
+            c2.march()
+        t1 = time.perf_counter()
+        e2e_times.append(t1 - t0)
+    e2e_s = dist.max(statistics.median(e2e_times))
+    e2e_value = D * nsteps * dist.world / e2e_s
+    ctx.close()
+
+    if dist.rank != 0:
+        return 0
+    peaks, peak_kind = measured_peaks()
+    traffic = ncu_traffic()
+    dom = max(stats, key=lambda k: stats[k]["ms"])
+    st = stats[dom]
+    if dom == "conv":
+        achieved = st["bytes"] / (st["ms"] / 1e3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_conv", "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "peak_source": f"hbm_gbs of {peak_kind}"}
+    else:
+        achieved = st["flops"] / (st["ms"] / 1e3) / 1e12
+        fp64 = peaks.get("fp64_tflops")
+        roof = {"bound": "fp64" if prec == lib.FP64 else "fp32", "kernel": "k_assemble_items",
+                "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+                "frac": (achieved / fp64) if fp64 else None,
+                "peak_source": "fp64_tflops of measured" if fp64 else "no measured FP64 peak"}
+    roof["launches"] = st["launches"]
+    roof["avg_launch_ms"] = st["ms"] / max(1, st["launches"])
+    t = traffic.get(f"{args.workload}:{args.precision}:{dom}")
+    roof["traffic"] = t
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == lib.FP64 else "f32+f64", "data": "synthetic",
+            "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": ctx.M,
+                       "alpha": list(ALPHA), "precision": args.precision,
+                       "parallelism": f"replicas{dist.world}",
+                       "l2": "inputs larger than L2: the level store is "
+                             f"{ctx.level_bytes(prec) / 1e9:.1f} GB"},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "roofline": roof,
+            "phases_ms": phase,
+            "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                            "share": v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values()))}
+                        for k, v in stats.items()},
+            "clocks": clk}
+    if dist.world == 1 and not args.no_cpu_baseline:
+        r = cpu_sample(model, ctx.M, nsteps, *ALPHA, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
+                                "kind": "port", "sample": r["sample"]}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere_6x16x16")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,177 @@
+/*
+ * tdbem.h -- C ABI of tdbem-gb300, the GB300 (sm_103a) implementation of the
+ * TD-BEM time-domain elastodynamic boundary-element hot path:
+ *
+ *   (a) assembly of the G^k / H^k influence-matrix levels (collocation node x
+ *       element x time level quadrature of the time-integrated Stokes kernel
+ *       with linear temporal shape functions, Duffy-transformed singular
+ *       elements, Kelvin-traction regularisation), and
+ *   (b) time marching: the history convolution sum_k (G^k t^{n-k} - H^k u^{n-k})
+ *       followed by the H^0 solve, with the reference's weighted collocation
+ *       (alpha_1, alpha_2).
+ *
+ * Plain pointers and sizes only.  Every call returns a status (0 = OK, < 0 =
+ * error kind below); tdbem_last_error() gives the message of the last failure
+ * on the calling thread.  A context is bound to one CUDA device and one
+ * stream; calls on one context must not overlap (the host API is not
+ * re-entrant per context), different contexts may be used from different
+ * threads.  There is no CPU fallback: without a usable CUDA device
+ * tdbem_ctx_create fails with TDBEM_ERR_CUDA.
+ *
+ * Index conventions follow the reference: node ids and dof ids are 0-based,
+ * dof = 3*node + direction, matrices are row-major with row = collocation dof
+ * and column = field dof (ElastoDynamicsT.cpp:235-259).
+ */
+#ifndef TDBEM_H
+#define TDBEM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------- */
+#define TDBEM_OK 0
+#define TDBEM_ERR_ARG (-1)         /* invalid argument (size, index, range)   */
+#define TDBEM_ERR_CUDA (-2)        /* CUDA runtime failure / no device        */
+#define TDBEM_ERR_NOMEM (-3)       /* device or host allocation failed         */
+#define TDBEM_ERR_SINGULAR (-4)    /* zero pivot in the H^0 factorisation      */
+#define TDBEM_ERR_UNSUPPORTED (-5) /* valid input this build does not support  */
+#define TDBEM_ERR_STATE (-6)       /* call out of order (e.g. march before assembly) */
+
+/* ---- precision of the assembled levels and of the marching ---------- */
+#define TDBEM_FP64 0  /* the reference's method in FP64 (plain form)         */
+#define TDBEM_MIXED 1 /* FP32 far field / FP32 levels, FP64 near field + solve */
+
+typedef struct tdbem_ctx tdbem_ctx;
+
+/* Surface mesh; arrays are copied at tdbem_ctx_create.
+ * Replaces ModelManagerT::GetNND/GetNEL/GetElementType/GetIEN/GetCoords
+ * (ModelManagerT.h:46-68). */
+typedef struct {
+    int nnd;              /* number of nodes                                  */
+    int nel;              /* number of elements                               */
+    int etype;            /* 1 = 4-node bilinear quad (8-node: UNSUPPORTED)   */
+    const double* coords; /* nnd x 3                                          */
+    const int* ien;       /* nel x 4, 0-based node ids                        */
+} tdbem_mesh;
+
+/* Replaces ModelManagerT::GetMaterialConstants (ModelManagerT.h:92). */
+typedef struct {
+    double E;   /* Young's modulus  */
+    double nu;  /* Poisson's ratio  */
+    double rho; /* density          */
+} tdbem_material;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* tdbem_last_error(void);
+
+/* Library version string. */
+const char* tdbem_version(void);
+
+/* Create a context on the current CUDA device: copies the mesh, computes
+ * MaxStep exactly as SolverT::ComputeMaxStep (SolverT.cpp:211-250), colours
+ * the elements for deterministic assembly.  nq = Gauss points per direction
+ * (6, 10, 20 or 40; ShapeFunctionT.cpp:71-169); if_ext != 0 adds the exterior
+ * free term 0.5*dt at the first step (ElastoDynamicsT.cpp:212-225).
+ * Replaces the constructors of ModelManagerT / ElastoDynamicsT / SolverT
+ * (main.cpp:43-57). */
+int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double dt, int nq,
+                     int if_ext, tdbem_ctx** out);
+int tdbem_ctx_destroy(tdbem_ctx* ctx);
+
+/* MaxStep M (SolverT::GetMaxStep, SolverT.cpp:252-255); levels are 0..M. */
+int tdbem_max_step(const tdbem_ctx* ctx, int* M);
+/* Number of dofs D = 3*nnd. */
+int tdbem_num_dof(const tdbem_ctx* ctx, int* D);
+/* The CUDA stream (cudaStream_t) all work of this context is ordered on. */
+int tdbem_get_stream(const tdbem_ctx* ctx, void** stream);
+
+/* ---- (a) assembly --------------------------------------------------- */
+
+/* One call of ElastoDynamicsT::G_H_Driver(t = step*dt, t_1 = dt) followed by
+ * GetGHLinear (ElastoDynamicsT.cpp:108-231, 283-289) for collocation rows
+ * node_lo..node_hi (inclusive; the reference's SetLowerUpper range).
+ * G_I/G_J/H_I/H_J are host buffers of (3*(node_hi-node_lo+1)) x D doubles:
+ * the I part (fG_1/fH_1) and J part (fG_2/fH_2) of the step response at that
+ * time, C term and exterior free term included at step 1.  FP64. */
+int tdbem_gh_driver(tdbem_ctx* ctx, int step, int node_lo, int node_hi, double* G_I,
+                    double* G_J, double* H_I, double* H_J);
+
+/* Assemble the device-resident level store G^k, H^k for k = 0..M: the result
+ * of main()'s steps 1..min(M, nsteps) of G_H_Driver + UpdateGHLinear
+ * (main.cpp:89-121, SolverStepLinearT.cpp:58-97): level 0 = J(dt), level k =
+ * I(k dt) + J((k+1) dt), level M = I(M dt).  precision: TDBEM_FP64 or
+ * TDBEM_MIXED. */
+int tdbem_assemble_levels(tdbem_ctx* ctx, int nsteps, int precision);
+
+/* Copy level k of G (which = 0) or H (which = 1) to host (D x D doubles).
+ * FP32 levels are widened to double. */
+int tdbem_get_level(tdbem_ctx* ctx, int k, int which, double* host_out);
+
+/* ---- (b) marching --------------------------------------------------- */
+
+/* Boundary conditions (ModelManagerT::SetBCs, ModelManagerT.cpp:337-354):
+ * prescribed displacement values on ubc dofs, traction values on fbc dofs. */
+int tdbem_set_bc(tdbem_ctx* ctx, const int* ubc_dofs, const double* ubc_vals, int n_u,
+                 const int* fbc_dofs, const double* fbc_vals, int n_f);
+
+/* Weighted-collocation weights (alpha.txt, main.cpp:78-81); range checked as
+ * SolverStepLinearT::Solve_Averaging (SolverStepLinearT.cpp:317-322). */
+int tdbem_set_alpha(tdbem_ctx* ctx, double a1, double a2);
+
+/* Load amplitude per step: amp[s] multiplies the traction values at step s
+ * (time s*dt).  Without a call the reference's Heaviside amp = 1 is used
+ * (SolverT::LoadTimeVariation, SolverT.cpp:379-394).  nsteps values. */
+int tdbem_set_load_history(tdbem_ctx* ctx, const double* amp, int nsteps);
+
+/* March numstep steps of main()'s loop (SetLoad + Solve(a1,a2),
+ * SolverT.cpp:344-377, SolverStepLinearT.cpp:314-544) on the assembled
+ * levels.  u_hist / t_hist: host buffers of (numstep+1) x D doubles receiving
+ * fDis_DB / fTrac_DB[0..numstep] (entry numstep stays 0 as in the reference),
+ * or NULL to keep the histories on the device only. */
+int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
+
+/* Device pointers of the histories of the last tdbem_march (FP64,
+ * (numstep+1) x D each); valid until the next march or destroy. */
+int tdbem_history_device(const tdbem_ctx* ctx, const double** u_hist, const double** t_hist);
+
+/* ---- level store export / import (checkpoint) ----------------------- */
+
+/* Device bytes the level store of this context takes at a precision. */
+int tdbem_level_bytes(const tdbem_ctx* ctx, int precision, size_t* bytes);
+
+/* Timing of the phases of the last assemble / march, in milliseconds of
+ * device time (CUDA events on the context stream): [0] assembly,
+ * [1] H^0 factorisation, [2] marching steps.  */
+int tdbem_last_timings(const tdbem_ctx* ctx, double* ms3);
+
+/* ---- profiling ------------------------------------------------------ */
+
+/* Kernel classes for tdbem_kernel_stats. */
+#define TDBEM_K_ASSEMBLE 0 /* level quadrature items (FP64 or FP32 pipe)      */
+#define TDBEM_K_CONV 1     /* history convolution over the stored levels (HBM) */
+#define TDBEM_K_FACTOR 2   /* H^0 inverse (Gauss-Jordan)                       */
+#define TDBEM_K_SOLVE 3    /* per-step solve and state update                  */
+#define TDBEM_K_COUNT 4
+
+/* With on != 0, every launch of the kernel classes above is bracketed by CUDA
+ * events on the context stream and its algorithmic bytes / flops are counted
+ * (adds event overhead; off by default).  Resets the counters. */
+int tdbem_set_profiling(tdbem_ctx* ctx, int on);
+
+/* Accumulated launches, device milliseconds, algorithmic bytes moved and
+ * algorithmic floating-point operations of one kernel class since profiling
+ * was switched on. */
+int tdbem_kernel_stats(const tdbem_ctx* ctx, int kclass, long long* launches, double* ms,
+                       double* bytes, double* flops);
+
+/* Number of CUDA kernels this context has launched so far. */
+int tdbem_launch_count(const tdbem_ctx* ctx, long long* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TDBEM_H */

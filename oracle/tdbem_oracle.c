@@ -1,0 +1,902 @@
+/*
+ * tdbem_oracle.c -- CPU oracle for the TD-BEM hot path (TEST INFRASTRUCTURE).
+ *
+ * Plain-C restatement of the reference's algorithm.  Each function names the
+ * reference file:line it follows; arithmetic is written in the reference's
+ * order (pow, left-to-right sums, the same temporaries) so that, compiled
+ * with -ffp-contract=off, it reproduces the reference bit for bit on the
+ * golden inputs.  Parallelism (OpenMP over collocation rows) mirrors the
+ * reference's MPI row split and does not change any sum order.
+ *
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * call this code.
+ */
+#include "tdbem_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Gauss tables: ShapeFunctionT::SetNQ (ShapeFunctionT.cpp:71-169).     */
+/* The 20-point abscissa table keeps the reference's missing minus sign */
+/* on entry 19 (ShapeFunctionT.cpp:121).                                */
+/* ------------------------------------------------------------------ */
+static const double GX6[6] = {0.6612093864662645, -0.6612093864662645, -0.2386191860831969,
+                              0.2386191860831969, -0.9324695142031521, 0.9324695142031521};
+static const double GW6[6] = {0.3607615730481386, 0.3607615730481386, 0.4679139345726910,
+                              0.4679139345726910, 0.1713244923791704, 0.1713244923791704};
+static const double GX10[10] = {-0.148874339, 0.148874339, -0.433395394, 0.433395394,
+                                -0.679409568, 0.679409568, -0.865063367, 0.865063367,
+                                -0.973906529, 0.973906529};
+static const double GW10[10] = {0.295524225, 0.295524225, 0.269266719, 0.269266719,
+                                0.219086363, 0.219086363, 0.149451349, 0.149451349,
+                                0.066671344, 0.066671344};
+static const double GX20[20] = {-0.076526521, 0.076526521, -0.227785851, 0.227785851,
+                                -0.373706089, 0.373706089, -0.510867002, 0.510867002,
+                                -0.636053681, 0.636053681, -0.746331906, 0.746331906,
+                                -0.839116972, 0.839116972, -0.912234428, 0.912234428,
+                                -0.963971927, 0.963971927, 0.993128599, 0.993128599};
+static const double GW20[20] = {0.152753387, 0.152753387, 0.149172986, 0.149172986,
+                                0.142096109, 0.142096109, 0.131688638, 0.131688638,
+                                0.118194532, 0.118194532, 0.10193012,  0.10193012,
+                                0.083276742, 0.083276742, 0.062672048, 0.062672048,
+                                0.04060143,  0.04060143,  0.017614007, 0.017614007};
+static const double GX40[40] = {
+    -0.0387724175060508, 0.0387724175060508, -0.1160840706752552, 0.1160840706752552,
+    -0.1926975807013711, 0.1926975807013711, -0.2681521850072537, 0.2681521850072537,
+    -0.3419940908257585, 0.3419940908257585, -0.4137792043716050, 0.4137792043716050,
+    -0.4830758016861787, 0.4830758016861787, -0.5494671250951282, 0.5494671250951282,
+    -0.6125538896679802, 0.6125538896679802, -0.6719566846141796, 0.6719566846141796,
+    -0.7273182551899271, 0.7273182551899271, -0.7783056514265194, 0.7783056514265194,
+    -0.8246122308333117, 0.8246122308333117, -0.8659595032122595, 0.8659595032122595,
+    -0.9020988069688743, 0.9020988069688743, -0.9328128082786765, 0.9328128082786765,
+    -0.9579168192137917, 0.9579168192137917, -0.9772599499837743, 0.9772599499837743,
+    -0.9907262386994570, 0.9907262386994570, -0.9982377097105593, 0.9982377097105593};
+static const double GW40[40] = {
+    0.0775059479784248, 0.0775059479784248, 0.0770398181642480, 0.0770398181642480,
+    0.0761103619006262, 0.0761103619006262, 0.0747231690579683, 0.0747231690579683,
+    0.0728865823958041, 0.0728865823958041, 0.0706116473912868, 0.0706116473912868,
+    0.0679120458152339, 0.0679120458152339, 0.0648040134566010, 0.0648040134566010,
+    0.0613062424929289, 0.0613062424929289, 0.0574397690993916, 0.0574397690993916,
+    0.0532278469839368, 0.0532278469839368, 0.0486958076350722, 0.0486958076350722,
+    0.0438709081856733, 0.0438709081856733, 0.0387821679744720, 0.0387821679744720,
+    0.0334601952825478, 0.0334601952825478, 0.0279370069800234, 0.0279370069800234,
+    0.0222458491941670, 0.0222458491941670, 0.0164210583819079, 0.0164210583819079,
+    0.0104982845311528, 0.0104982845311528, 0.0045212770985332, 0.0045212770985332};
+
+static int gauss_table(int nq, const double** x, const double** w) {
+    switch (nq) {
+    case 6: *x = GX6; *w = GW6; return 0;
+    case 10: *x = GX10; *w = GW10; return 0;
+    case 20: *x = GX20; *w = GW20; return 0;
+    case 40: *x = GX40; *w = GW40; return 0;
+    default: return -1;
+    }
+}
+
+/* MathOperationT::VecNormal (MathOperationT.cpp:345-359). */
+static double vec_normal3(const double* v) {
+    double s = 0;
+    for (int i = 0; i < 3; i++) s += pow(v[i], 2);
+    return sqrt(s);
+}
+
+/* ------------------------------------------------------------------ */
+/* ShapeFunctionT::Evaluate(eta_1, eta_2) (ShapeFunctionT.cpp:236-366)  */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    double N[8];
+    double x[3];
+    double n[3]; /* unit outward normal */
+    double J;
+} shape_pt;
+
+static void shape_eval(int etype, const double* c, double e1, double e2, shape_pt* s) {
+    double DN[16];
+    int ennd;
+    if (etype == 1) {
+        ennd = 4;
+        s->N[0] = 0.25 * (1 - e1) * (1 - e2);
+        s->N[1] = 0.25 * (1 + e1) * (1 - e2);
+        s->N[2] = 0.25 * (1 + e1) * (1 + e2);
+        s->N[3] = 0.25 * (1 - e1) * (1 + e2);
+        DN[0] = -0.25 * (1 - e2);
+        DN[1] = 0.25 * (1 - e2);
+        DN[2] = 0.25 * (1 + e2);
+        DN[3] = -0.25 * (1 + e2);
+        DN[4] = -0.25 * (1 - e1);
+        DN[5] = -0.25 * (1 + e1);
+        DN[6] = 0.25 * (1 + e1);
+        DN[7] = 0.25 * (1 - e1);
+    } else {
+        ennd = 8;
+        s->N[0] = 0.25 * (1 - e1) * (1 - e2) * (-e1 - e2 - 1);
+        s->N[1] = 0.25 * (1 + e1) * (1 - e2) * (e1 - e2 - 1);
+        s->N[2] = 0.25 * (1 + e1) * (1 + e2) * (e1 + e2 - 1);
+        s->N[3] = 0.25 * (1 - e1) * (1 + e2) * (-e1 + e2 - 1);
+        s->N[4] = 0.5 * (1 - pow(e1, 2)) * (1 - e2);
+        s->N[5] = 0.5 * (1 + e1) * (1 - pow(e2, 2));
+        s->N[6] = 0.5 * (1 - pow(e1, 2)) * (1 + e2);
+        s->N[7] = 0.5 * (1 - e1) * (1 - pow(e2, 2));
+        DN[0] = -0.25 * (1 - e1) * (1 - e2) - 0.25 * (1 - e2) * (-1 - e1 - e2);
+        DN[1] = 0.25 * (1 + e1) * (1 - e2) + 0.25 * (1 - e2) * (-1 + e1 - e2);
+        DN[2] = 0.25 * (1 + e1) * (1 + e2) + 0.25 * (1 + e2) * (-1 + e1 + e2);
+        DN[3] = -0.25 * (1 - e1) * (1 + e2) - 0.25 * (1 + e2) * (-1 - e1 + e2);
+        DN[4] = -e1 * (1 - e2);
+        DN[5] = 0.5 * (1 - pow(e2, 2));
+        DN[6] = -e1 * (1 + e2);
+        DN[7] = -0.5 * (1 - pow(e2, 2));
+        DN[8] = -0.25 * (1 - e1) * (1 - e2) - 0.25 * (1 - e1) * (-1 - e1 - e2);
+        DN[9] = -0.25 * (1 + e1) * (1 - e2) - 0.25 * (1 + e1) * (-1 + e1 - e2);
+        DN[10] = 0.25 * (1 + e1) * (1 + e2) + 0.25 * (1 + e1) * (-1 + e1 + e2);
+        DN[11] = 0.25 * (1 - e1) * (1 + e2) + 0.25 * (1 - e1) * (-1 - e1 + e2);
+        DN[12] = -0.5 * (1 - pow(e1, 2));
+        DN[13] = -(1 + e1) * e2;
+        DN[14] = 0.5 * (1 - pow(e1, 2));
+        DN[15] = -(1 - e1) * e2;
+    }
+    s->x[0] = s->x[1] = s->x[2] = 0;
+    for (int a = 0; a < ennd; a++)
+        for (int d = 0; d < 3; d++) s->x[d] += s->N[a] * c[a * 3 + d];
+    double dx1[3] = {0, 0, 0}, dx2[3] = {0, 0, 0};
+    for (int a = 0; a < ennd; a++)
+        for (int d = 0; d < 3; d++) {
+            dx1[d] += DN[a] * c[a * 3 + d];
+            dx2[d] += DN[a + ennd] * c[a * 3 + d];
+        }
+    /* MathOperationT::VecCross (MathOperationT.cpp:244-250) */
+    s->n[0] = dx1[1] * dx2[2] - dx1[2] * dx2[1];
+    s->n[1] = dx1[2] * dx2[0] - dx1[0] * dx2[2];
+    s->n[2] = dx1[0] * dx2[1] - dx1[1] * dx2[0];
+    s->J = vec_normal3(s->n);
+    for (int d = 0; d < 3; d++) s->n[d] /= s->J;
+}
+
+/* ------------------------------------------------------------------ */
+/* Green's function, type 4 path (GreenFunctionT.cpp)                   */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    double E, nu, mu, rho, cp, cs;
+    double rv[3], r, n[3];
+    double T, T1;
+} green;
+
+/* GreenFunctionT::SetMaterial + WaveSpeed (GreenFunctionT.cpp:76-93). */
+static void green_material(green* g, double E, double nu, double rho) {
+    g->E = E;
+    g->nu = nu;
+    g->rho = rho;
+    g->mu = E / (2 * (1 + nu));
+    double L = E * nu / ((1 + nu) * (1 - 2 * nu));
+    g->cp = sqrt((L + 2 * g->mu) / rho);
+    g->cs = sqrt(g->mu / rho);
+}
+
+/* GreenFunctionT::SetSpatial (GreenFunctionT.cpp:95-109). */
+static void green_spatial(green* g, const double* dir, const double* nrm) {
+    g->r = vec_normal3(dir);
+    for (int i = 0; i < 3; i++) g->rv[i] = dir[i] / g->r;
+    double R = vec_normal3(nrm);
+    for (int i = 0; i < 3; i++) g->n[i] = nrm[i] / R;
+}
+
+static double dot3(const double* a, const double* b) {
+    double d = 0;
+    for (int i = 0; i < 3; i++) d += a[i] * b[i];
+    return d;
+}
+
+/* GreenFunctionT::Kelvin_Linear (GreenFunctionT.cpp:205-231). */
+static void green_kelvin_linear(const green* g, double* K) {
+    double rdn = dot3(g->rv, g->n);
+    double divider = -(8 * M_PI) * (1 - g->nu) * g->r * g->r;
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) {
+            int dik = (i == k);
+            double rirk = g->rv[i] * g->rv[k];
+            double rink = g->rv[i] * g->n[k];
+            double rkni = g->rv[k] * g->n[i];
+            double v = ((1 - 2 * g->nu) * dik + 3 * rirk) * rdn - (1 - 2 * g->nu) * (rkni - rink);
+            v /= divider;
+            v *= 0.5 * g->T1;
+            K[i * 3 + k] = v;
+        }
+}
+
+/* GreenFunctionT::Stokes_Heaviside_Linear (GreenFunctionT.cpp:241-416) at time T. */
+static void green_heaviside_linear(const green* g, double T, double* DU1, double* DU2,
+                                   double* DT1, double* DT2) {
+    const double T1 = g->T1, R = g->r, cp = g->cp, cs = g->cs;
+    double I1, I2, I3, I4, I5, I6, J1, J2, J3, J4, J5, J6, b;
+
+    double t_ref = T - R / cp;
+    if (T1 <= t_ref) { b = T1; I5 = 0; J5 = 0; }
+    else if (0 <= t_ref && T1 > t_ref) { b = t_ref; I5 = (T1 - t_ref) / T1; J5 = t_ref / T1; }
+    else { b = 0; I5 = 0; J5 = 0; }
+    I1 = (-3 * pow(b, 4) + (8 * T + 4 * T1) * pow(b, 3) - (6 * pow(T, 2) + 12 * T * T1) * pow(b, 2) +
+          12 * T1 * pow(T, 2) * b) / (12 * pow(R, 2)) -
+         (T1 * b - pow(b, 2) / 2.0) / pow(cp, 2);
+    I1 = I1 / T1;
+    J1 = -(-3 * pow(b, 4) + 8 * T * pow(b, 3) - 6 * pow(T, 2) * pow(b, 2)) / (12 * pow(R, 2)) -
+         (pow(b, 2) / 2.0) / pow(cp, 2);
+    J1 = J1 / T1;
+    I3 = (T1 * b - pow(b, 2) / 2.0) / T1;
+    J3 = pow(b, 2) / (2.0 * T1);
+
+    t_ref = T - R / cs;
+    if (T1 <= t_ref) { b = T1; I6 = 0; J6 = 0; }
+    else if (0 <= t_ref && T1 > t_ref) { b = t_ref; I6 = (T1 - t_ref) / T1; J6 = t_ref / T1; }
+    else { b = 0; I6 = 0; J6 = 0; }
+    I2 = (-3 * pow(b, 4) + (8 * T + 4 * T1) * pow(b, 3) - (6 * pow(T, 2) + 12 * T * T1) * pow(b, 2) +
+          12 * T1 * pow(T, 2) * b) / (12 * pow(R, 2)) -
+         (T1 * b - pow(b, 2) / 2.0) / pow(cs, 2);
+    I2 = I2 / T1;
+    J2 = -(-3 * pow(b, 4) + 8 * T * pow(b, 3) - 6 * pow(T, 2) * pow(b, 2)) / (12 * pow(R, 2)) -
+         (pow(b, 2) / 2.0) / pow(cs, 2);
+    J2 = J2 / T1;
+    I4 = (T1 * b - pow(b, 2) / 2.0) / T1;
+    J4 = pow(b, 2) / (2.0 * T1);
+
+    double It_1, It_2, It_3, It_4, It_5, Jt_1, Jt_2, Jt_3, Jt_4, Jt_5;
+    It_1 = 0.5 * (I1 - I2);
+    It_2 = 1 / pow(cp, 2) * I3 - 1 / pow(cs, 2) * I4;
+    It_3 = I4;
+    Jt_1 = 0.5 * (J1 - J2);
+    Jt_2 = 1.0 / pow(cp, 2) * J3 - 1.0 / pow(cs, 2) * J4;
+    Jt_3 = J4;
+
+    double divider = 4 * M_PI * g->rho * R;
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) {
+            int dik = (i == k);
+            double rirk = g->rv[i] * g->rv[k];
+            double s1 = 3 * rirk - dik;
+            double s2 = rirk;
+            double s3 = dik / pow(cs, 2);
+            double v1 = s1 * It_1 + s2 * It_2 + s3 * It_3;
+            v1 /= divider;
+            double v2 = s1 * Jt_1 + s2 * Jt_2 + s3 * Jt_3;
+            v2 /= divider;
+            DU1[i * 3 + k] = v1;
+            DU2[i * 3 + k] = v2;
+        }
+
+    It_1 = 0.5 * (I1 - I2);
+    It_2 = I4 - pow(cs / cp, 2) * I3;
+    It_3 = I6 - pow(cs / cp, 3) * I5;
+    It_4 = I3 + R / cp * I5;
+    It_5 = I4 + R / cs * I6;
+    Jt_1 = 0.5 * (J1 - J2);
+    Jt_2 = J4 - pow(cs / cp, 2) * J3;
+    Jt_3 = J6 - pow(cs / cp, 3) * J5;
+    Jt_4 = J3 + R / cp * J5;
+    Jt_5 = J4 + R / cs * J6;
+
+    double rdn = dot3(g->rv, g->n);
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) {
+            int dik = (i == k);
+            double RR = pow(R, 2);
+            double rirk = g->rv[i] * g->rv[k];
+            double nirk = g->n[i] * g->rv[k];
+            double nkri = g->n[k] * g->rv[i];
+            double s1 = -6 * pow(cs, 2) * (5 * rirk * rdn - (nirk + nkri + dik * rdn)) / RR;
+            double s2 = 2 * (6 * rirk * rdn - (nirk + nkri + dik * rdn)) / RR;
+            double s3 = 2 * rirk * rdn / (cs * R);
+            double s4 = -nirk * (1 - 2 * pow(cs / cp, 2)) / RR;
+            double s5 = -(dik * rdn + nkri) / RR;
+            double v1 = s1 * It_1 + s2 * It_2 + s3 * It_3 + s4 * It_4 + s5 * It_5;
+            v1 /= 4.0 * M_PI;
+            double v2 = s1 * Jt_1 + s2 * Jt_2 + s3 * Jt_3 + s4 * Jt_4 + s5 * Jt_5;
+            v2 /= 4.0 * M_PI;
+            DT1[i * 3 + k] = v1;
+            DT2[i * 3 + k] = v2;
+        }
+}
+
+/* GreenFunctionT::Compute(4) = Kelvin_Linear + Stokes_Step_Linear
+ * (GreenFunctionT.cpp:134-136, 424-446): the step response is the Heaviside
+ * response at T minus the one at T - T1, entry by entry (VecPlus 1, -1).
+ * Like the reference, the stored time is shifted down and back up
+ * (fT=fT-fT_1; ...; fT=fT+fT_1), which can move it by an ulp between calls. */
+static void green_compute4(green* g, double* DU1, double* DU2, double* DT1, double* DT2,
+                           double* K) {
+    double u1[9], u2[9], t1[9], t2[9];
+    green_kelvin_linear(g, K);
+    green_heaviside_linear(g, g->T, DU1, DU2, DT1, DT2);
+    g->T = g->T - g->T1;
+    green_heaviside_linear(g, g->T, u1, u2, t1, t2);
+    g->T = g->T + g->T1;
+    for (int i = 0; i < 9; i++) {
+        DU1[i] = 1 * DU1[i] + -1 * u1[i];
+        DU2[i] = 1 * DU2[i] + -1 * u2[i];
+        DT1[i] = 1 * DT1[i] + -1 * t1[i];
+        DT2[i] = 1 * DT2[i] + -1 * t2[i];
+    }
+}
+
+void orc_green_step_linear(double E, double nu, double rho, const double* direction,
+                           const double* normal, double t, double t_1, double* DU_1,
+                           double* DU_2, double* DT_1, double* DT_2, double* DT_K) {
+    green g;
+    green_material(&g, E, nu, rho);
+    g.T = t;
+    g.T1 = t_1;
+    green_spatial(&g, direction, normal);
+    green_compute4(&g, DU_1, DU_2, DT_1, DT_2, DT_K);
+}
+
+/* ------------------------------------------------------------------ */
+/* Element integration (TDElementStepLinearT.cpp)                       */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int ennd;
+    double GE1[72], GE2[72], HE1[72], HE2[72]; /* 3 x 3*ennd */
+    double C1[9], C2[9];
+} elem_out;
+
+/* Accumulate one quadrature point with weight wj (the reference's w*J or
+ * w*J_tri*J): multATB(DU, NMatrix) then VecPlus(1, GE, wj, temp)
+ * (TDElementStepLinearT.cpp:91-101), and the C term at the first step
+ * (103-109).  temp[i][3a+j] = DU[j][i] * N[a]: multATB's other two terms are
+ * products with the zero entries of NMatrix. */
+static void accumulate_point(elem_out* o, int ennd, const double* N, double wj, double cwj,
+                             int first_step, const double* DU1, const double* DU2,
+                             const double* DT1, const double* DT2, const double* K) {
+    const int ncol = 3 * ennd;
+    for (int i = 0; i < 3; i++)
+        for (int a = 0; a < ennd; a++)
+            for (int j = 0; j < 3; j++) {
+                const int idx = i * ncol + 3 * a + j;
+                o->GE1[idx] = 1 * o->GE1[idx] + wj * (DU1[j * 3 + i] * N[a]);
+                o->GE2[idx] = 1 * o->GE2[idx] + wj * (DU2[j * 3 + i] * N[a]);
+                o->HE1[idx] = 1 * o->HE1[idx] + wj * (DT1[j * 3 + i] * N[a]);
+                o->HE2[idx] = 1 * o->HE2[idx] + wj * (DT2[j * 3 + i] * N[a]);
+            }
+    if (first_step) {
+        /* transMatrix(3,3,K) then VecPlus(1, C, -w*J, K^T) */
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) {
+                o->C1[i * 3 + k] = 1 * o->C1[i * 3 + k] + cwj * K[k * 3 + i];
+                o->C2[i * 3 + k] = 1 * o->C2[i * 3 + k] + cwj * K[k * 3 + i];
+            }
+    }
+}
+
+/* FormGH_Regular (TDElementStepLinearT.cpp:28-125). */
+static void form_regular(green* g, int etype, int nq, const double* coords, const double* colloc,
+                         elem_out* o) {
+    const int ennd = etype == 1 ? 4 : 8;
+    const double *gx = GX6, *gw = GW6;
+    gauss_table(nq, &gx, &gw);
+    memset(o, 0, sizeof(*o));
+    o->ennd = ennd;
+    const int first = (g->T == g->T1);
+    for (int q1 = 0; q1 < nq; q1++)
+        for (int q2 = 0; q2 < nq; q2++) {
+            shape_pt s;
+            shape_eval(etype, coords, gx[q1], gx[q2], &s);
+            const double w = gw[q1] * gw[q2];
+            double dir[3];
+            for (int d = 0; d < 3; d++) dir[d] = 1 * s.x[d] + -1 * colloc[d];
+            green_spatial(g, dir, s.n);
+            double DU1[9], DU2[9], DT1[9], DT2[9], K[9];
+            green_compute4(g, DU1, DU2, DT1, DT2, K);
+            accumulate_point(o, ennd, s.N, w * s.J, -w * s.J, first, DU1, DU2, DT1, DT2, K);
+        }
+}
+
+/* FormGH_Singular_1 (TDElementStepLinearT.cpp:389-592): two degenerate
+ * triangles (Duffy) from the singular corner, each nq x nq.  Always uses the
+ * 4-node shape (it is called on Q4 elements or Q4 sub-elements). */
+static void form_singular_q4(green* g, int nq, const double* coords, const double* colloc,
+                             int singular, elem_out* o) {
+    const double *gx = GX6, *gw = GW6;
+    gauss_table(nq, &gx, &gw);
+    memset(o, 0, sizeof(*o));
+    o->ennd = 4;
+    double ec0, ec1;
+    switch (singular) {
+    case 0: ec0 = -1; ec1 = -1; break;
+    case 1: ec0 = 1; ec1 = -1; break;
+    case 2: ec0 = 1; ec1 = 1; break;
+    default: ec0 = -1; ec1 = 1; break;
+    }
+    const int first = (g->T == g->T1);
+    for (int tri = 0; tri < 2; tri++)
+        for (int q1 = 0; q1 < nq; q1++)
+            for (int q2 = 0; q2 < nq; q2++) {
+                const double et1 = gx[q1], et2 = gx[q2], w = gw[q1] * gw[q2];
+                const double J_tri = 0.5 * (1 - et1);
+                double e1, e2;
+                if (tri == 0) { /* triangle A (436-511) */
+                    e1 = ec0 * (1 - 0.5 * (1 - et1) * (1 + ec0 * ec1 * et2));
+                    e2 = ec1 * et1;
+                } else { /* triangle B (516-590) */
+                    e1 = ec0 * et1;
+                    e2 = ec1 * (1 - 0.5 * (1 - et1) * (1 - ec0 * ec1 * et2));
+                }
+                shape_pt s;
+                shape_eval(1, coords, e1, e2, &s);
+                double dir[3];
+                dir[0] = s.x[0] - colloc[0];
+                dir[1] = s.x[1] - colloc[1];
+                dir[2] = s.x[2] - colloc[2];
+                green_spatial(g, dir, s.n);
+                double DU1[9], DU2[9], DT1[9], DT2[9], K[9];
+                green_compute4(g, DU1, DU2, DT1, DT2, K);
+                accumulate_point(o, 4, s.N, w * J_tri * s.J, -w * s.J * J_tri, first, DU1, DU2,
+                                 DT1, DT2, K);
+            }
+}
+
+/* SubElement table (TDElementStepLinearT.cpp:192-386): singular node of an
+ * 8-node element -> Q4 sub-elements (parent node ids) and their singular corner. */
+static int q8_subelements(int singular, int ids[2][4], int cid[2]) {
+    static const int mid[4][2][4] = {
+        {{4, 6, 3, 0}, {4, 1, 2, 6}},
+        {{5, 2, 3, 7}, {5, 7, 0, 1}},
+        {{6, 3, 0, 4}, {6, 4, 1, 2}},
+        {{7, 0, 1, 5}, {7, 5, 2, 3}},
+    };
+    if (singular >= 0 && singular < 4) {
+        for (int i = 0; i < 4; i++) ids[0][i] = i;
+        cid[0] = singular;
+        return 1;
+    }
+    for (int e = 0; e < 2; e++) {
+        for (int i = 0; i < 4; i++) ids[e][i] = mid[singular - 4][e][i];
+        cid[e] = 0;
+    }
+    return 2;
+}
+
+/* FormGH_Singular (TDElementStepLinearT.cpp:128-190) incl. AssembleSubElement (597-626). */
+static void form_singular(green* g, int etype, int nq, const double* coords,
+                          const double* colloc, int singular, elem_out* o) {
+    if (etype == 1) {
+        form_singular_q4(g, nq, coords, colloc, singular, o);
+        return;
+    }
+    memset(o, 0, sizeof(*o));
+    o->ennd = 8;
+    int ids[2][4], cid[2];
+    const int nsub = q8_subelements(singular, ids, cid);
+    for (int se = 0; se < nsub; se++) {
+        double sub[12];
+        for (int i = 0; i < 4; i++)
+            for (int d = 0; d < 3; d++) sub[3 * i + d] = coords[3 * ids[se][i] + d];
+        elem_out so;
+        form_singular_q4(g, nq, sub, colloc, cid[se], &so);
+        for (int ni = 0; ni < 4; ni++) {
+            const int id = ids[se][ni];
+            for (int ri = 0; ri < 3; ri++)
+                for (int ci = 0; ci < 3; ci++) {
+                    const int dst = ri * 24 + 3 * id + ci, src = ri * 12 + 3 * ni + ci;
+                    o->GE1[dst] += so.GE1[src];
+                    o->GE2[dst] += so.GE2[src];
+                    o->HE1[dst] += so.HE1[src];
+                    o->HE2[dst] += so.HE2[src];
+                }
+        }
+        for (int i = 0; i < 9; i++) {
+            o->C1[i] += so.C1[i];
+            o->C2[i] += so.C2[i];
+        }
+    }
+}
+
+int orc_element_gh(int etype, int nq, double E, double nu, double rho, const double* coords,
+                   const double* collocation, double t, double t_1, int singular, double* GE_1,
+                   double* GE_2, double* HE_1, double* HE_2, double* C_1, double* C_2) {
+    const double *gx = GX6, *gw = GW6;
+    if (gauss_table(nq, &gx, &gw) != 0 || (etype != 1 && etype != 2)) return -1;
+    const int ennd = etype == 1 ? 4 : 8;
+    if (singular >= ennd) return -1;
+    green g;
+    green_material(&g, E, nu, rho);
+    g.T = t;
+    g.T1 = t_1;
+    elem_out o;
+    if (singular < 0) form_regular(&g, etype, nq, coords, collocation, &o);
+    else form_singular(&g, etype, nq, coords, collocation, singular, &o);
+    memcpy(GE_1, o.GE1, sizeof(double) * 9 * ennd);
+    memcpy(GE_2, o.GE2, sizeof(double) * 9 * ennd);
+    memcpy(HE_1, o.HE1, sizeof(double) * 9 * ennd);
+    memcpy(HE_2, o.HE2, sizeof(double) * 9 * ennd);
+    memcpy(C_1, o.C1, sizeof(double) * 9);
+    memcpy(C_2, o.C2, sizeof(double) * 9);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Assembly driver (ElastoDynamicsT.cpp:108-280)                        */
+/* ------------------------------------------------------------------ */
+int orc_gh_driver(const orc_model* m, double t, double t_1, int node_lo, int node_hi,
+                  double* G_I, double* G_J, double* H_I, double* H_J, int nthreads) {
+    const double *gx = GX6, *gw = GW6;
+    if (gauss_table(m->nq, &gx, &gw) != 0) return -1;
+    if (m->etype != 1 && m->etype != 2) return -1;
+    if (node_lo < 0 || node_hi >= m->nnd || node_lo > node_hi) return -1;
+    const int ennd = m->etype == 1 ? 4 : 8;
+    const int D = 3 * m->nnd;
+    const size_t rows = (size_t)(node_hi - node_lo + 1) * 3;
+    memset(G_I, 0, sizeof(double) * rows * D);
+    memset(G_J, 0, sizeof(double) * rows * D);
+    memset(H_I, 0, sizeof(double) * rows * D);
+    memset(H_J, 0, sizeof(double) * rows * D);
+    if (nthreads < 1) nthreads = 1;
+    int err = 0;
+    /* One Green's-function state per thread, set once per call like the
+     * reference's element object (SetTime at ElastoDynamicsT.cpp:141) and
+     * carried across rows; with one thread the sequence of states is the
+     * reference's. */
+#pragma omp parallel num_threads(nthreads)
+    {
+    green g;
+    green_material(&g, m->E, m->nu, m->rho);
+    g.T = t;
+    g.T1 = t_1;
+#pragma omp for schedule(dynamic, 1)
+    for (int n_i = node_lo; n_i <= node_hi; n_i++) {
+        double colloc[3], en[24];
+        for (int d = 0; d < 3; d++) colloc[d] = m->coords[n_i * 3 + d];
+        const int lc = n_i - node_lo;
+        elem_out o;
+        for (int e_i = 0; e_i < m->nel; e_i++) {
+            for (int a = 0; a < ennd; a++) {
+                const int gid = m->ien[e_i * ennd + a];
+                for (int d = 0; d < 3; d++) en[a * 3 + d] = m->coords[gid * 3 + d];
+            }
+            /* singular test (166-175): the last node within r^2 < 1e-9 */
+            int singular = -1;
+            for (int a = 0; a < ennd; a++) {
+                double r2 = pow(en[a * 3] - colloc[0], 2) + pow(en[a * 3 + 1] - colloc[1], 2) +
+                            pow(en[a * 3 + 2] - colloc[2], 2);
+                if (r2 < 1e-9) singular = a;
+            }
+            if (singular == -1) form_regular(&g, m->etype, m->nq, en, colloc, &o);
+            else form_singular(&g, m->etype, m->nq, en, colloc, singular, &o);
+            /* AssembleGH x4 (235-259) */
+            for (int ni = 0; ni < ennd; ni++) {
+                const int nid = m->ien[e_i * ennd + ni];
+                for (int i = 0; i < 3; i++)
+                    for (int j = 0; j < 3; j++) {
+                        const size_t dst = (size_t)(i + lc * 3) * D + nid * 3 + j;
+                        const int src = i * (ennd * 3) + ni * 3 + j;
+                        G_I[dst] += o.GE1[src];
+                        G_J[dst] += o.GE2[src];
+                        H_I[dst] += o.HE1[src];
+                        H_J[dst] += o.HE2[src];
+                    }
+            }
+            /* AssembleC x2 (261-280) */
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) {
+                    const size_t dst = (size_t)(lc * 3 + i) * D + n_i * 3 + j;
+                    H_I[dst] += o.C1[i * 3 + j];
+                    H_J[dst] += o.C2[i * 3 + j];
+                }
+        }
+        /* exterior free term at the first step (212-225) */
+        if (m->if_ext && t == t_1)
+            for (int d = 0; d < 3; d++) {
+                const size_t dst = (size_t)(lc * 3 + d) * D + n_i * 3 + d;
+                H_I[dst] += 0.5 * t_1;
+                H_J[dst] += 0.5 * t_1;
+            }
+    }
+    }
+    return err;
+}
+
+/* SolverT::ComputeMaxStep (SolverT.cpp:211-250). */
+int orc_max_step(const orc_model* m) {
+    double Mu = m->E / (2.0 * (1.0 + m->nu));
+    double Cs = sqrt(Mu / m->rho);
+    double max_dis = 0;
+    for (int i = 0; i < m->nnd - 1; i++)
+        for (int j = i + 1; j < m->nnd; j++) {
+            double tmp = 0;
+            for (int d = 0; d < 3; d++) tmp += pow(m->coords[i * 3 + d] - m->coords[j * 3 + d], 2);
+            tmp = sqrt(tmp);
+            if (tmp > max_dis) max_dis = tmp;
+        }
+    return (int)(ceil(max_dis / (Cs * m->dt)) + 1);
+}
+
+/* main.cpp:89-121 + SolverStepLinearT::UpdateGHLinear (SolverStepLinearT.cpp:58-97):
+ * step 1 inserts J(dt) at level 0; step n adds J(n dt) to level n-1; every
+ * step n <= M inserts I(n dt) at level n. */
+int orc_assemble_levels(const orc_model* m, int M, int nsteps, double* G_levels,
+                        double* H_levels, int nthreads) {
+    const size_t D = 3 * (size_t)m->nnd, D2 = D * D;
+    memset(G_levels, 0, sizeof(double) * (M + 1) * D2);
+    memset(H_levels, 0, sizeof(double) * (M + 1) * D2);
+    double* GI = malloc(sizeof(double) * D2);
+    double* GJ = malloc(sizeof(double) * D2);
+    double* HI = malloc(sizeof(double) * D2);
+    double* HJ = malloc(sizeof(double) * D2);
+    if (!GI || !GJ || !HI || !HJ) {
+        free(GI); free(GJ); free(HI); free(HJ);
+        return -4;
+    }
+    int err = 0;
+    const int last = nsteps < M ? nsteps : M;
+    for (int step = 1; step <= last && !err; step++) {
+        err = orc_gh_driver(m, step * m->dt, m->dt, 0, m->nnd - 1, GI, GJ, HI, HJ, nthreads);
+        if (err) break;
+        double* g0 = G_levels + (size_t)(step - 1) * D2;
+        double* h0 = H_levels + (size_t)(step - 1) * D2;
+        if (step == 1) {
+            memcpy(g0, GJ, sizeof(double) * D2);
+            memcpy(h0, HJ, sizeof(double) * D2);
+        } else {
+            for (size_t i = 0; i < D2; i++) {
+                g0[i] += GJ[i];
+                h0[i] += HJ[i];
+            }
+        }
+        memcpy(G_levels + (size_t)step * D2, GI, sizeof(double) * D2);
+        memcpy(H_levels + (size_t)step * D2, HI, sizeof(double) * D2);
+    }
+    free(GI); free(GJ); free(HI); free(HJ);
+    return err;
+}
+
+/* ------------------------------------------------------------------ */
+/* Marching (SolverT.cpp:265-394, SolverStepLinearT.cpp:314-544)        */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int n;
+    double* lu;
+    int* piv;
+    double* cached;
+} lu_cache;
+
+/* Exact dense LU with partial pivoting in place of KSPSolve
+ * (SolverStepLinearT.cpp:503-504), refactored only when the operator's
+ * entries change (the reference rebuilds the same LHS every step). */
+static int lu_solve(lu_cache* c, const double* A, int n, const double* b, double* x,
+                    int nthreads) {
+    const size_t n2 = (size_t)n * n;
+    if (!c->cached || memcmp(c->cached, A, sizeof(double) * n2) != 0) {
+        if (!c->cached) {
+            c->cached = malloc(sizeof(double) * n2);
+            c->lu = malloc(sizeof(double) * n2);
+            c->piv = malloc(sizeof(int) * n);
+            if (!c->cached || !c->lu || !c->piv) return -4;
+        }
+        memcpy(c->cached, A, sizeof(double) * n2);
+        memcpy(c->lu, A, sizeof(double) * n2);
+        double* a = c->lu;
+        for (int k = 0; k < n; k++) {
+            int p = k;
+            double best = fabs(a[(size_t)k * n + k]);
+            for (int r = k + 1; r < n; r++) {
+                double v = fabs(a[(size_t)r * n + k]);
+                if (v > best) { best = v; p = r; }
+            }
+            c->piv[k] = p;
+            if (p != k)
+                for (int j = 0; j < n; j++) {
+                    double tmp = a[(size_t)k * n + j];
+                    a[(size_t)k * n + j] = a[(size_t)p * n + j];
+                    a[(size_t)p * n + j] = tmp;
+                }
+            const double d = a[(size_t)k * n + k];
+            if (d == 0.0) {
+                free(c->cached);
+                c->cached = NULL;
+                return -3;
+            }
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+            for (int r = k + 1; r < n; r++) {
+                double* rr = &a[(size_t)r * n];
+                rr[k] /= d;
+                const double l = rr[k];
+                if (l == 0.0) continue;
+                const double* ur = &a[(size_t)k * n];
+                for (int j = k + 1; j < n; j++) rr[j] -= l * ur[j];
+            }
+        }
+    }
+    double* y = x;
+    if (y != b) memcpy(y, b, sizeof(double) * n);
+    for (int k = 0; k < n; k++)
+        if (c->piv[k] != k) {
+            double tmp = y[k];
+            y[k] = y[c->piv[k]];
+            y[c->piv[k]] = tmp;
+        }
+    const double* a = c->lu;
+    for (int r = 0; r < n; r++) {
+        double s = y[r];
+        for (int j = 0; j < r; j++) s -= a[(size_t)r * n + j] * y[j];
+        y[r] = s;
+    }
+    for (int r = n - 1; r >= 0; r--) {
+        double s = y[r];
+        for (int j = r + 1; j < n; j++) s -= a[(size_t)r * n + j] * y[j];
+        y[r] = s / a[(size_t)r * n + r];
+    }
+    return 0;
+}
+
+int orc_lu_factor(int n, double* A, int nthreads) {
+    lu_cache c = {0, NULL, NULL, NULL};
+    double b0 = 0.0, x0;
+    double* b = malloc(sizeof(double) * n);
+    double* x = malloc(sizeof(double) * n);
+    if (!b || !x) { free(b); free(x); return -4; }
+    for (int i = 0; i < n; i++) b[i] = 1.0;
+    int rc = lu_solve(&c, A, n, b, x, nthreads < 1 ? 1 : nthreads);
+    (void)b0; (void)x0;
+    free(b); free(x); free(c.lu); free(c.piv); free(c.cached);
+    return rc;
+}
+
+/* y = y + A x, each row as a left-to-right dot product added to y (MatMultAdd). */
+static void mat_mult_add(const double* A, int n, const double* x, double* y, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = 0; i < n; i++) {
+        const double* row = &A[(size_t)i * n];
+        double s = 0.0;
+        for (int j = 0; j < n; j++) s += row[j] * x[j];
+        y[i] = y[i] + s;
+    }
+}
+static void mat_zero(double* A, size_t n2, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (size_t i = 0; i < n2; i++) A[i] = 0.0;
+}
+static void mat_axpy(double* Y, double a, const double* X, size_t n2, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (size_t i = 0; i < n2; i++) Y[i] += a * X[i];
+}
+static void mat_scale(double* A, double a, size_t n2, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (size_t i = 0; i < n2; i++) A[i] *= a;
+}
+
+/* temp = 0; temp += c*X; temp *= sign; rhs += temp*v  (the reference's per-term
+ * MatZeroEntries / MatAXPY / MatScale / MatMultAdd sequence). */
+static void term(double* tmp, const double* X, double c, double sign, int D, const double* v,
+                 double* rhs, int nthreads) {
+    const size_t D2 = (size_t)D * D;
+    mat_zero(tmp, D2, nthreads);
+    mat_axpy(tmp, c, X, D2, nthreads);
+    if (sign != 1.0) mat_scale(tmp, sign, D2, nthreads);
+    mat_mult_add(tmp, D, v, rhs, nthreads);
+}
+
+int orc_march_range(int D, int M, const double* G_levels, const double* H_levels,
+                    int ubc_num, const int* ubc_dofs, const double* ubc_vals, int fbc_num,
+                    const int* fbc_dofs, const double* fbc_vals, const double* amp, double a1,
+                    double a2, int step_lo, int step_hi, double* u_hist, double* t_hist,
+                    int nthreads) {
+    double a3;
+    if (a1 >= 0 && a1 <= 1 && a2 >= 0 && a2 < 1 && a1 + a2 <= 1) a3 = 1 - a1 - a2;
+    else return -2;
+    if (nthreads < 1) nthreads = 1;
+    for (int i = 0; i < ubc_num; i++)
+        if (ubc_dofs[i] < 0 || ubc_dofs[i] >= D) return -1;
+    for (int i = 0; i < fbc_num; i++)
+        if (fbc_dofs[i] < 0 || fbc_dofs[i] >= D) return -1;
+    const size_t D2 = (size_t)D * D;
+    const int dof_low = 0, dof_high = D - 1; /* single row block: LocalIndexing (SolverT.cpp:158-194) */
+    double* Gc = malloc(sizeof(double) * D2);
+    double* Hc = malloc(sizeof(double) * D2);
+    double* Gt = malloc(sizeof(double) * D2);
+    double* Ht = malloc(sizeof(double) * D2);
+    double* tmp = malloc(sizeof(double) * D2);
+    double* load = malloc(sizeof(double) * D);
+    double* rhs = malloc(sizeof(double) * D);
+    double* x = malloc(sizeof(double) * D);
+    lu_cache lc = {0, NULL, NULL, NULL};
+    int err = 0;
+    if (!Gc || !Hc || !Gt || !Ht || !tmp || !load || !rhs || !x) err = -4;
+#define LEV(L, k) ((L) + (size_t)(k) * D2)
+#define UH(s) (u_hist + (size_t)(s) * D)
+#define TH(s) (t_hist + (size_t)(s) * D)
+    for (int curr = step_lo; curr <= step_hi && !err; curr++) {
+        const double a = amp ? amp[curr - 1] : 1.0;
+        /* SetLoad (SolverT.cpp:344-377): FBC*amp, then UBC values (not scaled) */
+        for (int i = 0; i < D; i++) load[i] = 0;
+        for (int i = 0; i < fbc_num; i++) load[fbc_dofs[i]] = fbc_vals[i] * a;
+        for (int i = 0; i < ubc_num; i++) load[ubc_dofs[i]] = ubc_vals[i];
+        const int s = curr - 1; /* solve_step */
+        if (curr == 1) continue;
+        if (curr == 2) {
+            memcpy(Gc, LEV(G_levels, 0), sizeof(double) * D2);
+            memcpy(Hc, LEV(H_levels, 0), sizeof(double) * D2);
+        } else {
+            mat_zero(Gc, D2, nthreads);
+            mat_zero(Hc, D2, nthreads);
+            mat_axpy(Gc, 2 * a1 + a3, LEV(G_levels, 0), D2, nthreads);
+            mat_axpy(Gc, a1, LEV(G_levels, 1), D2, nthreads);
+            mat_axpy(Hc, 2 * a1 + a3, LEV(H_levels, 0), D2, nthreads);
+            mat_axpy(Hc, a1, LEV(H_levels, 1), D2, nthreads);
+        }
+        /* ExchangeColumns (SolverT.cpp:265-342) */
+        memcpy(Gt, Gc, sizeof(double) * D2);
+        memcpy(Ht, Hc, sizeof(double) * D2);
+        for (int u = 0; u < ubc_num; u++) {
+            const int col = ubc_dofs[u];
+            for (int r = 0; r < D; r++) {
+                Gc[(size_t)r * D + col] = -1 * Ht[(size_t)r * D + col];
+                Hc[(size_t)r * D + col] = -1 * Gt[(size_t)r * D + col];
+            }
+        }
+        /* RHS = G_c * load */
+        for (int i = 0; i < D; i++) rhs[i] = 0;
+        mat_mult_add(Gc, D, load, rhs, nthreads);
+        /* The reference then multiplies its fG_DB_bgn/fH_DB_bgn matrices with
+         * fTrac_DB[0]/fDis_DB[0] (SolverStepLinearT.cpp:377, 446-455, 473-482);
+         * those vectors are the zero initial state (SolverStepLinearT.cpp:50,
+         * SolverT.cpp:121-122) and are never written, so each such MatMultAdd
+         * adds exactly +0 and is omitted here. */
+        if (curr >= 3) {
+            /* Eqn M+1 terms (409-430) */
+            mat_zero(tmp, D2, nthreads);
+            mat_axpy(tmp, a1, LEV(H_levels, 2), D2, nthreads);
+            mat_axpy(tmp, -a1, LEV(H_levels, 0), D2, nthreads);
+            mat_scale(tmp, -1, D2, nthreads);
+            mat_mult_add(tmp, D, UH(s - 1), rhs, nthreads);
+            mat_zero(tmp, D2, nthreads);
+            mat_axpy(tmp, a1, LEV(G_levels, 2), D2, nthreads);
+            mat_axpy(tmp, -a1, LEV(G_levels, 0), D2, nthreads);
+            mat_mult_add(tmp, D, TH(s - 1), rhs, nthreads);
+            const int f1 = (s + 1 < M) ? s + 1 : M;
+            for (int f = 3; f <= f1; f++) {
+                term(tmp, LEV(H_levels, f), a1, -1, D, UH(s + 1 - f), rhs, nthreads);
+                term(tmp, LEV(G_levels, f), a1, 1, D, TH(s + 1 - f), rhs, nthreads);
+            }
+            /* Eqn M terms (433-443) */
+            const int f2 = (s - 1 < M) ? s - 1 : M;
+            for (int f = 1; f <= f2; f++) {
+                term(tmp, LEV(H_levels, f), a3, -1, D, UH(s - f), rhs, nthreads);
+                term(tmp, LEV(G_levels, f), a3, 1, D, TH(s - f), rhs, nthreads);
+            }
+            /* Eqn M-1 terms (460-470) */
+            const int f3 = (s - 2 < M) ? s - 2 : M;
+            for (int f = 0; f <= f3; f++) {
+                term(tmp, LEV(H_levels, f), a2, -1, D, UH(s - 1 - f), rhs, nthreads);
+                term(tmp, LEV(G_levels, f), a2, 1, D, TH(s - 1 - f), rhs, nthreads);
+            }
+        }
+        /* KSPSolve (503-504) */
+        err = lu_solve(&lc, Hc, D, rhs, x, nthreads);
+        if (err) break;
+        /* u^s = x; u[UBC] = prescribed (512-515) */
+        memcpy(UH(s), x, sizeof(double) * D);
+        for (int i = 0; i < ubc_num; i++) UH(s)[ubc_dofs[i]] = ubc_vals[i];
+        /* t^s[FBC] = FBC*amp; t^s[UBC] = x[UBC] for dof_low <= dof < dof_high (520-535) */
+        for (int i = 0; i < fbc_num; i++) TH(s)[fbc_dofs[i]] = fbc_vals[i] * a;
+        for (int i = 0; i < ubc_num; i++) {
+            const int ud = ubc_dofs[i];
+            if (ud >= dof_low && ud < dof_high) TH(s)[ud] = x[ud];
+        }
+    }
+#undef LEV
+#undef UH
+#undef TH
+    free(Gc); free(Hc); free(Gt); free(Ht); free(tmp); free(load); free(rhs); free(x);
+    free(lc.lu); free(lc.piv); free(lc.cached);
+    return err;
+}
+
+int orc_march(int D, int M, const double* G_levels, const double* H_levels, int ubc_num,
+              const int* ubc_dofs, const double* ubc_vals, int fbc_num, const int* fbc_dofs,
+              const double* fbc_vals, const double* amp, double a1, double a2, int numstep,
+              double* u_hist, double* t_hist, int nthreads) {
+    memset(u_hist, 0, sizeof(double) * (size_t)(numstep + 1) * D);
+    memset(t_hist, 0, sizeof(double) * (size_t)(numstep + 1) * D);
+    return orc_march_range(D, M, G_levels, H_levels, ubc_num, ubc_dofs, ubc_vals, fbc_num,
+                           fbc_dofs, fbc_vals, amp, a1, a2, 1, numstep, u_hist, t_hist,
+                           nthreads);
+}

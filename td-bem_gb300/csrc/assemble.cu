@@ -1,0 +1,603 @@
+// G^k / H^k level assembly on sm_103a (FP64 plain form and FP32 level store).
+//
+// Work decomposition.  The unit of work is one (collocation node c, element e,
+// time level k) item.  For a pair (c, e) only the levels whose time window
+// meets the P- or S-wave front crossing the element can be non-zero: the
+// Heaviside response H(T) of GreenFunctionT::Stokes_Heaviside_Linear
+// (GreenFunctionT.cpp:241-416) is exactly 0 for T < r/c_p (b = 0 for both waves)
+// and constant for T - r/c_s >= dt (b = dt for both waves, I5 = I6 = 0), so the
+// step response H(T) - H(T - dt) (Stokes_Step_Linear, GreenFunctionT.cpp:424-446)
+// vanishes outside  r/(c_p dt) <= n < r/(c_s dt) + 2.  A window kernel bounds r
+// over the element with its bounding sphere, a scan turns the per-pair level
+// counts into item offsets, and one thread per item integrates all Gauss points
+// of the element for its level.  Levels outside every window stay exactly zero
+// (the reference stores round-off noise there).
+//
+// Level placement follows main.cpp:89-121 + SolverStepLinearT::UpdateGHLinear
+// (SolverStepLinearT.cpp:58-97): level k = I(k dt) + J((k+1) dt), so one item
+// sums the I part at time k dt and the J part at time (k+1) dt before the
+// scatter, halving the scatter traffic.
+//
+// Determinism.  Elements are coloured so that no two elements of a colour share
+// a node; one launch per colour, so every level entry receives at most one
+// read-modify-write per launch and the result does not depend on scheduling.
+//
+// Arithmetic.  The time integrals are the reference's closed forms
+// (GreenFunctionT.cpp:251-314) in Horner form; the 3x3 kernels are written as
+// DU = A r r^T + B I and DT = alpha rdn r r^T + beta n r^T + gamma (r n^T + rdn I)
+// (GreenFunctionT.cpp:332-406 with the s1..s5 terms collected), so an item does
+// the per-level work with ~300 FP64 operations per Gauss point.
+#include <cub/device/device_scan.cuh>
+
+#include "tdbem_internal.cuh"
+
+namespace tdbem {
+
+namespace {
+
+constexpr int kGeomStride = 12;  // x[3], n[3], wJ, N[4], pad
+
+// ShapeFunctionT::Evaluate for the 4-node quad (ShapeFunctionT.cpp:241-301).
+__device__ __forceinline__ void q4_eval(const double* c, double e1, double e2, double N[4],
+                                        double x[3], double n[3], double& J) {
+    N[0] = 0.25 * (1 - e1) * (1 - e2);
+    N[1] = 0.25 * (1 + e1) * (1 - e2);
+    N[2] = 0.25 * (1 + e1) * (1 + e2);
+    N[3] = 0.25 * (1 - e1) * (1 + e2);
+    const double d1[4] = {-0.25 * (1 - e2), 0.25 * (1 - e2), 0.25 * (1 + e2), -0.25 * (1 + e2)};
+    const double d2[4] = {-0.25 * (1 - e1), -0.25 * (1 + e1), 0.25 * (1 + e1), 0.25 * (1 - e1)};
+    double dx1[3] = {0, 0, 0}, dx2[3] = {0, 0, 0};
+    x[0] = x[1] = x[2] = 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            x[d] += N[a] * c[a * 3 + d];
+            dx1[d] += d1[a] * c[a * 3 + d];
+            dx2[d] += d2[a] * c[a * 3 + d];
+        }
+    n[0] = dx1[1] * dx2[2] - dx1[2] * dx2[1];
+    n[1] = dx1[2] * dx2[0] - dx1[0] * dx2[2];
+    n[2] = dx1[0] * dx2[1] - dx1[1] * dx2[0];
+    J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] /= J;
+    n[1] /= J;
+    n[2] /= J;
+}
+
+// Duffy point of the singular integration (TDElementStepLinearT.cpp:406-590):
+// triangle tri of the corner `corner`, tensor Gauss point (et1, et2) of weight w.
+__device__ __forceinline__ void duffy_point(const double* c, int corner, int tri, double et1,
+                                            double et2, double w, double N[4], double x[3],
+                                            double n[3], double& wJ) {
+    const double ec0 = (corner == 1 || corner == 2) ? 1.0 : -1.0;
+    const double ec1 = (corner >= 2) ? 1.0 : -1.0;
+    const double J_tri = 0.5 * (1 - et1);
+    double e1, e2;
+    if (tri == 0) {
+        e1 = ec0 * (1 - 0.5 * (1 - et1) * (1 + ec0 * ec1 * et2));
+        e2 = ec1 * et1;
+    } else {
+        e1 = ec0 * et1;
+        e2 = ec1 * (1 - 0.5 * (1 - et1) * (1 - ec0 * ec1 * et2));
+    }
+    double J;
+    q4_eval(c, e1, e2, N, x, n, J);
+    wJ = w * J_tri * J;
+}
+
+// I-part time integrals of one wave at time T (GreenFunctionT.cpp:251-279):
+// I1 (or I2), I3 (or I4), I5 (or I6).  cA = 8T + 4T1, cB = 6T^2 + 12 T T1,
+// cC = 12 T1 T^2 are per-thread constants.
+__device__ __forceinline__ void wave_I(double T, double cA, double cB, double cC, double roc,
+                                       double inv12R2, double invc2, const Phys& ph,
+                                       double& I1, double& I3, double& I5) {
+    const double tr = T - roc;
+    double b, x5;
+    if (ph.dt <= tr) {
+        b = ph.dt;
+        x5 = 0;
+    } else if (0 <= tr) {
+        b = tr;
+        x5 = (ph.dt - tr) * ph.inv_dt;
+    } else {
+        b = 0;
+        x5 = 0;
+    }
+    const double poly = b * (cC + b * (-cB + b * (cA - 3 * b)));
+    const double q = b * (ph.dt - 0.5 * b);
+    I1 = (poly * inv12R2 - q * invc2) * ph.inv_dt;
+    I3 = q * ph.inv_dt;
+    I5 = x5;
+}
+
+// J-part time integrals (GreenFunctionT.cpp:275-280, 309-314): dA = 8T, dB = 6T^2.
+__device__ __forceinline__ void wave_J(double T, double dA, double dB, double roc,
+                                       double inv12R2, double invc2, const Phys& ph,
+                                       double& J1, double& J3, double& J5) {
+    const double tr = T - roc;
+    double b, x5;
+    if (ph.dt <= tr) {
+        b = ph.dt;
+        x5 = 0;
+    } else if (0 <= tr) {
+        b = tr;
+        x5 = tr * ph.inv_dt;
+    } else {
+        b = 0;
+        x5 = 0;
+    }
+    const double b2 = b * b;
+    const double poly = b2 * (dB + b * (3 * b - dA));
+    J1 = (poly * inv12R2 - 0.5 * b2 * invc2) * ph.inv_dt;
+    J3 = 0.5 * b2 * ph.inv_dt;
+    J5 = x5;
+}
+
+struct TimeConsts {
+    bool doI, doJ;
+    double TI0, TI1, TJ0, TJ1;          // I part at TI0 minus at TI1 = TI0 - dt; same for J
+    double cA0, cB0, cC0, cA1, cB1, cC1;
+    double dA0, dB0, dA1, dB1;
+};
+
+__device__ __forceinline__ void time_consts(TimeConsts& tc, double TI, double TJ, double dt) {
+    tc.TI0 = TI;
+    tc.TI1 = TI - dt;
+    tc.TJ0 = TJ;
+    tc.TJ1 = TJ - dt;
+    tc.cA0 = 8 * tc.TI0 + 4 * dt;
+    tc.cB0 = 6 * tc.TI0 * tc.TI0 + 12 * tc.TI0 * dt;
+    tc.cC0 = 12 * dt * tc.TI0 * tc.TI0;
+    tc.cA1 = 8 * tc.TI1 + 4 * dt;
+    tc.cB1 = 6 * tc.TI1 * tc.TI1 + 12 * tc.TI1 * dt;
+    tc.cC1 = 12 * dt * tc.TI1 * tc.TI1;
+    tc.dA0 = 8 * tc.TJ0;
+    tc.dB0 = 6 * tc.TJ0 * tc.TJ0;
+    tc.dA1 = 8 * tc.TJ1;
+    tc.dB1 = 6 * tc.TJ1 * tc.TJ1;
+}
+
+// Accumulators of one item: the 4 node blocks of G (symmetric, 6 entries)
+// and H (9 entries, [i][j] of HE[i][3a+j]).
+struct ItemAcc {
+    double g[4][6];
+    double h[4][9];
+};
+
+// One Gauss point of one item: step responses for the item's time(s), the
+// collected 3x3 kernels and the accumulation into the 4 node blocks.
+__device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, const Phys& ph,
+                                            const double xc[3], const double xq[3],
+                                            const double nq[3], double wJ, const double N[4]) {
+    const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
+    const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    const double inv_r = 1.0 / r;
+    const double rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+    const double rdn = rv[0] * nq[0] + rv[1] * nq[1] + rv[2] * nq[2];
+    const double inv12R2 = inv_r * inv_r * (1.0 / 12.0);
+    const double roc_p = r * ph.inv_cp, roc_s = r * ph.inv_cs;
+
+    double P1 = 0, P3 = 0, P5 = 0, S2 = 0, S4 = 0, S6 = 0;
+    if (tc.doI) {
+        double a1, a3, a5, b1, b3, b5;
+        wave_I(tc.TI0, tc.cA0, tc.cB0, tc.cC0, roc_p, inv12R2, ph.inv_cp2, ph, a1, a3, a5);
+        wave_I(tc.TI1, tc.cA1, tc.cB1, tc.cC1, roc_p, inv12R2, ph.inv_cp2, ph, b1, b3, b5);
+        P1 = a1 - b1;
+        P3 = a3 - b3;
+        P5 = a5 - b5;
+        wave_I(tc.TI0, tc.cA0, tc.cB0, tc.cC0, roc_s, inv12R2, ph.inv_cs2, ph, a1, a3, a5);
+        wave_I(tc.TI1, tc.cA1, tc.cB1, tc.cC1, roc_s, inv12R2, ph.inv_cs2, ph, b1, b3, b5);
+        S2 = a1 - b1;
+        S4 = a3 - b3;
+        S6 = a5 - b5;
+    }
+    if (tc.doJ) {
+        double a1, a3, a5, b1, b3, b5;
+        wave_J(tc.TJ0, tc.dA0, tc.dB0, roc_p, inv12R2, ph.inv_cp2, ph, a1, a3, a5);
+        wave_J(tc.TJ1, tc.dA1, tc.dB1, roc_p, inv12R2, ph.inv_cp2, ph, b1, b3, b5);
+        P1 += a1 - b1;
+        P3 += a3 - b3;
+        P5 += a5 - b5;
+        wave_J(tc.TJ0, tc.dA0, tc.dB0, roc_s, inv12R2, ph.inv_cs2, ph, a1, a3, a5);
+        wave_J(tc.TJ1, tc.dA1, tc.dB1, roc_s, inv12R2, ph.inv_cs2, ph, b1, b3, b5);
+        S2 += a1 - b1;
+        S4 += a3 - b3;
+        S6 += a5 - b5;
+    }
+    // DU (GreenFunctionT.cpp:321-353): A r r^T + B I
+    const double It1 = 0.5 * (P1 - S2);
+    const double It2u = P3 * ph.inv_cp2 - S4 * ph.inv_cs2;
+    const double invDiv = inv_r * ph.inv_4pi_rho;
+    const double A = (3 * It1 + It2u) * invDiv;
+    const double B = (S4 * ph.inv_cs2 - It1) * invDiv;
+    // DT (GreenFunctionT.cpp:360-406): alpha rdn r r^T + beta n r^T + gamma (r n^T + rdn I)
+    const double It2t = S4 - ph.ratio2 * P3;
+    const double It3t = S6 - ph.ratio3 * P5;
+    const double It4 = P3 + roc_p * P5;
+    const double It5 = S4 + roc_s * S6;
+    const double ir2 = inv_r * inv_r * ph.inv_4pi;
+    const double Q = 6 * ph.cs2 * It1 - 2 * It2t;
+    const double alpha = ((-30 * ph.cs2) * It1 + 12 * It2t) * ir2 +
+                         (2 * ph.inv_cs * ph.inv_4pi) * inv_r * It3t;
+    const double beta = (Q - (1 - 2 * ph.ratio2) * It4) * ir2;
+    const double gamma = (Q - It5) * ir2;
+
+    const double rr00 = rv[0] * rv[0], rr01 = rv[0] * rv[1], rr02 = rv[0] * rv[2];
+    const double rr11 = rv[1] * rv[1], rr12 = rv[1] * rv[2], rr22 = rv[2] * rv[2];
+    const double sg[6] = {A * rr00 + B, A * rr01, A * rr02, A * rr11 + B, A * rr12, A * rr22 + B};
+    const double ar = alpha * rdn, gd = gamma * rdn;
+    // T[i][j] = DT[j][i] = ar r_i r_j + beta n_j r_i + gamma n_i r_j (+ gamma rdn on i == j)
+    double th[9];
+    const double rrm[9] = {rr00, rr01, rr02, rr01, rr11, rr12, rr02, rr12, rr22};
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            th[i * 3 + j] = ar * rrm[i * 3 + j] + beta * (nq[j] * rv[i]) +
+                            gamma * (nq[i] * rv[j]) + (i == j ? gd : 0.0);
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const double w = wJ * N[a];
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] += w * sg[m];
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] += w * th[m];
+    }
+}
+
+__global__ void k_gauss_geom(const double* __restrict__ coords, const int* __restrict__ ien,
+                             int nel, int nq, const double* __restrict__ gx,
+                             const double* __restrict__ gw, double* __restrict__ geom) {
+    const int nq2 = nq * nq;
+    const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (gid >= (long long)nel * nq2) return;
+    const int e = (int)(gid / nq2), q = (int)(gid % nq2);
+    double c[12];
+    for (int a = 0; a < 4; a++) {
+        const int nid = ien[e * 4 + a];
+        for (int d = 0; d < 3; d++) c[a * 3 + d] = coords[nid * 3 + d];
+    }
+    // FormGH_Regular's loop order: q_1 outer, q_2 inner (TDElementStepLinearT.cpp:52-56)
+    const int q1 = q / nq, q2 = q % nq;
+    double N[4], x[3], n[3], J;
+    q4_eval(c, gx[q1], gx[q2], N, x, n, J);
+    double* g = geom + gid * kGeomStride;
+    g[0] = x[0];
+    g[1] = x[1];
+    g[2] = x[2];
+    g[3] = n[0];
+    g[4] = n[1];
+    g[5] = n[2];
+    g[6] = (gw[q1] * gw[q2]) * J;
+    g[7] = N[0];
+    g[8] = N[1];
+    g[9] = N[2];
+    g[10] = N[3];
+    g[11] = 0;
+}
+
+// Singular test of ElastoDynamicsT::G_H_Driver (ElastoDynamicsT.cpp:166-175):
+// the last element node with r^2 < 1e-9 (unfused, as the reference's pow sum).
+__device__ __forceinline__ int singular_corner(const double* c, const double xc[3]) {
+    int s = -1;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const double dx = c[a * 3] - xc[0], dy = c[a * 3 + 1] - xc[1], dz = c[a * 3 + 2] - xc[2];
+        const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        if (r2 < 1e-9) s = a;
+    }
+    return s;
+}
+
+__global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
+                              const int* __restrict__ elems, int ne, int node_lo, int nnodes,
+                              Phys ph, int mode, int level_last, int step_n,
+                              PairInfo* __restrict__ pairs, unsigned* __restrict__ counts) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= (long long)nnodes * ne) return;
+    const int c = node_lo + (int)(p / ne);
+    const int e = elems[p % ne];
+    const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
+    double nd[12];
+    double ctr[3] = {0, 0, 0};
+    for (int a = 0; a < 4; a++) {
+        const int nid = ien[e * 4 + a];
+        for (int d = 0; d < 3; d++) {
+            nd[a * 3 + d] = coords[nid * 3 + d];
+            ctr[d] += 0.25 * nd[a * 3 + d];
+        }
+    }
+    double rad = 0;
+    for (int a = 0; a < 4; a++) {
+        const double dx = nd[a * 3] - ctr[0], dy = nd[a * 3 + 1] - ctr[1], dz = nd[a * 3 + 2] - ctr[2];
+        rad = fmax(rad, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    const double dx = xc[0] - ctr[0], dy = xc[1] - ctr[1], dz = xc[2] - ctr[2];
+    const double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    const double margin = 1e-3 * rad + 1e-12;
+    const double rmin = fmax(0.0, dist - rad - margin), rmax = dist + rad + margin;
+    const int sing = singular_corner(nd, xc);
+    // the step response at time n dt can be non-zero only for n_lo <= n <= n_hi
+    int n_lo = (int)floor(rmin * ph.inv_cp * ph.inv_dt) - 1;
+    const int n_hi = (int)ceil(rmax * ph.inv_cs * ph.inv_dt) + 3;
+    if (sing >= 0) n_lo = 0;
+    PairInfo pi;
+    pi.sing = sing;
+    if (mode == ASM_LEVELS) {
+        // level k takes n = k (I part) and n = k + 1 (J part)
+        const int klo = max(0, n_lo - 1);
+        const int khi = min(level_last, n_hi);
+        pi.klo = klo;
+        pi.cnt = max(0, khi - klo + 1);
+    } else {
+        pi.klo = step_n;
+        pi.cnt = (step_n >= n_lo && step_n <= n_hi) ? 1 : 0;
+    }
+    pairs[p] = pi;
+    counts[p] = (unsigned)pi.cnt;
+}
+
+// mode ASM_LEVELS: item = (pair, level k), I part at k dt (k >= 1) plus J part at
+// (k+1) dt ((k+1) <= level_last), scattered into level k of G0/H0 (or the FP32 store).
+// mode ASM_STEP:   item = (pair, step_n), part = 0 -> I part into G0/H0,
+//                  part = 1 -> J part into G1/H1 (row block starting at row_node_lo).
+template <int MODE>
+__global__ void __launch_bounds__(128) k_assemble_items(
+    const double* __restrict__ coords, const int* __restrict__ ien,
+    const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
+    const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
+    int step_n, int part, const PairInfo* __restrict__ pairs,
+    const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= nitems) return;
+    // the pair owning this item: last p with offsets[p] <= gid
+    unsigned lo = 0, hi = npairs - 1;
+    while (lo < hi) {
+        const unsigned mid = (lo + hi + 1) >> 1;
+        if (__ldg(offsets + mid) <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    const unsigned p = lo;
+    const PairInfo pi = pairs[p];
+    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
+    const int c = node_lo + (int)(p / ne);
+    const int e = elems[p % ne];
+    const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
+    int nid[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
+
+    TimeConsts tc;
+    if (MODE == ASM_LEVELS) {
+        tc.doI = (k >= 1);
+        tc.doJ = (k + 1 <= level_last);
+        time_consts(tc, k * ph.dt, (k + 1) * ph.dt, ph.dt);
+    } else {
+        tc.doI = (part == 0);
+        tc.doJ = (part == 1);
+        time_consts(tc, step_n * ph.dt, step_n * ph.dt, ph.dt);
+    }
+
+    ItemAcc acc;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] = 0;
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] = 0;
+    }
+    const int nq2 = nq * nq;
+    if (pi.sing < 0) {
+        const double* g = geom + (size_t)e * nq2 * kGeomStride;
+        for (int q = 0; q < nq2; q++, g += kGeomStride) {
+            const double xq[3] = {__ldg(g), __ldg(g + 1), __ldg(g + 2)};
+            const double nqv[3] = {__ldg(g + 3), __ldg(g + 4), __ldg(g + 5)};
+            const double N[4] = {__ldg(g + 7), __ldg(g + 8), __ldg(g + 9), __ldg(g + 10)};
+            gauss_point(acc, tc, ph, xc, xq, nqv, __ldg(g + 6), N);
+        }
+    } else {
+        double cn[12];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int d = 0; d < 3; d++) cn[a * 3 + d] = coords[nid[a] * 3 + d];
+        for (int qq = 0; qq < 2 * nq2; qq++) {
+            const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+            double N[4], xq[3], nqv[3], wJ;
+            duffy_point(cn, pi.sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nqv, wJ);
+            gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
+        }
+    }
+
+    // scatter: rows 3c+i, columns 3*nid[a]+j
+    const size_t D = (size_t)out.D;
+    double* G;
+    double* H;
+    float* Gf = nullptr;
+    float* Hf = nullptr;
+    size_t rowbase;
+    if (MODE == ASM_LEVELS) {
+        G = out.G0;
+        H = out.H0;
+        Gf = out.G0f;
+        Hf = out.H0f;
+        rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
+    } else {
+        G = part == 0 ? out.G0 : out.G1;
+        H = part == 0 ? out.H0 : out.H1;
+        rowbase = (size_t)(3 * (c - out.row_node_lo)) * D;
+    }
+    constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const size_t idx = rowbase + (size_t)i * D + 3 * (size_t)nid[a] + j;
+                if (Gf) {
+                    Gf[idx] += (float)acc.g[a][sym[i * 3 + j]];
+                    Hf[idx] += (float)acc.h[a][i * 3 + j];
+                } else {
+                    G[idx] += acc.g[a][sym[i * 3 + j]];
+                    H[idx] += acc.h[a][i * 3 + j];
+                }
+            }
+}
+
+// C term (TDElementStepLinearT.cpp:103-109, 501-508, 577-584 with AssembleC,
+// ElastoDynamicsT.cpp:261-280): C_c = -sum_e sum_q wJ DT_Kelvin(q)^T over the whole
+// surface, added to the diagonal block of the first step's I and J parts, plus the
+// exterior free term 0.5 dt I (ElastoDynamicsT.cpp:212-225).  One block per node,
+// fixed-order tree reduction.
+__global__ void __launch_bounds__(128) k_cterm(const double* __restrict__ coords,
+                                               const int* __restrict__ ien, int nel,
+                                               int node_lo, int nq,
+                                               const double* __restrict__ gx,
+                                               const double* __restrict__ gw,
+                                               const double* __restrict__ geom, Phys ph,
+                                               int if_ext, int mode, AsmOut out) {
+    const int c = node_lo + blockIdx.x;
+    const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int nq2 = nq * nq;
+    const double div0 = -(8 * M_PI) * (1 - ph.nu);
+    const double onem2nu = 1 - 2 * ph.nu;
+    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
+        double cn[12];
+        for (int a = 0; a < 4; a++) {
+            const int nid = ien[e * 4 + a];
+            for (int d = 0; d < 3; d++) cn[a * 3 + d] = coords[nid * 3 + d];
+        }
+        const int sing = singular_corner(cn, xc);
+        const int npts = sing < 0 ? nq2 : 2 * nq2;
+        for (int qq = 0; qq < npts; qq++) {
+            double xq[3], nv[3], wJ;
+            if (sing < 0) {
+                const double* g = geom + ((size_t)e * nq2 + qq) * kGeomStride;
+                xq[0] = g[0]; xq[1] = g[1]; xq[2] = g[2];
+                nv[0] = g[3]; nv[1] = g[4]; nv[2] = g[5];
+                wJ = g[6];
+            } else {
+                const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+                double N[4];
+                duffy_point(cn, sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
+            }
+            const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
+            const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+            const double rv[3] = {d0 / r, d1 / r, d2 / r};
+            const double rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
+            // Kelvin_Linear (GreenFunctionT.cpp:205-231), K[i][k]; C[i][k] -= wJ K[k][i]
+            const double scale = (0.5 * ph.dt) / (div0 * r * r);
+            for (int i = 0; i < 3; i++)
+                for (int kk = 0; kk < 3; kk++) {
+                    const double Kki = ((kk == i ? onem2nu : 0.0) + 3 * rv[kk] * rv[i]) * rdn -
+                                       onem2nu * (rv[i] * nv[kk] - rv[kk] * nv[i]);
+                    acc[i * 3 + kk] -= wJ * (Kki * scale);
+                }
+        }
+    }
+    __shared__ double red[9][128];
+    for (int m = 0; m < 9; m++) red[m][threadIdx.x] = acc[m];
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int m = 0; m < 9; m++) red[m][threadIdx.x] += red[m][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    const size_t D = (size_t)out.D;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            const double v = red[i * 3 + j][0] + ((if_ext && i == j) ? 0.5 * ph.dt : 0.0);
+            const size_t off = (size_t)(3 * c + i) * D + 3 * (size_t)c + j;
+            if (mode == ASM_LEVELS) {
+                // level 0 = J(dt), level 1 = I(dt) + J(2dt)
+                if (out.H0f) {
+                    out.H0f[off] += (float)v;
+                    out.H0f[out.level_stride + off] += (float)v;
+                } else {
+                    out.H0[off] += v;
+                    out.H0[out.level_stride + off] += v;
+                }
+            } else {
+                const size_t roff = (size_t)(3 * (c - out.row_node_lo) + i) * D + 3 * (size_t)c + j;
+                out.H0[roff] += v;
+                out.H1[roff] += v;
+            }
+        }
+}
+
+}  // namespace
+
+cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
+                              const double* gx, const double* gw, double* geom,
+                              cudaStream_t s) {
+    const long long n = (long long)nel * nq * nq;
+    const int bs = 128;
+    k_gauss_geom<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
+                               int nelem_color, int node_lo, int nnodes, const Phys& ph,
+                               int mode, int level_last, int step_n, PairInfo* pairs,
+                               unsigned* counts, cudaStream_t s) {
+    const long long n = (long long)nnodes * nelem_color;
+    if (n == 0) return cudaSuccess;
+    const int bs = 256;
+    k_pair_window<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(
+        coords, ien, elems, nelem_color, node_lo, nnodes, ph, mode, level_last, step_n, pairs,
+        counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
+                                  int nelem_color, int node_lo, int nq, const double* gx,
+                                  const double* gw, const double* geom, const Phys& ph,
+                                  int mode, int level_last, int step_n,
+                                  const PairInfo* pairs, const unsigned* offsets,
+                                  unsigned npairs, unsigned nitems, const AsmOut& out,
+                                  int /*precision*/, cudaStream_t s) {
+    if (nitems == 0) return cudaSuccess;
+    const int bs = 128;
+    const unsigned grid = (nitems + bs - 1) / bs;
+    if (mode == ASM_LEVELS) {
+        k_assemble_items<ASM_LEVELS><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
+                                                         node_lo, nq, gx, gw, geom, ph,
+                                                         level_last, step_n, 0, pairs, offsets,
+                                                         npairs, nitems, out);
+    } else {
+        for (int part = 0; part < 2; part++)
+            k_assemble_items<ASM_STEP><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
+                                                           node_lo, nq, gx, gw, geom, ph,
+                                                           level_last, step_n, part, pairs,
+                                                           offsets, npairs, nitems, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
+                         int nnodes, int nq, const double* gx, const double* gw,
+                         const double* geom, const Phys& ph, int if_ext, int mode,
+                         int /*step_n*/, const AsmOut& out, cudaStream_t s) {
+    if (nnodes == 0) return cudaSuccess;
+    k_cterm<<<nnodes, 128, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, if_ext,
+                                   mode, out);
+    return cudaGetLastError();
+}
+
+size_t scan_temp_bytes(unsigned n) {
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (const unsigned*)nullptr, (unsigned*)nullptr,
+                                  (int)n);
+    return bytes;
+}
+
+cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
+                           size_t tmp_bytes, cudaStream_t s) {
+    return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
+}
+
+}  // namespace tdbem

@@ -1,0 +1,770 @@
+// C ABI of tdbem-gb300 (include/tdbem.h): context lifetime, element colouring,
+// and the host-side sequencing of the assembly and marching kernels.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "tdbem_internal.cuh"
+
+using namespace tdbem;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            const int code_ = (e_ == cudaErrorMemoryAllocation) ? TDBEM_ERR_NOMEM        \
+                                                                : TDBEM_ERR_CUDA;        \
+            return fail(code_, "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                       \
+        }                                                                                \
+    } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// Gauss tables of ShapeFunctionT::SetNQ (ShapeFunctionT.cpp:71-169); the
+// 20-point abscissae keep the reference's unsigned entry 19 (ShapeFunctionT.cpp:121).
+bool gauss_table(int nq, std::vector<double>& x, std::vector<double>& w) {
+    static const double x6[] = {0.6612093864662645, -0.6612093864662645, -0.2386191860831969,
+                                0.2386191860831969, -0.9324695142031521, 0.9324695142031521};
+    static const double w6[] = {0.3607615730481386, 0.3607615730481386, 0.4679139345726910,
+                                0.4679139345726910, 0.1713244923791704, 0.1713244923791704};
+    static const double x10[] = {-0.148874339, 0.148874339, -0.433395394, 0.433395394,
+                                 -0.679409568, 0.679409568, -0.865063367, 0.865063367,
+                                 -0.973906529, 0.973906529};
+    static const double w10[] = {0.295524225, 0.295524225, 0.269266719, 0.269266719,
+                                 0.219086363, 0.219086363, 0.149451349, 0.149451349,
+                                 0.066671344, 0.066671344};
+    static const double x20[] = {-0.076526521, 0.076526521, -0.227785851, 0.227785851,
+                                 -0.373706089, 0.373706089, -0.510867002, 0.510867002,
+                                 -0.636053681, 0.636053681, -0.746331906, 0.746331906,
+                                 -0.839116972, 0.839116972, -0.912234428, 0.912234428,
+                                 -0.963971927, 0.963971927, 0.993128599, 0.993128599};
+    static const double w20[] = {0.152753387, 0.152753387, 0.149172986, 0.149172986,
+                                 0.142096109, 0.142096109, 0.131688638, 0.131688638,
+                                 0.118194532, 0.118194532, 0.10193012,  0.10193012,
+                                 0.083276742, 0.083276742, 0.062672048, 0.062672048,
+                                 0.04060143,  0.04060143,  0.017614007, 0.017614007};
+    static const double x40[] = {
+        -0.0387724175060508, 0.0387724175060508, -0.1160840706752552, 0.1160840706752552,
+        -0.1926975807013711, 0.1926975807013711, -0.2681521850072537, 0.2681521850072537,
+        -0.3419940908257585, 0.3419940908257585, -0.4137792043716050, 0.4137792043716050,
+        -0.4830758016861787, 0.4830758016861787, -0.5494671250951282, 0.5494671250951282,
+        -0.6125538896679802, 0.6125538896679802, -0.6719566846141796, 0.6719566846141796,
+        -0.7273182551899271, 0.7273182551899271, -0.7783056514265194, 0.7783056514265194,
+        -0.8246122308333117, 0.8246122308333117, -0.8659595032122595, 0.8659595032122595,
+        -0.9020988069688743, 0.9020988069688743, -0.9328128082786765, 0.9328128082786765,
+        -0.9579168192137917, 0.9579168192137917, -0.9772599499837743, 0.9772599499837743,
+        -0.9907262386994570, 0.9907262386994570, -0.9982377097105593, 0.9982377097105593};
+    static const double w40[] = {
+        0.0775059479784248, 0.0775059479784248, 0.0770398181642480, 0.0770398181642480,
+        0.0761103619006262, 0.0761103619006262, 0.0747231690579683, 0.0747231690579683,
+        0.0728865823958041, 0.0728865823958041, 0.0706116473912868, 0.0706116473912868,
+        0.0679120458152339, 0.0679120458152339, 0.0648040134566010, 0.0648040134566010,
+        0.0613062424929289, 0.0613062424929289, 0.0574397690993916, 0.0574397690993916,
+        0.0532278469839368, 0.0532278469839368, 0.0486958076350722, 0.0486958076350722,
+        0.0438709081856733, 0.0438709081856733, 0.0387821679744720, 0.0387821679744720,
+        0.0334601952825478, 0.0334601952825478, 0.0279370069800234, 0.0279370069800234,
+        0.0222458491941670, 0.0222458491941670, 0.0164210583819079, 0.0164210583819079,
+        0.0104982845311528, 0.0104982845311528, 0.0045212770985332, 0.0045212770985332};
+    const double *px, *pw;
+    switch (nq) {
+    case 6: px = x6; pw = w6; break;
+    case 10: px = x10; pw = w10; break;
+    case 20: px = x20; pw = w20; break;
+    case 40: px = x40; pw = w40; break;
+    default: return false;
+    }
+    x.assign(px, px + nq);
+    w.assign(pw, pw + nq);
+    return true;
+}
+
+// SolverT::ComputeMaxStep (SolverT.cpp:211-250), same arithmetic.
+int compute_max_step(const std::vector<double>& x, int nnd, double E, double nu, double rho,
+                     double dt) {
+    const double Mu = E / (2.0 * (1.0 + nu));
+    const double Cs = std::sqrt(Mu / rho);
+    double max_dis = 0;
+    for (int i = 0; i < nnd - 1; i++)
+        for (int j = i + 1; j < nnd; j++) {
+            double t = 0;
+            for (int d = 0; d < 3; d++) {
+                const double v = x[i * 3 + d] - x[j * 3 + d];
+                t += v * v;
+            }
+            t = std::sqrt(t);
+            if (t > max_dis) max_dis = t;
+        }
+    return (int)(std::ceil(max_dis / (Cs * dt)) + 1);
+}
+
+// Greedy colouring: no two elements of one colour share a node.
+void color_elements(const std::vector<int>& ien, int nel, int nnd, std::vector<int>& order,
+                    std::vector<int>& start) {
+    std::vector<std::vector<int>> node_elems(nnd);
+    for (int e = 0; e < nel; e++)
+        for (int a = 0; a < 4; a++) node_elems[ien[e * 4 + a]].push_back(e);
+    std::vector<int> color(nel, -1);
+    int ncolor = 0;
+    std::vector<int> used;
+    for (int e = 0; e < nel; e++) {
+        used.assign(ncolor + 1, 0);
+        for (int a = 0; a < 4; a++)
+            for (int o : node_elems[ien[e * 4 + a]])
+                if (color[o] >= 0) used[color[o]] = 1;
+        int c = 0;
+        while (c < ncolor && used[c]) c++;
+        color[e] = c;
+        if (c == ncolor) ncolor++;
+    }
+    start.assign(ncolor + 1, 0);
+    for (int e = 0; e < nel; e++) start[color[e] + 1]++;
+    for (int c = 0; c < ncolor; c++) start[c + 1] += start[c];
+    order.assign(nel, 0);
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int e = 0; e < nel; e++) order[fill[color[e]]++] = e;
+}
+
+void free_levels(tdbem_ctx* c) {
+    dfree(c->d_G);
+    dfree(c->d_H);
+    dfree(c->d_Gf);
+    dfree(c->d_Hf);
+    c->level_precision = -1;
+    c->levels_last = 0;
+}
+
+void free_march(tdbem_ctx* c) {
+    dfree(c->d_u);
+    dfree(c->d_t);
+    if (c->d_Ainv[1] == c->d_Ainv[0]) c->d_Ainv[1] = nullptr;
+    dfree(c->d_Ainv[0]);
+    dfree(c->d_Ainv[1]);
+    c->hist_steps = -1;
+}
+
+// Algorithmic FP64 operations of one (item, Gauss point) of the level quadrature
+// with both the I and the J part (FMA = 2): geometry 22, four I-part and four
+// J-part wave integrals with their differences 150, kernel scalars 37, the two
+// 3x3 kernels 65, accumulation into the 4 node blocks 124.
+constexpr double kFlopsPerItemPoint = 398.0;
+
+int prof_begin(tdbem_ctx* c, int cls) {
+    if (!c->prof) return -1;
+    tdbem_ctx::ProfEvent ev{cls, nullptr, nullptr, 0, 0};
+    cudaEventCreate(&ev.a);
+    cudaEventCreate(&ev.b);
+    cudaEventRecord(ev.a, c->stream);
+    c->prof_pending.push_back(ev);
+    return (int)c->prof_pending.size() - 1;
+}
+
+void prof_end(tdbem_ctx* c, int idx, double bytes, double flops) {
+    if (idx < 0) return;
+    auto& ev = c->prof_pending[idx];
+    cudaEventRecord(ev.b, c->stream);
+    ev.bytes = bytes;
+    ev.flops = flops;
+}
+
+// Resolve pending event pairs (the stream must have been synchronised).
+void prof_flush(tdbem_ctx* c) {
+    for (auto& ev : c->prof_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, ev.a, ev.b) == cudaSuccess) {
+            c->prof_launches[ev.cls]++;
+            c->prof_ms[ev.cls] += ms;
+            c->prof_bytes[ev.cls] += ev.bytes;
+            c->prof_flops[ev.cls] += ev.flops;
+        }
+        cudaEventDestroy(ev.a);
+        cudaEventDestroy(ev.b);
+    }
+    c->prof_pending.clear();
+    cudaGetLastError();
+}
+
+// Run the window / scan / item kernels of one colour over collocation nodes
+// [node_lo, node_lo + nnodes), chunked so that item indices fit in 32 bits.
+int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, int level_last,
+                   int step_n, const AsmOut& out, int precision) {
+    const int e0 = c->color_start[color], ne = c->color_start[color + 1] - e0;
+    if (ne == 0 || nnodes == 0) return TDBEM_OK;
+    const int* elems = c->d_color_elems + e0;
+    const long long per_node_items = (long long)ne * (mode == ASM_LEVELS ? level_last + 1 : 1);
+    const long long max_nodes_items = (1LL << 31) / std::max(1LL, per_node_items);
+    const long long max_nodes_pairs = (long long)c->pair_cap / ne;
+    const int chunk = (int)std::max(1LL, std::min(max_nodes_items, max_nodes_pairs));
+    for (int n0 = node_lo; n0 < node_lo + nnodes; n0 += chunk) {
+        const int nn = std::min(chunk, node_lo + nnodes - n0);
+        const unsigned npairs = (unsigned)((long long)nn * ne);
+        CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, elems, ne, n0, nn, c->ph, mode,
+                                    level_last, step_n, c->d_pairs, c->d_counts, c->stream));
+        CUDA_TRY(exclusive_scan(c->d_counts, c->d_offsets, npairs, c->d_scan_tmp,
+                                c->scan_tmp_bytes, c->stream));
+        c->launches += 3;  // window + the scan's init and scan kernels
+        unsigned last[2];
+        CUDA_TRY(cudaMemcpyAsync(&last[0], c->d_offsets + npairs - 1, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaMemcpyAsync(&last[1], c->d_counts + npairs - 1, sizeof(unsigned),
+                                 cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        const unsigned nitems = last[0] + last[1];
+        const int pe = prof_begin(c, TDBEM_K_ASSEMBLE);
+        CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, elems, ne, n0, c->nq, c->d_gx,
+                                       c->d_gw, c->d_geom, c->ph, mode, level_last, step_n,
+                                       c->d_pairs, c->d_offsets, npairs, nitems, out, precision,
+                                       c->stream));
+        if (nitems) c->launches += (mode == ASM_STEP ? 2 : 1);
+        const double pts = (double)c->nq * c->nq;
+        const double items = (double)nitems * (mode == ASM_STEP ? 2.0 : 1.0);
+        prof_end(c, pe, items * 4 * 45 * (precision == TDBEM_FP64 ? 8.0 : 4.0) * 2,
+                 items * pts * kFlopsPerItemPoint * (mode == ASM_STEP ? 0.5 : 1.0));
+    }
+    return TDBEM_OK;
+}
+
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer() {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+    }
+    ~EventTimer() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    void start(cudaStream_t s) { cudaEventRecord(a, s); }
+    double stop_ms(cudaStream_t s) {
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* tdbem_last_error(void) { return g_last_error.c_str(); }
+
+const char* tdbem_version(void) { return "tdbem-gb300 0.1 (sm_103a)"; }
+
+int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double dt, int nq,
+                     int if_ext, tdbem_ctx** out) {
+    if (!out) return fail(TDBEM_ERR_ARG, "out is null");
+    *out = nullptr;
+    if (!mesh || !mat || !mesh->coords || !mesh->ien)
+        return fail(TDBEM_ERR_ARG, "mesh/material pointers are null");
+    if (mesh->etype != 1)
+        return fail(TDBEM_ERR_UNSUPPORTED, "element type %d: only 4-node quads (EType=1)",
+                    mesh->etype);
+    if (mesh->nnd < 2 || mesh->nel < 1) return fail(TDBEM_ERR_ARG, "empty mesh");
+    if (!(dt > 0) || !(mat->rho > 0) || !(mat->E > 0) || !(mat->nu > -1 && mat->nu < 0.5))
+        return fail(TDBEM_ERR_ARG, "invalid dt or material");
+    std::vector<double> gx, gw;
+    if (!gauss_table(nq, gx, gw))
+        return fail(TDBEM_ERR_ARG, "unsupported number of Gauss points %d", nq);
+    for (long long i = 0; i < 4LL * mesh->nel; i++)
+        if (mesh->ien[i] < 0 || mesh->ien[i] >= mesh->nnd)
+            return fail(TDBEM_ERR_ARG, "IEN entry %lld = %d out of range", i, mesh->ien[i]);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(TDBEM_ERR_CUDA, "no CUDA device available (tdbem has no CPU path)");
+    }
+    tdbem_ctx* c = new (std::nothrow) tdbem_ctx;
+    if (!c) return fail(TDBEM_ERR_NOMEM, "host allocation failed");
+    cudaGetDevice(&c->device);
+    c->nnd = mesh->nnd;
+    c->nel = mesh->nel;
+    c->D = 3 * mesh->nnd;
+    c->nq = nq;
+    c->if_ext = if_ext ? 1 : 0;
+    c->E = mat->E;
+    c->nu = mat->nu;
+    c->rho = mat->rho;
+    c->dt = dt;
+    c->h_coords.assign(mesh->coords, mesh->coords + 3 * (size_t)mesh->nnd);
+    c->h_ien.assign(mesh->ien, mesh->ien + 4 * (size_t)mesh->nel);
+    c->M = compute_max_step(c->h_coords, c->nnd, c->E, c->nu, c->rho, dt);
+    // GreenFunctionT::WaveSpeed (GreenFunctionT.cpp:76-84)
+    const double mu = c->E / (2 * (1 + c->nu));
+    const double lam = c->E * c->nu / ((1 + c->nu) * (1 - 2 * c->nu));
+    Phys& ph = c->ph;
+    ph.dt = dt;
+    ph.inv_dt = 1.0 / dt;
+    ph.cp = std::sqrt((lam + 2 * mu) / c->rho);
+    ph.cs = std::sqrt(mu / c->rho);
+    ph.inv_cp = 1.0 / ph.cp;
+    ph.inv_cs = 1.0 / ph.cs;
+    ph.inv_cp2 = 1.0 / (ph.cp * ph.cp);
+    ph.inv_cs2 = 1.0 / (ph.cs * ph.cs);
+    ph.cs2 = ph.cs * ph.cs;
+    ph.ratio2 = (ph.cs / ph.cp) * (ph.cs / ph.cp);
+    ph.ratio3 = ph.ratio2 * (ph.cs / ph.cp);
+    ph.inv_4pi_rho = 1.0 / (4 * M_PI * c->rho);
+    ph.inv_4pi = 1.0 / (4 * M_PI);
+    ph.nu = c->nu;
+    std::vector<int> order;
+    color_elements(c->h_ien, c->nel, c->nnd, order, c->color_start);
+    int max_color = 0;
+    for (size_t k = 0; k + 1 < c->color_start.size(); k++)
+        max_color = std::max(max_color, c->color_start[k + 1] - c->color_start[k]);
+    auto cleanup_fail = [&](int code) {
+        tdbem_ctx_destroy(c);
+        return code;
+    };
+#define CTX_TRY(expr)                                                                        \
+    do {                                                                                     \
+        cudaError_t e_ = (expr);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            fail(e_ == cudaErrorMemoryAllocation ? TDBEM_ERR_NOMEM : TDBEM_ERR_CUDA, "%s: %s", \
+                 #expr, cudaGetErrorString(e_));                                             \
+            return cleanup_fail(e_ == cudaErrorMemoryAllocation ? TDBEM_ERR_NOMEM           \
+                                                                : TDBEM_ERR_CUDA);          \
+        }                                                                                    \
+    } while (0)
+    CTX_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CTX_TRY(dalloc(&c->d_coords, c->h_coords.size()));
+    CTX_TRY(dalloc(&c->d_ien, c->h_ien.size()));
+    CTX_TRY(dalloc(&c->d_gx, nq));
+    CTX_TRY(dalloc(&c->d_gw, nq));
+    CTX_TRY(dalloc(&c->d_geom, (size_t)c->nel * nq * nq * 12));
+    CTX_TRY(dalloc(&c->d_color_elems, order.size()));
+    CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
+                            cudaMemcpyHostToDevice, c->stream));
+    CTX_TRY(cudaMemcpyAsync(c->d_ien, c->h_ien.data(), sizeof(int) * c->h_ien.size(),
+                            cudaMemcpyHostToDevice, c->stream));
+    CTX_TRY(cudaMemcpyAsync(c->d_gx, gx.data(), sizeof(double) * nq, cudaMemcpyHostToDevice,
+                            c->stream));
+    CTX_TRY(cudaMemcpyAsync(c->d_gw, gw.data(), sizeof(double) * nq, cudaMemcpyHostToDevice,
+                            c->stream));
+    CTX_TRY(cudaMemcpyAsync(c->d_color_elems, order.data(), sizeof(int) * order.size(),
+                            cudaMemcpyHostToDevice, c->stream));
+    CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, nq, c->d_gx, c->d_gw, c->d_geom,
+                              c->stream));
+    c->pair_cap = std::min<size_t>((size_t)c->nnd * max_color, (size_t)1 << 26);
+    c->pair_cap = std::max<size_t>(c->pair_cap, (size_t)max_color);
+    CTX_TRY(dalloc(&c->d_pairs, c->pair_cap));
+    CTX_TRY(dalloc(&c->d_counts, c->pair_cap));
+    CTX_TRY(dalloc(&c->d_offsets, c->pair_cap));
+    c->scan_tmp_bytes = scan_temp_bytes((unsigned)c->pair_cap);
+    CTX_TRY(cudaMalloc(&c->d_scan_tmp, std::max<size_t>(c->scan_tmp_bytes, 16)));
+    CTX_TRY(cudaStreamSynchronize(c->stream));
+#undef CTX_TRY
+    *out = c;
+    return TDBEM_OK;
+}
+
+int tdbem_ctx_destroy(tdbem_ctx* c) {
+    if (!c) return TDBEM_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_levels(c);
+    free_march(c);
+    dfree(c->d_coords);
+    dfree(c->d_ien);
+    dfree(c->d_gx);
+    dfree(c->d_gw);
+    dfree(c->d_geom);
+    dfree(c->d_color_elems);
+    dfree(c->d_pairs);
+    dfree(c->d_counts);
+    dfree(c->d_offsets);
+    if (c->d_scan_tmp) cudaFree(c->d_scan_tmp);
+    dfree(c->d_ubc_map);
+    dfree(c->d_fbc_map);
+    dfree(c->d_is_ubc);
+    dfree(c->d_is_fbc);
+    dfree(c->d_tmp_rows);
+    dfree(c->d_load_t);
+    dfree(c->d_load_u);
+    dfree(c->d_Wt);
+    dfree(c->d_Wu);
+    dfree(c->d_partial);
+    dfree(c->d_rhs);
+    dfree(c->d_x);
+    dfree(c->d_perm);
+    dfree(c->d_colk);
+    dfree(c->d_rowk);
+    dfree(c->d_status);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TDBEM_OK;
+}
+
+int tdbem_max_step(const tdbem_ctx* c, int* M) {
+    if (!c || !M) return fail(TDBEM_ERR_ARG, "null argument");
+    *M = c->M;
+    return TDBEM_OK;
+}
+
+int tdbem_num_dof(const tdbem_ctx* c, int* D) {
+    if (!c || !D) return fail(TDBEM_ERR_ARG, "null argument");
+    *D = c->D;
+    return TDBEM_OK;
+}
+
+int tdbem_get_stream(const tdbem_ctx* c, void** stream) {
+    if (!c || !stream) return fail(TDBEM_ERR_ARG, "null argument");
+    *stream = (void*)c->stream;
+    return TDBEM_OK;
+}
+
+int tdbem_level_bytes(const tdbem_ctx* c, int precision, size_t* bytes) {
+    if (!c || !bytes) return fail(TDBEM_ERR_ARG, "null argument");
+    const size_t per = precision == TDBEM_FP64 ? 8 : 4;
+    *bytes = 2 * (size_t)(c->M + 1) * c->D * (size_t)c->D * per;
+    return TDBEM_OK;
+}
+
+int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_I, double* G_J,
+                    double* H_I, double* H_J) {
+    if (!c || !G_I || !G_J || !H_I || !H_J) return fail(TDBEM_ERR_ARG, "null argument");
+    if (step < 1) return fail(TDBEM_ERR_ARG, "step must be >= 1");
+    if (node_lo < 0 || node_hi >= c->nnd || node_lo > node_hi)
+        return fail(TDBEM_ERR_ARG, "node range [%d, %d] invalid", node_lo, node_hi);
+    const int nn = node_hi - node_lo + 1;
+    const size_t n = (size_t)3 * nn * c->D;
+    double* buf = nullptr;
+    CUDA_TRY(dalloc(&buf, 4 * n));
+    AsmOut out{};
+    out.G0 = buf;
+    out.H0 = buf + n;
+    out.G1 = buf + 2 * n;
+    out.H1 = buf + 3 * n;
+    out.D = c->D;
+    out.row_node_lo = node_lo;
+    int rc = TDBEM_OK;
+    cudaError_t e = cudaMemsetAsync(buf, 0, sizeof(double) * 4 * n, c->stream);
+    if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
+    for (size_t col = 0; rc == TDBEM_OK && col + 1 < c->color_start.size(); col++)
+        rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, step, out, TDBEM_FP64);
+    if (rc == TDBEM_OK && step == 1) {
+        e = launch_cterm(c->d_coords, c->d_ien, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
+                         c->d_geom, c->ph, c->if_ext, ASM_STEP, step, out, c->stream);
+        if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "cterm: %s", cudaGetErrorString(e));
+    }
+    double* hosts[4] = {G_I, H_I, G_J, H_J};
+    for (int k = 0; rc == TDBEM_OK && k < 4; k++) {
+        e = cudaMemcpyAsync(hosts[k], buf + k * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                            c->stream);
+        if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "copy: %s", cudaGetErrorString(e));
+    }
+    e = cudaStreamSynchronize(c->stream);
+    if (rc == TDBEM_OK && e != cudaSuccess)
+        rc = fail(TDBEM_ERR_CUDA, "gh_driver: %s", cudaGetErrorString(e));
+    cudaFree(buf);
+    return rc;
+}
+
+int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (nsteps < 1) return fail(TDBEM_ERR_ARG, "nsteps must be >= 1");
+    if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
+        return fail(TDBEM_ERR_ARG, "unknown precision %d", precision);
+    const size_t stride = (size_t)c->D * c->D;
+    const size_t total = (size_t)(c->M + 1) * stride;
+    if (c->level_precision != precision) {
+        free_levels(c);
+        if (precision == TDBEM_FP64) {
+            CUDA_TRY(dalloc(&c->d_G, total));
+            CUDA_TRY(dalloc(&c->d_H, total));
+        } else {
+            CUDA_TRY(dalloc(&c->d_Gf, total));
+            CUDA_TRY(dalloc(&c->d_Hf, total));
+        }
+        c->level_precision = precision;
+    }
+    EventTimer tm;
+    tm.start(c->stream);
+    const size_t esz = precision == TDBEM_FP64 ? 8 : 4;
+    void* G = precision == TDBEM_FP64 ? (void*)c->d_G : (void*)c->d_Gf;
+    void* H = precision == TDBEM_FP64 ? (void*)c->d_H : (void*)c->d_Hf;
+    CUDA_TRY(cudaMemsetAsync(G, 0, esz * total, c->stream));
+    CUDA_TRY(cudaMemsetAsync(H, 0, esz * total, c->stream));
+    const int last = std::min(c->M, nsteps);
+    AsmOut out{};
+    out.G0 = c->d_G;
+    out.H0 = c->d_H;
+    out.G0f = c->d_Gf;
+    out.H0f = c->d_Hf;
+    out.level_stride = stride;
+    out.D = c->D;
+    for (size_t col = 0; col + 1 < c->color_start.size(); col++) {
+        const int rc = assemble_color(c, (int)col, 0, c->nnd, ASM_LEVELS, last, 0, out, precision);
+        if (rc != TDBEM_OK) return rc;
+    }
+    CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+                          c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, out, c->stream));
+    c->launches += 1;
+    c->timings[0] = tm.stop_ms(c->stream);
+    CUDA_TRY(cudaGetLastError());
+    prof_flush(c);
+    c->levels_last = last;
+    return TDBEM_OK;
+}
+
+int tdbem_get_level(tdbem_ctx* c, int k, int which, double* host_out) {
+    if (!c || !host_out) return fail(TDBEM_ERR_ARG, "null argument");
+    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
+    if (k < 0 || k > c->M || (which != 0 && which != 1))
+        return fail(TDBEM_ERR_ARG, "level %d / which %d out of range", k, which);
+    const size_t stride = (size_t)c->D * c->D;
+    if (c->level_precision == TDBEM_FP64) {
+        const double* src = (which == 0 ? c->d_G : c->d_H) + k * stride;
+        CUDA_TRY(cudaMemcpyAsync(host_out, src, sizeof(double) * stride, cudaMemcpyDeviceToHost,
+                                 c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    } else {
+        std::vector<float> tmp(stride);
+        const float* src = (which == 0 ? c->d_Gf : c->d_Hf) + k * stride;
+        CUDA_TRY(cudaMemcpyAsync(tmp.data(), src, sizeof(float) * stride, cudaMemcpyDeviceToHost,
+                                 c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+        for (size_t i = 0; i < stride; i++) host_out[i] = tmp[i];
+    }
+    return TDBEM_OK;
+}
+
+int tdbem_set_bc(tdbem_ctx* c, const int* ubc_dofs, const double* ubc_vals, int n_u,
+                 const int* fbc_dofs, const double* fbc_vals, int n_f) {
+    if (!c || n_u < 0 || n_f < 0 || (n_u && (!ubc_dofs || !ubc_vals)) ||
+        (n_f && (!fbc_dofs || !fbc_vals)))
+        return fail(TDBEM_ERR_ARG, "invalid boundary-condition arrays");
+    for (int i = 0; i < n_u; i++)
+        if (ubc_dofs[i] < 0 || ubc_dofs[i] >= c->D)
+            return fail(TDBEM_ERR_ARG, "UBC dof %d out of range", ubc_dofs[i]);
+    for (int i = 0; i < n_f; i++)
+        if (fbc_dofs[i] < 0 || fbc_dofs[i] >= c->D)
+            return fail(TDBEM_ERR_ARG, "FBC dof %d out of range", fbc_dofs[i]);
+    c->ubc.assign(ubc_dofs, ubc_dofs + n_u);
+    c->ubc_v.assign(ubc_vals, ubc_vals + n_u);
+    c->fbc.assign(fbc_dofs, fbc_dofs + n_f);
+    c->fbc_v.assign(fbc_vals, fbc_vals + n_f);
+    return TDBEM_OK;
+}
+
+int tdbem_set_alpha(tdbem_ctx* c, double a1, double a2) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    // SolverStepLinearT::Solve_Averaging range check (SolverStepLinearT.cpp:317-322)
+    if (!(a1 >= 0 && a1 <= 1 && a2 >= 0 && a2 < 1 && a1 + a2 <= 1))
+        return fail(TDBEM_ERR_ARG, "Alpha is out of range (alpha_1=%g alpha_2=%g)", a1, a2);
+    c->a1 = a1;
+    c->a2 = a2;
+    return TDBEM_OK;
+}
+
+int tdbem_set_load_history(tdbem_ctx* c, const double* amp, int nsteps) {
+    if (!c || nsteps < 0 || (nsteps && !amp)) return fail(TDBEM_ERR_ARG, "invalid load history");
+    c->amp.assign(amp, amp + nsteps);
+    return TDBEM_OK;
+}
+
+int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (numstep < 1) return fail(TDBEM_ERR_ARG, "numstep must be >= 1");
+    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
+    if (c->levels_last < std::min(c->M, numstep))
+        return fail(TDBEM_ERR_STATE, "levels assembled for %d steps, %d needed", c->levels_last,
+                    std::min(c->M, numstep));
+    if (!c->amp.empty() && (int)c->amp.size() < numstep)
+        return fail(TDBEM_ERR_ARG, "load history has %zu values, %d steps", c->amp.size(),
+                    numstep);
+    const int D = c->D;
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    // per-dof boundary-condition maps; the last list entry of a dof wins (VecSetValues)
+    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
+    std::vector<double> umap(D, 0.0), fmap(D, 0.0), load_t(D, 0.0), load_u(D, 0.0);
+    for (size_t i = 0; i < c->ubc.size(); i++) {
+        is_u[c->ubc[i]] = 1;
+        umap[c->ubc[i]] = c->ubc_v[i];
+    }
+    for (size_t i = 0; i < c->fbc.size(); i++) {
+        is_f[c->fbc[i]] = 1;
+        fmap[c->fbc[i]] = c->fbc_v[i];
+    }
+    for (int j = 0; j < D; j++) {
+        if (is_u[j]) load_u[j] = umap[j];
+        else if (is_f[j]) load_t[j] = fmap[j];
+    }
+    if (!c->d_ubc_map) {
+        CUDA_TRY(dalloc(&c->d_ubc_map, D));
+        CUDA_TRY(dalloc(&c->d_fbc_map, D));
+        CUDA_TRY(dalloc(&c->d_is_ubc, D));
+        CUDA_TRY(dalloc(&c->d_is_fbc, D));
+        CUDA_TRY(dalloc(&c->d_load_t, D));
+        CUDA_TRY(dalloc(&c->d_load_u, D));
+        CUDA_TRY(dalloc(&c->d_Wt, (size_t)(c->M + 1) * D));
+        CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
+        CUDA_TRY(dalloc(&c->d_rhs, D));
+        CUDA_TRY(dalloc(&c->d_x, D));
+        CUDA_TRY(dalloc(&c->d_perm, D));
+        CUDA_TRY(dalloc(&c->d_colk, D));
+        CUDA_TRY(dalloc(&c->d_rowk, D));
+        CUDA_TRY(dalloc(&c->d_status, 1));
+        CUDA_TRY(dalloc(&c->d_tmp_rows, (size_t)kPermuteBlocks * D));
+        c->partial_cap = (size_t)(c->M + 1) * D;
+        CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
+    }
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(c->d_ubc_map, umap.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_fbc_map, fmap.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_is_ubc, is_u.data(), D, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_is_fbc, is_f.data(), D, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_load_t, load_t.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_load_u, load_u.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    if (c->hist_steps != numstep) {
+        dfree(c->d_u);
+        dfree(c->d_t);
+        CUDA_TRY(dalloc(&c->d_u, (size_t)(numstep + 1) * D));
+        CUDA_TRY(dalloc(&c->d_t, (size_t)(numstep + 1) * D));
+        c->hist_steps = numstep;
+    }
+    CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (numstep + 1) * D, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (numstep + 1) * D, s));
+
+    const size_t stride = (size_t)D * D;
+    // LHS of step 2 (SolverStepLinearT.cpp:357-371) and of steps >= 3 (381-393)
+    const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
+    EventTimer tf;
+    tf.start(s);
+    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
+    for (int v = 0; v < 2; v++)
+        if (c->d_Ainv[v] == c->d_Ainv[1 - v]) c->d_Ainv[v] = nullptr;
+    for (int v = 0; v < ninv; v++) {
+        if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
+        CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
+                                  lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
+        const int pe = prof_begin(c, TDBEM_K_FACTOR);
+        cudaError_t e = gje_invert(c->d_Ainv[v], D, c->d_perm, c->d_colk, c->d_rowk, c->d_status,
+                                   c->d_tmp_rows, s);
+        prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
+        c->launches += 1 + 2LL * D + 1;  // LHS build, 2 per column, column permutation
+        if (e == cudaErrorInvalidValue)
+            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
+        CUDA_TRY(e);
+    }
+    if (ninv == 1) {
+        if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
+        c->d_Ainv[1] = c->d_Ainv[0];
+    }
+    c->timings[1] = tf.stop_ms(s);
+
+    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
+    EventTimer tmr;
+    tmr.start(s);
+    for (int curr = 2; curr <= numstep; curr++) {
+        const int st = curr - 1;
+        const int L = std::min(std::max(st, 1), c->M);
+        const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
+        const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
+        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
+        CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
+                                        c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
+        const int nch = conv_chunks(L, D);
+        const double esz = c->d_G ? 8.0 : 4.0;
+        int pe = prof_begin(c, TDBEM_K_CONV);
+        CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
+        prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
+                 (L + 1) * 4.0 * (double)stride);
+        pe = prof_begin(c, TDBEM_K_SOLVE);
+        CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
+                                     c->d_x, s));
+        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
+        prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
+        c->launches += 5;  // combine, conv, reduce, gemv, update
+    }
+    c->timings[2] = tmr.stop_ms(s);
+    if (u_hist)
+        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    if (t_hist)
+        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    prof_flush(c);
+    return TDBEM_OK;
+}
+
+int tdbem_history_device(const tdbem_ctx* c, const double** u_hist, const double** t_hist) {
+    if (!c || !u_hist || !t_hist) return fail(TDBEM_ERR_ARG, "null argument");
+    if (c->hist_steps < 0) return fail(TDBEM_ERR_STATE, "no march has run");
+    *u_hist = c->d_u;
+    *t_hist = c->d_t;
+    return TDBEM_OK;
+}
+
+int tdbem_set_profiling(tdbem_ctx* c, int on) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    prof_flush(c);
+    c->prof = on != 0;
+    for (int k = 0; k < TDBEM_K_COUNT; k++) {
+        c->prof_launches[k] = 0;
+        c->prof_ms[k] = c->prof_bytes[k] = c->prof_flops[k] = 0;
+    }
+    return TDBEM_OK;
+}
+
+int tdbem_kernel_stats(const tdbem_ctx* c, int k, long long* launches, double* ms,
+                       double* bytes, double* flops) {
+    if (!c || k < 0 || k >= TDBEM_K_COUNT) return fail(TDBEM_ERR_ARG, "bad kernel class");
+    if (launches) *launches = c->prof_launches[k];
+    if (ms) *ms = c->prof_ms[k];
+    if (bytes) *bytes = c->prof_bytes[k];
+    if (flops) *flops = c->prof_flops[k];
+    return TDBEM_OK;
+}
+
+int tdbem_launch_count(const tdbem_ctx* c, long long* n) {
+    if (!c || !n) return fail(TDBEM_ERR_ARG, "null argument");
+    *n = c->launches;
+    return TDBEM_OK;
+}
+
+int tdbem_last_timings(const tdbem_ctx* c, double* ms3) {
+    if (!c || !ms3) return fail(TDBEM_ERR_ARG, "null argument");
+    for (int i = 0; i < 3; i++) ms3[i] = c->timings[i];
+    return TDBEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// Internal declarations shared by the tdbem-gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tdbem.h"
+
+namespace tdbem {
+
+// Material / time constants every quadrature kernel needs, passed by value.
+struct Phys {
+    double dt, inv_dt;           // time step T1 and 1/T1
+    double cp, cs;               // wave speeds (GreenFunctionT::WaveSpeed, GreenFunctionT.cpp:76-84)
+    double inv_cp, inv_cs;       // 1/cp, 1/cs
+    double inv_cp2, inv_cs2;     // 1/cp^2, 1/cs^2
+    double cs2;                  // cs^2
+    double ratio2, ratio3;       // (cs/cp)^2, (cs/cp)^3
+    double inv_4pi_rho;          // 1/(4 pi rho)
+    double inv_4pi;              // 1/(4 pi)
+    double nu;                   // Poisson ratio (Kelvin traction)
+};
+
+// Level-window bounds of one (collocation node, element) pair.
+struct PairInfo {
+    int klo;    // first level with a possibly non-zero contribution
+    int cnt;    // number of levels (0 = pair contributes nothing)
+    int sing;   // singular corner (last element node within r^2 < 1e-9), -1 if regular
+};
+
+// Assembly output selection.
+enum AsmMode : int {
+    ASM_LEVELS = 0,  // level k <- I(k dt) + J((k+1) dt)  (UpdateGHLinear placement)
+    ASM_STEP = 1,    // one time n: I part -> out0, J part -> out1 (G_H_Driver outputs)
+};
+
+struct AsmOut {
+    double* G0;   // ASM_LEVELS: G level store; ASM_STEP: G_I rows
+    double* H0;   // ASM_LEVELS: H level store; ASM_STEP: H_I rows
+    double* G1;   // ASM_STEP: G_J rows
+    double* H1;   // ASM_STEP: H_J rows
+    float* G0f;   // FP32 level store (mixed precision), or null
+    float* H0f;
+    size_t level_stride;  // entries per level (D*D) in ASM_LEVELS
+    int D;
+    int row_node_lo;      // first collocation node of the row block
+};
+
+// Launch helpers (assemble.cu).
+cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
+                              const double* gx, const double* gw, double* geom,
+                              cudaStream_t s);
+cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
+                               int nelem_color, int node_lo, int nnodes, const Phys& ph,
+                               int mode, int level_last, int step_n, PairInfo* pairs,
+                               unsigned* counts, cudaStream_t s);
+cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
+                                  int nelem_color, int node_lo, int nq, const double* gx,
+                                  const double* gw, const double* geom, const Phys& ph,
+                                  int mode, int level_last, int step_n,
+                                  const PairInfo* pairs, const unsigned* offsets,
+                                  unsigned npairs, unsigned nitems, const AsmOut& out,
+                                  int precision, cudaStream_t s);
+cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
+                         int nnodes, int nq, const double* gx, const double* gw,
+                         const double* geom, const Phys& ph, int if_ext, int mode,
+                         int step_n, const AsmOut& out, cudaStream_t s);
+size_t scan_temp_bytes(unsigned n);
+cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
+                           size_t tmp_bytes, cudaStream_t s);
+
+// Marching helpers (march.cu).
+struct MarchDev {
+    int D, M;
+    const double* G;   // FP64 level store (M+1) x D x D, or null
+    const double* H;
+    const float* Gf;   // FP32 level store, or null
+    const float* Hf;
+};
+cudaError_t launch_build_lhs(const double* G, const double* H, const float* Gf,
+                             const float* Hf, size_t level_stride, int D, double c0,
+                             double c1, const unsigned char* is_ubc, double* A,
+                             cudaStream_t s);
+constexpr int kPermuteBlocks = 152;  // scratch rows the final GJE column permutation uses
+cudaError_t gje_invert(double* A, int n, int* perm, double* colk, double* rowk,
+                       int* d_status, double* tmp_rows, cudaStream_t s);
+cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
+                                   int L, double a1, double a2, double a3, double c0,
+                                   double c1, double amp, const double* load_t,
+                                   const double* load_u,
+                                   double* Wt, double* Wu, cudaStream_t st);
+cudaError_t launch_conv(const MarchDev& md, int L, const double* Wt, const double* Wu,
+                        double* partial, int nchunks, cudaStream_t s);
+cudaError_t launch_reduce_solve(const double* partial, int nchunks, int D,
+                                const double* Ainv, double* rhs, double* x, cudaStream_t s);
+cudaError_t launch_update_state(const double* x, int D, int s, const unsigned char* is_u,
+                                const double* ubc_val, const unsigned char* is_f,
+                                const double* fbc_val, double amp, double* u_hist,
+                                double* t_hist, cudaStream_t st);
+int conv_chunks(int L, int D);
+
+}  // namespace tdbem
+
+// The context (capi.cu owns its lifetime).
+struct tdbem_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nnd = 0, nel = 0, D = 0, M = 0, nq = 6, if_ext = 0;
+    double E = 0, nu = 0, rho = 0, dt = 0;
+    tdbem::Phys ph{};
+    std::vector<double> h_coords;
+    std::vector<int> h_ien;
+    // device mesh and quadrature tables
+    double* d_coords = nullptr;
+    int* d_ien = nullptr;
+    double* d_gx = nullptr;
+    double* d_gw = nullptr;
+    double* d_geom = nullptr;        // regular Gauss-point geometry, nel x nq^2 x 12
+    // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
+    std::vector<int> color_start;
+    int* d_color_elems = nullptr;
+    // pair/item scratch
+    tdbem::PairInfo* d_pairs = nullptr;
+    unsigned* d_counts = nullptr;
+    unsigned* d_offsets = nullptr;
+    void* d_scan_tmp = nullptr;
+    size_t scan_tmp_bytes = 0;
+    size_t pair_cap = 0;
+    // level store
+    int level_precision = -1;
+    int levels_last = 0;             // levels hold steps 1..levels_last
+    double* d_G = nullptr;
+    double* d_H = nullptr;
+    float* d_Gf = nullptr;
+    float* d_Hf = nullptr;
+    // boundary conditions and marching parameters
+    std::vector<int> ubc, fbc;
+    std::vector<double> ubc_v, fbc_v;
+    double a1 = 0, a2 = 0;
+    std::vector<double> amp;
+    // marching buffers
+    int hist_steps = -1;
+    double* d_u = nullptr;
+    double* d_t = nullptr;
+    double* d_Ainv[2] = {nullptr, nullptr};
+    double* d_ubc_map = nullptr;     // per-dof prescribed displacement
+    double* d_fbc_map = nullptr;     // per-dof traction value
+    unsigned char* d_is_ubc = nullptr;
+    unsigned char* d_is_fbc = nullptr;
+    double* d_tmp_rows = nullptr;
+    double* d_load_t = nullptr;
+    double* d_load_u = nullptr;
+    double* d_Wt = nullptr;
+    double* d_Wu = nullptr;
+    double* d_partial = nullptr;
+    double* d_rhs = nullptr;
+    double* d_x = nullptr;
+    int* d_perm = nullptr;
+    double* d_colk = nullptr;
+    double* d_rowk = nullptr;
+    int* d_status = nullptr;
+    size_t partial_cap = 0;
+    double timings[3] = {0, 0, 0};
+    // profiling (tdbem_set_profiling): pending event pairs and per-class totals
+    struct ProfEvent {
+        int cls;
+        cudaEvent_t a, b;
+        double bytes, flops;
+    };
+    long long launches = 0;          // kernels this context has launched (tdbem_launch_count)
+    bool prof = false;
+    std::vector<ProfEvent> prof_pending;
+    long long prof_launches[4] = {0, 0, 0, 0};
+    double prof_ms[4] = {0, 0, 0, 0};
+    double prof_bytes[4] = {0, 0, 0, 0};
+    double prof_flops[4] = {0, 0, 0, 0};
+};

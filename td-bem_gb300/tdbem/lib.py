@@ -1,0 +1,222 @@
+"""ctypes binding of the C ABI in include/tdbem.h (libtdbem.so).
+
+Fails loudly when the library is missing or no CUDA device is present; there
+is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "_build", "libtdbem.so")
+
+FP64 = 0
+MIXED = 1
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+# Every symbol include/tdbem.h declares, with its ctypes signature.
+SIGNATURES = {
+    "tdbem_last_error": (ctypes.c_char_p, []),
+    "tdbem_version": (ctypes.c_char_p, []),
+    "tdbem_ctx_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "tdbem_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tdbem_max_step": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "tdbem_num_dof": (ctypes.c_int, [ctypes.c_void_p, _ip]),
+    "tdbem_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "tdbem_gh_driver": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       _dp, _dp, _dp, _dp]),
+    "tdbem_assemble_levels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tdbem_get_level": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp]),
+    "tdbem_set_bc": (ctypes.c_int, [ctypes.c_void_p, _ip, _dp, ctypes.c_int, _ip, _dp,
+                                    ctypes.c_int]),
+    "tdbem_set_alpha": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
+    "tdbem_set_load_history": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int]),
+    "tdbem_march": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "tdbem_history_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                            ctypes.POINTER(ctypes.c_void_p)]),
+    "tdbem_level_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_size_t)]),
+    "tdbem_last_timings": (ctypes.c_int, [ctypes.c_void_p, _dp]),
+    "tdbem_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_kernel_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp]),
+    "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+}
+
+KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve"}
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("nnd", ctypes.c_int), ("nel", ctypes.c_int), ("etype", ctypes.c_int),
+                ("coords", _dp), ("ien", _ip)]
+
+
+class Material(ctypes.Structure):
+    _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double)]
+
+
+class TdbemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tdbem error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: Optional[str] = None):
+    """Load libtdbem.so (built by td-bem_gb300/build.py); raise if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is missing: run td-bem_gb300/build.py (no CPU fallback)")
+    L = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise TdbemError(rc, load().tdbem_last_error().decode())
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class Context:
+    """One tdbem_ctx: a mesh + material + time step on the current CUDA device."""
+
+    def __init__(self, model, nq: Optional[int] = None):
+        L = load()
+        self.model = model
+        self._coords = np.ascontiguousarray(model.coords, np.float64)
+        self._ien = np.ascontiguousarray(model.ien, np.int32)
+        mesh = Mesh(model.nnd, model.nel, model.etype, _d(self._coords), _i(self._ien))
+        mat = Material(model.E, model.nu, model.rho)
+        h = ctypes.c_void_p()
+        _check(L.tdbem_ctx_create(ctypes.byref(mesh), ctypes.byref(mat), model.dt,
+                                  nq or model.nq, model.if_ext, ctypes.byref(h)))
+        self.h = h
+        self.D = 3 * model.nnd
+        m = ctypes.c_int()
+        _check(L.tdbem_max_step(h, ctypes.byref(m)))
+        self.M = m.value
+        self.set_bc(model.ubc_dofs, model.ubc_vals, model.fbc_dofs, model.fbc_vals)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().tdbem_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _check(load().tdbem_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def set_bc(self, ubc_dofs, ubc_vals, fbc_dofs, fbc_vals):
+        self._ud = np.ascontiguousarray(ubc_dofs, np.int32)
+        self._uv = np.ascontiguousarray(ubc_vals, np.float64)
+        self._fd = np.ascontiguousarray(fbc_dofs, np.int32)
+        self._fv = np.ascontiguousarray(fbc_vals, np.float64)
+        _check(load().tdbem_set_bc(self.h, _i(self._ud), _d(self._uv), len(self._ud),
+                                   _i(self._fd), _d(self._fv), len(self._fd)))
+
+    def set_alpha(self, a1: float, a2: float):
+        _check(load().tdbem_set_alpha(self.h, a1, a2))
+
+    def set_load_history(self, amp):
+        self._amp = np.ascontiguousarray(amp, np.float64)
+        _check(load().tdbem_set_load_history(self.h, _d(self._amp), len(self._amp)))
+
+    def assemble(self, nsteps: Optional[int] = None, precision: int = FP64):
+        ns = self.model.numstep if nsteps is None else nsteps
+        _check(load().tdbem_assemble_levels(self.h, ns, precision))
+
+    def level(self, k: int, which: int) -> np.ndarray:
+        out = np.empty((self.D, self.D))
+        _check(load().tdbem_get_level(self.h, k, which, _d(out)))
+        return out
+
+    def levels(self):
+        G = np.stack([self.level(k, 0) for k in range(self.M + 1)])
+        H = np.stack([self.level(k, 1) for k in range(self.M + 1)])
+        return G, H
+
+    def gh_driver(self, step: int, node_lo: int = 0, node_hi: Optional[int] = None):
+        hi = self.model.nnd - 1 if node_hi is None else node_hi
+        rows = 3 * (hi - node_lo + 1)
+        outs = [np.empty((rows, self.D)) for _ in range(4)]
+        _check(load().tdbem_gh_driver(self.h, step, node_lo, hi, *[_d(o) for o in outs]))
+        return outs  # G_I, G_J, H_I, H_J
+
+    def march(self, numstep: Optional[int] = None, to_host: bool = True):
+        n = self.model.numstep if numstep is None else numstep
+        if to_host:
+            u = np.empty((n + 1, self.D))
+            t = np.empty((n + 1, self.D))
+            _check(load().tdbem_march(self.h, n, _d(u), _d(t)))
+            return u, t
+        _check(load().tdbem_march(self.h, n, None, None))
+        return None
+
+    def timings(self):
+        out = np.zeros(3)
+        _check(load().tdbem_last_timings(self.h, _d(out)))
+        return {"assemble_ms": out[0], "factor_ms": out[1], "march_ms": out[2]}
+
+    def set_profiling(self, on: bool):
+        _check(load().tdbem_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_stats(self):
+        out = {}
+        for k, name in KERNEL_CLASSES.items():
+            n = ctypes.c_longlong()
+            ms, by, fl = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+            _check(load().tdbem_kernel_stats(self.h, k, ctypes.byref(n), ctypes.byref(ms),
+                                             ctypes.byref(by), ctypes.byref(fl)))
+            out[name] = {"launches": n.value, "ms": ms.value, "bytes": by.value,
+                         "flops": fl.value}
+        return out
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        _check(load().tdbem_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def level_bytes(self, precision: int = FP64) -> int:
+        b = ctypes.c_size_t()
+        _check(load().tdbem_level_bytes(self.h, precision, ctypes.byref(b)))
+        return b.value

@@ -1,0 +1,154 @@
+"""Synthetic surface meshes for the benchmark workloads, written as Models.
+
+* :func:`bar` -- prismatic bar, 4-node quads, one end fixed and a unit
+  Heaviside normal traction on the other (the layout of the reference's
+  ``geometry/Bar_1.txt``: outward normals, u = 0 on every dof of the fixed
+  end's nodes, traction on the axial dof of the loaded end's nodes).
+* :func:`cubed_sphere` -- spherical cavity in a full space (``if_ext = 1``),
+  equiangular cubed-sphere quads with normals pointing into the cavity like
+  the reference's ``geometry/SphericalCavity_*.txt``, uniform internal
+  pressure p: traction ``t = p * x / |x|`` on every dof.
+
+The mesh size h of a cubed sphere is the equiangular arc spacing
+``radius * (pi/2) / n``; the time step is ``dt = beta * h / c_p``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .inputfile import Model
+
+
+def material_for(mu: float = 1.0, nu: float = 0.25, rho: float = 1.0):
+    """Young's modulus giving shear modulus mu at Poisson ratio nu."""
+    return 2.0 * mu * (1.0 + nu), nu, rho
+
+
+def _orient(coords, ien, outward_of):
+    """Reorder each quad so that (p1-p0) x (p3-p0) agrees with outward_of(centroid)."""
+    out = ien.copy()
+    for e, q in enumerate(ien):
+        p = coords[q]
+        n = np.cross(p[1] - p[0], p[3] - p[0])
+        if np.dot(n, outward_of(p.mean(0))) < 0:
+            out[e] = q[[0, 3, 2, 1]]
+    return out
+
+
+def bar(lx: float = 1.0, ly: float = 1.0, lz: float = 4.0, per_unit: int = 2,
+        mu: float = 1.0, nu: float = 0.25, rho: float = 1.0, beta: float = 0.6,
+        numstep: int = 200, traction: float = 1.0) -> Model:
+    """Surface mesh of a lx x ly x lz bar along z, quads at per_unit per unit length."""
+    nx, ny, nz = (int(round(l * per_unit)) for l in (lx, ly, lz))
+    grid = {}
+    coords = []
+
+    def node(i, j, k):
+        key = (i, j, k)
+        if key not in grid:
+            grid[key] = len(coords)
+            coords.append((lx * i / nx, ly * j / ny, lz * k / nz))
+        return grid[key]
+
+    quads = []
+    normals = []
+    # lateral faces x=0, x=lx, y=0, y=ly and the two end caps
+    for (fixed, val, a, b, na, nb, nvec) in (
+            ("x", 0, "y", "z", ny, nz, (-1, 0, 0)), ("x", nx, "y", "z", ny, nz, (1, 0, 0)),
+            ("y", 0, "x", "z", nx, nz, (0, -1, 0)), ("y", ny, "x", "z", nx, nz, (0, 1, 0)),
+            ("z", 0, "x", "y", nx, ny, (0, 0, -1)), ("z", nz, "x", "y", nx, ny, (0, 0, 1))):
+        for ia in range(na):
+            for ib in range(nb):
+                ids = []
+                for (da, db) in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                    idx = {fixed: val, a: ia + da, b: ib + db}
+                    ids.append(node(idx["x"], idx["y"], idx["z"]))
+                quads.append(ids)
+                normals.append(nvec)
+    coords = np.array(coords, float)
+    ien = np.array(quads, np.int32)
+    for e in range(len(ien)):
+        p = coords[ien[e]]
+        if np.dot(np.cross(p[1] - p[0], p[3] - p[0]), normals[e]) < 0:
+            ien[e] = ien[e][[0, 3, 2, 1]]
+    E, nu_, rho_ = material_for(mu, nu, rho)
+    m = Model(coords=coords, ien=ien, etype=1, E=E, nu=nu_, rho=rho_, numstep=numstep)
+    _, _, cp, _ = m.material()
+    m.dt = beta * (1.0 / per_unit) / cp
+    z = coords[:, 2]
+    fixed_nodes = np.nonzero(np.isclose(z, 0.0))[0]
+    loaded = np.nonzero(np.isclose(z, lz))[0]
+    m.ubc_dofs = np.array([3 * n + d for n in fixed_nodes for d in range(3)], np.int32)
+    m.ubc_vals = np.zeros(len(m.ubc_dofs))
+    m.fbc_dofs = np.array([3 * n + 2 for n in loaded], np.int32)
+    m.fbc_vals = np.full(len(m.fbc_dofs), float(traction))
+    return m
+
+
+def cubed_sphere(n: int = 16, radius: float = 1.0, mu: float = 1.0, nu: float = 0.25,
+                 rho: float = 1.0, beta: float = 0.6, numstep: int = 400,
+                 pressure: float = 1.0) -> Model:
+    """Equiangular cubed sphere with 6*n*n quads and 6*n*n+2 nodes, if_ext = 1."""
+    ang = np.linspace(-np.pi / 4, np.pi / 4, n + 1)
+    t = np.tan(ang)
+    faces = [  # (axis, sign) of each cube face; (u, v) span the other two axes
+        (0, 1), (0, -1), (1, 1), (1, -1), (2, 1), (2, -1)]
+    key_to_id = {}
+    coords = []
+    quads = []
+    for axis, sign in faces:
+        others = [d for d in range(3) if d != axis]
+        ids = np.zeros((n + 1, n + 1), np.int64)
+        for i in range(n + 1):
+            for j in range(n + 1):
+                p = np.zeros(3)
+                p[axis] = sign
+                p[others[0]] = t[i]
+                p[others[1]] = t[j]
+                p = radius * p / np.linalg.norm(p)
+                key = tuple(np.round(p, 10))
+                if key not in key_to_id:
+                    key_to_id[key] = len(coords)
+                    coords.append(p)
+                ids[i, j] = key_to_id[key]
+        for i in range(n):
+            for j in range(n):
+                quads.append([ids[i, j], ids[i + 1, j], ids[i + 1, j + 1], ids[i, j + 1]])
+    coords = np.array(coords, float)
+    ien = np.array(quads, np.int32)
+    # normals into the cavity (toward the centre), as the reference's cavity meshes
+    ien = _orient(coords, ien, lambda c: -c)
+    E, nu_, rho_ = material_for(mu, nu, rho)
+    m = Model(coords=coords, ien=ien, etype=1, E=E, nu=nu_, rho=rho_, numstep=numstep,
+              if_ext=1)
+    _, _, cp, _ = m.material()
+    h = radius * (np.pi / 2) / n
+    m.dt = beta * h / cp
+    rhat = coords / np.linalg.norm(coords, axis=1, keepdims=True)
+    m.fbc_dofs = np.arange(3 * len(coords), dtype=np.int32)
+    m.fbc_vals = (pressure * rhat).reshape(-1).astype(float)
+    return m
+
+
+def sphere_cavity_closed_form(t: np.ndarray, radius: float = 1.0, mu: float = 1.0,
+                              nu: float = 0.25, rho: float = 1.0, p: float = 1.0) -> np.ndarray:
+    """Radial wall displacement u_r(a, t) of a spherical cavity under step pressure p H(t).
+
+    With the P-wave potential phi = f(tau)/r, tau = t - (r - a)/c_p and
+    sigma_rr(a) = -p H(t):  f'' + (4 c_s^2/(c_p a)) f' + (4 c_s^2/a^2) f = -p a H(t)/rho
+    and u_r(a, t) = -f'/(c_p a) - f/a^2.  Static limit p a / (4 mu)."""
+    lam = 2 * mu * nu / (1 - 2 * nu)
+    cp = np.sqrt((lam + 2 * mu) / rho)
+    cs = np.sqrt(mu / rho)
+    a = radius
+    b1 = 4 * cs ** 2 / (cp * a)
+    b0 = 4 * cs ** 2 / a ** 2
+    zeta = b1 / 2
+    omega = np.sqrt(b0 - zeta ** 2)
+    fs = -p * a / (rho * b0)  # particular solution
+    t = np.asarray(t, float)
+    e = np.exp(-zeta * t)
+    f = fs * (1 - e * (np.cos(omega * t) + (zeta / omega) * np.sin(omega * t)))
+    fp = fs * e * (zeta ** 2 / omega + omega) * np.sin(omega * t)
+    u = -fp / (cp * a) - f / a ** 2
+    return np.where(t > 0, u, 0.0)

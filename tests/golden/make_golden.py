@@ -1,0 +1,90 @@
+"""Generate the golden fixtures that pin the oracle to the TD-BEM reference.
+
+Run here (where the reference sources are):  python tests/golden/make_golden.py
+
+It builds the reference's own sources, unmodified, against the single-rank
+dense PETSc/MPI stand-in (oracle/Makefile.ref -> oracle/_ref/ref_driver), runs
+the reference's main-loop sequence on each case and stores, per case, an .npz
+holding: the input text it ran, alpha, the level count, seeded random
+projections of every G/H level (G_k @ w and w @ G_k; the full levels for the
+tiny cases) and the u/t histories (every dof for small meshes, a fixed subset
+of dofs otherwise).  Tests rebuild the model from the stored text, so they
+need neither the reference nor this script at run time.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "td-bem_gb300"))
+from tdbem import inputfile, meshes  # noqa: E402
+
+REF_ROOT = os.environ.get("TDBEM_REFERENCE", "/root/reference")
+OUT = os.path.join(ROOT, "tests", "golden")
+SEED = 20151022
+
+
+def projection_vector(D: int) -> np.ndarray:
+    return np.random.default_rng(SEED).standard_normal(D)
+
+
+def build_reference() -> str:
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF_SRC={REF_ROOT}/src", "-j8"],
+                   cwd=ROOT, check=True)
+    return os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def run_case(driver, name, text, a1=0.0, a2=0.0, full_levels=False, dof_stride=1):
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "input.txt")
+        with open(path, "w") as f:
+            f.write(text)
+        prefix = os.path.join(tmp, "out")
+        subprocess.run([driver, path, repr(a1), repr(a2), prefix], cwd=tmp, check=True,
+                       stdout=subprocess.DEVNULL)
+        D, M, ns = map(int, open(prefix + ".meta").read().split())
+        G = np.fromfile(prefix + ".G").reshape(M + 1, D, D)
+        H = np.fromfile(prefix + ".H").reshape(M + 1, D, D)
+        u = np.fromfile(prefix + ".u").reshape(ns + 1, D)
+        t = np.fromfile(prefix + ".t").reshape(ns + 1, D)
+    w = projection_vector(D)
+    dofs = np.arange(0, D, dof_stride, dtype=np.int32)
+    rec = dict(input_text=np.array(text), a1=a1, a2=a2, D=D, M=M, numstep=ns, seed=SEED,
+               G_w=G @ w, H_w=H @ w, w_G=np.einsum("d,kde->ke", w, G),
+               w_H=np.einsum("d,kde->ke", w, H), G_absmax=np.abs(G).max(axis=(1, 2)),
+               H_absmax=np.abs(H).max(axis=(1, 2)), dofs=dofs, u=u[:, dofs], t=t[:, dofs])
+    if full_levels:
+        rec.update(G=G, H=H)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **rec)
+    print(f"{name}: D={D} M={M} steps={ns}")
+
+
+def main():
+    driver = build_reference()
+    geo = os.path.join(REF_ROOT, "geometry")
+    bar1 = open(os.path.join(geo, "Bar_1.txt")).read()
+    run_case(driver, "ref_bar1", bar1, full_levels=True)
+    run_case(driver, "ref_bar1_alpha", bar1, a1=0.25, a2=0.25)
+    run_case(driver, "ref_halfspace_plane_1e",
+             open(os.path.join(geo, "HalfSpacePlane_1E.txt")).read(), full_levels=True)
+    # The 1x1x4 bar at 2 quads per unit length, 200 steps (the CPU-runnable workload).
+    bar = meshes.bar(1, 1, 4, per_unit=2, numstep=200)
+    run_case(driver, "bar_1x1x4_q2", inputfile.dumps(bar))
+    bar.numstep = 60
+    run_case(driver, "bar_1x1x4_q2_alpha", inputfile.dumps(bar), a1=0.25, a2=0.1)
+    # A coarse cubed-sphere cavity (6x4x4 quads), if_ext = 1, uniform pressure.
+    sph = meshes.cubed_sphere(4, numstep=80)
+    run_case(driver, "sphere_6x4x4", inputfile.dumps(sph))
+    # The reference's own spherical cavity mesh, first 40 steps, every 4th dof.
+    cav = open(os.path.join(geo, "SphericalCavity_1.txt")).read().replace(
+        "numstep=200;", "numstep=40;")
+    run_case(driver, "ref_spherical_cavity_1_40", cav, dof_stride=4)
+
+
+if __name__ == "__main__":
+    main()
