@@ -320,6 +320,8 @@ def run_ours(args, dist):
         e2e_times.append(t1 - t0)
     e2e_s = dist.max(statistics.median(e2e_times))
     e2e_value = D * nsteps * dist.world / e2e_s
+    level_gb = ctx.level_bytes(prec) / 1e9
+    M = ctx.M
     ctx.close()
 
     if dist.rank != 0:
@@ -348,11 +350,11 @@ def run_ours(args, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == lib.FP64 else "f32+f64", "data": "synthetic",
-            "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": ctx.M,
+            "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": M,
                        "alpha": list(ALPHA), "precision": args.precision,
                        "parallelism": f"replicas{dist.world}",
                        "l2": "inputs larger than L2: the level store is "
-                             f"{ctx.level_bytes(prec) / 1e9:.1f} GB"},
+                             f"{level_gb:.1f} GB"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -363,7 +365,7 @@ def run_ours(args, dist):
                         for k, v in stats.items()},
             "clocks": clk}
     if dist.world == 1 and not args.no_cpu_baseline:
-        r = cpu_sample(model, ctx.M, nsteps, *ALPHA, os.cpu_count() or 1)
+        r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
                                 "kind": "port", "sample": r["sample"]}
     print(json.dumps(line))

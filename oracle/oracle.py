@@ -71,10 +71,33 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
-class Oracle:
-    """Oracle handle bound to one Model (tdbem.inputfile.Model)."""
+class _Clean:
+    """Context manager setting orc_clean_passed_waves (exact zero step response once
+    both wave fronts have passed a quadrature point, instead of the reference's
+    round-off there)."""
 
-    def __init__(self, model, nthreads: int = 0):
+    def __init__(self, on):
+        self.on = on
+
+    def __enter__(self):
+        self.flag = ctypes.c_int.in_dll(lib(), "orc_clean_passed_waves")
+        self.old = self.flag.value
+        self.flag.value = 1 if self.on else 0
+
+    def __exit__(self, *a):
+        self.flag.value = self.old
+
+
+class Oracle:
+    """Oracle handle bound to one Model (tdbem.inputfile.Model).
+
+    clean=False reproduces the reference's arithmetic bit for bit; clean=True
+    replaces the step response by its exact value 0 wherever both wave fronts
+    have passed the quadrature point at both evaluation times (the reference
+    leaves round-off there)."""
+
+    def __init__(self, model, nthreads: int = 0, clean: bool = False):
+        self.clean = clean
         self.m = model
         self.coords = np.ascontiguousarray(model.coords, np.float64)
         self.ien = np.ascontiguousarray(model.ien, np.int32)
@@ -93,8 +116,9 @@ class Oracle:
         hi = self.m.nnd - 1 if node_hi is None else node_hi
         rows = 3 * (hi - node_lo + 1)
         outs = [np.zeros((rows, self.D)) for _ in range(4)]
-        rc = lib().orc_gh_driver(ctypes.byref(self.st), t, t_1, node_lo, hi,
-                                 *[_d(o) for o in outs], self.nthreads)
+        with _Clean(self.clean):
+            rc = lib().orc_gh_driver(ctypes.byref(self.st), t, t_1, node_lo, hi,
+                                     *[_d(o) for o in outs], self.nthreads)
         if rc:
             raise RuntimeError(f"orc_gh_driver failed ({rc})")
         return outs  # G_I, G_J, H_I, H_J
@@ -104,8 +128,9 @@ class Oracle:
         nsteps = self.m.numstep if nsteps is None else nsteps
         G = np.zeros((M + 1, self.D, self.D))
         H = np.zeros((M + 1, self.D, self.D))
-        rc = lib().orc_assemble_levels(ctypes.byref(self.st), M, nsteps, _d(G), _d(H),
-                                       self.nthreads)
+        with _Clean(self.clean):
+            rc = lib().orc_assemble_levels(ctypes.byref(self.st), M, nsteps, _d(G), _d(H),
+                                           self.nthreads)
         if rc:
             raise RuntimeError(f"orc_assemble_levels failed ({rc})")
         return G, H

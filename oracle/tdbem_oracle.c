@@ -303,9 +303,20 @@ static void green_heaviside_linear(const green* g, double T, double* DU1, double
  * response at T minus the one at T - T1, entry by entry (VecPlus 1, -1).
  * Like the reference, the stored time is shifted down and back up
  * (fT=fT-fT_1; ...; fT=fT+fT_1), which can move it by an ulp between calls. */
+/* Test hook: when non-zero, the step response is set to its exact value 0 once
+ * both wave fronts have passed the point at both evaluation times (where the
+ * reference's arithmetic leaves only round-off).  Used by the tests to measure
+ * the reference's round-off floor; never set in normal use. */
+int orc_clean_passed_waves = 0;
+
 static void green_compute4(green* g, double* DU1, double* DU2, double* DT1, double* DT2,
                            double* K) {
     double u1[9], u2[9], t1[9], t2[9];
+    if (orc_clean_passed_waves && (g->T - g->T1) - g->r / g->cs >= g->T1) {
+        green_kelvin_linear(g, K);
+        for (int i = 0; i < 9; i++) DU1[i] = DU2[i] = DT1[i] = DT2[i] = 0.0;
+        return;
+    }
     green_kelvin_linear(g, K);
     green_heaviside_linear(g, g->T, DU1, DU2, DT1, DT2);
     g->T = g->T - g->T1;

@@ -31,6 +31,13 @@ typedef struct {
     int if_ext;           /* exterior problem: +0.5*dt on the first-step diagonal */
 } orc_model;
 
+/* Test hook (0 by default): non-zero makes the oracle return the exact value 0
+ * for the step response once both wave fronts have passed a quadrature point at
+ * both evaluation times, where the reference's arithmetic leaves round-off
+ * (GreenFunctionT.cpp:241-446 evaluated with b = dt and I5 = I6 = 0 at T and at
+ * T - dt).  Used to measure the reference's round-off floor. */
+extern int orc_clean_passed_waves;
+
 /* SolverT::ComputeMaxStep (SolverT.cpp:211-250). */
 int orc_max_step(const orc_model* m);
 

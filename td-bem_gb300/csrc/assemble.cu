@@ -178,8 +178,14 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
     const double inv12R2 = inv_r * inv_r * (1.0 / 12.0);
     const double roc_p = r * ph.inv_cp, roc_s = r * ph.inv_cs;
 
+    // Once the S front has passed the point at both evaluation times of a part
+    // ((T - dt) - r/c_s >= dt), that part's step response is identically zero
+    // (b = dt and I5 = I6 = 0 at both times): skip it instead of summing round-off.
+    const bool doI = tc.doI && !(tc.TI1 - roc_s >= ph.dt);
+    const bool doJ = tc.doJ && !(tc.TJ1 - roc_s >= ph.dt);
+    if (!doI && !doJ) return;
     double P1 = 0, P3 = 0, P5 = 0, S2 = 0, S4 = 0, S6 = 0;
-    if (tc.doI) {
+    if (doI) {
         double a1, a3, a5, b1, b3, b5;
         wave_I(tc.TI0, tc.cA0, tc.cB0, tc.cC0, roc_p, inv12R2, ph.inv_cp2, ph, a1, a3, a5);
         wave_I(tc.TI1, tc.cA1, tc.cB1, tc.cC1, roc_p, inv12R2, ph.inv_cp2, ph, b1, b3, b5);
@@ -192,7 +198,7 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
         S4 = a3 - b3;
         S6 = a5 - b5;
     }
-    if (tc.doJ) {
+    if (doJ) {
         double a1, a3, a5, b1, b3, b5;
         wave_J(tc.TJ0, tc.dA0, tc.dB0, roc_p, inv12R2, ph.inv_cp2, ph, a1, a3, a5);
         wave_J(tc.TJ1, tc.dA1, tc.dB1, roc_p, inv12R2, ph.inv_cp2, ph, b1, b3, b5);

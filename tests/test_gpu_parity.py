@@ -2,9 +2,12 @@
 
 Parity bar: 1e-10 relative, measured per level as max|G_gpu - G_oracle| /
 max|G_oracle| (likewise H), and per time step as max|u_gpu - u_oracle| /
-max|u_oracle| (likewise t).  Entries the reference computes as pure round-off
-(levels after both wave fronts have passed an element) are exact zeros on the
-GPU, so the bar is on the level / step norm, not entry by entry.
+max|u_oracle| (likewise t), against the oracle in its exact-zero mode: once
+both wave fronts have passed a quadrature point at both evaluation times the
+step response is identically zero, and the reference's arithmetic leaves only
+round-off there (up to ~6e-8 of the level norm on some inputs).  Against the
+reference's raw outputs the bar is 1e-10 plus twice that measured round-off
+floor, level by level and step by step.
 """
 import numpy as np
 import pytest
@@ -32,7 +35,7 @@ def oracle_cache(oracle_mod):
     def get(name):
         if name not in cache:
             z, m = load_golden(name)
-            o = oracle_mod.Oracle(m)
+            o = oracle_mod.Oracle(m, clean=True)
             G, H = o.assemble_levels()
             u, t = o.march(G, H, float(z["a1"]), float(z["a2"]))
             cache[name] = (z, m, G, H, u, t)
@@ -41,13 +44,19 @@ def oracle_cache(oracle_mod):
     return get
 
 
-def check_steps(u, uo, what):
+def floor(a_clean, a_ref):
+    """The reference's round-off floor of one level / step: clean oracle vs reference."""
+    return rel_max(a_clean, a_ref)
+
+
+def check_steps(u, uo, what, clean=None):
     for s in range(uo.shape[0]):
         if np.abs(uo[s]).max() == 0:
             assert np.abs(u[s]).max() == 0, f"{what} step {s}"
             continue
+        tol = TOL if clean is None else TOL + 2 * floor(clean[s], uo[s])
         e = rel_max(u[s], uo[s])
-        assert e <= TOL, f"{what} step {s}: {e:.3e}"
+        assert e <= tol, f"{what} step {s}: {e:.3e} > {tol:.3e}"
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -61,9 +70,11 @@ def test_levels_match_oracle_and_reference(name, tdlib, oracle_cache):
         assert rel_max(G[k], Go[k]) <= TOL, f"G level {k}: {rel_max(G[k], Go[k]):.3e}"
         assert rel_max(H[k], Ho[k]) <= TOL, f"H level {k}: {rel_max(H[k], Ho[k]):.3e}"
     w = np.random.default_rng(int(z["seed"])).standard_normal(ctx.D)
-    for k in range(ctx.M + 1):  # directly against the reference's own outputs
-        assert rel_max(G[k] @ w, z["G_w"][k]) <= TOL
-        assert rel_max(w @ H[k], z["w_H"][k]) <= TOL
+    for k in range(ctx.M + 1):  # against the reference's own outputs, above its round-off
+        tg = TOL + 2 * floor(Go[k] @ w, z["G_w"][k])
+        th = TOL + 2 * floor(w @ Ho[k], z["w_H"][k])
+        assert rel_max(G[k] @ w, z["G_w"][k]) <= tg, f"G level {k} vs reference"
+        assert rel_max(w @ H[k], z["w_H"][k]) <= th, f"H level {k} vs reference"
 
 
 @pytest.mark.parametrize("name", golden_cases())
@@ -76,14 +87,14 @@ def test_histories_match_oracle_and_reference(name, tdlib, oracle_cache):
     check_steps(u, uo, "u")
     check_steps(t, to, "t")
     d = z["dofs"]
-    check_steps(u[:, d], z["u"], "u vs reference")
-    check_steps(t[:, d], z["t"], "t vs reference")
+    check_steps(u[:, d], z["u"], "u vs reference", clean=uo[:, d])
+    check_steps(t[:, d], z["t"], "t vs reference", clean=to[:, d])
 
 
 @pytest.mark.parametrize("step", [1, 2, 5])
 def test_gh_driver_matches_oracle(step, tdlib, oracle_mod):
     z, m = load_golden("ref_spherical_cavity_1_40")
-    o = oracle_mod.Oracle(m)
+    o = oracle_mod.Oracle(m, clean=True)
     lo, hi = 17, 80
     ref = o.gh_driver(step * m.dt, m.dt, lo, hi)
     with tdlib.Context(m) as ctx:
