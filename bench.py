@@ -322,6 +322,29 @@ def run_ours(args, dist):
     e2e_value = D * nsteps * dist.world / e2e_s
     level_gb = ctx.level_bytes(prec) / 1e9
     M = ctx.M
+    # the plain FP64 form on the same workload: its time, and the mixed form's error
+    compare = None
+    if prec == lib.MIXED and not args.no_compare:
+        u32, t32 = ctx.march()  # histories of the mixed form (levels already assembled)
+        with lib.Context(model) as c64:
+            c64.set_alpha(*ALPHA)
+            c64.assemble(precision=lib.FP64)
+            c64.march(to_host=False)
+            torch.cuda.synchronize()
+            s64 = torch.cuda.ExternalStream(c64.stream)
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(s64)
+            c64.assemble(precision=lib.FP64)
+            u64, t64 = c64.march()
+            a1.record(s64)
+            a1.synchronize()
+            ms64 = a0.elapsed_time(a1)
+        compare = {"plain_fp64_value": D * nsteps / (ms64 / 1e3),
+                   "plain_fp64_ms_per_step": ms64,
+                   "speedup_vs_plain_fp64": (D * nsteps / (ms_step / 1e3)) / (D * nsteps / (ms64 / 1e3)),
+                   "u_rel_l2_err": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+                   "t_rel_l2_err": float(np.linalg.norm(t32 - t64) / np.linalg.norm(t64))}
     ctx.close()
 
     if dist.rank != 0:
@@ -364,6 +387,8 @@ def run_ours(args, dist):
                             "share": v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values()))}
                         for k, v in stats.items()},
             "clocks": clk}
+    if compare:
+        line["vs_plain_fp64"] = compare
     if dist.world == 1 and not args.no_cpu_baseline:
         r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
@@ -379,7 +404,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="sphere_6x16x16")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the plain FP64 run that measures the mixed form's error")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

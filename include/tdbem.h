@@ -133,6 +133,11 @@ int tdbem_set_load_history(tdbem_ctx* ctx, const double* amp, int nsteps);
  * or NULL to keep the histories on the device only. */
 int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
 
+/* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
+ * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64
+ * residual-refinement sweeps per solve (0..4; default 1). */
+int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
+
 /* Device pointers of the histories of the last tdbem_march (FP64,
  * (numstep+1) x D each); valid until the next march or destroy. */
 int tdbem_history_device(const tdbem_ctx* ctx, const double** u_hist, const double** t_hist);

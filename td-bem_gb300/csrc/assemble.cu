@@ -298,8 +298,9 @@ __device__ __forceinline__ int singular_corner(const double* c, const double xc[
 
 __global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
                               const int* __restrict__ elems, int ne, int node_lo, int nnodes,
-                              Phys ph, int mode, int level_last, int step_n,
-                              PairInfo* __restrict__ pairs, unsigned* __restrict__ counts) {
+                              Phys ph, int mode, int level_last, int level_cap, int step_n,
+                              int select, PairInfo* __restrict__ pairs,
+                              unsigned* __restrict__ counts) {
     const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= (long long)nnodes * ne) return;
     const int c = node_lo + (int)(p / ne);
@@ -333,13 +334,15 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
     if (mode == ASM_LEVELS) {
         // level k takes n = k (I part) and n = k + 1 (J part)
         const int klo = max(0, n_lo - 1);
-        const int khi = min(level_last, n_hi);
+        const int khi = min(min(level_last, n_hi), level_cap);
         pi.klo = klo;
         pi.cnt = max(0, khi - klo + 1);
     } else {
         pi.klo = step_n;
         pi.cnt = (step_n >= n_lo && step_n <= n_hi) ? 1 : 0;
     }
+    const bool far = sing < 0 && rmin > kFarRatio * rad;
+    if ((select == SEL_NEAR && far) || (select == SEL_FAR && !far)) pi.cnt = 0;
     pairs[p] = pi;
     counts[p] = (unsigned)pi.cnt;
 }
@@ -417,7 +420,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(
     }
 
     // scatter: rows 3c+i, columns 3*nid[a]+j
-    const size_t D = (size_t)out.D;
+    const size_t D = (size_t)out.ld;
     double* G;
     double* H;
     float* Gf = nullptr;
@@ -449,6 +452,217 @@ __global__ void __launch_bounds__(128) k_assemble_items(
                     G[idx] += acc.g[a][sym[i * 3 + j]];
                     H[idx] += acc.h[a][i * 3 + j];
                 }
+            }
+}
+
+
+// ---------------------------------------------------------------------------
+// FP32 far-field quadrature (mixed precision).
+//
+// The reference's time integrals carry the absolute time T through terms like
+// T^2 b^2 / (12 r^2) that cancel in the step response; in FP32 that loses
+// ~(T/dt)^2 of the 24 mantissa bits.  With tau = T - r/c (time since the front
+// passed the point, b = clamp(tau, 0, dt)) and rho = r/c, the rho^2 part of those
+// polynomials cancels the -(dt b - b^2/2)/c^2 (and -(b^2/2)/c^2) terms exactly:
+//   I1 = (rho Q1 + Q0) / (12 r^2 dt),  J1 = (rho R1 + R0) / (12 r^2 dt)
+//   Q1 = 8b^3 - 12 tau b^2 - 12 dt b^2 + 24 dt tau b
+//   Q0 = -3b^4 + (8 tau + 4 dt) b^3 - 6 tau^2 b^2 - 12 tau dt b^2 + 12 dt tau^2 b
+//   R1 = -8b^3 + 12 tau b^2,   R0 = 3b^4 - 8 tau b^3 + 6 tau^2 b^2
+// (GreenFunctionT.cpp:271-277 with T = rho + tau).  Only differences of
+// polynomials in tau remain, whose relative error is ~ eps32 * T/dt.
+// ---------------------------------------------------------------------------
+struct PhysF {
+    float dt, inv_dt, inv_cp, inv_cs, inv_cp2, inv_cs2, cs2, ratio2, ratio3, inv_4pi_rho,
+        inv_4pi, c4;  // c4 = 1 - 2 (cs/cp)^2
+};
+
+__device__ __forceinline__ PhysF to_f(const Phys& p) {
+    PhysF f;
+    f.dt = (float)p.dt;
+    f.inv_dt = (float)p.inv_dt;
+    f.inv_cp = (float)p.inv_cp;
+    f.inv_cs = (float)p.inv_cs;
+    f.inv_cp2 = (float)p.inv_cp2;
+    f.inv_cs2 = (float)p.inv_cs2;
+    f.cs2 = (float)p.cs2;
+    f.ratio2 = (float)p.ratio2;
+    f.ratio3 = (float)p.ratio3;
+    f.inv_4pi_rho = (float)p.inv_4pi_rho;
+    f.inv_4pi = (float)p.inv_4pi;
+    f.c4 = (float)(1 - 2 * p.ratio2);
+    return f;
+}
+
+// One wave at local time tau: F_I = rho Q1 + Q0, I3, I5 and F_J = rho R1 + R0, J3, J5.
+__device__ __forceinline__ void wave_tau_I(float tau, float rho, const PhysF& f, float& FI,
+                                           float& I3, float& I5) {
+    float b, x5;
+    if (f.dt <= tau) { b = f.dt; x5 = 0.f; }
+    else if (0.f <= tau) { b = tau; x5 = (f.dt - tau) * f.inv_dt; }
+    else { b = 0.f; x5 = 0.f; }
+    const float b2 = b * b;
+    const float q1 = b * (8.f * b2 - 12.f * tau * b - 12.f * f.dt * b + 24.f * f.dt * tau);
+    const float q0 = b * (b2 * (-3.f * b + 8.f * tau + 4.f * f.dt) - 6.f * tau * tau * b -
+                          12.f * tau * f.dt * b + 12.f * f.dt * tau * tau);
+    FI = rho * q1 + q0;
+    I3 = b * (f.dt - 0.5f * b) * f.inv_dt;
+    I5 = x5;
+}
+
+__device__ __forceinline__ void wave_tau_J(float tau, float rho, const PhysF& f, float& FJ,
+                                           float& J3, float& J5) {
+    float b, x5;
+    if (f.dt <= tau) { b = f.dt; x5 = 0.f; }
+    else if (0.f <= tau) { b = tau; x5 = tau * f.inv_dt; }
+    else { b = 0.f; x5 = 0.f; }
+    const float b2 = b * b;
+    const float r1 = b2 * (-8.f * b + 12.f * tau);
+    const float r0 = b2 * (3.f * b2 - 8.f * tau * b + 6.f * tau * tau);
+    FJ = rho * r1 + r0;
+    J3 = 0.5f * b2 * f.inv_dt;
+    J5 = x5;
+}
+
+struct ItemAccF {
+    float g[4][6];
+    float h[4][9];
+};
+
+// One Gauss point of a far item in FP32: TI = k dt (I part), TJ = (k+1) dt (J part).
+__device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool doJ0, float TI,
+                                                const PhysF& f, const float xc[3],
+                                                const float xq[3], const float nq[3], float wJ,
+                                                const float N[4]) {
+    const float d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
+    const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+    const float inv_r = rsqrtf(r2);
+    const float r = r2 * inv_r;
+    const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+    const float rdn = rv[0] * nq[0] + rv[1] * nq[1] + rv[2] * nq[2];
+    const float rho_p = r * f.inv_cp, rho_s = r * f.inv_cs;
+    const float tp = TI - rho_p, ts = TI - rho_s;  // tau of each wave at T = TI
+    // exact zero once the S front has passed at both times of a part
+    const bool doI = doI0 && !(ts - f.dt >= f.dt);
+    const bool doJ = doJ0 && !(ts >= f.dt);
+    if (!doI && !doJ) return;
+    float P1 = 0.f, P3 = 0.f, P5 = 0.f, S2 = 0.f, S4 = 0.f, S6 = 0.f;
+    float a1, a3, a5, b1, b3, b5;
+    if (doI) {
+        wave_tau_I(tp, rho_p, f, a1, a3, a5);
+        wave_tau_I(tp - f.dt, rho_p, f, b1, b3, b5);
+        P1 = a1 - b1; P3 = a3 - b3; P5 = a5 - b5;
+        wave_tau_I(ts, rho_s, f, a1, a3, a5);
+        wave_tau_I(ts - f.dt, rho_s, f, b1, b3, b5);
+        S2 = a1 - b1; S4 = a3 - b3; S6 = a5 - b5;
+    }
+    if (doJ) {
+        wave_tau_J(tp + f.dt, rho_p, f, a1, a3, a5);
+        wave_tau_J(tp, rho_p, f, b1, b3, b5);
+        P1 += a1 - b1; P3 += a3 - b3; P5 += a5 - b5;
+        wave_tau_J(ts + f.dt, rho_s, f, a1, a3, a5);
+        wave_tau_J(ts, rho_s, f, b1, b3, b5);
+        S2 += a1 - b1; S4 += a3 - b3; S6 += a5 - b5;
+    }
+    const float inv_r2 = inv_r * inv_r;
+    const float scale1 = inv_r2 * (1.f / 12.f) * f.inv_dt;  // 1/(12 r^2 dt) of I1/J1
+    P1 *= scale1;
+    S2 *= scale1;
+    const float It1 = 0.5f * (P1 - S2);
+    const float It2u = P3 * f.inv_cp2 - S4 * f.inv_cs2;
+    const float invDiv = inv_r * f.inv_4pi_rho;
+    const float A = (3.f * It1 + It2u) * invDiv;
+    const float B = (S4 * f.inv_cs2 - It1) * invDiv;
+    const float It2t = S4 - f.ratio2 * P3;
+    const float It3t = S6 - f.ratio3 * P5;
+    const float It4 = P3 + rho_p * P5;
+    const float It5 = S4 + rho_s * S6;
+    const float ir2 = inv_r2 * f.inv_4pi;
+    const float Q = 6.f * f.cs2 * It1 - 2.f * It2t;
+    const float alpha = ((-30.f * f.cs2) * It1 + 12.f * It2t) * ir2 +
+                        (2.f * f.inv_cs * f.inv_4pi) * inv_r * It3t;
+    const float beta = (Q - f.c4 * It4) * ir2;
+    const float gamma = (Q - It5) * ir2;
+    const float rr00 = rv[0] * rv[0], rr01 = rv[0] * rv[1], rr02 = rv[0] * rv[2];
+    const float rr11 = rv[1] * rv[1], rr12 = rv[1] * rv[2], rr22 = rv[2] * rv[2];
+    const float sg[6] = {A * rr00 + B, A * rr01, A * rr02, A * rr11 + B, A * rr12, A * rr22 + B};
+    const float ar = alpha * rdn, gd = gamma * rdn;
+    const float rrm[9] = {rr00, rr01, rr02, rr01, rr11, rr12, rr02, rr12, rr22};
+    float th[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++)
+            th[i * 3 + j] = ar * rrm[i * 3 + j] + beta * (nq[j] * rv[i]) +
+                            gamma * (nq[i] * rv[j]) + (i == j ? gd : 0.f);
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const float w = wJ * N[a];
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] += w * sg[m];
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] += w * th[m];
+    }
+}
+
+// Far (well-separated, non-singular) items in FP32, ASM_LEVELS placement into the
+// FP32 level store.  The Gauss-point geometry is read from the FP64 table and
+// rounded; coordinates are shifted to the collocation point in FP64 first.
+__global__ void __launch_bounds__(256) k_assemble_far_f32(
+    const double* __restrict__ coords, const int* __restrict__ ien,
+    const int* __restrict__ elems, int ne, int node_lo, int nq2,
+    const double* __restrict__ geom, Phys ph, int level_last,
+    const PairInfo* __restrict__ pairs, const unsigned* __restrict__ offsets, unsigned npairs,
+    unsigned nitems, AsmOut out) {
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= nitems) return;
+    unsigned lo = 0, hi = npairs - 1;
+    while (lo < hi) {
+        const unsigned mid = (lo + hi + 1) >> 1;
+        if (__ldg(offsets + mid) <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    const unsigned p = lo;
+    const PairInfo pi = pairs[p];
+    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
+    const int c = node_lo + (int)(p / ne);
+    const int e = elems[p % ne];
+    const double xcd[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
+    const float zero3[3] = {0.f, 0.f, 0.f};
+    int nid[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
+    const PhysF f = to_f(ph);
+    const bool doI = (k >= 1), doJ = (k + 1 <= level_last);
+    const float TI = (float)(k * ph.dt);
+    ItemAccF acc;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] = 0.f;
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] = 0.f;
+    }
+    const double* g = geom + (size_t)e * nq2 * kGeomStride;
+    for (int q = 0; q < nq2; q++, g += kGeomStride) {
+        const float xq[3] = {(float)(__ldg(g) - xcd[0]), (float)(__ldg(g + 1) - xcd[1]),
+                             (float)(__ldg(g + 2) - xcd[2])};
+        const float nqv[3] = {(float)__ldg(g + 3), (float)__ldg(g + 4), (float)__ldg(g + 5)};
+        const float N[4] = {(float)__ldg(g + 7), (float)__ldg(g + 8), (float)__ldg(g + 9),
+                            (float)__ldg(g + 10)};
+        gauss_point_f32(acc, doI, doJ, TI, f, zero3, xq, nqv, (float)__ldg(g + 6), N);
+    }
+    const size_t D = (size_t)out.ld;
+    const size_t rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
+    constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const size_t idx = rowbase + (size_t)i * D + 3 * (size_t)nid[a] + j;
+                out.G0f[idx] += acc.g[a][sym[i * 3 + j]];
+                out.H0f[idx] += acc.h[a][i * 3 + j];
             }
 }
 
@@ -513,7 +727,7 @@ __global__ void __launch_bounds__(128) k_cterm(const double* __restrict__ coords
         __syncthreads();
     }
     if (threadIdx.x != 0) return;
-    const size_t D = (size_t)out.D;
+    const size_t D = (size_t)out.ld;
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) {
             const double v = red[i * 3 + j][0] + ((if_ext && i == j) ? 0.5 * ph.dt : 0.0);
@@ -548,14 +762,14 @@ cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int
 
 cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
-                               int mode, int level_last, int step_n, PairInfo* pairs,
-                               unsigned* counts, cudaStream_t s) {
+                               int mode, int level_last, int level_cap, int step_n, int select,
+                               PairInfo* pairs, unsigned* counts, cudaStream_t s) {
     const long long n = (long long)nnodes * nelem_color;
     if (n == 0) return cudaSuccess;
     const int bs = 256;
     k_pair_window<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(
-        coords, ien, elems, nelem_color, node_lo, nnodes, ph, mode, level_last, step_n, pairs,
-        counts);
+        coords, ien, elems, nelem_color, node_lo, nnodes, ph, mode, level_last, level_cap, step_n,
+        select, pairs, counts);
     return cudaGetLastError();
 }
 
@@ -565,11 +779,15 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, const in
                                   int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  int /*precision*/, cudaStream_t s) {
+                                  int fp32_far, cudaStream_t s) {
     if (nitems == 0) return cudaSuccess;
     const int bs = 128;
     const unsigned grid = (nitems + bs - 1) / bs;
-    if (mode == ASM_LEVELS) {
+    if (fp32_far) {
+        k_assemble_far_f32<<<(nitems + 255) / 256, 256, 0, s>>>(
+            coords, ien, elems, nelem_color, node_lo, nq * nq, geom, ph, level_last, pairs,
+            offsets, npairs, nitems, out);
+    } else if (mode == ASM_LEVELS) {
         k_assemble_items<ASM_LEVELS><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
                                                          node_lo, nq, gx, gw, geom, ph,
                                                          level_last, step_n, 0, pairs, offsets,

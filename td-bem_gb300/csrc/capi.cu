@@ -160,6 +160,8 @@ void free_levels(tdbem_ctx* c) {
     dfree(c->d_H);
     dfree(c->d_Gf);
     dfree(c->d_Hf);
+    dfree(c->d_G01);
+    dfree(c->d_H01);
     c->level_precision = -1;
     c->levels_last = 0;
 }
@@ -167,6 +169,23 @@ void free_levels(tdbem_ctx* c) {
 void free_march(tdbem_ctx* c) {
     dfree(c->d_u);
     dfree(c->d_t);
+    for (int v = 0; v < 2; v++) {
+        if (v == 1 && c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
+        if (v == 1 && c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
+        dfree(c->d_inv32[v]);
+        dfree(c->d_Hc64[v]);
+    }
+    dfree(c->d_Wt_old);
+    dfree(c->d_Wu_old);
+    dfree(c->d_Wt_new);
+    dfree(c->d_Wu_new);
+    dfree(c->d_Yold);
+    dfree(c->d_pmix);
+    dfree(c->d_res);
+    dfree(c->d_dx);
+    dfree(c->d_colk32);
+    dfree(c->d_rowk32);
+    dfree(c->d_tmp32);
     if (c->d_Ainv[1] == c->d_Ainv[0]) c->d_Ainv[1] = nullptr;
     dfree(c->d_Ainv[0]);
     dfree(c->d_Ainv[1]);
@@ -178,6 +197,9 @@ void free_march(tdbem_ctx* c) {
 // J-part wave integrals with their differences 150, kernel scalars 37, the two
 // 3x3 kernels 65, accumulation into the 4 node blocks 124.
 constexpr double kFlopsPerItemPoint = 398.0;
+// The FP32 far-field form (tau variables): geometry 20, wave polynomials and
+// differences 176, scalars 40, kernels 65, accumulation 124.
+constexpr double kFlopsPerItemPointF32 = 425.0;
 
 int prof_begin(tdbem_ctx* c, int cls) {
     if (!c->prof) return -1;
@@ -217,7 +239,7 @@ void prof_flush(tdbem_ctx* c) {
 // Run the window / scan / item kernels of one colour over collocation nodes
 // [node_lo, node_lo + nnodes), chunked so that item indices fit in 32 bits.
 int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, int level_last,
-                   int step_n, const AsmOut& out, int precision) {
+                   int level_cap, int step_n, int select, int fp32_far, const AsmOut& out) {
     const int e0 = c->color_start[color], ne = c->color_start[color + 1] - e0;
     if (ne == 0 || nnodes == 0) return TDBEM_OK;
     const int* elems = c->d_color_elems + e0;
@@ -229,7 +251,8 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
         const int nn = std::min(chunk, node_lo + nnodes - n0);
         const unsigned npairs = (unsigned)((long long)nn * ne);
         CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, elems, ne, n0, nn, c->ph, mode,
-                                    level_last, step_n, c->d_pairs, c->d_counts, c->stream));
+                                    level_last, level_cap, step_n, select, c->d_pairs,
+                                    c->d_counts, c->stream));
         CUDA_TRY(exclusive_scan(c->d_counts, c->d_offsets, npairs, c->d_scan_tmp,
                                 c->scan_tmp_bytes, c->stream));
         c->launches += 3;  // window + the scan's init and scan kernels
@@ -243,13 +266,14 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
         const int pe = prof_begin(c, TDBEM_K_ASSEMBLE);
         CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, elems, ne, n0, c->nq, c->d_gx,
                                        c->d_gw, c->d_geom, c->ph, mode, level_last, step_n,
-                                       c->d_pairs, c->d_offsets, npairs, nitems, out, precision,
+                                       c->d_pairs, c->d_offsets, npairs, nitems, out, fp32_far,
                                        c->stream));
         if (nitems) c->launches += (mode == ASM_STEP ? 2 : 1);
         const double pts = (double)c->nq * c->nq;
         const double items = (double)nitems * (mode == ASM_STEP ? 2.0 : 1.0);
-        prof_end(c, pe, items * 4 * 45 * (precision == TDBEM_FP64 ? 8.0 : 4.0) * 2,
-                 items * pts * kFlopsPerItemPoint * (mode == ASM_STEP ? 0.5 : 1.0));
+        prof_end(c, pe, items * 4 * 45 * (out.G0f ? 4.0 : 8.0) * 2,
+                 items * pts * (fp32_far ? kFlopsPerItemPointF32 : kFlopsPerItemPoint) *
+                     (mode == ASM_STEP ? 0.5 : 1.0));
     }
     return TDBEM_OK;
 }
@@ -273,6 +297,111 @@ struct EventTimer {
         return ms;
     }
 };
+
+
+// Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
+// inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
+int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
+    const int D = c->D, M = c->M, nb = c->nb;
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const size_t DD = (size_t)D * D;
+    const int ldw = mixed_ldw(D);
+    cudaStream_t s = c->stream;
+    if (!c->d_Wt_old) {
+        CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
+        CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
+        CUDA_TRY(dalloc(&c->d_Wt_new, (size_t)(M + 1) * ldw));
+        CUDA_TRY(dalloc(&c->d_Wu_new, (size_t)(M + 1) * ldw));
+        CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
+        CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
+        CUDA_TRY(dalloc(&c->d_res, D));
+        CUDA_TRY(dalloc(&c->d_dx, D));
+        CUDA_TRY(dalloc(&c->d_colk32, D));
+        CUDA_TRY(dalloc(&c->d_rowk32, D));
+        CUDA_TRY(dalloc(&c->d_tmp32, (size_t)kPermuteBlocks * D));
+    }
+    // distinct LHS: step 2 and steps >= 3
+    EventTimer tf;
+    tf.start(s);
+    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
+    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
+    for (int v = 0; v < 2; v++) {
+        if (c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
+        if (c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
+    }
+    for (int v = 0; v < ninv; v++) {
+        if (!c->d_Hc64[v]) CUDA_TRY(dalloc(&c->d_Hc64[v], DD));
+        if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
+        CUDA_TRY(launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
+                                  lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], s));
+        const int pe = prof_begin(c, TDBEM_K_FACTOR);
+        cudaError_t e = gje_invert_f32(c->d_Hc64[v], c->d_inv32[v], D, c->d_perm, c->d_colk32,
+                                       c->d_rowk32, c->d_status, c->d_tmp32, s);
+        prof_end(c, pe, 2.0 * 4 * DD, 2.0 * (double)D * D * D);
+        c->launches += 2 + 2LL * D + 1;
+        if (e == cudaErrorInvalidValue)
+            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
+        CUDA_TRY(e);
+    }
+    if (ninv == 1) {
+        if (c->d_inv32[1] && c->d_inv32[1] != c->d_inv32[0]) dfree(c->d_inv32[1]);
+        if (c->d_Hc64[1] && c->d_Hc64[1] != c->d_Hc64[0]) dfree(c->d_Hc64[1]);
+        c->d_inv32[1] = c->d_inv32[0];
+        c->d_Hc64[1] = c->d_Hc64[0];
+    }
+    c->timings[1] = tf.stop_ms(s);
+
+    EventTimer tmr;
+    tmr.start(s);
+    const size_t lstride = (size_t)D * c->ldf;
+    const int last_s = numstep - 1;  // solve steps 1..numstep-1
+    for (int S = 1; S <= last_s; S += nb) {
+        const int nbe = std::min(nb, last_s - S + 1);
+        if (S > 1) {
+            const int nlev = std::min(M, S + nbe - 1) + 1;
+            CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, ldw,
+                                        c->d_Wt_old, c->d_Wu_old, s));
+            const int nch = mixed_chunks(nlev, D);
+            const int pe = prof_begin(c, TDBEM_K_CONV);
+            CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
+                                     c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch, s));
+            prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
+                     nlev * 4.0 * nb * (double)DD);
+            CUDA_TRY(launch_reduce_cols(c->d_pmix, nch, nb, D, nullptr, c->d_Yold, s));
+            c->launches += 3;
+        } else {
+            CUDA_TRY(cudaMemsetAsync(c->d_Yold, 0, sizeof(double) * nb * D, s));
+        }
+        for (int j = 0; j < nbe; j++) {
+            const int st = S + j;
+            const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
+            const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
+            const double amp = c->amp.empty() ? 1.0 : c->amp[st];
+            const int L = std::min(M, std::max(1, st + 1 - S));
+            CUDA_TRY(launch_build_w_new(c->d_u, c->d_t, D, st, S, L + 1, a1, a2, a3, c0, c1, amp,
+                                        c->d_load_t, c->d_load_u, ldw, c->d_Wt_new, c->d_Wu_new,
+                                        s));
+            const int nch = mixed_chunks(L + 1, D);
+            int pe = prof_begin(c, TDBEM_K_CONV);
+            CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, L, 1, c->d_Wt_new,
+                                     c->d_Wu_new, ldw, c->d_pmix, nch, s));
+            prof_end(c, pe, (L + 1) * 2.0 * (double)lstride * 4, (L + 1) * 4.0 * (double)DD);
+            pe = prof_begin(c, TDBEM_K_SOLVE);
+            CUDA_TRY(launch_reduce_cols(c->d_pmix, nch, 1, D, c->d_Yold + (size_t)j * D,
+                                        c->d_rhs, s));
+            const int v = st == 1 ? 0 : 1;
+            CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_rhs, c->d_x,
+                                        c->d_res, c->d_dx, c->n_refine, s));
+            CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+                                         c->d_fbc_map, amp, c->d_u, c->d_t, s));
+            prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine) / 1.0,
+                     2.0 * (double)DD * (1 + 2 * c->n_refine));
+            c->launches += 4 + 1 + 3LL * c->n_refine + 1;
+        }
+    }
+    c->timings[2] = tmr.stop_ms(s);
+    return TDBEM_OK;
+}
 
 }  // namespace
 
@@ -445,8 +574,9 @@ int tdbem_get_stream(const tdbem_ctx* c, void** stream) {
 
 int tdbem_level_bytes(const tdbem_ctx* c, int precision, size_t* bytes) {
     if (!c || !bytes) return fail(TDBEM_ERR_ARG, "null argument");
-    const size_t per = precision == TDBEM_FP64 ? 8 : 4;
-    *bytes = 2 * (size_t)(c->M + 1) * c->D * (size_t)c->D * per;
+    const size_t D = c->D;
+    if (precision == TDBEM_FP64) *bytes = 2 * (size_t)(c->M + 1) * D * D * 8;
+    else *bytes = 2 * (size_t)(c->M + 1) * D * mixed_ld(c->D) * 4 + 4 * D * D * 8;
     return TDBEM_OK;
 }
 
@@ -466,12 +596,14 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
     out.G1 = buf + 2 * n;
     out.H1 = buf + 3 * n;
     out.D = c->D;
+    out.ld = c->D;
     out.row_node_lo = node_lo;
     int rc = TDBEM_OK;
     cudaError_t e = cudaMemsetAsync(buf, 0, sizeof(double) * 4 * n, c->stream);
     if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
     for (size_t col = 0; rc == TDBEM_OK && col + 1 < c->color_start.size(); col++)
-        rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, step, out, TDBEM_FP64);
+        rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, 1 << 30, step, SEL_ALL, 0,
+                            out);
     if (rc == TDBEM_OK && step == 1) {
         e = launch_cterm(c->d_coords, c->d_ien, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
                          c->d_geom, c->ph, c->if_ext, ASM_STEP, step, out, c->stream);
@@ -495,41 +627,78 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
     if (nsteps < 1) return fail(TDBEM_ERR_ARG, "nsteps must be >= 1");
     if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
         return fail(TDBEM_ERR_ARG, "unknown precision %d", precision);
-    const size_t stride = (size_t)c->D * c->D;
-    const size_t total = (size_t)(c->M + 1) * stride;
+    const size_t D = c->D;
+    const int ldf = mixed_ld(c->D);
     if (c->level_precision != precision) {
         free_levels(c);
         if (precision == TDBEM_FP64) {
-            CUDA_TRY(dalloc(&c->d_G, total));
-            CUDA_TRY(dalloc(&c->d_H, total));
+            CUDA_TRY(dalloc(&c->d_G, (size_t)(c->M + 1) * D * D));
+            CUDA_TRY(dalloc(&c->d_H, (size_t)(c->M + 1) * D * D));
         } else {
-            CUDA_TRY(dalloc(&c->d_Gf, total));
-            CUDA_TRY(dalloc(&c->d_Hf, total));
+            CUDA_TRY(dalloc(&c->d_Gf, (size_t)(c->M + 1) * D * ldf));
+            CUDA_TRY(dalloc(&c->d_Hf, (size_t)(c->M + 1) * D * ldf));
+            CUDA_TRY(dalloc(&c->d_G01, 2 * D * D));
+            CUDA_TRY(dalloc(&c->d_H01, 2 * D * D));
         }
         c->level_precision = precision;
+        c->ldf = ldf;
     }
     EventTimer tm;
     tm.start(c->stream);
-    const size_t esz = precision == TDBEM_FP64 ? 8 : 4;
-    void* G = precision == TDBEM_FP64 ? (void*)c->d_G : (void*)c->d_Gf;
-    void* H = precision == TDBEM_FP64 ? (void*)c->d_H : (void*)c->d_Hf;
-    CUDA_TRY(cudaMemsetAsync(G, 0, esz * total, c->stream));
-    CUDA_TRY(cudaMemsetAsync(H, 0, esz * total, c->stream));
     const int last = std::min(c->M, nsteps);
-    AsmOut out{};
-    out.G0 = c->d_G;
-    out.H0 = c->d_H;
-    out.G0f = c->d_Gf;
-    out.H0f = c->d_Hf;
-    out.level_stride = stride;
-    out.D = c->D;
-    for (size_t col = 0; col + 1 < c->color_start.size(); col++) {
-        const int rc = assemble_color(c, (int)col, 0, c->nnd, ASM_LEVELS, last, 0, out, precision);
-        if (rc != TDBEM_OK) return rc;
+    const int ncol = (int)c->color_start.size() - 1;
+    if (precision == TDBEM_FP64) {
+        const size_t total = (size_t)(c->M + 1) * D * D;
+        CUDA_TRY(cudaMemsetAsync(c->d_G, 0, 8 * total, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->d_H, 0, 8 * total, c->stream));
+        AsmOut out{};
+        out.G0 = c->d_G;
+        out.H0 = c->d_H;
+        out.level_stride = D * D;
+        out.D = c->D;
+        out.ld = c->D;
+        for (int col = 0; col < ncol; col++) {
+            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_ALL,
+                                          0, out);
+            if (rc != TDBEM_OK) return rc;
+        }
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, out, c->stream));
+        c->launches += 1;
+    } else {
+        // FP32 store for all levels: near pairs with the FP64 quadrature, far pairs with
+        // the FP32 tau form; levels 0 and 1 again in FP64 for the LHS of the solve.
+        const size_t total = (size_t)(c->M + 1) * D * ldf;
+        CUDA_TRY(cudaMemsetAsync(c->d_Gf, 0, 4 * total, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->d_Hf, 0, 4 * total, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->d_G01, 0, 16 * D * D, c->stream));
+        CUDA_TRY(cudaMemsetAsync(c->d_H01, 0, 16 * D * D, c->stream));
+        AsmOut o32{};
+        o32.G0f = c->d_Gf;
+        o32.H0f = c->d_Hf;
+        o32.level_stride = D * ldf;
+        o32.D = c->D;
+        o32.ld = ldf;
+        AsmOut o64{};
+        o64.G0 = c->d_G01;
+        o64.H0 = c->d_H01;
+        o64.level_stride = D * D;
+        o64.D = c->D;
+        o64.ld = c->D;
+        for (int col = 0; col < ncol; col++) {
+            int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_NEAR, 0, o32);
+            if (rc == TDBEM_OK)
+                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_FAR, 1, o32);
+            if (rc == TDBEM_OK)
+                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, 0, o64);
+            if (rc != TDBEM_OK) return rc;
+        }
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, o32, c->stream));
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, o64, c->stream));
+        c->launches += 2;
     }
-    CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                          c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, out, c->stream));
-    c->launches += 1;
     c->timings[0] = tm.stop_ms(c->stream);
     CUDA_TRY(cudaGetLastError());
     prof_flush(c);
@@ -550,9 +719,10 @@ int tdbem_get_level(tdbem_ctx* c, int k, int which, double* host_out) {
         CUDA_TRY(cudaStreamSynchronize(c->stream));
     } else {
         std::vector<float> tmp(stride);
-        const float* src = (which == 0 ? c->d_Gf : c->d_Hf) + k * stride;
-        CUDA_TRY(cudaMemcpyAsync(tmp.data(), src, sizeof(float) * stride, cudaMemcpyDeviceToHost,
-                                 c->stream));
+        const float* src = (which == 0 ? c->d_Gf : c->d_Hf) + (size_t)k * c->D * c->ldf;
+        CUDA_TRY(cudaMemcpy2DAsync(tmp.data(), sizeof(float) * c->D, src, sizeof(float) * c->ldf,
+                                   sizeof(float) * c->D, c->D, cudaMemcpyDeviceToHost,
+                                   c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         for (size_t i = 0; i < stride; i++) host_out[i] = tmp[i];
     }
@@ -663,6 +833,19 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
     const size_t stride = (size_t)D * D;
     // LHS of step 2 (SolverStepLinearT.cpp:357-371) and of steps >= 3 (381-393)
     const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+    if (c->level_precision == TDBEM_MIXED) {
+        const int rc = march_mixed(c, numstep, lhs_c);
+        if (rc != TDBEM_OK) return rc;
+        if (u_hist)
+            CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
+                                     cudaMemcpyDeviceToHost, s));
+        if (t_hist)
+            CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
+                                     cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        prof_flush(c);
+        return TDBEM_OK;
+    }
     const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
     EventTimer tf;
     tf.start(s);
@@ -722,6 +905,30 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
                                  cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     prof_flush(c);
+    return TDBEM_OK;
+}
+
+int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (block_steps != 1 && block_steps != 8 && block_steps != 12 && block_steps != 16)
+        return fail(TDBEM_ERR_ARG, "block_steps must be 1, 8, 12 or 16");
+    if (refine_sweeps < 0 || refine_sweeps > 4)
+        return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
+    if (block_steps != c->nb) {  // scratch sized by the block
+        dfree(c->d_Wt_old);
+        dfree(c->d_Wu_old);
+        dfree(c->d_Wt_new);
+        dfree(c->d_Wu_new);
+        dfree(c->d_Yold);
+        dfree(c->d_pmix);
+        dfree(c->d_res);
+        dfree(c->d_dx);
+        dfree(c->d_colk32);
+        dfree(c->d_rowk32);
+        dfree(c->d_tmp32);
+    }
+    c->nb = block_steps;
+    c->n_refine = refine_sweeps;
     return TDBEM_OK;
 }
 

@@ -1,0 +1,398 @@
+// Mixed-precision time marching on sm_103a: FP32 level store, time-blocked
+// history convolution, FP32 inverse of the column-exchanged LHS with FP64
+// iterative refinement against the FP64 LHS.
+//
+// Time blocking.  The right-hand side of step s (SolverStepLinearT.cpp:400-482)
+// is sum_f X^f w_f(s) with w_f(s) a combination of the history vectors x^m,
+// m in {s+1-f, s-f, s-1-f} (and -a1 x^{s-1} on level 0).  For a block of NB steps
+// s = S..S+NB-1, the part with m < S (history known when the block starts) is
+// one pass over the levels with NB right-hand-side columns,
+//     Y_old[:, j] = sum_f X^f W_f^old[:, j],
+// so each level is read once per block instead of once per step.  The part with
+// S <= m < s needs only levels f <= s - S + 1 and is added step by step.
+#include <algorithm>
+
+#include "tdbem_internal.cuh"
+
+namespace tdbem {
+
+namespace {
+
+constexpr int kRowsPerWarp = 4;
+constexpr int kWarps = 8;
+constexpr int kRows = kRowsPerWarp * kWarps;  // rows per block
+constexpr int kKC = 256;                      // columns staged in shared memory per pass
+
+// partial[chunk][j][row] = sum_{f in chunk} (G^f[row,:] . Wt[f][j] - H^f[row,:] . Wu[f][j])
+// for NB right-hand-side columns.  Levels are FP32 with row stride ld (a multiple
+// of 4, zero-padded); W is FP32 [f][j][ldw] with ldw a multiple of kKC,
+// zero-padded; products and per-lane sums are FP32, the cross-lane and
+// cross-chunk sums FP64.
+template <int NB>
+__global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
+                                                  const float* __restrict__ H, size_t lstride,
+                                                  int ld, int D, int f_lo, int f_hi,
+                                                  int per_chunk, const float* __restrict__ Wt,
+                                                  const float* __restrict__ Wu, int ldw,
+                                                  double* __restrict__ partial) {
+    __shared__ float4 sw[2][NB][kKC / 4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = blockIdx.x * kRows + warp * kRowsPerWarp;
+    const int f0 = f_lo + blockIdx.y * per_chunk;
+    const int f1 = min(f_hi, f0 + per_chunk - 1);
+    float acc[kRowsPerWarp][NB];
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; r++)
+#pragma unroll
+        for (int j = 0; j < NB; j++) acc[r][j] = 0.f;
+    size_t rowoff[kRowsPerWarp];
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; r++) rowoff[r] = (size_t)min(row0 + r, D - 1) * ld;
+    for (int f = f0; f <= f1; f++) {
+        const float* Gf = G + (size_t)f * lstride;
+        const float* Hf = H + (size_t)f * lstride;
+        const float4* wt = reinterpret_cast<const float4*>(Wt + (size_t)f * NB * ldw);
+        const float4* wu = reinterpret_cast<const float4*>(Wu + (size_t)f * NB * ldw);
+        for (int k0 = 0; k0 < ld; k0 += kKC) {
+            __syncthreads();
+            for (int i = threadIdx.x; i < NB * (kKC / 4); i += blockDim.x) {
+                const int j = i / (kKC / 4), kk = i % (kKC / 4);
+                sw[0][j][kk] = wt[(size_t)j * (ldw / 4) + k0 / 4 + kk];
+                sw[1][j][kk] = wu[(size_t)j * (ldw / 4) + k0 / 4 + kk];
+            }
+            __syncthreads();
+#pragma unroll 2
+            for (int kk = lane; kk < kKC / 4; kk += 32) {
+                const int k = k0 + 4 * kk;
+                if (k >= ld) break;
+#pragma unroll
+                for (int r = 0; r < kRowsPerWarp; r++) {
+                    const float4 g = __ldcs(reinterpret_cast<const float4*>(Gf + rowoff[r] + k));
+                    const float4 h = __ldcs(reinterpret_cast<const float4*>(Hf + rowoff[r] + k));
+#pragma unroll
+                    for (int j = 0; j < NB; j++) {
+                        const float4 a = sw[0][j][kk], b = sw[1][j][kk];
+                        acc[r][j] += (g.x * a.x + g.y * a.y + g.z * a.z + g.w * a.w) -
+                                     (h.x * b.x + h.y * b.y + h.z * b.z + h.w * b.w);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kRowsPerWarp; r++)
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            double v = acc[r][j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && row0 + r < D)
+                partial[((size_t)blockIdx.y * NB + j) * D + row0 + r] = v;
+        }
+}
+
+// W_f^old[:, j] for s = S + j, history indices 1 <= m < S only (no load terms).
+__global__ void k_build_w_old(const double* __restrict__ u_hist,
+                              const double* __restrict__ t_hist, int D, int S, int nb, int nlev,
+                              double a1, double a2, double a3, int ldw, float* __restrict__ Wt,
+                              float* __restrict__ Wu) {
+    const size_t total = (size_t)nlev * nb * ldw;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % ldw);
+        const int j = (int)((idx / ldw) % nb);
+        const int f = (int)(idx / ((size_t)ldw * nb));
+        const int s = S + j;
+        double wt = 0, wu = 0;
+        if (k < D) {
+            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+            if (f >= 2 && m1 >= 1 && m1 < S) {
+                wt += a1 * t_hist[(size_t)m1 * D + k];
+                wu += a1 * u_hist[(size_t)m1 * D + k];
+            }
+            if (f >= 1 && m3 >= 1 && m3 < S) {
+                wt += a3 * t_hist[(size_t)m3 * D + k];
+                wu += a3 * u_hist[(size_t)m3 * D + k];
+            }
+            if (m2 >= 1 && m2 < S) {
+                wt += a2 * t_hist[(size_t)m2 * D + k];
+                wu += a2 * u_hist[(size_t)m2 * D + k];
+            }
+            if (f == 0 && s - 1 >= 1 && s - 1 < S) {
+                wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
+                wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
+            }
+        }
+        Wt[idx] = (float)wt;
+        Wu[idx] = (float)wu;
+    }
+}
+
+// w_f^new for step s: history indices S <= m <= s-1, plus the known-load terms
+// of levels 0/1 (c0, c1: the LHS weights of those levels).
+__global__ void k_build_w_new(const double* __restrict__ u_hist,
+                              const double* __restrict__ t_hist, int D, int s, int S, int nlev,
+                              double a1, double a2, double a3, double c0, double c1, double amp,
+                              const double* __restrict__ load_t,
+                              const double* __restrict__ load_u, int ldw,
+                              float* __restrict__ Wt, float* __restrict__ Wu) {
+    const size_t total = (size_t)nlev * ldw;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % ldw), f = (int)(idx / ldw);
+        double wt = 0, wu = 0;
+        if (k < D) {
+            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+            if (f >= 2 && m1 >= S && m1 >= 1) {
+                wt += a1 * t_hist[(size_t)m1 * D + k];
+                wu += a1 * u_hist[(size_t)m1 * D + k];
+            }
+            if (f >= 1 && m3 >= S && m3 >= 1) {
+                wt += a3 * t_hist[(size_t)m3 * D + k];
+                wu += a3 * u_hist[(size_t)m3 * D + k];
+            }
+            if (m2 >= S && m2 >= 1) {
+                wt += a2 * t_hist[(size_t)m2 * D + k];
+                wu += a2 * u_hist[(size_t)m2 * D + k];
+            }
+            if (f == 0) {
+                if (s - 1 >= S && s - 1 >= 1) {
+                    wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
+                    wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
+                }
+                wt += c0 * (amp * load_t[k]);
+                wu += c0 * load_u[k];
+            } else if (f == 1) {
+                wt += c1 * (amp * load_t[k]);
+                wu += c1 * load_u[k];
+            }
+        }
+        Wt[idx] = (float)wt;
+        Wu[idx] = (float)wu;
+    }
+}
+
+// out[j][row] = sum over chunks of partial[chunk][j][row] (+ add[j][row] if given).
+__global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, int nb, int D,
+                              const double* __restrict__ add, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nb * D) return;
+    double s = add ? add[i] : 0.0;
+    for (int c = 0; c < nchunks; c++) s += partial[(size_t)c * nb * D + i];
+    out[i] = s;
+}
+
+// y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per row.
+__global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, int D,
+                                                  const double* __restrict__ v,
+                                                  double* __restrict__ y, int accumulate) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= D) return;
+    const float* a = A + (size_t)row * D;
+    float acc = 0.f;
+    for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * (float)v[j];
+    double s = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) y[row] = accumulate ? y[row] + s : s;
+}
+
+// r = b - A64 x, FP64; warp per row.
+__global__ void __launch_bounds__(256) k_residual_f64(const double* __restrict__ A, int D,
+                                                      const double* __restrict__ x,
+                                                      const double* __restrict__ b,
+                                                      double* __restrict__ r) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= D) return;
+    const double* a = A + (size_t)row * D;
+    double acc = 0;
+    for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * x[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) r[row] = b[row] - acc;
+}
+
+__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// Gauss-Jordan with partial pivoting in FP32 (same structure as the FP64 one).
+__global__ void __launch_bounds__(1024) k_gje_pivot_f32(float* __restrict__ A, int n, int k,
+                                                        int* __restrict__ perm,
+                                                        float* __restrict__ colk,
+                                                        float* __restrict__ rowk,
+                                                        int* __restrict__ status) {
+    __shared__ float sv[1024];
+    __shared__ int si[1024];
+    float best = -1.f;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+        const float v = fabsf(A[(size_t)i * n + k]);
+        if (v > best) { best = v; bi = i; }
+    }
+    sv[threadIdx.x] = best;
+    si[threadIdx.x] = bi;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            const float v2 = sv[threadIdx.x + s];
+            const int i2 = si[threadIdx.x + s];
+            if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
+                sv[threadIdx.x] = v2;
+                si[threadIdx.x] = i2;
+            }
+        }
+        __syncthreads();
+    }
+    const int p = si[0];
+    if (p >= n || sv[0] == 0.f) {
+        if (threadIdx.x == 0) *status = 1;
+        return;
+    }
+    if (threadIdx.x == 0) perm[k] = p;
+    if (p != k)
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            const float t = A[(size_t)k * n + j];
+            A[(size_t)k * n + j] = A[(size_t)p * n + j];
+            A[(size_t)p * n + j] = t;
+        }
+    __syncthreads();
+    const float inv = 1.f / A[(size_t)k * n + k];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        colk[i] = A[(size_t)i * n + k];
+        rowk[i] = (i == k ? 1.f : A[(size_t)k * n + i]) * inv;
+    }
+}
+
+__global__ void k_gje_update_f32(float* __restrict__ A, int n, int k,
+                                 const float* __restrict__ colk, const float* __restrict__ rowk,
+                                 const int* __restrict__ status) {
+    if (*status) return;
+    const size_t total = (size_t)n * n;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(idx / n), j = (int)(idx % n);
+        if (i == k) A[idx] = rowk[j];
+        else A[idx] = (j == k ? 0.f : A[idx]) - colk[i] * rowk[j];
+    }
+}
+
+__global__ void k_permute_cols_f32(float* __restrict__ A, int n, const int* __restrict__ cols,
+                                   float* __restrict__ tmp) {
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        float* row = A + (size_t)i * n;
+        float* t = tmp + (size_t)blockIdx.x * n;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) t[j] = row[cols[j]];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) row[j] = t[j];
+        __syncthreads();
+    }
+}
+
+__global__ void k_add(double* __restrict__ x, const double* __restrict__ d, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += d[i];
+}
+
+}  // namespace
+
+int mixed_ldw(int D) { return (D + kKC - 1) / kKC * kKC; }
+int mixed_ld(int D) { return (D + 3) / 4 * 4; }
+
+int mixed_chunks(int nlev, int D) {
+    const int tiles = (D + kRows - 1) / kRows;
+    const int chunks = (4 * 152 + tiles - 1) / tiles;
+    return std::max(1, std::min(chunks, nlev));
+}
+
+cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int ld, int D,
+                            int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
+                            int ldw, double* partial, int nchunks, cudaStream_t s) {
+    const int nlev = f_hi - f_lo + 1;
+    const int per_chunk = (nlev + nchunks - 1) / nchunks;
+    dim3 grid((D + kRows - 1) / kRows, nchunks);
+    // W for level f sits at W + (f - f_lo) * nb * ldw: pass shifted base pointers
+    const float* wt = Wt - (size_t)f_lo * nb * ldw;
+    const float* wu = Wu - (size_t)f_lo * nb * ldw;
+    switch (nb) {
+    case 1: k_conv_f32<1><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 8: k_conv_f32<8><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 12: k_conv_f32<12><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 16: k_conv_f32<16><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
+                               int nlev, double a1, double a2, double a3, int ldw, float* Wt,
+                               float* Wu, cudaStream_t s) {
+    const size_t total = (size_t)nlev * nb * ldw;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 8192);
+    k_build_w_old<<<grid, 256, 0, s>>>(u_hist, t_hist, D, S, nb, nlev, a1, a2, a3, ldw, Wt, Wu);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_new(const double* u_hist, const double* t_hist, int D, int st, int S,
+                               int nlev, double a1, double a2, double a3, double c0, double c1,
+                               double amp, const double* load_t, const double* load_u, int ldw,
+                               float* Wt, float* Wu, cudaStream_t s) {
+    const size_t total = (size_t)nlev * ldw;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 4096);
+    k_build_w_new<<<grid, 256, 0, s>>>(u_hist, t_hist, D, st, S, nlev, a1, a2, a3, c0, c1, amp,
+                                       load_t, load_u, ldw, Wt, Wu);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
+                               const double* add, double* out, cudaStream_t s) {
+    k_reduce_cols<<<(nb * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, D, add, out);
+    return cudaGetLastError();
+}
+
+// x = inv32 rhs, then n_refine times: r = rhs - A64 x; x += inv32 r.
+cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
+                               double* x, double* r, double* dx, int n_refine, cudaStream_t s) {
+    const unsigned g = (D * 32 + 255) / 256;
+    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, rhs, x, 0);
+    for (int it = 0; it < n_refine; it++) {
+        k_residual_f64<<<g, 256, 0, s>>>(A64, D, x, rhs, r);
+        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, r, dx, 0);
+        k_add<<<(D + 255) / 256, 256, 0, s>>>(x, dx, D);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t gje_invert_f32(const double* A64, float* A, int n, int* perm, float* colk,
+                           float* rowk, int* d_status, float* tmp_rows, cudaStream_t s) {
+    k_f64_to_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
+    cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < n; k++) {
+        k_gje_pivot_f32<<<1, 1024, 0, s>>>(A, n, k, perm, colk, rowk, d_status);
+        k_gje_update_f32<<<2432, 256, 0, s>>>(A, n, k, colk, rowk, d_status);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int status = 0;
+    std::vector<int> hperm(n);
+    e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (status) return cudaErrorInvalidValue;
+    std::vector<int> cols(n);
+    for (int j = 0; j < n; j++) cols[j] = j;
+    for (int k = n - 1; k >= 0; k--) std::swap(cols[k], cols[hperm[k]]);
+    e = cudaMemcpyAsync(perm, cols.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    k_permute_cols_f32<<<kPermuteBlocks, 256, 0, s>>>(A, n, perm, tmp_rows);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
+}  // namespace tdbem

@@ -32,6 +32,15 @@ struct PairInfo {
     int sing;   // singular corner (last element node within r^2 < 1e-9), -1 if regular
 };
 
+// Which pairs a window pass selects (mixed precision integrates well-separated
+// pairs in FP32 and the rest in FP64).
+enum PairSelect : int {
+    SEL_ALL = 0,   // every pair
+    SEL_NEAR = 1,  // singular pairs and pairs closer than kFarRatio element radii
+    SEL_FAR = 2,   // the others
+};
+constexpr double kFarRatio = 2.0;  // far: distance to the element's bounding sphere > 2 radii
+
 // Assembly output selection.
 enum AsmMode : int {
     ASM_LEVELS = 0,  // level k <- I(k dt) + J((k+1) dt)  (UpdateGHLinear placement)
@@ -45,8 +54,9 @@ struct AsmOut {
     double* H1;   // ASM_STEP: H_J rows
     float* G0f;   // FP32 level store (mixed precision), or null
     float* H0f;
-    size_t level_stride;  // entries per level (D*D) in ASM_LEVELS
+    size_t level_stride;  // entries per level in ASM_LEVELS (D * ld)
     int D;
+    int ld;               // row stride of the store written (D, or D padded for FP32)
     int row_node_lo;      // first collocation node of the row block
 };
 
@@ -56,15 +66,15 @@ cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int
                               cudaStream_t s);
 cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
-                               int mode, int level_last, int step_n, PairInfo* pairs,
-                               unsigned* counts, cudaStream_t s);
+                               int mode, int level_last, int level_cap, int step_n, int select,
+                               PairInfo* pairs, unsigned* counts, cudaStream_t s);
 cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
                                   int nelem_color, int node_lo, int nq, const double* gx,
                                   const double* gw, const double* geom, const Phys& ph,
                                   int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  int precision, cudaStream_t s);
+                                  int fp32_far, cudaStream_t s);
 cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, int if_ext, int mode,
@@ -103,6 +113,27 @@ cudaError_t launch_update_state(const double* x, int D, int s, const unsigned ch
                                 double* t_hist, cudaStream_t st);
 int conv_chunks(int L, int D);
 
+// Mixed-precision marching (march_mixed.cu).
+int mixed_ldw(int D);
+int mixed_ld(int D);
+int mixed_chunks(int nlev, int D);
+cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int ld, int D,
+                            int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
+                            int ldw, double* partial, int nchunks, cudaStream_t s);
+cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
+                               int nlev, double a1, double a2, double a3, int ldw, float* Wt,
+                               float* Wu, cudaStream_t s);
+cudaError_t launch_build_w_new(const double* u_hist, const double* t_hist, int D, int st, int S,
+                               int nlev, double a1, double a2, double a3, double c0, double c1,
+                               double amp, const double* load_t, const double* load_u, int ldw,
+                               float* Wt, float* Wu, cudaStream_t s);
+cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
+                               const double* add, double* out, cudaStream_t s);
+cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
+                               double* x, double* r, double* dx, int n_refine, cudaStream_t s);
+cudaError_t gje_invert_f32(const double* A64, float* A, int n, int* perm, float* colk,
+                           float* rowk, int* d_status, float* tmp_rows, cudaStream_t s);
+
 }  // namespace tdbem
 
 // The context (capi.cu owns its lifetime).
@@ -135,8 +166,27 @@ struct tdbem_ctx {
     int levels_last = 0;             // levels hold steps 1..levels_last
     double* d_G = nullptr;
     double* d_H = nullptr;
-    float* d_Gf = nullptr;
+    float* d_Gf = nullptr;          // mixed: FP32 levels 0..M, row stride ldf
     float* d_Hf = nullptr;
+    int ldf = 0;
+    double* d_G01 = nullptr;        // mixed: levels 0 and 1 in FP64 (the LHS)
+    double* d_H01 = nullptr;
+    // mixed marching
+    int nb = 12;                    // steps per time block
+    int n_refine = 1;               // FP64 refinement sweeps per solve
+    float* d_inv32[2] = {nullptr, nullptr};
+    double* d_Hc64[2] = {nullptr, nullptr};
+    float* d_Wt_old = nullptr;
+    float* d_Wu_old = nullptr;
+    float* d_Wt_new = nullptr;
+    float* d_Wu_new = nullptr;
+    double* d_Yold = nullptr;
+    double* d_pmix = nullptr;       // conv partials, chunks x nb x D
+    double* d_res = nullptr;
+    double* d_dx = nullptr;
+    float* d_colk32 = nullptr;
+    float* d_rowk32 = nullptr;
+    float* d_tmp32 = nullptr;
     // boundary conditions and marching parameters
     std::vector<int> ubc, fbc;
     std::vector<double> ubc_v, fbc_v;

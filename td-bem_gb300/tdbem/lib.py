@@ -50,6 +50,7 @@ SIGNATURES = {
     "tdbem_kernel_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp]),
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }
 
 KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve"}
@@ -156,6 +157,9 @@ class Context:
 
     def set_alpha(self, a1: float, a2: float):
         _check(load().tdbem_set_alpha(self.h, a1, a2))
+
+    def set_march_options(self, block_steps: int = 12, refine_sweeps: int = 1):
+        _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
 
     def set_load_history(self, amp):
         self._amp = np.ascontiguousarray(amp, np.float64)

@@ -1,0 +1,73 @@
+"""Mixed precision (FP32 far-field quadrature, FP32 levels, time-blocked FP32
+convolution, FP32 inverse with FP64 refinement) against the plain FP64 GPU form.
+
+Bar: relative L2 error of the displacement and traction histories <= 1e-4
+(||u_mixed - u_fp64||_2 / ||u_fp64||_2 over all steps and dofs)."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+TOL_L2 = 1e-4
+
+
+@pytest.fixture(scope="module")
+def tdlib():
+    import build as b
+    b.build()
+    from tdbem import lib
+    lib.load()
+    return lib
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def run(lib, m, precision, alpha=(0.25, 0.0), block=12, refine=1, numstep=None):
+    with lib.Context(m) as ctx:
+        ctx.set_alpha(*alpha)
+        ctx.set_march_options(block, refine)
+        ctx.assemble(precision=precision)
+        u, t = ctx.march(numstep)
+        lev = (ctx.level(3, 0), ctx.level(3, 1), ctx.level(ctx.M, 1))
+    return u, t, lev
+
+
+@pytest.fixture(scope="module")
+def sphere8(tdlib):
+    from tdbem import meshes
+    m = meshes.cubed_sphere(8, numstep=160)
+    return m, run(tdlib, m, tdlib.FP64)
+
+
+def test_mixed_levels_close_to_fp64(tdlib, sphere8):
+    m, (u, t, lev) = sphere8
+    _, _, lev32 = run(tdlib, m, tdlib.MIXED)
+    for a, b in zip(lev32, lev):
+        assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("block", [1, 8, 12, 16])
+def test_mixed_histories_within_1e4(tdlib, sphere8, block):
+    m, (u, t, _) = sphere8
+    u32, t32, _ = run(tdlib, m, tdlib.MIXED, block=block)
+    assert rel_l2(u32, u) <= TOL_L2
+    assert rel_l2(t32, t) <= TOL_L2
+
+
+def test_mixed_bar_with_prescribed_displacements(tdlib):
+    """UBC columns swapped into the LHS, alpha_2 != 0, traction at the loaded end."""
+    z, m = load_golden("bar_1x1x4_q2_alpha")
+    u, t, _ = run(tdlib, m, tdlib.FP64, alpha=(0.25, 0.1))
+    u32, t32, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1))
+    assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
+
+
+def test_refinement_recovers_fp64_solve(tdlib, sphere8):
+    m, (u, t, _) = sphere8
+    e0 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=0)[0], u)
+    e2 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=2)[0], u)
+    assert e2 <= e0 and e2 <= TOL_L2
