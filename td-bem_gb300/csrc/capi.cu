@@ -183,9 +183,7 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_pmix);
     dfree(c->d_res);
     dfree(c->d_dx);
-    dfree(c->d_colk32);
-    dfree(c->d_rowk32);
-    dfree(c->d_tmp32);
+
     if (c->d_Ainv[1] == c->d_Ainv[0]) c->d_Ainv[1] = nullptr;
     dfree(c->d_Ainv[0]);
     dfree(c->d_Ainv[1]);
@@ -316,9 +314,6 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
         CUDA_TRY(dalloc(&c->d_res, D));
         CUDA_TRY(dalloc(&c->d_dx, D));
-        CUDA_TRY(dalloc(&c->d_colk32, D));
-        CUDA_TRY(dalloc(&c->d_rowk32, D));
-        CUDA_TRY(dalloc(&c->d_tmp32, (size_t)kPermuteBlocks * D));
     }
     // distinct LHS: step 2 and steps >= 3
     EventTimer tf;
@@ -334,11 +329,12 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
         CUDA_TRY(launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
                                   lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], s));
+        if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(D)));
         const int pe = prof_begin(c, TDBEM_K_FACTOR);
-        cudaError_t e = gje_invert_f32(c->d_Hc64[v], c->d_inv32[v], D, c->d_perm, c->d_colk32,
-                                       c->d_rowk32, c->d_status, c->d_tmp32, s);
+        cudaError_t e = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, c->d_perm, c->d_status,
+                                   c->d_inv_scratch32, &c->launches, s);
         prof_end(c, pe, 2.0 * 4 * DD, 2.0 * (double)D * D * D);
-        c->launches += 2 + 2LL * D + 1;
+        c->launches += 1;
         if (e == cudaErrorInvalidValue)
             return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
         CUDA_TRY(e);
@@ -537,7 +533,8 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_fbc_map);
     dfree(c->d_is_ubc);
     dfree(c->d_is_fbc);
-    dfree(c->d_tmp_rows);
+    dfree(c->d_inv_scratch);
+    dfree(c->d_inv_scratch32);
     dfree(c->d_load_t);
     dfree(c->d_load_u);
     dfree(c->d_Wt);
@@ -546,8 +543,6 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_rhs);
     dfree(c->d_x);
     dfree(c->d_perm);
-    dfree(c->d_colk);
-    dfree(c->d_rowk);
     dfree(c->d_status);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -801,11 +796,8 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
         CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
         CUDA_TRY(dalloc(&c->d_rhs, D));
         CUDA_TRY(dalloc(&c->d_x, D));
-        CUDA_TRY(dalloc(&c->d_perm, D));
-        CUDA_TRY(dalloc(&c->d_colk, D));
-        CUDA_TRY(dalloc(&c->d_rowk, D));
+        CUDA_TRY(dalloc(&c->d_perm, D + kMaxPivotBlocks));
         CUDA_TRY(dalloc(&c->d_status, 1));
-        CUDA_TRY(dalloc(&c->d_tmp_rows, (size_t)kPermuteBlocks * D));
         c->partial_cap = (size_t)(c->M + 1) * D;
         CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
     }
@@ -856,11 +848,12 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
         if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
         CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
                                   lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
+        if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
         const int pe = prof_begin(c, TDBEM_K_FACTOR);
-        cudaError_t e = gje_invert(c->d_Ainv[v], D, c->d_perm, c->d_colk, c->d_rowk, c->d_status,
-                                   c->d_tmp_rows, s);
+        cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
+                                   &c->launches, s);
         prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
-        c->launches += 1 + 2LL * D + 1;  // LHS build, 2 per column, column permutation
+        c->launches += 1;  // LHS build
         if (e == cudaErrorInvalidValue)
             return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
         CUDA_TRY(e);
@@ -923,9 +916,6 @@ int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
         dfree(c->d_pmix);
         dfree(c->d_res);
         dfree(c->d_dx);
-        dfree(c->d_colk32);
-        dfree(c->d_rowk32);
-        dfree(c->d_tmp32);
     }
     c->nb = block_steps;
     c->n_refine = refine_sweeps;

@@ -1,0 +1,383 @@
+// Blocked in-place Gauss-Jordan inversion with partial pivoting (FP32 / FP64).
+//
+// Replaces KSPSolve's factorisation (SolverStepLinearT.cpp:503-504) by an
+// explicit inverse of the column-exchanged LHS, computed once per distinct LHS.
+// Panel step for columns C1 = [k0, k0+bw):
+//   1. LU with partial pivoting of the tall panel A[k0:, C1] (one block; pivots
+//      are searched among rows >= the current column, as unblocked GJE does);
+//   2. the panel's row swaps applied to all columns;
+//   3. Ainv11 = A11^-1 from the panel's L11 U11;
+//   4. T12 = Ainv11 A[R1, :]            (R1 = the bw pivot rows);
+//   5. A[i, j] -= A[i, C1] T12[:, j]     for rows i not in R1, columns j not in C1;
+//   6. A[R1, j] = T12[:, j] (j not in C1), A[R1, C1] = Ainv11,
+//      A[i, C1] = -A[i, C1] Ainv11       for rows i not in R1.
+// After the last panel the columns are permuted back (reverse order of the
+// row swaps).  Step 5 is a rank-bw update with bw-deep dot products, so the
+// whole inversion is 2 n^3 flops in GEMM form.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "tdbem_internal.cuh"
+
+namespace tdbem {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
+
+// Pivot sequence of the panel: LU with partial pivoting of rows k0..n-1 of
+// columns C1, spread over a cooperative grid (all blocks co-resident, so the
+// grid barriers always complete).  Each block keeps `rpb` panel rows in shared
+// memory; per column one barrier publishes the blocks' local maxima (ties to
+// the lowest row), a second one the exchanged pivot rows.
+// Only the pivot rows (perm) are produced: the swapped panel itself is re-read
+// from A by the later steps.
+template <typename T, int BW>
+__global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, int n, int k0,
+                                                      int bw, int rpb, int* __restrict__ perm,
+                                                      int* __restrict__ status,
+                                                      T* __restrict__ gval,
+                                                      int* __restrict__ gidx,
+                                                      T* __restrict__ grows) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    extern __shared__ unsigned char smem_raw[];
+    T* ws = reinterpret_cast<T*>(smem_raw);  // rpb x BW
+    __shared__ T sv[256];
+    __shared__ int si[256];
+    __shared__ T su[BW];
+    __shared__ int s_p;
+    const int rows = n - k0;
+    const int r0 = blockIdx.x * rpb, r1 = min(rows, r0 + rpb);
+    for (int idx = threadIdx.x; idx < rpb * BW; idx += blockDim.x) {
+        const int r = idx / BW, c = idx % BW;
+        ws[idx] = (r0 + r < r1 && c < bw) ? A[(size_t)(k0 + r0 + r) * n + k0 + c] : T(0);
+    }
+    __syncthreads();
+    for (int c = 0; c < bw; c++) {
+        T best = T(-1);
+        int bi = rows;
+        for (int r = max(r0, c) + threadIdx.x; r < r1; r += blockDim.x) {
+            const T v = absv(ws[(r - r0) * BW + c]);
+            if (v > best) { best = v; bi = r; }
+        }
+        sv[threadIdx.x] = best;
+        si[threadIdx.x] = bi;
+        __syncthreads();
+        for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+            if (threadIdx.x < st) {
+                const T v2 = sv[threadIdx.x + st];
+                const int i2 = si[threadIdx.x + st];
+                if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
+                    sv[threadIdx.x] = v2;
+                    si[threadIdx.x] = i2;
+                }
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            gval[blockIdx.x] = sv[0];
+            gidx[blockIdx.x] = si[0];
+        }
+        grid.sync();
+        if (threadIdx.x == 0) {  // every block reduces the same list in the same order
+            T bv = T(-1);
+            int bp = rows;
+            for (int b = 0; b < gridDim.x; b++) {
+                const T v = gval[b];
+                const int i = gidx[b];
+                if (v > bv || (v == bv && i < bp)) { bv = v; bp = i; }
+            }
+            s_p = (bp < rows && bv != T(0)) ? bp : -1;
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p < 0) {  // zero pivot: every block sees it and leaves
+            if (blockIdx.x == 0 && threadIdx.x == 0) *status = 1;
+            return;
+        }
+        // publish rows c and p, then swap them
+        if (c >= r0 && c < r1 && threadIdx.x < BW) grows[threadIdx.x] = ws[(c - r0) * BW + threadIdx.x];
+        if (p >= r0 && p < r1 && threadIdx.x < BW) grows[BW + threadIdx.x] = ws[(p - r0) * BW + threadIdx.x];
+        grid.sync();
+        if (threadIdx.x < BW) su[threadIdx.x] = grows[BW + threadIdx.x];
+        if (c >= r0 && c < r1 && threadIdx.x < BW) ws[(c - r0) * BW + threadIdx.x] = grows[BW + threadIdx.x];
+        if (p != c && p >= r0 && p < r1 && threadIdx.x < BW)
+            ws[(p - r0) * BW + threadIdx.x] = grows[threadIdx.x];
+        if (blockIdx.x == 0 && threadIdx.x == 0) perm[k0 + c] = k0 + p;
+        __syncthreads();
+        const T inv = T(1) / su[c];
+        for (int r = max(r0, c + 1) + threadIdx.x; r < r1; r += blockDim.x) {
+            T* wr = ws + (r - r0) * BW;
+            const T l = wr[c] * inv;
+            wr[c] = l;
+            for (int j = c + 1; j < bw; j++) wr[j] -= l * su[j];
+        }
+        // No barrier here: the next column's candidates and published rows are written
+        // only after every block has passed this column's second barrier.
+    }
+}
+
+// Row swaps of the panel applied to every column, in pivot order.
+template <typename T>
+__global__ void k_apply_swaps(T* __restrict__ A, int n, int k0, int bw,
+                              const int* __restrict__ perm, const int* __restrict__ status) {
+    if (*status) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    for (int c = 0; c < bw; c++) {
+        const int p = perm[k0 + c];
+        if (p != k0 + c) {
+            const T t = A[(size_t)(k0 + c) * n + j];
+            A[(size_t)(k0 + c) * n + j] = A[(size_t)p * n + j];
+            A[(size_t)p * n + j] = t;
+        }
+    }
+}
+
+// Ainv11 = A11^-1 for the swapped pivot block A[R1, C1]: Gauss-Jordan without
+// further pivoting in shared memory (A11 = L11 U11 with the panel's pivots, so
+// its pivots are U11's diagonal).  Entries beyond a narrow last panel are zero.
+template <typename T, int BW>
+__global__ void __launch_bounds__(1024) k_panel_inv(const T* __restrict__ A, int n, int k0,
+                                                    int bw, T* __restrict__ Ainv,
+                                                    const int* __restrict__ status) {
+    if (*status) return;
+    __shared__ T m[BW][BW + 1];
+    __shared__ T col[BW], row[BW];
+    for (int idx = threadIdx.x; idx < BW * BW; idx += blockDim.x) {
+        const int i = idx / BW, j = idx % BW;
+        m[i][j] = (i < bw && j < bw) ? A[(size_t)(k0 + i) * n + k0 + j] : T(i == j ? 1 : 0);
+    }
+    __syncthreads();
+    for (int c = 0; c < bw; c++) {
+        const T inv = T(1) / m[c][c];
+        if (threadIdx.x < BW) {
+            col[threadIdx.x] = m[threadIdx.x][c];
+            row[threadIdx.x] = (threadIdx.x == c ? T(1) : m[c][threadIdx.x]) * inv;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < BW * BW; idx += blockDim.x) {
+            const int i = idx / BW, j = idx % BW;
+            if (i == c) m[i][j] = row[j];
+            else m[i][j] = (j == c ? T(0) : m[i][j]) - col[i] * row[j];
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < BW * BW; idx += blockDim.x) {
+        const int i = idx / BW, j = idx % BW;
+        Ainv[idx] = (i < bw && j < bw) ? m[i][j] : T(0);
+    }
+}
+
+// T12[c][j] = sum_d Ainv11[c][d] A[k0+d][j] for every column j.
+template <typename T, int BW>
+__global__ void __launch_bounds__(256) k_panel_t12(const T* __restrict__ A, int n, int k0,
+                                                   int bw, const T* __restrict__ Ainv,
+                                                   T* __restrict__ T12,
+                                                   const int* __restrict__ status) {
+    if (*status) return;
+    __shared__ T sa[BW * BW];
+    for (int i = threadIdx.x; i < BW * BW; i += blockDim.x) sa[i] = Ainv[i];
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    T a[BW];
+#pragma unroll
+    for (int d = 0; d < BW; d++) a[d] = d < bw ? A[(size_t)(k0 + d) * n + j] : T(0);
+    for (int c = 0; c < bw; c++) {
+        T s = T(0);
+#pragma unroll
+        for (int d = 0; d < BW; d++) s += sa[c * BW + d] * a[d];
+        T12[(size_t)c * n + j] = s;
+    }
+}
+
+// A[i][j] -= sum_c A[i][k0+c] T12[c][j] for i not in R1, j not in C1.  64 x 64 tiles.
+template <typename T, int BW>
+__global__ void __launch_bounds__(256) k_panel_update(T* __restrict__ A, int n, int k0, int bw,
+                                                      const T* __restrict__ T12,
+                                                      const int* __restrict__ status) {
+    if (*status) return;
+    constexpr int TS = 64;
+    __shared__ T sp[TS][BW + 1];
+    __shared__ T st[BW][TS];
+    const int i0 = blockIdx.y * TS, j0 = blockIdx.x * TS;
+    for (int idx = threadIdx.x; idx < TS * BW; idx += blockDim.x) {
+        const int r = idx / BW, c = idx % BW;
+        const int i = i0 + r;
+        sp[r][c] = (i < n && c < bw) ? A[(size_t)i * n + k0 + c] : T(0);
+    }
+    for (int idx = threadIdx.x; idx < TS * BW; idx += blockDim.x) {
+        const int c = idx / TS, q = idx % TS;
+        const int j = j0 + q;
+        st[c][q] = (j < n && c < bw) ? T12[(size_t)c * n + j] : T(0);
+    }
+    __syncthreads();
+    const int tr = (threadIdx.x / 16) * 4, tc = (threadIdx.x % 16) * 4;
+    T acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = T(0);
+#pragma unroll 8
+    for (int c = 0; c < BW; c++) {
+        T pa[4], tb[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) pa[a] = sp[tr + a][c];
+#pragma unroll
+        for (int b = 0; b < 4; b++) tb[b] = st[c][tc + b];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc[a][b] += pa[a] * tb[b];
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const int i = i0 + tr + a;
+        if (i >= n || (i >= k0 && i < k0 + bw)) continue;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int j = j0 + tc + b;
+            if (j >= n || (j >= k0 && j < k0 + bw)) continue;
+            A[(size_t)i * n + j] -= acc[a][b];
+        }
+    }
+}
+
+// Rows R1 <- [T12 | Ainv11]; other rows' C1 block <- -A[i, C1] Ainv11.
+template <typename T, int BW>
+__global__ void __launch_bounds__(256) k_panel_finish(T* __restrict__ A, int n, int k0, int bw,
+                                                      const T* __restrict__ T12,
+                                                      const T* __restrict__ Ainv,
+                                                      const int* __restrict__ status) {
+    if (*status) return;
+    __shared__ T sa[BW * BW];
+    for (int i = threadIdx.x; i < BW * BW; i += blockDim.x) sa[i] = Ainv[i];
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) {  // row t, columns C1
+        const int i = t;
+        if (i >= k0 && i < k0 + bw) {
+            for (int d = 0; d < bw; d++) A[(size_t)i * n + k0 + d] = sa[(i - k0) * BW + d];
+        } else {
+            T a[BW];
+#pragma unroll
+            for (int c = 0; c < BW; c++) a[c] = c < bw ? A[(size_t)i * n + k0 + c] : T(0);
+            for (int d = 0; d < bw; d++) {
+                T s = T(0);
+#pragma unroll
+                for (int c = 0; c < BW; c++) s += a[c] * sa[c * BW + d];
+                A[(size_t)i * n + k0 + d] = -s;
+            }
+        }
+    }
+    // rows R1, columns outside C1 (a grid-stride pass over bw x n)
+    for (size_t idx = t; idx < (size_t)bw * n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int c = (int)(idx / n), j = (int)(idx % n);
+        if (j >= k0 && j < k0 + bw) continue;
+        A[(size_t)(k0 + c) * n + j] = T12[(size_t)c * n + j];
+    }
+}
+
+template <typename T>
+__global__ void k_permute_cols_t(T* __restrict__ A, int n, const int* __restrict__ cols,
+                                 T* __restrict__ tmp) {
+    for (int i = blockIdx.x; i < n; i += gridDim.x) {
+        T* row = A + (size_t)i * n;
+        T* t = tmp + (size_t)blockIdx.x * n;
+        for (int j = threadIdx.x; j < n; j += blockDim.x) t[j] = row[cols[j]];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) row[j] = t[j];
+        __syncthreads();
+    }
+}
+
+__global__ void k_cast_f64_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+template <typename T, int BW>
+cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
+                           cudaStream_t s) {
+    T* W = scratch;                          // 2*BW*n: permutation scratch rows at the end
+    T* T12 = W + (size_t)n * BW;             // BW x n
+    T* Ainv = T12 + (size_t)n * BW;          // BW x BW
+    T* gval = Ainv + BW * BW;                // per-block pivot candidates
+    T* grows = gval + kMaxPivotBlocks;       // the two exchanged pivot rows
+    int* gidx = perm + n;                    // perm has n + kMaxPivotBlocks ints
+    cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const dim3 ugrid((n + 63) / 64, (n + 63) / 64);
+    for (int k0 = 0; k0 < n; k0 += BW) {
+        const int bw = std::min(BW, n - k0);
+        const int rows = n - k0;
+        const int nblk = std::max(1, std::min(kMaxPivotBlocks, (rows + 31) / 32));
+        int rpb = (rows + nblk - 1) / nblk;
+        size_t smem = (size_t)rpb * BW * sizeof(T);
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute((const void*)k_panel_pivots<T, BW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        int kk0 = k0, kbw = bw, kn = n;
+        const T* cA = A;
+        void* args[] = {&cA, &kn, &kk0, &kbw, &rpb, &perm, &d_status, &gval, &gidx, &grows};
+        e = cudaLaunchCooperativeKernel((const void*)k_panel_pivots<T, BW>, dim3(nblk), dim3(256),
+                                        args, smem, s);
+        if (e != cudaSuccess) return e;
+        k_apply_swaps<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
+        k_panel_inv<T, BW><<<1, 1024, 0, s>>>(A, n, k0, bw, Ainv, d_status);
+        k_panel_t12<T, BW><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, Ainv, T12, d_status);
+        k_panel_update<T, BW><<<ugrid, 256, 0, s>>>(A, n, k0, bw, T12, d_status);
+        k_panel_finish<T, BW><<<std::max(1, (n + 255) / 256), 256, 0, s>>>(A, n, k0, bw, T12,
+                                                                           Ainv, d_status);
+        *nlaunch += 6;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int status = 0;
+    std::vector<int> hperm(n);
+    e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    if (status) return cudaErrorInvalidValue;  // zero pivot
+    std::vector<int> cols(n);
+    for (int j = 0; j < n; j++) cols[j] = j;
+    for (int k = n - 1; k >= 0; k--) std::swap(cols[k], cols[hperm[k]]);
+    e = cudaMemcpyAsync(perm, cols.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return e;
+    // column permutation with the panel buffers as scratch rows (needs kPermuteBlocks*n <= 2*BW*n)
+    k_permute_cols_t<T><<<std::min(kPermuteBlocks, 2 * BW), 256, 0, s>>>(A, n, perm, W);
+    *nlaunch += 1;
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e;
+}
+
+}  // namespace
+
+size_t inverse_scratch_elems(int n) {
+    return (size_t)2 * 64 * n + 64 * 64 + kMaxPivotBlocks + 2 * 64;
+}
+
+cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
+                       long long* nlaunch, cudaStream_t s) {
+    return invert_blocked<double, 16>(A, n, perm, d_status, scratch, nlaunch, s);
+}
+
+cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
+                       float* scratch, long long* nlaunch, cudaStream_t s) {
+    k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
+    *nlaunch += 1;
+    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, s);
+}
+
+}  // namespace tdbem

@@ -11,8 +11,7 @@
 // stored level with its combined vector computes the whole right-hand side:
 //     rhs = sum_f (G^f W_t[f] - H^f W_u[f]).
 // The solve uses the inverse of the column-exchanged LHS (ExchangeColumns,
-// SolverT.cpp:265-342), computed once per distinct LHS by Gauss-Jordan
-// elimination with partial pivoting in FP64.
+// SolverT.cpp:265-342), computed once per distinct LHS (inverse.cu).
 #include <algorithm>
 
 #include "tdbem_internal.cuh"
@@ -39,83 +38,6 @@ __global__ void k_build_lhs(const double* __restrict__ G, const double* __restri
         const double gc = c0 * g0 + c1 * g1;
         const double hc = c0 * h0 + c1 * h1;
         A[idx] = is_ubc[j] ? -1 * gc : hc;
-    }
-}
-
-// Gauss-Jordan, column k, part 1 (one block): pivot search (largest |A[i][k]|,
-// i >= k, first index on ties), row swap, and the pivot row / column copies.
-__global__ void __launch_bounds__(1024) k_gje_pivot(double* __restrict__ A, int n, int k,
-                                                    int* __restrict__ perm,
-                                                    double* __restrict__ colk,
-                                                    double* __restrict__ rowk,
-                                                    int* __restrict__ status) {
-    __shared__ double sv[1024];
-    __shared__ int si[1024];
-    double best = -1.0;
-    int bi = n;
-    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-        const double v = fabs(A[(size_t)i * n + k]);
-        if (v > best) { best = v; bi = i; }
-    }
-    sv[threadIdx.x] = best;
-    si[threadIdx.x] = bi;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            const double v2 = sv[threadIdx.x + s];
-            const int i2 = si[threadIdx.x + s];
-            if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
-                sv[threadIdx.x] = v2;
-                si[threadIdx.x] = i2;
-            }
-        }
-        __syncthreads();
-    }
-    const int p = si[0];
-    if (p >= n || sv[0] == 0.0) {
-        if (threadIdx.x == 0) *status = 1;
-        return;
-    }
-    if (threadIdx.x == 0) perm[k] = p;
-    if (p != k)
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            const double t = A[(size_t)k * n + j];
-            A[(size_t)k * n + j] = A[(size_t)p * n + j];
-            A[(size_t)p * n + j] = t;
-        }
-    __syncthreads();
-    const double inv = 1.0 / A[(size_t)k * n + k];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        colk[i] = A[(size_t)i * n + k];
-        rowk[i] = (i == k ? 1.0 : A[(size_t)k * n + i]) * inv;
-    }
-}
-
-// Gauss-Jordan, column k, part 2: rank-1 update of every row.
-__global__ void k_gje_update(double* __restrict__ A, int n, int k,
-                             const double* __restrict__ colk, const double* __restrict__ rowk,
-                             const int* __restrict__ status) {
-    if (*status) return;
-    const size_t total = (size_t)n * n;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / n), j = (int)(idx % n);
-        if (i == k) A[idx] = rowk[j];
-        else A[idx] = (j == k ? 0.0 : A[idx]) - colk[i] * rowk[j];
-    }
-}
-
-// Final column permutation of the in-place Gauss-Jordan inverse: row i of the
-// result is row i of A with columns taken from cols[].
-__global__ void k_permute_cols(double* __restrict__ A, int n, const int* __restrict__ cols,
-                               double* __restrict__ tmp) {
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-        double* row = A + (size_t)i * n;
-        double* t = tmp + (size_t)blockIdx.x * n;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) t[j] = row[cols[j]];
-        __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) row[j] = t[j];
-        __syncthreads();
     }
 }
 
@@ -267,36 +189,6 @@ cudaError_t launch_build_lhs(const double* G, const double* H, const float* Gf,
                              cudaStream_t s) {
     k_build_lhs<<<1216, 256, 0, s>>>(G, H, Gf, Hf, level_stride, D, c0, c1, is_ubc, A);
     return cudaGetLastError();
-}
-
-cudaError_t gje_invert(double* A, int n, int* perm, double* colk, double* rowk, int* d_status,
-                       double* tmp_rows, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    for (int k = 0; k < n; k++) {
-        k_gje_pivot<<<1, 1024, 0, s>>>(A, n, k, perm, colk, rowk, d_status);
-        k_gje_update<<<2432, 256, 0, s>>>(A, n, k, colk, rowk, d_status);
-    }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    int status = 0;
-    std::vector<int> hperm(n);
-    e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
-    if (status) return cudaErrorInvalidValue;  // singular: reported by the caller
-    std::vector<int> cols(n);
-    for (int j = 0; j < n; j++) cols[j] = j;
-    for (int k = n - 1; k >= 0; k--) std::swap(cols[k], cols[hperm[k]]);
-    // reuse perm as the column map and colk.. as scratch rows (n doubles per block)
-    e = cudaMemcpyAsync(perm, cols.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
-    k_permute_cols<<<kPermuteBlocks, 256, 0, s>>>(A, n, perm, tmp_rows);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return e;
 }
 
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,

@@ -212,85 +212,6 @@ __global__ void __launch_bounds__(256) k_residual_f64(const double* __restrict__
     if (lane == 0) r[row] = b[row] - acc;
 }
 
-__global__ void k_f64_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * blockDim.x)
-        b[i] = (float)a[i];
-}
-
-// Gauss-Jordan with partial pivoting in FP32 (same structure as the FP64 one).
-__global__ void __launch_bounds__(1024) k_gje_pivot_f32(float* __restrict__ A, int n, int k,
-                                                        int* __restrict__ perm,
-                                                        float* __restrict__ colk,
-                                                        float* __restrict__ rowk,
-                                                        int* __restrict__ status) {
-    __shared__ float sv[1024];
-    __shared__ int si[1024];
-    float best = -1.f;
-    int bi = n;
-    for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-        const float v = fabsf(A[(size_t)i * n + k]);
-        if (v > best) { best = v; bi = i; }
-    }
-    sv[threadIdx.x] = best;
-    si[threadIdx.x] = bi;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            const float v2 = sv[threadIdx.x + s];
-            const int i2 = si[threadIdx.x + s];
-            if (v2 > sv[threadIdx.x] || (v2 == sv[threadIdx.x] && i2 < si[threadIdx.x])) {
-                sv[threadIdx.x] = v2;
-                si[threadIdx.x] = i2;
-            }
-        }
-        __syncthreads();
-    }
-    const int p = si[0];
-    if (p >= n || sv[0] == 0.f) {
-        if (threadIdx.x == 0) *status = 1;
-        return;
-    }
-    if (threadIdx.x == 0) perm[k] = p;
-    if (p != k)
-        for (int j = threadIdx.x; j < n; j += blockDim.x) {
-            const float t = A[(size_t)k * n + j];
-            A[(size_t)k * n + j] = A[(size_t)p * n + j];
-            A[(size_t)p * n + j] = t;
-        }
-    __syncthreads();
-    const float inv = 1.f / A[(size_t)k * n + k];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        colk[i] = A[(size_t)i * n + k];
-        rowk[i] = (i == k ? 1.f : A[(size_t)k * n + i]) * inv;
-    }
-}
-
-__global__ void k_gje_update_f32(float* __restrict__ A, int n, int k,
-                                 const float* __restrict__ colk, const float* __restrict__ rowk,
-                                 const int* __restrict__ status) {
-    if (*status) return;
-    const size_t total = (size_t)n * n;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(idx / n), j = (int)(idx % n);
-        if (i == k) A[idx] = rowk[j];
-        else A[idx] = (j == k ? 0.f : A[idx]) - colk[i] * rowk[j];
-    }
-}
-
-__global__ void k_permute_cols_f32(float* __restrict__ A, int n, const int* __restrict__ cols,
-                                   float* __restrict__ tmp) {
-    for (int i = blockIdx.x; i < n; i += gridDim.x) {
-        float* row = A + (size_t)i * n;
-        float* t = tmp + (size_t)blockIdx.x * n;
-        for (int j = threadIdx.x; j < n; j += blockDim.x) t[j] = row[cols[j]];
-        __syncthreads();
-        for (int j = threadIdx.x; j < n; j += blockDim.x) row[j] = t[j];
-        __syncthreads();
-    }
-}
-
 __global__ void k_add(double* __restrict__ x, const double* __restrict__ d, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] += d[i];
@@ -363,36 +284,6 @@ cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, con
         k_add<<<(D + 255) / 256, 256, 0, s>>>(x, dx, D);
     }
     return cudaGetLastError();
-}
-
-cudaError_t gje_invert_f32(const double* A64, float* A, int n, int* perm, float* colk,
-                           float* rowk, int* d_status, float* tmp_rows, cudaStream_t s) {
-    k_f64_to_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
-    cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
-    if (e != cudaSuccess) return e;
-    for (int k = 0; k < n; k++) {
-        k_gje_pivot_f32<<<1, 1024, 0, s>>>(A, n, k, perm, colk, rowk, d_status);
-        k_gje_update_f32<<<2432, 256, 0, s>>>(A, n, k, colk, rowk, d_status);
-    }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    int status = 0;
-    std::vector<int> hperm(n);
-    e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return e;
-    if (status) return cudaErrorInvalidValue;
-    std::vector<int> cols(n);
-    for (int j = 0; j < n; j++) cols[j] = j;
-    for (int k = n - 1; k >= 0; k--) std::swap(cols[k], cols[hperm[k]]);
-    e = cudaMemcpyAsync(perm, cols.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return e;
-    k_permute_cols_f32<<<kPermuteBlocks, 256, 0, s>>>(A, n, perm, tmp_rows);
-    e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    return e;
 }
 
 }  // namespace tdbem

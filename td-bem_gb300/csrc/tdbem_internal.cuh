@@ -95,9 +95,15 @@ cudaError_t launch_build_lhs(const double* G, const double* H, const float* Gf,
                              const float* Hf, size_t level_stride, int D, double c0,
                              double c1, const unsigned char* is_ubc, double* A,
                              cudaStream_t s);
-constexpr int kPermuteBlocks = 152;  // scratch rows the final GJE column permutation uses
-cudaError_t gje_invert(double* A, int n, int* perm, double* colk, double* rowk,
-                       int* d_status, double* tmp_rows, cudaStream_t s);
+constexpr int kPermuteBlocks = 152;  // scratch rows the final column permutation may use
+// Blocked Gauss-Jordan inverse (inverse.cu); scratch holds inverse_scratch_elems(n)
+// elements, perm has n + kMaxPivotBlocks ints.
+constexpr int kMaxPivotBlocks = 128;
+size_t inverse_scratch_elems(int n);
+cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
+                       long long* nlaunch, cudaStream_t s);
+cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
+                       float* scratch, long long* nlaunch, cudaStream_t s);
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
                                    int L, double a1, double a2, double a3, double c0,
                                    double c1, double amp, const double* load_t,
@@ -131,8 +137,6 @@ cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D
                                const double* add, double* out, cudaStream_t s);
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
                                double* x, double* r, double* dx, int n_refine, cudaStream_t s);
-cudaError_t gje_invert_f32(const double* A64, float* A, int n, int* perm, float* colk,
-                           float* rowk, int* d_status, float* tmp_rows, cudaStream_t s);
 
 }  // namespace tdbem
 
@@ -184,9 +188,7 @@ struct tdbem_ctx {
     double* d_pmix = nullptr;       // conv partials, chunks x nb x D
     double* d_res = nullptr;
     double* d_dx = nullptr;
-    float* d_colk32 = nullptr;
-    float* d_rowk32 = nullptr;
-    float* d_tmp32 = nullptr;
+
     // boundary conditions and marching parameters
     std::vector<int> ubc, fbc;
     std::vector<double> ubc_v, fbc_v;
@@ -201,7 +203,8 @@ struct tdbem_ctx {
     double* d_fbc_map = nullptr;     // per-dof traction value
     unsigned char* d_is_ubc = nullptr;
     unsigned char* d_is_fbc = nullptr;
-    double* d_tmp_rows = nullptr;
+    double* d_inv_scratch = nullptr;  // blocked inverse scratch (FP64)
+    float* d_inv_scratch32 = nullptr;
     double* d_load_t = nullptr;
     double* d_load_u = nullptr;
     double* d_Wt = nullptr;
@@ -210,8 +213,6 @@ struct tdbem_ctx {
     double* d_rhs = nullptr;
     double* d_x = nullptr;
     int* d_perm = nullptr;
-    double* d_colk = nullptr;
-    double* d_rowk = nullptr;
     int* d_status = nullptr;
     size_t partial_cap = 0;
     double timings[3] = {0, 0, 0};
