@@ -141,6 +141,31 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def measure_fp_peaks(torch):
+    """FP64 and FP32 (no TF32) GEMM throughput on this GPU, TFLOP/s, via cuBLAS (best of 3)."""
+    out = {}
+    for name, dt, n in (("fp64_tflops", torch.float64, 4096), ("fp32_tflops", torch.float32, 8192)):
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        a = torch.randn(n, n, dtype=dt, device="cuda")
+        b = torch.randn(n, n, dtype=dt, device="cuda")
+        torch.mm(a, b)
+        best = 0.0
+        for _ in range(3):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.mm(a, b)
+            e1.record()
+            e1.synchronize()
+            best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+        torch.backends.cuda.matmul.allow_tf32 = prev
+        out[name] = best
+        del a, b
+    torch.cuda.empty_cache()
+    return out
+
+
 def ncu_traffic():
     """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary."""
     try:
@@ -350,21 +375,28 @@ def run_ours(args, dist):
     if dist.rank != 0:
         return 0
     peaks, peak_kind = measured_peaks()
+    peaks.update(measure_fp_peaks(torch))
     traffic = ncu_traffic()
     dom = max(stats, key=lambda k: stats[k]["ms"])
     st = stats[dom]
-    if dom == "conv":
+    if dom in ("conv", "conv_block"):
         achieved = st["bytes"] / (st["ms"] / 1e3) / 1e9
-        roof = {"bound": "hbm", "kernel": "k_conv", "achieved": achieved,
+        kname = {"conv": "k_conv" if prec == lib.FP64 else "k_conv_f32<1>",
+                 "conv_block": "k_conv_f32<NB>"}[dom]
+        roof = {"bound": "hbm", "kernel": kname, "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "peak_source": f"hbm_gbs of {peak_kind}"}
     else:
         achieved = st["flops"] / (st["ms"] / 1e3) / 1e12
-        fp64 = peaks.get("fp64_tflops")
-        roof = {"bound": "fp64" if prec == lib.FP64 else "fp32", "kernel": "k_assemble_items",
+        key = "fp32_tflops" if dom == "assemble_f32" or prec != lib.FP64 and dom == "factor" \
+            else "fp64_tflops"
+        fp64 = peaks.get(key)
+        roof = {"bound": "fp32" if key == "fp32_tflops" else "fp64",
+                "kernel": {"assemble": "k_assemble_items", "assemble_f32": "k_assemble_far_f32",
+                           "factor": "blocked Gauss-Jordan", "solve": "solve"}.get(dom, dom),
                 "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                 "frac": (achieved / fp64) if fp64 else None,
-                "peak_source": "fp64_tflops of measured" if fp64 else "no measured FP64 peak"}
+                "peak_source": f"{key}: cuBLAS GEMM measured in this run"}
     roof["launches"] = st["launches"]
     roof["avg_launch_ms"] = st["ms"] / max(1, st["launches"])
     t = traffic.get(f"{args.workload}:{args.precision}:{dom}")
@@ -384,9 +416,12 @@ def run_ours(args, dist):
             "roofline": roof,
             "phases_ms": phase,
             "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
-                            "share": v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values()))}
-                        for k, v in stats.items()},
-            "clocks": clk}
+                            "share": v["ms"] / max(1e-9, sum(x["ms"] for x in stats.values())),
+                            "GB/s": v["bytes"] / max(1e-9, v["ms"]) / 1e6,
+                            "TFLOP/s": v["flops"] / max(1e-9, v["ms"]) / 1e9}
+                        for k, v in stats.items() if v["launches"]},
+            "clocks": clk,
+            "peaks_used": {k: peaks.get(k) for k in ("hbm_gbs", "fp64_tflops", "fp32_tflops")}}
     if compare:
         line["vs_plain_fp64"] = compare
     if dist.world == 1 and not args.no_cpu_baseline:

@@ -155,11 +155,14 @@ int tdbem_last_timings(const tdbem_ctx* ctx, double* ms3);
 /* ---- profiling ------------------------------------------------------ */
 
 /* Kernel classes for tdbem_kernel_stats. */
-#define TDBEM_K_ASSEMBLE 0 /* level quadrature items (FP64 or FP32 pipe)      */
-#define TDBEM_K_CONV 1     /* history convolution over the stored levels (HBM) */
-#define TDBEM_K_FACTOR 2   /* H^0 inverse (Gauss-Jordan)                       */
-#define TDBEM_K_SOLVE 3    /* per-step solve and state update                  */
-#define TDBEM_K_COUNT 4
+#define TDBEM_K_ASSEMBLE 0     /* FP64 level quadrature items (all pairs, or near pairs) */
+#define TDBEM_K_CONV 1         /* per-step history convolution (HBM)                 */
+#define TDBEM_K_FACTOR 2       /* H^0 inverse (Gauss-Jordan)                         */
+#define TDBEM_K_SOLVE 3        /* per-step solve and state update                    */
+#define TDBEM_K_ASSEMBLE_F32 4 /* FP32 far-field quadrature items (mixed)            */
+#define TDBEM_K_CONV_BLOCK 5   /* time-block history convolution, NB columns (mixed) */
+#define TDBEM_K_AUX 6          /* window/scan, C term, LHS build, W vectors          */
+#define TDBEM_K_COUNT 7
 
 /* With on != 0, every launch of the kernel classes above is bracketed by CUDA
  * events on the context stream and its algorithmic bytes / flops are counted

@@ -254,7 +254,8 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
 
 __global__ void k_gauss_geom(const double* __restrict__ coords, const int* __restrict__ ien,
                              int nel, int nq, const double* __restrict__ gx,
-                             const double* __restrict__ gw, double* __restrict__ geom) {
+                             const double* __restrict__ gw, double* __restrict__ geom,
+                             float* __restrict__ geomf) {
     const int nq2 = nq * nq;
     const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (gid >= (long long)nel * nq2) return;
@@ -281,6 +282,50 @@ __global__ void k_gauss_geom(const double* __restrict__ coords, const int* __res
     g[9] = N[2];
     g[10] = N[3];
     g[11] = 0;
+    // FP32 copy for the far-field kernel: the point relative to the element's first
+    // node (small numbers, so FP32 differences to the collocation point stay
+    // accurate), the unit normal, w J and N.
+    float* gf = geomf + gid * kGeomStride;
+    gf[0] = (float)(x[0] - c[0]);
+    gf[1] = (float)(x[1] - c[1]);
+    gf[2] = (float)(x[2] - c[2]);
+    gf[3] = (float)n[0];
+    gf[4] = (float)n[1];
+    gf[5] = (float)n[2];
+    gf[6] = (float)g[6];
+    gf[7] = (float)N[0];
+    gf[8] = (float)N[1];
+    gf[9] = (float)N[2];
+    gf[10] = (float)N[3];
+    gf[11] = 0.f;
+}
+
+// Last pair p in [lo, hi] with offsets[p] <= gid (the pair owning item gid).
+__device__ __forceinline__ unsigned find_pair(const unsigned* __restrict__ offsets, unsigned lo,
+                                              unsigned hi, unsigned gid) {
+    while (lo < hi) {
+        const unsigned mid = (lo + hi + 1) >> 1;
+        if (__ldg(offsets + mid) <= gid) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The pair of this thread's item: one full search per block for its first and
+// last items, then a short search inside that range.  Call with all threads of
+// the block (it synchronises); returns false for threads past the last item.
+__device__ __forceinline__ bool item_pair(const unsigned* __restrict__ offsets, unsigned npairs,
+                                          unsigned nitems, unsigned& p) {
+    __shared__ unsigned s_lo, s_hi;
+    const unsigned first = blockIdx.x * blockDim.x;
+    const unsigned last = min(first + blockDim.x, nitems) - 1;
+    if (threadIdx.x == 0) s_lo = find_pair(offsets, 0, npairs - 1, first);
+    if (threadIdx.x == 32) s_hi = find_pair(offsets, 0, npairs - 1, last);
+    __syncthreads();
+    const unsigned gid = first + threadIdx.x;
+    if (gid >= nitems) return false;
+    p = find_pair(offsets, s_lo, s_hi, gid);
+    return true;
 }
 
 // Singular test of ElastoDynamicsT::G_H_Driver (ElastoDynamicsT.cpp:166-175):
@@ -325,16 +370,19 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
     const double margin = 1e-3 * rad + 1e-12;
     const double rmin = fmax(0.0, dist - rad - margin), rmax = dist + rad + margin;
     const int sing = singular_corner(nd, xc);
-    // the step response at time n dt can be non-zero only for n_lo <= n <= n_hi
+    // The step response at time n dt is exactly zero unless r/c_p <= n dt and
+    // n < r/(c_s dt) + 2; level k takes n = k (I part) and n = k + 1 (J part), so it
+    // can be non-zero only for r_min/(c_p dt) - 1 <= k < r_max/(c_s dt) + 1 (one level
+    // of margin on the low side for rounding).
     int n_lo = (int)floor(rmin * ph.inv_cp * ph.inv_dt) - 1;
-    const int n_hi = (int)ceil(rmax * ph.inv_cs * ph.inv_dt) + 3;
+    const int n_hi = (int)ceil(rmax * ph.inv_cs * ph.inv_dt) + 2;
     if (sing >= 0) n_lo = 0;
     PairInfo pi;
     pi.sing = sing;
     if (mode == ASM_LEVELS) {
-        // level k takes n = k (I part) and n = k + 1 (J part)
-        const int klo = max(0, n_lo - 1);
-        const int khi = min(min(level_last, n_hi), level_cap);
+        const int klo = max(0, n_lo);
+        const int khi = min(min(level_last, (int)ceil(rmax * ph.inv_cs * ph.inv_dt) + 1),
+                            level_cap);
         pi.klo = klo;
         pi.cnt = max(0, khi - klo + 1);
     } else {
@@ -358,16 +406,9 @@ __global__ void __launch_bounds__(128) k_assemble_items(
     const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
     int step_n, int part, const PairInfo* __restrict__ pairs,
     const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
+    unsigned p;
+    if (!item_pair(offsets, npairs, nitems, p)) return;
     const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= nitems) return;
-    // the pair owning this item: last p with offsets[p] <= gid
-    unsigned lo = 0, hi = npairs - 1;
-    while (lo < hi) {
-        const unsigned mid = (lo + hi + 1) >> 1;
-        if (__ldg(offsets + mid) <= gid) lo = mid;
-        else hi = mid - 1;
-    }
-    const unsigned p = lo;
     const PairInfo pi = pairs[p];
     const int k = pi.klo + (int)(gid - __ldg(offsets + p));
     const int c = node_lo + (int)(p / ne);
@@ -496,10 +537,9 @@ __device__ __forceinline__ PhysF to_f(const Phys& p) {
 // One wave at local time tau: F_I = rho Q1 + Q0, I3, I5 and F_J = rho R1 + R0, J3, J5.
 __device__ __forceinline__ void wave_tau_I(float tau, float rho, const PhysF& f, float& FI,
                                            float& I3, float& I5) {
-    float b, x5;
-    if (f.dt <= tau) { b = f.dt; x5 = 0.f; }
-    else if (0.f <= tau) { b = tau; x5 = (f.dt - tau) * f.inv_dt; }
-    else { b = 0.f; x5 = 0.f; }
+    // b = clamp(tau, 0, dt); the I5 term lives on 0 <= tau < dt (GreenFunctionT.cpp:251-269)
+    const float b = fminf(fmaxf(tau, 0.f), f.dt);
+    const float x5 = (tau >= 0.f && tau < f.dt) ? (f.dt - tau) * f.inv_dt : 0.f;
     const float b2 = b * b;
     const float q1 = b * (8.f * b2 - 12.f * tau * b - 12.f * f.dt * b + 24.f * f.dt * tau);
     const float q0 = b * (b2 * (-3.f * b + 8.f * tau + 4.f * f.dt) - 6.f * tau * tau * b -
@@ -511,10 +551,8 @@ __device__ __forceinline__ void wave_tau_I(float tau, float rho, const PhysF& f,
 
 __device__ __forceinline__ void wave_tau_J(float tau, float rho, const PhysF& f, float& FJ,
                                            float& J3, float& J5) {
-    float b, x5;
-    if (f.dt <= tau) { b = f.dt; x5 = 0.f; }
-    else if (0.f <= tau) { b = tau; x5 = tau * f.inv_dt; }
-    else { b = 0.f; x5 = 0.f; }
+    const float b = fminf(fmaxf(tau, 0.f), f.dt);
+    const float x5 = (tau >= 0.f && tau < f.dt) ? tau * f.inv_dt : 0.f;
     const float b2 = b * b;
     const float r1 = b2 * (-8.f * b + 12.f * tau);
     const float r0 = b2 * (3.f * b2 - 8.f * tau * b + 6.f * tau * tau);
@@ -605,32 +643,29 @@ __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool d
 }
 
 // Far (well-separated, non-singular) items in FP32, ASM_LEVELS placement into the
-// FP32 level store.  The Gauss-point geometry is read from the FP64 table and
-// rounded; coordinates are shifted to the collocation point in FP64 first.
+// FP32 level store.  Gauss-point geometry comes from the FP32 table (points
+// relative to the element's first node); no FP64 arithmetic or conversion in the
+// point loop, which on GB300 would run on the narrow FP64 pipe.
 __global__ void __launch_bounds__(256) k_assemble_far_f32(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq2,
-    const double* __restrict__ geom, Phys ph, int level_last,
+    const float* __restrict__ geomf, Phys ph, int level_last,
     const PairInfo* __restrict__ pairs, const unsigned* __restrict__ offsets, unsigned npairs,
     unsigned nitems, AsmOut out) {
+    unsigned p;
+    if (!item_pair(offsets, npairs, nitems, p)) return;
     const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gid >= nitems) return;
-    unsigned lo = 0, hi = npairs - 1;
-    while (lo < hi) {
-        const unsigned mid = (lo + hi + 1) >> 1;
-        if (__ldg(offsets + mid) <= gid) lo = mid;
-        else hi = mid - 1;
-    }
-    const unsigned p = lo;
     const PairInfo pi = pairs[p];
     const int k = pi.klo + (int)(gid - __ldg(offsets + p));
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
-    const double xcd[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
-    const float zero3[3] = {0.f, 0.f, 0.f};
     int nid[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
+    // collocation point relative to the element's first node, rounded once
+    const float xc[3] = {(float)(coords[c * 3] - coords[nid[0] * 3]),
+                         (float)(coords[c * 3 + 1] - coords[nid[0] * 3 + 1]),
+                         (float)(coords[c * 3 + 2] - coords[nid[0] * 3 + 2])};
     const PhysF f = to_f(ph);
     const bool doI = (k >= 1), doJ = (k + 1 <= level_last);
     const float TI = (float)(k * ph.dt);
@@ -642,14 +677,13 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
 #pragma unroll
         for (int m = 0; m < 9; m++) acc.h[a][m] = 0.f;
     }
-    const double* g = geom + (size_t)e * nq2 * kGeomStride;
-    for (int q = 0; q < nq2; q++, g += kGeomStride) {
-        const float xq[3] = {(float)(__ldg(g) - xcd[0]), (float)(__ldg(g + 1) - xcd[1]),
-                             (float)(__ldg(g + 2) - xcd[2])};
-        const float nqv[3] = {(float)__ldg(g + 3), (float)__ldg(g + 4), (float)__ldg(g + 5)};
-        const float N[4] = {(float)__ldg(g + 7), (float)__ldg(g + 8), (float)__ldg(g + 9),
-                            (float)__ldg(g + 10)};
-        gauss_point_f32(acc, doI, doJ, TI, f, zero3, xq, nqv, (float)__ldg(g + 6), N);
+    const float4* g4 = reinterpret_cast<const float4*>(geomf + (size_t)e * nq2 * kGeomStride);
+    for (int q = 0; q < nq2; q++) {
+        const float4 p0 = __ldg(g4 + 3 * q), p1 = __ldg(g4 + 3 * q + 1), p2 = __ldg(g4 + 3 * q + 2);
+        const float xq[3] = {p0.x, p0.y, p0.z};
+        const float nqv[3] = {p0.w, p1.x, p1.y};
+        const float N[4] = {p1.w, p2.x, p2.y, p2.z};
+        gauss_point_f32(acc, doI, doJ, TI, f, xc, xq, nqv, p1.z, N);
     }
     const size_t D = (size_t)out.ld;
     const size_t rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
@@ -668,22 +702,22 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
 
 // C term (TDElementStepLinearT.cpp:103-109, 501-508, 577-584 with AssembleC,
 // ElastoDynamicsT.cpp:261-280): C_c = -sum_e sum_q wJ DT_Kelvin(q)^T over the whole
-// surface, added to the diagonal block of the first step's I and J parts, plus the
-// exterior free term 0.5 dt I (ElastoDynamicsT.cpp:212-225).  One block per node,
-// fixed-order tree reduction.
-__global__ void __launch_bounds__(128) k_cterm(const double* __restrict__ coords,
+// surface, with the reference's regular / Duffy quadrature per element.  One
+// block per node, fixed-order tree reduction; the result goes to cbuf[c][9].
+__global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords,
                                                const int* __restrict__ ien, int nel,
                                                int node_lo, int nq,
                                                const double* __restrict__ gx,
                                                const double* __restrict__ gw,
                                                const double* __restrict__ geom, Phys ph,
-                                               int if_ext, int mode, AsmOut out) {
+                                               double* __restrict__ cbuf) {
     const int c = node_lo + blockIdx.x;
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int nq2 = nq * nq;
-    const double div0 = -(8 * M_PI) * (1 - ph.nu);
     const double onem2nu = 1 - 2 * ph.nu;
+    // Kelvin_Linear (GreenFunctionT.cpp:205-231): K = [..] / (-8 pi (1-nu) r^2) * 0.5 dt
+    const double kscale = (0.5 * ph.dt) / (-(8 * M_PI) * (1 - ph.nu));
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
         double cn[12];
         for (int a = 0; a < 4; a++) {
@@ -705,58 +739,68 @@ __global__ void __launch_bounds__(128) k_cterm(const double* __restrict__ coords
                 duffy_point(cn, sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
             }
             const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
-            const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-            const double rv[3] = {d0 / r, d1 / r, d2 / r};
+            const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+            const double inv_r = 1.0 / sqrt(r2);
+            const double rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
             const double rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
-            // Kelvin_Linear (GreenFunctionT.cpp:205-231), K[i][k]; C[i][k] -= wJ K[k][i]
-            const double scale = (0.5 * ph.dt) / (div0 * r * r);
+            const double w = wJ * (kscale * inv_r * inv_r);
+            // C[i][k] -= wJ K[k][i]
+#pragma unroll
             for (int i = 0; i < 3; i++)
+#pragma unroll
                 for (int kk = 0; kk < 3; kk++) {
                     const double Kki = ((kk == i ? onem2nu : 0.0) + 3 * rv[kk] * rv[i]) * rdn -
                                        onem2nu * (rv[i] * nv[kk] - rv[kk] * nv[i]);
-                    acc[i * 3 + kk] -= wJ * (Kki * scale);
+                    acc[i * 3 + kk] -= w * Kki;
                 }
         }
     }
-    __shared__ double red[9][128];
+    __shared__ double red[9][256];
     for (int m = 0; m < 9; m++) red[m][threadIdx.x] = acc[m];
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int m = 0; m < 9; m++) red[m][threadIdx.x] += red[m][threadIdx.x + s];
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+            for (int m = 0; m < 9; m++) red[m][threadIdx.x] += red[m][threadIdx.x + st];
         __syncthreads();
     }
-    if (threadIdx.x != 0) return;
-    const size_t D = (size_t)out.ld;
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-            const double v = red[i * 3 + j][0] + ((if_ext && i == j) ? 0.5 * ph.dt : 0.0);
-            const size_t off = (size_t)(3 * c + i) * D + 3 * (size_t)c + j;
-            if (mode == ASM_LEVELS) {
-                // level 0 = J(dt), level 1 = I(dt) + J(2dt)
-                if (out.H0f) {
-                    out.H0f[off] += (float)v;
-                    out.H0f[out.level_stride + off] += (float)v;
-                } else {
-                    out.H0[off] += v;
-                    out.H0[out.level_stride + off] += v;
-                }
-            } else {
-                const size_t roff = (size_t)(3 * (c - out.row_node_lo) + i) * D + 3 * (size_t)c + j;
-                out.H0[roff] += v;
-                out.H1[roff] += v;
-            }
+    if (threadIdx.x < 9) cbuf[(size_t)(c - node_lo) * 9 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
+// diagonal blocks of the first step's I and J parts: levels 0 and 1 of a level
+// store, or the H_I / H_J row blocks of a single-step call.
+__global__ void k_cterm_apply(const double* __restrict__ cbuf, int node_lo, int nnodes,
+                              double dt, int if_ext, int mode, AsmOut out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * 9) return;
+    const int cl = t / 9, m = t % 9, i = m / 3, j = m % 3, c = node_lo + cl;
+    const double v = cbuf[t] + ((if_ext && i == j) ? 0.5 * dt : 0.0);
+    const size_t ld = (size_t)out.ld;
+    if (mode == ASM_LEVELS) {
+        const size_t off = (size_t)(3 * c + i) * ld + 3 * (size_t)c + j;
+        if (out.H0f) {
+            out.H0f[off] += (float)v;
+            out.H0f[out.level_stride + off] += (float)v;
+        } else {
+            out.H0[off] += v;
+            out.H0[out.level_stride + off] += v;
         }
+    } else {
+        const size_t roff = (size_t)(3 * cl + i) * ld + 3 * (size_t)c + j;
+        out.H0[roff] += v;
+        out.H1[roff] += v;
+    }
 }
 
 }  // namespace
 
 cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
-                              const double* gx, const double* gw, double* geom,
+                              const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s) {
     const long long n = (long long)nel * nq * nq;
     const int bs = 128;
-    k_gauss_geom<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom);
+    k_gauss_geom<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom,
+                                                               geomf);
     return cudaGetLastError();
 }
 
@@ -775,8 +819,8 @@ cudaError_t launch_pair_window(const double* coords, const int* ien, const int* 
 
 cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
                                   int nelem_color, int node_lo, int nq, const double* gx,
-                                  const double* gw, const double* geom, const Phys& ph,
-                                  int mode, int level_last, int step_n,
+                                  const double* gw, const double* geom, const float* geomf,
+                                  const Phys& ph, int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
                                   int fp32_far, cudaStream_t s) {
@@ -785,7 +829,7 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, const in
     const unsigned grid = (nitems + bs - 1) / bs;
     if (fp32_far) {
         k_assemble_far_f32<<<(nitems + 255) / 256, 256, 0, s>>>(
-            coords, ien, elems, nelem_color, node_lo, nq * nq, geom, ph, level_last, pairs,
+            coords, ien, elems, nelem_color, node_lo, nq * nq, geomf, ph, level_last, pairs,
             offsets, npairs, nitems, out);
     } else if (mode == ASM_LEVELS) {
         k_assemble_items<ASM_LEVELS><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
@@ -804,11 +848,17 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, const in
 
 cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
-                         const double* geom, const Phys& ph, int if_ext, int mode,
-                         int /*step_n*/, const AsmOut& out, cudaStream_t s) {
+                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s) {
     if (nnodes == 0) return cudaSuccess;
-    k_cterm<<<nnodes, 128, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, if_ext,
-                                   mode, out);
+    k_cterm<<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
+                               int if_ext, int mode, const AsmOut& out, cudaStream_t s) {
+    if (nnodes == 0) return cudaSuccess;
+    k_cterm_apply<<<(nnodes * 9 + 255) / 256, 256, 0, s>>>(cbuf, node_lo, nnodes, dt, if_ext,
+                                                             mode, out);
     return cudaGetLastError();
 }
 

@@ -248,11 +248,13 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
     for (int n0 = node_lo; n0 < node_lo + nnodes; n0 += chunk) {
         const int nn = std::min(chunk, node_lo + nnodes - n0);
         const unsigned npairs = (unsigned)((long long)nn * ne);
+        const int pw = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, elems, ne, n0, nn, c->ph, mode,
                                     level_last, level_cap, step_n, select, c->d_pairs,
                                     c->d_counts, c->stream));
         CUDA_TRY(exclusive_scan(c->d_counts, c->d_offsets, npairs, c->d_scan_tmp,
                                 c->scan_tmp_bytes, c->stream));
+        prof_end(c, pw, 0, 0);
         c->launches += 3;  // window + the scan's init and scan kernels
         unsigned last[2];
         CUDA_TRY(cudaMemcpyAsync(&last[0], c->d_offsets + npairs - 1, sizeof(unsigned),
@@ -261,9 +263,10 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
                                  cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         const unsigned nitems = last[0] + last[1];
-        const int pe = prof_begin(c, TDBEM_K_ASSEMBLE);
+        const int pe = prof_begin(c, fp32_far ? TDBEM_K_ASSEMBLE_F32 : TDBEM_K_ASSEMBLE);
         CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, elems, ne, n0, c->nq, c->d_gx,
-                                       c->d_gw, c->d_geom, c->ph, mode, level_last, step_n,
+                                       c->d_gw, c->d_geom, c->d_geomf, c->ph, mode, level_last,
+                                       step_n,
                                        c->d_pairs, c->d_offsets, npairs, nitems, out, fp32_far,
                                        c->stream));
         if (nitems) c->launches += (mode == ASM_STEP ? 2 : 1);
@@ -358,7 +361,7 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, ldw,
                                         c->d_Wt_old, c->d_Wu_old, s));
             const int nch = mixed_chunks(nlev, D);
-            const int pe = prof_begin(c, TDBEM_K_CONV);
+            const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
             CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
                                      c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch, s));
             prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
@@ -488,6 +491,8 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_gx, nq));
     CTX_TRY(dalloc(&c->d_gw, nq));
     CTX_TRY(dalloc(&c->d_geom, (size_t)c->nel * nq * nq * 12));
+    CTX_TRY(dalloc(&c->d_cterm, (size_t)c->nnd * 9));
+    CTX_TRY(dalloc(&c->d_geomf, (size_t)c->nel * nq * nq * 12));
     CTX_TRY(dalloc(&c->d_color_elems, order.size()));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
@@ -500,7 +505,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(cudaMemcpyAsync(c->d_color_elems, order.data(), sizeof(int) * order.size(),
                             cudaMemcpyHostToDevice, c->stream));
     CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, nq, c->d_gx, c->d_gw, c->d_geom,
-                              c->stream));
+                              c->d_geomf, c->stream));
     c->pair_cap = std::min<size_t>((size_t)c->nnd * max_color, (size_t)1 << 26);
     c->pair_cap = std::max<size_t>(c->pair_cap, (size_t)max_color);
     CTX_TRY(dalloc(&c->d_pairs, c->pair_cap));
@@ -524,6 +529,8 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_gx);
     dfree(c->d_gw);
     dfree(c->d_geom);
+    dfree(c->d_cterm);
+    dfree(c->d_geomf);
     dfree(c->d_color_elems);
     dfree(c->d_pairs);
     dfree(c->d_counts);
@@ -601,7 +608,10 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
                             out);
     if (rc == TDBEM_OK && step == 1) {
         e = launch_cterm(c->d_coords, c->d_ien, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
-                         c->d_geom, c->ph, c->if_ext, ASM_STEP, step, out, c->stream);
+                         c->d_geom, c->ph, c->d_cterm, c->stream);
+        if (e == cudaSuccess)
+            e = launch_cterm_apply(c->d_cterm, node_lo, nn, c->dt, c->if_ext, ASM_STEP, out,
+                                   c->stream);
         if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "cterm: %s", cudaGetErrorString(e));
     }
     double* hosts[4] = {G_I, H_I, G_J, H_J};
@@ -657,9 +667,13 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                                           0, out);
             if (rc != TDBEM_OK) return rc;
         }
+        const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, out, c->stream));
-        c->launches += 1;
+                              c->d_geom, c->ph, c->d_cterm, c->stream));
+        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, out,
+                                    c->stream));
+        prof_end(c, pc, 0, 0);
+        c->launches += 2;
     } else {
         // FP32 store for all levels: near pairs with the FP64 quadrature, far pairs with
         // the FP32 tau form; levels 0 and 1 again in FP64 for the LHS of the solve.
@@ -688,11 +702,15 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                 rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, 0, o64);
             if (rc != TDBEM_OK) return rc;
         }
+        const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, o32, c->stream));
-        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                              c->d_geom, c->ph, c->if_ext, ASM_LEVELS, 1, o64, c->stream));
-        c->launches += 2;
+                              c->d_geom, c->ph, c->d_cterm, c->stream));
+        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o32,
+                                    c->stream));
+        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
+                                    c->stream));
+        prof_end(c, pc, 0, 0);
+        c->launches += 3;
     }
     c->timings[0] = tm.stop_ms(c->stream);
     CUDA_TRY(cudaGetLastError());
@@ -796,7 +814,7 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
         CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
         CUDA_TRY(dalloc(&c->d_rhs, D));
         CUDA_TRY(dalloc(&c->d_x, D));
-        CUDA_TRY(dalloc(&c->d_perm, D + kMaxPivotBlocks));
+        CUDA_TRY(dalloc(&c->d_perm, D + 2 * kMaxPivotBlocks));
         CUDA_TRY(dalloc(&c->d_status, 1));
         c->partial_cap = (size_t)(c->M + 1) * D;
         CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
@@ -939,6 +957,7 @@ int tdbem_set_profiling(tdbem_ctx* c, int on) {
         c->prof_launches[k] = 0;
         c->prof_ms[k] = c->prof_bytes[k] = c->prof_flops[k] = 0;
     }
+    (void)0;
     return TDBEM_OK;
 }
 

@@ -30,11 +30,13 @@ __device__ __forceinline__ T absv(T x) { return x < T(0) ? -x : x; }
 
 // Pivot sequence of the panel: LU with partial pivoting of rows k0..n-1 of
 // columns C1, spread over a cooperative grid (all blocks co-resident, so the
-// grid barriers always complete).  Each block keeps `rpb` panel rows in shared
-// memory; per column one barrier publishes the blocks' local maxima (ties to
-// the lowest row), a second one the exchanged pivot rows.
-// Only the pivot rows (perm) are produced: the swapped panel itself is re-read
-// from A by the later steps.
+// grid barrier always completes).  Each block keeps `rpb` panel rows in shared
+// memory.  Per column, each block publishes its best candidate together with
+// that candidate's row (and the owner of row c publishes row c); after one grid
+// barrier every block picks the same pivot (largest magnitude, lowest row on
+// ties), swaps, and updates its own rows.  Publications alternate between two
+// buffers by column parity, so a fast block never overwrites what a slow block
+// still reads.
 template <typename T, int BW>
 __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, int n, int k0,
                                                       int bw, int rpb, int* __restrict__ perm,
@@ -49,7 +51,8 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
     __shared__ T sv[256];
     __shared__ int si[256];
     __shared__ T su[BW];
-    __shared__ int s_p;
+    __shared__ int s_p, s_b;
+    const int nb = gridDim.x;
     const int rows = n - k0;
     const int r0 = blockIdx.x * rpb, r1 = min(rows, r0 + rpb);
     for (int idx = threadIdx.x; idx < rpb * BW; idx += blockDim.x) {
@@ -58,6 +61,10 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
     }
     __syncthreads();
     for (int c = 0; c < bw; c++) {
+        const int par = c & 1;
+        T* cval = gval + par * nb;
+        int* cidx = gidx + par * nb;
+        T* crows = grows + (size_t)par * (nb + 1) * BW;  // nb candidate rows, then row c
         T best = T(-1);
         int bi = rows;
         for (int r = max(r0, c) + threadIdx.x; r < r1; r += blockDim.x) {
@@ -78,20 +85,26 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
             }
             __syncthreads();
         }
+        const int li = si[0];
         if (threadIdx.x == 0) {
-            gval[blockIdx.x] = sv[0];
-            gidx[blockIdx.x] = si[0];
+            cval[blockIdx.x] = sv[0];
+            cidx[blockIdx.x] = li;
+        }
+        if (threadIdx.x < BW) {
+            if (li < r1) crows[(size_t)blockIdx.x * BW + threadIdx.x] = ws[(li - r0) * BW + threadIdx.x];
+            if (c >= r0 && c < r1) crows[(size_t)nb * BW + threadIdx.x] = ws[(c - r0) * BW + threadIdx.x];
         }
         grid.sync();
         if (threadIdx.x == 0) {  // every block reduces the same list in the same order
             T bv = T(-1);
-            int bp = rows;
-            for (int b = 0; b < gridDim.x; b++) {
-                const T v = gval[b];
-                const int i = gidx[b];
-                if (v > bv || (v == bv && i < bp)) { bv = v; bp = i; }
+            int bp = rows, bb = 0;
+            for (int b = 0; b < nb; b++) {
+                const T v = cval[b];
+                const int i = cidx[b];
+                if (v > bv || (v == bv && i < bp)) { bv = v; bp = i; bb = b; }
             }
             s_p = (bp < rows && bv != T(0)) ? bp : -1;
+            s_b = bb;
         }
         __syncthreads();
         const int p = s_p;
@@ -99,14 +112,13 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
             if (blockIdx.x == 0 && threadIdx.x == 0) *status = 1;
             return;
         }
-        // publish rows c and p, then swap them
-        if (c >= r0 && c < r1 && threadIdx.x < BW) grows[threadIdx.x] = ws[(c - r0) * BW + threadIdx.x];
-        if (p >= r0 && p < r1 && threadIdx.x < BW) grows[BW + threadIdx.x] = ws[(p - r0) * BW + threadIdx.x];
-        grid.sync();
-        if (threadIdx.x < BW) su[threadIdx.x] = grows[BW + threadIdx.x];
-        if (c >= r0 && c < r1 && threadIdx.x < BW) ws[(c - r0) * BW + threadIdx.x] = grows[BW + threadIdx.x];
-        if (p != c && p >= r0 && p < r1 && threadIdx.x < BW)
-            ws[(p - r0) * BW + threadIdx.x] = grows[threadIdx.x];
+        if (threadIdx.x < BW) {
+            const T pv = crows[(size_t)s_b * BW + threadIdx.x];  // the pivot row
+            su[threadIdx.x] = pv;
+            if (c >= r0 && c < r1) ws[(c - r0) * BW + threadIdx.x] = pv;
+            if (p != c && p >= r0 && p < r1)
+                ws[(p - r0) * BW + threadIdx.x] = crows[(size_t)nb * BW + threadIdx.x];
+        }
         if (blockIdx.x == 0 && threadIdx.x == 0) perm[k0 + c] = k0 + p;
         __syncthreads();
         const T inv = T(1) / su[c];
@@ -116,8 +128,7 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
             wr[c] = l;
             for (int j = c + 1; j < bw; j++) wr[j] -= l * su[j];
         }
-        // No barrier here: the next column's candidates and published rows are written
-        // only after every block has passed this column's second barrier.
+        __syncthreads();
     }
 }
 
@@ -308,16 +319,16 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
     T* W = scratch;                          // 2*BW*n: permutation scratch rows at the end
     T* T12 = W + (size_t)n * BW;             // BW x n
     T* Ainv = T12 + (size_t)n * BW;          // BW x BW
-    T* gval = Ainv + BW * BW;                // per-block pivot candidates
-    T* grows = gval + kMaxPivotBlocks;       // the two exchanged pivot rows
-    int* gidx = perm + n;                    // perm has n + kMaxPivotBlocks ints
+    T* gval = Ainv + BW * BW;                // per-block pivot candidates, 2 buffers
+    T* grows = gval + 2 * kMaxPivotBlocks;   // candidate rows + row c, 2 buffers
+    int* gidx = perm + n;                    // perm has n + 2*kMaxPivotBlocks ints
     cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     const dim3 ugrid((n + 63) / 64, (n + 63) / 64);
     for (int k0 = 0; k0 < n; k0 += BW) {
         const int bw = std::min(BW, n - k0);
         const int rows = n - k0;
-        const int nblk = std::max(1, std::min(kMaxPivotBlocks, (rows + 31) / 32));
+        const int nblk = std::max(1, std::min(kMaxPivotBlocks, (rows + 63) / 64));
         int rpb = (rows + nblk - 1) / nblk;
         size_t smem = (size_t)rpb * BW * sizeof(T);
         if (smem > 48 * 1024) {
@@ -365,7 +376,7 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
 }  // namespace
 
 size_t inverse_scratch_elems(int n) {
-    return (size_t)2 * 64 * n + 64 * 64 + kMaxPivotBlocks + 2 * 64;
+    return (size_t)2 * 64 * n + 64 * 64 + 2 * kMaxPivotBlocks + 2 * (kMaxPivotBlocks + 1) * 64;
 }
 
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,

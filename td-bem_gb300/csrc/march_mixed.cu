@@ -65,16 +65,21 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
             for (int kk = lane; kk < kKC / 4; kk += 32) {
                 const int k = k0 + 4 * kk;
                 if (k >= ld) break;
+                // all rows' G/H segments first, then each W column once from shared
+                // memory for the 4 rows (one LDS.128 pair per column, not per row)
+                float4 g[kRowsPerWarp], h[kRowsPerWarp];
 #pragma unroll
                 for (int r = 0; r < kRowsPerWarp; r++) {
-                    const float4 g = __ldcs(reinterpret_cast<const float4*>(Gf + rowoff[r] + k));
-                    const float4 h = __ldcs(reinterpret_cast<const float4*>(Hf + rowoff[r] + k));
+                    g[r] = __ldcs(reinterpret_cast<const float4*>(Gf + rowoff[r] + k));
+                    h[r] = __ldcs(reinterpret_cast<const float4*>(Hf + rowoff[r] + k));
+                }
 #pragma unroll
-                    for (int j = 0; j < NB; j++) {
-                        const float4 a = sw[0][j][kk], b = sw[1][j][kk];
-                        acc[r][j] += (g.x * a.x + g.y * a.y + g.z * a.z + g.w * a.w) -
-                                     (h.x * b.x + h.y * b.y + h.z * b.z + h.w * b.w);
-                    }
+                for (int j = 0; j < NB; j++) {
+                    const float4 a = sw[0][j][kk], b = sw[1][j][kk];
+#pragma unroll
+                    for (int r = 0; r < kRowsPerWarp; r++)
+                        acc[r][j] += (g[r].x * a.x + g[r].y * a.y + g[r].z * a.z + g[r].w * a.w) -
+                                     (h[r].x * b.x + h[r].y * b.y + h[r].z * b.z + h[r].w * b.w);
                 }
             }
         }
@@ -182,7 +187,8 @@ __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, i
     out[i] = s;
 }
 
-// y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per row.
+// y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
+// row, pairs of columns per load when D is even.
 __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, int D,
                                                   const double* __restrict__ v,
                                                   double* __restrict__ y, int accumulate) {
@@ -190,7 +196,17 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
     if (row >= D) return;
     const float* a = A + (size_t)row * D;
     float acc = 0.f;
-    for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * (float)v[j];
+    if ((D & 1) == 0) {
+        const float2* a2 = reinterpret_cast<const float2*>(a);
+        const double2* v2 = reinterpret_cast<const double2*>(v);
+        for (int j = lane; j < D / 2; j += 32) {
+            const float2 x = __ldcs(a2 + j);
+            const double2 w = v2[j];
+            acc += x.x * (float)w.x + x.y * (float)w.y;
+        }
+    } else {
+        for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * (float)v[j];
+    }
     double s = acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

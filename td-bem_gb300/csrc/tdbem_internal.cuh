@@ -62,7 +62,7 @@ struct AsmOut {
 
 // Launch helpers (assemble.cu).
 cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
-                              const double* gx, const double* gw, double* geom,
+                              const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s);
 cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
@@ -70,15 +70,16 @@ cudaError_t launch_pair_window(const double* coords, const int* ien, const int* 
                                PairInfo* pairs, unsigned* counts, cudaStream_t s);
 cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
                                   int nelem_color, int node_lo, int nq, const double* gx,
-                                  const double* gw, const double* geom, const Phys& ph,
-                                  int mode, int level_last, int step_n,
+                                  const double* gw, const double* geom, const float* geomf,
+                                  const Phys& ph, int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
                                   int fp32_far, cudaStream_t s);
 cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
-                         const double* geom, const Phys& ph, int if_ext, int mode,
-                         int step_n, const AsmOut& out, cudaStream_t s);
+                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s);
+cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
+                               int if_ext, int mode, const AsmOut& out, cudaStream_t s);
 size_t scan_temp_bytes(unsigned n);
 cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
                            size_t tmp_bytes, cudaStream_t s);
@@ -97,8 +98,8 @@ cudaError_t launch_build_lhs(const double* G, const double* H, const float* Gf,
                              cudaStream_t s);
 constexpr int kPermuteBlocks = 152;  // scratch rows the final column permutation may use
 // Blocked Gauss-Jordan inverse (inverse.cu); scratch holds inverse_scratch_elems(n)
-// elements, perm has n + kMaxPivotBlocks ints.
-constexpr int kMaxPivotBlocks = 128;
+// elements, perm has n + 2 * kMaxPivotBlocks ints.
+constexpr int kMaxPivotBlocks = 32;
 size_t inverse_scratch_elems(int n);
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
                        long long* nlaunch, cudaStream_t s);
@@ -155,6 +156,8 @@ struct tdbem_ctx {
     double* d_gx = nullptr;
     double* d_gw = nullptr;
     double* d_geom = nullptr;        // regular Gauss-point geometry, nel x nq^2 x 12
+    double* d_cterm = nullptr;       // C term of every node, nnd x 9
+    float* d_geomf = nullptr;        // FP32 copy of the geometry (element-relative points)
     // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
     std::vector<int> color_start;
     int* d_color_elems = nullptr;
@@ -225,8 +228,8 @@ struct tdbem_ctx {
     long long launches = 0;          // kernels this context has launched (tdbem_launch_count)
     bool prof = false;
     std::vector<ProfEvent> prof_pending;
-    long long prof_launches[4] = {0, 0, 0, 0};
-    double prof_ms[4] = {0, 0, 0, 0};
-    double prof_bytes[4] = {0, 0, 0, 0};
-    double prof_flops[4] = {0, 0, 0, 0};
+    long long prof_launches[TDBEM_K_COUNT] = {};
+    double prof_ms[TDBEM_K_COUNT] = {};
+    double prof_bytes[TDBEM_K_COUNT] = {};
+    double prof_flops[TDBEM_K_COUNT] = {};
 };

@@ -53,7 +53,8 @@ SIGNATURES = {
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
 }
 
-KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve"}
+KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve", 4: "assemble_f32",
+                  5: "conv_block", 6: "aux"}
 
 
 class Mesh(ctypes.Structure):
