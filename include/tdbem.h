@@ -99,6 +99,24 @@ int tdbem_get_stream(const tdbem_ctx* ctx, void** stream);
 int tdbem_gh_driver(tdbem_ctx* ctx, int step, int node_lo, int node_hi, double* G_I,
                     double* G_J, double* H_I, double* H_J);
 
+/* Allocation-free variant of tdbem_gh_driver for callers that cannot allocate
+ * device memory (applications that reserve all device memory at start-up and
+ * forbid later cudaMalloc/cudaFree, or latency-critical loops that cannot take
+ * their implicit synchronisation).  No counterpart in the reference.  Same
+ * result as tdbem_gh_driver, written into caller-owned DEVICE buffers
+ * (3*(node_hi-node_lo+1) x D doubles each, zeroed by the call), with work
+ * ordered on `stream` (a cudaStream_t; NULL = the context's stream) and not
+ * waited for.  Its kernels' scratch is one fixed 8 MiB array in device memory
+ * that every GPU loading the library holds until exit; meshes whose largest
+ * element colour exceeds 262144 elements are rejected (TDBEM_ERR_UNSUPPORTED).
+ * All calls share that array: calls that overlap on the GPU race, so serialise
+ * them.  The first call on a device looks the array up with that device
+ * current (the context's device must be current); make it before any stream
+ * capture.  Calls no cudaMalloc, cudaFree or allocating library routine. */
+int tdbem_gh_driver_noalloc(const tdbem_ctx* ctx, int step, int node_lo, int node_hi,
+                            double* d_G_I, double* d_G_J, double* d_H_I, double* d_H_J,
+                            void* stream);
+
 /* Assemble the device-resident level store G^k, H^k for k = 0..M: the result
  * of main()'s steps 1..min(M, nsteps) of G_H_Driver + UpdateGHLinear
  * (main.cpp:89-121, SolverStepLinearT.cpp:58-97): level 0 = J(dt), level k =

@@ -404,6 +404,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
 
 }  // namespace
 
+void tdbem::note_error(const char* msg) { g_last_error = msg; }
+
 extern "C" {
 
 const char* tdbem_last_error(void) { return g_last_error.c_str(); }

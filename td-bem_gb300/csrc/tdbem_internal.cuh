@@ -120,6 +120,9 @@ cudaError_t launch_update_state(const double* x, int D, int s, const unsigned ch
                                 double* t_hist, cudaStream_t st);
 int conv_chunks(int L, int D);
 
+// Sets the calling thread's tdbem_last_error() message (capi.cu).
+void note_error(const char* msg);
+
 // Mixed-precision marching (march_mixed.cu).
 int mixed_ldw(int D);
 int mixed_ld(int D);

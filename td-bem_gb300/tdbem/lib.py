@@ -34,6 +34,10 @@ SIGNATURES = {
     "tdbem_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "tdbem_gh_driver": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        _dp, _dp, _dp, _dp]),
+    "tdbem_gh_driver_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "tdbem_assemble_levels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_get_level": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp]),
     "tdbem_set_bc": (ctypes.c_int, [ctypes.c_void_p, _ip, _dp, ctypes.c_int, _ip, _dp,
