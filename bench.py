@@ -9,7 +9,12 @@ quads (1536 elements, 1538 nodes, 4614 DOF), uniform step pressure, mu = 1,
 nu = 0.25, rho = 1, dt = 0.6 h / c_p, 400 steps, alpha = (0.25, 0).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+    python bench.py --workload sphere_6x16x16_batch64   (64 load cases, batched march)
     python bench.py --impl reference ...   (the reference's algorithm on the host cores)
+
+Batched workloads march many load cases on one mesh: a step is the assembly
+plus one batched march of every case (seeded Gaussian pulses on random
+4-element patches); DOF*steps counts every case.
 
 Multi-GPU runs (torchrun, one process per GPU) are independent replicas of the
 workload (the path does not shard): value = total DOF*steps of all ranks / the
@@ -37,6 +42,7 @@ WORKLOADS = {
     "sphere_6x24x24": dict(kind="sphere", n=24, numstep=500),
     "sphere_6x8x8": dict(kind="sphere", n=8, numstep=200),
     "bar_1x1x4_q2": dict(kind="bar", numstep=200),
+    "sphere_6x16x16_batch64": dict(kind="sphere", n=16, numstep=400, cases=64),
 }
 METRIC = "DOF*steps/s"
 
@@ -178,7 +184,7 @@ def ncu_traffic():
 # --------------------------------------------------------------------------
 # CPU baseline: the reference's algorithm (the oracle restatement) on a sample
 # --------------------------------------------------------------------------
-def cpu_sample(model, M, numstep, a1, a2, nthreads):
+def cpu_sample(model, M, numstep, a1, a2, nthreads, cases=0):
     """Estimate the reference CPU path's time for the whole workload from a bounded sample.
 
     assembly: ElastoDynamicsT::G_H_Driver on the first R collocation rows at a mid step
@@ -188,7 +194,10 @@ def cpu_sample(model, M, numstep, a1, a2, nthreads):
       levels, giving the per-step cost c0 + c1 * (level terms); summed over the
       workload's steps with the reference's level-term count;
     LU: the KSPSolve stand-in's dense LU timed at n = 2000 and scaled by (D/2000)^3,
-      once per distinct LHS."""
+      once per distinct LHS.
+    With cases > 0 (a batch of load cases) the reference runs once per case; the
+    estimate keeps its levels and LU from the first case (one assembly, one LU,
+    cases x marching), which favours the reference."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     D = model.ndof
@@ -237,13 +246,16 @@ def cpu_sample(model, M, numstep, a1, a2, nthreads):
     t0 = time.perf_counter()
     oracle.lu_factor(A, nthreads)
     t_lu = (time.perf_counter() - t0) * (D / 2000.0) ** 3 * n_lu
-    total = t_asm + t_march + t_lu
-    return {"seconds": total, "assembly_s": t_asm, "march_s": t_march, "lu_s": t_lu,
-            "value": D * numstep / total,
+    nc = max(1, cases)
+    total = t_asm + nc * t_march + t_lu
+    return {"seconds": total, "assembly_s": t_asm, "march_s": nc * t_march, "lu_s": t_lu,
+            "value": nc * D * numstep / total,
             "sample": (f"G_H_Driver on {R} of {model.nnd} rows at one step scaled to all rows "
                        f"x {M} steps; Solve_Averaging steps at D={D} on synthetic {m_a}- and "
                        f"{m_b}-level stores fitted to c0+c1*terms and summed over {numstep} "
-                       f"steps; dense LU timed at n=2000 scaled by (D/2000)^3 x {n_lu}")}
+                       f"steps; dense LU timed at n=2000 scaled by (D/2000)^3 x {n_lu}"
+                       + (f"; {nc} load cases: one assembly and LU, {nc} marches" if cases
+                          else ""))}
 
 
 def run_reference(args, dist):
@@ -252,21 +264,23 @@ def run_reference(args, dist):
     model = make_model(args.workload)
     M = model.max_step()
     nthreads = os.cpu_count() or 1
+    cases = WORKLOADS[args.workload].get("cases", 0)
     vals = []
     last = None
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(model, M, model.numstep, *ALPHA, nthreads)
+        r = cpu_sample(model, M, model.numstep, *ALPHA, nthreads, cases)
         if i >= args.warmup:
             vals.append(r["value"])
             last = r
     value = statistics.median(vals)
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * model.ndof * model.numstep / value,
+            "ms_per_step": 1000.0 * max(1, cases) * model.ndof * model.numstep / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": args.workload, "dof": model.ndof, "steps": model.numstep,
-                       "max_step": M, "alpha": list(ALPHA), "precision": "fp64"},
+                       "max_step": M, "alpha": list(ALPHA), "precision": "fp64",
+                       "load_cases": max(1, cases)},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
                              "sample": last["sample"]},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
@@ -279,6 +293,38 @@ def run_reference(args, dist):
 # --------------------------------------------------------------------------
 # our arm
 # --------------------------------------------------------------------------
+def compare_batch(lib, torch, ctx, model, trac, amp, ms_step, check=(0, 1, 2)):
+    """Plain FP64 form of a batched workload: one FP64 assembly and one FP64 march
+    per case (timed on the first case), and the batch's error on a few cases."""
+    from tdbem import loads
+    D, n, nc = model.ndof, model.numstep, trac.shape[0]
+    ub, tb = ctx.march_batch(trac, amp)
+    errs_u, errs_t = [], []
+    with lib.Context(model) as c64:
+        c64.set_alpha(*ALPHA)
+        s64 = torch.cuda.ExternalStream(c64.stream)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(s64)
+        c64.assemble(precision=lib.FP64)
+        ev[1].record(s64)
+        for i, c in enumerate(check):
+            c64.set_bc(*loads.single_case_bc(model, trac[c]))
+            c64.set_load_history(amp[c])
+            u, t = c64.march()
+            if i == 0:
+                ev[2].record(s64)
+                ev[2].synchronize()
+                t_asm = ev[0].elapsed_time(ev[1])
+                t_march = ev[1].elapsed_time(ev[2])
+            errs_u.append(float(np.linalg.norm(ub[:, c] - u) / np.linalg.norm(u)))
+            errs_t.append(float(np.linalg.norm(tb[:, c] - t) / np.linalg.norm(t)))
+    ms64 = t_asm + nc * t_march
+    return {"plain_fp64_value": nc * D * n / (ms64 / 1e3), "plain_fp64_ms_per_step": ms64,
+            "plain_fp64_assembly_ms": t_asm, "plain_fp64_march_ms_per_case": t_march,
+            "speedup_vs_plain_fp64": ms64 / ms_step, "cases_checked": list(check),
+            "u_rel_l2_err": max(errs_u), "t_rel_l2_err": max(errs_t)}
+
+
 def run_ours(args, dist):
     import torch
     from tdbem import lib
@@ -290,13 +336,24 @@ def run_ours(args, dist):
     prec = lib.FP64 if args.precision == "fp64" else lib.MIXED
     model = make_model(args.workload)
     D, nsteps = model.ndof, model.numstep
+    cases = WORKLOADS[args.workload].get("cases", 0)
+    nc = max(1, cases)
+    trac = amp = None
+    if cases:
+        if prec != lib.MIXED:
+            raise SystemExit("batched workloads march FP32 levels: use --precision mixed")
+        from tdbem import loads
+        trac, amp = loads.gaussian_patch_cases(model, cases, seed=0)
     ctx = lib.Context(model)
     ctx.set_alpha(*ALPHA)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def job():
         ctx.assemble(precision=prec)
-        ctx.march(to_host=False)
+        if cases:
+            ctx.march_batch(trac, amp, to_host=False)
+        else:
+            ctx.march(to_host=False)
 
     for _ in range(args.warmup):
         job()
@@ -319,7 +376,7 @@ def run_ours(args, dist):
     launches = ctx.launch_count() - n0
     ms_total = dist.max(e0.elapsed_time(e1))
     ms_step = ms_total / args.steps
-    value = D * nsteps * args.steps * dist.world / (ms_total / 1000.0)
+    value = nc * D * nsteps * args.steps * dist.world / (ms_total / 1000.0)
 
     # untimed profiling pass: per-kernel-class device time and algorithmic units
     ctx.set_profiling(True)
@@ -333,23 +390,30 @@ def run_ours(args, dist):
     h2d = model.coords.nbytes + model.ien.astype(np.int32).nbytes + \
         model.fbc_dofs.nbytes + model.fbc_vals.nbytes + model.ubc_dofs.nbytes + \
         model.ubc_vals.nbytes
-    d2h = 2 * (nsteps + 1) * D * 8
+    d2h = 2 * (nsteps + 1) * nc * D * 8
+    if cases:
+        h2d += trac.nbytes + amp.nbytes
     for _ in range(max(1, args.e2e_steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with lib.Context(model) as c2:
             c2.set_alpha(*ALPHA)
             c2.assemble(precision=prec)
-            c2.march()
+            if cases:
+                c2.march_batch(trac, amp)
+            else:
+                c2.march()
         t1 = time.perf_counter()
         e2e_times.append(t1 - t0)
     e2e_s = dist.max(statistics.median(e2e_times))
-    e2e_value = D * nsteps * dist.world / e2e_s
+    e2e_value = nc * D * nsteps * dist.world / e2e_s
     level_gb = ctx.level_bytes(prec) / 1e9
     M = ctx.M
     # the plain FP64 form on the same workload: its time, and the mixed form's error
     compare = None
-    if prec == lib.MIXED and not args.no_compare:
+    if cases and not args.no_compare:
+        compare = compare_batch(lib, torch, ctx, model, trac, amp, ms_step)
+    elif prec == lib.MIXED and not args.no_compare:
         u32, t32 = ctx.march()  # histories of the mixed form (levels already assembled)
         with lib.Context(model) as c64:
             c64.set_alpha(*ALPHA)
@@ -379,7 +443,22 @@ def run_ours(args, dist):
     traffic = ncu_traffic()
     dom = max(stats, key=lambda k: stats[k]["ms"])
     st = stats[dom]
-    if dom in ("conv", "conv_block"):
+    if dom == "conv_batch":
+        # split-BF16 GEMM: 3 BF16 MMA products per useful FP32 product
+        mma_tf = 3.0 * st["flops"] / (st["ms"] / 1e3) / 1e12
+        gbs = st["bytes"] / (st["ms"] / 1e3) / 1e9
+        f_t, f_h = mma_tf / peaks["bf16_tflops"], gbs / peaks["hbm_gbs"]
+        if f_t >= f_h:
+            roof = {"bound": "tensor", "kernel": "k_conv_mma", "achieved": mma_tf,
+                    "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": f_t,
+                    "peak_source": f"bf16_tflops of {peak_kind} (BF16 MMA flops, 3 per "
+                                   "split product)", "hbm_frac": f_h, "hbm_gbs": gbs}
+        else:
+            roof = {"bound": "hbm", "kernel": "k_conv_mma", "achieved": gbs,
+                    "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": f_h,
+                    "peak_source": f"hbm_gbs of {peak_kind}", "tensor_frac": f_t,
+                    "bf16_mma_tflops": mma_tf}
+    elif dom in ("conv", "conv_block"):
         achieved = st["bytes"] / (st["ms"] / 1e3) / 1e9
         kname = {"conv": "k_conv" if prec == lib.FP64 else "k_conv_f32<1>",
                  "conv_block": "k_conv_f32<NB>"}[dom]
@@ -407,7 +486,7 @@ def run_ours(args, dist):
             "dtype": "f64" if prec == lib.FP64 else "f32+f64", "data": "synthetic",
             "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": M,
                        "alpha": list(ALPHA), "precision": args.precision,
-                       "parallelism": f"replicas{dist.world}",
+                       "parallelism": f"replicas{dist.world}", "load_cases": nc,
                        "l2": "inputs larger than L2: the level store is "
                              f"{level_gb:.1f} GB"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
@@ -425,7 +504,7 @@ def run_ours(args, dist):
     if compare:
         line["vs_plain_fp64"] = compare
     if dist.world == 1 and not args.no_cpu_baseline:
-        r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1)
+        r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1, cases)
         line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
                                 "kind": "port", "sample": r["sample"]}
     print(json.dumps(line))

@@ -151,6 +151,22 @@ int tdbem_set_load_history(tdbem_ctx* ctx, const double* amp, int nsteps);
  * or NULL to keep the histories on the device only. */
 int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
 
+/* Batched marching of nrhs load cases on this context's mesh, boundary
+ * conditions, weights and (TDBEM_MIXED) levels: tdbem_march run for every case
+ * at once.  Case c's known traction at step s is amp[c*numstep + s] *
+ * traction[c*D + d] at every dof d that is not a prescribed-displacement dof
+ * (amp NULL: 1 at every step).  Replaces running SolverStepLinearT::
+ * Solve_Averaging (SolverStepLinearT.cpp:314-544) once per load case with
+ * SolverT::SetLoad (SolverT.cpp:344-377) per case; the reference has no batched
+ * form.  Each step's convolution of all cases is one tensor-core GEMM (split
+ * BF16 products, FP32 accumulation, compensated sum over levels); the solve
+ * applies the FP32 inverse with tdbem_set_march_options' refinement sweeps
+ * (residual in FP32 double-word arithmetic against the FP64 LHS).
+ * u_hist / t_hist: host buffers of (numstep+1) x nrhs x D doubles,
+ * [step][case][dof], or NULL. */
+int tdbem_march_batch(tdbem_ctx* ctx, int numstep, int nrhs, const double* traction,
+                      const double* amp, double* u_hist, double* t_hist);
+
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
  * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64
  * residual-refinement sweeps per solve (0..4; default 1). */
@@ -180,7 +196,9 @@ int tdbem_last_timings(const tdbem_ctx* ctx, double* ms3);
 #define TDBEM_K_ASSEMBLE_F32 4 /* FP32 far-field quadrature items (mixed)            */
 #define TDBEM_K_CONV_BLOCK 5   /* time-block history convolution, NB columns (mixed) */
 #define TDBEM_K_AUX 6          /* window/scan, C term, LHS build, W vectors          */
-#define TDBEM_K_COUNT 7
+#define TDBEM_K_CONV_BATCH 7   /* batched convolution GEMM on the tensor cores       */
+#define TDBEM_K_SOLVE_BATCH 8  /* batched inverse product, refinement, state update  */
+#define TDBEM_K_COUNT 9
 
 /* With on != 0, every launch of the kernel classes above is bracketed by CUDA
  * events on the context stream and its algorithmic bytes / flops are counted

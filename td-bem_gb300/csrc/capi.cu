@@ -166,6 +166,22 @@ void free_levels(tdbem_ctx* c) {
     c->levels_last = 0;
 }
 
+void free_batch(tdbem_ctx* c) {
+    dfree(c->d_bu);
+    dfree(c->d_bt);
+    dfree(c->d_btrac);
+    dfree(c->d_bamp);
+    dfree(c->d_bWt);
+    dfree(c->d_bWu);
+    dfree(c->d_bpart);
+    dfree(c->d_brhs);
+    dfree(c->d_bx);
+    dfree(c->d_br);
+    c->bpart_cap = 0;
+    c->batch_C = 0;
+    c->batch_steps = -1;
+}
+
 void free_march(tdbem_ctx* c) {
     dfree(c->d_u);
     dfree(c->d_t);
@@ -188,6 +204,7 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_Ainv[0]);
     dfree(c->d_Ainv[1]);
     c->hist_steps = -1;
+    free_batch(c);
 }
 
 // Algorithmic FP64 operations of one (item, Gauss point) of the level quadrature
@@ -300,25 +317,12 @@ struct EventTimer {
 };
 
 
-// Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
-// inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
-int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
-    const int D = c->D, M = c->M, nb = c->nb;
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+// FP64 column-exchanged LHS and its FP32 inverse for each distinct LHS of the
+// mixed form (step 2 and steps >= 3); c->timings[1] gets the time taken.
+int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
+    const int D = c->D;
     const size_t DD = (size_t)D * D;
-    const int ldw = mixed_ldw(D);
     cudaStream_t s = c->stream;
-    if (!c->d_Wt_old) {
-        CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
-        CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
-        CUDA_TRY(dalloc(&c->d_Wt_new, (size_t)(M + 1) * ldw));
-        CUDA_TRY(dalloc(&c->d_Wu_new, (size_t)(M + 1) * ldw));
-        CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
-        CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
-        CUDA_TRY(dalloc(&c->d_res, D));
-        CUDA_TRY(dalloc(&c->d_dx, D));
-    }
-    // distinct LHS: step 2 and steps >= 3
     EventTimer tf;
     tf.start(s);
     const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
@@ -349,6 +353,29 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         c->d_Hc64[1] = c->d_Hc64[0];
     }
     c->timings[1] = tf.stop_ms(s);
+    return TDBEM_OK;
+}
+
+// Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
+// inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
+int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
+    const int D = c->D, M = c->M, nb = c->nb;
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const size_t DD = (size_t)D * D;
+    const int ldw = mixed_ldw(D);
+    cudaStream_t s = c->stream;
+    if (!c->d_Wt_old) {
+        CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
+        CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
+        CUDA_TRY(dalloc(&c->d_Wt_new, (size_t)(M + 1) * ldw));
+        CUDA_TRY(dalloc(&c->d_Wu_new, (size_t)(M + 1) * ldw));
+        CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
+        CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
+        CUDA_TRY(dalloc(&c->d_res, D));
+        CUDA_TRY(dalloc(&c->d_dx, D));
+    }
+    const int rc = mixed_inverses(c, numstep, lhs_c);
+    if (rc != TDBEM_OK) return rc;
 
     EventTimer tmr;
     tmr.start(s);
@@ -399,6 +426,129 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         }
     }
     c->timings[2] = tmr.stop_ms(s);
+    return TDBEM_OK;
+}
+
+
+// Per-dof boundary-condition maps and the marching scratch shared by every
+// marching form.
+int upload_bc(tdbem_ctx* c) {
+    const int D = c->D;
+    // per-dof boundary-condition maps; the last list entry of a dof wins (VecSetValues)
+    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
+    std::vector<double> umap(D, 0.0), fmap(D, 0.0), load_t(D, 0.0), load_u(D, 0.0);
+    for (size_t i = 0; i < c->ubc.size(); i++) {
+        is_u[c->ubc[i]] = 1;
+        umap[c->ubc[i]] = c->ubc_v[i];
+    }
+    for (size_t i = 0; i < c->fbc.size(); i++) {
+        is_f[c->fbc[i]] = 1;
+        fmap[c->fbc[i]] = c->fbc_v[i];
+    }
+    for (int j = 0; j < D; j++) {
+        if (is_u[j]) load_u[j] = umap[j];
+        else if (is_f[j]) load_t[j] = fmap[j];
+    }
+    if (!c->d_ubc_map) {
+        CUDA_TRY(dalloc(&c->d_ubc_map, D));
+        CUDA_TRY(dalloc(&c->d_fbc_map, D));
+        CUDA_TRY(dalloc(&c->d_is_ubc, D));
+        CUDA_TRY(dalloc(&c->d_is_fbc, D));
+        CUDA_TRY(dalloc(&c->d_load_t, D));
+        CUDA_TRY(dalloc(&c->d_load_u, D));
+        CUDA_TRY(dalloc(&c->d_Wt, (size_t)(c->M + 1) * D));
+        CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
+        CUDA_TRY(dalloc(&c->d_rhs, D));
+        CUDA_TRY(dalloc(&c->d_x, D));
+        CUDA_TRY(dalloc(&c->d_perm, D + 2 * kMaxPivotBlocks));
+        CUDA_TRY(dalloc(&c->d_status, 1));
+        c->partial_cap = (size_t)(c->M + 1) * D;
+        CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
+    }
+    cudaStream_t s = c->stream;
+    CUDA_TRY(cudaMemcpyAsync(c->d_ubc_map, umap.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_fbc_map, fmap.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_is_ubc, is_u.data(), D, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_is_fbc, is_f.data(), D, cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_load_t, load_t.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    CUDA_TRY(cudaMemcpyAsync(c->d_load_u, load_u.data(), sizeof(double) * D,
+                             cudaMemcpyHostToDevice, s));
+    // the host vectors above are pageable: finish the copies before they go
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return TDBEM_OK;
+}
+
+// Plain FP64 marching: one level-streamed convolution and one FP64 inverse
+// product per step.
+int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hist,
+               double* t_hist) {
+    const int D = c->D;
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const size_t stride = (size_t)D * D;
+    cudaStream_t s = c->stream;
+    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
+    EventTimer tf;
+    tf.start(s);
+    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
+    for (int v = 0; v < 2; v++)
+        if (c->d_Ainv[v] == c->d_Ainv[1 - v]) c->d_Ainv[v] = nullptr;
+    for (int v = 0; v < ninv; v++) {
+        if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
+        CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
+                                  lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
+        if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
+        const int pe = prof_begin(c, TDBEM_K_FACTOR);
+        cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
+                                   &c->launches, s);
+        prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
+        c->launches += 1;  // LHS build
+        if (e == cudaErrorInvalidValue)
+            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
+        CUDA_TRY(e);
+    }
+    if (ninv == 1) {
+        if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
+        c->d_Ainv[1] = c->d_Ainv[0];
+    }
+    c->timings[1] = tf.stop_ms(s);
+
+    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
+    EventTimer tmr;
+    tmr.start(s);
+    for (int curr = 2; curr <= numstep; curr++) {
+        const int st = curr - 1;
+        const int L = std::min(std::max(st, 1), c->M);
+        const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
+        const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
+        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
+        CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
+                                        c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
+        const int nch = conv_chunks(L, D);
+        const double esz = c->d_G ? 8.0 : 4.0;
+        int pe = prof_begin(c, TDBEM_K_CONV);
+        CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
+        prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
+                 (L + 1) * 4.0 * (double)stride);
+        pe = prof_begin(c, TDBEM_K_SOLVE);
+        CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
+                                     c->d_x, s));
+        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
+        prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
+        c->launches += 5;  // combine, conv, reduce, gemv, update
+    }
+    c->timings[2] = tmr.stop_ms(s);
+    if (u_hist)
+        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    if (t_hist)
+        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    prof_flush(c);
     return TDBEM_OK;
 }
 
@@ -790,48 +940,9 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
                     numstep);
     const int D = c->D;
     const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    // per-dof boundary-condition maps; the last list entry of a dof wins (VecSetValues)
-    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
-    std::vector<double> umap(D, 0.0), fmap(D, 0.0), load_t(D, 0.0), load_u(D, 0.0);
-    for (size_t i = 0; i < c->ubc.size(); i++) {
-        is_u[c->ubc[i]] = 1;
-        umap[c->ubc[i]] = c->ubc_v[i];
-    }
-    for (size_t i = 0; i < c->fbc.size(); i++) {
-        is_f[c->fbc[i]] = 1;
-        fmap[c->fbc[i]] = c->fbc_v[i];
-    }
-    for (int j = 0; j < D; j++) {
-        if (is_u[j]) load_u[j] = umap[j];
-        else if (is_f[j]) load_t[j] = fmap[j];
-    }
-    if (!c->d_ubc_map) {
-        CUDA_TRY(dalloc(&c->d_ubc_map, D));
-        CUDA_TRY(dalloc(&c->d_fbc_map, D));
-        CUDA_TRY(dalloc(&c->d_is_ubc, D));
-        CUDA_TRY(dalloc(&c->d_is_fbc, D));
-        CUDA_TRY(dalloc(&c->d_load_t, D));
-        CUDA_TRY(dalloc(&c->d_load_u, D));
-        CUDA_TRY(dalloc(&c->d_Wt, (size_t)(c->M + 1) * D));
-        CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
-        CUDA_TRY(dalloc(&c->d_rhs, D));
-        CUDA_TRY(dalloc(&c->d_x, D));
-        CUDA_TRY(dalloc(&c->d_perm, D + 2 * kMaxPivotBlocks));
-        CUDA_TRY(dalloc(&c->d_status, 1));
-        c->partial_cap = (size_t)(c->M + 1) * D;
-        CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
-    }
+    const int rc0 = upload_bc(c);
+    if (rc0 != TDBEM_OK) return rc0;
     cudaStream_t s = c->stream;
-    CUDA_TRY(cudaMemcpyAsync(c->d_ubc_map, umap.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_fbc_map, fmap.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_is_ubc, is_u.data(), D, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_is_fbc, is_f.data(), D, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_load_t, load_t.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_load_u, load_u.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
     if (c->hist_steps != numstep) {
         dfree(c->d_u);
         dfree(c->d_t);
@@ -842,7 +953,6 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
     CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (numstep + 1) * D, s));
     CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (numstep + 1) * D, s));
 
-    const size_t stride = (size_t)D * D;
     // LHS of step 2 (SolverStepLinearT.cpp:357-371) and of steps >= 3 (381-393)
     const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
     if (c->level_precision == TDBEM_MIXED) {
@@ -858,63 +968,103 @@ int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
         prof_flush(c);
         return TDBEM_OK;
     }
-    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-    EventTimer tf;
-    tf.start(s);
-    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
-    for (int v = 0; v < 2; v++)
-        if (c->d_Ainv[v] == c->d_Ainv[1 - v]) c->d_Ainv[v] = nullptr;
-    for (int v = 0; v < ninv; v++) {
-        if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
-        CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
-                                  lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
-        if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
-        const int pe = prof_begin(c, TDBEM_K_FACTOR);
-        cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
-                                   &c->launches, s);
-        prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
-        c->launches += 1;  // LHS build
-        if (e == cudaErrorInvalidValue)
-            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
-        CUDA_TRY(e);
-    }
-    if (ninv == 1) {
-        if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
-        c->d_Ainv[1] = c->d_Ainv[0];
-    }
-    c->timings[1] = tf.stop_ms(s);
+    return march_fp64(c, numstep, lhs_c, u_hist, t_hist);
+}
 
-    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
+int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* traction,
+                      const double* amp, double* u_hist, double* t_hist) {
+    if (!c || !traction) return fail(TDBEM_ERR_ARG, "null argument");
+    if (numstep < 1 || nrhs < 1) return fail(TDBEM_ERR_ARG, "numstep and nrhs must be >= 1");
+    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
+    if (c->level_precision != TDBEM_MIXED)
+        return fail(TDBEM_ERR_UNSUPPORTED,
+                    "batched marching runs on FP32 levels: assemble with TDBEM_MIXED");
+    if (c->levels_last < std::min(c->M, numstep))
+        return fail(TDBEM_ERR_STATE, "levels assembled for %d steps, %d needed", c->levels_last,
+                    std::min(c->M, numstep));
+    const int D = c->D, M = c->M, C = nrhs;
+    if ((size_t)C * D > (size_t)INT32_MAX / 2)
+        return fail(TDBEM_ERR_ARG, "nrhs x D = %zu is too large", (size_t)C * D);
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const int rc0 = upload_bc(c);
+    if (rc0 != TDBEM_OK) return rc0;
+    cudaStream_t s = c->stream;
+    const size_t CD = (size_t)C * D;
+    const int ldw = batch_ldw(D);
+    if (c->batch_C != C || c->batch_steps != numstep) {
+        free_batch(c);
+        CUDA_TRY(dalloc(&c->d_bu, (size_t)(numstep + 1) * CD));
+        CUDA_TRY(dalloc(&c->d_bt, (size_t)(numstep + 1) * CD));
+        CUDA_TRY(dalloc(&c->d_btrac, CD));
+        CUDA_TRY(dalloc(&c->d_bamp, (size_t)C * numstep));
+        CUDA_TRY(dalloc(&c->d_bWt, (size_t)(M + 1) * C * ldw));
+        CUDA_TRY(dalloc(&c->d_bWu, (size_t)(M + 1) * C * ldw));
+        int smax = batch_apply_splits(D, C);
+        for (int nlev = 2; nlev <= M + 1; nlev++)
+            smax = std::max(smax, batch_conv_splits(nlev, D, C));
+        c->bpart_cap = (size_t)smax * CD;
+        CUDA_TRY(dalloc(&c->d_bpart, c->bpart_cap));
+        CUDA_TRY(dalloc(&c->d_brhs, CD));
+        CUDA_TRY(dalloc(&c->d_bx, CD));
+        CUDA_TRY(dalloc(&c->d_br, CD));
+        c->batch_C = C;
+        c->batch_steps = numstep;
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->d_btrac, traction, sizeof(double) * CD, cudaMemcpyHostToDevice, s));
+    if (amp)
+        CUDA_TRY(cudaMemcpyAsync(c->d_bamp, amp, sizeof(double) * C * numstep,
+                                 cudaMemcpyHostToDevice, s));
+    const double* d_amp = amp ? c->d_bamp : nullptr;
+    CUDA_TRY(cudaMemsetAsync(c->d_bu, 0, sizeof(double) * (numstep + 1) * CD, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_bt, 0, sizeof(double) * (numstep + 1) * CD, s));
+    c->launches += 0;
+
+    const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+    const int rc = mixed_inverses(c, numstep, lhs_c);
+    if (rc != TDBEM_OK) return rc;
+
     EventTimer tmr;
     tmr.start(s);
-    for (int curr = 2; curr <= numstep; curr++) {
-        const int st = curr - 1;
-        const int L = std::min(std::max(st, 1), c->M);
+    const size_t lstride = (size_t)D * c->ldf;
+    const double DD = (double)D * D;
+    const int sp = batch_apply_splits(D, C);
+    for (int st = 1; st <= numstep - 1; st++) {
+        const int L = std::min(M, std::max(1, st));
+        const int nlev = L + 1;
         const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
         const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
-        CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
-                                        c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
-        const int nch = conv_chunks(L, D);
-        const double esz = c->d_G ? 8.0 : 4.0;
-        int pe = prof_begin(c, TDBEM_K_CONV);
-        CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
-        prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
-                 (L + 1) * 4.0 * (double)stride);
-        pe = prof_begin(c, TDBEM_K_SOLVE);
-        CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
-                                     c->d_x, s));
-        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
-        prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
-        c->launches += 5;  // combine, conv, reduce, gemv, update
+        CUDA_TRY(launch_build_w_batch(c->d_bu, c->d_bt, D, C, st, nlev, a1, a2, a3, c0, c1, d_amp,
+                                      numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map, ldw,
+                                      c->d_bWt, c->d_bWu, s));
+        const int splits = batch_conv_splits(nlev, D, C);
+        int pe = prof_begin(c, TDBEM_K_CONV_BATCH);
+        CUDA_TRY(launch_conv_mma(c->d_Gf, c->d_Hf, lstride, c->ldf, D, nlev, c->d_bWt, c->d_bWu,
+                                 ldw, C, c->d_bpart, splits, s));
+        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * C * ldw * 4,
+                 nlev * 4.0 * DD * C);
+        pe = prof_begin(c, TDBEM_K_SOLVE_BATCH);
+        CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
+        const int v = st == 1 ? 0 : 1;
+        CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_brhs, C, c->d_bpart, sp, s));
+        CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, nullptr, c->d_bx, s));
+        for (int it = 0; it < c->n_refine; it++) {
+            CUDA_TRY(launch_apply_cols(c->d_Hc64[v], 1, D, c->d_bx, C, c->d_bpart, sp, s));
+            CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_brhs, c->d_br, s));
+            CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_br, C, c->d_bpart, sp, s));
+            CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_bx, c->d_bx, s));
+        }
+        CUDA_TRY(launch_update_batch(c->d_bx, D, C, st, c->d_is_ubc, c->d_ubc_map, c->d_btrac,
+                                     d_amp, numstep, c->d_bu, c->d_bt, s));
+        prof_end(c, pe, DD * 4 * (1 + c->n_refine) + DD * 8 * c->n_refine,
+                 2.0 * DD * C * (1 + 2 * c->n_refine));
+        c->launches += 6 + 4LL * c->n_refine;
     }
     c->timings[2] = tmr.stop_ms(s);
     if (u_hist)
-        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
+        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_bu, sizeof(double) * (numstep + 1) * CD,
                                  cudaMemcpyDeviceToHost, s));
     if (t_hist)
-        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
+        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_bt, sizeof(double) * (numstep + 1) * CD,
                                  cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     prof_flush(c);

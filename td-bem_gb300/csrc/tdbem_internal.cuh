@@ -142,6 +142,26 @@ cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
                                double* x, double* r, double* dx, int n_refine, cudaStream_t s);
 
+// Batched marching of many load cases (batch.cu).
+int batch_block_cases();            // cases per tensor-core column block
+int batch_ldw(int D);               // row stride of the batched history vectors
+int batch_conv_splits(int nlev, int D, int C);
+int batch_apply_splits(int D, int C);
+cudaError_t launch_conv_mma(const float* G, const float* H, size_t lstride, int ld, int D,
+                            int nlev, const float* Wt, const float* Wu, int ldw, int C,
+                            double* partial, int splits, cudaStream_t s);
+cudaError_t launch_apply_cols(const void* A, int fp64_residual, int D, const double* X, int C,
+                              double* partial, int splits, cudaStream_t s);
+cudaError_t launch_build_w_batch(const double* u_hist, const double* t_hist, int D, int C, int s,
+                                 int nlev, double a1, double a2, double a3, double c0, double c1,
+                                 const double* amp, int numstep, const double* traction,
+                                 const unsigned char* is_u, const double* ubc_val, int ldw,
+                                 float* Wt, float* Wu, cudaStream_t st);
+cudaError_t launch_update_batch(const double* x, int D, int C, int s, const unsigned char* is_u,
+                                const double* ubc_val, const double* traction,
+                                const double* amp, int numstep, double* u_hist, double* t_hist,
+                                cudaStream_t st);
+
 }  // namespace tdbem
 
 // The context (capi.cu owns its lifetime).
@@ -194,6 +214,19 @@ struct tdbem_ctx {
     double* d_pmix = nullptr;       // conv partials, chunks x nb x D
     double* d_res = nullptr;
     double* d_dx = nullptr;
+    // batched marching (tdbem_march_batch): C cases, histories [step][case][dof]
+    int batch_C = 0, batch_steps = -1;
+    double* d_bu = nullptr;
+    double* d_bt = nullptr;
+    double* d_btrac = nullptr;      // C x D traction vectors
+    double* d_bamp = nullptr;       // C x numstep amplitudes
+    float* d_bWt = nullptr;         // (M+1) x C x ldw history vectors
+    float* d_bWu = nullptr;
+    double* d_bpart = nullptr;      // split partial sums
+    size_t bpart_cap = 0;
+    double* d_brhs = nullptr;       // C x D
+    double* d_bx = nullptr;
+    double* d_br = nullptr;
 
     // boundary conditions and marching parameters
     std::vector<int> ubc, fbc;

@@ -45,6 +45,8 @@ SIGNATURES = {
     "tdbem_set_alpha": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]),
     "tdbem_set_load_history": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int]),
     "tdbem_march": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "tdbem_march_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp,
+                                         _dp, _dp]),
     "tdbem_history_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                             ctypes.POINTER(ctypes.c_void_p)]),
     "tdbem_level_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
@@ -58,7 +60,7 @@ SIGNATURES = {
 }
 
 KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve", 4: "assemble_f32",
-                  5: "conv_block", 6: "aux"}
+                  5: "conv_block", 6: "aux", 7: "conv_batch", 8: "solve_batch"}
 
 
 class Mesh(ctypes.Structure):
@@ -199,6 +201,32 @@ class Context:
             _check(load().tdbem_march(self.h, n, _d(u), _d(t)))
             return u, t
         _check(load().tdbem_march(self.h, n, None, None))
+        return None
+
+    def march_batch(self, traction, amp=None, numstep: Optional[int] = None,
+                    to_host: bool = True):
+        """March every load case of ``traction`` (cases x D) at once.
+
+        ``amp`` (cases x numstep) scales case c's traction at step s; None means
+        a unit step load.  Returns u, t of shape (numstep + 1, cases, D)."""
+        n = self.model.numstep if numstep is None else numstep
+        tr = np.ascontiguousarray(traction, dtype=np.float64)
+        if tr.ndim != 2 or tr.shape[1] != self.D:
+            raise ValueError(f"traction must be (cases, {self.D})")
+        nc = tr.shape[0]
+        a = None
+        if amp is not None:
+            a = np.ascontiguousarray(amp, dtype=np.float64)
+            if a.shape != (nc, n):
+                raise ValueError(f"amp must be ({nc}, {n})")
+        if to_host:
+            u = np.empty((n + 1, nc, self.D))
+            t = np.empty((n + 1, nc, self.D))
+            _check(load().tdbem_march_batch(self.h, n, nc, _d(tr), None if a is None else _d(a),
+                                            _d(u), _d(t)))
+            return u, t
+        _check(load().tdbem_march_batch(self.h, n, nc, _d(tr), None if a is None else _d(a),
+                                        None, None))
         return None
 
     def timings(self):
