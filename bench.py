@@ -503,12 +503,35 @@ def run_ours(args, dist):
             "peaks_used": {k: peaks.get(k) for k in ("hbm_gbs", "fp64_tflops", "fp32_tflops")}}
     if compare:
         line["vs_plain_fp64"] = compare
+    if args.serve_requests > 0:
+        line["serve"] = run_serve(lib, args, dev)
     if dist.world == 1 and not args.no_cpu_baseline:
         r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1, cases)
         line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
                                 "kind": "port", "sample": r["sample"]}
     print(json.dumps(line))
     return 0
+
+
+def run_serve(lib, args, dev):
+    """Seeded Poisson stream of mixed transient solves through the server
+    (continuous batching, admission by HBM footprint): latency percentiles and
+    throughput.  Not part of the timed region of the headline number."""
+    from tdbem import serve
+    reqs = serve.request_mix(args.serve_requests, args.serve_rate, seed=0)
+    with lib.Server(dev, 0, slots=args.serve_slots) as srv:
+        res = serve.run_stream(srv, reqs, alpha=ALPHA)
+    mix = {}
+    for r in res["records"]:
+        k = r["name"].split("_")[0]
+        mix[k] = mix.get(k, 0) + 1
+    return {"requests": len(reqs), "rate_hz": args.serve_rate, "slots": args.serve_slots,
+            "precision": "mixed", "p50_s": res["p50_s"], "p99_s": res["p99_s"],
+            "mean_queued_s": res["mean_queued_s"], "wall_s": res["wall_s"],
+            "dof_steps_per_s": res["dof_steps_per_s"], "mix": mix,
+            "dof_range": [min(r["dof"] for r in reqs), max(r["dof"] for r in reqs)],
+            "steps_range": [min(r["steps"] for r in reqs), max(r["steps"] for r in reqs)],
+            "seed": 0}
 
 
 def main():
@@ -523,6 +546,10 @@ def main():
                     help="skip the plain FP64 run that measures the mixed form's error")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=16,
+                    help="requests of the serving stream reported beside the headline (0: off)")
+    ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, 1/s")
+    ap.add_argument("--serve-slots", type=int, default=4)
     args = ap.parse_args()
     dist = Dist()
     try:

@@ -214,6 +214,65 @@ int tdbem_kernel_stats(const tdbem_ctx* ctx, int kclass, long long* launches, do
 /* Number of CUDA kernels this context has launched so far. */
 int tdbem_launch_count(const tdbem_ctx* ctx, long long* n);
 
+/* ---- serving: continuous batching of transient solves ---------------- */
+/* The reference runs one solve per process (main.cpp); it has no server.  The
+ * server below accepts whole solves as they arrive, admits them by device
+ * footprint into a fixed number of slots, and runs the admitted solves'
+ * kernels concurrently, each on its own stream with its levels and histories
+ * resident on the device until it completes. */
+
+/* Device bytes a solve needs: the level store (levels x D x D x bytes x 2)
+ * plus the assembly and marching state of tdbem_assemble_levels + tdbem_march
+ * at this precision. */
+int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt, int nq,
+                    int numstep, int precision, size_t* bytes);
+
+typedef struct tdbem_server tdbem_server;
+
+/* One transient solve: the inputs of tdbem_ctx_create, tdbem_set_bc,
+ * tdbem_set_alpha, tdbem_set_load_history (amp: numstep values or NULL) and
+ * tdbem_assemble_levels / tdbem_march.  The server copies every array. */
+typedef struct tdbem_request {
+    tdbem_mesh mesh;
+    tdbem_material mat;
+    double dt;
+    int nq;
+    int if_ext;
+    const int* ubc_dofs;
+    const double* ubc_vals;
+    int n_u;
+    const int* fbc_dofs;
+    const double* fbc_vals;
+    int n_f;
+    double alpha1, alpha2;
+    const double* amp;
+    int numstep;
+    int precision;
+} tdbem_request;
+
+#define TDBEM_REQ_QUEUED 0
+#define TDBEM_REQ_RUNNING 1
+#define TDBEM_REQ_DONE 2
+#define TDBEM_REQ_FAILED 3
+
+/* Server on a device with an HBM budget in bytes (0: 90% of the free memory at
+ * creation) and `slots` concurrently resident solves (1..64). */
+int tdbem_server_create(int device, size_t hbm_budget, int slots, tdbem_server** out);
+/* Queue a solve; fails with TDBEM_ERR_NOMEM when it can never fit the budget. */
+int tdbem_server_submit(tdbem_server* srv, const tdbem_request* req, long long* id);
+/* Wait until the request is done or failed, or timeout_s passes (< 0: no
+ * limit); *state is its TDBEM_REQ_* state. */
+int tdbem_server_wait(tdbem_server* srv, long long id, double timeout_s, int* state);
+/* Histories of a finished request ((numstep+1) x D doubles each, or NULL) and
+ * times[3] = {seconds queued, seconds running, latency}; releases the request.
+ * A failed request returns its error code and message. */
+int tdbem_server_result(tdbem_server* srv, long long id, double* u_hist, double* t_hist,
+                        double* times);
+int tdbem_server_stats(tdbem_server* srv, size_t* used_bytes, size_t* budget_bytes, int* active,
+                       int* queued, long long* completed);
+/* Finish every queued and running request, then stop. */
+int tdbem_server_destroy(tdbem_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,7 +34,7 @@ def nvcc() -> str:
 
 
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
 
 def _headers():
@@ -50,7 +50,7 @@ def _stale(target, deps):
 
 
 def _compile(src, verbose, ptxas_info):
-    obj = os.path.join(OUT, os.path.basename(src).replace(".cu", ".o"))
+    obj = os.path.join(OUT, os.path.splitext(os.path.basename(src))[0] + ".o")
     if not _stale(obj, [src] + _headers()) and not ptxas_info:
         return obj, ""
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + \
@@ -73,7 +73,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         for _, log in results:
             sys.stderr.write(log)
     if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -1129,6 +1129,47 @@ int tdbem_launch_count(const tdbem_ctx* c, long long* n) {
     return TDBEM_OK;
 }
 
+int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt, int nq,
+                    int numstep, int precision, size_t* bytes) {
+    if (!mesh || !mat || !bytes || !mesh->coords || !mesh->ien)
+        return fail(TDBEM_ERR_ARG, "null argument");
+    if (mesh->nnd < 2 || mesh->nel < 1 || !(dt > 0) || numstep < 1 || !(mat->rho > 0) ||
+        !(mat->E > 0) || !(mat->nu > -1 && mat->nu < 0.5) || mesh->etype != 1)
+        return fail(TDBEM_ERR_ARG, "invalid mesh, material, time step or step count");
+    if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
+        return fail(TDBEM_ERR_ARG, "precision must be TDBEM_FP64 or TDBEM_MIXED");
+    std::vector<double> x(mesh->coords, mesh->coords + 3 * (size_t)mesh->nnd);
+    std::vector<int> ien(mesh->ien, mesh->ien + 4 * (size_t)mesh->nel);
+    for (int v : ien)
+        if (v < 0 || v >= mesh->nnd) return fail(TDBEM_ERR_ARG, "element node out of range");
+    const int M = compute_max_step(x, mesh->nnd, mat->E, mat->nu, mat->rho, dt);
+    std::vector<int> order, start;
+    color_elements(ien, mesh->nel, mesh->nnd, order, start);
+    size_t max_color = 0;
+    for (size_t k = 0; k + 1 < start.size(); k++)
+        max_color = std::max<size_t>(max_color, (size_t)(start[k + 1] - start[k]));
+    const size_t D = 3 * (size_t)mesh->nnd, DD = D * D, L = (size_t)M + 1;
+    const size_t nel = mesh->nel, q2 = (size_t)nq * nq;
+    size_t pair_cap = std::min<size_t>((size_t)mesh->nnd * max_color, (size_t)1 << 26);
+    pair_cap = std::max(pair_cap, max_color);
+    // tdbem_ctx_create: mesh, Gauss geometry (FP64 + FP32), C term, colours, pair scratch
+    size_t b = 24 * (size_t)mesh->nnd + 20 * nel + q2 * nel * 12 * 12 + 72 * (size_t)mesh->nnd +
+               pair_cap * (sizeof(PairInfo) + 8) + pair_cap / 8 + ((size_t)1 << 16);  // + scan
+    // marching state common to both forms: maps, W vectors, partials, histories
+    b += 8 * D * 8 + 3 * L * D * 8 + 2 * ((size_t)numstep + 1) * D * 8 + 4 * (D + 64);
+    if (precision == TDBEM_FP64) {
+        b += 2 * L * DD * 8;                    // levels
+        b += 2 * DD * 8 + inverse_scratch_elems((int)D) * 8;  // inverses
+    } else {
+        const size_t ld = mixed_ld((int)D), ldw = mixed_ldw((int)D), nb = 16;
+        b += 2 * L * D * ld * 4 + 4 * DD * 8;   // FP32 levels, FP64 levels 0 and 1
+        b += 2 * DD * 8 + 2 * DD * 4 + inverse_scratch_elems((int)D) * 4;  // LHS, inverses
+        b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
+    }
+    *bytes = b;
+    return TDBEM_OK;
+}
+
 int tdbem_last_timings(const tdbem_ctx* c, double* ms3) {
     if (!c || !ms3) return fail(TDBEM_ERR_ARG, "null argument");
     for (int i = 0; i < 3; i++) ms3[i] = c->timings[i];

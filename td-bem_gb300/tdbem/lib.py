@@ -57,6 +57,20 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp]),
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tdbem_footprint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_size_t)]),
+    "tdbem_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+    "tdbem_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "tdbem_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double,
+                                         _ip]),
+    "tdbem_server_result": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, _dp, _dp, _dp]),
+    "tdbem_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
+                                          ctypes.POINTER(ctypes.c_size_t), _ip, _ip,
+                                          ctypes.POINTER(ctypes.c_longlong)]),
+    "tdbem_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve", 4: "assemble_f32",
@@ -70,6 +84,93 @@ class Mesh(ctypes.Structure):
 
 class Material(ctypes.Structure):
     _fields_ = [("E", ctypes.c_double), ("nu", ctypes.c_double), ("rho", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("mesh", Mesh), ("mat", Material), ("dt", ctypes.c_double), ("nq", ctypes.c_int),
+                ("if_ext", ctypes.c_int), ("ubc_dofs", _ip), ("ubc_vals", _dp),
+                ("n_u", ctypes.c_int), ("fbc_dofs", _ip), ("fbc_vals", _dp),
+                ("n_f", ctypes.c_int), ("alpha1", ctypes.c_double), ("alpha2", ctypes.c_double),
+                ("amp", _dp), ("numstep", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+def footprint(model, precision: int = 1, numstep: Optional[int] = None) -> int:
+    """Device bytes a solve of ``model`` needs (tdbem_footprint)."""
+    c = np.ascontiguousarray(model.coords, np.float64)
+    e = np.ascontiguousarray(model.ien, np.int32)
+    mesh = Mesh(model.nnd, model.nel, model.etype, _d(c), _i(e))
+    mat = Material(model.E, model.nu, model.rho)
+    b = ctypes.c_size_t()
+    _check(load().tdbem_footprint(ctypes.byref(mesh), ctypes.byref(mat), model.dt, model.nq,
+                                  model.numstep if numstep is None else numstep, precision,
+                                  ctypes.byref(b)))
+    return b.value
+
+
+class Server:
+    """Continuous-batching server of transient solves (tdbem_server_*)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, slots: int = 4):
+        h = ctypes.c_void_p()
+        _check(load().tdbem_server_create(device, budget_bytes, slots, ctypes.byref(h)))
+        self.h = h
+        self._meta = {}
+
+    def submit(self, model, alpha=(0.25, 0.0), amp=None, precision: int = 1) -> int:
+        keep = [np.ascontiguousarray(model.coords, np.float64),
+                np.ascontiguousarray(model.ien, np.int32),
+                np.ascontiguousarray(model.ubc_dofs, np.int32),
+                np.ascontiguousarray(model.ubc_vals, np.float64),
+                np.ascontiguousarray(model.fbc_dofs, np.int32),
+                np.ascontiguousarray(model.fbc_vals, np.float64)]
+        a = None if amp is None else np.ascontiguousarray(amp, np.float64)
+        if a is not None and len(a) < model.numstep:
+            raise ValueError("amp needs numstep values")
+        req = Request(Mesh(model.nnd, model.nel, model.etype, _d(keep[0]), _i(keep[1])),
+                      Material(model.E, model.nu, model.rho), model.dt, model.nq, model.if_ext,
+                      _i(keep[2]), _d(keep[3]), len(keep[2]), _i(keep[4]), _d(keep[5]),
+                      len(keep[4]), alpha[0], alpha[1], None if a is None else _d(a),
+                      model.numstep, precision)
+        rid = ctypes.c_longlong()
+        _check(load().tdbem_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid)))
+        self._meta[rid.value] = (model.numstep, 3 * model.nnd)
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = -1.0) -> int:
+        st = ctypes.c_int()
+        _check(load().tdbem_server_wait(self.h, rid, timeout, ctypes.byref(st)))
+        return st.value
+
+    def result(self, rid: int):
+        """(u, t, {queued_s, run_s, latency_s}) of a finished request."""
+        n, D = self._meta.pop(rid)
+        u = np.empty((n + 1, D))
+        t = np.empty((n + 1, D))
+        times = np.zeros(3)
+        _check(load().tdbem_server_result(self.h, rid, _d(u), _d(t), _d(times)))
+        return u, t, {"queued_s": times[0], "run_s": times[1], "latency_s": times[2]}
+
+    def stats(self):
+        used, budget = ctypes.c_size_t(), ctypes.c_size_t()
+        act, q, done = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong()
+        _check(load().tdbem_server_stats(self.h, ctypes.byref(used), ctypes.byref(budget),
+                                         ctypes.byref(act), ctypes.byref(q), ctypes.byref(done)))
+        return {"used_bytes": used.value, "budget_bytes": budget.value, "active": act.value,
+                "queued": q.value, "completed": done.value}
+
+    def close(self):
+        if self.h:
+            load().tdbem_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class TdbemError(RuntimeError):

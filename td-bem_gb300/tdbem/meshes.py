@@ -8,6 +8,10 @@
   equiangular cubed-sphere quads with normals pointing into the cavity like
   the reference's ``geometry/SphericalCavity_*.txt``, uniform internal
   pressure p: traction ``t = p * x / |x|`` on every dof.
+* :func:`halfspace_cavity` -- box-truncated half-space with a spherical
+  cavity: a square free-surface patch at z = 0 (normals +z, out of the solid)
+  over a cubed-sphere cavity at depth d (normals into the cavity), internal
+  pressure on the cavity, the patch traction-free.
 
 The mesh size h of a cubed sphere is the equiangular arc spacing
 ``radius * (pi/2) / n``; the time step is ``dt = beta * h / c_p``.
@@ -126,6 +130,63 @@ def cubed_sphere(n: int = 16, radius: float = 1.0, mu: float = 1.0, nu: float = 
     m.dt = beta * h / cp
     rhat = coords / np.linalg.norm(coords, axis=1, keepdims=True)
     m.fbc_dofs = np.arange(3 * len(coords), dtype=np.int32)
+    m.fbc_vals = (pressure * rhat).reshape(-1).astype(float)
+    return m
+
+
+def _cubed_sphere_surface(n: int, radius: float, centre=(0.0, 0.0, 0.0)):
+    ang = np.linspace(-np.pi / 4, np.pi / 4, n + 1)
+    t = np.tan(ang)
+    key_to_id, coords, quads = {}, [], []
+    for axis, sign in ((0, 1), (0, -1), (1, 1), (1, -1), (2, 1), (2, -1)):
+        others = [d for d in range(3) if d != axis]
+        ids = np.zeros((n + 1, n + 1), np.int64)
+        for i in range(n + 1):
+            for j in range(n + 1):
+                p = np.zeros(3)
+                p[axis] = sign
+                p[others[0]] = t[i]
+                p[others[1]] = t[j]
+                p = radius * p / np.linalg.norm(p)
+                key = tuple(np.round(p, 10))
+                if key not in key_to_id:
+                    key_to_id[key] = len(coords)
+                    coords.append(p)
+                ids[i, j] = key_to_id[key]
+        for i in range(n):
+            for j in range(n):
+                quads.append([ids[i, j], ids[i + 1, j], ids[i + 1, j + 1], ids[i, j + 1]])
+    coords = np.array(coords, float)
+    ien = np.array(quads, np.int32)
+    ien = _orient(coords, ien, lambda c: -c)  # into the cavity
+    return coords + np.asarray(centre, float), ien
+
+
+def halfspace_cavity(depth: float = 3.0, patch: float = 10.0, per_unit: int = 1,
+                     n_sphere: int = 6, radius: float = 1.0, mu: float = 1.0, nu: float = 0.25,
+                     rho: float = 1.0, beta: float = 0.6, numstep: int = 200,
+                     pressure: float = 1.0) -> Model:
+    """Cavity of radius ``radius`` centred at depth ``depth`` under a ``patch`` x
+    ``patch`` free-surface square meshed at ``per_unit`` quads per unit length."""
+    ns = int(round(patch * per_unit))
+    xs = np.linspace(-patch / 2, patch / 2, ns + 1)
+    grid = np.array([(x, y, 0.0) for y in xs for x in xs])
+    quads = [[j * (ns + 1) + i, j * (ns + 1) + i + 1, (j + 1) * (ns + 1) + i + 1,
+              (j + 1) * (ns + 1) + i] for j in range(ns) for i in range(ns)]
+    ien_s = _orient(grid, np.array(quads, np.int32), lambda c: np.array([0.0, 0.0, 1.0]))
+    c_sph, ien_c = _cubed_sphere_surface(n_sphere, radius, (0.0, 0.0, -depth))
+    coords = np.vstack([grid, c_sph])
+    ien = np.vstack([ien_s, ien_c + len(grid)]).astype(np.int32)
+    E, nu_, rho_ = material_for(mu, nu, rho)
+    m = Model(coords=coords, ien=ien, etype=1, E=E, nu=nu_, rho=rho_, numstep=numstep,
+              if_ext=1)
+    _, _, cp, _ = m.material()
+    h = min(1.0 / per_unit, radius * (np.pi / 2) / n_sphere)
+    m.dt = beta * h / cp
+    rel = c_sph - np.array([0.0, 0.0, -depth])
+    rhat = rel / np.linalg.norm(rel, axis=1, keepdims=True)
+    nodes = np.arange(len(grid), len(coords))
+    m.fbc_dofs = np.array([3 * a + d for a in nodes for d in range(3)], np.int32)
     m.fbc_vals = (pressure * rhat).reshape(-1).astype(float)
     return m
 

@@ -1,0 +1,63 @@
+"""Serving on the host: the request stream, the footprint estimate and the
+server's refusal without a GPU (no CPU fallback)."""
+import numpy as np
+import pytest
+
+from tdbem import meshes, serve
+
+
+@pytest.fixture(scope="module")
+def tdlib():
+    import build as b
+    b.build()
+    from tdbem import lib
+    lib.load()
+    return lib
+
+
+def test_request_mix_seeded():
+    a = serve.request_mix(12, rate_hz=4.0, seed=5)
+    b = serve.request_mix(12, rate_hz=4.0, seed=5)
+    assert [r["name"] for r in a] == [r["name"] for r in b]
+    assert [r["arrival_s"] for r in a] == [r["arrival_s"] for r in b]
+    arr = np.array([r["arrival_s"] for r in a])
+    assert np.all(np.diff(arr) > 0)
+    for r in a:
+        assert 300 <= r["dof"] <= 8000
+        assert 100 <= r["steps"] <= 400
+        assert r["amp"] is None or len(r["amp"]) == r["steps"]
+    kinds = {r["name"].split("_")[0] for r in serve.request_mix(40, 4.0, seed=1)}
+    assert kinds == {"bar", "sphere", "halfspace"}
+
+
+def test_footprint_counts_the_level_store(tdlib):
+    m = meshes.cubed_sphere(8, numstep=200)
+    M = m.max_step()
+    D = 3 * m.nnd
+    f64 = tdlib.footprint(m, tdlib.FP64)
+    f32 = tdlib.footprint(m, tdlib.MIXED)
+    levels64 = 2 * (M + 1) * D * D * 8
+    assert levels64 < f64 < 1.3 * levels64
+    assert 2 * (M + 1) * D * D * 4 < f32 < f64
+    # more steps: longer histories, same levels
+    assert tdlib.footprint(m, tdlib.MIXED, numstep=400) > f32
+
+
+def test_halfspace_cavity_mesh():
+    m = meshes.halfspace_cavity(n_sphere=4)
+    assert m.nnd == 121 + 6 * 16 + 2 and m.nel == 100 + 6 * 16
+    assert m.if_ext == 1
+    # patch normals point up (+z), cavity normals toward the cavity centre
+    p = m.coords[m.ien]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 3] - p[:, 0])
+    assert np.all(n[:100, 2] > 0)
+    c = p[100:].mean(1) - np.array([0, 0, -3.0])
+    assert np.all(np.einsum("ij,ij->i", n[100:], c) < 0)
+
+
+def test_server_refuses_without_gpu(tdlib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(tdlib.TdbemError):
+        tdlib.Server(0, 0, 2)
