@@ -346,6 +346,8 @@ def run_ours(args, dist):
         trac, amp = loads.gaussian_patch_cases(model, cases, seed=0)
     ctx = lib.Context(model)
     ctx.set_alpha(*ALPHA)
+    ctx.set_march_options(12, args.refine)
+    ctx.set_batch_engine(lib.ENGINE_TCGEN05 if args.engine == "tcgen05" else lib.ENGINE_MMA_SYNC)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
     def job():
@@ -398,6 +400,9 @@ def run_ours(args, dist):
         t0 = time.perf_counter()
         with lib.Context(model) as c2:
             c2.set_alpha(*ALPHA)
+            c2.set_march_options(12, args.refine)
+            c2.set_batch_engine(lib.ENGINE_TCGEN05 if args.engine == "tcgen05"
+                                else lib.ENGINE_MMA_SYNC)
             c2.assemble(precision=prec)
             if cases:
                 c2.march_batch(trac, amp)
@@ -445,16 +450,17 @@ def run_ours(args, dist):
     st = stats[dom]
     if dom == "conv_batch":
         # split-BF16 GEMM: 3 BF16 MMA products per useful FP32 product
+        kname_b = "k_conv_tc (tcgen05)" if args.engine == "tcgen05" else "k_conv_mma (mma.sync)"
         mma_tf = 3.0 * st["flops"] / (st["ms"] / 1e3) / 1e12
         gbs = st["bytes"] / (st["ms"] / 1e3) / 1e9
         f_t, f_h = mma_tf / peaks["bf16_tflops"], gbs / peaks["hbm_gbs"]
         if f_t >= f_h:
-            roof = {"bound": "tensor", "kernel": "k_conv_mma", "achieved": mma_tf,
+            roof = {"bound": "tensor", "kernel": kname_b, "achieved": mma_tf,
                     "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": f_t,
                     "peak_source": f"bf16_tflops of {peak_kind} (BF16 MMA flops, 3 per "
                                    "split product)", "hbm_frac": f_h, "hbm_gbs": gbs}
         else:
-            roof = {"bound": "hbm", "kernel": "k_conv_mma", "achieved": gbs,
+            roof = {"bound": "hbm", "kernel": kname_b, "achieved": gbs,
                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": f_h,
                     "peak_source": f"hbm_gbs of {peak_kind}", "tensor_frac": f_t,
                     "bf16_mma_tflops": mma_tf}
@@ -487,6 +493,8 @@ def run_ours(args, dist):
             "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": M,
                        "alpha": list(ALPHA), "precision": args.precision,
                        "parallelism": f"replicas{dist.world}", "load_cases": nc,
+                       "refine_sweeps": args.refine,
+                       "batch_engine": args.engine if cases else None,
                        "l2": "inputs larger than L2: the level store is "
                              f"{level_gb:.1f} GB"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
@@ -545,6 +553,10 @@ def main():
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the plain FP64 run that measures the mixed form's error")
     ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--refine", type=int, default=1,
+                    help="refinement sweeps of the mixed-precision solves (0..4)")
+    ap.add_argument("--engine", choices=["tcgen05", "mma_sync"], default="tcgen05",
+                    help="tensor-core engine of the batched convolution")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests of the serving stream reported beside the headline (0: off)")

@@ -167,6 +167,14 @@ int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
 int tdbem_march_batch(tdbem_ctx* ctx, int numstep, int nrhs, const double* traction,
                       const double* amp, double* u_hist, double* t_hist);
 
+/* Engine of the batched convolution: TDBEM_ENGINE_TCGEN05 (default; tcgen05.mma
+ * with TMEM accumulators, TMA-loaded BF16 hi/lo planes of the levels, which take
+ * as much device memory again as the FP32 levels) or TDBEM_ENGINE_MMA_SYNC
+ * (warp-level mma.sync splitting the FP32 levels on the fly, no extra memory). */
+#define TDBEM_ENGINE_TCGEN05 0
+#define TDBEM_ENGINE_MMA_SYNC 1
+int tdbem_set_batch_engine(tdbem_ctx* ctx, int engine);
+
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
  * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64
  * residual-refinement sweeps per solve (0..4; default 1). */

@@ -164,6 +164,9 @@ void free_levels(tdbem_ctx* c) {
     dfree(c->d_H01);
     c->level_precision = -1;
     c->levels_last = 0;
+    if (c->d_tc_planes) cudaFree(c->d_tc_planes);
+    c->d_tc_planes = nullptr;
+    c->tc_planes_valid = false;
 }
 
 void free_batch(tdbem_ctx* c) {
@@ -180,6 +183,10 @@ void free_batch(tdbem_ctx* c) {
     c->bpart_cap = 0;
     c->batch_C = 0;
     c->batch_steps = -1;
+    if (c->d_tc_W) cudaFree(c->d_tc_W);
+    c->d_tc_W = nullptr;
+    c->tc_W_bytes = 0;
+    dfree(c->d_tc_err);
 }
 
 void free_march(tdbem_ctx* c) {
@@ -868,6 +875,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
     CUDA_TRY(cudaGetLastError());
     prof_flush(c);
     c->levels_last = last;
+    c->tc_planes_valid = false;  // the BF16 planes follow the levels
     return TDBEM_OK;
 }
 
@@ -1001,7 +1009,8 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         CUDA_TRY(dalloc(&c->d_bWu, (size_t)(M + 1) * C * ldw));
         int smax = batch_apply_splits(D, C);
         for (int nlev = 2; nlev <= M + 1; nlev++)
-            smax = std::max(smax, batch_conv_splits(nlev, D, C));
+            smax = std::max(smax, std::max(batch_conv_splits(nlev, D, C),
+                                           tc_conv_splits(nlev, D, C)));
         c->bpart_cap = (size_t)smax * CD;
         CUDA_TRY(dalloc(&c->d_bpart, c->bpart_cap));
         CUDA_TRY(dalloc(&c->d_brhs, CD));
@@ -1023,6 +1032,31 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
     const int rc = mixed_inverses(c, numstep, lhs_c);
     if (rc != TDBEM_OK) return rc;
 
+    const bool tc = c->batch_engine == TDBEM_ENGINE_TCGEN05;
+    const int Lw = M + 1;
+    if (tc) {
+        if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 1));
+        CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), s));
+        if (!c->tc_planes_valid) {
+            if (!c->d_tc_planes) CUDA_TRY(cudaMalloc(&c->d_tc_planes, tc_plane_bytes(D, M + 1)));
+            const int pe = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_split_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_tc_planes, s));
+            prof_end(c, pe, 2.0 * (M + 1) * (double)D * (c->ldf + tc_ldb(D)) * 4, 0);
+            c->launches += 1;
+            c->tc_planes_valid = true;
+        }
+        const size_t wb = tc_w_bytes(D, C, Lw);
+        if (c->tc_W_bytes < wb) {
+            if (c->d_tc_W) cudaFree(c->d_tc_W);
+            c->d_tc_W = nullptr;
+            c->tc_W_bytes = 0;
+            CUDA_TRY(cudaMalloc(&c->d_tc_W, wb));
+            c->tc_W_bytes = wb;
+        }
+        if (!make_tc_maps(c->d_tc_planes, D, M + 1, c->d_tc_W, C, Lw, &c->tc_maps))
+            return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched planes");
+    }
+
     EventTimer tmr;
     tmr.start(s);
     const size_t lstride = (size_t)D * c->ldf;
@@ -1033,17 +1067,32 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         const int nlev = L + 1;
         const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
         const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-        CUDA_TRY(launch_build_w_batch(c->d_bu, c->d_bt, D, C, st, nlev, a1, a2, a3, c0, c1, d_amp,
-                                      numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map, ldw,
-                                      c->d_bWt, c->d_bWu, s));
-        const int splits = batch_conv_splits(nlev, D, C);
-        int pe = prof_begin(c, TDBEM_K_CONV_BATCH);
-        CUDA_TRY(launch_conv_mma(c->d_Gf, c->d_Hf, lstride, c->ldf, D, nlev, c->d_bWt, c->d_bWu,
-                                 ldw, C, c->d_bpart, splits, s));
-        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * C * ldw * 4,
-                 nlev * 4.0 * DD * C);
+        int pe;
+        if (tc) {
+            CUDA_TRY(launch_build_w_tc(c->d_bu, c->d_bt, D, C, st, nlev, Lw, a1, a2, a3, c0, c1,
+                                       d_amp, numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map,
+                                       c->d_tc_W, s));
+            const int splits = tc_conv_splits(nlev, D, C);
+            const double ldb = tc_ldb(D), cp = tc_cases_pad(C);
+            pe = prof_begin(c, TDBEM_K_CONV_BATCH);
+            CUDA_TRY(launch_conv_tc(c->tc_maps, D, M + 1, Lw, nlev, C, c->d_bpart, splits,
+                                    c->d_tc_err, s));
+            prof_end(c, pe, nlev * 2.0 * (double)D * ldb * 4 + nlev * 2.0 * cp * ldb * 4,
+                     nlev * 4.0 * DD * C);
+            CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
+        } else {
+            CUDA_TRY(launch_build_w_batch(c->d_bu, c->d_bt, D, C, st, nlev, a1, a2, a3, c0, c1,
+                                          d_amp, numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map,
+                                          ldw, c->d_bWt, c->d_bWu, s));
+            const int splits = batch_conv_splits(nlev, D, C);
+            pe = prof_begin(c, TDBEM_K_CONV_BATCH);
+            CUDA_TRY(launch_conv_mma(c->d_Gf, c->d_Hf, lstride, c->ldf, D, nlev, c->d_bWt,
+                                     c->d_bWu, ldw, C, c->d_bpart, splits, s));
+            prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * C * ldw * 4,
+                     nlev * 4.0 * DD * C);
+            CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
+        }
         pe = prof_begin(c, TDBEM_K_SOLVE_BATCH);
-        CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
         const int v = st == 1 ? 0 : 1;
         CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_brhs, C, c->d_bpart, sp, s));
         CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, nullptr, c->d_bx, s));
@@ -1060,6 +1109,14 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         c->launches += 6 + 4LL * c->n_refine;
     }
     c->timings[2] = tmr.stop_ms(s);
+    if (tc) {
+        int code = 0;
+        CUDA_TRY(cudaMemcpyAsync(&code, c->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (code)
+            return fail(TDBEM_ERR_CUDA,
+                        "tensor-core convolution: a pipeline wait timed out (code %d)", code);
+    }
     if (u_hist)
         CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_bu, sizeof(double) * (numstep + 1) * CD,
                                  cudaMemcpyDeviceToHost, s));
@@ -1068,6 +1125,14 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
                                  cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     prof_flush(c);
+    return TDBEM_OK;
+}
+
+int tdbem_set_batch_engine(tdbem_ctx* c, int engine) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (engine != TDBEM_ENGINE_TCGEN05 && engine != TDBEM_ENGINE_MMA_SYNC)
+        return fail(TDBEM_ERR_ARG, "unknown batch engine %d", engine);
+    c->batch_engine = engine;
     return TDBEM_OK;
 }
 

@@ -1,0 +1,493 @@
+// Batched history convolution on the 5th-generation tensor cores (tcgen05).
+//
+// Same product as k_conv_mma (batch.cu),
+//     partial[split][c][row] = sum_f ( G^f[row,:] . Wt[f][c] - H^f[row,:] . Wu[f][c] ),
+// with both operands pre-split into BF16 planes (x = hi + lo, hi = bf16(x),
+// lo = bf16(x - hi)) so that no conversion runs in the product kernel:
+//   level planes  [(mat*2 + plane)*L  + f][row][ldb]   mat 0 = G, 1 = H
+//   vector planes [(mat*2 + plane)*Lw + f][case][ldb]  mat 1 holds -Wu
+// with ldb = D rounded up to 64 (zero-padded K).
+//
+// One CTA owns a 128-row tile of all (<= 64) cases for a range of levels:
+//   warp 0      TMA producer: per stage a 128 x 64 tile of the hi and lo level
+//               planes and a 64 x 64 tile of the hi and lo vector planes
+//               (128-byte swizzle), completion counted on an mbarrier;
+//   warp 1      allocates 128 TMEM columns and issues tcgen05.mma
+//               (kind::f16, BF16 x BF16 -> FP32, M = 128, N = 64, K = 16):
+//               lo*hi + hi*lo + hi*hi per K step into the accumulator of the
+//               current level; tcgen05.commit frees the stage / hands the
+//               finished level to the epilogue;
+//   warps 2..5  epilogue: tcgen05.ld of a finished level's accumulator (double
+//               buffered in TMEM, columns 0-63 / 64-127), compensated (Kahan)
+//               FP32 sum over the levels, FP64 partial sums at the end.
+// Every mbarrier wait is bounded (%globaltimer); a wait that runs out sets an
+// error code, makes every role stop, and the CTA still drains its MMAs before
+// it frees TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+
+#include "tdbem_internal.cuh"
+
+namespace tdbem {
+
+namespace {
+
+constexpr int TC_BM = 128, TC_BN = 64, TC_BK = 64, TC_STAGES = 4;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;                      // 16 KiB
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;                      // 8 KiB
+constexpr int TC_STAGE_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;    // 48 KiB
+constexpr int TC_THREADS = 192;
+constexpr int TC_TMEM_COLS = 128;
+constexpr int TC_NBAR = 2 * TC_STAGES + 5;  // full, empty, tmem full x2, tmem empty x2, done
+constexpr int TC_SMEM = 1024 + TC_STAGES * TC_STAGE_BYTES + TC_NBAR * 8 + 16;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+// Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
+// (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) |
+                            ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of `parity`: false when it runs out (error code
+// recorded, every role told to stop) or when another role has stopped.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
+                          int code, bool honour_abort = true) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    while (true) {
+        if (honour_abort && *abort_flag) return false;
+        if (mbar_try(bar, parity)) return true;
+        if (gtimer() - t0 > kWaitNs) {
+            *abort_flag = 1;
+            atomicExch(err, code);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// start address >> 4 (bits 0-13), leading byte offset 16 B (unused for this
+// layout), stride byte offset 1024 B between 8-row groups (bits 32-45),
+// descriptor version 1 (bits 46-47), swizzle mode 128 B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) |
+           ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::
+                     "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+        "%11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              int D, int L, int Lw, int nlev, int per_split, int nk, int C,
+              double* __restrict__ partial, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+    const uint32_t sbase = smem_u32(base);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + TC_STAGES * TC_STAGE_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + TC_NBAR);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    auto bar = [&](int i) { return smem_u32(bars + i); };
+    const int FULL = 0, EMPTY = TC_STAGES, TFULL = 2 * TC_STAGES, TEMPTY = 2 * TC_STAGES + 2,
+              DONE = 2 * TC_STAGES + 4;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = blockIdx.x * TC_BM;
+    const int f0 = blockIdx.y * per_split;
+    const int nlv = max(0, min(nlev, f0 + per_split) - f0);
+    const int c0 = blockIdx.z * TC_BN;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; s++) {
+            mbar_init(bar(FULL + s), 1);
+            mbar_init(bar(EMPTY + s), 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            mbar_init(bar(TFULL + b), 1);
+            mbar_init(bar(TEMPTY + b), 128);
+        }
+        mbar_init(bar(DONE), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {  // ---------------- TMA producer
+            int it = 0;
+            bool ok = true;
+            for (int j = 0; j < nlv && ok; j++) {
+                const int f = f0 + j;
+                for (int mat = 0; mat < 2 && ok; mat++)
+                    for (int kc = 0; kc < nk && ok; kc++, it++) {
+                        const int s = it % TC_STAGES, n = it / TC_STAGES;
+                        if (n >= 1 && !mbar_wait(bar(EMPTY + s), (n - 1) & 1, abort_flag, err, 1)) {
+                            ok = false;
+                            break;
+                        }
+                        const uint32_t st = sbase + s * TC_STAGE_BYTES;
+                        mbar_expect_tx(bar(FULL + s), TC_STAGE_BYTES);
+                        const int x = kc * TC_BK;
+                        tma_load_3d(st, &tmA, x, row0, (mat * 2 + 0) * L + f, bar(FULL + s));
+                        tma_load_3d(st + TC_A_BYTES, &tmA, x, row0, (mat * 2 + 1) * L + f,
+                                    bar(FULL + s));
+                        tma_load_3d(st + 2 * TC_A_BYTES, &tmB, x, c0, (mat * 2 + 0) * Lw + f,
+                                    bar(FULL + s));
+                        tma_load_3d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, x, c0,
+                                    (mat * 2 + 1) * Lw + f, bar(FULL + s));
+                    }
+            }
+            // every issued copy has landed before the CTA can exit
+            for (int k = std::max(0, it - TC_STAGES); k < it; k++)
+                mbar_wait(bar(FULL + k % TC_STAGES), (k / TC_STAGES) & 1, abort_flag, err, 5,
+                          false);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // ---------------- MMA issuer
+            int it = 0;
+            bool ok = true;
+            for (int j = 0; j < nlv && ok; j++) {
+                const int b = j & 1, u = j >> 1;
+                if (u >= 1 && !mbar_wait(bar(TEMPTY + b), (u - 1) & 1, abort_flag, err, 2)) break;
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + (uint32_t)(b * TC_BN);
+                uint32_t acc = 0;
+                for (int mat = 0; mat < 2 && ok; mat++)
+                    for (int kc = 0; kc < nk; kc++, it++) {
+                        const int s = it % TC_STAGES, n = it / TC_STAGES;
+                        if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint32_t ah = sbase + s * TC_STAGE_BYTES, al = ah + TC_A_BYTES;
+                        const uint32_t bh = ah + 2 * TC_A_BYTES, bl = bh + TC_B_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < TC_BK / 16; kk++) {
+                            const uint32_t o = kk * 32;  // 16 BF16 along K inside the swizzle atom
+                            umma_bf16(d_tmem, sw128_desc(al + o), sw128_desc(bh + o), acc);
+                            umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bl + o), 1);
+                            umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bh + o), 1);
+                            acc = 1;
+                        }
+                        umma_commit(bar(EMPTY + s));
+                    }
+                if (ok) umma_commit(bar(TFULL + b));
+            }
+            // all MMAs of this thread complete before TMEM is released
+            umma_commit(bar(DONE));
+            mbar_wait(bar(DONE), 0, abort_flag, err, 6, false);
+        }
+    } else {  // ---------------- epilogue, warps 2..5 -> TMEM lanes 32 * (warp % 4)
+        const int q = warp & 3;
+        float sum[TC_BN], cmp[TC_BN];
+#pragma unroll
+        for (int i = 0; i < TC_BN; i++) sum[i] = cmp[i] = 0.f;
+        for (int j = 0; j < nlv; j++) {
+            const int b = j & 1, u = j >> 1;
+            if (!mbar_wait(bar(TFULL + b), u & 1, abort_flag, err, 4)) break;
+            tc_fence_after();
+#pragma unroll
+            for (int ch = 0; ch < TC_BN / 16; ch++) {
+                float v[16];
+                tmem_ld16(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * TC_BN + ch * 16),
+                          v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int k = ch * 16 + i;
+                    const float y = __fsub_rn(v[i], cmp[k]);
+                    const float t = __fadd_rn(sum[k], y);
+                    cmp[k] = __fsub_rn(__fsub_rn(t, sum[k]), y);
+                    sum[k] = t;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(bar(TEMPTY + b));
+        }
+        const int row = row0 + q * 32 + lane;
+        const int Cl = min(TC_BN, C - c0);
+        if (row < D) {
+#pragma unroll
+            for (int k = 0; k < TC_BN; k++)
+                if (k < Cl)
+                    partial[((size_t)blockIdx.y * C + c0 + k) * D + row] =
+                        (double)sum[k] - (double)cmp[k];
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+    }
+}
+
+// FP32 level store [f][row][ldf] -> BF16 hi/lo planes [(mat*2+plane)*L + f][row][ldb].
+__global__ void k_split_levels(const float* __restrict__ Gf, const float* __restrict__ Hf,
+                               int ldf, int D, int L, int ldb, __nv_bfloat16* __restrict__ P) {
+    const size_t per_mat = (size_t)L * D * ldb;
+    const size_t plane = per_mat;  // one (mat, plane) block = L * D * ldb
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < 2 * per_mat;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int mat = (int)(idx / per_mat);
+        const size_t r = idx % per_mat;
+        const int k = (int)(r % ldb);
+        const size_t fr = r / ldb;  // f * D + row
+        float x = 0.f;
+        if (k < D) x = (mat == 0 ? Gf : Hf)[fr * ldf + k];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(x, __bfloat162float(hi)));
+        P[(size_t)(mat * 2) * plane + r] = hi;
+        P[(size_t)(mat * 2 + 1) * plane + r] = lo;
+    }
+}
+
+// Batched history vectors of step s as BF16 hi/lo planes
+// [(mat*2+plane)*Lw + f][c][ldb] (c < Cpad, zero beyond C and D; mat 1 = -Wu).
+// The combination is that of k_build_w_batch (batch.cu).
+__global__ void k_build_w_tc(const double* __restrict__ u_hist, const double* __restrict__ t_hist,
+                             int D, int C, int Cpad, int s, int nlev, int Lw, double a1, double a2,
+                             double a3, double c0, double c1, const double* __restrict__ amp,
+                             int numstep, const double* __restrict__ traction,
+                             const unsigned char* __restrict__ is_u,
+                             const double* __restrict__ ubc_val, int ldb,
+                             __nv_bfloat16* __restrict__ W) {
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const size_t plane = (size_t)Lw * Cpad * ldb;
+    const size_t cs = (size_t)C * D;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % ldb);
+        const int c = (int)((idx / ldb) % Cpad);
+        const int f = (int)(idx / ((size_t)ldb * Cpad));
+        double wt = 0, wu = 0;
+        if (k < D && c < C) {
+            const size_t o = (size_t)c * D + k;
+            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+            if (f >= 2 && m1 >= 1) {
+                wt += a1 * t_hist[m1 * cs + o];
+                wu += a1 * u_hist[m1 * cs + o];
+            }
+            if (f >= 1 && m3 >= 1) {
+                wt += a3 * t_hist[m3 * cs + o];
+                wu += a3 * u_hist[m3 * cs + o];
+            }
+            if (m2 >= 1) {
+                wt += a2 * t_hist[m2 * cs + o];
+                wu += a2 * u_hist[m2 * cs + o];
+            }
+            if (f <= 1) {
+                const double cf = f == 0 ? c0 : c1;
+                if (f == 0 && s - 1 >= 1) {
+                    wt -= a1 * t_hist[(size_t)(s - 1) * cs + o];
+                    wu -= a1 * u_hist[(size_t)(s - 1) * cs + o];
+                }
+                const double a = amp ? amp[(size_t)c * numstep + s] : 1.0;
+                if (is_u[k]) wu += cf * ubc_val[k];
+                else wt += cf * (a * traction[o]);
+            }
+        }
+        const double vals[2] = {wt, -wu};
+#pragma unroll
+        for (int mat = 0; mat < 2; mat++) {
+            const float xf = (float)vals[mat];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+            const __nv_bfloat16 lo =
+                __float2bfloat16_rn((float)(vals[mat] - (double)__bfloat162float(hi)));
+            W[(size_t)(mat * 2) * plane + idx] = hi;
+            W[(size_t)(mat * 2 + 1) * plane + idx] = lo;
+        }
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 3-D BF16 tensor [slabs][rows][ldb] with a 64 x box_rows x 1 box, 128-byte swizzle.
+bool encode_map(void* map, void* gaddr, int ldb, int rows, int slabs, int box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)ldb, (cuuint64_t)rows, (cuuint64_t)slabs};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldb * 2, (cuuint64_t)rows * ldb * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return fn(static_cast<CUtensorMap*>(map), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, gaddr, dims,
+              strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+}  // namespace
+
+static_assert(sizeof(CUtensorMap) == kTensorMapBytes, "tensor map size");
+
+int tc_ldb(int D) { return (D + TC_BK - 1) / TC_BK * TC_BK; }
+int tc_cases_pad(int C) { return (C + TC_BN - 1) / TC_BN * TC_BN; }
+
+int tc_conv_splits(int nlev, int D, int C) {
+    const int tiles = (D + TC_BM - 1) / TC_BM * ((C + TC_BN - 1) / TC_BN);
+    return std::max(1, std::min(nlev, 152 / std::max(1, tiles)));
+}
+
+cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
+                                void* planes, cudaStream_t s) {
+    const size_t total = 2 * (size_t)L * D * tc_ldb(D);
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 152 * 16);
+    k_split_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, tc_ldb(D),
+                                        static_cast<__nv_bfloat16*>(planes));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D, int C, int s,
+                              int nlev, int Lw, double a1, double a2, double a3, double c0,
+                              double c1, const double* amp, int numstep, const double* traction,
+                              const unsigned char* is_u, const double* ubc_val, void* W,
+                              cudaStream_t st) {
+    const int Cpad = tc_cases_pad(C), ldb = tc_ldb(D);
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
+    k_build_w_tc<<<grid, 256, 0, st>>>(u_hist, t_hist, D, C, Cpad, s, nlev, Lw, a1, a2, a3, c0,
+                                       c1, amp, numstep, traction, is_u, ubc_val, ldb,
+                                       static_cast<__nv_bfloat16*>(W));
+    return cudaGetLastError();
+}
+
+bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out) {
+    const int ldb = tc_ldb(D);
+    return encode_map(out->a, planes, ldb, D, 4 * L, TC_BM) &&
+           encode_map(out->b, W, ldb, tc_cases_pad(C), 4 * Lw, TC_BN);
+}
+
+cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
+                           double* partial, int splits, int* d_err, cudaStream_t s) {
+    static unsigned long long attr_set = 0;  // devices with the shared-memory attribute set
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!(attr_set & (1ull << dev))) {
+        e = cudaFuncSetAttribute(k_conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set |= 1ull << dev;
+    }
+    if (splits < 1 || nlev < 1) return cudaErrorInvalidValue;
+    CUtensorMap ma, mb;
+    std::memcpy(&ma, maps.a, sizeof(ma));
+    std::memcpy(&mb, maps.b, sizeof(mb));
+    const int per = (nlev + splits - 1) / splits;
+    dim3 grid((D + TC_BM - 1) / TC_BM, splits, (C + TC_BN - 1) / TC_BN);
+    k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, per, tc_ldb(D) / TC_BK, C,
+                                                partial, d_err);
+    return cudaGetLastError();
+}
+
+size_t tc_plane_bytes(int D, int L) { return 4 * (size_t)L * D * tc_ldb(D) * 2; }
+size_t tc_w_bytes(int D, int C, int Lw) { return 4 * (size_t)Lw * tc_cases_pad(C) * tc_ldb(D) * 2; }
+
+}  // namespace tdbem

@@ -120,6 +120,28 @@ cudaError_t launch_update_state(const double* x, int D, int s, const unsigned ch
                                 double* t_hist, cudaStream_t st);
 int conv_chunks(int L, int D);
 
+// Batched convolution on tcgen05 tensor cores (conv_tc.cu).
+constexpr int kTensorMapBytes = 128;
+struct TcMaps {
+    alignas(64) unsigned char a[kTensorMapBytes];  // BF16 level planes
+    alignas(64) unsigned char b[kTensorMapBytes];  // BF16 history-vector planes
+};
+int tc_ldb(int D);
+int tc_cases_pad(int C);
+int tc_conv_splits(int nlev, int D, int C);
+size_t tc_plane_bytes(int D, int L);
+size_t tc_w_bytes(int D, int C, int Lw);
+cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
+                                void* planes, cudaStream_t s);
+cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D, int C, int s,
+                              int nlev, int Lw, double a1, double a2, double a3, double c0,
+                              double c1, const double* amp, int numstep, const double* traction,
+                              const unsigned char* is_u, const double* ubc_val, void* W,
+                              cudaStream_t st);
+bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out);
+cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
+                           double* partial, int splits, int* d_err, cudaStream_t s);
+
 // Sets the calling thread's tdbem_last_error() message (capi.cu).
 void note_error(const char* msg);
 
@@ -227,6 +249,13 @@ struct tdbem_ctx {
     double* d_brhs = nullptr;       // C x D
     double* d_bx = nullptr;
     double* d_br = nullptr;
+    int batch_engine = TDBEM_ENGINE_TCGEN05;
+    void* d_tc_planes = nullptr;    // BF16 hi/lo planes of the FP32 levels
+    bool tc_planes_valid = false;
+    void* d_tc_W = nullptr;         // BF16 hi/lo planes of the batched history vectors
+    size_t tc_W_bytes = 0;
+    int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
+    tdbem::TcMaps tc_maps{};
 
     // boundary conditions and marching parameters
     std::vector<int> ubc, fbc;

@@ -5,7 +5,7 @@ that case's traction list and load history.  Tolerances: relative L2 error
 <= 1e-4 against the plain FP64 GPU form (itself parity-tested against the
 oracle at 1e-10) over all steps and dofs of the case; duplicated cases in
 different column blocks are bitwise equal; the batch is linear in its loads to
-1e-9 of the history norm."""
+1e-4 of the history norm; the tcgen05 and mma.sync engines agree to 1e-5."""
 import numpy as np
 import pytest
 
@@ -39,10 +39,11 @@ def single(lib, m, trac_row, amp_row, precision, alpha):
         return ctx.march()
 
 
-def batch(lib, m, trac, amp, alpha, refine=1):
+def batch(lib, m, trac, amp, alpha, refine=1, engine=0):
     with lib.Context(m) as ctx:
         ctx.set_alpha(*alpha)
         ctx.set_march_options(12, refine)
+        ctx.set_batch_engine(engine)
         ctx.assemble(precision=lib.MIXED)
         return ctx.march_batch(trac, amp)
 
@@ -70,10 +71,11 @@ def bar_cases():
     return m, trac, amp
 
 
-def test_batch_cases_match_single_fp64_bar(tdlib, bar_cases):
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
+def test_batch_cases_match_single_fp64_bar(tdlib, bar_cases, engine):
     m, trac, amp = bar_cases
     alpha = (0.25, 0.1)
-    ub, tb = batch(tdlib, m, trac, amp, alpha)
+    ub, tb = batch(tdlib, m, trac, amp, alpha, engine=engine)
     assert ub.shape == (m.numstep + 1, 3, 3 * m.nnd)
     for c in range(3):
         u, t = single(tdlib, m, trac[c], amp[c], tdlib.FP64, alpha)
@@ -81,20 +83,36 @@ def test_batch_cases_match_single_fp64_bar(tdlib, bar_cases):
         assert rel_l2(tb[:, c], t) <= TOL_L2, c
 
 
-def test_batch_gaussian_patches_sphere(tdlib):
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
+def test_batch_gaussian_patches_sphere(tdlib, engine):
     """Seeded Gaussian pulses on random 4-element patches of a 6x8x8 sphere."""
     from tdbem import loads, meshes
     m = meshes.cubed_sphere(8, numstep=120)
     trac, amp = loads.gaussian_patch_cases(m, 6, seed=0)
     alpha = (0.25, 0.0)
-    ub, tb = batch(tdlib, m, trac, amp, alpha)
+    ub, tb = batch(tdlib, m, trac, amp, alpha, engine=engine)
     for c in (0, 3, 5):
         u, t = single(tdlib, m, trac[c], amp[c], tdlib.FP64, alpha)
         assert rel_l2(ub[:, c], u) <= TOL_L2, c
         assert rel_l2(tb[:, c], t) <= TOL_L2, c
 
 
-def test_batch_column_blocks_and_linearity(tdlib, bar_cases):
+def test_batch_engines_agree(tdlib):
+    """tcgen05 and mma.sync compute the same split-BF16 products in different
+    orders: the histories agree to 1e-5 of their norm; rows past a 128-row
+    tile edge (D = 1158) and 70 cases (two column blocks) included."""
+    from tdbem import loads, meshes
+    m = meshes.cubed_sphere(8, numstep=60)
+    trac, amp = loads.gaussian_patch_cases(m, 70, seed=4, numstep=60)
+    u0, _ = batch(tdlib, m, trac, amp, (0.25, 0.0), engine=0)
+    u1, _ = batch(tdlib, m, trac, amp, (0.25, 0.0), engine=1)
+    assert np.linalg.norm(u0 - u1) <= 1e-5 * np.linalg.norm(u1)
+    for c in (0, 63, 64, 69):
+        assert np.linalg.norm(u0[:, c] - u1[:, c]) <= 1e-5 * np.linalg.norm(u1[:, c])
+
+
+@pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
+def test_batch_column_blocks_and_linearity(tdlib, bar_cases, engine):
     """70 cases span two column blocks of 64: cases 64..69 repeat cases 0..5 and
     must come out bitwise equal; case 6 = case 0 + case 2 (same amplitude)."""
     m, trac3, amp3 = bar_cases
@@ -105,7 +123,7 @@ def test_batch_column_blocks_and_linearity(tdlib, bar_cases):
     trac[0], trac[2] = trac3[0], trac3[2]
     trac[6] = trac[0] + trac[2]
     trac[64:70] = trac[0:6]
-    ub, tb = batch(tdlib, m, trac, amp, (0.25, 0.1))
+    ub, tb = batch(tdlib, m, trac, amp, (0.25, 0.1), engine=engine)
     assert np.array_equal(ub[:, 64:70], ub[:, 0:6])
     assert np.array_equal(tb[:, 64:70], tb[:, 0:6])
     lin = ub[:, 0] + ub[:, 2]
