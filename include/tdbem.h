@@ -160,20 +160,23 @@ int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
  * SolverT::SetLoad (SolverT.cpp:344-377) per case; the reference has no batched
  * form.  Each step's convolution of all cases is one tensor-core GEMM (split
  * BF16 products, FP32 accumulation, compensated sum over levels); the solve
- * applies the FP32 inverse with tdbem_set_march_options' refinement sweeps
+ * applies the FP32 inverse with tdbem_set_batch_options' refinement sweeps
  * (residual in FP32 double-word arithmetic against the FP64 LHS).
  * u_hist / t_hist: host buffers of (numstep+1) x nrhs x D doubles,
  * [step][case][dof], or NULL. */
 int tdbem_march_batch(tdbem_ctx* ctx, int numstep, int nrhs, const double* traction,
                       const double* amp, double* u_hist, double* t_hist);
 
-/* Engine of the batched convolution: TDBEM_ENGINE_TCGEN05 (default; tcgen05.mma
- * with TMEM accumulators, TMA-loaded BF16 hi/lo planes of the levels, which take
- * as much device memory again as the FP32 levels) or TDBEM_ENGINE_MMA_SYNC
- * (warp-level mma.sync splitting the FP32 levels on the fly, no extra memory). */
+/* Options of tdbem_march_batch.  engine: TDBEM_ENGINE_TCGEN05 (default;
+ * tcgen05.mma with TMEM accumulators, TMA-loaded BF16 hi/lo planes of the
+ * levels, which take as much device memory again as the FP32 levels) or
+ * TDBEM_ENGINE_MMA_SYNC (warp-level mma.sync splitting the FP32 levels on the
+ * fly, no extra memory).  refine_sweeps (0..4, default 0): refinement sweeps of
+ * the batched solve; the split-BF16 convolution, not the FP32 inverse, sets the
+ * batched form's error, so the default skips them. */
 #define TDBEM_ENGINE_TCGEN05 0
 #define TDBEM_ENGINE_MMA_SYNC 1
-int tdbem_set_batch_engine(tdbem_ctx* ctx, int engine);
+int tdbem_set_batch_options(tdbem_ctx* ctx, int engine, int refine_sweeps);
 
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
  * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64

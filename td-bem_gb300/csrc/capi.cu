@@ -1096,7 +1096,7 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         const int v = st == 1 ? 0 : 1;
         CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_brhs, C, c->d_bpart, sp, s));
         CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, nullptr, c->d_bx, s));
-        for (int it = 0; it < c->n_refine; it++) {
+        for (int it = 0; it < c->batch_refine; it++) {
             CUDA_TRY(launch_apply_cols(c->d_Hc64[v], 1, D, c->d_bx, C, c->d_bpart, sp, s));
             CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_brhs, c->d_br, s));
             CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_br, C, c->d_bpart, sp, s));
@@ -1104,9 +1104,9 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         }
         CUDA_TRY(launch_update_batch(c->d_bx, D, C, st, c->d_is_ubc, c->d_ubc_map, c->d_btrac,
                                      d_amp, numstep, c->d_bu, c->d_bt, s));
-        prof_end(c, pe, DD * 4 * (1 + c->n_refine) + DD * 8 * c->n_refine,
-                 2.0 * DD * C * (1 + 2 * c->n_refine));
-        c->launches += 6 + 4LL * c->n_refine;
+        prof_end(c, pe, DD * 4 * (1 + c->batch_refine) + DD * 8 * c->batch_refine,
+                 2.0 * DD * C * (1 + 2 * c->batch_refine));
+        c->launches += 6 + 4LL * c->batch_refine;
     }
     c->timings[2] = tmr.stop_ms(s);
     if (tc) {
@@ -1128,11 +1128,14 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
     return TDBEM_OK;
 }
 
-int tdbem_set_batch_engine(tdbem_ctx* c, int engine) {
+int tdbem_set_batch_options(tdbem_ctx* c, int engine, int refine_sweeps) {
     if (!c) return fail(TDBEM_ERR_ARG, "null context");
     if (engine != TDBEM_ENGINE_TCGEN05 && engine != TDBEM_ENGINE_MMA_SYNC)
         return fail(TDBEM_ERR_ARG, "unknown batch engine %d", engine);
+    if (refine_sweeps < 0 || refine_sweeps > 4)
+        return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
     c->batch_engine = engine;
+    c->batch_refine = refine_sweeps;
     return TDBEM_OK;
 }
 

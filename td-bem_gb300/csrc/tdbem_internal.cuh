@@ -250,6 +250,7 @@ struct tdbem_ctx {
     double* d_bx = nullptr;
     double* d_br = nullptr;
     int batch_engine = TDBEM_ENGINE_TCGEN05;
+    int batch_refine = 0;           // refinement sweeps of the batched solve
     void* d_tc_planes = nullptr;    // BF16 hi/lo planes of the FP32 levels
     bool tc_planes_valid = false;
     void* d_tc_W = nullptr;         // BF16 hi/lo planes of the batched history vectors

@@ -57,7 +57,7 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp]),
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
-    "tdbem_set_batch_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_footprint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_size_t)]),
@@ -271,8 +271,8 @@ class Context:
     def set_march_options(self, block_steps: int = 12, refine_sweeps: int = 1):
         _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
 
-    def set_batch_engine(self, engine: int):
-        _check(load().tdbem_set_batch_engine(self.h, engine))
+    def set_batch_options(self, engine: int = 0, refine_sweeps: int = 0):
+        _check(load().tdbem_set_batch_options(self.h, engine, refine_sweeps))
 
     def set_load_history(self, amp):
         self._amp = np.ascontiguousarray(amp, np.float64)

@@ -39,11 +39,10 @@ def single(lib, m, trac_row, amp_row, precision, alpha):
         return ctx.march()
 
 
-def batch(lib, m, trac, amp, alpha, refine=1, engine=0):
+def batch(lib, m, trac, amp, alpha, refine=0, engine=0):
     with lib.Context(m) as ctx:
         ctx.set_alpha(*alpha)
-        ctx.set_march_options(12, refine)
-        ctx.set_batch_engine(engine)
+        ctx.set_batch_options(engine, refine)
         ctx.assemble(precision=lib.MIXED)
         return ctx.march_batch(trac, amp)
 
