@@ -151,6 +151,27 @@ int tdbem_set_load_history(tdbem_ctx* ctx, const double* amp, int nsteps);
  * or NULL to keep the histories on the device only. */
 int tdbem_march(tdbem_ctx* ctx, int numstep, double* u_hist, double* t_hist);
 
+/* ---- stepwise form of main()'s loop (the C++ host classes use these) ---- */
+
+/* SolverStepLinearT::UpdateGHLinear (SolverStepLinearT.cpp:58-175) for host row
+ * blocks of one step, rows 3*node_lo .. 3*node_hi+2 of D columns, row-major:
+ * G_I / H_I (ElastoDynamicsT's fG_1 / fH_1, the I part) go to level `step`,
+ * G_J / H_J (fG_2 / fH_2, the J part) to level step-1 (inserted at step 1,
+ * added after).  Steps beyond MaxStep are ignored, as in the reference.  Builds
+ * the FP64 level store that tdbem_march and tdbem_march_step read. */
+int tdbem_update_gh_linear(tdbem_ctx* ctx, int step, int node_lo, int node_hi, const double* G_I,
+                           const double* G_J, const double* H_I, const double* H_J);
+
+/* Stepwise marching on FP64 levels.  tdbem_march_begin allocates and zeroes the
+ * histories of numstep steps (SolverT::Initialize, SolverT::SetTimeControl);
+ * tdbem_march_step runs SetLoad + Solve(a1, a2) of main()'s step curr_step
+ * (1..numstep; step 1 does nothing, step n >= 2 solves history n-1 as
+ * Solve_Averaging, SolverStepLinearT.cpp:314-544) on the levels present and
+ * copies history curr_step-1 to u / t (D doubles each, or NULL), the vectors
+ * RecordResult prints (SolverStepLinearT.cpp:549-603). */
+int tdbem_march_begin(tdbem_ctx* ctx, int numstep);
+int tdbem_march_step(tdbem_ctx* ctx, int curr_step, double* u, double* t);
+
 /* Batched marching of nrhs load cases on this context's mesh, boundary
  * conditions, weights and (TDBEM_MIXED) levels: tdbem_march run for every case
  * at once.  Case c's known traction at step s is amp[c*numstep + s] *
@@ -191,6 +212,22 @@ int tdbem_history_device(const tdbem_ctx* ctx, const double** u_hist, const doub
 
 /* Device bytes the level store of this context takes at a precision. */
 int tdbem_level_bytes(const tdbem_ctx* ctx, int precision, size_t* bytes);
+
+/* Binary checkpoint of the level store: a 64-byte header (magic "TDBEMLVL",
+ * version 1, D, MaxStep, precision, levels held, row stride) and the raw levels
+ * (FP64: G then H, (M+1) x D x D; TDBEM_MIXED: FP32 G then H, (M+1) x D x ld,
+ * then the FP64 levels 0-1 of G and H).  Import needs a context of the same
+ * mesh size (D and MaxStep) and replaces its levels.  The reference keeps its
+ * levels in memory only; this is the resume point that saves the assembly. */
+int tdbem_export_levels(tdbem_ctx* ctx, const char* path);
+int tdbem_import_levels(tdbem_ctx* ctx, const char* path);
+
+/* SolverT::WriteGH (SolverT.cpp:670-732) on one rank: writes
+ * <name_prefix><step>.txt with num_row lines of num_column values (row stride
+ * num_column), each "%15.5e", the file the reference's FE-BE coupling reads
+ * (FE-BE Matlab/BE_Matrices/ReadGH.m). */
+int tdbem_write_gh(const char* name_prefix, int step, int num_row, int num_column,
+                   const double* data);
 
 /* Timing of the phases of the last assemble / march, in milliseconds of
  * device time (CUDA events on the context stream): [0] assembly,

@@ -1,0 +1,164 @@
+// C++ host classes of tdbem-gb300 with the reference's interfaces.
+//
+// They mirror the classes main.cpp drives (src/main.cpp:42-130) so that its
+// sequence runs unchanged on the GPU:
+//   ModelManagerT        ModelManagerT.h:16-196 (input reading and getters)
+//   ElastoDynamicsGpuT   ElastoDynamicsT.h:22-39 (G_H_Driver, GetGHLinear)
+//   SolverStepLinearGpuT SolverT.h:22-128 / SolverStepLinearT (SetTimeControl,
+//                        Initialize, GetMaxStep, UpdateGHLinear, SetLoad,
+//                        Solve, RecordResult, WriteGH)
+// Names, argument meaning and error behaviour follow the reference: failures
+// throw `const char*` (the message stays valid until the next failure on this
+// thread), as main.cpp catches.  Everything runs on one GPU through the C ABI of
+// tdbem.h; the classes live in namespace tdbem so that they can be linked next
+// to the reference's own classes.
+//
+// G_H_Driver assembles a step's row blocks on the device and GetGHLinear returns
+// host copies of them (the reference's pointers, valid until the next
+// G_H_Driver); UpdateGHLinear places host row blocks into the solver's device
+// level store and Solve marches one step on the device.  An ElastoDynamicsGpuT
+// built with a SolverStepLinearGpuT shares its device context (one copy of the
+// mesh and quadrature tables).  The whole-run path without per-step host copies
+// is tdbem_assemble_levels + tdbem_march (tdbem_run --fast).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "tdbem.h"
+
+namespace tdbem {
+
+class ModelManagerT {
+   public:
+    ModelManagerT() = default;
+
+    // InputT::ReadInput (InputT.cpp:84-994): the keyword format, tokens split at
+    // " \t=;,", integers by atoi and reals by atof, 1-based ids in the file.
+    void ReadInput(const char* name);
+
+    int GetFormulation() { return formulation_; }
+    int GetNumStep() { return numstep_; }
+    void SetNumStep(int n) { numstep_ = n; }
+    double GetDT() { return dt_; }
+    void SetDT(double dt) { dt_ = dt; }
+    int GetTimeInterpolation() { return interpolation_; }
+    int GetNQ() { return nq_; }
+    int GetSD() { return sd_; }
+    int GetIfExt() { return if_ext_; }
+    int GetNND() { return nnd_; }
+    int GetElementType() { return etype_; }
+    int GetENND() { return ennd_; }
+    int GetNEL() { return nel_; }
+    const int* GetIEN() { return ien_.data(); }
+    const double* GetCoords() { return coords_.data(); }
+    void GetMaterialConstants(double& E, double& nu, double& rho) {
+        E = E_;
+        nu = nu_;
+        rho = rho_;
+    }
+    void SetMaterialConstants(double E, double nu, double rho) {
+        E_ = E;
+        nu_ = nu;
+        rho_ = rho;
+    }
+    void BoundaryCondition_Global(int& UBC_num, int** UBC_DOFs, double** UBC_Values,
+                                  int& FBC_num, int** FBC_DOFs, double** FBC_Values);
+    void SetBCs(int UBC_num, const int* UBC_DOFs, const double* UBC_values, int FBC_num,
+                const int* FBC_DOFs, const double* FBC_values);
+    int GetNumInterface() { return (int)interface_.size(); }
+    const int* GetInterface() { return interface_.data(); }
+    // Single process: every dof is local (ModelManagerT::Distributed_BC keeps all).
+    void Distributed_BC(int, int) {}
+
+    // The C-ABI views of the model.
+    tdbem_mesh Mesh() const;
+    tdbem_material Material() const;
+
+   private:
+    int formulation_ = 1, numstep_ = 1, interpolation_ = 1, nq_ = 6, sd_ = 3, if_ext_ = 0;
+    int nnd_ = 0, nel_ = 0, etype_ = 1, ennd_ = 4;
+    double dt_ = 0, E_ = 1, nu_ = 0, rho_ = 1;
+    std::vector<double> coords_;
+    std::vector<int> ien_;
+    std::vector<int> ubc_dof_, fbc_dof_, interface_;
+    std::vector<double> ubc_val_, fbc_val_;
+};
+
+class SolverStepLinearGpuT;
+
+class ElastoDynamicsGpuT {
+   public:
+    // Own device context for the model.
+    explicit ElastoDynamicsGpuT(ModelManagerT* model);
+    // Shares the solver's device context.
+    ElastoDynamicsGpuT(ModelManagerT* model, SolverStepLinearGpuT* solver);
+    ~ElastoDynamicsGpuT();
+    ElastoDynamicsGpuT(const ElastoDynamicsGpuT&) = delete;
+    ElastoDynamicsGpuT& operator=(const ElastoDynamicsGpuT&) = delete;
+
+    void SetLowerUpper(int lower, int upper);
+    // G_H_Driver (ElastoDynamicsT.cpp:108-231) at time t = n * t_1.
+    void G_H_Driver(double t, double t_1);
+    // The step's I parts (G_1, H_1) and J parts (G_2, H_2), rows of the node range.
+    void GetGHLinear(double** G_1, double** G_2, double** H_1, double** H_2);
+
+    int Step() const { return step_; }
+    tdbem_ctx* Context() const { return ctx_; }
+
+   private:
+    ModelManagerT* model_;
+    tdbem_ctx* ctx_ = nullptr;
+    bool own_ctx_ = false;
+    int lo_ = 0, hi_ = -1, step_ = 0;
+    std::vector<double> G1_, G2_, H1_, H2_;
+};
+
+class SolverStepLinearGpuT {
+   public:
+    explicit SolverStepLinearGpuT(ModelManagerT* model);
+    ~SolverStepLinearGpuT();
+    SolverStepLinearGpuT(const SolverStepLinearGpuT&) = delete;
+    SolverStepLinearGpuT& operator=(const SolverStepLinearGpuT&) = delete;
+
+    void GetNodeLowHigh(int* low, int* high);
+    void GetDofLowHigh(int* low, int* high);
+    void SetTimeControl(double dt, int num_steps);
+    void Initialize();
+    int GetMaxStep();
+    void SetCurrStep(int curr_step);
+    // Row blocks of the current step (SolverStepLinearT.cpp:58-175): G_0 / H_0 the
+    // I parts, G_1 / H_1 the J parts, as main.cpp passes GetGHLinear's outputs.
+    void UpdateGHLinear(const double* G_0, const double* G_1, const double* H_0,
+                        const double* H_1);
+    void SetLoad();
+    void Solve(double a1, double a2);
+    // One line per step to displacement.txt (SolverStepLinearT.cpp:549-603):
+    // time, load amplitude, displacement and traction of dof 2.
+    void RecordResult();
+    // SolverT::LoadTimeVariation (SolverT.cpp:379-394): amp[s] at step s when a
+    // load history is set, else the reference's unit step.
+    double LoadTimeVariation(double t);
+    void SetLoadHistory(const std::vector<double>& amp);
+    void SetResultFile(const std::string& path) { result_file_ = path; }
+    // SolverT::WriteGH (SolverT.cpp:670-732) on one process.
+    void WriteGH(const char* name_prefix, int step, int num_row, int num_column, double* data,
+                 int comm_size = 1, int comm_rank = 0);
+
+    // Histories so far: step s of u / t is Displacement(s) / Traction(s).
+    const std::vector<double>& Displacement(int s) const { return u_[s]; }
+    const std::vector<double>& Traction(int s) const { return t_[s]; }
+    tdbem_ctx* Context() const { return ctx_; }
+
+   private:
+    ModelManagerT* model_;
+    tdbem_ctx* ctx_ = nullptr;
+    double dt_ = 0;
+    int num_steps_ = 0, curr_ = 0, max_step_ = 0;
+    bool begun_ = false;
+    std::vector<double> amp_;
+    std::vector<std::vector<double>> u_, t_;
+    std::string result_file_ = "displacement.txt";
+};
+
+}  // namespace tdbem

@@ -33,13 +33,20 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
+RUN = os.path.join(OUT, "tdbem_run")
+RUN_SRC = os.path.join(CSRC, "host", "tdbem_run.cpp")
+
+
 def _sources():
-    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
+    host = [p for p in glob.glob(os.path.join(CSRC, "host", "*.cpp")) if p != RUN_SRC]
+    return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")) +
+                  host)
 
 
 def _headers():
     return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h")) +
-            glob.glob(os.path.join(ROOT, "include", "*.h")))
+            glob.glob(os.path.join(ROOT, "include", "*.h")) +
+            glob.glob(os.path.join(ROOT, "include", "*.hpp")))
 
 
 def _stale(target, deps):
@@ -50,7 +57,8 @@ def _stale(target, deps):
 
 
 def _compile(src, verbose, ptxas_info):
-    obj = os.path.join(OUT, os.path.splitext(os.path.basename(src))[0] + ".o")
+    sub = "host_" if os.path.basename(os.path.dirname(src)) == "host" else ""
+    obj = os.path.join(OUT, sub + os.path.splitext(os.path.basename(src))[0] + ".o")
     if not _stale(obj, [src] + _headers()) and not ptxas_info:
         return obj, ""
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + (["-Xptxas", "-v"] if ptxas_info else []) + \
@@ -77,6 +85,16 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)
+    # tdbem_run: main.cpp's sequence over the host classes, linked to the library
+    if _stale(RUN, [RUN_SRC, LIB] + _headers()):
+        cmd = [nvcc()] + ARCH + ["-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"),
+                                 RUN_SRC, "-o", RUN, "-L" + OUT, "-ltdbem", "-lcudart",
+                                 "-Xlinker", "-rpath=$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {RUN_SRC}:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 

@@ -211,6 +211,8 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_Ainv[0]);
     dfree(c->d_Ainv[1]);
     c->hist_steps = -1;
+    dfree(c->d_upd_tmp);
+    c->upd_tmp_cap = 0;
     free_batch(c);
 }
 
@@ -488,33 +490,70 @@ int upload_bc(tdbem_ctx* c) {
     return TDBEM_OK;
 }
 
+// FP64 inverse of the column-exchanged LHS v (0: step 2's, 1: steps >= 3) into
+// c->d_Ainv[v] (SolverStepLinearT.cpp:357-393, KSPSolve as an explicit inverse).
+int fp64_inverse(tdbem_ctx* c, int v, const double lhs_c[2][2]) {
+    const int D = c->D;
+    const size_t stride = (size_t)D * D;
+    cudaStream_t s = c->stream;
+    if (c->d_Ainv[1 - v] == c->d_Ainv[v]) c->d_Ainv[v] = nullptr;  // was an alias of the other
+    if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
+    CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
+                              lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
+    if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
+    const int pe = prof_begin(c, TDBEM_K_FACTOR);
+    cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
+                               &c->launches, s);
+    prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
+    c->launches += 1;  // LHS build
+    if (e == cudaErrorInvalidValue)
+        return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
+    CUDA_TRY(e);
+    return TDBEM_OK;
+}
+
+// One FP64 Solve_Averaging step: solve step st (history st) from histories < st.
+int fp64_step(tdbem_ctx* c, int st, const double lhs_c[2][2]) {
+    const int D = c->D;
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const size_t stride = (size_t)D * D;
+    cudaStream_t s = c->stream;
+    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
+    const int L = std::min(std::max(st, 1), c->M);
+    const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
+    const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
+    const double amp = c->amp.empty() ? 1.0 : c->amp[st];
+    CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
+                                    c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
+    const int nch = conv_chunks(L, D);
+    const double esz = c->d_G ? 8.0 : 4.0;
+    int pe = prof_begin(c, TDBEM_K_CONV);
+    CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
+    prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
+             (L + 1) * 4.0 * (double)stride);
+    pe = prof_begin(c, TDBEM_K_SOLVE);
+    CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
+                                 c->d_x, s));
+    CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+                                 c->d_fbc_map, amp, c->d_u, c->d_t, s));
+    prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
+    c->launches += 5;  // combine, conv, reduce, gemv, update
+    return TDBEM_OK;
+}
+
 // Plain FP64 marching: one level-streamed convolution and one FP64 inverse
 // product per step.
 int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hist,
                double* t_hist) {
     const int D = c->D;
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    const size_t stride = (size_t)D * D;
     cudaStream_t s = c->stream;
     const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
     EventTimer tf;
     tf.start(s);
     const int ninv = (numstep >= 3 && !same) ? 2 : 1;
-    for (int v = 0; v < 2; v++)
-        if (c->d_Ainv[v] == c->d_Ainv[1 - v]) c->d_Ainv[v] = nullptr;
     for (int v = 0; v < ninv; v++) {
-        if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
-        CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
-                                  lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
-        if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
-        const int pe = prof_begin(c, TDBEM_K_FACTOR);
-        cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
-                                   &c->launches, s);
-        prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
-        c->launches += 1;  // LHS build
-        if (e == cudaErrorInvalidValue)
-            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
-        CUDA_TRY(e);
+        const int rc = fp64_inverse(c, v, lhs_c);
+        if (rc != TDBEM_OK) return rc;
     }
     if (ninv == 1) {
         if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
@@ -522,30 +561,11 @@ int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hi
     }
     c->timings[1] = tf.stop_ms(s);
 
-    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
     EventTimer tmr;
     tmr.start(s);
-    for (int curr = 2; curr <= numstep; curr++) {
-        const int st = curr - 1;
-        const int L = std::min(std::max(st, 1), c->M);
-        const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
-        const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
-        CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
-                                        c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
-        const int nch = conv_chunks(L, D);
-        const double esz = c->d_G ? 8.0 : 4.0;
-        int pe = prof_begin(c, TDBEM_K_CONV);
-        CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
-        prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
-                 (L + 1) * 4.0 * (double)stride);
-        pe = prof_begin(c, TDBEM_K_SOLVE);
-        CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
-                                     c->d_x, s));
-        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
-        prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
-        c->launches += 5;  // combine, conv, reduce, gemv, update
+    for (int st = 1; st <= numstep - 1; st++) {
+        const int rc = fp64_step(c, st, lhs_c);
+        if (rc != TDBEM_OK) return rc;
     }
     c->timings[2] = tmr.stop_ms(s);
     if (u_hist)
@@ -556,6 +576,21 @@ int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hi
                                  cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaStreamSynchronize(s));
     prof_flush(c);
+    return TDBEM_OK;
+}
+
+// FP64 level store of (M+1) levels, zeroed, for levels fed from host row blocks
+// or a checkpoint.
+int ensure_fp64_store(tdbem_ctx* c) {
+    if (c->level_precision == TDBEM_FP64 && c->d_G) return TDBEM_OK;
+    free_levels(c);
+    const size_t n = (size_t)(c->M + 1) * c->D * c->D;
+    CUDA_TRY(dalloc(&c->d_G, n));
+    CUDA_TRY(dalloc(&c->d_H, n));
+    CUDA_TRY(cudaMemsetAsync(c->d_G, 0, sizeof(double) * n, c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->d_H, 0, sizeof(double) * n, c->stream));
+    c->level_precision = TDBEM_FP64;
+    c->levels_last = 0;
     return TDBEM_OK;
 }
 
@@ -1126,6 +1161,259 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
     CUDA_TRY(cudaStreamSynchronize(s));
     prof_flush(c);
     return TDBEM_OK;
+}
+
+int tdbem_update_gh_linear(tdbem_ctx* c, int step, int node_lo, int node_hi, const double* G_I,
+                           const double* G_J, const double* H_I, const double* H_J) {
+    if (!c || !G_I || !G_J || !H_I || !H_J) return fail(TDBEM_ERR_ARG, "null argument");
+    if (step < 1) return fail(TDBEM_ERR_ARG, "step must be >= 1");
+    if (node_lo < 0 || node_hi >= c->nnd || node_lo > node_hi)
+        return fail(TDBEM_ERR_ARG, "node range [%d, %d] invalid", node_lo, node_hi);
+    if (step > c->M) return TDBEM_OK;  // SolverStepLinearT.cpp:66: only steps <= MaxStep
+    const int rc = ensure_fp64_store(c);
+    if (rc != TDBEM_OK) return rc;
+    const int D = c->D;
+    const size_t rows = 3 * (size_t)(node_hi - node_lo + 1), n = rows * D;
+    const size_t off = 3 * (size_t)node_lo * D, lev = (size_t)D * D;
+    cudaStream_t s = c->stream;
+    if (c->upd_tmp_cap < n) {
+        dfree(c->d_upd_tmp);
+        c->upd_tmp_cap = 0;
+        CUDA_TRY(dalloc(&c->d_upd_tmp, n));
+        c->upd_tmp_cap = n;
+    }
+    const double* J[2] = {G_J, H_J};
+    const double* I[2] = {G_I, H_I};
+    double* store[2] = {c->d_G, c->d_H};
+    for (int m = 0; m < 2; m++) {
+        double* lvl_prev = store[m] + (size_t)(step - 1) * lev + off;  // level step-1 <- J part
+        double* lvl_cur = store[m] + (size_t)step * lev + off;         // level step   <- I part
+        if (step == 1) {
+            CUDA_TRY(cudaMemcpyAsync(lvl_prev, J[m], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        } else {
+            CUDA_TRY(cudaMemcpyAsync(c->d_upd_tmp, J[m], sizeof(double) * n,
+                                     cudaMemcpyHostToDevice, s));
+            CUDA_TRY(launch_add_inplace(lvl_prev, c->d_upd_tmp, n, s));
+            c->launches += 1;
+        }
+        CUDA_TRY(cudaMemcpyAsync(lvl_cur, I[m], sizeof(double) * n, cudaMemcpyHostToDevice, s));
+        CUDA_TRY(cudaStreamSynchronize(s));  // the temporary is reused for H
+    }
+    c->levels_last = std::max(c->levels_last, step);
+    c->tc_planes_valid = false;
+    c->step_inv_ready[0] = c->step_inv_ready[1] = false;
+    return TDBEM_OK;
+}
+
+int tdbem_march_begin(tdbem_ctx* c, int numstep) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (numstep < 1) return fail(TDBEM_ERR_ARG, "numstep must be >= 1");
+    if (!c->amp.empty() && (int)c->amp.size() < numstep)
+        return fail(TDBEM_ERR_ARG, "load history has %zu values, %d steps", c->amp.size(),
+                    numstep);
+    const int rc = upload_bc(c);
+    if (rc != TDBEM_OK) return rc;
+    const int D = c->D;
+    cudaStream_t s = c->stream;
+    if (c->hist_steps != numstep) {
+        dfree(c->d_u);
+        dfree(c->d_t);
+        CUDA_TRY(dalloc(&c->d_u, (size_t)(numstep + 1) * D));
+        CUDA_TRY(dalloc(&c->d_t, (size_t)(numstep + 1) * D));
+        c->hist_steps = numstep;
+    }
+    CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (numstep + 1) * D, s));
+    CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (numstep + 1) * D, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    c->step_numstep = numstep;
+    c->step_inv_ready[0] = c->step_inv_ready[1] = false;
+    return TDBEM_OK;
+}
+
+int tdbem_march_step(tdbem_ctx* c, int curr_step, double* u, double* t) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (c->step_numstep < 1) return fail(TDBEM_ERR_STATE, "tdbem_march_begin has not run");
+    if (curr_step < 1 || curr_step > c->step_numstep)
+        return fail(TDBEM_ERR_ARG, "step %d outside 1..%d", curr_step, c->step_numstep);
+    const int D = c->D, st = curr_step - 1;
+    cudaStream_t s = c->stream;
+    if (st >= 1) {
+        if (c->level_precision != TDBEM_FP64)
+            return fail(TDBEM_ERR_UNSUPPORTED, "stepwise marching runs on FP64 levels");
+        if (c->levels_last < std::min(c->M, curr_step))
+            return fail(TDBEM_ERR_STATE, "levels hold %d steps, step %d needs %d", c->levels_last,
+                        curr_step, std::min(c->M, curr_step));
+        const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+        const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+        const int v = st == 1 ? 0 : 1;
+        if (!c->step_inv_ready[v]) {
+            const int rc = fp64_inverse(c, v, lhs_c);
+            if (rc != TDBEM_OK) return rc;
+            c->step_inv_ready[v] = true;
+        }
+        const int rc = fp64_step(c, st, lhs_c);
+        if (rc != TDBEM_OK) return rc;
+    }
+    if (u)
+        CUDA_TRY(cudaMemcpyAsync(u, c->d_u + (size_t)st * D, sizeof(double) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    if (t)
+        CUDA_TRY(cudaMemcpyAsync(t, c->d_t + (size_t)st * D, sizeof(double) * D,
+                                 cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    prof_flush(c);
+    return TDBEM_OK;
+}
+
+// Level checkpoint: a 64-byte header (magic, version, D, M, precision, levels held,
+// row stride) followed by the raw level store (FP64: G then H, (M+1) x D x D;
+// mixed: FP32 G then H, (M+1) x D x ld, then FP64 levels 0-1 of G and H).
+namespace {
+constexpr char kCkptMagic[8] = {'T', 'D', 'B', 'E', 'M', 'L', 'V', 'L'};
+struct CkptHeader {
+    char magic[8];
+    int32_t version, D, M, precision, levels_last, ld;
+    int32_t pad[8];
+};
+static_assert(sizeof(CkptHeader) == 64, "checkpoint header is 64 bytes");
+
+struct LevelArrays {
+    void* dev[4];
+    size_t bytes[4];
+    int n;
+};
+
+LevelArrays level_arrays(tdbem_ctx* c) {
+    LevelArrays a{};
+    const size_t L = (size_t)c->M + 1, D = c->D;
+    if (c->level_precision == TDBEM_FP64) {
+        a.n = 2;
+        a.dev[0] = c->d_G;
+        a.dev[1] = c->d_H;
+        a.bytes[0] = a.bytes[1] = L * D * D * 8;
+    } else {
+        a.n = 4;
+        a.dev[0] = c->d_Gf;
+        a.dev[1] = c->d_Hf;
+        a.bytes[0] = a.bytes[1] = L * D * c->ldf * 4;
+        a.dev[2] = c->d_G01;
+        a.dev[3] = c->d_H01;
+        a.bytes[2] = a.bytes[3] = 2 * D * D * 8;
+    }
+    return a;
+}
+}  // namespace
+
+int tdbem_export_levels(tdbem_ctx* c, const char* path) {
+    if (!c || !path) return fail(TDBEM_ERR_ARG, "null argument");
+    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s for writing", path);
+    CkptHeader h{};
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = 1;
+    h.D = c->D;
+    h.M = c->M;
+    h.precision = c->level_precision;
+    h.levels_last = c->levels_last;
+    h.ld = c->level_precision == TDBEM_FP64 ? c->D : c->ldf;
+    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
+    const LevelArrays a = level_arrays(c);
+    std::vector<unsigned char> buf;
+    const size_t chunk = (size_t)64 << 20;
+    for (int k = 0; k < a.n && ok; k++)
+        for (size_t o = 0; o < a.bytes[k] && ok; o += chunk) {
+            const size_t b = std::min(chunk, a.bytes[k] - o);
+            buf.resize(b);
+            if (cudaMemcpy(buf.data(), static_cast<unsigned char*>(a.dev[k]) + o, b,
+                           cudaMemcpyDeviceToHost) != cudaSuccess) {
+                std::fclose(f);
+                return fail(TDBEM_ERR_CUDA, "level copy to host failed");
+            }
+            ok = std::fwrite(buf.data(), 1, b, f) == b;
+        }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(TDBEM_ERR_ARG, "write to %s failed", path);
+    return TDBEM_OK;
+}
+
+int tdbem_import_levels(tdbem_ctx* c, const char* path) {
+    if (!c || !path) return fail(TDBEM_ERR_ARG, "null argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s", path);
+    CkptHeader h{};
+    if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 ||
+        h.version != 1) {
+        std::fclose(f);
+        return fail(TDBEM_ERR_ARG, "%s is not a level checkpoint", path);
+    }
+    if (h.D != c->D || h.M != c->M) {
+        std::fclose(f);
+        return fail(TDBEM_ERR_ARG, "checkpoint is for D=%d, M=%d; this mesh has D=%d, M=%d", h.D,
+                    h.M, c->D, c->M);
+    }
+    int rc = TDBEM_OK;
+    if (h.precision == TDBEM_FP64) {
+        rc = ensure_fp64_store(c);
+    } else if (h.precision == TDBEM_MIXED && h.ld == mixed_ld(c->D)) {
+        if (c->level_precision != TDBEM_MIXED || !c->d_Gf) {
+            free_levels(c);
+            const size_t n = (size_t)(c->M + 1) * c->D * mixed_ld(c->D);
+            cudaError_t e = dalloc(&c->d_Gf, n);
+            if (e == cudaSuccess) e = dalloc(&c->d_Hf, n);
+            if (e == cudaSuccess) e = dalloc(&c->d_G01, 2 * (size_t)c->D * c->D);
+            if (e == cudaSuccess) e = dalloc(&c->d_H01, 2 * (size_t)c->D * c->D);
+            if (e != cudaSuccess) rc = fail(TDBEM_ERR_NOMEM, "level allocation failed");
+            c->ldf = mixed_ld(c->D);
+            c->level_precision = TDBEM_MIXED;
+        }
+    } else {
+        rc = fail(TDBEM_ERR_ARG, "checkpoint precision %d / row stride %d not supported",
+                  h.precision, h.ld);
+    }
+    if (rc != TDBEM_OK) {
+        std::fclose(f);
+        return rc;
+    }
+    const LevelArrays a = level_arrays(c);
+    std::vector<unsigned char> buf;
+    const size_t chunk = (size_t)64 << 20;
+    bool ok = true;
+    for (int k = 0; k < a.n && ok; k++)
+        for (size_t o = 0; o < a.bytes[k] && ok; o += chunk) {
+            const size_t b = std::min(chunk, a.bytes[k] - o);
+            buf.resize(b);
+            ok = std::fread(buf.data(), 1, b, f) == b &&
+                 cudaMemcpy(static_cast<unsigned char*>(a.dev[k]) + o, buf.data(), b,
+                            cudaMemcpyHostToDevice) == cudaSuccess;
+        }
+    std::fclose(f);
+    if (!ok) {
+        free_levels(c);
+        return fail(TDBEM_ERR_ARG, "%s is truncated or the copy failed", path);
+    }
+    c->levels_last = h.levels_last;
+    c->tc_planes_valid = false;
+    c->step_inv_ready[0] = c->step_inv_ready[1] = false;
+    return TDBEM_OK;
+}
+
+int tdbem_write_gh(const char* name_prefix, int step, int num_row, int num_column,
+                   const double* data) {
+    if (!name_prefix || !data || num_row < 0 || num_column < 0)
+        return fail(TDBEM_ERR_ARG, "invalid arguments");
+    char path[4096];
+    std::snprintf(path, sizeof(path), "%s%d.txt", name_prefix, step);
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s", path);
+    bool ok = true;
+    for (int i = 0; i < num_row && ok; i++) {
+        for (int j = 0; j < num_column && ok; j++)
+            ok = std::fprintf(f, "%15.5e", data[(size_t)i * num_column + j]) > 0;
+        ok = ok && std::fputc('\n', f) != EOF;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? TDBEM_OK : fail(TDBEM_ERR_ARG, "write to %s failed", path);
 }
 
 int tdbem_set_batch_options(tdbem_ctx* c, int engine, int refine_sweeps) {

@@ -181,7 +181,19 @@ __global__ void k_update_state(const double* __restrict__ x, int D, int s,
     t_hist[(size_t)s * D + j] = tv;
 }
 
+__global__ void k_add_inplace(double* __restrict__ y, const double* __restrict__ x, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        y[i] += x[i];
+}
+
 }  // namespace
+
+cudaError_t launch_add_inplace(double* y, const double* x, size_t n, cudaStream_t s) {
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 8);
+    k_add_inplace<<<grid, 256, 0, s>>>(y, x, n);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_build_lhs(const double* G, const double* H, const float* Gf,
                              const float* Hf, size_t level_stride, int D, double c0,

@@ -114,6 +114,7 @@ cudaError_t launch_conv(const MarchDev& md, int L, const double* Wt, const doubl
                         double* partial, int nchunks, cudaStream_t s);
 cudaError_t launch_reduce_solve(const double* partial, int nchunks, int D,
                                 const double* Ainv, double* rhs, double* x, cudaStream_t s);
+cudaError_t launch_add_inplace(double* y, const double* x, size_t n, cudaStream_t s);
 cudaError_t launch_update_state(const double* x, int D, int s, const unsigned char* is_u,
                                 const double* ubc_val, const unsigned char* is_f,
                                 const double* fbc_val, double amp, double* u_hist,
@@ -257,6 +258,11 @@ struct tdbem_ctx {
     size_t tc_W_bytes = 0;
     int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
     tdbem::TcMaps tc_maps{};
+    // stepwise marching (tdbem_march_begin / tdbem_march_step) and host-block levels
+    int step_numstep = -1;
+    bool step_inv_ready[2] = {false, false};
+    double* d_upd_tmp = nullptr;    // one row block of tdbem_update_gh_linear
+    size_t upd_tmp_cap = 0;
 
     // boundary conditions and marching parameters
     std::vector<int> ubc, fbc;

@@ -58,6 +58,14 @@ SIGNATURES = {
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tdbem_update_gh_linear": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.c_int, _dp, _dp, _dp, _dp]),
+    "tdbem_march_begin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_march_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp]),
+    "tdbem_export_levels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tdbem_import_levels": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tdbem_write_gh": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      _dp]),
     "tdbem_footprint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double,
                                        ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_size_t)]),
@@ -97,6 +105,12 @@ class Request(ctypes.Structure):
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 ENGINE_TCGEN05, ENGINE_MMA_SYNC = 0, 1
+
+
+def write_gh(prefix: str, step: int, data) -> None:
+    """SolverT::WriteGH's <prefix><step>.txt for a row block (tdbem_write_gh)."""
+    a = np.ascontiguousarray(data, np.float64)
+    _check(load().tdbem_write_gh(prefix.encode(), step, a.shape[0], a.shape[1], _d(a)))
 
 
 def footprint(model, precision: int = 1, numstep: Optional[int] = None) -> int:
@@ -334,6 +348,28 @@ class Context:
         _check(load().tdbem_march_batch(self.h, n, nc, _d(tr), None if a is None else _d(a),
                                         None, None))
         return None
+
+    def update_gh_linear(self, step: int, G_I, G_J, H_I, H_J, node_lo: int = 0):
+        blocks = [np.ascontiguousarray(x, np.float64) for x in (G_I, G_J, H_I, H_J)]
+        rows = blocks[0].shape[0]
+        hi = node_lo + rows // 3 - 1
+        _check(load().tdbem_update_gh_linear(self.h, step, node_lo, hi, *[_d(b) for b in blocks]))
+
+    def march_begin(self, numstep: Optional[int] = None):
+        n = self.model.numstep if numstep is None else numstep
+        _check(load().tdbem_march_begin(self.h, n))
+
+    def march_step(self, curr_step: int):
+        u = np.empty(self.D)
+        t = np.empty(self.D)
+        _check(load().tdbem_march_step(self.h, curr_step, _d(u), _d(t)))
+        return u, t
+
+    def export_levels(self, path: str):
+        _check(load().tdbem_export_levels(self.h, path.encode()))
+
+    def import_levels(self, path: str):
+        _check(load().tdbem_import_levels(self.h, path.encode()))
 
     def timings(self):
         out = np.zeros(3)
