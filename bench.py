@@ -519,6 +519,8 @@ def run_ours(args, dist):
             "peaks_used": {k: peaks.get(k) for k in ("hbm_gbs", "fp64_tflops", "fp32_tflops")}}
     if compare:
         line["vs_plain_fp64"] = compare
+    if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_batched:
+        line["batched"] = run_batched(lib, torch, args)
     if args.serve_requests > 0:
         line["serve"] = run_serve(lib, args, dev)
     if dist.world == 1 and not args.no_cpu_baseline:
@@ -527,6 +529,53 @@ def run_ours(args, dist):
                                 "kind": "port", "sample": r["sample"]}
     print(json.dumps(line))
     return 0
+
+
+def run_batched(lib, torch, args, workload="sphere_6x16x16_batch64"):
+    """The batched mixed form on the 64-load-case workload, timed like the headline
+    (W warm-up and K timed solves between CUDA events on the library's stream), with
+    its tensor-core convolution's share and bandwidth and its error against the plain
+    FP64 form.  Reported as the "batched" object of the headline line."""
+    from tdbem import loads
+    model = make_model(workload)
+    cases = WORKLOADS[workload]["cases"]
+    D, n = model.ndof, model.numstep
+    trac, amp = loads.gaussian_patch_cases(model, cases, seed=0)
+    ctx = lib.Context(model)
+    ctx.set_alpha(*ALPHA)
+    ctx.set_batch_options(lib.ENGINE_TCGEN05, 0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def job():
+        ctx.assemble(precision=lib.MIXED)
+        ctx.march_batch(trac, amp, to_host=False)
+
+    for _ in range(args.warmup):
+        job()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        job()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ctx.set_profiling(True)
+    job()
+    stats = ctx.kernel_stats()
+    ctx.set_profiling(False)
+    cb = stats["conv_batch"]
+    out = {"workload": workload, "load_cases": cases, "dof": D, "steps": n,
+           "value": cases * D * n / (ms / 1e3), "unit": METRIC, "ms_per_step": ms,
+           "engine": "tcgen05", "refine_sweeps": 0,
+           "conv_batch": {"kernel": "k_conv_tc (tcgen05)", "launches": cb["launches"],
+                          "share": cb["ms"] / max(1e-9, sum(v["ms"] for v in stats.values())),
+                          "GB/s": cb["bytes"] / max(1e-9, cb["ms"]) / 1e6}}
+    if not args.no_compare:
+        out["vs_plain_fp64"] = compare_batch(lib, torch, ctx, model, trac, amp, ms)
+    ctx.close()
+    return out
 
 
 def run_serve(lib, args, dev):
@@ -567,6 +616,8 @@ def main():
     ap.add_argument("--engine", choices=["tcgen05", "mma_sync"], default="tcgen05",
                     help="tensor-core engine of the batched convolution")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 64-load-case batched measurement beside the headline")
     ap.add_argument("--serve-requests", type=int, default=16,
                     help="requests of the serving stream reported beside the headline (0: off)")
     ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, 1/s")
