@@ -44,7 +44,20 @@ WORKLOADS = {
     "bar_1x1x4_q2": dict(kind="bar", numstep=200),
     "sphere_6x16x16_batch64": dict(kind="sphere", n=16, numstep=400, cases=64),
     "sphere_6x8x8_batch64": dict(kind="sphere", n=8, numstep=200, cases=64),
+    "bars32_group": dict(kind="bars", count=32, numstep=200),
 }
+
+
+def group_models(count, numstep, seed=0):
+    """Bars 1 x 1 x L, L ~ U{2..8}, 1..3 quads per unit length (seeded)."""
+    from tdbem import meshes
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        L = int(rng.integers(2, 9))
+        p = int(rng.integers(1, 4))
+        out.append(meshes.bar(1, 1, L, per_unit=p, numstep=numstep))
+    return out
 METRIC = "DOF*steps/s"
 
 
@@ -335,6 +348,8 @@ def run_ours(args, dist):
     torch.cuda.init()
     lib.load()
     prec = lib.FP64 if args.precision == "fp64" else lib.MIXED
+    if WORKLOADS[args.workload]["kind"] == "bars":
+        return run_group(lib, torch, args, dist)
     model = make_model(args.workload)
     D, nsteps = model.ndof, model.numstep
     cases = WORKLOADS[args.workload].get("cases", 0)
@@ -576,6 +591,97 @@ def run_batched(lib, torch, args, workload="sphere_6x16x16_batch64"):
         out["vs_plain_fp64"] = compare_batch(lib, torch, ctx, model, trac, amp, ms)
     ctx.close()
     return out
+
+
+def run_group(lib, torch, args, dist):
+    """Many meshes at once: grouped assembly + one persistent launch for every step
+    of every mesh, against the same meshes solved one after another (plain FP64
+    both ways)."""
+    w = WORKLOADS[args.workload]
+    models = group_models(w["count"], w["numstep"])
+    dofs = [m.ndof for m in models]
+    units = sum(d * m.numstep for d, m in zip(dofs, models))
+    ctxs = [lib.Context(m) for m in models]
+    for c in ctxs:
+        c.set_alpha(*ALPHA)
+    stream = torch.cuda.ExternalStream(ctxs[0].stream)
+
+    def job():
+        lib.assemble_group(ctxs)
+        lib.march_group(ctxs, to_host=False)
+
+    for _ in range(args.warmup):
+        job()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    n0 = sum(c.launch_count() for c in ctxs)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        job()
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = sum(c.launch_count() for c in ctxs) - n0
+    ms_total = dist.max(e0.elapsed_time(e1))
+    ms = ms_total / args.steps
+    value = units * args.steps * dist.world / (ms_total / 1e3)
+    timing = ctxs[0].timings()
+    shape = lib.group_shape()
+    # e2e through the C ABI: contexts from host meshes, grouped assembly and march,
+    # histories back to the host
+    t0 = time.perf_counter()
+    c2 = [lib.Context(m) for m in models]
+    for c in c2:
+        c.set_alpha(*ALPHA)
+    lib.assemble_group(c2)
+    outs = lib.march_group(c2)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    for c in c2:
+        c.close()
+    line_extra = {}
+    if not args.no_compare:
+        # the meshes one after another (plain FP64 per-mesh path), and the difference
+        torch.cuda.synchronize()
+        a0 = time.perf_counter()
+        err = 0.0
+        for c, (u, _) in zip(ctxs, outs):
+            c.assemble(precision=lib.FP64)
+            ur, _ = c.march()
+            err = max(err, float(np.abs(u - ur).max() / max(1e-300, np.abs(ur).max())))
+        seq_s = time.perf_counter() - a0
+        line_extra = {"sequential_fp64_value": units / seq_s, "sequential_s": seq_s,
+                      "speedup_vs_sequential": seq_s / (ms / 1e3),
+                      "max_rel_diff_vs_sequential": err}
+    for c in ctxs:
+        c.close()
+    if dist.rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": args.workload, "meshes": len(models),
+                       "dof_range": [min(dofs), max(dofs)], "dof_total": sum(dofs),
+                       "steps": w["numstep"], "alpha": list(ALPHA), "precision": "fp64",
+                       "parallelism": f"replicas{dist.world}",
+                       "l2": "levels of all meshes together are larger than L2" if
+                             sum((m.max_step() + 1) * d * d * 16 for m, d in zip(models, dofs))
+                             > 129e6 else "levels fit in L2"},
+            "e2e": {"value": units * dist.world / e2e_s, "unit": METRIC,
+                    "h2d_bytes_per_step": int(sum(m.coords.nbytes + m.ien.nbytes for m in models)),
+                    "d2h_bytes_per_step": int(sum(2 * (m.numstep + 1) * d * 8
+                                                  for m, d in zip(models, dofs)))},
+            "gpu_launches": int(launches), "phases_ms": timing, "autotuned_shape": shape,
+            "clocks": clk}
+    line.update(line_extra)
+    print(json.dumps(line))
+    return 0
 
 
 def run_serve(lib, args, dev):

@@ -172,6 +172,28 @@ int tdbem_update_gh_linear(tdbem_ctx* ctx, int step, int node_lo, int node_hi, c
 int tdbem_march_begin(tdbem_ctx* ctx, int numstep);
 int tdbem_march_step(tdbem_ctx* ctx, int curr_step, double* u, double* t);
 
+/* ---- many meshes at once --------------------------------------------- */
+
+/* Assemble the FP64 levels of n contexts (different meshes) together: one pair
+ * window, scan and quadrature launch per colour index for all meshes, one C-term
+ * launch for all nodes, instead of a sequence per mesh.  Levels hold steps
+ * 1..min(MaxStep, nsteps[i]) of context i, as tdbem_assemble_levels(ctx,
+ * nsteps[i], TDBEM_FP64) gives them.  The reference assembles one mesh per run. */
+int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps);
+
+/* March n contexts with FP64 levels (each with its own boundary conditions,
+ * weights and load history) for numsteps[i] steps each in ONE persistent
+ * cooperative launch: every step of every mesh, three grid-wide phases per step
+ * (history vectors, convolution, solve + update).  The launch shape (lanes per
+ * row, threads per block, blocks per SM) is picked the first time a group size
+ * is seen by timing the candidates on the first steps.  u_hist[i] / t_hist[i]:
+ * host buffers of (numsteps[i]+1) x D_i doubles, or NULL (arrays or entries). */
+int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double* const* u_hist,
+                      double* const* t_hist);
+
+/* The launch shape the last grouped march used. */
+int tdbem_group_shape(int* lanes, int* block, int* blocks_per_sm);
+
 /* Batched marching of nrhs load cases on this context's mesh, boundary
  * conditions, weights and (TDBEM_MIXED) levels: tdbem_march run for every case
  * at once.  Case c's known traction at step s is amp[c*numstep + s] *

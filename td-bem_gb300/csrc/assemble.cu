@@ -341,13 +341,14 @@ __device__ __forceinline__ int singular_corner(const double* c, const double xc[
     return s;
 }
 
-__global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
-                              const int* __restrict__ elems, int ne, int node_lo, int nnodes,
-                              Phys ph, int mode, int level_last, int level_cap, int step_n,
-                              int select, PairInfo* __restrict__ pairs,
-                              unsigned* __restrict__ counts) {
-    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (p >= (long long)nnodes * ne) return;
+// Level window (or step membership) and singular corner of pair p (collocation
+// node node_lo + p / ne, element elems[p % ne]).
+__device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ coords,
+                                                     const int* __restrict__ ien,
+                                                     const int* __restrict__ elems, int ne,
+                                                     int node_lo, const Phys& ph, int mode,
+                                                     int level_last, int level_cap, int step_n,
+                                                     int select, long long p) {
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
@@ -391,6 +392,18 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
     }
     const bool far = sing < 0 && rmin > kFarRatio * rad;
     if ((select == SEL_NEAR && far) || (select == SEL_FAR && !far)) pi.cnt = 0;
+    return pi;
+}
+
+__global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
+                              const int* __restrict__ elems, int ne, int node_lo, int nnodes,
+                              Phys ph, int mode, int level_last, int level_cap, int step_n,
+                              int select, PairInfo* __restrict__ pairs,
+                              unsigned* __restrict__ counts) {
+    const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= (long long)nnodes * ne) return;
+    const PairInfo pi = pair_window_info(coords, ien, elems, ne, node_lo, ph, mode, level_last,
+                                         level_cap, step_n, select, p);
     pairs[p] = pi;
     counts[p] = (unsigned)pi.cnt;
 }
@@ -399,18 +412,15 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
 // (k+1) dt ((k+1) <= level_last), scattered into level k of G0/H0 (or the FP32 store).
 // mode ASM_STEP:   item = (pair, step_n), part = 0 -> I part into G0/H0,
 //                  part = 1 -> J part into G1/H1 (row block starting at row_node_lo).
+// One item: pair p (collocation node node_lo + p / ne, element elems[p % ne]) at
+// level (or step) k; accumulates its Gauss points and scatters into out.
 template <int MODE>
-__global__ void __launch_bounds__(128) k_assemble_items(
+__device__ __forceinline__ void assemble_item(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
-    const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
-    int step_n, int part, const PairInfo* __restrict__ pairs,
-    const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
-    unsigned p;
-    if (!item_pair(offsets, npairs, nitems, p)) return;
-    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const PairInfo pi = pairs[p];
-    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
+    const double* __restrict__ gw, const double* __restrict__ geom, const Phys& ph,
+    int level_last, int step_n, int part, const PairInfo& pi, unsigned p, int k,
+    const AsmOut& out) {
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
@@ -496,6 +506,23 @@ __global__ void __launch_bounds__(128) k_assemble_items(
             }
 }
 
+
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_assemble_items(
+    const double* __restrict__ coords, const int* __restrict__ ien,
+    const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
+    const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
+    int step_n, int part, const PairInfo* __restrict__ pairs,
+    const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
+    unsigned p;
+    if (!item_pair(offsets, npairs, nitems, p)) return;
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const PairInfo pi = pairs[p];
+    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
+    assemble_item<MODE>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, level_last, step_n,
+                        part, pi, p, k, out);
+}
 
 // ---------------------------------------------------------------------------
 // FP32 far-field quadrature (mixed precision).
@@ -704,14 +731,13 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
 // ElastoDynamicsT.cpp:261-280): C_c = -sum_e sum_q wJ DT_Kelvin(q)^T over the whole
 // surface, with the reference's regular / Duffy quadrature per element.  One
 // block per node, fixed-order tree reduction; the result goes to cbuf[c][9].
-__global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords,
-                                               const int* __restrict__ ien, int nel,
-                                               int node_lo, int nq,
-                                               const double* __restrict__ gx,
-                                               const double* __restrict__ gw,
-                                               const double* __restrict__ geom, Phys ph,
-                                               double* __restrict__ cbuf) {
-    const int c = node_lo + blockIdx.x;
+// C term of node c, computed by the whole block (256 threads), into dst[9].
+__device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
+                                           const int* __restrict__ ien, int nel, int c, int nq,
+                                           const double* __restrict__ gx,
+                                           const double* __restrict__ gw,
+                                           const double* __restrict__ geom, const Phys& ph,
+                                           double* __restrict__ dst) {
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int nq2 = nq * nq;
@@ -763,7 +789,18 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
             for (int m = 0; m < 9; m++) red[m][threadIdx.x] += red[m][threadIdx.x + st];
         __syncthreads();
     }
-    if (threadIdx.x < 9) cbuf[(size_t)(c - node_lo) * 9 + threadIdx.x] = red[threadIdx.x][0];
+    if (threadIdx.x < 9) dst[threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords,
+                                               const int* __restrict__ ien, int nel,
+                                               int node_lo, int nq,
+                                               const double* __restrict__ gx,
+                                               const double* __restrict__ gw,
+                                               const double* __restrict__ geom, Phys ph,
+                                               double* __restrict__ cbuf) {
+    cterm_node(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
+               cbuf + (size_t)blockIdx.x * 9);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -789,6 +826,69 @@ __global__ void k_cterm_apply(const double* __restrict__ cbuf, int node_lo, int 
         const size_t roff = (size_t)(3 * cl + i) * ld + 3 * (size_t)c + j;
         out.H0[roff] += v;
         out.H1[roff] += v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Grouped assembly: the pairs, items and C-term nodes of many meshes in one
+// launch each.  gm[] holds one descriptor per mesh; a thread finds its mesh by
+// binary search on the first pair (or node) of each mesh.  Meshes share no
+// rows, so one launch per colour index stays free of write conflicts.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int group_of(const GroupAsm* __restrict__ gm, int nmesh, unsigned x,
+                                        bool by_node) {
+    int lo = 0, hi = nmesh - 1;  // last mesh whose first pair / node is <= x
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const unsigned b = by_node ? gm[mid].node_begin : gm[mid].pair_begin;
+        if (b <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_pair_window_group(const GroupAsm* __restrict__ gm, int nmesh, unsigned npairs,
+                                    PairInfo* __restrict__ pairs,
+                                    unsigned* __restrict__ counts) {
+    const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const GroupAsm& g = gm[group_of(gm, nmesh, p, false)];
+    const PairInfo pi = pair_window_info(g.coords, g.ien, g.elems, g.ne, 0, g.ph, ASM_LEVELS,
+                                         g.level_last, g.level_cap, 0, SEL_ALL,
+                                         (long long)(p - g.pair_begin));
+    pairs[p] = pi;
+    counts[p] = (unsigned)pi.cnt;
+}
+
+__global__ void __launch_bounds__(128) k_assemble_group(const GroupAsm* __restrict__ gm,
+                                                        int nmesh,
+                                                        const PairInfo* __restrict__ pairs,
+                                                        const unsigned* __restrict__ offsets,
+                                                        unsigned npairs, unsigned nitems) {
+    unsigned p;
+    if (!item_pair(offsets, npairs, nitems, p)) return;
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const GroupAsm& g = gm[group_of(gm, nmesh, p, false)];
+    const PairInfo pi = pairs[p];
+    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
+    assemble_item<ASM_LEVELS>(g.coords, g.ien, g.elems, g.ne, 0, g.nq, g.gx, g.gw, g.geom, g.ph,
+                              g.level_last, 0, 0, pi, p - g.pair_begin, k, g.out);
+}
+
+// One block per node of every mesh: the C term, then its application to levels 0
+// and 1 of the mesh (+ 0.5 dt I for exterior problems), as k_cterm + k_cterm_apply.
+__global__ void __launch_bounds__(256) k_cterm_group(const GroupAsm* __restrict__ gm, int nmesh) {
+    const GroupAsm& g = gm[group_of(gm, nmesh, blockIdx.x, true)];
+    const int c = (int)(blockIdx.x - g.node_begin);
+    double* dst = g.cbuf + (size_t)c * 9;
+    cterm_node(g.coords, g.ien, g.nel, c, g.nq, g.gx, g.gw, g.geom, g.ph, dst);
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        const int i = threadIdx.x / 3, j = threadIdx.x % 3;
+        const double v = dst[threadIdx.x] + ((g.if_ext && i == j) ? 0.5 * g.ph.dt : 0.0);
+        const size_t off = (size_t)(3 * c + i) * g.out.ld + 3 * (size_t)c + j;
+        g.out.H0[off] += v;
+        g.out.H0[g.out.level_stride + off] += v;
     }
 }
 
@@ -872,6 +972,28 @@ size_t scan_temp_bytes(unsigned n) {
 cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
                            size_t tmp_bytes, cudaStream_t s) {
     return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
+}
+
+cudaError_t launch_pair_window_group(const GroupAsm* gm, int nmesh, unsigned npairs,
+                                     PairInfo* pairs, unsigned* counts, cudaStream_t s) {
+    if (npairs == 0) return cudaSuccess;
+    k_pair_window_group<<<(npairs + 255) / 256, 256, 0, s>>>(gm, nmesh, npairs, pairs, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_group(const GroupAsm* gm, int nmesh, const PairInfo* pairs,
+                                  const unsigned* offsets, unsigned npairs, unsigned nitems,
+                                  cudaStream_t s) {
+    if (nitems == 0) return cudaSuccess;
+    k_assemble_group<<<(nitems + 127) / 128, 128, 0, s>>>(gm, nmesh, pairs, offsets, npairs,
+                                                          nitems);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cterm_group(const GroupAsm* gm, int nmesh, unsigned nnodes, cudaStream_t s) {
+    if (nnodes == 0) return cudaSuccess;
+    k_cterm_group<<<nnodes, 256, 0, s>>>(gm, nmesh);
+    return cudaGetLastError();
 }
 
 }  // namespace tdbem

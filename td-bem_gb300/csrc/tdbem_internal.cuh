@@ -81,6 +81,63 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
                                int if_ext, int mode, const AsmOut& out, cudaStream_t s);
 size_t scan_temp_bytes(unsigned n);
+
+// One mesh of a grouped assembly launch (many meshes in one launch; assemble.cu).
+struct GroupAsm {
+    const double* coords;
+    const int* ien;
+    const int* elems;      // this launch's colour of the mesh
+    int ne;                // elements of that colour
+    int nnd, nel, nq;
+    const double* gx;
+    const double* gw;
+    const double* geom;
+    Phys ph;
+    int level_last;        // levels hold steps 1..level_last
+    int level_cap;
+    int if_ext;
+    AsmOut out;            // FP64 level store of the mesh
+    unsigned pair_begin;   // first pair of the mesh in the launch's pair list
+    unsigned node_begin;   // first node of the mesh in the C-term launches
+    double* cbuf;          // nnd x 9 C term of the mesh
+};
+cudaError_t launch_pair_window_group(const GroupAsm* gm, int nmesh, unsigned npairs,
+                                     PairInfo* pairs, unsigned* counts, cudaStream_t s);
+cudaError_t launch_assemble_group(const GroupAsm* gm, int nmesh, const PairInfo* pairs,
+                                  const unsigned* offsets, unsigned npairs, unsigned nitems,
+                                  cudaStream_t s);
+cudaError_t launch_cterm_group(const GroupAsm* gm, int nmesh, unsigned nnodes, cudaStream_t s);
+
+// One mesh of a persistent grouped march (group_march.cu): FP64 levels and inverses.
+struct GroupMarch {
+    int D, M, numstep;
+    const double* G;       // (M+1) x D x D
+    const double* H;
+    const double* Ainv0;   // inverse of step 2's LHS
+    const double* Ainv1;   // inverse of the LHS of steps >= 3
+    double* u;             // (numstep+1) x D histories
+    double* t;
+    const unsigned char* is_u;
+    const unsigned char* is_f;
+    const double* ubc;
+    const double* fbc;
+    const double* load_t;
+    const double* load_u;
+    const double* amp;     // numstep values, or null (unit step)
+    double a1, a2, a3, c0, c1;  // weights; LHS weights of steps >= 3
+    double* Wt;            // (M+1) x D
+    double* Wu;
+    double* rhs;           // D
+    unsigned row_begin;    // first row of the mesh in the grid's row list
+    unsigned w_begin;      // first (level, dof) entry of the mesh in the W list
+};
+struct GroupShape {
+    int lanes;             // lanes per row: 8, 16 or 32
+    int block;             // threads per block
+    int blocks_per_sm;     // at most the occupancy limit
+};
+cudaError_t launch_march_group(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
+                               int st_lo, int st_hi, const GroupShape& shape, cudaStream_t s);
 cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
                            size_t tmp_bytes, cudaStream_t s);
 

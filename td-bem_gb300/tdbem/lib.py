@@ -58,6 +58,10 @@ SIGNATURES = {
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip]),
+    "tdbem_march_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
+                                         ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
+    "tdbem_group_shape": (ctypes.c_int, [_ip, _ip, _ip]),
     "tdbem_update_gh_linear": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                               ctypes.c_int, _dp, _dp, _dp, _dp]),
     "tdbem_march_begin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
@@ -105,6 +109,40 @@ class Request(ctypes.Structure):
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 ENGINE_TCGEN05, ENGINE_MMA_SYNC = 0, 1
+
+
+def _ctx_array(ctxs):
+    arr = (ctypes.c_void_p * len(ctxs))()
+    for i, c in enumerate(ctxs):
+        arr[i] = c.h.value if isinstance(c.h, ctypes.c_void_p) else c.h
+    return arr
+
+
+def assemble_group(ctxs, nsteps=None):
+    """FP64 levels of several contexts in grouped launches (tdbem_assemble_group)."""
+    ns = [c.model.numstep for c in ctxs] if nsteps is None else list(nsteps)
+    n_arr = np.ascontiguousarray(ns, np.int32)
+    _check(load().tdbem_assemble_group(_ctx_array(ctxs), len(ctxs), _i(n_arr)))
+
+
+def march_group(ctxs, numsteps=None, to_host: bool = True):
+    """March several FP64 contexts in one persistent launch; [(u, t)] per context."""
+    ns = [c.model.numstep for c in ctxs] if numsteps is None else list(numsteps)
+    n_arr = np.ascontiguousarray(ns, np.int32)
+    outs = [(np.empty((k + 1, c.D)), np.empty((k + 1, c.D))) for c, k in zip(ctxs, ns)]
+    U = (_dp * len(ctxs))(*[_d(u) for u, _ in outs])
+    T = (_dp * len(ctxs))(*[_d(t) for _, t in outs])
+    if to_host:
+        _check(load().tdbem_march_group(_ctx_array(ctxs), len(ctxs), _i(n_arr), U, T))
+        return outs
+    _check(load().tdbem_march_group(_ctx_array(ctxs), len(ctxs), _i(n_arr), None, None))
+    return None
+
+
+def group_shape():
+    a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _check(load().tdbem_group_shape(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return {"lanes": a.value, "block": b.value, "blocks_per_sm": c.value}
 
 
 def write_gh(prefix: str, step: int, data) -> None:
