@@ -174,20 +174,24 @@ int tdbem_march_step(tdbem_ctx* ctx, int curr_step, double* u, double* t);
 
 /* ---- many meshes at once --------------------------------------------- */
 
-/* Assemble the FP64 levels of n contexts (different meshes) together: one pair
- * window, scan and quadrature launch per colour index for all meshes, one C-term
- * launch for all nodes, instead of a sequence per mesh.  Levels hold steps
- * 1..min(MaxStep, nsteps[i]) of context i, as tdbem_assemble_levels(ctx,
- * nsteps[i], TDBEM_FP64) gives them.  The reference assembles one mesh per run. */
-int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps);
+/* Assemble the levels of n contexts (different meshes) together.  TDBEM_FP64:
+ * one pair window, scan and quadrature launch per colour index for all meshes and
+ * one C-term launch for all nodes, instead of a sequence per mesh; TDBEM_MIXED:
+ * each mesh's near/far assembly from its own host thread on its own stream, the
+ * meshes overlapping on the GPU.  Levels hold steps 1..min(MaxStep, nsteps[i]) of
+ * context i, as tdbem_assemble_levels(ctx, nsteps[i], precision) gives them.
+ * The reference assembles one mesh per run. */
+int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int precision);
 
-/* March n contexts with FP64 levels (each with its own boundary conditions,
- * weights and load history) for numsteps[i] steps each in ONE persistent
- * cooperative launch: every step of every mesh, three grid-wide phases per step
- * (history vectors, convolution, solve + update).  The launch shape (lanes per
- * row, threads per block, blocks per SM) is picked the first time a group size
- * is seen by timing the candidates on the first steps.  u_hist[i] / t_hist[i]:
- * host buffers of (numsteps[i]+1) x D_i doubles, or NULL (arrays or entries). */
+/* March n contexts (each with its own boundary conditions, weights and load
+ * history; all FP64 or all TDBEM_MIXED levels) for numsteps[i] steps each in ONE
+ * persistent cooperative launch: every step of every mesh in grid-wide phases
+ * (history vectors, convolution, solve + update; mixed: FP32 levels and inverse
+ * with one FP64 refinement sweep when tdbem_set_march_options asks for one).  The
+ * launch shape (lanes per row, threads per block, blocks per SM) is picked the
+ * first time a group size is seen by timing the candidates on the first steps.
+ * u_hist[i] / t_hist[i]: host buffers of (numsteps[i]+1) x D_i doubles, or NULL
+ * (arrays or entries). */
 int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double* const* u_hist,
                       double* const* t_hist);
 

@@ -8,6 +8,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "tdbem_internal.cuh"
@@ -1417,8 +1418,36 @@ int tdbem_write_gh(const char* name_prefix, int step, int num_row, int num_colum
     return ok ? TDBEM_OK : fail(TDBEM_ERR_ARG, "write to %s failed", path);
 }
 
-int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps) {
+}  // extern "C"
+
+namespace {
+// Runs fn(i) for i < n on n host threads (each sets the context's device) and
+// returns the first failure with its message.
+template <typename F>
+int parallel_contexts(tdbem_ctx* const* ctxs, int n, F fn) {
+    std::vector<int> rc(n, TDBEM_OK);
+    std::vector<std::string> msg(n);
+    std::vector<std::thread> th;
+    th.reserve(n);
+    for (int i = 0; i < n; i++)
+        th.emplace_back([&, i] {
+            cudaSetDevice(ctxs[i]->device);
+            rc[i] = fn(i);
+            if (rc[i] != TDBEM_OK) msg[i] = tdbem_last_error();
+        });
+    for (auto& t : th) t.join();
+    for (int i = 0; i < n; i++)
+        if (rc[i] != TDBEM_OK) return fail(rc[i], "mesh %d: %s", i, msg[i].c_str());
+    return TDBEM_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int precision) {
     if (!ctxs || !nsteps || n < 1) return fail(TDBEM_ERR_ARG, "invalid group");
+    if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
+        return fail(TDBEM_ERR_ARG, "unknown precision %d", precision);
     for (int i = 0; i < n; i++) {
         if (!ctxs[i]) return fail(TDBEM_ERR_ARG, "null context %d", i);
         if (ctxs[i]->device != ctxs[0]->device)
@@ -1427,6 +1456,10 @@ int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps) {
         for (int j = 0; j < i; j++)
             if (ctxs[j] == ctxs[i]) return fail(TDBEM_ERR_ARG, "context %d appears twice", i);
     }
+    if (precision == TDBEM_MIXED)  // near/far split per mesh; the meshes' streams overlap
+        return parallel_contexts(ctxs, n, [&](int i) {
+            return tdbem_assemble_levels(ctxs[i], nsteps[i], TDBEM_MIXED);
+        });
     tdbem_ctx* c0 = ctxs[0];
     cudaStream_t s = c0->stream;
     EventTimer tm;
@@ -1581,8 +1614,10 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
         for (int j = 0; j < i; j++)
             if (ctxs[j] == c) return fail(TDBEM_ERR_ARG, "context %d appears twice", i);
         if (numsteps[i] < 1) return fail(TDBEM_ERR_ARG, "numsteps[%d] must be >= 1", i);
-        if (c->level_precision != TDBEM_FP64)
-            return fail(TDBEM_ERR_UNSUPPORTED, "grouped marching runs on FP64 levels (mesh %d)", i);
+        if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "mesh %d: levels not assembled", i);
+        if (c->level_precision != ctxs[0]->level_precision)
+            return fail(TDBEM_ERR_UNSUPPORTED,
+                        "a group marches FP64 levels or TDBEM_MIXED levels, not both (mesh %d)", i);
         if (c->levels_last < std::min(c->M, numsteps[i]))
             return fail(TDBEM_ERR_STATE, "mesh %d: levels hold %d steps, %d needed", i,
                         c->levels_last, std::min(c->M, numsteps[i]));
@@ -1590,6 +1625,7 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
             return fail(TDBEM_ERR_ARG, "mesh %d: load history shorter than its steps", i);
         max_steps = std::max(max_steps, numsteps[i]);
     }
+    const bool mixed = ctxs[0]->level_precision == TDBEM_MIXED;
     cudaStream_t s = ctxs[0]->stream;
     std::vector<GroupMarch> gm(n);
     std::vector<double*> d_amp(n, nullptr);
@@ -1602,11 +1638,13 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
     unsigned nrows = 0, nw = 0;
     EventTimer tf;
     tf.start(s);
-    for (int i = 0; i < n; i++) {
+    // per mesh: boundary conditions, histories, inverses, load history -- on the
+    // mesh's own stream from its own host thread, so the meshes overlap
+    int rc = parallel_contexts(ctxs, n, [&](int i) -> int {
         tdbem_ctx* c = ctxs[i];
         const int D = c->D, ns = numsteps[i];
-        int rc = upload_bc(c);
-        if (rc != TDBEM_OK) return rc;
+        int r = upload_bc(c);
+        if (r != TDBEM_OK) return r;
         if (c->hist_steps != ns) {
             dfree(c->d_u);
             dfree(c->d_t);
@@ -1618,15 +1656,21 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
         CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (ns + 1) * D, c->stream));
         const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
         const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-        const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-        const int ninv = (ns >= 3 && !same) ? 2 : 1;
-        for (int v = 0; v < ninv; v++) {
-            rc = fp64_inverse(c, v, lhs_c);
-            if (rc != TDBEM_OK) return rc;
-        }
-        if (ninv == 1) {
-            if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
-            c->d_Ainv[1] = c->d_Ainv[0];
+        if (mixed) {
+            if (!c->d_res) CUDA_TRY(dalloc(&c->d_res, D));
+            r = mixed_inverses(c, ns, lhs_c);
+            if (r != TDBEM_OK) return r;
+        } else {
+            const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
+            const int ninv = (ns >= 3 && !same) ? 2 : 1;
+            for (int v = 0; v < ninv; v++) {
+                r = fp64_inverse(c, v, lhs_c);
+                if (r != TDBEM_OK) return r;
+            }
+            if (ninv == 1) {
+                if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
+                c->d_Ainv[1] = c->d_Ainv[0];
+            }
         }
         if (!c->amp.empty()) {
             CUDA_TRY(dalloc(&d_amp[i], (size_t)ns));
@@ -1660,10 +1704,64 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
         g.Wt = c->d_Wt;
         g.Wu = c->d_Wu;
         g.rhs = c->d_rhs;
-        g.row_begin = nrows;
-        g.w_begin = nw;
-        nrows += (unsigned)D;
-        nw += (unsigned)((c->M + 1) * D);
+        g.Gf = c->d_Gf;
+        g.Hf = c->d_Hf;
+        g.ldf = c->ldf;
+        g.inv32_0 = c->d_inv32[0];
+        g.inv32_1 = c->d_inv32[1];
+        g.Hc0 = c->d_Hc64[0];
+        g.Hc1 = c->d_Hc64[1];
+        g.x = c->d_x;
+        g.r = c->d_res;
+        g.refine = c->n_refine > 0 ? 1 : 0;
+        return TDBEM_OK;
+    });
+    if (rc != TDBEM_OK) return rc;
+    unsigned nquads = 0, nwold = 0;
+    size_t nwf = 0, nwoldf = 0, nyold = 0;  // FP32 scratch (row stride ldf) and Y_old sizes
+    for (int i = 0; i < n; i++) {
+        const tdbem_ctx* c = ctxs[i];
+        gm[i].row_begin = nrows;
+        gm[i].w_begin = nw;
+        gm[i].quad_begin = nquads;
+        gm[i].wold_begin = nwold;
+        nrows += (unsigned)c->D;
+        nw += (unsigned)((c->M + 1) * c->D);
+        nquads += (unsigned)((c->D + 3) / 4);
+        nwold += (unsigned)((c->M + 1) * kGroupNB * c->D);
+        nwf += (size_t)(c->M + 1) * c->ldf;
+        nwoldf += (size_t)(c->M + 1) * kGroupNB * c->ldf;
+        nyold += (size_t)kGroupNB * c->D;
+    }
+    float* d_wf = nullptr;    // FP32 history vectors of every mesh (mixed)
+    double* d_yold = nullptr;
+    struct FreeWf {
+        float*& p;
+        double*& q;
+        ~FreeWf() {
+            dfree(p);
+            dfree(q);
+        }
+    } wf_guard{d_wf, d_yold};
+    if (mixed) {
+        // new-W (2 x nwf) and old-W (2 x nwoldf) planes, zeroed: the padding columns
+        // ldf > D are read by the 16-byte loads and must stay zero
+        const size_t tot = 2 * nwf + 2 * nwoldf;
+        CUDA_TRY(dalloc(&d_wf, tot));
+        CUDA_TRY(cudaMemsetAsync(d_wf, 0, sizeof(float) * tot, s));
+        CUDA_TRY(dalloc(&d_yold, nyold));
+        size_t ow = 0, oo = 0, oy = 0;
+        for (int i = 0; i < n; i++) {
+            const tdbem_ctx* c = ctxs[i];
+            gm[i].Wtf = d_wf + ow;
+            gm[i].Wuf = d_wf + nwf + ow;
+            gm[i].Wold_t = d_wf + 2 * nwf + oo;
+            gm[i].Wold_u = d_wf + 2 * nwf + nwoldf + oo;
+            gm[i].Yold = d_yold + oy;
+            ow += (size_t)(c->M + 1) * c->ldf;
+            oo += (size_t)(c->M + 1) * kGroupNB * c->ldf;
+            oy += (size_t)kGroupNB * c->D;
+        }
     }
     const double factor_ms = tf.stop_ms(s);
     GroupMarch* d_gm = nullptr;
@@ -1676,7 +1774,7 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
 
     // launch shape: the fastest of the candidates on the first steps, remembered per
     // group size (the march is deterministic: every step is recomputed by the full run)
-    const ShapeKey key{n, nrows, nw};
+    const ShapeKey key{n * (mixed ? -1 : 1), nrows, nw};
     GroupShape shape{0, 0, 0};
     {
         std::lock_guard<std::mutex> lock(g_shape_mu);
@@ -1684,7 +1782,8 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
             if (kv.first == key) shape = kv.second;
     }
     if (shape.lanes == 0) {
-        const int probe_hi = std::min(max_steps, 8);
+        // the probe covers one old-history pass of the time-blocked form
+        const int probe_hi = std::min(max_steps, mixed ? 2 * kGroupNB + 1 : 8);
         float best = 1e30f;
         GroupShape best_shape{32, 256, 1};
         for (int lanes : {8, 16, 32})
@@ -1695,7 +1794,8 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
                     if (probe_hi <= 1) break;
                     EventTimer t;
                     t.start(s);
-                    const cudaError_t e = launch_march_group(d_gm, n, nrows, nw, 1, probe_hi, cand, s);
+                    const cudaError_t e = launch_march_group(d_gm, n, nrows, nw, nquads, nwold, 1,
+                                                             probe_hi, cand, mixed, s);
                     if (e == cudaErrorInvalidConfiguration || e == cudaErrorCooperativeLaunchTooLarge) {
                         cudaGetLastError();
                         t.stop_ms(s);
@@ -1714,7 +1814,7 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
     }
     EventTimer tmr;
     tmr.start(s);
-    CUDA_TRY(launch_march_group(d_gm, n, nrows, nw, 1, max_steps, shape, s));
+    CUDA_TRY(launch_march_group(d_gm, n, nrows, nw, nquads, nwold, 1, max_steps, shape, mixed, s));
     ctxs[0]->launches += 1;
     const double march_ms = tmr.stop_ms(s);
     for (int i = 0; i < n; i++) {

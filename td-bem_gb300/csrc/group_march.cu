@@ -1,18 +1,29 @@
 // Persistent marching of many meshes: every step of every mesh in one
 // cooperative launch.
 //
-// Each mesh is a plain FP64 solve (SolverStepLinearT::Solve_Averaging,
-// SolverStepLinearT.cpp:314-544, as march.cu's per-step kernels).  Per step the
-// grid runs three phases separated by grid-wide barriers:
+// Each mesh is a Solve_Averaging march (SolverStepLinearT.cpp:314-544).
+//
+// FP64 levels (k_march_group, as march.cu's per-step kernels), per step three
+// phases separated by grid-wide barriers:
 //   A  combined history vectors W_f of every mesh (march.cu: k_history_combine);
 //   B  rhs = sum_f (G^f W_t[f] - H^f W_u[f]): one group of LANES lanes per row
 //      of every mesh, FP64 partial sums per lane, fixed-order shuffle reduction;
 //   C  x = inv(LHS) rhs with the mesh's FP64 inverse, one lane group per row,
 //      and the state update of that dof (march.cu: k_update_state).
-// Meshes with fewer steps idle once done.  Small meshes (a few hundred DOF)
-// would otherwise spend their time in launch latency: five launches per step
-// per mesh become three barriers per step for all of them.  The lane count per
-// row and the launch shape are picked by timing (capi.cu: the group autotuner).
+//
+// Mixed levels (k_march_group_tb, as march_mixed.cu): FP32 levels, time blocks of
+// kGroupNB steps.  At the start of a block, the part of the next kGroupNB
+// right-hand sides that only needs history from before the block is one pass
+// over the levels with kGroupNB columns (old-W build | product, each lane group
+// four rows of one mesh so that every 16-byte load of W serves four rows); then
+// per step the new-history part over levels f <= s - S + 1 (new-W build |
+// product), x0 = inv32 rhs | r = rhs - A64 x0 (FP64) | x = x0 + inv32 r with the
+// state update.
+//
+// Meshes with fewer steps idle once done.  The row loops are uniform across
+// each warp and every lane joins the shuffle reductions (rows past the end or of
+// a finished mesh contribute zero).  The lane count per row and the launch shape
+// are picked by timing (capi.cu: the group autotuner).
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -25,17 +36,31 @@ namespace tdbem {
 
 namespace {
 
-__device__ __forceinline__ int mesh_of_row(const GroupMarch* __restrict__ gm, int nmesh,
-                                           unsigned x, bool by_w) {
-    int lo = 0, hi = nmesh - 1;  // last mesh whose first row / W entry is <= x
+// Last mesh whose first entry of the given list is <= x.
+template <typename F>
+__device__ __forceinline__ int mesh_of(const GroupMarch* __restrict__ gm, int nmesh, unsigned x,
+                                       F begin) {
+    int lo = 0, hi = nmesh - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        const unsigned b = by_w ? gm[mid].w_begin : gm[mid].row_begin;
-        if (b <= x) lo = mid;
+        if (begin(gm[mid]) <= x) lo = mid;
         else hi = mid - 1;
     }
     return lo;
 }
+
+struct RowBegin {
+    __device__ unsigned operator()(const GroupMarch& g) const { return g.row_begin; }
+};
+struct WBegin {
+    __device__ unsigned operator()(const GroupMarch& g) const { return g.w_begin; }
+};
+struct QuadBegin {
+    __device__ unsigned operator()(const GroupMarch& g) const { return g.quad_begin; }
+};
+struct WoldBegin {
+    __device__ unsigned operator()(const GroupMarch& g) const { return g.wold_begin; }
+};
 
 template <int LANES>
 __device__ __forceinline__ double group_sum(double v) {
@@ -44,6 +69,58 @@ __device__ __forceinline__ double group_sum(double v) {
     return v;
 }
 
+__device__ __forceinline__ float dot4(const float4 a, const float4 b) {
+    return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+}
+
+// The history combination of k_history_combine / k_build_w_old / k_build_w_new:
+// histories m with lo <= m < hi (and m >= 1) enter; loads only when with_load.
+__device__ __forceinline__ void combine(const GroupMarch& g, int s, int f, int j, int lo, int hi,
+                                        bool with_load, double& wt, double& wu) {
+    const double* th = g.t;
+    const double* uh = g.u;
+    const int D = g.D;
+    wt = 0;
+    wu = 0;
+    const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+    auto in = [&](int m) { return m >= 1 && m >= lo && m < hi; };
+    if (f >= 2 && in(m1)) {
+        wt += g.a1 * th[(size_t)m1 * D + j];
+        wu += g.a1 * uh[(size_t)m1 * D + j];
+    }
+    if (f >= 1 && in(m3)) {
+        wt += g.a3 * th[(size_t)m3 * D + j];
+        wu += g.a3 * uh[(size_t)m3 * D + j];
+    }
+    if (in(m2)) {
+        wt += g.a2 * th[(size_t)m2 * D + j];
+        wu += g.a2 * uh[(size_t)m2 * D + j];
+    }
+    if (f == 0 && in(s - 1)) {
+        wt -= g.a1 * th[(size_t)(s - 1) * D + j];
+        wu -= g.a1 * uh[(size_t)(s - 1) * D + j];
+    }
+    if (with_load && f <= 1) {
+        const double c0 = s == 1 ? 1.0 : g.c0, c1 = s == 1 ? 0.0 : g.c1;
+        const double cf = f == 0 ? c0 : c1;
+        const double amp = g.amp ? g.amp[s] : 1.0;
+        wt += cf * (amp * g.load_t[j]);
+        wu += cf * g.load_u[j];
+    }
+}
+
+// State update of dof j at step s (march.cu: k_update_state).
+__device__ __forceinline__ void update_dof(const GroupMarch& g, int s, int j, double x) {
+    const int D = g.D;
+    const double amp = g.amp ? g.amp[s] : 1.0;
+    const bool u = g.is_u[j] != 0, f = g.is_f[j] != 0;
+    g.u[(size_t)s * D + j] = u ? g.ubc[j] : x;
+    double tv = f ? g.fbc[j] * amp : 0.0;
+    if (u && j < D - 1) tv = x;
+    g.t[(size_t)s * D + j] = tv;
+}
+
+// ---------------------------------------------------------------- FP64 levels
 template <int LANES>
 __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restrict__ gm, int nmesh,
                                                      unsigned nrows, unsigned nw, int st_lo,
@@ -53,59 +130,26 @@ __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restric
     const unsigned nthreads = gridDim.x * blockDim.x;
     const unsigned lane = threadIdx.x % LANES;
     const unsigned ngroups = nthreads / LANES;
-    // the warp's first lane group and this lane's group within the warp
-    const unsigned warp_group0 = (tid / 32) * (32 / LANES);
-    const unsigned sub = (threadIdx.x % 32) / LANES;
+    const unsigned warp_group0 = (tid / 32) * (32 / LANES);  // the warp's first lane group
+    const unsigned sub = (threadIdx.x % 32) / LANES;          // this lane's group in the warp
     for (int st = st_lo; st < st_hi; st++) {
         // ---- A: combined history vectors (levels f <= L of each mesh)
         for (unsigned idx = tid; idx < nw; idx += nthreads) {
-            const GroupMarch& g = gm[mesh_of_row(gm, nmesh, idx, true)];
+            const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WBegin{})];
             if (st >= g.numstep) continue;
             const unsigned loc = idx - g.w_begin;
             const int f = (int)(loc / g.D), j = (int)(loc % g.D);
-            const int L = min(max(st, 1), g.M);
-            if (f > L) continue;
-            const double c0 = st == 1 ? 1.0 : g.c0, c1 = st == 1 ? 0.0 : g.c1;
-            const double amp = g.amp ? g.amp[st] : 1.0;
-            const double* uh = g.u;
-            const double* th = g.t;
-            const int D = g.D;
-            double wt = 0, wu = 0;
-            const int m1 = st + 1 - f, m3 = st - f, m2 = st - 1 - f;
-            if (f >= 2 && m1 >= 1) {
-                wt += g.a1 * th[(size_t)m1 * D + j];
-                wu += g.a1 * uh[(size_t)m1 * D + j];
-            }
-            if (f >= 1 && m3 >= 1) {
-                wt += g.a3 * th[(size_t)m3 * D + j];
-                wu += g.a3 * uh[(size_t)m3 * D + j];
-            }
-            if (m2 >= 1) {
-                wt += g.a2 * th[(size_t)m2 * D + j];
-                wu += g.a2 * uh[(size_t)m2 * D + j];
-            }
-            if (f == 0) {
-                if (st - 1 >= 1) {
-                    wt -= g.a1 * th[(size_t)(st - 1) * D + j];
-                    wu -= g.a1 * uh[(size_t)(st - 1) * D + j];
-                }
-                wt += c0 * (amp * g.load_t[j]);
-                wu += c0 * g.load_u[j];
-            } else if (f == 1) {
-                wt += c1 * (amp * g.load_t[j]);
-                wu += c1 * g.load_u[j];
-            }
+            if (f > min(max(st, 1), g.M)) continue;
+            double wt, wu;
+            combine(g, st, f, j, 1, st, true, wt, wu);
             g.Wt[loc] = wt;
             g.Wu[loc] = wu;
         }
         grid.sync();
-        // ---- B: history convolution, one lane group per row.  The row loop is
-        // uniform across each warp (stepped by the warp's first group) and every
-        // lane joins the shuffle reduction, also for rows past the end or of a
-        // finished mesh, which contribute zero.
+        // ---- B: history convolution, one lane group per row
         for (unsigned base = warp_group0; base < nrows; base += ngroups) {
             const unsigned r = base + sub;
-            const GroupMarch* g = r < nrows ? &gm[mesh_of_row(gm, nmesh, r, false)] : nullptr;
+            const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
             const bool live = g && st < g->numstep;
             double acc = 0;
             if (live) {
@@ -127,62 +171,240 @@ __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restric
         // ---- C: solve with the inverse, state update of the row's dof
         for (unsigned base = warp_group0; base < nrows; base += ngroups) {
             const unsigned r = base + sub;
-            const GroupMarch* g = r < nrows ? &gm[mesh_of_row(gm, nmesh, r, false)] : nullptr;
+            const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
             const bool live = g && st < g->numstep;
             double acc = 0;
             int j = 0;
             if (live) {
                 j = (int)(r - g->row_begin);
-                const int D = g->D;
-                const double* Ar = (st == 1 ? g->Ainv0 : g->Ainv1) + (size_t)j * D;
-                for (int k = lane; k < D; k += LANES) acc += Ar[k] * g->rhs[k];
+                const double* Ar = (st == 1 ? g->Ainv0 : g->Ainv1) + (size_t)j * g->D;
+                for (int k = lane; k < g->D; k += LANES) acc += Ar[k] * g->rhs[k];
             }
             acc = group_sum<LANES>(acc);
-            if (live && lane == 0) {
-                const int D = g->D;
-                const double amp = g->amp ? g->amp[st] : 1.0;
-                const bool u = g->is_u[j] != 0, f = g->is_f[j] != 0;
-                g->u[(size_t)st * D + j] = u ? g->ubc[j] : acc;
-                double tv = f ? g->fbc[j] * amp : 0.0;
-                if (u && j < D - 1) tv = acc;
-                g->t[(size_t)st * D + j] = tv;
-            }
+            if (live && lane == 0) update_dof(*g, st, j, acc);
         }
         grid.sync();
     }
 }
 
+// ---------------------------------------------------------------- mixed levels
 template <int LANES>
-cudaError_t launch_lanes(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw, int st_lo,
-                         int st_hi, int block, int blocks_per_sm, cudaStream_t s) {
+__global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __restrict__ gm,
+                                                        int nmesh, unsigned nrows, unsigned nw,
+                                                        unsigned nquads, unsigned nwold,
+                                                        int st_lo, int st_hi) {
+    constexpr int NB = kGroupNB, RQ = 4;
+    cg::grid_group grid = cg::this_grid();
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned nthreads = gridDim.x * blockDim.x;
+    const unsigned lane = threadIdx.x % LANES;
+    const unsigned ngroups = nthreads / LANES;
+    const unsigned warp_group0 = (tid / 32) * (32 / LANES);
+    const unsigned sub = (threadIdx.x % 32) / LANES;
+    for (int S = st_lo; S < st_hi; S += NB) {
+        if (S > 1) {
+            // ---- old-history vectors of the block: W_f^old[:, j], s = S + j, m < S
+            for (unsigned idx = tid; idx < nwold; idx += nthreads) {
+                const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WoldBegin{})];
+                if (S >= g.numstep) continue;
+                const unsigned loc = idx - g.wold_begin;
+                const int k = (int)(loc % g.D);
+                const int j = (int)((loc / g.D) % NB);
+                const int f = (int)(loc / ((unsigned)g.D * NB));
+                const int nbe = min(NB, g.numstep - S);
+                if (f > min(g.M, S + nbe - 1)) continue;
+                double wt, wu;
+                combine(g, S + j, f, k, 1, S, false, wt, wu);
+                const size_t o = ((size_t)f * NB + j) * g.ldf + k;
+                g.Wold_t[o] = (float)wt;
+                g.Wold_u[o] = (float)wu;
+            }
+            grid.sync();
+            // ---- Y_old[j][row] = sum_f X^f[row] . W_f^old[j], four rows per lane group
+            for (unsigned base = warp_group0; base < nquads; base += ngroups) {
+                const unsigned q = base + sub;
+                const GroupMarch* g =
+                    q < nquads ? &gm[mesh_of(gm, nmesh, q, QuadBegin{})] : nullptr;
+                const bool live = g && S < g->numstep;
+                float acc[RQ][NB];
+#pragma unroll
+                for (int r = 0; r < RQ; r++)
+#pragma unroll
+                    for (int j = 0; j < NB; j++) acc[r][j] = 0.f;
+                int row0 = 0;
+                if (live) {
+                    const int D = g->D, ld4 = g->ldf / 4;
+                    row0 = (int)(q - g->quad_begin) * RQ;
+                    const int nbe = min(NB, g->numstep - S);
+                    const int nlev = min(g->M, S + nbe - 1) + 1;
+                    size_t rowoff[RQ];
+#pragma unroll
+                    for (int r = 0; r < RQ; r++) rowoff[r] = (size_t)min(row0 + r, D - 1) * ld4;
+                    for (int f = 0; f < nlev; f++) {
+                        const float4* G4 =
+                            reinterpret_cast<const float4*>(g->Gf) + (size_t)f * D * ld4;
+                        const float4* H4 =
+                            reinterpret_cast<const float4*>(g->Hf) + (size_t)f * D * ld4;
+                        const float4* wt =
+                            reinterpret_cast<const float4*>(g->Wold_t) + (size_t)f * NB * ld4;
+                        const float4* wu =
+                            reinterpret_cast<const float4*>(g->Wold_u) + (size_t)f * NB * ld4;
+                        for (int k4 = lane; k4 < ld4; k4 += LANES) {
+                            float4 a[RQ], b[RQ];
+#pragma unroll
+                            for (int r = 0; r < RQ; r++) {
+                                a[r] = __ldcs(G4 + rowoff[r] + k4);
+                                b[r] = __ldcs(H4 + rowoff[r] + k4);
+                            }
+#pragma unroll
+                            for (int j = 0; j < NB; j++) {
+                                const float4 x = wt[(size_t)j * ld4 + k4];
+                                const float4 y = wu[(size_t)j * ld4 + k4];
+#pragma unroll
+                                for (int r = 0; r < RQ; r++)
+                                    acc[r][j] += dot4(a[r], x) - dot4(b[r], y);
+                            }
+                        }
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < RQ; r++)
+#pragma unroll
+                    for (int j = 0; j < NB; j++) {
+                        const double v = group_sum<LANES>((double)acc[r][j]);
+                        if (live && lane == 0 && row0 + r < g->D)
+                            g->Yold[(size_t)j * g->D + row0 + r] = v;
+                    }
+            }
+            grid.sync();
+        }
+        for (int jb = 0; jb < NB && S + jb < st_hi; jb++) {
+            const int st = S + jb;
+            // ---- new-history vectors: m >= S, and the known loads, levels f <= s - S + 1
+            for (unsigned idx = tid; idx < nw; idx += nthreads) {
+                const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WBegin{})];
+                if (st >= g.numstep) continue;
+                const unsigned loc = idx - g.w_begin;
+                const int f = (int)(loc / g.D), k = (int)(loc % g.D);
+                if (f > min(g.M, max(1, st + 1 - S))) continue;
+                double wt, wu;
+                combine(g, st, f, k, S, st, true, wt, wu);
+                g.Wtf[(size_t)f * g.ldf + k] = (float)wt;
+                g.Wuf[(size_t)f * g.ldf + k] = (float)wu;
+            }
+            grid.sync();
+            // ---- rhs = Y_old[jb] + sum_{f <= L} X^f . W_f^new
+            for (unsigned base = warp_group0; base < nrows; base += ngroups) {
+                const unsigned r = base + sub;
+                const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
+                const bool live = g && st < g->numstep;
+                double acc = 0;
+                int row = 0;
+                if (live) {
+                    row = (int)(r - g->row_begin);
+                    const int D = g->D, ld4 = g->ldf / 4;
+                    const int L = min(g->M, max(1, st + 1 - S));
+                    for (int f = 0; f <= L; f++) {
+                        const float4* G4 =
+                            reinterpret_cast<const float4*>(g->Gf) + ((size_t)f * D + row) * ld4;
+                        const float4* H4 =
+                            reinterpret_cast<const float4*>(g->Hf) + ((size_t)f * D + row) * ld4;
+                        const float4* wt = reinterpret_cast<const float4*>(g->Wtf) + (size_t)f * ld4;
+                        const float4* wu = reinterpret_cast<const float4*>(g->Wuf) + (size_t)f * ld4;
+                        float a32 = 0.f;
+                        for (int k4 = lane; k4 < ld4; k4 += LANES)
+                            a32 += dot4(__ldcs(G4 + k4), wt[k4]) - dot4(__ldcs(H4 + k4), wu[k4]);
+                        acc += (double)a32;
+                    }
+                }
+                acc = group_sum<LANES>(acc);
+                if (live && lane == 0)
+                    g->rhs[row] = acc + (S > 1 ? g->Yold[(size_t)jb * g->D + row] : 0.0);
+            }
+            grid.sync();
+            // ---- x0 = inv32 rhs | r = rhs - A64 x0 | x = x0 + inv32 r, state update
+            for (int sweep = 0; sweep < 3; sweep++) {
+                for (unsigned base = warp_group0; base < nrows; base += ngroups) {
+                    const unsigned r = base + sub;
+                    const GroupMarch* g =
+                        r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
+                    const bool live = g && st < g->numstep && (sweep == 0 || g->refine > 0);
+                    double acc = 0;
+                    int j = 0;
+                    if (live) {
+                        j = (int)(r - g->row_begin);
+                        const int D = g->D;
+                        if (sweep == 1) {
+                            const double* Ar = (st == 1 ? g->Hc0 : g->Hc1) + (size_t)j * D;
+                            for (int k = lane; k < D; k += LANES) acc += Ar[k] * g->x[k];
+                        } else {
+                            const float* Ar = (st == 1 ? g->inv32_0 : g->inv32_1) + (size_t)j * D;
+                            const double* v = sweep == 0 ? g->rhs : g->r;
+                            float a32 = 0.f;
+                            for (int k = lane; k < D; k += LANES) a32 += Ar[k] * (float)v[k];
+                            acc = a32;
+                        }
+                    }
+                    acc = group_sum<LANES>(acc);
+                    if (live && lane == 0) {
+                        if (sweep == 0) {
+                            g->x[j] = acc;
+                            if (g->refine == 0) update_dof(*g, st, j, acc);
+                        } else if (sweep == 1) {
+                            g->r[j] = g->rhs[j] - acc;
+                        } else {
+                            update_dof(*g, st, j, g->x[j] + acc);
+                        }
+                    }
+                }
+                grid.sync();
+            }
+        }
+    }
+}
+
+template <int LANES>
+cudaError_t launch_lanes(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
+                         unsigned nquads, unsigned nwold, int st_lo, int st_hi, int block,
+                         int blocks_per_sm, bool mixed, cudaStream_t s) {
     int dev = 0, nsm = 0, occ = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march_group<LANES>, block, 0);
+    const void* fn =
+        mixed ? (const void*)k_march_group_tb<LANES> : (const void*)k_march_group<LANES>;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, block, 0);
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     const int grid = nsm * std::min(occ, blocks_per_sm);  // every block resident: grid.sync is safe
+    if (mixed) {
+        void* args[] = {(void*)&gm,     (void*)&nmesh, (void*)&nrows, (void*)&nw,
+                        (void*)&nquads, (void*)&nwold, (void*)&st_lo, (void*)&st_hi};
+        return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, s);
+    }
     void* args[] = {(void*)&gm, (void*)&nmesh, (void*)&nrows, (void*)&nw, (void*)&st_lo,
                     (void*)&st_hi};
-    return cudaLaunchCooperativeKernel((const void*)k_march_group<LANES>, dim3(grid), dim3(block),
-                                       args, 0, s);
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, s);
 }
 
 }  // namespace
 
 cudaError_t launch_march_group(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
-                               int st_lo, int st_hi, const GroupShape& shape, cudaStream_t s) {
+                               unsigned nquads, unsigned nwold, int st_lo, int st_hi,
+                               const GroupShape& shape, bool mixed, cudaStream_t s) {
     if (shape.block < 32 || shape.block > 512 || shape.block % 32 || shape.blocks_per_sm < 1)
         return cudaErrorInvalidValue;
     switch (shape.lanes) {
-    case 8: return launch_lanes<8>(gm, nmesh, nrows, nw, st_lo, st_hi, shape.block,
-                                   shape.blocks_per_sm, s);
-    case 16: return launch_lanes<16>(gm, nmesh, nrows, nw, st_lo, st_hi, shape.block,
-                                     shape.blocks_per_sm, s);
-    case 32: return launch_lanes<32>(gm, nmesh, nrows, nw, st_lo, st_hi, shape.block,
-                                     shape.blocks_per_sm, s);
-    default: return cudaErrorInvalidValue;
+    case 8:
+        return launch_lanes<8>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
+                               shape.blocks_per_sm, mixed, s);
+    case 16:
+        return launch_lanes<16>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
+                                shape.blocks_per_sm, mixed, s);
+    case 32:
+        return launch_lanes<32>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
+                                shape.blocks_per_sm, mixed, s);
+    default:
+        return cudaErrorInvalidValue;
     }
 }
 

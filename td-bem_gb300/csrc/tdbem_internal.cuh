@@ -130,14 +130,36 @@ struct GroupMarch {
     double* rhs;           // D
     unsigned row_begin;    // first row of the mesh in the grid's row list
     unsigned w_begin;      // first (level, dof) entry of the mesh in the W list
+    // mixed precision (TDBEM_MIXED levels): FP32 levels and inverses, FP64 LHS
+    const float* Gf;       // (M+1) x D x ldf
+    const float* Hf;
+    int ldf;
+    const float* inv32_0;  // FP32 inverses of the two LHS
+    const float* inv32_1;
+    const double* Hc0;     // FP64 column-exchanged LHS (refinement residual)
+    const double* Hc1;
+    float* Wtf;            // (M+1) x D FP32 history vectors (group scratch)
+    float* Wuf;
+    double* x;             // D: first solution, then the refined one
+    double* r;             // D: residual
+    int refine;            // refinement sweeps (0 or 1)
+    // time blocks of kGroupNB steps (mixed): old-history vectors and their product
+    float* Wold_t;         // (M+1) x kGroupNB x ldf
+    float* Wold_u;
+    double* Yold;          // kGroupNB x D
+    unsigned quad_begin;   // first 4-row block of the mesh in the grid's list
+    unsigned wold_begin;   // first (level, column, dof) entry in the old-W list
 };
+constexpr int kGroupNB = 12;  // steps per time block of the mixed grouped march
 struct GroupShape {
     int lanes;             // lanes per row: 8, 16 or 32
     int block;             // threads per block
     int blocks_per_sm;     // at most the occupancy limit
 };
+// nquads / nwold: 4-row blocks and old-W entries of all meshes (mixed form only).
 cudaError_t launch_march_group(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
-                               int st_lo, int st_hi, const GroupShape& shape, cudaStream_t s);
+                               unsigned nquads, unsigned nwold, int st_lo, int st_hi,
+                               const GroupShape& shape, bool mixed, cudaStream_t s);
 cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
                            size_t tmp_bytes, cudaStream_t s);
 

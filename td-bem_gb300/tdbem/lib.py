@@ -58,7 +58,8 @@ SIGNATURES = {
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
-    "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip]),
+    "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
+                                            ctypes.c_int]),
     "tdbem_march_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
                                          ctypes.POINTER(_dp), ctypes.POINTER(_dp)]),
     "tdbem_group_shape": (ctypes.c_int, [_ip, _ip, _ip]),
@@ -118,11 +119,11 @@ def _ctx_array(ctxs):
     return arr
 
 
-def assemble_group(ctxs, nsteps=None):
-    """FP64 levels of several contexts in grouped launches (tdbem_assemble_group)."""
+def assemble_group(ctxs, nsteps=None, precision: int = FP64):
+    """Levels of several contexts together (tdbem_assemble_group)."""
     ns = [c.model.numstep for c in ctxs] if nsteps is None else list(nsteps)
     n_arr = np.ascontiguousarray(ns, np.int32)
-    _check(load().tdbem_assemble_group(_ctx_array(ctxs), len(ctxs), _i(n_arr)))
+    _check(load().tdbem_assemble_group(_ctx_array(ctxs), len(ctxs), _i(n_arr), precision))
 
 
 def march_group(ctxs, numsteps=None, to_host: bool = True):

@@ -92,11 +92,38 @@ def test_group_errors(tdlib):
     with tdlib.Context(m) as a, tdlib.Context(m) as b:
         with pytest.raises(tdlib.TdbemError) as ei:
             tdlib.march_group([a, b])
-        assert ei.value.code == -5  # no FP64 levels yet
+        assert ei.value.code == -6  # TDBEM_ERR_STATE: no levels yet
         with pytest.raises(tdlib.TdbemError):
             tdlib.assemble_group([a, a])
         a.assemble(precision=tdlib.MIXED)
         tdlib.assemble_group([b])
         with pytest.raises(tdlib.TdbemError) as ei:
             tdlib.march_group([a, b])
-        assert ei.value.code == -5  # mixed levels are not marched in a group
+        assert ei.value.code == -5  # FP64 and mixed levels are not marched together
+
+
+def test_group_mixed_within_1e4_of_fp64(tdlib):
+    """TDBEM_MIXED group (FP32 levels and inverses, one FP64 refinement sweep in the
+    persistent march) against each mesh's plain FP64 march: relative L2 error of
+    the displacement histories <= 1e-4, as the single-mesh mixed form."""
+    ms, setup = group_models()
+    keep = [i for i, (alpha, _) in enumerate(setup) if alpha[0] > 0]  # stable alpha only
+    ms = [ms[i] for i in keep]
+    setup = [setup[i] for i in keep]
+    ref = []
+    for m, (alpha, ak) in zip(ms, setup):
+        with tdlib.Context(m) as ctx:
+            configure(ctx, m, alpha, ak)
+            ctx.assemble(precision=tdlib.FP64)
+            ref.append(ctx.march()[0])
+    ctxs = [tdlib.Context(m) for m in ms]
+    try:
+        for ctx, m, (alpha, ak) in zip(ctxs, ms, setup):
+            configure(ctx, m, alpha, ak)
+        tdlib.assemble_group(ctxs, precision=tdlib.MIXED)
+        out = tdlib.march_group(ctxs)
+        for (u, _), ur in zip(out, ref):
+            assert np.linalg.norm(u - ur) <= 1e-4 * np.linalg.norm(ur)
+    finally:
+        for c in ctxs:
+            c.close()
