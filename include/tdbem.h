@@ -225,6 +225,12 @@ int tdbem_march_batch(tdbem_ctx* ctx, int numstep, int nrhs, const double* tract
 #define TDBEM_ENGINE_MMA_SYNC 1
 int tdbem_set_batch_options(tdbem_ctx* ctx, int engine, int refine_sweeps);
 
+/* tdbem_march replays its per-step loop (every kernel of every step) as a CUDA
+ * graph, captured on the context's stream the first time and again whenever the
+ * step count, block size, refinement, weights, load history or buffers change
+ * (on by default; off with on = 0, and off while profiling is on). */
+int tdbem_set_graphs(tdbem_ctx* ctx, int on);
+
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
  * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64
  * residual-refinement sweeps per solve (0..4; default 1). */

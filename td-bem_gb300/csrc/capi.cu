@@ -328,6 +328,52 @@ struct EventTimer {
 };
 
 
+// Runs a marching loop (kernel launches only, no host synchronisation) through a
+// CUDA graph: captured on the context's stream the first time and whenever a
+// captured value changes (kind of loop, step count, block size, refinement
+// sweeps, weights, load history, buffer addresses), replayed otherwise.  With
+// profiling on (per-launch events) or graphs off the loop runs directly.
+template <typename F>
+int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const void*>& ptrs,
+                   F loop) {
+    if (c->prof || !c->use_graphs) return loop();
+    MarchGraph& g = c->graph;
+    cudaStream_t s = c->stream;
+    const bool same = g.exec && g.kind == kind && g.numstep == numstep && g.nb == c->nb &&
+                      g.refine == c->n_refine && g.a1 == c->a1 && g.a2 == c->a2 &&
+                      g.amp == c->amp && g.ptrs == ptrs;
+    if (!same) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        const long long l0 = c->launches;
+        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int rc = loop();
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(s, &graph);
+        if (rc != TDBEM_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CUDA_TRY(e);
+        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CUDA_TRY(ei);
+        g.launches = c->launches - l0;
+        c->launches = l0;
+        g.kind = kind;
+        g.numstep = numstep;
+        g.nb = c->nb;
+        g.refine = c->n_refine;
+        g.a1 = c->a1;
+        g.a2 = c->a2;
+        g.amp = c->amp;
+        g.ptrs = ptrs;
+    }
+    CUDA_TRY(cudaGraphLaunch(g.exec, s));
+    c->launches += g.launches;
+    return TDBEM_OK;
+}
+
 // FP64 column-exchanged LHS and its FP32 inverse for each distinct LHS of the
 // mixed form (step 2 and steps >= 3); c->timings[1] gets the time taken.
 int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
@@ -392,6 +438,12 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     tmr.start(s);
     const size_t lstride = (size_t)D * c->ldf;
     const int last_s = numstep - 1;  // solve steps 1..numstep-1
+    const std::vector<const void*> ptrs = {
+        c->d_u,      c->d_t,      c->d_Gf,       c->d_Hf,       c->d_inv32[0], c->d_inv32[1],
+        c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old, c->d_Wu_old,   c->d_Wt_new,   c->d_Wu_new,
+        c->d_Yold,   c->d_pmix,   c->d_rhs,      c->d_x,        c->d_res,      c->d_dx,
+        c->d_load_t, c->d_load_u, c->d_is_ubc,   c->d_ubc_map,  c->d_is_fbc,   c->d_fbc_map};
+    const int lrc = run_march_loop(c, 1, numstep, ptrs, [&]() -> int {
     for (int S = 1; S <= last_s; S += nb) {
         const int nbe = std::min(nb, last_s - S + 1);
         if (S > 1) {
@@ -436,6 +488,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             c->launches += 4 + 1 + 3LL * c->n_refine + 1;
         }
     }
+    return TDBEM_OK;
+    });
+    if (lrc != TDBEM_OK) return lrc;
     c->timings[2] = tmr.stop_ms(s);
     return TDBEM_OK;
 }
@@ -565,10 +620,19 @@ int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hi
 
     EventTimer tmr;
     tmr.start(s);
-    for (int st = 1; st <= numstep - 1; st++) {
-        const int rc = fp64_step(c, st, lhs_c);
-        if (rc != TDBEM_OK) return rc;
-    }
+    const std::vector<const void*> ptrs = {
+        c->d_u,     c->d_t,   c->d_G,       c->d_H,      c->d_Gf,       c->d_Hf,
+        c->d_Ainv[0], c->d_Ainv[1], c->d_Wt, c->d_Wu,    c->d_partial,  c->d_rhs,
+        c->d_x,     c->d_load_t, c->d_load_u, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+        c->d_fbc_map};
+    const int lrc = run_march_loop(c, 0, numstep, ptrs, [&]() -> int {
+        for (int st = 1; st <= numstep - 1; st++) {
+            const int rc = fp64_step(c, st, lhs_c);
+            if (rc != TDBEM_OK) return rc;
+        }
+        return TDBEM_OK;
+    });
+    if (lrc != TDBEM_OK) return lrc;
     c->timings[2] = tmr.stop_ms(s);
     if (u_hist)
         CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
@@ -718,6 +782,10 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
 int tdbem_ctx_destroy(tdbem_ctx* c) {
     if (!c) return TDBEM_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->graph.exec) {
+        cudaGraphExecDestroy(c->graph.exec);
+        c->graph.exec = nullptr;
+    }
     free_levels(c);
     free_march(c);
     dfree(c->d_coords);
@@ -1838,6 +1906,17 @@ int tdbem_group_shape(int* lanes, int* block, int* blocks_per_sm) {
     if (lanes) *lanes = sh.lanes;
     if (block) *block = sh.block;
     if (blocks_per_sm) *blocks_per_sm = sh.blocks_per_sm;
+    return TDBEM_OK;
+}
+
+int tdbem_set_graphs(tdbem_ctx* c, int on) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    c->use_graphs = on != 0;
+    if (!c->use_graphs && c->graph.exec) {
+        cudaStreamSynchronize(c->stream);
+        cudaGraphExecDestroy(c->graph.exec);
+        c->graph.exec = nullptr;
+    }
     return TDBEM_OK;
 }
 

@@ -266,6 +266,17 @@ cudaError_t launch_update_batch(const double* x, int D, int C, int s, const unsi
 
 }  // namespace tdbem
 
+// A captured marching loop and the values its kernel arguments were captured
+// with (a change of any of them means a new capture).
+struct MarchGraph {
+    cudaGraphExec_t exec = nullptr;
+    int kind = -1, numstep = 0, nb = 0, refine = 0;
+    double a1 = 0, a2 = 0;
+    std::vector<double> amp;
+    std::vector<const void*> ptrs;
+    long long launches = 0;  // kernels in the graph
+};
+
 // The context (capi.cu owns its lifetime).
 struct tdbem_ctx {
     int device = 0;
@@ -338,6 +349,8 @@ struct tdbem_ctx {
     int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
     tdbem::TcMaps tc_maps{};
     // stepwise marching (tdbem_march_begin / tdbem_march_step) and host-block levels
+    bool use_graphs = true;         // replay the marching loop as a CUDA graph
+    MarchGraph graph;
     int step_numstep = -1;
     bool step_inv_ready[2] = {false, false};
     double* d_upd_tmp = nullptr;    // one row block of tdbem_update_gh_linear

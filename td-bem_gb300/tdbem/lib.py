@@ -58,6 +58,7 @@ SIGNATURES = {
     "tdbem_launch_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "tdbem_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
                                             ctypes.c_int]),
     "tdbem_march_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
@@ -323,6 +324,9 @@ class Context:
 
     def set_march_options(self, block_steps: int = 12, refine_sweeps: int = 1):
         _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
+
+    def set_graphs(self, on: bool):
+        _check(load().tdbem_set_graphs(self.h, 1 if on else 0))
 
     def set_batch_options(self, engine: int = 0, refine_sweeps: int = 0):
         _check(load().tdbem_set_batch_options(self.h, engine, refine_sweeps))

@@ -71,3 +71,28 @@ def test_refinement_recovers_fp64_solve(tdlib, sphere8):
     e0 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=0)[0], u)
     e2 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=2)[0], u)
     assert e2 <= e0 and e2 <= TOL_L2
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_graph_replay_is_bitwise_the_direct_loop(tdlib, precision):
+    """The marching loop replayed as a CUDA graph gives the histories of the direct
+    loop bitwise; a new load history is captured anew."""
+    z, m = load_golden("bar_1x1x4_q2_alpha")
+    prec = tdlib.MIXED if precision == "mixed" else tdlib.FP64
+    t = np.arange(m.numstep) * m.dt
+    amp2 = np.exp(-0.5 * ((t - 10 * m.dt) / (4 * m.dt)) ** 2)
+    out = {}
+    for graphs in (False, True):
+        with tdlib.Context(m) as ctx:
+            ctx.set_alpha(0.25, 0.1)
+            ctx.set_graphs(graphs)
+            ctx.assemble(precision=prec)
+            first = ctx.march()
+            again = ctx.march()  # replay (or the same direct loop)
+            ctx.set_load_history(amp2)
+            other = ctx.march()  # a new capture
+            out[graphs] = (first, again, other)
+    for a, b in zip(out[False], out[True]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(out[True][0][0], out[True][1][0])
+    assert not np.array_equal(out[True][0][0], out[True][2][0])
