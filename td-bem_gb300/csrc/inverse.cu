@@ -1,4 +1,7 @@
 // Blocked in-place Gauss-Jordan inversion with partial pivoting (FP32 / FP64).
+// The pivot search of each panel runs in one thread-block cluster with the panel in
+// distributed shared memory (k_panel_pivots_cluster) when the panel fits in 16
+// CTAs' shared memory, else on a cooperative grid (k_panel_pivots).
 //
 // Replaces KSPSolve's factorisation (SolverStepLinearT.cpp:503-504) by an
 // explicit inverse of the column-exchanged LHS, computed once per distinct LHS.
@@ -130,6 +133,139 @@ __global__ void __launch_bounds__(256) k_panel_pivots(const T* __restrict__ A, i
         }
         __syncthreads();
     }
+}
+
+// The same pivot sequence with the panel held in the distributed shared memory of
+// one thread-block cluster (CS CTAs): per column every CTA publishes its best
+// candidate (value, row, the row's panel entries) and, if it owns it, row c in
+// its own shared memory; after a hardware cluster barrier every CTA reads all
+// CTAs' candidates through DSMEM and picks the same pivot as k_panel_pivots.
+// Publications alternate between two slots by column parity: a CTA can only
+// reuse a slot after the next column's barrier, which every reader passes only
+// once it has finished reading.  A final barrier keeps every CTA's shared memory
+// alive until no other CTA can read it.
+template <typename T, int BW>
+__global__ void __launch_bounds__(1024) k_panel_pivots_cluster(const T* __restrict__ A, int n,
+                                                               int k0, int bw, int rpb,
+                                                               int* __restrict__ perm,
+                                                               int* __restrict__ status) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ unsigned char smem_raw[];
+    T* ws = reinterpret_cast<T*>(smem_raw);  // rpb x BW
+    __shared__ T wv[32];
+    __shared__ int wi[32];
+    __shared__ T su[BW];
+    __shared__ T cand_val[2];
+    __shared__ int cand_idx[2];
+    __shared__ T cand_row[2][BW];
+    __shared__ T row_c[2][BW];
+    __shared__ int s_p, s_b;
+    const int nb = (int)cluster.num_blocks();
+    const int me = (int)cluster.block_rank();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int rows = n - k0;
+    const int r0 = me * rpb, r1 = min(rows, r0 + rpb);
+    for (int idx = threadIdx.x; idx < rpb * BW; idx += blockDim.x) {
+        const int r = idx / BW, c = idx % BW;
+        ws[idx] = (r0 + r < r1 && c < bw) ? A[(size_t)(k0 + r0 + r) * n + k0 + c] : T(0);
+    }
+    __syncthreads();
+    // (value, row): larger value wins, then the lower row
+    auto better = [](T v2, int i2, T v, int i) { return v2 > v || (v2 == v && i2 < i); };
+    for (int c = 0; c < bw; c++) {
+        const int par = c & 1;
+        // ---- this CTA's candidate: thread, warp, then block arg-max
+        T best = T(-1);
+        int bi = rows;
+        for (int r = max(r0, c) + threadIdx.x; r < r1; r += blockDim.x) {
+            const T v = absv(ws[(r - r0) * BW + c]);
+            if (better(v, r, best, bi)) { best = v; bi = r; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const T v2 = __shfl_xor_sync(0xffffffffu, best, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (better(v2, i2, best, bi)) { best = v2; bi = i2; }
+        }
+        if (lane == 0) {
+            wv[warp] = best;
+            wi[warp] = bi;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            best = lane < nwarp ? wv[lane] : T(-1);
+            bi = lane < nwarp ? wi[lane] : rows;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const T v2 = __shfl_xor_sync(0xffffffffu, best, o);
+                const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (better(v2, i2, best, bi)) { best = v2; bi = i2; }
+            }
+            if (lane == 0) {
+                cand_val[par] = best;
+                cand_idx[par] = bi;
+            }
+            // the candidate row (and row c, if this CTA owns it) for the other CTAs
+            for (int t = lane; t < BW; t += 32) {
+                if (bi < r1) cand_row[par][t] = ws[(bi - r0) * BW + t];
+                if (c >= r0 && c < r1) row_c[par][t] = ws[(c - r0) * BW + t];
+            }
+        }
+        cluster.sync();
+        if (warp == 0) {  // one lane per CTA reads its candidate; the same arg-max in every CTA
+            T bv = T(-1);
+            int bp = rows, bb = lane;
+            if (lane < nb) {
+                bv = *cluster.map_shared_rank(&cand_val[par], lane);
+                bp = *cluster.map_shared_rank(&cand_idx[par], lane);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const T v2 = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int i2 = __shfl_xor_sync(0xffffffffu, bp, o);
+                const int b2 = __shfl_xor_sync(0xffffffffu, bb, o);
+                if (better(v2, i2, bv, bp)) { bv = v2; bp = i2; bb = b2; }
+            }
+            if (lane == 0) {
+                s_p = (bp < rows && bv != T(0)) ? bp : -1;
+                s_b = bb;
+            }
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p < 0) {  // zero pivot: every CTA sees it; leave together
+            if (me == 0 && threadIdx.x == 0) *status = 1;
+            cluster.sync();
+            return;
+        }
+        if (threadIdx.x < BW) {
+            const T pv = cluster.map_shared_rank(&cand_row[par][0], s_b)[threadIdx.x];
+            su[threadIdx.x] = pv;
+            if (c >= r0 && c < r1) ws[(c - r0) * BW + threadIdx.x] = pv;
+            if (p != c && p >= r0 && p < r1)
+                ws[(p - r0) * BW + threadIdx.x] =
+                    cluster.map_shared_rank(&row_c[par][0], c / rpb)[threadIdx.x];
+        }
+        if (me == 0 && threadIdx.x == 0) perm[k0 + c] = k0 + p;
+        __syncthreads();
+        // ---- eliminate below row c: multipliers, then the (row, column) updates
+        const T inv = T(1) / su[c];
+        const int rb = max(r0, c + 1);
+        for (int r = rb + threadIdx.x; r < r1; r += blockDim.x) ws[(r - r0) * BW + c] *= inv;
+        __syncthreads();
+        const int w = bw - c - 1;
+        if (w > 0) {
+            const int cnt = (r1 > rb) ? (r1 - rb) * w : 0;
+            for (int idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
+                const int r = rb + idx / w, j = c + 1 + idx % w;
+                T* wr = ws + (r - r0) * BW;
+                wr[j] -= wr[c] * su[j];
+            }
+        }
+        __syncthreads();
+    }
+    cluster.sync();
 }
 
 // Row swaps of the panel applied to every column, in pivot order.
@@ -313,6 +449,46 @@ __global__ void k_cast_f64_f32(const double* __restrict__ a, float* __restrict__
         b[i] = (float)a[i];
 }
 
+constexpr size_t kClusterPanelBytes = 200 * 1024;  // panel rows per CTA of a cluster
+
+// Whether a cluster of cs CTAs of the pivot kernel can be resident on this device
+// (checked once per size; 16 needs the non-portable cluster size).
+bool cluster_ok(int cs) {
+    static int ok[2] = {-1, -1};  // cluster sizes 8 and 16
+    int& v = ok[cs == 16 ? 1 : 0];
+    if (v >= 0) return v == 1;
+    v = 0;
+    const void* fn8 = (const void*)k_panel_pivots_cluster<float, 64>;
+    const void* fn16 = (const void*)k_panel_pivots_cluster<double, 16>;
+    for (const void* fn : {fn8, fn16}) {
+        if (cs == 16 &&
+            cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess)
+            return false;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kClusterPanelBytes) != cudaSuccess)
+            return false;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(1024);
+        cfg.dynamicSmemBytes = kClusterPanelBytes;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cs;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess || nclusters < 1) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    v = 1;
+    return true;
+}
+
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
                            cudaStream_t s) {
@@ -338,10 +514,39 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         }
         int kk0 = k0, kbw = bw, kn = n;
         const T* cA = A;
-        void* args[] = {&cA, &kn, &kk0, &kbw, &rpb, &perm, &d_status, &gval, &gidx, &grows};
-        e = cudaLaunchCooperativeKernel((const void*)k_panel_pivots<T, BW>, dim3(nblk), dim3(256),
-                                        args, smem, s);
-        if (e != cudaSuccess) return e;
+        // the panel in one cluster's distributed shared memory when it fits
+        bool done = false;
+        for (int cs : {16, 8}) {
+            const int crpb = (rows + cs - 1) / cs;
+            const size_t csmem = (size_t)crpb * BW * sizeof(T);
+            if (csmem > kClusterPanelBytes || !cluster_ok(cs)) continue;
+            e = cudaFuncSetAttribute((const void*)k_panel_pivots_cluster<T, BW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
+            if (e != cudaSuccess) return e;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(cs);
+            cfg.blockDim = dim3(1024);
+            cfg.dynamicSmemBytes = csmem;
+            cfg.stream = s;
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = cs;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            e = cudaLaunchKernelEx(&cfg, k_panel_pivots_cluster<T, BW>, cA, kn, kk0, kbw, crpb,
+                                   perm, d_status);
+            if (e != cudaSuccess) return e;
+            done = true;
+            break;
+        }
+        if (!done) {
+            void* args[] = {&cA, &kn, &kk0, &kbw, &rpb, &perm, &d_status, &gval, &gidx, &grows};
+            e = cudaLaunchCooperativeKernel((const void*)k_panel_pivots<T, BW>, dim3(nblk),
+                                            dim3(256), args, smem, s);
+            if (e != cudaSuccess) return e;
+        }
         k_apply_swaps<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
         k_panel_inv<T, BW><<<1, 1024, 0, s>>>(A, n, k0, bw, Ainv, d_status);
         k_panel_t12<T, BW><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, Ainv, T12, d_status);
