@@ -606,9 +606,11 @@ __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool d
     const float rdn = rv[0] * nq[0] + rv[1] * nq[1] + rv[2] * nq[2];
     const float rho_p = r * f.inv_cp, rho_s = r * f.inv_cs;
     const float tp = TI - rho_p, ts = TI - rho_s;  // tau of each wave at T = TI
-    // exact zero once the S front has passed at both times of a part
-    const bool doI = doI0 && !(ts - f.dt >= f.dt);
-    const bool doJ = doJ0 && !(ts >= f.dt);
+    // exact zero once the S front has passed at both times of a part, and before the
+    // P front arrives (b = 0 and no I5/J5 step at both times of the part: every term
+    // of the part is then exactly zero)
+    const bool doI = doI0 && !(ts - f.dt >= f.dt) && !(tp < 0.f);
+    const bool doJ = doJ0 && !(ts >= f.dt) && !(tp + f.dt < 0.f);
     if (!doI && !doJ) return;
     float P1 = 0.f, P3 = 0.f, P5 = 0.f, S2 = 0.f, S4 = 0.f, S6 = 0.f;
     float a1, a3, a5, b1, b3, b5;

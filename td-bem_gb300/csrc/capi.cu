@@ -395,13 +395,14 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                                   lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], s));
         if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(D)));
         const int pe = prof_begin(c, TDBEM_K_FACTOR);
+        bool singular = false;
         cudaError_t e = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, c->d_perm, c->d_status,
-                                   c->d_inv_scratch32, &c->launches, s);
+                                   c->d_inv_scratch32, &c->launches, &singular, s);
         prof_end(c, pe, 2.0 * 4 * DD, 2.0 * (double)D * D * D);
         c->launches += 1;
-        if (e == cudaErrorInvalidValue)
-            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
         CUDA_TRY(e);
+        if (singular)
+            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
     }
     if (ninv == 1) {
         if (c->d_inv32[1] && c->d_inv32[1] != c->d_inv32[0]) dfree(c->d_inv32[1]);
@@ -479,13 +480,15 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             CUDA_TRY(launch_reduce_cols(c->d_pmix, nch, 1, D, c->d_Yold + (size_t)j * D,
                                         c->d_rhs, s));
             const int v = st == 1 ? 0 : 1;
+            // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
             CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_rhs, c->d_x,
-                                        c->d_res, c->d_dx, c->n_refine, s));
+                                        c->d_res, reinterpret_cast<float*>(c->d_dx), c->n_refine,
+                                        s));
             CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
                                          c->d_fbc_map, amp, c->d_u, c->d_t, s));
             prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine) / 1.0,
                      2.0 * (double)DD * (1 + 2 * c->n_refine));
-            c->launches += 4 + 1 + 3LL * c->n_refine + 1;
+            c->launches += 6 + 2LL * c->n_refine;  // W, conv, reduce, cast, gemv(s), update
         }
     }
     return TDBEM_OK;
@@ -559,13 +562,14 @@ int fp64_inverse(tdbem_ctx* c, int v, const double lhs_c[2][2]) {
                               lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
     if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
     const int pe = prof_begin(c, TDBEM_K_FACTOR);
+    bool singular = false;
     cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
-                               &c->launches, s);
+                               &c->launches, &singular, s);
     prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
     c->launches += 1;  // LHS build
-    if (e == cudaErrorInvalidValue)
-        return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
     CUDA_TRY(e);
+    if (singular)
+        return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
     return TDBEM_OK;
 }
 

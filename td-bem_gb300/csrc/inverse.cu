@@ -489,9 +489,32 @@ bool cluster_ok(int cs) {
     return true;
 }
 
+// The pivot kernels' dynamic shared-memory limit, raised once per kernel to the
+// largest panel any call uses (a per-call setting would race between host threads
+// inverting at the same time: one could lower the limit under another's launch).
+template <typename T, int BW>
+cudaError_t pivot_attributes() {
+    static const cudaError_t e = [] {
+        cudaError_t r = cudaFuncSetAttribute((const void*)k_panel_pivots<T, BW>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kClusterPanelBytes);
+        if (r == cudaSuccess)
+            r = cudaFuncSetAttribute((const void*)k_panel_pivots_cluster<T, BW>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kClusterPanelBytes);
+        return r;
+    }();
+    return e;
+}
+
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
-                           cudaStream_t s) {
+                           bool* singular, cudaStream_t s) {
+    *singular = false;
+    {
+        const cudaError_t ea = pivot_attributes<T, BW>();
+        if (ea != cudaSuccess) return ea;
+    }
     T* W = scratch;                          // 2*BW*n: permutation scratch rows at the end
     T* T12 = W + (size_t)n * BW;             // BW x n
     T* Ainv = T12 + (size_t)n * BW;          // BW x BW
@@ -507,11 +530,7 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         const int nblk = std::max(1, std::min(kMaxPivotBlocks, (rows + 63) / 64));
         int rpb = (rows + nblk - 1) / nblk;
         size_t smem = (size_t)rpb * BW * sizeof(T);
-        if (smem > 48 * 1024) {
-            e = cudaFuncSetAttribute((const void*)k_panel_pivots<T, BW>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
+        if (smem > kClusterPanelBytes) return cudaErrorInvalidConfiguration;  // panel too tall
         int kk0 = k0, kbw = bw, kn = n;
         const T* cA = A;
         // the panel in one cluster's distributed shared memory when it fits
@@ -520,9 +539,6 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
             const int crpb = (rows + cs - 1) / cs;
             const size_t csmem = (size_t)crpb * BW * sizeof(T);
             if (csmem > kClusterPanelBytes || !cluster_ok(cs)) continue;
-            e = cudaFuncSetAttribute((const void*)k_panel_pivots_cluster<T, BW>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem);
-            if (e != cudaSuccess) return e;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(cs);
             cfg.blockDim = dim3(1024);
@@ -564,7 +580,10 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         e = cudaMemcpyAsync(hperm.data(), perm, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
-    if (status) return cudaErrorInvalidValue;  // zero pivot
+    if (status) {  // zero pivot
+        *singular = true;
+        return cudaSuccess;
+    }
     std::vector<int> cols(n);
     for (int j = 0; j < n; j++) cols[j] = j;
     for (int k = n - 1; k >= 0; k--) std::swap(cols[k], cols[hperm[k]]);
@@ -585,15 +604,15 @@ size_t inverse_scratch_elems(int n) {
 }
 
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
-                       long long* nlaunch, cudaStream_t s) {
-    return invert_blocked<double, 16>(A, n, perm, d_status, scratch, nlaunch, s);
+                       long long* nlaunch, bool* singular, cudaStream_t s) {
+    return invert_blocked<double, 16>(A, n, perm, d_status, scratch, nlaunch, singular, s);
 }
 
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
-                       float* scratch, long long* nlaunch, cudaStream_t s) {
+                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s) {
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
-    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, s);
+    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s);
 }
 
 }  // namespace tdbem

@@ -188,9 +188,10 @@ __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, i
 }
 
 // y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
-// row, pairs of columns per load when D is even.
+// row, pairs of columns per load when D is even.  v is FP32: converting an FP64
+// vector in every row would put D^2 conversions on GB300's narrow FP64 pipe.
 __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, int D,
-                                                  const double* __restrict__ v,
+                                                  const float* __restrict__ v,
                                                   double* __restrict__ y, int accumulate) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= D) return;
@@ -198,14 +199,14 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
     float acc = 0.f;
     if ((D & 1) == 0) {
         const float2* a2 = reinterpret_cast<const float2*>(a);
-        const double2* v2 = reinterpret_cast<const double2*>(v);
+        const float2* v2 = reinterpret_cast<const float2*>(v);
         for (int j = lane; j < D / 2; j += 32) {
             const float2 x = __ldcs(a2 + j);
-            const double2 w = v2[j];
-            acc += x.x * (float)w.x + x.y * (float)w.y;
+            const float2 w = v2[j];
+            acc += x.x * w.x + x.y * w.y;
         }
     } else {
-        for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * (float)v[j];
+        for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * v[j];
     }
     double s = acc;
 #pragma unroll
@@ -213,11 +214,12 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
     if (lane == 0) y[row] = accumulate ? y[row] + s : s;
 }
 
-// r = b - A64 x, FP64; warp per row.
+// r = b - A64 x, FP64, warp per row; also r in FP32 for the correction product.
 __global__ void __launch_bounds__(256) k_residual_f64(const double* __restrict__ A, int D,
                                                       const double* __restrict__ x,
                                                       const double* __restrict__ b,
-                                                      double* __restrict__ r) {
+                                                      double* __restrict__ r,
+                                                      float* __restrict__ r32) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= D) return;
     const double* a = A + (size_t)row * D;
@@ -225,12 +227,16 @@ __global__ void __launch_bounds__(256) k_residual_f64(const double* __restrict__
     for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * x[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) r[row] = b[row] - acc;
+    if (lane == 0) {
+        const double v = b[row] - acc;
+        r[row] = v;
+        r32[row] = (float)v;
+    }
 }
 
-__global__ void k_add(double* __restrict__ x, const double* __restrict__ d, int n) {
+__global__ void k_to_f32(const double* __restrict__ v, float* __restrict__ v32, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += d[i];
+    if (i < n) v32[i] = (float)v[i];
 }
 
 }  // namespace
@@ -289,15 +295,16 @@ cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D
     return cudaGetLastError();
 }
 
-// x = inv32 rhs, then n_refine times: r = rhs - A64 x; x += inv32 r.
+// x = inv32 rhs, then n_refine times: r = rhs - A64 x; x += inv32 r.  v32 is D
+// floats of scratch (the FP32 copy of the vector each product reads).
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
-                               double* x, double* r, double* dx, int n_refine, cudaStream_t s) {
+                               double* x, double* r, float* v32, int n_refine, cudaStream_t s) {
     const unsigned g = (D * 32 + 255) / 256;
-    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, rhs, x, 0);
+    k_to_f32<<<(D + 255) / 256, 256, 0, s>>>(rhs, v32, D);
+    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 0);
     for (int it = 0; it < n_refine; it++) {
-        k_residual_f64<<<g, 256, 0, s>>>(A64, D, x, rhs, r);
-        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, r, dx, 0);
-        k_add<<<(D + 255) / 256, 256, 0, s>>>(x, dx, D);
+        k_residual_f64<<<g, 256, 0, s>>>(A64, D, x, rhs, r, v32);
+        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 1);
     }
     return cudaGetLastError();
 }

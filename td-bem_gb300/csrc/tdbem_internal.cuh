@@ -180,10 +180,11 @@ constexpr int kPermuteBlocks = 152;  // scratch rows the final column permutatio
 // elements, perm has n + 2 * kMaxPivotBlocks ints.
 constexpr int kMaxPivotBlocks = 32;
 size_t inverse_scratch_elems(int n);
+// *singular is set (and cudaSuccess returned) when a pivot is exactly zero.
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
-                       long long* nlaunch, cudaStream_t s);
+                       long long* nlaunch, bool* singular, cudaStream_t s);
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
-                       float* scratch, long long* nlaunch, cudaStream_t s);
+                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s);
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
                                    int L, double a1, double a2, double a3, double c0,
                                    double c1, double amp, const double* load_t,
@@ -242,7 +243,7 @@ cudaError_t launch_build_w_new(const double* u_hist, const double* t_hist, int D
 cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
                                const double* add, double* out, cudaStream_t s);
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
-                               double* x, double* r, double* dx, int n_refine, cudaStream_t s);
+                               double* x, double* r, float* v32, int n_refine, cudaStream_t s);
 
 // Batched marching of many load cases (batch.cu).
 int batch_block_cases();            // cases per tensor-core column block
