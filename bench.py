@@ -364,7 +364,7 @@ def run_ours(args, dist):
     ctx.set_alpha(*ALPHA)
     engine = lib.ENGINE_TCGEN05 if args.engine == "tcgen05" else lib.ENGINE_MMA_SYNC
     refine = args.refine if args.refine is not None else (0 if cases else 1)
-    ctx.set_march_options(12, refine)
+    ctx.set_march_options(8, refine)
     ctx.set_batch_options(engine, refine)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -419,7 +419,7 @@ def run_ours(args, dist):
         t0 = time.perf_counter()
         with lib.Context(model) as c2:
             c2.set_alpha(*ALPHA)
-            c2.set_march_options(12, refine)
+            c2.set_march_options(8, refine)
             c2.set_batch_options(engine, refine)
             c2.assemble(precision=prec)
             if cases:

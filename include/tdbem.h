@@ -232,8 +232,9 @@ int tdbem_set_batch_options(tdbem_ctx* ctx, int engine, int refine_sweeps);
 int tdbem_set_graphs(tdbem_ctx* ctx, int on);
 
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
- * history convolution (1, 8, 12 or 16; default 12), refine_sweeps = FP64
- * residual-refinement sweeps per solve (0..4; default 1). */
+ * history convolution (1, 4, 6, 8, 12 or 16; default 8, the fastest on GB300 for
+ * the 4614-DOF sphere), refine_sweeps = FP64 residual-refinement sweeps per solve
+ * (0..4; default 1). */
 int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
 
 /* Device pointers of the histories of the last tdbem_march (FP64,

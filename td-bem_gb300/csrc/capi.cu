@@ -1937,8 +1937,9 @@ int tdbem_set_batch_options(tdbem_ctx* c, int engine, int refine_sweeps) {
 
 int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
     if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (block_steps != 1 && block_steps != 8 && block_steps != 12 && block_steps != 16)
-        return fail(TDBEM_ERR_ARG, "block_steps must be 1, 8, 12 or 16");
+    if (block_steps != 1 && block_steps != 4 && block_steps != 6 && block_steps != 8 &&
+        block_steps != 12 && block_steps != 16)
+        return fail(TDBEM_ERR_ARG, "block_steps must be 1, 4, 6, 8, 12 or 16");
     if (refine_sweeps < 0 || refine_sweeps > 4)
         return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
     if (block_steps != c->nb) {  // scratch sized by the block

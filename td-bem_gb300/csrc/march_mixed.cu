@@ -261,6 +261,8 @@ cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int 
     const float* wu = Wu - (size_t)f_lo * nb * ldw;
     switch (nb) {
     case 1: k_conv_f32<1><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 4: k_conv_f32<4><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 6: k_conv_f32<6><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
     case 8: k_conv_f32<8><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
     case 12: k_conv_f32<12><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
     case 16: k_conv_f32<16><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;

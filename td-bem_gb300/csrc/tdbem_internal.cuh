@@ -316,7 +316,7 @@ struct tdbem_ctx {
     double* d_G01 = nullptr;        // mixed: levels 0 and 1 in FP64 (the LHS)
     double* d_H01 = nullptr;
     // mixed marching
-    int nb = 12;                    // steps per time block
+    int nb = 8;                     // steps per time block
     int n_refine = 1;               // FP64 refinement sweeps per solve
     float* d_inv32[2] = {nullptr, nullptr};
     double* d_Hc64[2] = {nullptr, nullptr};
