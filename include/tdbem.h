@@ -52,9 +52,9 @@ typedef struct tdbem_ctx tdbem_ctx;
 typedef struct {
     int nnd;              /* number of nodes                                  */
     int nel;              /* number of elements                               */
-    int etype;            /* 1 = 4-node bilinear quad (8-node: UNSUPPORTED)   */
+    int etype;            /* 1 = 4-node bilinear quad, 2 = 8-node serendipity */
     const double* coords; /* nnd x 3                                          */
-    const int* ien;       /* nel x 4, 0-based node ids                        */
+    const int* ien;       /* nel x 4 (etype 1) or nel x 8 (etype 2), 0-based  */
 } tdbem_mesh;
 
 /* Replaces ModelManagerT::GetMaterialConstants (ModelManagerT.h:92). */

@@ -35,7 +35,8 @@ namespace tdbem {
 
 namespace {
 
-constexpr int kGeomStride = 12;  // x[3], n[3], wJ, N[4], pad
+constexpr int kGeomStride = 12;   // Q4: x[3], n[3], wJ, N[4], pad
+constexpr int kGeomStride8 = 16;  // Q8: x[3], n[3], wJ, N[8], pad
 
 // ShapeFunctionT::Evaluate for the 4-node quad (ShapeFunctionT.cpp:241-301).
 __device__ __forceinline__ void q4_eval(const double* c, double e1, double e2, double N[4],
@@ -84,6 +85,79 @@ __device__ __forceinline__ void duffy_point(const double* c, int corner, int tri
     double J;
     q4_eval(c, e1, e2, N, x, n, J);
     wJ = w * J_tri * J;
+}
+
+// ShapeFunctionT::Evaluate for the 8-node serendipity quad (ShapeFunctionT.cpp:303-366).
+__device__ __forceinline__ void q8_eval(const double* c, double e1, double e2, double N[8],
+                                        double x[3], double n[3], double& J) {
+    const double e1s = e1 * e1, e2s = e2 * e2;
+    N[0] = 0.25 * (1 - e1) * (1 - e2) * (-e1 - e2 - 1);
+    N[1] = 0.25 * (1 + e1) * (1 - e2) * (e1 - e2 - 1);
+    N[2] = 0.25 * (1 + e1) * (1 + e2) * (e1 + e2 - 1);
+    N[3] = 0.25 * (1 - e1) * (1 + e2) * (-e1 + e2 - 1);
+    N[4] = 0.5 * (1 - e1s) * (1 - e2);
+    N[5] = 0.5 * (1 + e1) * (1 - e2s);
+    N[6] = 0.5 * (1 - e1s) * (1 + e2);
+    N[7] = 0.5 * (1 - e1) * (1 - e2s);
+    const double d1[8] = {-0.25 * (1 - e1) * (1 - e2) - 0.25 * (1 - e2) * (-1 - e1 - e2),
+                          0.25 * (1 + e1) * (1 - e2) + 0.25 * (1 - e2) * (-1 + e1 - e2),
+                          0.25 * (1 + e1) * (1 + e2) + 0.25 * (1 + e2) * (-1 + e1 + e2),
+                          -0.25 * (1 - e1) * (1 + e2) - 0.25 * (1 + e2) * (-1 - e1 + e2),
+                          -e1 * (1 - e2),
+                          0.5 * (1 - e2s),
+                          -e1 * (1 + e2),
+                          -0.5 * (1 - e2s)};
+    const double d2[8] = {-0.25 * (1 - e1) * (1 - e2) - 0.25 * (1 - e1) * (-1 - e1 - e2),
+                          -0.25 * (1 + e1) * (1 - e2) - 0.25 * (1 + e1) * (-1 + e1 - e2),
+                          0.25 * (1 + e1) * (1 + e2) + 0.25 * (1 + e1) * (-1 + e1 + e2),
+                          0.25 * (1 - e1) * (1 + e2) + 0.25 * (1 - e1) * (-1 - e1 + e2),
+                          -0.5 * (1 - e1s),
+                          -(1 + e1) * e2,
+                          0.5 * (1 - e1s),
+                          -(1 - e1) * e2};
+    double dx1[3] = {0, 0, 0}, dx2[3] = {0, 0, 0};
+    x[0] = x[1] = x[2] = 0;
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            x[d] += N[a] * c[a * 3 + d];
+            dx1[d] += d1[a] * c[a * 3 + d];
+            dx2[d] += d2[a] * c[a * 3 + d];
+        }
+    n[0] = dx1[1] * dx2[2] - dx1[2] * dx2[1];
+    n[1] = dx1[2] * dx2[0] - dx1[0] * dx2[2];
+    n[2] = dx1[0] * dx2[1] - dx1[1] * dx2[0];
+    J = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] /= J;
+    n[1] /= J;
+    n[2] /= J;
+}
+
+// SubElement (TDElementStepLinearT.cpp:192-386): a singular 8-node element is
+// integrated as 4-node sub-elements over parent nodes; a singular corner keeps
+// the corner quad (its corner singular), a singular midside node splits the
+// element into two quads singular at their first corner.
+__device__ __forceinline__ int q8_subelements(int singular, int ids[2][4], int cid[2]) {
+    constexpr int mid[4][2][4] = {
+        {{4, 6, 3, 0}, {4, 1, 2, 6}},
+        {{5, 2, 3, 7}, {5, 7, 0, 1}},
+        {{6, 3, 0, 4}, {6, 4, 1, 2}},
+        {{7, 0, 1, 5}, {7, 5, 2, 3}},
+    };
+    if (singular < 4) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) ids[0][i] = i;
+        cid[0] = singular;
+        return 1;
+    }
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) ids[e][i] = mid[singular - 4][e][i];
+        cid[e] = 0;
+    }
+    return 2;
 }
 
 // I-part time integrals of one wave at time T (GreenFunctionT.cpp:251-279):
@@ -165,11 +239,13 @@ struct ItemAcc {
     double h[4][9];
 };
 
-// One Gauss point of one item: step responses for the item's time(s), the
-// collected 3x3 kernels and the accumulation into the 4 node blocks.
-__device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, const Phys& ph,
-                                            const double xc[3], const double xq[3],
-                                            const double nq[3], double wJ, const double N[4]) {
+// One Gauss point of one item: step responses for the item's time(s) and the
+// collected 3x3 kernels, sg = DU (symmetric, 6 entries) and th[i][j] = DT[j][i].
+// Returns false when both parts are exactly zero at this point.
+__device__ __forceinline__ bool point_kernels(const TimeConsts& tc, const Phys& ph,
+                                              const double xc[3], const double xq[3],
+                                              const double nq[3], double sg[6],
+                                              double th[9]) {
     const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
     const double r = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
     const double inv_r = 1.0 / r;
@@ -183,7 +259,7 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
     // (b = dt and I5 = I6 = 0 at both times): skip it instead of summing round-off.
     const bool doI = tc.doI && !(tc.TI1 - roc_s >= ph.dt);
     const bool doJ = tc.doJ && !(tc.TJ1 - roc_s >= ph.dt);
-    if (!doI && !doJ) return;
+    if (!doI && !doJ) return false;
     double P1 = 0, P3 = 0, P5 = 0, S2 = 0, S4 = 0, S6 = 0;
     if (doI) {
         double a1, a3, a5, b1, b3, b5;
@@ -231,10 +307,14 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
 
     const double rr00 = rv[0] * rv[0], rr01 = rv[0] * rv[1], rr02 = rv[0] * rv[2];
     const double rr11 = rv[1] * rv[1], rr12 = rv[1] * rv[2], rr22 = rv[2] * rv[2];
-    const double sg[6] = {A * rr00 + B, A * rr01, A * rr02, A * rr11 + B, A * rr12, A * rr22 + B};
+    sg[0] = A * rr00 + B;
+    sg[1] = A * rr01;
+    sg[2] = A * rr02;
+    sg[3] = A * rr11 + B;
+    sg[4] = A * rr12;
+    sg[5] = A * rr22 + B;
     const double ar = alpha * rdn, gd = gamma * rdn;
     // T[i][j] = DT[j][i] = ar r_i r_j + beta n_j r_i + gamma n_i r_j (+ gamma rdn on i == j)
-    double th[9];
     const double rrm[9] = {rr00, rr01, rr02, rr01, rr11, rr12, rr02, rr12, rr22};
 #pragma unroll
     for (int i = 0; i < 3; i++)
@@ -242,6 +322,15 @@ __device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, 
         for (int j = 0; j < 3; j++)
             th[i * 3 + j] = ar * rrm[i * 3 + j] + beta * (nq[j] * rv[i]) +
                             gamma * (nq[i] * rv[j]) + (i == j ? gd : 0.0);
+    return true;
+}
+
+// One Gauss point of one Q4 item, accumulated into the 4 node blocks.
+__device__ __forceinline__ void gauss_point(ItemAcc& acc, const TimeConsts& tc, const Phys& ph,
+                                            const double xc[3], const double xq[3],
+                                            const double nq[3], double wJ, const double N[4]) {
+    double sg[6], th[9];
+    if (!point_kernels(tc, ph, xc, xq, nq, sg, th)) return;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
         const double w = wJ * N[a];
@@ -300,6 +389,34 @@ __global__ void k_gauss_geom(const double* __restrict__ coords, const int* __res
     gf[11] = 0.f;
 }
 
+// Gauss-point geometry of 8-node elements: x[3], n[3], w J, N[8] (stride kGeomStride8).
+__global__ void k_gauss_geom8(const double* __restrict__ coords, const int* __restrict__ ien,
+                              int nel, int nq, const double* __restrict__ gx,
+                              const double* __restrict__ gw, double* __restrict__ geom) {
+    const int nq2 = nq * nq;
+    const long long gid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (gid >= (long long)nel * nq2) return;
+    const int e = (int)(gid / nq2), q = (int)(gid % nq2);
+    double c[24];
+    for (int a = 0; a < 8; a++) {
+        const int nid = ien[e * 8 + a];
+        for (int d = 0; d < 3; d++) c[a * 3 + d] = coords[nid * 3 + d];
+    }
+    const int q1 = q / nq, q2 = q % nq;
+    double N[8], x[3], n[3], J;
+    q8_eval(c, gx[q1], gx[q2], N, x, n, J);
+    double* g = geom + gid * kGeomStride8;
+    g[0] = x[0];
+    g[1] = x[1];
+    g[2] = x[2];
+    g[3] = n[0];
+    g[4] = n[1];
+    g[5] = n[2];
+    g[6] = (gw[q1] * gw[q2]) * J;
+    for (int a = 0; a < 8; a++) g[7 + a] = N[a];
+    g[15] = 0;
+}
+
 // Last pair p in [lo, hi] with offsets[p] <= gid (the pair owning item gid).
 __device__ __forceinline__ unsigned find_pair(const unsigned* __restrict__ offsets, unsigned lo,
                                               unsigned hi, unsigned gid) {
@@ -311,29 +428,33 @@ __device__ __forceinline__ unsigned find_pair(const unsigned* __restrict__ offse
     return lo;
 }
 
-// The pair of this thread's item: one full search per block for its first and
-// last items, then a short search inside that range.  Call with all threads of
-// the block (it synchronises); returns false for threads past the last item.
+// The pair of this thread's item (item = global thread index >> SH): one full
+// search per block for its first and last items, then a short search inside that
+// range.  Call with all threads of the block (it synchronises); returns false
+// for threads past the last item.
+template <int SH = 0>
 __device__ __forceinline__ bool item_pair(const unsigned* __restrict__ offsets, unsigned npairs,
                                           unsigned nitems, unsigned& p) {
     __shared__ unsigned s_lo, s_hi;
-    const unsigned first = blockIdx.x * blockDim.x;
-    const unsigned last = min(first + blockDim.x, nitems) - 1;
+    const unsigned first = (blockIdx.x * blockDim.x) >> SH;
+    if (first >= nitems) return false;  // uniform over the block
+    const unsigned last = min(first + (blockDim.x >> SH), nitems) - 1;
     if (threadIdx.x == 0) s_lo = find_pair(offsets, 0, npairs - 1, first);
     if (threadIdx.x == 32) s_hi = find_pair(offsets, 0, npairs - 1, last);
     __syncthreads();
-    const unsigned gid = first + threadIdx.x;
-    if (gid >= nitems) return false;
-    p = find_pair(offsets, s_lo, s_hi, gid);
+    const unsigned item = first + (threadIdx.x >> SH);
+    if (item >= nitems) return false;
+    p = find_pair(offsets, s_lo, s_hi, item);
     return true;
 }
 
 // Singular test of ElastoDynamicsT::G_H_Driver (ElastoDynamicsT.cpp:166-175):
 // the last element node with r^2 < 1e-9 (unfused, as the reference's pow sum).
+template <int ENND = 4>
 __device__ __forceinline__ int singular_corner(const double* c, const double xc[3]) {
     int s = -1;
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
+    for (int a = 0; a < ENND; a++) {
         const double dx = c[a * 3] - xc[0], dy = c[a * 3 + 1] - xc[1], dz = c[a * 3 + 2] - xc[2];
         const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
         if (r2 < 1e-9) s = a;
@@ -343,6 +464,7 @@ __device__ __forceinline__ int singular_corner(const double* c, const double xc[
 
 // Level window (or step membership) and singular corner of pair p (collocation
 // node node_lo + p / ne, element elems[p % ne]).
+template <int ENND = 4>
 __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ coords,
                                                      const int* __restrict__ ien,
                                                      const int* __restrict__ elems, int ne,
@@ -352,25 +474,29 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
-    double nd[12];
+    double nd[3 * ENND];
     double ctr[3] = {0, 0, 0};
-    for (int a = 0; a < 4; a++) {
-        const int nid = ien[e * 4 + a];
+    for (int a = 0; a < ENND; a++) {
+        const int nid = ien[e * ENND + a];
         for (int d = 0; d < 3; d++) {
             nd[a * 3 + d] = coords[nid * 3 + d];
-            ctr[d] += 0.25 * nd[a * 3 + d];
+            ctr[d] += (1.0 / ENND) * nd[a * 3 + d];
         }
     }
     double rad = 0;
-    for (int a = 0; a < 4; a++) {
+    for (int a = 0; a < ENND; a++) {
         const double dx = nd[a * 3] - ctr[0], dy = nd[a * 3 + 1] - ctr[1], dz = nd[a * 3 + 2] - ctr[2];
         rad = fmax(rad, sqrt(dx * dx + dy * dy + dz * dz));
     }
+    // An 8-node element's surface x = sum N_a x_a is no convex combination of its
+    // nodes; sum |N_a| <= 3 on the reference square (at its centre), so the surface
+    // lies within 3 rad of the node centroid.
+    if (ENND == 8) rad *= 3.0;
     const double dx = xc[0] - ctr[0], dy = xc[1] - ctr[1], dz = xc[2] - ctr[2];
     const double dist = sqrt(dx * dx + dy * dy + dz * dz);
     const double margin = 1e-3 * rad + 1e-12;
     const double rmin = fmax(0.0, dist - rad - margin), rmax = dist + rad + margin;
-    const int sing = singular_corner(nd, xc);
+    const int sing = singular_corner<ENND>(nd, xc);
     // The step response at time n dt is exactly zero unless r/c_p <= n dt and
     // n < r/(c_s dt) + 2; level k takes n = k (I part) and n = k + 1 (J part), so it
     // can be non-zero only for r_min/(c_p dt) - 1 <= k < r_max/(c_s dt) + 1 (one level
@@ -395,6 +521,7 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
     return pi;
 }
 
+template <int ENND>
 __global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
                               const int* __restrict__ elems, int ne, int node_lo, int nnodes,
                               Phys ph, int mode, int level_last, int level_cap, int step_n,
@@ -402,8 +529,8 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
                               unsigned* __restrict__ counts) {
     const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= (long long)nnodes * ne) return;
-    const PairInfo pi = pair_window_info(coords, ien, elems, ne, node_lo, ph, mode, level_last,
-                                         level_cap, step_n, select, p);
+    const PairInfo pi = pair_window_info<ENND>(coords, ien, elems, ne, node_lo, ph, mode,
+                                               level_last, level_cap, step_n, select, p);
     pairs[p] = pi;
     counts[p] = (unsigned)pi.cnt;
 }
@@ -413,20 +540,22 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
 // mode ASM_STEP:   item = (pair, step_n), part = 0 -> I part into G0/H0,
 //                  part = 1 -> J part into G1/H1 (row block starting at row_node_lo).
 // One item: pair p (collocation node node_lo + p / ne, element elems[p % ne]) at
-// level (or step) k; accumulates its Gauss points and scatters into out.
-template <int MODE>
+// level (or step) k; accumulates its Gauss points and scatters into out.  An
+// 8-node element's item is split over two threads, half 0 holding the blocks of
+// nodes 0-3 and half 1 those of nodes 4-7 (each evaluates every point's kernels).
+template <int MODE, int ENND = 4>
 __device__ __forceinline__ void assemble_item(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
     const double* __restrict__ gw, const double* __restrict__ geom, const Phys& ph,
     int level_last, int step_n, int part, const PairInfo& pi, unsigned p, int k,
-    const AsmOut& out) {
+    const AsmOut& out, int half = 0) {
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     int nid[4];
 #pragma unroll
-    for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
+    for (int a = 0; a < 4; a++) nid[a] = ien[e * ENND + 4 * half + a];
 
     TimeConsts tc;
     if (MODE == ASM_LEVELS) {
@@ -448,13 +577,48 @@ __device__ __forceinline__ void assemble_item(
         for (int m = 0; m < 9; m++) acc.h[a][m] = 0;
     }
     const int nq2 = nq * nq;
+    constexpr int stride = ENND == 8 ? kGeomStride8 : kGeomStride;
     if (pi.sing < 0) {
-        const double* g = geom + (size_t)e * nq2 * kGeomStride;
-        for (int q = 0; q < nq2; q++, g += kGeomStride) {
+        const double* g = geom + (size_t)e * nq2 * stride;
+        const int n0 = 7 + 4 * half;
+        for (int q = 0; q < nq2; q++, g += stride) {
             const double xq[3] = {__ldg(g), __ldg(g + 1), __ldg(g + 2)};
             const double nqv[3] = {__ldg(g + 3), __ldg(g + 4), __ldg(g + 5)};
-            const double N[4] = {__ldg(g + 7), __ldg(g + 8), __ldg(g + 9), __ldg(g + 10)};
+            const double N[4] = {__ldg(g + n0), __ldg(g + n0 + 1), __ldg(g + n0 + 2),
+                                 __ldg(g + n0 + 3)};
             gauss_point(acc, tc, ph, xc, xq, nqv, __ldg(g + 6), N);
+        }
+    } else if (ENND == 8) {
+        // 4-node sub-elements over parent nodes, each with the Duffy rule from its
+        // singular corner; a sub-element node's shape value goes to its parent node
+        // when that node belongs to this half (AssembleSubElement,
+        // TDElementStepLinearT.cpp:597-626).
+        int ids[2][4], cid[2];
+        const int nsub = q8_subelements(pi.sing, ids, cid);
+        for (int se = 0; se < nsub; se++) {
+            double cn[12];
+            int slot[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int id = ids[se][i];
+                slot[i] = id - 4 * half;  // in [0, 4) when parent node id is in this half
+                const int n = ien[e * 8 + id];
+#pragma unroll
+                for (int d = 0; d < 3; d++) cn[i * 3 + d] = coords[n * 3 + d];
+            }
+            for (int qq = 0; qq < 2 * nq2; qq++) {
+                const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+                double N4[4], xq[3], nqv[3], wJ;
+                duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N4, xq, nqv,
+                            wJ);
+                double N[4] = {0, 0, 0, 0};
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+                        if (slot[i] == a) N[a] = N4[i];
+                gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
+            }
         }
     } else {
         double cn[12];
@@ -508,20 +672,23 @@ __device__ __forceinline__ void assemble_item(
 
 
 
-template <int MODE>
+// One thread per item (4-node elements) or two adjacent threads per item (8-node
+// elements, one per half of the element's nodes).
+template <int MODE, int ENND>
 __global__ void __launch_bounds__(128) k_assemble_items(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
     const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
     int step_n, int part, const PairInfo* __restrict__ pairs,
     const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
+    constexpr int SH = ENND == 8 ? 1 : 0;
     unsigned p;
-    if (!item_pair(offsets, npairs, nitems, p)) return;
+    if (!item_pair<SH>(offsets, npairs, nitems, p)) return;
     const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
     const PairInfo pi = pairs[p];
-    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
-    assemble_item<MODE>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, level_last, step_n,
-                        part, pi, p, k, out);
+    const int k = pi.klo + (int)((gid >> SH) - __ldg(offsets + p));
+    assemble_item<MODE, ENND>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, level_last,
+                              step_n, part, pi, p, k, out, (int)(gid & SH));
 }
 
 // ---------------------------------------------------------------------------
@@ -733,7 +900,9 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
 // ElastoDynamicsT.cpp:261-280): C_c = -sum_e sum_q wJ DT_Kelvin(q)^T over the whole
 // surface, with the reference's regular / Duffy quadrature per element.  One
 // block per node, fixed-order tree reduction; the result goes to cbuf[c][9].
-// C term of node c, computed by the whole block (256 threads), into dst[9].
+// C term of node c, computed by the whole block (256 threads), into dst[9].  A
+// singular 8-node element contributes through its 4-node sub-elements.
+template <int ENND = 4>
 __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const int* __restrict__ ien, int nel, int c, int nq,
                                            const double* __restrict__ gx,
@@ -746,25 +915,38 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
     const double onem2nu = 1 - 2 * ph.nu;
     // Kelvin_Linear (GreenFunctionT.cpp:205-231): K = [..] / (-8 pi (1-nu) r^2) * 0.5 dt
     const double kscale = (0.5 * ph.dt) / (-(8 * M_PI) * (1 - ph.nu));
+    constexpr int stride = ENND == 8 ? kGeomStride8 : kGeomStride;
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-        double cn[12];
-        for (int a = 0; a < 4; a++) {
-            const int nid = ien[e * 4 + a];
-            for (int d = 0; d < 3; d++) cn[a * 3 + d] = coords[nid * 3 + d];
+        double en[3 * ENND];
+        for (int a = 0; a < ENND; a++) {
+            const int nid = ien[e * ENND + a];
+            for (int d = 0; d < 3; d++) en[a * 3 + d] = coords[nid * 3 + d];
         }
-        const int sing = singular_corner(cn, xc);
-        const int npts = sing < 0 ? nq2 : 2 * nq2;
+        const int sing = singular_corner<ENND>(en, xc);
+        // singular: sub-elements (one for a 4-node element: itself) x 2 triangles
+        int ids[2][4] = {{0, 1, 2, 3}, {0, 1, 2, 3}}, cid[2] = {sing, sing};
+        int nsub = 1;
+        if (ENND == 8 && sing >= 0) nsub = q8_subelements(sing, ids, cid);
+        const int npts = sing < 0 ? nq2 : nsub * 2 * nq2;
+        double cn[12];
+        int cur = -1;
         for (int qq = 0; qq < npts; qq++) {
             double xq[3], nv[3], wJ;
             if (sing < 0) {
-                const double* g = geom + ((size_t)e * nq2 + qq) * kGeomStride;
+                const double* g = geom + ((size_t)e * nq2 + qq) * stride;
                 xq[0] = g[0]; xq[1] = g[1]; xq[2] = g[2];
                 nv[0] = g[3]; nv[1] = g[4]; nv[2] = g[5];
                 wJ = g[6];
             } else {
-                const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+                const int se = qq / (2 * nq2), r = qq % (2 * nq2);
+                if (se != cur) {
+                    for (int i = 0; i < 4; i++)
+                        for (int d = 0; d < 3; d++) cn[i * 3 + d] = en[ids[se][i] * 3 + d];
+                    cur = se;
+                }
+                const int tri = r / nq2, q = r % nq2, q1 = q / nq, q2 = q % nq;
                 double N[4];
-                duffy_point(cn, sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
+                duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
             }
             const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
             const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
@@ -794,6 +976,7 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
     if (threadIdx.x < 9) dst[threadIdx.x] = red[threadIdx.x][0];
 }
 
+template <int ENND>
 __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords,
                                                const int* __restrict__ ien, int nel,
                                                int node_lo, int nq,
@@ -801,8 +984,8 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
                                                const double* __restrict__ gw,
                                                const double* __restrict__ geom, Phys ph,
                                                double* __restrict__ cbuf) {
-    cterm_node(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
-               cbuf + (size_t)blockIdx.x * 9);
+    cterm_node<ENND>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
+                     cbuf + (size_t)blockIdx.x * 9);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -896,63 +1079,89 @@ __global__ void __launch_bounds__(256) k_cterm_group(const GroupAsm* __restrict_
 
 }  // namespace
 
-cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
+cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int ennd, int nq,
                               const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s) {
     const long long n = (long long)nel * nq * nq;
     const int bs = 128;
-    k_gauss_geom<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom,
-                                                               geomf);
+    const unsigned grid = (unsigned)((n + bs - 1) / bs);
+    if (ennd == 8) k_gauss_geom8<<<grid, bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom);
+    else k_gauss_geom<<<grid, bs, 0, s>>>(coords, ien, nel, nq, gx, gw, geom, geomf);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
+cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
                                int mode, int level_last, int level_cap, int step_n, int select,
                                PairInfo* pairs, unsigned* counts, cudaStream_t s) {
     const long long n = (long long)nnodes * nelem_color;
     if (n == 0) return cudaSuccess;
     const int bs = 256;
-    k_pair_window<<<(unsigned)((n + bs - 1) / bs), bs, 0, s>>>(
-        coords, ien, elems, nelem_color, node_lo, nnodes, ph, mode, level_last, level_cap, step_n,
-        select, pairs, counts);
+    const unsigned grid = (unsigned)((n + bs - 1) / bs);
+    if (ennd == 8)
+        k_pair_window<8><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo, nnodes, ph,
+                                             mode, level_last, level_cap, step_n, select, pairs,
+                                             counts);
+    else
+        k_pair_window<4><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo, nnodes, ph,
+                                             mode, level_last, level_cap, step_n, select, pairs,
+                                             counts);
     return cudaGetLastError();
 }
 
-cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
-                                  int nelem_color, int node_lo, int nq, const double* gx,
-                                  const double* gw, const double* geom, const float* geomf,
-                                  const Phys& ph, int mode, int level_last, int step_n,
-                                  const PairInfo* pairs, const unsigned* offsets,
+template <int ENND>
+static void launch_items_fp64(const double* coords, const int* ien, const int* elems,
+                              int nelem_color, int node_lo, int nq, const double* gx,
+                              const double* gw, const double* geom, const Phys& ph, int mode,
+                              int level_last, int step_n, const PairInfo* pairs,
+                              const unsigned* offsets, unsigned npairs, unsigned nitems,
+                              const AsmOut& out, cudaStream_t s) {
+    const int bs = 128;
+    const unsigned long long threads = (unsigned long long)nitems << (ENND == 8 ? 1 : 0);
+    const unsigned grid = (unsigned)((threads + bs - 1) / bs);
+    if (mode == ASM_LEVELS) {
+        k_assemble_items<ASM_LEVELS, ENND><<<grid, bs, 0, s>>>(
+            coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last, step_n, 0,
+            pairs, offsets, npairs, nitems, out);
+    } else {
+        for (int part = 0; part < 2; part++)
+            k_assemble_items<ASM_STEP, ENND><<<grid, bs, 0, s>>>(
+                coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last,
+                step_n, part, pairs, offsets, npairs, nitems, out);
+    }
+}
+
+cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd,
+                                  const int* elems, int nelem_color, int node_lo, int nq,
+                                  const double* gx, const double* gw, const double* geom,
+                                  const float* geomf, const Phys& ph, int mode, int level_last,
+                                  int step_n, const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
                                   int fp32_far, cudaStream_t s) {
     if (nitems == 0) return cudaSuccess;
-    const int bs = 128;
-    const unsigned grid = (nitems + bs - 1) / bs;
-    if (fp32_far) {
+    if (ennd == 8) {
+        if (fp32_far) return cudaErrorInvalidValue;  // the FP32 far form is 4-node only
+        launch_items_fp64<8>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
+                             level_last, step_n, pairs, offsets, npairs, nitems, out, s);
+    } else if (fp32_far) {
         k_assemble_far_f32<<<(nitems + 255) / 256, 256, 0, s>>>(
             coords, ien, elems, nelem_color, node_lo, nq * nq, geomf, ph, level_last, pairs,
             offsets, npairs, nitems, out);
-    } else if (mode == ASM_LEVELS) {
-        k_assemble_items<ASM_LEVELS><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
-                                                         node_lo, nq, gx, gw, geom, ph,
-                                                         level_last, step_n, 0, pairs, offsets,
-                                                         npairs, nitems, out);
     } else {
-        for (int part = 0; part < 2; part++)
-            k_assemble_items<ASM_STEP><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color,
-                                                           node_lo, nq, gx, gw, geom, ph,
-                                                           level_last, step_n, part, pairs,
-                                                           offsets, npairs, nitems, out);
+        launch_items_fp64<4>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
+                             level_last, step_n, pairs, offsets, npairs, nitems, out, s);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
+cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s) {
     if (nnodes == 0) return cudaSuccess;
-    k_cterm<<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
+    if (ennd == 8)
+        k_cterm<8><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
+    else
+        k_cterm<4><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
     return cudaGetLastError();
 }
 

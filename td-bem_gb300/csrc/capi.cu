@@ -131,18 +131,18 @@ int compute_max_step(const std::vector<double>& x, int nnd, double E, double nu,
 }
 
 // Greedy colouring: no two elements of one colour share a node.
-void color_elements(const std::vector<int>& ien, int nel, int nnd, std::vector<int>& order,
-                    std::vector<int>& start) {
+void color_elements(const std::vector<int>& ien, int nel, int ennd, int nnd,
+                    std::vector<int>& order, std::vector<int>& start) {
     std::vector<std::vector<int>> node_elems(nnd);
     for (int e = 0; e < nel; e++)
-        for (int a = 0; a < 4; a++) node_elems[ien[e * 4 + a]].push_back(e);
+        for (int a = 0; a < ennd; a++) node_elems[ien[e * ennd + a]].push_back(e);
     std::vector<int> color(nel, -1);
     int ncolor = 0;
     std::vector<int> used;
     for (int e = 0; e < nel; e++) {
         used.assign(ncolor + 1, 0);
-        for (int a = 0; a < 4; a++)
-            for (int o : node_elems[ien[e * 4 + a]])
+        for (int a = 0; a < ennd; a++)
+            for (int o : node_elems[ien[e * ennd + a]])
                 if (color[o] >= 0) used[color[o]] = 1;
         int c = 0;
         while (c < ncolor && used[c]) c++;
@@ -270,14 +270,16 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
     if (ne == 0 || nnodes == 0) return TDBEM_OK;
     const int* elems = c->d_color_elems + e0;
     const long long per_node_items = (long long)ne * (mode == ASM_LEVELS ? level_last + 1 : 1);
-    const long long max_nodes_items = (1LL << 31) / std::max(1LL, per_node_items);
+    // item threads (one per item, two for an 8-node element) stay below 2^31
+    const long long max_nodes_items =
+        (1LL << (c->ennd == 8 ? 30 : 31)) / std::max(1LL, per_node_items);
     const long long max_nodes_pairs = (long long)c->pair_cap / ne;
     const int chunk = (int)std::max(1LL, std::min(max_nodes_items, max_nodes_pairs));
     for (int n0 = node_lo; n0 < node_lo + nnodes; n0 += chunk) {
         const int nn = std::min(chunk, node_lo + nnodes - n0);
         const unsigned npairs = (unsigned)((long long)nn * ne);
         const int pw = prof_begin(c, TDBEM_K_AUX);
-        CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, elems, ne, n0, nn, c->ph, mode,
+        CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, nn, c->ph, mode,
                                     level_last, level_cap, step_n, select, c->d_pairs,
                                     c->d_counts, c->stream));
         CUDA_TRY(exclusive_scan(c->d_counts, c->d_offsets, npairs, c->d_scan_tmp,
@@ -292,7 +294,7 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         const unsigned nitems = last[0] + last[1];
         const int pe = prof_begin(c, fp32_far ? TDBEM_K_ASSEMBLE_F32 : TDBEM_K_ASSEMBLE);
-        CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, elems, ne, n0, c->nq, c->d_gx,
+        CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq, c->d_gx,
                                        c->d_gw, c->d_geom, c->d_geomf, c->ph, mode, level_last,
                                        step_n,
                                        c->d_pairs, c->d_offsets, npairs, nitems, out, fp32_far,
@@ -680,16 +682,18 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     *out = nullptr;
     if (!mesh || !mat || !mesh->coords || !mesh->ien)
         return fail(TDBEM_ERR_ARG, "mesh/material pointers are null");
-    if (mesh->etype != 1)
-        return fail(TDBEM_ERR_UNSUPPORTED, "element type %d: only 4-node quads (EType=1)",
+    if (mesh->etype != 1 && mesh->etype != 2)
+        return fail(TDBEM_ERR_UNSUPPORTED,
+                    "element type %d: 4-node (EType=1) or 8-node (EType=2) quads only",
                     mesh->etype);
+    const int ennd = mesh->etype == 2 ? 8 : 4;
     if (mesh->nnd < 2 || mesh->nel < 1) return fail(TDBEM_ERR_ARG, "empty mesh");
     if (!(dt > 0) || !(mat->rho > 0) || !(mat->E > 0) || !(mat->nu > -1 && mat->nu < 0.5))
         return fail(TDBEM_ERR_ARG, "invalid dt or material");
     std::vector<double> gx, gw;
     if (!gauss_table(nq, gx, gw))
         return fail(TDBEM_ERR_ARG, "unsupported number of Gauss points %d", nq);
-    for (long long i = 0; i < 4LL * mesh->nel; i++)
+    for (long long i = 0; i < (long long)ennd * mesh->nel; i++)
         if (mesh->ien[i] < 0 || mesh->ien[i] >= mesh->nnd)
             return fail(TDBEM_ERR_ARG, "IEN entry %lld = %d out of range", i, mesh->ien[i]);
     int ndev = 0;
@@ -702,6 +706,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     cudaGetDevice(&c->device);
     c->nnd = mesh->nnd;
     c->nel = mesh->nel;
+    c->ennd = ennd;
     c->D = 3 * mesh->nnd;
     c->nq = nq;
     c->if_ext = if_ext ? 1 : 0;
@@ -710,7 +715,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     c->rho = mat->rho;
     c->dt = dt;
     c->h_coords.assign(mesh->coords, mesh->coords + 3 * (size_t)mesh->nnd);
-    c->h_ien.assign(mesh->ien, mesh->ien + 4 * (size_t)mesh->nel);
+    c->h_ien.assign(mesh->ien, mesh->ien + ennd * (size_t)mesh->nel);
     c->M = compute_max_step(c->h_coords, c->nnd, c->E, c->nu, c->rho, dt);
     // GreenFunctionT::WaveSpeed (GreenFunctionT.cpp:76-84)
     const double mu = c->E / (2 * (1 + c->nu));
@@ -731,7 +736,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     ph.inv_4pi = 1.0 / (4 * M_PI);
     ph.nu = c->nu;
     std::vector<int> order;
-    color_elements(c->h_ien, c->nel, c->nnd, order, c->color_start);
+    color_elements(c->h_ien, c->nel, c->ennd, c->nnd, order, c->color_start);
     int max_color = 0;
     for (size_t k = 0; k + 1 < c->color_start.size(); k++)
         max_color = std::max(max_color, c->color_start[k + 1] - c->color_start[k]);
@@ -754,9 +759,9 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_ien, c->h_ien.size()));
     CTX_TRY(dalloc(&c->d_gx, nq));
     CTX_TRY(dalloc(&c->d_gw, nq));
-    CTX_TRY(dalloc(&c->d_geom, (size_t)c->nel * nq * nq * 12));
+    CTX_TRY(dalloc(&c->d_geom, (size_t)c->nel * nq * nq * (ennd == 8 ? 16 : 12)));
     CTX_TRY(dalloc(&c->d_cterm, (size_t)c->nnd * 9));
-    CTX_TRY(dalloc(&c->d_geomf, (size_t)c->nel * nq * nq * 12));
+    if (ennd == 4) CTX_TRY(dalloc(&c->d_geomf, (size_t)c->nel * nq * nq * 12));
     CTX_TRY(dalloc(&c->d_color_elems, order.size()));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
@@ -768,8 +773,8 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
                             c->stream));
     CTX_TRY(cudaMemcpyAsync(c->d_color_elems, order.data(), sizeof(int) * order.size(),
                             cudaMemcpyHostToDevice, c->stream));
-    CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, nq, c->d_gx, c->d_gw, c->d_geom,
-                              c->d_geomf, c->stream));
+    CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, ennd, nq, c->d_gx, c->d_gw,
+                              c->d_geom, c->d_geomf, c->stream));
     c->pair_cap = std::min<size_t>((size_t)c->nnd * max_color, (size_t)1 << 26);
     c->pair_cap = std::max<size_t>(c->pair_cap, (size_t)max_color);
     CTX_TRY(dalloc(&c->d_pairs, c->pair_cap));
@@ -875,7 +880,7 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
         rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, 1 << 30, step, SEL_ALL, 0,
                             out);
     if (rc == TDBEM_OK && step == 1) {
-        e = launch_cterm(c->d_coords, c->d_ien, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
+        e = launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
                          c->d_geom, c->ph, c->d_cterm, c->stream);
         if (e == cudaSuccess)
             e = launch_cterm_apply(c->d_cterm, node_lo, nn, c->dt, c->if_ext, ASM_STEP, out,
@@ -936,7 +941,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             if (rc != TDBEM_OK) return rc;
         }
         const int pc = prof_begin(c, TDBEM_K_AUX);
-        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
                               c->d_geom, c->ph, c->d_cterm, c->stream));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, out,
                                     c->stream));
@@ -962,16 +967,20 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         o64.level_stride = D * D;
         o64.D = c->D;
         o64.ld = c->D;
+        // 8-node elements: every pair through the FP64 quadrature (the FP32 far form
+        // is written for 4-node elements)
+        const bool split = c->ennd == 4;
         for (int col = 0; col < ncol; col++) {
-            int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_NEAR, 0, o32);
-            if (rc == TDBEM_OK)
+            int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0,
+                                    split ? SEL_NEAR : SEL_ALL, 0, o32);
+            if (rc == TDBEM_OK && split)
                 rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_FAR, 1, o32);
             if (rc == TDBEM_OK)
                 rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, 0, o64);
             if (rc != TDBEM_OK) return rc;
         }
         const int pc = prof_begin(c, TDBEM_K_AUX);
-        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
                               c->d_geom, c->ph, c->d_cterm, c->stream));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o32,
                                     c->stream));
@@ -1528,9 +1537,13 @@ int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int p
         for (int j = 0; j < i; j++)
             if (ctxs[j] == ctxs[i]) return fail(TDBEM_ERR_ARG, "context %d appears twice", i);
     }
-    if (precision == TDBEM_MIXED)  // near/far split per mesh; the meshes' streams overlap
+    bool any_q8 = false;
+    for (int i = 0; i < n; i++) any_q8 = any_q8 || ctxs[i]->ennd == 8;
+    // mixed: near/far split per mesh; 8-node meshes: the single-mesh launches (the
+    // grouped kernels are written for 4-node elements).  The meshes' streams overlap.
+    if (precision == TDBEM_MIXED || any_q8)
         return parallel_contexts(ctxs, n, [&](int i) {
-            return tdbem_assemble_levels(ctxs[i], nsteps[i], TDBEM_MIXED);
+            return tdbem_assemble_levels(ctxs[i], nsteps[i], precision);
         });
     tdbem_ctx* c0 = ctxs[0];
     cudaStream_t s = c0->stream;
@@ -1999,17 +2012,19 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
     if (!mesh || !mat || !bytes || !mesh->coords || !mesh->ien)
         return fail(TDBEM_ERR_ARG, "null argument");
     if (mesh->nnd < 2 || mesh->nel < 1 || !(dt > 0) || numstep < 1 || !(mat->rho > 0) ||
-        !(mat->E > 0) || !(mat->nu > -1 && mat->nu < 0.5) || mesh->etype != 1)
+        !(mat->E > 0) || !(mat->nu > -1 && mat->nu < 0.5) ||
+        (mesh->etype != 1 && mesh->etype != 2))
         return fail(TDBEM_ERR_ARG, "invalid mesh, material, time step or step count");
+    const int ennd = mesh->etype == 2 ? 8 : 4;
     if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
         return fail(TDBEM_ERR_ARG, "precision must be TDBEM_FP64 or TDBEM_MIXED");
     std::vector<double> x(mesh->coords, mesh->coords + 3 * (size_t)mesh->nnd);
-    std::vector<int> ien(mesh->ien, mesh->ien + 4 * (size_t)mesh->nel);
+    std::vector<int> ien(mesh->ien, mesh->ien + ennd * (size_t)mesh->nel);
     for (int v : ien)
         if (v < 0 || v >= mesh->nnd) return fail(TDBEM_ERR_ARG, "element node out of range");
     const int M = compute_max_step(x, mesh->nnd, mat->E, mat->nu, mat->rho, dt);
     std::vector<int> order, start;
-    color_elements(ien, mesh->nel, mesh->nnd, order, start);
+    color_elements(ien, mesh->nel, ennd, mesh->nnd, order, start);
     size_t max_color = 0;
     for (size_t k = 0; k + 1 < start.size(); k++)
         max_color = std::max<size_t>(max_color, (size_t)(start[k + 1] - start[k]));
@@ -2017,8 +2032,10 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
     const size_t nel = mesh->nel, q2 = (size_t)nq * nq;
     size_t pair_cap = std::min<size_t>((size_t)mesh->nnd * max_color, (size_t)1 << 26);
     pair_cap = std::max(pair_cap, max_color);
-    // tdbem_ctx_create: mesh, Gauss geometry (FP64 + FP32), C term, colours, pair scratch
-    size_t b = 24 * (size_t)mesh->nnd + 20 * nel + q2 * nel * 12 * 12 + 72 * (size_t)mesh->nnd +
+    // tdbem_ctx_create: mesh, Gauss geometry (FP64 + FP32 for 4-node elements, FP64
+    // only, 16 per point, for 8-node ones), C term, colours, pair scratch
+    size_t b = 24 * (size_t)mesh->nnd + 4 * (ennd + 1) * nel + q2 * nel * 16 * 8 +
+               72 * (size_t)mesh->nnd +
                pair_cap * (sizeof(PairInfo) + 8) + pair_cap / 8 + ((size_t)1 << 16);  // + scan
     // marching state common to both forms: maps, W vectors, partials, histories
     b += 8 * D * 8 + 3 * L * D * 8 + 2 * ((size_t)numstep + 1) * D * 8 + 4 * (D + 64);

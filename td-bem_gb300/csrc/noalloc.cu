@@ -150,7 +150,7 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
         for (int n0 = node_lo; n0 <= node_hi; n0 += chunk) {
             const int cn = std::min(chunk, node_hi - n0 + 1);
             const unsigned npairs = (unsigned)((size_t)cn * ne);
-            NA_TRY(launch_pair_window(c->d_coords, c->d_ien, elems, ne, n0, cn, c->ph, ASM_STEP,
+            NA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, cn, c->ph, ASM_STEP,
                                       step, 1 << 30, step, SEL_ALL, pairs, counts, s));
             NA_TRY(exclusive_scan(counts, offsets, npairs, scan_tmp, kScanBytes, s));
             unsigned last[2];
@@ -159,7 +159,7 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
             NA_TRY(cudaMemcpyAsync(&last[1], counts + npairs - 1, sizeof(unsigned),
                                    cudaMemcpyDeviceToHost, s));
             NA_TRY(cudaStreamSynchronize(s));
-            NA_TRY(launch_assemble_items(c->d_coords, c->d_ien, elems, ne, n0, c->nq, c->d_gx,
+            NA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq, c->d_gx,
                                          c->d_gw, c->d_geom, c->d_geomf, c->ph, ASM_STEP, step,
                                          step, pairs, offsets, npairs, last[0] + last[1], out, 0,
                                          s));
@@ -168,7 +168,7 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
     if (step == 1) {
         for (int n0 = node_lo; n0 <= node_hi; n0 += (int)kMaxNodes) {
             const int cn = std::min((int)kMaxNodes, node_hi - n0 + 1);
-            NA_TRY(launch_cterm(c->d_coords, c->d_ien, c->nel, n0, cn, c->nq, c->d_gx, c->d_gw,
+            NA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, n0, cn, c->nq, c->d_gx, c->d_gw,
                                 c->d_geom, c->ph, cbuf, s));
             AsmOut o2 = out;
             // rows of this chunk inside the caller's row block

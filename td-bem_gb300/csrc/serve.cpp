@@ -189,7 +189,7 @@ int tdbem_server_submit(tdbem_server* s, const tdbem_request* q, long long* id) 
         return sfail(TDBEM_ERR_NOMEM, "request needs %zu bytes, the budget is %zu", fp, s->budget);
     auto r = std::make_unique<Request>();
     r->coords.assign(m.coords, m.coords + 3 * (size_t)m.nnd);
-    r->ien.assign(m.ien, m.ien + 4 * (size_t)m.nel);
+    r->ien.assign(m.ien, m.ien + (m.etype == 2 ? 8 : 4) * (size_t)m.nel);
     r->nnd = m.nnd;
     r->nel = m.nel;
     r->etype = m.etype;

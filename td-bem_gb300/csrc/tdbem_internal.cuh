@@ -61,21 +61,24 @@ struct AsmOut {
 };
 
 // Launch helpers (assemble.cu).
-cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int nq,
+// ennd: nodes per element (4 or 8).  8-node elements keep a wider geometry
+// table (kGeomStride8 doubles per Gauss point, no FP32 copy) and take the FP64
+// quadrature only (fp32_far must be 0).
+cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int ennd, int nq,
                               const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s);
-cudaError_t launch_pair_window(const double* coords, const int* ien, const int* elems,
+cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
                                int mode, int level_last, int level_cap, int step_n, int select,
                                PairInfo* pairs, unsigned* counts, cudaStream_t s);
-cudaError_t launch_assemble_items(const double* coords, const int* ien, const int* elems,
-                                  int nelem_color, int node_lo, int nq, const double* gx,
-                                  const double* gw, const double* geom, const float* geomf,
-                                  const Phys& ph, int mode, int level_last, int step_n,
-                                  const PairInfo* pairs, const unsigned* offsets,
+cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd,
+                                  const int* elems, int nelem_color, int node_lo, int nq,
+                                  const double* gx, const double* gw, const double* geom,
+                                  const float* geomf, const Phys& ph, int mode, int level_last,
+                                  int step_n, const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
                                   int fp32_far, cudaStream_t s);
-cudaError_t launch_cterm(const double* coords, const int* ien, int nel, int node_lo,
+cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
@@ -283,6 +286,7 @@ struct tdbem_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int nnd = 0, nel = 0, D = 0, M = 0, nq = 6, if_ext = 0;
+    int ennd = 4;                    // nodes per element: 4 (EType 1) or 8 (EType 2)
     double E = 0, nu = 0, rho = 0, dt = 0;
     tdbem::Phys ph{};
     std::vector<double> h_coords;

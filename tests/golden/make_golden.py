@@ -65,8 +65,17 @@ def run_case(driver, name, text, a1=0.0, a2=0.0, full_levels=False, dof_stride=1
 
 
 def main():
+    """All cases, or only those named on the command line."""
+    only = set(sys.argv[1:])
     driver = build_reference()
     geo = os.path.join(REF_ROOT, "geometry")
+    if only:
+        global run_case
+        full = run_case
+
+        def run_case(drv, name, *a, **k):  # noqa: F811
+            if name in only:
+                full(drv, name, *a, **k)
     bar1 = open(os.path.join(geo, "Bar_1.txt")).read()
     run_case(driver, "ref_bar1", bar1, full_levels=True)
     run_case(driver, "ref_bar1_alpha", bar1, a1=0.25, a2=0.25)
@@ -84,6 +93,10 @@ def main():
     cav = open(os.path.join(geo, "SphericalCavity_1.txt")).read().replace(
         "numstep=200;", "numstep=40;")
     run_case(driver, "ref_spherical_cavity_1_40", cav, dof_stride=4)
+    # The reference's 8-node (Q8) bar: serendipity shapes, singular sub-elements.
+    bar2 = open(os.path.join(geo, "Bar_2.txt")).read()
+    run_case(driver, "ref_bar2", bar2)
+    run_case(driver, "ref_bar2_alpha", bar2, a1=0.25, a2=0.1)
 
 
 if __name__ == "__main__":

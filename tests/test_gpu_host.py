@@ -19,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
 RUN = os.path.join(ROOT, "td-bem_gb300", "_build", "tdbem_run")
-CASES = ["ref_bar1_alpha", "bar_1x1x4_q2_alpha", "ref_halfspace_plane_1e"]
+CASES = ["ref_bar1_alpha", "bar_1x1x4_q2_alpha", "ref_halfspace_plane_1e", "ref_bar2_alpha"]
 
 
 @pytest.fixture(scope="module")

@@ -66,6 +66,17 @@ def test_mixed_bar_with_prescribed_displacements(tdlib):
     assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
 
 
+def test_mixed_q8_bar(tdlib):
+    """8-node elements in mixed precision: every pair through the FP64 quadrature
+    into the FP32 store, FP32 convolution and FP32 inverse with refinement."""
+    z, m = load_golden("ref_bar2_alpha")
+    a = (float(z["a1"]), float(z["a2"]))
+    u, t, _ = run(tdlib, m, tdlib.FP64, alpha=a)
+    u32, t32, _ = run(tdlib, m, tdlib.MIXED, alpha=a)
+    assert rel_l2(u32, u) <= TOL_L2
+    assert rel_l2(t32, t) <= TOL_L2
+
+
 def test_refinement_recovers_fp64_solve(tdlib, sphere8):
     m, (u, t, _) = sphere8
     e0 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=0)[0], u)

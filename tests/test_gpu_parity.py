@@ -103,6 +103,21 @@ def test_gh_driver_matches_oracle(step, tdlib, oracle_mod):
         assert rel_max(a, b) <= TOL, f"{nm}: {rel_max(a, b):.3e}"
 
 
+@pytest.mark.parametrize("step", [1, 3])
+def test_gh_driver_q8_matches_oracle(step, tdlib, oracle_mod):
+    """8-node elements: serendipity shapes, corner and midside singular nodes
+    (sub-element Duffy rules), the C term, on a row block of the reference's bar."""
+    z, m = load_golden("ref_bar2")
+    assert m.etype == 2
+    o = oracle_mod.Oracle(m, clean=True)
+    lo, hi = 5, 40
+    ref = o.gh_driver(step * m.dt, m.dt, lo, hi)
+    with tdlib.Context(m) as ctx:
+        got = ctx.gh_driver(step, lo, hi)
+    for a, b, nm in zip(got, ref, ["G_I", "G_J", "H_I", "H_J"]):
+        assert rel_max(a, b) <= TOL, f"{nm}: {rel_max(a, b):.3e}"
+
+
 def test_reruns_are_bitwise_identical(tdlib):
     z, m = load_golden("sphere_6x4x4")
     with tdlib.Context(m) as ctx:
