@@ -68,6 +68,14 @@ class ModelManagerT {
                 const int* FBC_DOFs, const double* FBC_values);
     int GetNumInterface() { return (int)interface_.size(); }
     const int* GetInterface() { return interface_.data(); }
+    // Auxiliary mesh of a multi-region input (ModelManagerT.cpp:236-304); read, not
+    // used by the assembly or the marching.
+    int GetNND_Aux() { return nnd_aux_; }
+    int GetElementType_Aux() { return etype_aux_; }
+    int GetENND_Aux() { return ennd_aux_; }
+    int GetNEL_Aux() { return nel_aux_; }
+    const int* GetIEN_Aux() { return ien_aux_.data(); }
+    const double* GetCoords_Aux() { return coords_aux_.data(); }
     // Single process: every dof is local (ModelManagerT::Distributed_BC keeps all).
     void Distributed_BC(int, int) {}
 
@@ -78,9 +86,10 @@ class ModelManagerT {
    private:
     int formulation_ = 1, numstep_ = 1, interpolation_ = 1, nq_ = 6, sd_ = 3, if_ext_ = 0;
     int nnd_ = 0, nel_ = 0, etype_ = 1, ennd_ = 4;
+    int nnd_aux_ = 0, nel_aux_ = 0, etype_aux_ = 1, ennd_aux_ = 4;
     double dt_ = 0, E_ = 1, nu_ = 0, rho_ = 1;
-    std::vector<double> coords_;
-    std::vector<int> ien_;
+    std::vector<double> coords_, coords_aux_;
+    std::vector<int> ien_, ien_aux_;
     std::vector<int> ubc_dof_, fbc_dof_, interface_;
     std::vector<double> ubc_val_, fbc_val_;
 };

@@ -54,6 +54,10 @@ def lib():
         L.orc_march_range.argtypes = march_args + [ctypes.c_int, ctypes.c_int, _dp, _dp,
                                                    ctypes.c_int]
         L.orc_lu_factor.argtypes = [ctypes.c_int, _dp, ctypes.c_int]
+        L.orc_mrt_amplitude.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.orc_mrt_amplitude.restype = ctypes.c_double
+        L.orc_mrt_march.argtypes = [ctypes.c_int] * 3 + [_dp, _dp, _dp, ctypes.c_int, _dp,
+                                                         ctypes.c_int]
         L.orc_green_step_linear.argtypes = [ctypes.c_double] * 3 + [_dp, _dp, ctypes.c_double,
                                                                     ctypes.c_double] + [_dp] * 5
         L.orc_element_gh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -152,6 +156,146 @@ class Oracle:
         if rc:
             raise RuntimeError(f"orc_march failed ({rc})")
         return u, t
+
+
+class MultiRegion:
+    """Two-region solver, restated from SolverMRT (SolverMRT.cpp).
+
+    Region r's model m_r lists its interface nodes (m_r.interface, 0-based); the
+    interface of region 2 is matched to region 1's node by node (coordinates
+    within 1e-10, the first match, SolverMRT.cpp:458-494).  The unknowns of the
+    combined system are, in this order (LocalIndexing / InterfaceIndexing,
+    SolverMRT.cpp:158-566):
+      the interior displacements of region 1, of region 2 (interior nodes in
+      ascending order), the interface displacements and the interface tractions
+      of region 1 (interface-list order);
+    its rows are region 1's collocation dofs, then region 2's; the known vector
+    holds the interior tractions of both regions.  Region 2 sees the interface
+    traction with the opposite sign.  Levels k = 0..max_step are the regions'
+    levels (I(k) + J(k+1), level max_step = I(max_step)) placed by
+    Assemble_GH_R1/R2 (SolverMRT.cpp:663-847, UpdateGHLinear 850-949), for the
+    steps the marching loop reaches (n <= min(max_step, numstep)); marching
+    is Solve_Direct (1028-1097) with SetLoad's load (867-966): the FBC values at
+    interior dofs times p0 t exp(-2000 t), or times amp[n] when a load history is
+    given.  Displacements of region r at step n (ExtractField, 1261-1309) are
+    the combined unknowns mapped back to its dofs."""
+
+    def __init__(self, m1, m2, max_step: int = 10, clean: bool = False, nthreads: int = 0):
+        self.r = (Oracle(m1, nthreads, clean), Oracle(m2, nthreads, clean))
+        self.L = int(max_step)
+        self.nthreads = self.r[0].nthreads
+        self._index(m1, m2)
+
+    def _index(self, m1, m2):
+        if1 = np.asarray(m1.interface, np.int64)
+        if2 = np.asarray(m2.interface, np.int64)
+        if len(if1) != len(if2):
+            raise ValueError("the regions list different numbers of interface nodes")
+        nz = len(if1)
+
+        def dofs(nodes):
+            return (3 * np.asarray(nodes, np.int64)[:, None] + np.arange(3)).reshape(-1)
+
+        def interior(m, iface):
+            lab = np.zeros(m.nnd, bool)
+            lab[iface] = True
+            return np.nonzero(~lab)[0]
+
+        self.int1, self.int2 = dofs(interior(m1, if1)), dofs(interior(m2, if2))
+        self.ifc1, self.ifc2 = dofs(if1), dofs(if2)
+        x1, x2 = m1.coords, m2.coords
+        match = np.empty(nz, np.int64)
+        for ni in range(nz):
+            p = x2[if2[ni]]
+            found = -1
+            for nj in range(nz):
+                q = x1[if1[nj]]
+                r = np.sqrt((q[0] - p[0]) * (q[0] - p[0]) + (q[1] - p[1]) * (q[1] - p[1]) +
+                            (q[2] - p[2]) * (q[2] - p[2]))
+                if r < 1e-10:
+                    found = nj
+                    break
+            if found < 0:
+                raise ValueError(f"interface node {ni} of region 2 has no match in region 1")
+            match[ni] = found
+        self.match = match
+        self.d2to1 = dofs(match)
+        self.D1, self.D2 = 3 * m1.nnd, 3 * m2.nnd
+        self.NI1, self.NI2, self.NZ = len(self.int1), len(self.int2), 3 * nz
+        self.N = self.D1 + self.D2
+        self.NG = self.NI1 + self.NI2
+        base_z = self.NI1 + self.NI2
+        base_t = base_z + self.NZ
+        # region-local dof -> combined column of its displacement; of its traction
+        # (interface dofs only; -1 elsewhere) and that traction's sign
+        self.ucol = (np.empty(self.D1, np.int64), np.empty(self.D2, np.int64))
+        self.tcol = (np.full(self.D1, -1, np.int64), np.full(self.D2, -1, np.int64))
+        self.tsign = (1.0, -1.0)
+        self.ucol[0][self.int1] = np.arange(self.NI1)
+        self.ucol[0][self.ifc1] = base_z + np.arange(self.NZ)
+        self.tcol[0][self.ifc1] = base_t + np.arange(self.NZ)
+        self.ucol[1][self.int2] = self.NI1 + np.arange(self.NI2)
+        self.ucol[1][self.ifc2] = base_z + self.d2to1
+        self.tcol[1][self.ifc2] = base_t + self.d2to1
+        self.gcol = (np.arange(self.NI1), self.NI1 + np.arange(self.NI2))
+
+    def region_levels(self, numstep=None):
+        """Each region's levels 0..max_step: G_H_Driver runs for the steps
+        1..min(max_step, numstep) of the marching loop, so level k holds
+        I(k) + J(k+1) up to that step and zeros beyond."""
+        numstep = self.r[0].m.numstep if numstep is None else numstep
+        return [o.assemble_levels(M=self.L, nsteps=min(self.L, numstep)) for o in self.r]
+
+    def combine(self, G1, H1, G2, H2):
+        """Assemble_GH_R1 / Assemble_GH_R2 for every level: (L+1) x N x NG and
+        (L+1) x N x N."""
+        L1 = G1.shape[0]
+        GG = np.zeros((L1, self.N, self.NG))
+        HH = np.zeros((L1, self.N, self.N))
+        rows = (slice(0, self.D1), slice(self.D1, self.N))
+        ints = (self.int1, self.int2)
+        ifcs = (self.ifc1, self.ifc2)
+        base_z = self.NI1 + self.NI2
+        zc = (base_z + np.arange(self.NZ), base_z + self.d2to1)
+        for r, (G, H) in enumerate(((G1, H1), (G2, H2))):
+            rw = rows[r]
+            GG[:, rw, self.gcol[r]] = G[:, :, ints[r]]
+            HH[:, rw, self.ucol[r][ints[r]]] = H[:, :, ints[r]]
+            HH[:, rw, zc[r]] = H[:, :, ifcs[r]]
+            # region 1 moves -G_z to the left, region 2 +G_z (its traction is -t_z)
+            HH[:, rw, self.NZ + zc[r]] = -self.tsign[r] * G[:, :, ifcs[r]]
+        return GG, HH
+
+    def assemble_levels(self, numstep=None):
+        (G1, H1), (G2, H2) = self.region_levels(numstep)
+        return self.combine(G1, H1, G2, H2)
+
+    def loads(self, numstep, amp=None):
+        """fLoad of every step (row n, row 0 zero): interior FBC values x amplitude."""
+        dt = self.r[0].m.dt
+        out = np.zeros((numstep + 1, self.NG))
+        for n in range(1, numstep + 1):
+            a = lib().orc_mrt_amplitude(n, dt) if amp is None else (
+                float(amp[n]) if n < len(amp) else 0.0)
+            for r, o in enumerate(self.r):
+                loc = np.zeros(3 * o.m.nnd)
+                for d, v in zip(o.m.fbc_dofs, o.m.fbc_vals):
+                    loc[d] = v * a
+                out[n, self.gcol[r]] = loc[(self.int1, self.int2)[r]]
+        return out
+
+    def march(self, GG, HH, numstep=None, amp=None):
+        """Combined unknowns x^n (n = 0..numstep) and the region displacements."""
+        numstep = self.r[0].m.numstep if numstep is None else numstep
+        load = np.ascontiguousarray(self.loads(numstep, amp))
+        X = np.zeros((numstep + 1, self.N))
+        L = GG.shape[0] - 1
+        rc = lib().orc_mrt_march(self.N, self.NG, L, _d(np.ascontiguousarray(GG)),
+                                 _d(np.ascontiguousarray(HH)), _d(load), numstep, _d(X),
+                                 self.nthreads)
+        if rc:
+            raise RuntimeError(f"orc_mrt_march failed ({rc})")
+        return X, X[:, self.ucol[0]], X[:, self.ucol[1]]
 
 
 def lu_factor(A, nthreads=0):

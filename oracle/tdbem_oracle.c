@@ -911,3 +911,68 @@ int orc_march(int D, int M, const double* G_levels, const double* H_levels, int 
                            fbc_dofs, fbc_vals, amp, a1, a2, 1, numstep, u_hist, t_hist,
                            nthreads);
 }
+
+/* ------------------------------------------------------------------ */
+/* Two-region solver (SolverMRT.cpp)                                    */
+/* ------------------------------------------------------------------ */
+double orc_mrt_amplitude(int n, double dt) {
+    const double p0 = 5.46366e9; /* SolverMRT.cpp:884-887 */
+    const double t = n * dt;
+    return p0 * t * exp(-2000 * t);
+}
+
+/* y = y + A x for an m x n row-major A (the stand-in's MatMultAdd). */
+static void rect_mult_add(const double* A, int m, int n, const double* x, double sign,
+                          double* y, int nthreads) {
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+    for (int i = 0; i < m; i++) {
+        const double* row = &A[(size_t)i * n];
+        double s = 0.0;
+        for (int j = 0; j < n; j++) s += (sign * row[j]) * x[j];
+        y[i] = y[i] + s;
+    }
+}
+
+int orc_mrt_march(int N, int NG, int L, const double* GG, const double* HH,
+                  const double* load, int numstep, double* X, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    lu_cache c = {0, NULL, NULL, NULL};
+    double* rhs = malloc(sizeof(double) * N);
+    double* zero = calloc((size_t)NG, sizeof(double));
+    if (!rhs || !zero) {
+        free(rhs);
+        free(zero);
+        return -4;
+    }
+    memset(X, 0, sizeof(double) * (size_t)(numstep + 1) * N);
+    int rc = 0;
+    const size_t gs = (size_t)N * NG, hs = (size_t)N * N;
+    for (int n = 1; n <= numstep && !rc; n++) {
+        /* MatMult(G_Compute = G^0, fLoad, fRHS) */
+        for (int i = 0; i < N; i++) rhs[i] = 0.0;
+        {
+            const double* ld = load + (size_t)n * NG;
+            for (int i = 0; i < N; i++) {
+                const double* row = &GG[(size_t)i * NG];
+                double s = 0.0;
+                for (int j = 0; j < NG; j++) s += row[j] * ld[j];
+                rhs[i] = s;
+            }
+        }
+        const int fmax = n < L ? n : L;
+        for (int f = 1; f <= fmax; f++) {
+            const double* tg = (n - f) == 0 ? zero : load + (size_t)(n - f) * NG;
+            rect_mult_add(GG + (size_t)f * gs, N, NG, tg, 1.0, rhs, nthreads);
+            /* H_temp = -H^f (MatAXPY into zeros, MatScale(-1)) */
+            rect_mult_add(HH + (size_t)f * hs, N, N, X + (size_t)(n - f) * N, -1.0, rhs,
+                          nthreads);
+        }
+        rc = lu_solve(&c, HH, N, rhs, X + (size_t)n * N, nthreads);
+    }
+    free(rhs);
+    free(zero);
+    free(c.lu);
+    free(c.piv);
+    free(c.cached);
+    return rc;
+}

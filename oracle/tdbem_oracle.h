@@ -95,6 +95,23 @@ int orc_element_gh(int etype, int nq, double E, double nu, double rho, const dou
                    const double* collocation, double t, double t_1, int singular, double* GE_1,
                    double* GE_2, double* HE_1, double* HE_2, double* C_1, double* C_2);
 
+/* Two-region solver, SolverMRT (SolverMRT.cpp).  The index maps and the combined
+ * level placement (Assemble_GH_R1/R2, 663-847) are exact copies done by the
+ * caller; this is the arithmetic.
+ *
+ * orc_mrt_amplitude: SetLoad's amplitude p0 t exp(-2000 t) at t = n dt
+ * (SolverMRT.cpp:881-887).
+ *
+ * orc_mrt_march: Solve_Direct (SolverMRT.cpp:1028-1097) on the combined system:
+ * per step n, rhs = G^0 load^n + sum_{f=1}^{min(n,L)} (G^f tg^{n-f} - H^f x^{n-f}),
+ * x^n = H^0 \ rhs (the KSPSolve stand-in), tg^n = load^n.  GG: (L+1) x N x NG,
+ * HH: (L+1) x N x N, load: (numstep+1) x NG with row n = fLoad of step n (row 0
+ * unused: tg^0 = 0), X: (numstep+1) x N, row 0 = 0.  Returns 0, -3 (singular H^0)
+ * or -4 (no memory). */
+double orc_mrt_amplitude(int n, double dt);
+int orc_mrt_march(int N, int NG, int L, const double* GG, const double* HH,
+                  const double* load, int numstep, double* X, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,7 +7,8 @@
 // FBC_dof, FBC_values and interface read further lines until their count is
 // reached; node and dof ids are 1-based in the file and 0-based in memory
 // (InputT.cpp:529, 747, 856); an unknown keyword is an error (InputT.cpp:130-136).
-// The multi-region keywords (formulation = 3) are outside this path.
+// With formulation = 3 the auxiliary-mesh keywords nnd_aux, etype_aux, nel_aux,
+// nodes_aux and IEN_aux are read too (InputT::ReadGeometry_Aux, InputT.cpp:548-693).
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -128,11 +129,37 @@ void ModelManagerT::ReadInput(const char* name) {
         else if (k == "num_interface") num_if = std::atoi(need(t, i));
         else if (k == "interface")
             interface_ = read_list(i, num_if, [](const char* s) { return std::atoi(s) - 1; });
-        else if ((k == "nnd_aux" || k == "EType_aux" || k == "nel_aux" || k == "nodes_aux" ||
-                  k == "IEN_aux") &&
-                 formulation_ == 3)
-            raise("multi-region input (formulation=3) is not supported");
-        else
+        else if (formulation_ == 3 && k == "nnd_aux") nnd_aux_ = std::atoi(need(t, i));
+        else if (formulation_ == 3 && k == "nel_aux") nel_aux_ = std::atoi(need(t, i));
+        else if (formulation_ == 3 && k == "etype_aux") {
+            etype_aux_ = std::atoi(need(t, i));
+            if (etype_aux_ == 1) ennd_aux_ = 4;
+            else if (etype_ == 2) ennd_aux_ = 8;  // the reference tests the main EType (:599)
+            else raise("unsupported element type");
+        } else if (formulation_ == 3 && k == "nodes_aux") {
+            coords_aux_.assign(3 * (size_t)nnd_aux_, 0.0);
+            for (int n = 0; n < nnd_aux_; n++) {
+                if (++i >= lines.size()) raise("unexpected end of file in nodes_aux");
+                const auto c = tokens(lines[i]);
+                if (c.size() < 3)
+                    raise("line " + std::to_string(i + 1) + ": aux node " + std::to_string(n + 1) +
+                          " needs 3 coordinates");
+                for (int d = 0; d < 3; d++)
+                    coords_aux_[3 * (size_t)n + d] = std::atof(c[d].c_str());
+            }
+        } else if (formulation_ == 3 && k == "IEN_aux") {
+            ien_aux_.assign((size_t)ennd_aux_ * nel_aux_, 0);
+            for (int e = 0; e < nel_aux_; e++) {
+                if (++i >= lines.size()) raise("unexpected end of file in IEN_aux");
+                const auto c = tokens(lines[i]);
+                if ((int)c.size() < ennd_aux_)
+                    raise("line " + std::to_string(i + 1) + ": aux element " +
+                          std::to_string(e + 1) + " needs " + std::to_string(ennd_aux_) +
+                          " nodes");
+                for (int a = 0; a < ennd_aux_; a++)
+                    ien_aux_[(size_t)e * ennd_aux_ + a] = std::atoi(c[a].c_str()) - 1;
+            }
+        } else
             raise("line " + std::to_string(i + 1) + ": unaccepted key word " + k);
     }
     if (!have_nodes || !have_ien) raise("input has no nodes or no IEN block");

@@ -60,6 +60,10 @@ class Model:
     fbc_dofs: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
     fbc_vals: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0))
     interface: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0, np.int32))
+    # auxiliary mesh of a multi-region input (formulation = 3); read, not used by the path
+    etype_aux: int = 1
+    coords_aux: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 3)))
+    ien_aux: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 4), np.int32))
 
     @property
     def nnd(self) -> int:
@@ -129,7 +133,10 @@ def parse(text: str) -> Model:
     iface: List[int] = []
     ints = {"formulation", "numstep", "sd", "if_ext", "nnd", "nel"}
     reals = {"dt", "E", "nu", "density"}
-    aux = {"nnd_aux", "EType_aux", "nel_aux", "nodes_aux", "IEN_aux"}
+    nnd_aux = nel_aux = 0
+    etype_aux, ennd_aux = 1, 4
+    coords_aux = np.zeros((0, 3))
+    ien_aux = np.zeros((0, 4), np.int32)
     i = 0
     while i < len(lines):
         toks = _tokens(lines[i])
@@ -190,8 +197,39 @@ def parse(text: str) -> Model:
             num_if = c_atoi(val)
         elif k == "interface":
             i, iface = _read_list(lines, i, num_if, lambda t: c_atoi(t) - 1)
-        elif k in aux and kv["formulation"] == 3:
-            raise InputError("multi-region input (formulation=3) is not supported")
+        elif kv["formulation"] == 3 and k in ("nnd_aux", "etype_aux", "nel_aux"):
+            # InputT::ReadGeometry_Aux (InputT.cpp:548-693), read only when formulation = 3
+            if val is None:
+                raise InputError(f"line {i + 1}: {k} is not set properly")
+            if k == "nnd_aux":
+                nnd_aux = c_atoi(val)
+            elif k == "nel_aux":
+                nel_aux = c_atoi(val)
+            else:
+                etype_aux = c_atoi(val)
+                if etype_aux == 1:
+                    ennd_aux = 4
+                elif kv["EType"] == 2:  # the reference tests the main EType here (:599)
+                    ennd_aux = 8
+                else:
+                    raise InputError("unsupported element type")
+        elif kv["formulation"] == 3 and k == "nodes_aux":
+            coords_aux = np.zeros((nnd_aux, 3))
+            for nid in range(nnd_aux):
+                i += 1
+                t = _tokens(lines[i]) if i < len(lines) else []
+                if len(t) < 3:
+                    raise InputError(f"line {i + 1}: aux node {nid + 1} needs 3 coordinates")
+                coords_aux[nid] = [c_atof(t[0]), c_atof(t[1]), c_atof(t[2])]
+        elif kv["formulation"] == 3 and k == "IEN_aux":
+            ien_aux = np.zeros((nel_aux, ennd_aux), np.int32)
+            for eid in range(nel_aux):
+                i += 1
+                t = _tokens(lines[i]) if i < len(lines) else []
+                if len(t) < ennd_aux:
+                    raise InputError(f"line {i + 1}: aux element {eid + 1} needs "
+                                     f"{ennd_aux} nodes")
+                ien_aux[eid] = [c_atoi(x) - 1 for x in t[:ennd_aux]]
         else:
             raise InputError(f"line {i + 1}: unaccepted key word {k!r}")
         i += 1
@@ -207,7 +245,8 @@ def parse(text: str) -> Model:
                  interpolation=kv["interpolation"], sd=kv["sd"],
                  ubc_dofs=np.array(ubc_d, np.int32), ubc_vals=np.array(ubc_v, float),
                  fbc_dofs=np.array(fbc_d, np.int32), fbc_vals=np.array(fbc_v, float),
-                 interface=np.array(iface, np.int32))
+                 interface=np.array(iface, np.int32), etype_aux=etype_aux,
+                 coords_aux=coords_aux, ien_aux=ien_aux)
 
 
 def read(path: str) -> Model:
@@ -224,7 +263,8 @@ def _rows(vals, fmt, per_line=8):
 def dumps(m: Model) -> str:
     """Write a Model in the reference input format (round-trips through parse)."""
     r = repr
-    out = [f"numstep={m.numstep};", f"dt={r(float(m.dt))};",
+    out = [f"formulation={m.formulation};"] if m.formulation != 1 else []
+    out += [f"numstep={m.numstep};", f"dt={r(float(m.dt))};",
            f"interpolation={m.interpolation};", f"nq={m.nq};", "",
            f"E={r(float(m.E))};", f"nu={r(float(m.nu))};", f"density={r(float(m.rho))};", "",
            f"sd={m.sd};", f"nnd={m.nnd};", f"EType={m.etype};", f"nel={m.nel};", "",
@@ -240,6 +280,9 @@ def dumps(m: Model) -> str:
     if len(m.fbc_dofs):
         out += ["FBC_dof=", _rows(m.fbc_dofs, lambda v: str(int(v) + 1)),
                 "FBC_values=", _rows(m.fbc_vals, lambda v: r(float(v)))]
+    if len(m.interface):
+        out += ["", f"num_interface={len(m.interface)};", "interface=",
+                _rows(m.interface, lambda v: str(int(v) + 1))]
     return "\n".join(out) + "\n"
 
 

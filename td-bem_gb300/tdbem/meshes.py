@@ -13,6 +13,12 @@
   over a cubed-sphere cavity at depth d (normals into the cavity), internal
   pressure on the cavity, the patch traction-free.
 
+* :func:`two_region_bar` -- a bar split across its axis into two regions of
+  different material (the multi-region solver's setting, formulation = 3):
+  each region a closed box surface, the shared face listed as the interface of
+  both, a normal traction on the far end of region 2, no prescribed
+  displacements (the two-region solver has none).
+
 The mesh size h of a cubed sphere is the equiangular arc spacing
 ``radius * (pi/2) / n``; the time step is ``dt = beta * h / c_p``.
 """
@@ -87,6 +93,29 @@ def bar(lx: float = 1.0, ly: float = 1.0, lz: float = 4.0, per_unit: int = 2,
     m.fbc_dofs = np.array([3 * n + 2 for n in loaded], np.int32)
     m.fbc_vals = np.full(len(m.fbc_dofs), float(traction))
     return m
+
+
+def two_region_bar(per_unit: int = 2, l1: float = 2.0, l2: float = 2.0, width: float = 1.0,
+                   mu=(7.95e9, 1.59e10), nu=(0.25, 0.25), rho=(2650.0, 2650.0),
+                   beta: float = 0.6, numstep: int = 20, traction: float = 1.0):
+    """Regions 1 (0 <= z <= l1) and 2 (l1 <= z <= l1 + l2) of a width x width bar.
+
+    The default material (c_p = 3000 m/s in region 1) puts the time step near
+    1e-4 s, the scale of the two-region solver's built-in load pulse
+    p0 t exp(-2000 t).  dt = beta h / c_p of region 1, shared by both regions."""
+    m1 = bar(width, width, l1, per_unit, mu[0], nu[0], rho[0], beta, numstep, traction)
+    m2 = bar(width, width, l2, per_unit, mu[1], nu[1], rho[1], beta, numstep, traction)
+    m2.coords = m2.coords + np.array([0.0, 0.0, l1])
+    m2.dt = m1.dt
+    for m in (m1, m2):
+        m.formulation = 3
+        m.ubc_dofs = np.zeros(0, np.int32)
+        m.ubc_vals = np.zeros(0)
+    m1.interface = np.nonzero(np.isclose(m1.coords[:, 2], l1))[0].astype(np.int32)
+    m2.interface = np.nonzero(np.isclose(m2.coords[:, 2], l1))[0].astype(np.int32)
+    m1.fbc_dofs = np.zeros(0, np.int32)
+    m1.fbc_vals = np.zeros(0)
+    return m1, m2
 
 
 def cubed_sphere(n: int = 16, radius: float = 1.0, mu: float = 1.0, nu: float = 0.25,

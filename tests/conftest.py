@@ -17,7 +17,22 @@ def pytest_configure(config):
 
 
 def golden_cases():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """Single-region cases (the two-region ones are named mrt_*)."""
+    return sorted(n for n in (os.path.basename(p)[:-4]
+                              for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+                  if not n.startswith("mrt_"))
+
+
+def mrt_golden_cases():
+    return sorted(os.path.basename(p)[:-4]
+                  for p in glob.glob(os.path.join(GOLDEN, "mrt_*.npz")))
+
+
+def load_mrt_golden(name):
+    """The fixture and the two region models."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    from tdbem import inputfile
+    return z, inputfile.parse(str(z["input_text_1"])), inputfile.parse(str(z["input_text_2"]))
 
 
 def load_golden(name):

@@ -64,6 +64,33 @@ def run_case(driver, name, text, a1=0.0, a2=0.0, full_levels=False, dof_stride=1
     print(f"{name}: D={D} M={M} steps={ns}")
 
 
+def run_mrt_case(name, text1, text2, max_step):
+    """Two-region case through the reference's SolverMRT (oracle/ref_mrt_driver.cpp)."""
+    driver = os.path.join(ROOT, "oracle", "_ref", "ref_mrt_driver")
+    with tempfile.TemporaryDirectory() as tmp:
+        paths = [os.path.join(tmp, f"region{r}.txt") for r in (1, 2)]
+        for p, t in zip(paths, (text1, text2)):
+            with open(p, "w") as f:
+                f.write(t)
+        prefix = os.path.join(tmp, "out")
+        subprocess.run([driver, *paths, str(max_step), prefix], cwd=tmp, check=True,
+                       stdout=subprocess.DEVNULL)
+        N, NG, D1, D2, L, ns = map(int, open(prefix + ".meta").read().split())
+        G = np.fromfile(prefix + ".G").reshape(L + 1, N, NG)
+        H = np.fromfile(prefix + ".H").reshape(L + 1, N, N)
+        x = np.fromfile(prefix + ".x").reshape(ns + 1, N)
+        u1 = np.fromfile(prefix + ".u1").reshape(ns + 1, D1)
+        u2 = np.fromfile(prefix + ".u2").reshape(ns + 1, D2)
+    rng = np.random.default_rng(SEED)
+    wg, wh, wr = rng.standard_normal(NG), rng.standard_normal(N), rng.standard_normal(N)
+    rec = dict(input_text_1=np.array(text1), input_text_2=np.array(text2), max_step=L,
+               numstep=ns, N=N, NG=NG, seed=SEED, G_w=G @ wg, H_w=H @ wh,
+               w_G=np.einsum("d,kde->ke", wr, G), w_H=np.einsum("d,kde->ke", wr, H),
+               x=x, u1=u1, u2=u2)
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **rec)
+    print(f"{name}: N={N} NG={NG} L={L} steps={ns}")
+
+
 def main():
     """All cases, or only those named on the command line."""
     only = set(sys.argv[1:])
@@ -97,6 +124,21 @@ def main():
     bar2 = open(os.path.join(geo, "Bar_2.txt")).read()
     run_case(driver, "ref_bar2", bar2)
     run_case(driver, "ref_bar2_alpha", bar2, a1=0.25, a2=0.1)
+    # Two-region solver (SolverMRT): the reference's layer pair, and a bar split into
+    # two materials with the history truncated (max_step 10 < MaxStep of region 1) or
+    # longer than both regions' MaxStep.
+    if not only or any(n.startswith("mrt_") for n in only):
+        def mrt(name, *a):
+            if not only or name in only:
+                run_mrt_case(name, *a)
+
+        lay = [open(os.path.join(geo, f)).read() for f in ("Layer_B_test0.txt",
+                                                         "Layer_U_test0.txt")]
+        mrt("mrt_layer_test0", lay[0], lay[1], 10)
+        m1, m2 = meshes.two_region_bar(beta=0.6, numstep=20)
+        mrt("mrt_bar_2x2", inputfile.dumps(m1), inputfile.dumps(m2), 10)
+        m1, m2 = meshes.two_region_bar(beta=1.0, numstep=16)
+        mrt("mrt_bar_2x2_long", inputfile.dumps(m1), inputfile.dumps(m2), 24)
 
 
 if __name__ == "__main__":
