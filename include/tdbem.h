@@ -354,6 +354,51 @@ int tdbem_server_stats(tdbem_server* srv, size_t* used_bytes, size_t* budget_byt
 /* Finish every queued and running request, then stop. */
 int tdbem_server_destroy(tdbem_server* srv);
 
+/* ---------------------------------------------------------------------------
+ * Two-region solver: SolverMRT (SolverMRT.h:25-226, SolverMRT.cpp:22-1467).
+ *
+ * Two regions, each a context (its own mesh and material; its FBC list from
+ * tdbem_set_bc gives its loads; UBC lists are not used, as in the reference),
+ * joined at n_iface interface nodes: iface1 / iface2 are the 0-based node ids of
+ * each region's interface list (ModelManagerT::GetInterface).  Region 2's
+ * interface node i is paired with the region-1 interface node at the same
+ * coordinates (within 1e-10, the first such; InterfaceIndexing,
+ * SolverMRT.cpp:458-494); a node without a partner, or two on one partner, is
+ * TDBEM_ERR_ARG.  The combined unknowns (N = D1 + D2, LocalIndexing /
+ * InterfaceIndexing, SolverMRT.cpp:158-566) are the interior displacements of
+ * region 1 and of region 2 (interior nodes in ascending order), then the
+ * interface displacements and the interface tractions of region 1 (its interface
+ * order); region 2 sees the interface traction with the opposite sign.
+ * max_step is SolverMRT's level count (SetMaxStep; the reference's default is
+ * 10).  Both contexts need the same dt and device; the solver uses their FP64
+ * level stores (assemble them through tdbem_mrt_assemble only).
+ * ------------------------------------------------------------------------- */
+typedef struct tdbem_mrt tdbem_mrt;
+int tdbem_mrt_create(tdbem_ctx* region1, tdbem_ctx* region2, const int* iface1,
+                     const int* iface2, int n_iface, int max_step, tdbem_mrt** out);
+int tdbem_mrt_destroy(tdbem_mrt* m);
+/* N combined unknowns, NG interior traction dofs (the known vector). */
+int tdbem_mrt_size(const tdbem_mrt* m, int* N, int* NG);
+/* Combined column of each dof of region 1 or 2: its displacement (ucol) and, on
+ * interface dofs, its traction (tcol; -1 elsewhere).  Arrays of 3*nnd ints. */
+int tdbem_mrt_columns(const tdbem_mrt* m, int region, int* ucol, int* tcol);
+/* SetLoad's amplitude (SolverMRT.cpp:867-966): amp[k] at time k dt (k < n; 0
+ * beyond).  n = 0 restores the reference's pulse 5.46366e9 t exp(-2000 t). */
+int tdbem_mrt_set_load_history(tdbem_mrt* m, const double* amp, int n);
+/* FP64 refinement steps of each solve (0..8, default 1). */
+int tdbem_mrt_set_refine(tdbem_mrt* m, int refine);
+/* Levels of both regions for a run of numstep steps (G_H_Driver for the steps
+ * 1..min(max_step, numstep), as the per-step loop calls it; FP64) and the
+ * inverse of the combined H^0 (TDBEM_ERR_SINGULAR on a zero pivot). */
+int tdbem_mrt_assemble(tdbem_mrt* m, int numstep);
+/* Solve_Direct (SolverMRT.cpp:1028-1097) for steps 1..numstep.  Each output has
+ * numstep + 1 rows (row 0 = the zero initial state) and may be NULL: x_hist the
+ * N combined unknowns; u1/t1 region 1's displacements / tractions (3*nnd1 per
+ * row); u2/t2 region 2's.  Row n of u1 / u2 is what ExtractField stores for step
+ * n (the reference stores it one step later, while solving step n + 1). */
+int tdbem_mrt_march(tdbem_mrt* m, int numstep, double* x_hist, double* u1_hist,
+                    double* t1_hist, double* u2_hist, double* t2_hist);
+
 #ifdef __cplusplus
 }
 #endif

@@ -242,6 +242,17 @@ cudaError_t launch_reduce_solve(const double* partial, int nchunks, int D, const
     return cudaGetLastError();
 }
 
+cudaError_t launch_reduce_partial(const double* partial, int nchunks, int D, double* rhs,
+                                  cudaStream_t s) {
+    k_reduce_partial<<<(D + 255) / 256, 256, 0, s>>>(partial, nchunks, D, rhs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gemv(const double* A, int D, const double* v, double* x, cudaStream_t s) {
+    k_gemv<<<(D * 32 + 255) / 256, 256, 0, s>>>(A, D, v, x);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_update_state(const double* x, int D, int s, const unsigned char* is_u,
                                 const double* ubc_val, const unsigned char* is_f,
                                 const double* fbc_val, double amp, double* u_hist,

@@ -198,6 +198,12 @@ cudaError_t launch_conv(const MarchDev& md, int L, const double* Wt, const doubl
 cudaError_t launch_reduce_solve(const double* partial, int nchunks, int D,
                                 const double* Ainv, double* rhs, double* x, cudaStream_t s);
 cudaError_t launch_add_inplace(double* y, const double* x, size_t n, cudaStream_t s);
+// rhs[i] = sum over chunks of partial[chunk][i]; x = A v for a D x D row-major A.
+cudaError_t launch_reduce_partial(const double* partial, int nchunks, int D, double* rhs,
+                                  cudaStream_t s);
+cudaError_t launch_gemv(const double* A, int D, const double* v, double* x, cudaStream_t s);
+// Level chunks of the convolution over levels 0..L of a D-row store (march.cu).
+int conv_chunks(int L, int D);
 cudaError_t launch_update_state(const double* x, int D, int s, const unsigned char* is_u,
                                 const double* ubc_val, const unsigned char* is_f,
                                 const double* fbc_val, double amp, double* u_hist,

@@ -86,6 +86,15 @@ SIGNATURES = {
                                           ctypes.POINTER(ctypes.c_size_t), _ip, _ip,
                                           ctypes.POINTER(ctypes.c_longlong)]),
     "tdbem_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tdbem_mrt_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _ip, _ip, ctypes.c_int,
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "tdbem_mrt_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tdbem_mrt_size": (ctypes.c_int, [ctypes.c_void_p, _ip, _ip]),
+    "tdbem_mrt_columns": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _ip, _ip]),
+    "tdbem_mrt_set_load_history": (ctypes.c_int, [ctypes.c_void_p, _dp, ctypes.c_int]),
+    "tdbem_mrt_set_refine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_mrt_assemble": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_mrt_march": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
 }
 
 KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve", 4: "assemble_f32",
@@ -442,3 +451,77 @@ class Context:
         b = ctypes.c_size_t()
         _check(load().tdbem_level_bytes(self.h, precision, ctypes.byref(b)))
         return b.value
+
+
+class MultiRegion:
+    """Two-region solver (tdbem_mrt_*, SolverMRT): region models m1, m2 with their
+    interface lists (model.interface, 0-based), max_step levels (SolverMRT's
+    SetMaxStep; the reference's default 10).  Each region gets its own Context
+    (its FBC list gives its loads)."""
+
+    def __init__(self, m1, m2, max_step: int = 10, iface1=None, iface2=None):
+        L = load()
+        self.regions = (Context(m1), Context(m2))
+        i1 = np.ascontiguousarray(m1.interface if iface1 is None else iface1, np.int32)
+        i2 = np.ascontiguousarray(m2.interface if iface2 is None else iface2, np.int32)
+        if len(i1) != len(i2):
+            self.close()
+            raise ValueError("the regions list different numbers of interface nodes")
+        h = ctypes.c_void_p()
+        try:
+            _check(L.tdbem_mrt_create(self.regions[0].h, self.regions[1].h, _i(i1), _i(i2),
+                                      len(i1), max_step, ctypes.byref(h)))
+        except Exception:
+            self.close()
+            raise
+        self.h = h
+        self.numstep = m1.numstep
+        n, ng = ctypes.c_int(), ctypes.c_int()
+        _check(L.tdbem_mrt_size(h, ctypes.byref(n), ctypes.byref(ng)))
+        self.N, self.NG = n.value, ng.value
+        self.D = (self.regions[0].D, self.regions[1].D)
+
+    def columns(self, region: int):
+        u = np.zeros(self.D[region - 1], np.int32)
+        t = np.zeros(self.D[region - 1], np.int32)
+        _check(load().tdbem_mrt_columns(self.h, region, _i(u), _i(t)))
+        return u, t
+
+    def set_load_history(self, amp):
+        a = np.ascontiguousarray(np.zeros(0) if amp is None else amp, np.float64)
+        self._amp = a
+        _check(load().tdbem_mrt_set_load_history(self.h, _d(a), len(a)))
+
+    def set_refine(self, refine: int):
+        _check(load().tdbem_mrt_set_refine(self.h, refine))
+
+    def assemble(self, numstep: Optional[int] = None):
+        _check(load().tdbem_mrt_assemble(self.h, numstep or self.numstep))
+
+    def march(self, numstep: Optional[int] = None):
+        """Combined unknowns x and (u1, t1, u2, t2), numstep + 1 rows each."""
+        n = numstep or self.numstep
+        x = np.zeros((n + 1, self.N))
+        out = [np.zeros((n + 1, d)) for d in (self.D[0], self.D[0], self.D[1], self.D[1])]
+        _check(load().tdbem_mrt_march(self.h, n, _d(x), *[_d(o) for o in out]))
+        return x, out[0], out[1], out[2], out[3]
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().tdbem_mrt_destroy(self.h)
+            self.h = None
+        for c in getattr(self, "regions", ()):
+            c.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
