@@ -398,6 +398,14 @@ int tdbem_mrt_assemble(tdbem_mrt* m, int numstep);
  * n (the reference stores it one step later, while solving step n + 1). */
 int tdbem_mrt_march(tdbem_mrt* m, int numstep, double* x_hist, double* u1_hist,
                     double* t1_hist, double* u2_hist, double* t2_hist);
+/* Stepwise form for a per-step driver (SolverMRT::UpdateGHLinear / Solve per
+ * step): the caller places each region's step blocks with tdbem_update_gh_linear
+ * (steps <= max_step), then tdbem_mrt_step solves step curr_step (the first call
+ * forms and inverts H_DB^0 from level 0) and copies that step's x, u1, t1, u2, t2
+ * (each may be NULL).  tdbem_mrt_begin zeroes the state for numstep steps. */
+int tdbem_mrt_begin(tdbem_mrt* m, int numstep);
+int tdbem_mrt_step(tdbem_mrt* m, int curr_step, double* x, double* u1, double* t1, double* u2,
+                   double* t2);
 
 #ifdef __cplusplus
 }

@@ -7,6 +7,9 @@
 //   SolverStepLinearGpuT SolverT.h:22-128 / SolverStepLinearT (SetTimeControl,
 //                        Initialize, GetMaxStep, UpdateGHLinear, SetLoad,
 //                        Solve, RecordResult, WriteGH)
+//   SolverMRGpuT         SolverMRT.h:25-226 (the two-region solver: SetMaxStep,
+//                        SetTimeControl, UpdateGHLinear with both regions' blocks,
+//                        SetLoad, Solve, RecordResult)
 // Names, argument meaning and error behaviour follow the reference: failures
 // throw `const char*` (the message stays valid until the next failure on this
 // thread), as main.cpp catches.  Everything runs on one GPU through the C ABI of
@@ -95,6 +98,7 @@ class ModelManagerT {
 };
 
 class SolverStepLinearGpuT;
+class SolverMRGpuT;
 
 class ElastoDynamicsGpuT {
    public:
@@ -102,6 +106,8 @@ class ElastoDynamicsGpuT {
     explicit ElastoDynamicsGpuT(ModelManagerT* model);
     // Shares the solver's device context.
     ElastoDynamicsGpuT(ModelManagerT* model, SolverStepLinearGpuT* solver);
+    // Shares the device context of region 1 or 2 of a two-region solver.
+    ElastoDynamicsGpuT(ModelManagerT* model, SolverMRGpuT* solver, int region);
     ~ElastoDynamicsGpuT();
     ElastoDynamicsGpuT(const ElastoDynamicsGpuT&) = delete;
     ElastoDynamicsGpuT& operator=(const ElastoDynamicsGpuT&) = delete;
@@ -167,6 +173,70 @@ class SolverStepLinearGpuT {
     bool begun_ = false;
     std::vector<double> amp_;
     std::vector<std::vector<double>> u_, t_;
+    std::string result_file_ = "displacement.txt";
+};
+
+// SolverMRT (SolverMRT.cpp): two regions joined at the nodes of their interface
+// lists (ModelManagerT::GetInterface), marched with Solve_Direct.  One device
+// context per region (its FBC list gives its loads; UBC lists are not used, as
+// in the reference); the combined system runs on the device (tdbem_mrt_*).
+class SolverMRGpuT {
+   public:
+    // SolverMRT(model_1, model_2) (SolverMRT.cpp:22-64); LocalIndexing and
+    // InterfaceIndexing happen here, as in the reference's constructor.
+    SolverMRGpuT(ModelManagerT* model_1, ModelManagerT* model_2);
+    ~SolverMRGpuT();
+    SolverMRGpuT(const SolverMRGpuT&) = delete;
+    SolverMRGpuT& operator=(const SolverMRGpuT&) = delete;
+
+    void LocalIndexing() {}
+    void InterfaceIndexing() {}
+    // Level count (default 10, SolverMRT.cpp:35); set it before SetTimeControl as
+    // the reference sizes its level store there.
+    void SetMaxStep(int MaxStep);
+    int GetMaxStep() const { return max_step_; }
+    void SetTimeControl(double dt, int Numsteps);
+    void SetCurrStep(int curr_step) { curr_ = curr_step; }
+    // Both regions' blocks of the current step (SolverMRT.cpp:850-949): G_0 / H_0 /
+    // g_0 / h_0 the I parts, G_1 / H_1 / g_1 / h_1 the J parts; steps past MaxStep
+    // are ignored.
+    void UpdateGHLinear(const double* G_0, const double* G_1, const double* H_0,
+                        const double* H_1, const double* g_0, const double* g_1,
+                        const double* h_0, const double* h_1);
+    // The load (interior FBC values x amplitude) is formed on the device in Solve.
+    void SetLoad() {}
+    void Solve();
+    void ExtractField() {}
+    void GetNodeLowHigh(int* low_1, int* high_1, int* low_2, int* high_2);
+    void GetDofLowHigh(int* low_1, int* high_1, int* low_2, int* high_2);
+    // One line per step (SolverMRT.cpp:1337-1388): the time (curr - 1) dt and the
+    // displacement of region 2's record dof at that step.  The reference prints
+    // dof 137 (46*3-1) of its test mesh; here that dof when region 2 has it, else
+    // dof 2, or the dof set by SetRecordDof.  VTK output is not written.
+    void RecordResult();
+    void SetRecordDof(int dof) { record_dof_ = dof; }
+    void SetResultFile(const std::string& path) { result_file_ = path; }
+    // amp[n] at time n dt in place of the built-in pulse 5.46366e9 t exp(-2000 t).
+    void SetLoadHistory(const std::vector<double>& amp);
+
+    // Combined unknowns x of step s (the reference's fDis_DB_Global[s]) and the
+    // regions' displacements / tractions of step s.
+    const std::vector<double>& Unknowns(int s) const { return x_[s]; }
+    const std::vector<double>& Displacement(int region, int s) const { return u_[region - 1][s]; }
+    const std::vector<double>& Traction(int region, int s) const { return t_[region - 1][s]; }
+    int NumUnknowns() const { return N_; }
+    tdbem_ctx* Context(int region) const { return ctx_[region - 1]; }
+
+   private:
+    void make_solver();
+    ModelManagerT* model_[2];
+    tdbem_ctx* ctx_[2] = {nullptr, nullptr};
+    tdbem_mrt* mrt_ = nullptr;
+    int max_step_ = 10, num_steps_ = 0, curr_ = 0, N_ = 0, record_dof_ = -1;
+    double dt_ = 0;
+    bool begun_ = false;
+    std::vector<double> amp_;
+    std::vector<std::vector<double>> x_, u_[2], t_[2];
     std::string result_file_ = "displacement.txt";
 };
 

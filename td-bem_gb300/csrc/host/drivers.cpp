@@ -52,6 +52,17 @@ ElastoDynamicsGpuT::ElastoDynamicsGpuT(ModelManagerT* model, SolverStepLinearGpu
     SetLowerUpper(0, model->GetNND() - 1);
 }
 
+ElastoDynamicsGpuT::ElastoDynamicsGpuT(ModelManagerT* model, SolverMRGpuT* solver, int region)
+    : model_(model),
+      ctx_(solver && (region == 1 || region == 2) ? solver->Context(region) : nullptr),
+      own_ctx_(false) {
+    if (!ctx_) {
+        g_msg = "solver has no device context for that region";
+        throw g_msg.c_str();
+    }
+    SetLowerUpper(0, model->GetNND() - 1);
+}
+
 ElastoDynamicsGpuT::~ElastoDynamicsGpuT() {
     if (own_ctx_) tdbem_ctx_destroy(ctx_);
 }

@@ -23,6 +23,14 @@
 //                         H2_step, SolverT::WriteGH format)
 //   --export-levels file  --fast: write the level store after assembly
 //   --import-levels file  --fast: read the level store instead of assembling
+//   --region2 file        two-region run (SolverMRT, formulation = 3): input.txt
+//                         is region 1, file region 2; per step G_H_Driver on both
+//                         regions while step <= MaxStep, UpdateGHLinear with both
+//                         regions' blocks, SetLoad, Solve, RecordResult; --fast
+//                         assembles both regions' levels and marches in one call.
+//                         --dump writes int32 numstep, int32 N, then (numstep+1) x N
+//                         doubles of the combined unknowns
+//   --max-step L          two-region run: SolverMRT's level count (default 10)
 //   --parse-only          print the model summary and exit (no GPU needed)
 #include <cmath>
 #include <cstdio>
@@ -43,13 +51,15 @@ struct Options {
     bool fast = false, mixed = false, parse_only = false, have_alpha = false;
     double a1 = 0, a2 = 0;
     std::string load_history, result = "displacement.txt", dump, write_gh, export_levels,
-                import_levels;
+                import_levels, region2;
+    int max_step = 10;
 };
 
 void usage() {
     std::cerr << "usage: tdbem_run input.txt [--fast] [--mixed] [--alpha a1 a2] "
                  "[--load-history file] [--result file] [--dump file] [--write-gh prefix] "
-                 "[--export-levels file] [--import-levels file] [--parse-only]\n";
+                 "[--export-levels file] [--import-levels file] [--region2 file] "
+                 "[--max-step L] [--parse-only]\n";
 }
 
 bool parse_args(int argc, char** argv, Options& o) {
@@ -66,8 +76,13 @@ bool parse_args(int argc, char** argv, Options& o) {
             o.a1 = std::atof(x);
             o.a2 = std::atof(y);
             o.have_alpha = true;
+        } else if (a == "--max-step") {
+            const char* v = next();
+            if (!v) return false;
+            o.max_step = std::atoi(v);
         } else if (a == "--load-history" || a == "--result" || a == "--dump" ||
-                   a == "--write-gh" || a == "--export-levels" || a == "--import-levels") {
+                   a == "--write-gh" || a == "--export-levels" || a == "--import-levels" ||
+                   a == "--region2") {
             const char* v = next();
             if (!v) return false;
             if (a == "--load-history") o.load_history = v;
@@ -75,6 +90,7 @@ bool parse_args(int argc, char** argv, Options& o) {
             else if (a == "--dump") o.dump = v;
             else if (a == "--write-gh") o.write_gh = v;
             else if (a == "--export-levels") o.export_levels = v;
+            else if (a == "--region2") o.region2 = v;
             else o.import_levels = v;
         } else if (!a.empty() && a[0] == '-') return false;
         else if (!o.input) o.input = argv[i];
@@ -200,6 +216,76 @@ void run_fast(tdbem::ModelManagerT& model, const Options& o, double a1, double a
     if (!o.dump.empty()) dump(o.dump, n, D, u, t);
 }
 
+void dump_x(const std::string& path, int numstep, int N, const std::vector<double>& x) {
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw "cannot open the dump file";
+    const int32_t hdr[2] = {numstep, N};
+    f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+    f.write(reinterpret_cast<const char*>(x.data()), sizeof(double) * x.size());
+    if (!f) throw "writing the dump file failed";
+}
+
+// The two-region solver with the per-step pattern of main.cpp (89-126) applied to
+// both regions, or (--fast) the whole run on the device.
+void run_mrt(tdbem::ModelManagerT& m1, tdbem::ModelManagerT& m2, const Options& o,
+             const std::vector<double>& amp) {
+    const int num_step = m1.GetNumStep();
+    const double dt = m1.GetDT();
+    tdbem::SolverMRGpuT solver(&m1, &m2);
+    solver.SetResultFile(o.result);
+    solver.SetMaxStep(o.max_step);
+    solver.SetTimeControl(dt, num_step);
+    if (!amp.empty()) solver.SetLoadHistory(amp);
+    const int N = solver.NumUnknowns();
+    std::vector<double> x((size_t)(num_step + 1) * N, 0.0);
+    if (o.fast) {
+        tdbem_mrt* mrt = nullptr;
+        tcheck(tdbem_mrt_create(solver.Context(1), solver.Context(2), m1.GetInterface(),
+                                m2.GetInterface(), m1.GetNumInterface(), o.max_step, &mrt));
+        struct Guard {
+            tdbem_mrt* m;
+            ~Guard() { tdbem_mrt_destroy(m); }
+        } guard{mrt};
+        if (!amp.empty()) tcheck(tdbem_mrt_set_load_history(mrt, amp.data(), (int)amp.size()));
+        tcheck(tdbem_mrt_assemble(mrt, num_step));
+        const int D2 = 3 * m2.GetNND();
+        std::vector<double> u2((size_t)(num_step + 1) * D2);
+        tcheck(tdbem_mrt_march(mrt, num_step, x.data(), nullptr, nullptr, u2.data(), nullptr));
+        std::ofstream f(o.result, std::fstream::out | std::fstream::trunc);
+        if (!f) throw "cannot open the result file";
+        const int dof = D2 > 137 ? 137 : 2;  // SolverMRGpuT::RecordResult's default
+        f << std::setprecision(6);
+        for (int s = 0; s < num_step; s++)
+            f << std::setw(10) << dt * s << std::setw(15) << u2[(size_t)s * D2 + dof]
+              << std::endl;
+    } else {
+        tdbem::ElastoDynamicsGpuT ed1(&m1, &solver, 1), ed2(&m2, &solver, 2);
+        int l1, h1, l2, h2;
+        solver.GetNodeLowHigh(&l1, &h1, &l2, &h2);
+        ed1.SetLowerUpper(l1, h1);
+        ed2.SetLowerUpper(l2, h2);
+        const int max_step = solver.GetMaxStep();
+        for (int n = 1; n <= num_step; n++) {
+            if (n <= max_step) {
+                ed1.G_H_Driver(n * dt, dt);
+                ed2.G_H_Driver(n * dt, dt);
+            }
+            double *G_0, *G_1, *H_0, *H_1, *g_0, *g_1, *h_0, *h_1;
+            ed1.GetGHLinear(&G_0, &G_1, &H_0, &H_1);
+            ed2.GetGHLinear(&g_0, &g_1, &h_0, &h_1);
+            solver.SetCurrStep(n);
+            solver.UpdateGHLinear(G_0, G_1, H_0, H_1, g_0, g_1, h_0, h_1);
+            solver.SetLoad();
+            solver.Solve();
+            solver.RecordResult();
+        }
+        for (int n = 1; n <= num_step; n++)
+            std::copy(solver.Unknowns(n).begin(), solver.Unknowns(n).end(),
+                      x.begin() + (size_t)n * N);
+    }
+    if (!o.dump.empty()) dump_x(o.dump, num_step, N, x);
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -225,12 +311,31 @@ int main(int argc, char** argv) {
                 isum += (long)model.GetIEN()[i] * (1 + i % 5);
             for (int i = 0; i < nu; i++) bsum += (ud[i] + 1) * uv[i];
             for (int i = 0; i < nf; i++) bsum += (fd[i] + 1) * fv[i];
+            long ifsum = 0, auxsum = 0;
+            for (int i = 0; i < model.GetNumInterface(); i++)
+                ifsum += (long)(model.GetInterface()[i] + 1) * (1 + i % 3);
+            for (int i = 0; i < model.GetENND_Aux() * model.GetNEL_Aux(); i++)
+                auxsum += (long)model.GetIEN_Aux()[i] * (1 + i % 5);
             std::printf(
                 "nnd %d nel %d etype %d numstep %d dt %.17g nq %d if_ext %d E %.17g nu %.17g "
-                "rho %.17g ubc %d fbc %d coordsum %.17g iensum %ld bcsum %.17g\n",
+                "rho %.17g ubc %d fbc %d coordsum %.17g iensum %ld bcsum %.17g formulation %d "
+                "ninterface %d ifsum %ld nnd_aux %d nel_aux %d auxsum %ld\n",
                 model.GetNND(), model.GetNEL(), model.GetElementType(), model.GetNumStep(),
                 model.GetDT(), model.GetNQ(), model.GetIfExt(), E, nuv, rho, nu, nf, csum, isum,
-                bsum);
+                bsum, model.GetFormulation(), model.GetNumInterface(), ifsum, model.GetNND_Aux(),
+                model.GetNEL_Aux(), auxsum);
+            return 0;
+        }
+        if (!o.region2.empty()) {
+            tdbem::ModelManagerT model2;
+            model2.ReadInput(o.region2.c_str());
+            std::vector<double> amp;
+            if (!o.load_history.empty()) {
+                amp = read_values(o.load_history);
+                if ((int)amp.size() < model.GetNumStep() + 1)
+                    throw "load history shorter than numstep + 1 (amp[n] at n dt)";
+            }
+            run_mrt(model, model2, o, amp);
             return 0;
         }
         double a1 = o.a1, a2 = o.a2;

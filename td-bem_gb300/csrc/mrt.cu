@@ -159,6 +159,8 @@ struct tdbem_mrt {
     double* d_u[2] = {nullptr, nullptr};
     double* d_t[2] = {nullptr, nullptr};
     int hist_cap = -1;
+    int step_numstep = 0;        // stepwise path: tdbem_mrt_begin's step count
+    bool step_ready = false;     // stepwise path: H_DB^0 inverted
     long long launches = 0;
 
     double amplitude(int n) const {
@@ -213,6 +215,126 @@ std::vector<int> match_interface(const tdbem_ctx* c1, const tdbem_ctx* c2, const
         }
     }
     return match;
+}
+
+// H_DB^0 from the regions' level 0, its inverse, and the convolution buffers for
+// levels up to min(steps, MaxStep of the region).
+int prepare_solve(tdbem_mrt* m, int steps) {
+    cudaStream_t s = m->stream;
+    const size_t NN = (size_t)m->N * m->N;
+    MRT_TRY(cudaMemsetAsync(m->d_A, 0, sizeof(double) * NN, s));
+    for (int r = 0; r < 2; r++) {
+        const tdbem_ctx* c = m->reg[r];
+        const size_t DD = (size_t)c->D * c->D;
+        k_mrt_lhs<<<(unsigned)((DD + 255) / 256), 256, 0, s>>>(
+            c->d_H, c->d_G, c->D, m->d_ucol[r], m->d_tcol[r], m->tsign[r], m->row_lo[r], m->N,
+            m->d_A);
+        MRT_TRY(cudaGetLastError());
+        m->launches++;
+        // levels past the region's MaxStep are exactly zero: the convolution stops there
+        m->lev[r] = std::min(steps, c->M);
+        const int nch = conv_chunks(m->lev[r], c->D);
+        if (nch > m->nch_cap[r]) {
+            release(m->d_partial[r]);
+            MRT_TRY(alloc(&m->d_partial[r], (size_t)nch * c->D));
+            m->nch_cap[r] = nch;
+        }
+        release(m->d_Wt[r]);
+        release(m->d_Wu[r]);
+        MRT_TRY(alloc(&m->d_Wt[r], (size_t)(m->lev[r] + 1) * c->D));
+        MRT_TRY(alloc(&m->d_Wu[r], (size_t)(m->lev[r] + 1) * c->D));
+    }
+    MRT_TRY(cudaMemcpyAsync(m->d_Ainv, m->d_A, sizeof(double) * NN, cudaMemcpyDeviceToDevice, s));
+    bool singular = false;
+    MRT_TRY(invert_f64(m->d_Ainv, m->N, m->d_perm, m->d_status, m->d_scratch, &m->launches,
+                       &singular, s));
+    MRT_TRY(cudaStreamSynchronize(s));
+    if (singular) return mfail(TDBEM_ERR_SINGULAR, "zero pivot in the combined H^0");
+    return TDBEM_OK;
+}
+
+// Histories for numstep steps, row 0 (the initial state) zeroed.
+int ensure_history(tdbem_mrt* m, int numstep) {
+    cudaStream_t s = m->stream;
+    const int N = m->N;
+    if (numstep > m->hist_cap) {
+        release(m->d_X);
+        for (int r = 0; r < 2; r++) {
+            release(m->d_u[r]);
+            release(m->d_t[r]);
+        }
+        m->hist_cap = -1;
+        MRT_TRY(alloc(&m->d_X, (size_t)(numstep + 1) * N));
+        for (int r = 0; r < 2; r++) {
+            MRT_TRY(alloc(&m->d_u[r], (size_t)(numstep + 1) * m->D[r]));
+            MRT_TRY(alloc(&m->d_t[r], (size_t)(numstep + 1) * m->D[r]));
+        }
+        m->hist_cap = numstep;
+    }
+    MRT_TRY(cudaMemsetAsync(m->d_X, 0, sizeof(double) * N, s));
+    for (int r = 0; r < 2; r++) {
+        MRT_TRY(cudaMemsetAsync(m->d_u[r], 0, sizeof(double) * m->D[r], s));
+        MRT_TRY(cudaMemsetAsync(m->d_t[r], 0, sizeof(double) * m->D[r], s));
+    }
+    return TDBEM_OK;
+}
+
+// One step of Solve_Direct: the regions' history sums into the two row blocks
+// of the right-hand side, x = (H_DB^0)^-1 rhs with FP64 refinement, the regions'
+// states of step n.
+int mrt_step(tdbem_mrt* m, int n) {
+    cudaStream_t s = m->stream;
+    const int N = m->N;
+    const double amp = m->amplitude(n);
+    for (int r = 0; r < 2; r++) {
+        const tdbem_ctx* c = m->reg[r];
+        const int D = c->D;
+        const int L = std::min(n, m->lev[r]);
+        const size_t nw = (size_t)(L + 1) * D;
+        k_mrt_w<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(m->d_u[r], m->d_t[r], m->d_fl[r], D,
+                                                             n, L, amp, m->d_Wt[r], m->d_Wu[r]);
+        MRT_TRY(cudaGetLastError());
+        const MarchDev md{D, c->M, c->d_G, c->d_H, nullptr, nullptr};
+        const int nch = conv_chunks(L, D);
+        MRT_TRY(launch_conv(md, L, m->d_Wt[r], m->d_Wu[r], m->d_partial[r], nch, s));
+        MRT_TRY(launch_reduce_partial(m->d_partial[r], nch, D, m->d_rhs + m->row_lo[r], s));
+        m->launches += 3;
+    }
+    MRT_TRY(launch_gemv(m->d_Ainv, N, m->d_rhs, m->d_x, s));
+    m->launches++;
+    for (int it = 0; it < m->refine; it++) {
+        k_mrt_residual<<<(N * 32 + 255) / 256, 256, 0, s>>>(m->d_A, N, m->d_x, m->d_rhs, m->d_r);
+        MRT_TRY(cudaGetLastError());
+        MRT_TRY(launch_gemv(m->d_Ainv, N, m->d_r, m->d_dx, s));
+        MRT_TRY(launch_add_inplace(m->d_x, m->d_dx, N, s));
+        m->launches += 3;
+    }
+    MRT_TRY(cudaMemcpyAsync(m->d_X + (size_t)n * N, m->d_x, sizeof(double) * N,
+                            cudaMemcpyDeviceToDevice, s));
+    for (int r = 0; r < 2; r++) {
+        k_mrt_state<<<(m->D[r] + 255) / 256, 256, 0, s>>>(m->d_x, m->d_ucol[r], m->d_tcol[r],
+                                                          m->tsign[r], m->d_fl[r], amp, m->D[r],
+                                                          n, m->d_u[r], m->d_t[r]);
+        MRT_TRY(cudaGetLastError());
+        m->launches++;
+    }
+    return TDBEM_OK;
+}
+
+// Rows [row0, row0 + rows) of the histories to the host (null outputs skipped).
+int copy_out(tdbem_mrt* m, int row0, int rows, double* x, double* u1, double* t1, double* u2,
+             double* t2) {
+    cudaStream_t s = m->stream;
+    double* outs[5] = {x, u1, t1, u2, t2};
+    const double* srcs[5] = {m->d_X, m->d_u[0], m->d_t[0], m->d_u[1], m->d_t[1]};
+    const int widths[5] = {m->N, m->D[0], m->D[0], m->D[1], m->D[1]};
+    for (int k = 0; k < 5; k++)
+        if (outs[k])
+            MRT_TRY(cudaMemcpyAsync(outs[k], srcs[k] + (size_t)row0 * widths[k],
+                                    sizeof(double) * (size_t)rows * widths[k],
+                                    cudaMemcpyDeviceToHost, s));
+    MRT_TRY(cudaStreamSynchronize(s));
+    return TDBEM_OK;
 }
 
 }  // namespace
@@ -392,37 +514,8 @@ int tdbem_mrt_assemble(tdbem_mrt* m, int numstep) {
     for (int r = 0; r < 2; r++)
         if (rc[r] != TDBEM_OK) return mfail(rc[r], "region %d: %s", r + 1, msg[r].c_str());
     MRT_TRY(cudaStreamSynchronize(m->reg[1]->stream));
-    cudaStream_t s = m->stream;
-    const size_t NN = (size_t)m->N * m->N;
-    MRT_TRY(cudaMemsetAsync(m->d_A, 0, sizeof(double) * NN, s));
-    for (int r = 0; r < 2; r++) {
-        const tdbem_ctx* c = m->reg[r];
-        const size_t DD = (size_t)c->D * c->D;
-        k_mrt_lhs<<<(unsigned)((DD + 255) / 256), 256, 0, s>>>(
-            c->d_H, c->d_G, c->D, m->d_ucol[r], m->d_tcol[r], m->tsign[r], m->row_lo[r], m->N,
-            m->d_A);
-        MRT_TRY(cudaGetLastError());
-        m->launches++;
-        // levels past the region's MaxStep are exactly zero: the convolution stops there
-        m->lev[r] = std::min(steps, c->M);
-        const int nch = conv_chunks(m->lev[r], c->D);
-        if (nch > m->nch_cap[r]) {
-            release(m->d_partial[r]);
-            MRT_TRY(alloc(&m->d_partial[r], (size_t)nch * c->D));
-            m->nch_cap[r] = nch;
-        }
-        // the convolution vectors follow the level count of this assembly
-        release(m->d_Wt[r]);
-        release(m->d_Wu[r]);
-        MRT_TRY(alloc(&m->d_Wt[r], (size_t)(m->lev[r] + 1) * c->D));
-        MRT_TRY(alloc(&m->d_Wu[r], (size_t)(m->lev[r] + 1) * c->D));
-    }
-    MRT_TRY(cudaMemcpyAsync(m->d_Ainv, m->d_A, sizeof(double) * NN, cudaMemcpyDeviceToDevice, s));
-    bool singular = false;
-    MRT_TRY(invert_f64(m->d_Ainv, m->N, m->d_perm, m->d_status, m->d_scratch, &m->launches,
-                       &singular, s));
-    MRT_TRY(cudaStreamSynchronize(s));
-    if (singular) return mfail(TDBEM_ERR_SINGULAR, "zero pivot in the combined H^0");
+    const int rc2 = prepare_solve(m, steps);
+    if (rc2 != TDBEM_OK) return rc2;
     m->assembled = steps;
     return TDBEM_OK;
 }
@@ -436,72 +529,43 @@ int tdbem_mrt_march(tdbem_mrt* m, int numstep, double* x_hist, double* u1_hist,
     if (std::min(m->L, numstep) > m->assembled)
         return mfail(TDBEM_ERR_STATE, "levels assembled for %d steps, %d needed", m->assembled,
                      std::min(m->L, numstep));
-    cudaStream_t s = m->stream;
-    const int N = m->N;
-    if (numstep > m->hist_cap) {
-        release(m->d_X);
-        for (int r = 0; r < 2; r++) {
-            release(m->d_u[r]);
-            release(m->d_t[r]);
-        }
-        MRT_TRY(alloc(&m->d_X, (size_t)(numstep + 1) * N));
-        for (int r = 0; r < 2; r++) {
-            MRT_TRY(alloc(&m->d_u[r], (size_t)(numstep + 1) * m->D[r]));
-            MRT_TRY(alloc(&m->d_t[r], (size_t)(numstep + 1) * m->D[r]));
-        }
-        m->hist_cap = numstep;
-    }
-    MRT_TRY(cudaMemsetAsync(m->d_X, 0, sizeof(double) * N, s));
-    for (int r = 0; r < 2; r++) {
-        MRT_TRY(cudaMemsetAsync(m->d_u[r], 0, sizeof(double) * m->D[r], s));
-        MRT_TRY(cudaMemsetAsync(m->d_t[r], 0, sizeof(double) * m->D[r], s));
-    }
-    for (int n = 1; n <= numstep; n++) {
-        const double amp = m->amplitude(n);
-        for (int r = 0; r < 2; r++) {
-            const tdbem_ctx* c = m->reg[r];
-            const int D = c->D;
-            const int L = std::min(n, m->lev[r]);
-            const size_t nw = (size_t)(L + 1) * D;
-            k_mrt_w<<<(unsigned)((nw + 255) / 256), 256, 0, s>>>(
-                m->d_u[r], m->d_t[r], m->d_fl[r], D, n, L, amp, m->d_Wt[r], m->d_Wu[r]);
-            MRT_TRY(cudaGetLastError());
-            const MarchDev md{D, c->M, c->d_G, c->d_H, nullptr, nullptr};
-            const int nch = conv_chunks(L, D);
-            MRT_TRY(launch_conv(md, L, m->d_Wt[r], m->d_Wu[r], m->d_partial[r], nch, s));
-            MRT_TRY(launch_reduce_partial(m->d_partial[r], nch, D, m->d_rhs + m->row_lo[r], s));
-            m->launches += 3;
-        }
-        MRT_TRY(launch_gemv(m->d_Ainv, N, m->d_rhs, m->d_x, s));
-        m->launches++;
-        for (int it = 0; it < m->refine; it++) {
-            k_mrt_residual<<<(N * 32 + 255) / 256, 256, 0, s>>>(m->d_A, N, m->d_x, m->d_rhs,
-                                                                 m->d_r);
-            MRT_TRY(cudaGetLastError());
-            MRT_TRY(launch_gemv(m->d_Ainv, N, m->d_r, m->d_dx, s));
-            MRT_TRY(launch_add_inplace(m->d_x, m->d_dx, N, s));
-            m->launches += 3;
-        }
-        MRT_TRY(cudaMemcpyAsync(m->d_X + (size_t)n * N, m->d_x, sizeof(double) * N,
-                                cudaMemcpyDeviceToDevice, s));
-        for (int r = 0; r < 2; r++) {
-            k_mrt_state<<<(m->D[r] + 255) / 256, 256, 0, s>>>(
-                m->d_x, m->d_ucol[r], m->d_tcol[r], m->tsign[r], m->d_fl[r], amp, m->D[r], n,
-                m->d_u[r], m->d_t[r]);
-            MRT_TRY(cudaGetLastError());
-            m->launches++;
-        }
-    }
-    double* outs[5] = {x_hist, u1_hist, t1_hist, u2_hist, t2_hist};
-    const double* srcs[5] = {m->d_X, m->d_u[0], m->d_t[0], m->d_u[1], m->d_t[1]};
-    const int widths[5] = {N, m->D[0], m->D[0], m->D[1], m->D[1]};
-    for (int k = 0; k < 5; k++)
-        if (outs[k])
-            MRT_TRY(cudaMemcpyAsync(outs[k], srcs[k],
-                                    sizeof(double) * (size_t)(numstep + 1) * widths[k],
-                                    cudaMemcpyDeviceToHost, s));
-    MRT_TRY(cudaStreamSynchronize(s));
+    int rc = ensure_history(m, numstep);
+    for (int n = 1; rc == TDBEM_OK && n <= numstep; n++) rc = mrt_step(m, n);
+    if (rc != TDBEM_OK) return rc;
+    return copy_out(m, 0, numstep + 1, x_hist, u1_hist, t1_hist, u2_hist, t2_hist);
+}
+
+int tdbem_mrt_begin(tdbem_mrt* m, int numstep) {
+    if (!m) return mfail(TDBEM_ERR_ARG, "null solver");
+    if (numstep < 1) return mfail(TDBEM_ERR_ARG, "numstep must be >= 1");
+    const int rc = ensure_history(m, numstep);
+    if (rc != TDBEM_OK) return rc;
+    m->step_numstep = numstep;
+    m->step_ready = false;
+    m->assembled = -1;  // the levels now come from tdbem_update_gh_linear
     return TDBEM_OK;
+}
+
+int tdbem_mrt_step(tdbem_mrt* m, int curr_step, double* x, double* u1, double* t1, double* u2,
+                   double* t2) {
+    if (!m) return mfail(TDBEM_ERR_ARG, "null solver");
+    if (m->step_numstep < 1) return mfail(TDBEM_ERR_STATE, "tdbem_mrt_begin has not run");
+    if (curr_step < 1 || curr_step > m->step_numstep)
+        return mfail(TDBEM_ERR_ARG, "step %d outside 1..%d", curr_step, m->step_numstep);
+    for (int r = 0; r < 2; r++)
+        if (m->reg[r]->level_precision != TDBEM_FP64 || m->reg[r]->levels_last < 1)
+            return mfail(TDBEM_ERR_STATE, "region %d has no level 0 (UpdateGHLinear of step 1)",
+                         r + 1);
+    if (!m->step_ready) {
+        // H_DB^0 is final once step 1 is placed (level 0 holds only J(1)); the
+        // convolution reads levels up to the loop's last placed step
+        const int rc = prepare_solve(m, std::max(1, std::min(m->L, m->step_numstep)));
+        if (rc != TDBEM_OK) return rc;
+        m->step_ready = true;
+    }
+    const int rc = mrt_step(m, curr_step);
+    if (rc != TDBEM_OK) return rc;
+    return copy_out(m, curr_step, 1, x, u1, t1, u2, t2);
 }
 
 }  // extern "C"

@@ -95,6 +95,8 @@ SIGNATURES = {
     "tdbem_mrt_set_refine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_mrt_assemble": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_mrt_march": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
+    "tdbem_mrt_begin": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_mrt_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]),
 }
 
 KERNEL_CLASSES = {0: "assemble", 1: "conv", 2: "factor", 3: "solve", 4: "assemble_f32",
@@ -505,6 +507,16 @@ class MultiRegion:
         out = [np.zeros((n + 1, d)) for d in (self.D[0], self.D[0], self.D[1], self.D[1])]
         _check(load().tdbem_mrt_march(self.h, n, _d(x), *[_d(o) for o in out]))
         return x, out[0], out[1], out[2], out[3]
+
+    def begin(self, numstep: Optional[int] = None):
+        self._steps = numstep or self.numstep
+        _check(load().tdbem_mrt_begin(self.h, self._steps))
+
+    def step(self, curr_step: int):
+        """Solve step curr_step from the placed levels; x, u1, t1, u2, t2 of that step."""
+        out = [np.zeros(k) for k in (self.N, self.D[0], self.D[0], self.D[1], self.D[1])]
+        _check(load().tdbem_mrt_step(self.h, curr_step, *[_d(o) for o in out]))
+        return tuple(out)
 
     def close(self):
         if getattr(self, "h", None):

@@ -159,3 +159,37 @@ def test_stepwise_abi_equals_whole_run(tdlib):
                 c2.update_gh_linear(s, *c2.gh_driver(s))
             us, _ = c2.march_step(s)
             assert rel_max(us, u[s - 1]) <= TOL or np.abs(u[s - 1]).max() == 0
+
+
+@pytest.mark.parametrize("mode", ["stepwise", "fast"])
+@pytest.mark.parametrize("name", ["mrt_layer_test0", "mrt_bar_2x2_long"])
+def test_tdbem_run_two_regions_matches_oracle(tdlib, oracle_mod, name, mode, tmp_path):
+    """tdbem_run --region2: SolverMRGpuT in main()'s per-step pattern for two
+    regions (ElastoDynamicsGpuT on each region, UpdateGHLinear with both
+    regions' blocks, Solve), or the whole run (--fast); the combined unknowns
+    against the oracle's SolverMRT at 1e-10 per step (displacements and
+    interface tractions apart), RecordResult's lines from region 2's history."""
+    from conftest import load_mrt_golden
+    z, m1, m2 = load_mrt_golden(name)
+    L = int(z["max_step"])
+    mr = oracle_mod.MultiRegion(m1, m2, L, clean=True)
+    GG, HH = mr.assemble_levels()
+    Xo, _, u2o = mr.march(GG, HH)
+    (tmp_path / "r1.txt").write_text(str(z["input_text_1"]))
+    (tmp_path / "r2.txt").write_text(str(z["input_text_2"]))
+    cmd = [RUN, "r1.txt", "--region2", "r2.txt", "--max-step", str(L), "--dump", "x.bin"]
+    r = subprocess.run(cmd + (["--fast"] if mode == "fast" else []), cwd=tmp_path,
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    with open(tmp_path / "x.bin", "rb") as f:
+        n, N = np.frombuffer(f.read(8), np.int32)
+        X = np.frombuffer(f.read(), np.float64).reshape(n + 1, N)
+    assert X.shape == Xo.shape
+    k = mr.NI1 + mr.NI2 + mr.NZ
+    check_steps(X[:, :k], Xo[:, :k], "x displacements")
+    check_steps(X[:, k:], Xo[:, k:], "x interface tractions")
+    rows = np.loadtxt(tmp_path / "displacement.txt")
+    dof = 137 if mr.D2 > 137 else 2
+    assert rows.shape == (n, 2)
+    assert np.allclose(rows[:, 0], m1.dt * np.arange(n), rtol=1e-5, atol=1e-15)
+    assert np.allclose(rows[:, 1], u2o[:n, dof], rtol=1e-5, atol=1e-12 * np.abs(u2o).max())

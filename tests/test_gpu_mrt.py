@@ -136,3 +136,27 @@ def test_mrt_errors(tdlib):
     with pytest.raises(tdlib.TdbemError) as e:
         tdlib.MultiRegion(m1, m2, 10, iface2=shifted)
     assert e.value.code == -1 and "mismatch" in str(e.value)
+
+
+def test_mrt_stepwise_equals_whole_run(tdlib):
+    """Per-step placement (tdbem_update_gh_linear with tdbem_gh_driver blocks of each
+    region, steps <= max_step) + tdbem_mrt_step gives the whole run's histories."""
+    z, m1, m2 = load_mrt_golden("mrt_bar_2x2")
+    L, ns = int(z["max_step"]), m1.numstep
+    with tdlib.MultiRegion(m1, m2, L) as g:
+        g.assemble()
+        X, u1, _, u2, _ = g.march()
+    with tdlib.MultiRegion(m1, m2, L) as g:
+        g.begin(ns)
+        xs = [np.zeros(g.N)]
+        for n in range(1, ns + 1):
+            if n <= L:
+                for ctx in g.regions:
+                    GI, GJ, HI, HJ = ctx.gh_driver(n)
+                    ctx.update_gh_linear(n, GI, GJ, HI, HJ)
+            xs.append(g.step(n)[0])
+    Xs = np.array(xs)
+    assert Xs.shape == X.shape
+    mr_k = g.N - (g.N - g.NG) // 2  # displacement unknowns: NI1 + NI2 + NZ
+    check_steps(Xs[:, :mr_k], X[:, :mr_k], "stepwise x displacements")
+    check_steps(Xs[:, mr_k:], X[:, mr_k:], "stepwise x tractions")

@@ -7,7 +7,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import ROOT, golden_cases, load_golden
+from conftest import ROOT, golden_cases, load_golden, load_mrt_golden, mrt_golden_cases
 
 RUN = os.path.join(ROOT, "td-bem_gb300", "_build", "tdbem_run")
 
@@ -46,6 +46,41 @@ def test_native_reader_matches_python_parser(built, name, tmp_path):
     for k, v in zip(keys, ref):
         got = float(vals[k])
         assert got == pytest.approx(v, rel=1e-13, abs=1e-12), k
+
+
+@pytest.mark.parametrize("name", mrt_golden_cases())
+@pytest.mark.parametrize("region", [1, 2])
+def test_native_reader_two_region_inputs(built, name, region, tmp_path):
+    """formulation = 3 inputs: interface lists and the auxiliary mesh keywords."""
+    z, m1, m2 = load_mrt_golden(name)
+    m = (m1, m2)[region - 1]
+    p = tmp_path / "input.txt"
+    p.write_text(str(z[f"input_text_{region}"]))
+    r = subprocess.run([RUN, str(p), "--parse-only"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    tok = r.stdout.split()
+    vals = dict(zip(tok[0::2], tok[1::2]))
+    for k, v in zip(["nnd", "nel", "numstep", "dt", "E", "coordsum", "iensum", "bcsum"],
+                    [summary(m)[i] for i in (0, 1, 3, 4, 7, 12, 13, 14)]):
+        assert float(vals[k]) == pytest.approx(v, rel=1e-13, abs=1e-12), k
+    assert int(vals["formulation"]) == 3
+    assert int(vals["ninterface"]) == len(m.interface)
+    assert int(vals["ifsum"]) == sum((int(n) + 1) * (1 + i % 3) for i, n in enumerate(m.interface))
+    assert int(vals["nnd_aux"]) == len(m.coords_aux)
+    assert int(vals["nel_aux"]) == len(m.ien_aux)
+    e = m.ien_aux.reshape(-1)
+    assert int(vals["auxsum"]) == sum(int(e[i]) * (1 + i % 5) for i in range(len(e)))
+
+
+def test_reader_rejects_aux_keywords_outside_multiregion(built, tmp_path):
+    """InputT reads the auxiliary mesh only when formulation = 3 (InputT.cpp:117-122)."""
+    p = tmp_path / "bad.txt"
+    p.write_text("numstep=3;\nnnd_aux=4;\n")
+    r = subprocess.run([RUN, str(p), "--parse-only"], capture_output=True, text=True)
+    assert r.returncode == 1 and "unaccepted key word nnd_aux" in r.stderr
+    from tdbem import inputfile
+    with pytest.raises(inputfile.InputError):
+        inputfile.parse("numstep=3;\nnnd_aux=4;\n")
 
 
 def test_reader_rejects_unknown_keyword(built, tmp_path):
