@@ -532,7 +532,7 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
     const PairInfo pi = pair_window_info<ENND>(coords, ien, elems, ne, node_lo, ph, mode,
                                                level_last, level_cap, step_n, select, p);
     pairs[p] = pi;
-    counts[p] = (unsigned)pi.cnt;
+    if (counts) counts[p] = (unsigned)pi.cnt;
 }
 
 // mode ASM_LEVELS: item = (pair, level k), I part at k dt (k >= 1) plus J part at
@@ -838,23 +838,16 @@ __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool d
     }
 }
 
-// Far (well-separated, non-singular) items in FP32, ASM_LEVELS placement into the
-// FP32 level store.  Gauss-point geometry comes from the FP32 table (points
-// relative to the element's first node); no FP64 arithmetic or conversion in the
-// point loop, which on GB300 would run on the narrow FP64 pipe.
-__global__ void __launch_bounds__(256) k_assemble_far_f32(
-    const double* __restrict__ coords, const int* __restrict__ ien,
-    const int* __restrict__ elems, int ne, int node_lo, int nq2,
-    const float* __restrict__ geomf, Phys ph, int level_last,
-    const PairInfo* __restrict__ pairs, const unsigned* __restrict__ offsets, unsigned npairs,
-    unsigned nitems, AsmOut out) {
-    unsigned p;
-    if (!item_pair(offsets, npairs, nitems, p)) return;
-    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
-    const PairInfo pi = pairs[p];
-    const int k = pi.klo + (int)(gid - __ldg(offsets + p));
-    const int c = node_lo + (int)(p / ne);
-    const int e = elems[p % ne];
+// One far (well-separated, non-singular) item in FP32: collocation node c,
+// element e, level k (I part at k dt, J part at (k+1) dt), added into the FP32
+// level store.  Gauss-point geometry comes from the FP32 table (points relative to
+// the element's first node); no FP64 arithmetic in the point loop, which on GB300
+// would run on the narrow FP64 pipe.
+__device__ __forceinline__ void far_item(const double* __restrict__ coords,
+                                         const int* __restrict__ ien, int c, int e, int k,
+                                         int nq2, const float* __restrict__ geomf,
+                                         const PhysF& f, float TI, int level_last,
+                                         const AsmOut& out) {
     int nid[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
@@ -862,9 +855,7 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
     const float xc[3] = {(float)(coords[c * 3] - coords[nid[0] * 3]),
                          (float)(coords[c * 3 + 1] - coords[nid[0] * 3 + 1]),
                          (float)(coords[c * 3 + 2] - coords[nid[0] * 3 + 2])};
-    const PhysF f = to_f(ph);
     const bool doI = (k >= 1), doJ = (k + 1 <= level_last);
-    const float TI = (float)(k * ph.dt);
     ItemAccF acc;
 #pragma unroll
     for (int a = 0; a < 4; a++) {
@@ -894,6 +885,82 @@ __global__ void __launch_bounds__(256) k_assemble_far_f32(
                 out.G0f[idx] += acc.g[a][sym[i * 3 + j]];
                 out.H0f[idx] += acc.h[a][i * 3 + j];
             }
+}
+
+constexpr int kFarBlock = 128;  // threads of a far-field block
+constexpr int kFarChunk = 8;    // levels of a far-field block (the item code keeps 4 bits)
+
+// Exclusive scan of one value per thread over the block; returns the block total.
+__device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
+    __syncthreads();
+    int before = 0, total = 0;
+#pragma unroll
+    for (int i = 0; i < kFarBlock / 32; i++) {
+        const int t = s_warp[i];
+        before += i < w ? t : 0;
+        total += t;
+    }
+    excl = before + x - v;
+    __syncthreads();  // s_warp is reused by the next scan
+    return total;
+}
+
+// All far items of collocation node c = blockIdx.x at levels [k0, k0 + kFarChunk),
+// k0 = blockIdx.y * kFarChunk.  The block owns those rows of those levels, so it
+// walks the element colours in order (elements of one colour share no node:
+// their items write distinct entries) with a barrier between colours: every add
+// to a row lands while the rows are resident in L2, in a fixed order (bitwise
+// reproducible), and one launch covers all colours.  Candidate items (element,
+// level) of a batch of kFarBlock elements are compacted with a block scan and
+// spread over the threads.  pairs[c * nel + j] is the window of node c and the
+// j-th element in colour order.
+__global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
+    const double* __restrict__ coords, const int* __restrict__ ien,
+    const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
+    int nel, int nq2, const float* __restrict__ geomf, Phys ph, int level_last,
+    const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
+    __shared__ int s_warp[kFarBlock / 32];
+    __shared__ int s_items[kFarBlock * kFarChunk];
+    const int c = blockIdx.x;
+    const int k0 = blockIdx.y * kFarChunk;
+    const int k1 = min(k0 + kFarChunk, level_last + 1);
+    const PhysF f = to_f(ph);
+    const PairInfo* pc = pairs + (size_t)c * nel;
+    unsigned long long count = 0;
+    for (int col = 0; col < ncolor; col++) {
+        const int j0 = color_start[col], j1 = color_start[col + 1];
+        for (int base = j0; base < j1; base += kFarBlock) {  // uniform over the block
+            const int j = base + (int)threadIdx.x;
+            int na = 0, lo = 0;
+            if (j < j1) {
+                const PairInfo pi = pc[j];
+                lo = max(k0, pi.klo);
+                na = max(0, min(k1, pi.klo + pi.cnt) - lo);
+            }
+            int off;
+            const int total = far_block_scan(na, off, s_warp);
+            for (int t = 0; t < na; t++) s_items[off + t] = ((j - j0) << 4) | (lo + t - k0);
+            __syncthreads();
+            for (int i = threadIdx.x; i < total; i += kFarBlock) {
+                const int code = s_items[i];
+                const int k = k0 + (code & 15);
+                far_item(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, f,
+                         (float)k * f.dt, level_last, out);
+            }
+            count += total;
+            // s_items is rebuilt next; this batch's adds come before the next colour's
+            __syncthreads();
+        }
+    }
+    if (nitems && threadIdx.x == 0 && count) atomicAdd(nitems, count);
 }
 
 // C term (TDElementStepLinearT.cpp:103-109, 501-508, 577-584 with AssembleC,
@@ -1134,23 +1201,30 @@ static void launch_items_fp64(const double* coords, const int* ien, const int* e
 cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd,
                                   const int* elems, int nelem_color, int node_lo, int nq,
                                   const double* gx, const double* gw, const double* geom,
-                                  const float* geomf, const Phys& ph, int mode, int level_last,
-                                  int step_n, const PairInfo* pairs, const unsigned* offsets,
+                                  const Phys& ph, int mode, int level_last, int step_n,
+                                  const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  int fp32_far, cudaStream_t s) {
+                                  cudaStream_t s) {
     if (nitems == 0) return cudaSuccess;
     if (ennd == 8) {
-        if (fp32_far) return cudaErrorInvalidValue;  // the FP32 far form is 4-node only
         launch_items_fp64<8>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
                              level_last, step_n, pairs, offsets, npairs, nitems, out, s);
-    } else if (fp32_far) {
-        k_assemble_far_f32<<<(nitems + 255) / 256, 256, 0, s>>>(
-            coords, ien, elems, nelem_color, node_lo, nq * nq, geomf, ph, level_last, pairs,
-            offsets, npairs, nitems, out);
     } else {
         launch_items_fp64<4>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
                              level_last, step_n, pairs, offsets, npairs, nitems, out, s);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
+                                     const int* color_elems, const int* color_start, int ncolor,
+                                     int nnd, int nel, int nq, const float* geomf, const Phys& ph,
+                                     int level_last, const PairInfo* pairs, const AsmOut& out,
+                                     unsigned long long* nitems, cudaStream_t s) {
+    const dim3 grid(nnd, (level_last + kFarChunk) / kFarChunk);
+    k_assemble_far_rows<<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems, color_start, ncolor,
+                                                    nel, nq * nq, geomf, ph, level_last, pairs,
+                                                    out, nitems);
     return cudaGetLastError();
 }
 

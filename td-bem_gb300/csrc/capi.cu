@@ -265,7 +265,7 @@ void prof_flush(tdbem_ctx* c) {
 // Run the window / scan / item kernels of one colour over collocation nodes
 // [node_lo, node_lo + nnodes), chunked so that item indices fit in 32 bits.
 int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, int level_last,
-                   int level_cap, int step_n, int select, int fp32_far, const AsmOut& out) {
+                   int level_cap, int step_n, int select, const AsmOut& out) {
     const int e0 = c->color_start[color], ne = c->color_start[color + 1] - e0;
     if (ne == 0 || nnodes == 0) return TDBEM_OK;
     const int* elems = c->d_color_elems + e0;
@@ -293,18 +293,16 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
                                  cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
         const unsigned nitems = last[0] + last[1];
-        const int pe = prof_begin(c, fp32_far ? TDBEM_K_ASSEMBLE_F32 : TDBEM_K_ASSEMBLE);
-        CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq, c->d_gx,
-                                       c->d_gw, c->d_geom, c->d_geomf, c->ph, mode, level_last,
-                                       step_n,
-                                       c->d_pairs, c->d_offsets, npairs, nitems, out, fp32_far,
+        const int pe = prof_begin(c, TDBEM_K_ASSEMBLE);
+        CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
+                                       c->d_gx, c->d_gw, c->d_geom, c->ph, mode, level_last,
+                                       step_n, c->d_pairs, c->d_offsets, npairs, nitems, out,
                                        c->stream));
         if (nitems) c->launches += (mode == ASM_STEP ? 2 : 1);
         const double pts = (double)c->nq * c->nq;
         const double items = (double)nitems * (mode == ASM_STEP ? 2.0 : 1.0);
         prof_end(c, pe, items * 4 * 45 * (out.G0f ? 4.0 : 8.0) * 2,
-                 items * pts * (fp32_far ? kFlopsPerItemPointF32 : kFlopsPerItemPoint) *
-                     (mode == ASM_STEP ? 0.5 : 1.0));
+                 items * pts * kFlopsPerItemPoint * (mode == ASM_STEP ? 0.5 : 1.0));
     }
     return TDBEM_OK;
 }
@@ -763,6 +761,8 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_cterm, (size_t)c->nnd * 9));
     if (ennd == 4) CTX_TRY(dalloc(&c->d_geomf, (size_t)c->nel * nq * nq * 12));
     CTX_TRY(dalloc(&c->d_color_elems, order.size()));
+    CTX_TRY(dalloc(&c->d_color_start, c->color_start.size()));
+    CTX_TRY(dalloc(&c->d_far_items, 1));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
     CTX_TRY(cudaMemcpyAsync(c->d_ien, c->h_ien.data(), sizeof(int) * c->h_ien.size(),
@@ -770,6 +770,9 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(cudaMemcpyAsync(c->d_gx, gx.data(), sizeof(double) * nq, cudaMemcpyHostToDevice,
                             c->stream));
     CTX_TRY(cudaMemcpyAsync(c->d_gw, gw.data(), sizeof(double) * nq, cudaMemcpyHostToDevice,
+                            c->stream));
+    CTX_TRY(cudaMemcpyAsync(c->d_color_start, c->color_start.data(),
+                            sizeof(int) * c->color_start.size(), cudaMemcpyHostToDevice,
                             c->stream));
     CTX_TRY(cudaMemcpyAsync(c->d_color_elems, order.data(), sizeof(int) * order.size(),
                             cudaMemcpyHostToDevice, c->stream));
@@ -805,6 +808,9 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_cterm);
     dfree(c->d_geomf);
     dfree(c->d_color_elems);
+    dfree(c->d_color_start);
+    dfree(c->d_far_items);
+    dfree(c->d_far_pairs);
     dfree(c->d_pairs);
     dfree(c->d_counts);
     dfree(c->d_offsets);
@@ -877,8 +883,7 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
     cudaError_t e = cudaMemsetAsync(buf, 0, sizeof(double) * 4 * n, c->stream);
     if (e != cudaSuccess) rc = fail(TDBEM_ERR_CUDA, "memset: %s", cudaGetErrorString(e));
     for (size_t col = 0; rc == TDBEM_OK && col + 1 < c->color_start.size(); col++)
-        rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, 1 << 30, step, SEL_ALL, 0,
-                            out);
+        rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, 1 << 30, step, SEL_ALL, out);
     if (rc == TDBEM_OK && step == 1) {
         e = launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
                          c->d_geom, c->ph, c->d_cterm, c->stream);
@@ -937,7 +942,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         out.ld = c->D;
         for (int col = 0; col < ncol; col++) {
             const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_ALL,
-                                          0, out);
+                                          out);
             if (rc != TDBEM_OK) return rc;
         }
         const int pc = prof_begin(c, TDBEM_K_AUX);
@@ -972,12 +977,44 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         const bool split = c->ennd == 4;
         for (int col = 0; col < ncol; col++) {
             int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0,
-                                    split ? SEL_NEAR : SEL_ALL, 0, o32);
-            if (rc == TDBEM_OK && split)
-                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0, SEL_FAR, 1, o32);
+                                    split ? SEL_NEAR : SEL_ALL, o32);
             if (rc == TDBEM_OK)
-                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, 0, o64);
+                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, o64);
             if (rc != TDBEM_OK) return rc;
+        }
+        if (split) {
+            // far pairs: windows of every (node, element) pair, elements in colour order,
+            // then one row-local FP32 launch
+            const size_t np = (size_t)c->nnd * c->nel;
+            if (c->far_pairs_cap < np) {
+                dfree(c->d_far_pairs);
+                c->far_pairs_cap = 0;
+                CUDA_TRY(dalloc(&c->d_far_pairs, np));
+                c->far_pairs_cap = np;
+            }
+            const int pw = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
+                                        c->nnd, c->ph, ASM_LEVELS, last, c->M, 0, SEL_FAR,
+                                        c->d_far_pairs, nullptr, c->stream));
+            prof_end(c, pw, 0, 0);
+            const bool count = c->prof;  // the item count feeds the profile's byte/flop totals
+            if (count)
+                CUDA_TRY(cudaMemsetAsync(c->d_far_items, 0, sizeof(unsigned long long), c->stream));
+            const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
+            CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
+                                              c->d_color_start, ncol, c->nnd, c->nel, c->nq,
+                                              c->d_geomf, c->ph, last, c->d_far_pairs, o32,
+                                              count ? c->d_far_items : nullptr, c->stream));
+            prof_end(c, pe, 0, 0);
+            c->launches += 2;
+            if (count && pe >= 0) {
+                unsigned long long n = 0;
+                CUDA_TRY(cudaMemcpyAsync(&n, c->d_far_items, sizeof(n), cudaMemcpyDeviceToHost,
+                                         c->stream));
+                CUDA_TRY(cudaStreamSynchronize(c->stream));
+                c->prof_pending[pe].bytes = (double)n * 4 * 45 * 4.0 * 2;
+                c->prof_pending[pe].flops = (double)n * c->nq * c->nq * kFlopsPerItemPointF32;
+            }
         }
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,

@@ -159,9 +159,9 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
             NA_TRY(cudaMemcpyAsync(&last[1], counts + npairs - 1, sizeof(unsigned),
                                    cudaMemcpyDeviceToHost, s));
             NA_TRY(cudaStreamSynchronize(s));
-            NA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq, c->d_gx,
-                                         c->d_gw, c->d_geom, c->d_geomf, c->ph, ASM_STEP, step,
-                                         step, pairs, offsets, npairs, last[0] + last[1], out, 0,
+            NA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
+                                         c->d_gx, c->d_gw, c->d_geom, c->ph, ASM_STEP, step,
+                                         step, pairs, offsets, npairs, last[0] + last[1], out,
                                          s));
         }
     }

@@ -63,7 +63,7 @@ struct AsmOut {
 // Launch helpers (assemble.cu).
 // ennd: nodes per element (4 or 8).  8-node elements keep a wider geometry
 // table (kGeomStride8 doubles per Gauss point, no FP32 copy) and take the FP64
-// quadrature only (fp32_far must be 0).
+// quadrature only.
 cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int ennd, int nq,
                               const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s);
@@ -74,10 +74,19 @@ cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, c
 cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd,
                                   const int* elems, int nelem_color, int node_lo, int nq,
                                   const double* gx, const double* gw, const double* geom,
-                                  const float* geomf, const Phys& ph, int mode, int level_last,
-                                  int step_n, const PairInfo* pairs, const unsigned* offsets,
+                                  const Phys& ph, int mode, int level_last, int step_n,
+                                  const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  int fp32_far, cudaStream_t s);
+                                  cudaStream_t s);
+// Far (well-separated) items of every node in FP32, ASM_LEVELS, into the FP32 store:
+// one launch over (node, chunk of levels) blocks, colours walked inside each block.
+// pairs holds nnd x nel windows (SEL_FAR), elements in colour order; *nitems (if
+// not null) receives the item count.  4-node elements only.
+cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
+                                     const int* color_elems, const int* color_start, int ncolor,
+                                     int nnd, int nel, int nq, const float* geomf, const Phys& ph,
+                                     int level_last, const PairInfo* pairs, const AsmOut& out,
+                                     unsigned long long* nitems, cudaStream_t s);
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s);
@@ -308,6 +317,10 @@ struct tdbem_ctx {
     // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
     std::vector<int> color_start;
     int* d_color_elems = nullptr;
+    int* d_color_start = nullptr;    // color_start on the device
+    tdbem::PairInfo* d_far_pairs = nullptr;  // mixed: windows of all nnd x nel pairs (SEL_FAR)
+    size_t far_pairs_cap = 0;
+    unsigned long long* d_far_items = nullptr;  // far item count (profiling)
     // pair/item scratch
     tdbem::PairInfo* d_pairs = nullptr;
     unsigned* d_counts = nullptr;
