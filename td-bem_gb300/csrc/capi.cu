@@ -391,17 +391,50 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     for (int v = 0; v < ninv; v++) {
         if (!c->d_Hc64[v]) CUDA_TRY(dalloc(&c->d_Hc64[v], DD));
         if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
-        CUDA_TRY(launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
-                                  lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], s));
-        if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(D)));
-        const int pe = prof_begin(c, TDBEM_K_FACTOR);
+    }
+    if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(D)));
+    if (ninv == 2) {
+        // the second inverse on its own stream and scratch, from a second host thread:
+        // each inverse leaves most SMs idle during its pivot searches (one cluster of
+        // 16 CTAs), so the two overlap
+        if (!c->stream2) CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+        if (!c->d_inv_scratch32b)
+            CUDA_TRY(dalloc(&c->d_inv_scratch32b, inverse_scratch_elems(D)));
+        if (!c->d_perm2) CUDA_TRY(dalloc(&c->d_perm2, (size_t)D + 2 * kMaxPivotBlocks));
+        if (!c->d_status2) CUDA_TRY(dalloc(&c->d_status2, 1));
+        if (!c->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    }
+    const int pe = prof_begin(c, TDBEM_K_FACTOR);
+    struct Inv {
+        cudaError_t e = cudaSuccess;
         bool singular = false;
-        cudaError_t e = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, c->d_perm, c->d_status,
-                                   c->d_inv_scratch32, &c->launches, &singular, s);
-        prof_end(c, pe, 2.0 * 4 * DD, 2.0 * (double)D * D * D);
-        c->launches += 1;
-        CUDA_TRY(e);
-        if (singular)
+        long long launches = 0;
+    } inv[2];
+    auto invert = [&](int v, cudaStream_t st, int* perm, int* status, float* scratch) {
+        inv[v].e = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
+                                    lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
+        if (inv[v].e == cudaSuccess)
+            inv[v].e = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
+                                  &inv[v].launches, &inv[v].singular, st);
+        inv[v].launches += 1;
+    };
+    if (ninv == 2) {
+        CUDA_TRY(cudaEventRecord(c->ev_fork, s));  // the FP64 levels 0/1 are ready
+        CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+        std::thread second([&] {
+            cudaSetDevice(c->device);
+            invert(1, c->stream2, c->d_perm2, c->d_status2, c->d_inv_scratch32b);
+        });
+        invert(0, s, c->d_perm, c->d_status, c->d_inv_scratch32);
+        second.join();  // both inverses end with a synchronisation of their stream
+    } else {
+        invert(0, s, c->d_perm, c->d_status, c->d_inv_scratch32);
+    }
+    prof_end(c, pe, ninv * 2.0 * 4 * DD, ninv * 2.0 * (double)D * D * D);
+    for (int v = 0; v < ninv; v++) {
+        c->launches += inv[v].launches;
+        CUDA_TRY(inv[v].e);
+        if (inv[v].singular)
             return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
     }
     if (ninv == 1) {
@@ -452,12 +485,14 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, ldw,
                                         c->d_Wt_old, c->d_Wu_old, s));
             const int nch = mixed_chunks(nlev, D);
+            int nparts = 0;
             const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
             CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
-                                     c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch, s));
+                                     c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
+                                     mixed_ksplit(nch, D, M + 1), &nparts, s));
             prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
                      nlev * 4.0 * nb * (double)DD);
-            CUDA_TRY(launch_reduce_cols(c->d_pmix, nch, nb, D, nullptr, c->d_Yold, s));
+            CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, nb, D, nullptr, c->d_Yold, s));
             c->launches += 3;
         } else {
             CUDA_TRY(cudaMemsetAsync(c->d_Yold, 0, sizeof(double) * nb * D, s));
@@ -472,12 +507,14 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                                         c->d_load_t, c->d_load_u, ldw, c->d_Wt_new, c->d_Wu_new,
                                         s));
             const int nch = mixed_chunks(L + 1, D);
+            int nparts = 0;
             int pe = prof_begin(c, TDBEM_K_CONV);
             CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, L, 1, c->d_Wt_new,
-                                     c->d_Wu_new, ldw, c->d_pmix, nch, s));
+                                     c->d_Wu_new, ldw, c->d_pmix, nch,
+                                     mixed_ksplit(nch, D, (M + 1) * nb), &nparts, s));
             prof_end(c, pe, (L + 1) * 2.0 * (double)lstride * 4, (L + 1) * 4.0 * (double)DD);
             pe = prof_begin(c, TDBEM_K_SOLVE);
-            CUDA_TRY(launch_reduce_cols(c->d_pmix, nch, 1, D, c->d_Yold + (size_t)j * D,
+            CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, 1, D, c->d_Yold + (size_t)j * D,
                                         c->d_rhs, s));
             const int v = st == 1 ? 0 : 1;
             // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
@@ -830,6 +867,11 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_x);
     dfree(c->d_perm);
     dfree(c->d_status);
+    dfree(c->d_inv_scratch32b);
+    dfree(c->d_perm2);
+    dfree(c->d_status2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TDBEM_OK;

@@ -453,11 +453,7 @@ constexpr size_t kClusterPanelBytes = 200 * 1024;  // panel rows per CTA of a cl
 
 // Whether a cluster of cs CTAs of the pivot kernel can be resident on this device
 // (checked once per size; 16 needs the non-portable cluster size).
-bool cluster_ok(int cs) {
-    static int ok[2] = {-1, -1};  // cluster sizes 8 and 16
-    int& v = ok[cs == 16 ? 1 : 0];
-    if (v >= 0) return v == 1;
-    v = 0;
+bool cluster_probe(int cs) {
     const void* fn8 = (const void*)k_panel_pivots_cluster<float, 64>;
     const void* fn16 = (const void*)k_panel_pivots_cluster<double, 16>;
     for (const void* fn : {fn8, fn16}) {
@@ -485,8 +481,15 @@ bool cluster_ok(int cs) {
             return false;
         }
     }
-    v = 1;
     return true;
+}
+
+// Both sizes probed once, before any caller sees an answer (host threads invert
+// concurrently: a half-made answer would send one of them to another kernel).
+bool cluster_ok(int cs) {
+    static const bool ok8 = cluster_probe(8);
+    static const bool ok16 = cluster_probe(16);
+    return cs == 16 ? ok16 : ok8;
 }
 
 // The pivot kernels' dynamic shared-memory limit, raised once per kernel to the

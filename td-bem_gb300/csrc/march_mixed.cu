@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
                                                   int ld, int D, int f_lo, int f_hi,
                                                   int per_chunk, const float* __restrict__ Wt,
                                                   const float* __restrict__ Wu, int ldw,
-                                                  double* __restrict__ partial) {
+                                                  int kspan, double* __restrict__ partial) {
     __shared__ float4 sw[2][NB][kKC / 4];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * kRows + warp * kRowsPerWarp;
@@ -53,7 +53,8 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
         const float* Hf = H + (size_t)f * lstride;
         const float4* wt = reinterpret_cast<const float4*>(Wt + (size_t)f * NB * ldw);
         const float4* wu = reinterpret_cast<const float4*>(Wu + (size_t)f * NB * ldw);
-        for (int k0 = 0; k0 < ld; k0 += kKC) {
+        const int kbeg = blockIdx.z * kspan, kend = min(ld, kbeg + kspan);
+        for (int k0 = kbeg; k0 < kend; k0 += kKC) {
             __syncthreads();
             for (int i = threadIdx.x; i < NB * (kKC / 4); i += blockDim.x) {
                 const int j = i / (kKC / 4), kk = i % (kKC / 4);
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
 #pragma unroll 2
             for (int kk = lane; kk < kKC / 4; kk += 32) {
                 const int k = k0 + 4 * kk;
-                if (k >= ld) break;
+                if (k >= kend) break;
                 // all rows' G/H segments first, then each W column once from shared
                 // memory for the 4 rows (one LDS.128 pair per column, not per row)
                 float4 g[kRowsPerWarp], h[kRowsPerWarp];
@@ -92,7 +93,8 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0 && row0 + r < D)
-                partial[((size_t)blockIdx.y * NB + j) * D + row0 + r] = v;
+                partial[((size_t)(blockIdx.z * gridDim.y + blockIdx.y) * NB + j) * D + row0 + r] =
+                    v;
         }
 }
 
@@ -250,22 +252,36 @@ int mixed_chunks(int nlev, int D) {
     return std::max(1, std::min(chunks, nlev));
 }
 
+// Column splits: enough blocks for a full wave (8 per SM) when few levels leave
+// the row tiles x level chunks grid short of it; at most cap partial chunks.
+int mixed_ksplit(int nchunks, int D, int cap) {
+    const int tiles = (D + kRows - 1) / kRows;
+    const int want = (8 * 152 + tiles * nchunks - 1) / (tiles * nchunks);
+    const int ncol = (mixed_ld(D) + kKC - 1) / kKC;
+    return std::max(1, std::min(std::min(want, ncol), cap / std::max(1, nchunks)));
+}
+
 cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int ld, int D,
                             int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
-                            int ldw, double* partial, int nchunks, cudaStream_t s) {
+                            int ldw, double* partial, int nchunks, int ksplit, int* nparts,
+                            cudaStream_t s) {
     const int nlev = f_hi - f_lo + 1;
     const int per_chunk = (nlev + nchunks - 1) / nchunks;
-    dim3 grid((D + kRows - 1) / kRows, nchunks);
+    // column span of a split: a multiple of the staged chunk, covering ld
+    const int nkc = (ld + kKC - 1) / kKC;
+    const int kspan = (nkc + ksplit - 1) / ksplit * kKC;
+    dim3 grid((D + kRows - 1) / kRows, nchunks, (nkc * kKC + kspan - 1) / kspan);
+    *nparts = nchunks * (int)grid.z;  // partial sums the reduction adds
     // W for level f sits at W + (f - f_lo) * nb * ldw: pass shifted base pointers
     const float* wt = Wt - (size_t)f_lo * nb * ldw;
     const float* wu = Wu - (size_t)f_lo * nb * ldw;
     switch (nb) {
-    case 1: k_conv_f32<1><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
-    case 4: k_conv_f32<4><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
-    case 6: k_conv_f32<6><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
-    case 8: k_conv_f32<8><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
-    case 12: k_conv_f32<12><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
-    case 16: k_conv_f32<16><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, partial); break;
+    case 1: k_conv_f32<1><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 4: k_conv_f32<4><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 6: k_conv_f32<6><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 8: k_conv_f32<8><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 12: k_conv_f32<12><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 16: k_conv_f32<16><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

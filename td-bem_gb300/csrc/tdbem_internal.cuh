@@ -248,9 +248,13 @@ void note_error(const char* msg);
 int mixed_ldw(int D);
 int mixed_ld(int D);
 int mixed_chunks(int nlev, int D);
+// Column splits for a convolution of nchunks level chunks, at most cap partials.
+int mixed_ksplit(int nchunks, int D, int cap);
+// *nparts receives the number of partial sums written (level chunks x column splits).
 cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int ld, int D,
                             int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
-                            int ldw, double* partial, int nchunks, cudaStream_t s);
+                            int ldw, double* partial, int nchunks, int ksplit, int* nparts,
+                            cudaStream_t s);
 cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
                                int nlev, double a1, double a2, double a3, int ldw, float* Wt,
                                float* Wu, cudaStream_t s);
@@ -396,6 +400,12 @@ struct tdbem_ctx {
     unsigned char* d_is_fbc = nullptr;
     double* d_inv_scratch = nullptr;  // blocked inverse scratch (FP64)
     float* d_inv_scratch32 = nullptr;
+    // mixed: the second FP32 inverse's stream and scratch (the two run concurrently)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr;
+    float* d_inv_scratch32b = nullptr;
+    int* d_perm2 = nullptr;
+    int* d_status2 = nullptr;
     double* d_load_t = nullptr;
     double* d_load_u = nullptr;
     double* d_Wt = nullptr;
