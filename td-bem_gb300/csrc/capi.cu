@@ -158,6 +158,7 @@ void color_elements(const std::vector<int>& ien, int nel, int ennd, int nnd,
 }
 
 void free_levels(tdbem_ctx* c) {
+    c->inv_valid = false;
     dfree(c->d_G);
     dfree(c->d_H);
     dfree(c->d_Gf);
@@ -194,9 +195,10 @@ void free_batch(tdbem_ctx* c) {
 void free_march(tdbem_ctx* c) {
     dfree(c->d_u);
     dfree(c->d_t);
+    // one LHS: slot 1 aliases slot 0 (dropped before slot 0 is freed)
+    if (c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
+    if (c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
     for (int v = 0; v < 2; v++) {
-        if (v == 1 && c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
-        if (v == 1 && c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
         dfree(c->d_inv32[v]);
         dfree(c->d_Hc64[v]);
     }
@@ -227,22 +229,28 @@ constexpr double kFlopsPerItemPoint = 398.0;
 // differences 176, scalars 40, kernels 65, accumulation 124.
 constexpr double kFlopsPerItemPointF32 = 425.0;
 
-int prof_begin(tdbem_ctx* c, int cls) {
+int prof_begin_on(tdbem_ctx* c, int cls, cudaStream_t s) {
     if (!c->prof) return -1;
     tdbem_ctx::ProfEvent ev{cls, nullptr, nullptr, 0, 0};
     cudaEventCreate(&ev.a);
     cudaEventCreate(&ev.b);
-    cudaEventRecord(ev.a, c->stream);
+    cudaEventRecord(ev.a, s);
     c->prof_pending.push_back(ev);
     return (int)c->prof_pending.size() - 1;
 }
 
-void prof_end(tdbem_ctx* c, int idx, double bytes, double flops) {
+int prof_begin(tdbem_ctx* c, int cls) { return prof_begin_on(c, cls, c->stream); }
+
+void prof_end_on(tdbem_ctx* c, int idx, double bytes, double flops, cudaStream_t s) {
     if (idx < 0) return;
     auto& ev = c->prof_pending[idx];
-    cudaEventRecord(ev.b, c->stream);
+    cudaEventRecord(ev.b, s);
     ev.bytes = bytes;
     ev.flops = flops;
+}
+
+void prof_end(tdbem_ctx* c, int idx, double bytes, double flops) {
+    prof_end_on(c, idx, bytes, flops, c->stream);
 }
 
 // Resolve pending event pairs (the stream must have been synchronised).
@@ -375,15 +383,21 @@ int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const 
 }
 
 // FP64 column-exchanged LHS and its FP32 inverse for each distinct LHS of the
-// mixed form (step 2 and steps >= 3); c->timings[1] gets the time taken.
-int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
-    const int D = c->D;
-    const size_t DD = (size_t)D * D;
-    cudaStream_t s = c->stream;
-    EventTimer tf;
-    tf.start(s);
+// mixed form (step 2 and steps >= 3).  The inverses depend on alpha, the UBC dofs
+// (the column exchange) and levels 0/1; they are kept with that key and reused
+// while it holds (an assembly may have made them already, next to its far field).
+int mixed_ninv(int numstep, const double lhs_c[2][2]) {
     const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
+    return (numstep >= 3 && !same) ? 2 : 1;
+}
+
+bool inverses_current(const tdbem_ctx* c, int ninv) {
+    return c->inv_valid && c->inv_n == ninv && c->inv_a1 == c->a1 && c->inv_a2 == c->a2 &&
+           c->inv_ubc == c->ubc;
+}
+
+int prepare_inverses(tdbem_ctx* c, int ninv) {
+    const size_t DD = (size_t)c->D * c->D;
     for (int v = 0; v < 2; v++) {
         if (c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
         if (c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
@@ -392,49 +406,63 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         if (!c->d_Hc64[v]) CUDA_TRY(dalloc(&c->d_Hc64[v], DD));
         if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
     }
-    if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(D)));
+    if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(c->D)));
+    for (cudaStream_t* st : {&c->stream2, &c->stream3})
+        if (!*st) CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+    if (!c->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    if (!c->ev_fork2) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming));
     if (ninv == 2) {
-        // the second inverse on its own stream and scratch, from a second host thread:
-        // each inverse leaves most SMs idle during its pivot searches (one cluster of
-        // 16 CTAs), so the two overlap
-        if (!c->stream2) CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
         if (!c->d_inv_scratch32b)
-            CUDA_TRY(dalloc(&c->d_inv_scratch32b, inverse_scratch_elems(D)));
-        if (!c->d_perm2) CUDA_TRY(dalloc(&c->d_perm2, (size_t)D + 2 * kMaxPivotBlocks));
+            CUDA_TRY(dalloc(&c->d_inv_scratch32b, inverse_scratch_elems(c->D)));
+        if (!c->d_perm2) CUDA_TRY(dalloc(&c->d_perm2, (size_t)c->D + 2 * kMaxPivotBlocks));
         if (!c->d_status2) CUDA_TRY(dalloc(&c->d_status2, 1));
-        if (!c->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     }
-    const int pe = prof_begin(c, TDBEM_K_FACTOR);
-    struct Inv {
-        cudaError_t e = cudaSuccess;
-        bool singular = false;
-        long long launches = 0;
-    } inv[2];
+    return TDBEM_OK;
+}
+
+struct InvResult {
+    cudaError_t e[2] = {cudaSuccess, cudaSuccess};
+    bool singular[2] = {false, false};
+    long long launches[2] = {0, 0};
+};
+
+// The inverses on streams s0 and s1 (s1 after s0's prior work): the second from a
+// second host thread, as each inverse leaves most SMs idle during its pivot
+// searches (one cluster of 16 CTAs) and the two overlap.  Touches no profiling
+// state or shared counter, so it may run on a helper thread; returns after both
+// streams have finished.
+void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t s0,
+                  cudaStream_t s1, InvResult& r) {
+    const int D = c->D;
+    const size_t DD = (size_t)D * D;
     auto invert = [&](int v, cudaStream_t st, int* perm, int* status, float* scratch) {
-        inv[v].e = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
-                                    lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
-        if (inv[v].e == cudaSuccess)
-            inv[v].e = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
-                                  &inv[v].launches, &inv[v].singular, st);
-        inv[v].launches += 1;
+        r.e[v] = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
+                                  lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
+        if (r.e[v] == cudaSuccess)
+            r.e[v] = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
+                                &r.launches[v], &r.singular[v], st);
+        r.launches[v] += 1;
     };
     if (ninv == 2) {
-        CUDA_TRY(cudaEventRecord(c->ev_fork, s));  // the FP64 levels 0/1 are ready
-        CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+        r.e[1] = cudaEventRecord(c->ev_fork2, s0);  // levels 0/1 and the maps are ready
+        if (r.e[1] == cudaSuccess) r.e[1] = cudaStreamWaitEvent(s1, c->ev_fork2, 0);
+        if (r.e[1] != cudaSuccess) return;
         std::thread second([&] {
             cudaSetDevice(c->device);
-            invert(1, c->stream2, c->d_perm2, c->d_status2, c->d_inv_scratch32b);
+            invert(1, s1, c->d_perm2, c->d_status2, c->d_inv_scratch32b);
         });
-        invert(0, s, c->d_perm, c->d_status, c->d_inv_scratch32);
+        invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
         second.join();  // both inverses end with a synchronisation of their stream
     } else {
-        invert(0, s, c->d_perm, c->d_status, c->d_inv_scratch32);
+        invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
     }
-    prof_end(c, pe, ninv * 2.0 * 4 * DD, ninv * 2.0 * (double)D * D * D);
+}
+
+int finish_inverses(tdbem_ctx* c, int ninv, const InvResult& r) {
     for (int v = 0; v < ninv; v++) {
-        c->launches += inv[v].launches;
-        CUDA_TRY(inv[v].e);
-        if (inv[v].singular)
+        c->launches += r.launches[v];
+        CUDA_TRY(r.e[v]);
+        if (r.singular[v])
             return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
     }
     if (ninv == 1) {
@@ -443,8 +471,32 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         c->d_inv32[1] = c->d_inv32[0];
         c->d_Hc64[1] = c->d_Hc64[0];
     }
-    c->timings[1] = tf.stop_ms(s);
+    c->inv_valid = true;
+    c->inv_n = ninv;
+    c->inv_a1 = c->a1;
+    c->inv_a2 = c->a2;
+    c->inv_ubc = c->ubc;
     return TDBEM_OK;
+}
+
+// The inverses for a march of numstep steps, unless current; c->timings[1] gets
+// the time taken (left as it is when they are reused).
+int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
+    const int ninv = mixed_ninv(numstep, lhs_c);
+    if (inverses_current(c, ninv)) return TDBEM_OK;
+    const int rc = prepare_inverses(c, ninv);
+    if (rc != TDBEM_OK) return rc;
+    cudaStream_t s = c->stream;
+    EventTimer tf;
+    tf.start(s);
+    const int pe = prof_begin(c, TDBEM_K_FACTOR);
+    InvResult r;
+    run_inverses(c, ninv, lhs_c, s, c->stream2, r);
+    const double DD = (double)c->D * c->D;
+    prof_end(c, pe, ninv * 2.0 * 4 * DD, ninv * 2.0 * DD * c->D);
+    const int rc2 = finish_inverses(c, ninv, r);
+    c->timings[1] = tf.stop_ms(s);
+    return rc2;
 }
 
 // Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
@@ -837,6 +889,7 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     }
     free_levels(c);
     free_march(c);
+    c->inv_valid = false;
     dfree(c->d_coords);
     dfree(c->d_ien);
     dfree(c->d_gx);
@@ -871,6 +924,8 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_perm2);
     dfree(c->d_status2);
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_fork2) cudaEventDestroy(c->ev_fork2);
+    if (c->stream3) cudaStreamDestroy(c->stream3);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -968,6 +1023,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         c->level_precision = precision;
         c->ldf = ldf;
     }
+    c->inv_valid = false;  // levels 0/1 change
     EventTimer tm;
     tm.start(c->stream);
     const int last = std::min(c->M, nsteps);
@@ -1017,11 +1073,53 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         // 8-node elements: every pair through the FP64 quadrature (the FP32 far form
         // is written for 4-node elements)
         const bool split = c->ennd == 4;
+        // FP64 levels 0/1 first: with the C term they are final, and the inverses can
+        // start next to the rest of the assembly
         for (int col = 0; col < ncol; col++) {
-            int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0,
-                                    split ? SEL_NEAR : SEL_ALL, o32);
-            if (rc == TDBEM_OK)
-                rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, o64);
+            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, o64);
+            if (rc != TDBEM_OK) return rc;
+        }
+        // the C term (the FP32 store takes it after the far field)
+        const int pc = prof_begin(c, TDBEM_K_AUX);
+        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
+                              c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream));
+        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
+                                    c->stream));
+        prof_end(c, pc, 0, 0);
+        c->launches += 2;
+        // The march's FP32 inverses need only levels 0/1, alpha and the UBC dofs: made
+        // here on the side streams while the near and far fields run (the march reuses
+        // them while alpha, the UBC dofs and the levels stay as they are).
+        const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+        const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+        const int ninv = mixed_ninv(nsteps, lhs_c);
+        InvResult ir;  // written by the helper thread: declared before its joiner
+        EventTimer tf;
+        std::thread inv_thread;
+        struct Joiner {
+            std::thread& t;
+            ~Joiner() {
+                if (t.joinable()) t.join();
+            }
+        } joiner{inv_thread};
+        int pf = -1;
+        if (split) {
+            int rc = upload_bc(c);
+            if (rc == TDBEM_OK) rc = prepare_inverses(c, ninv);
+            if (rc != TDBEM_OK) return rc;
+            CUDA_TRY(cudaEventRecord(c->ev_fork, c->stream));
+            CUDA_TRY(cudaStreamWaitEvent(c->stream2, c->ev_fork, 0));
+            tf.start(c->stream2);
+            pf = prof_begin_on(c, TDBEM_K_FACTOR, c->stream2);
+            inv_thread = std::thread([&] {
+                cudaSetDevice(c->device);
+                run_inverses(c, ninv, lhs_c, c->stream2, c->stream3, ir);
+            });
+        }
+        // near pairs (FP64 quadrature into the FP32 store), colour by colour
+        for (int col = 0; col < ncol; col++) {
+            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0,
+                                          split ? SEL_NEAR : SEL_ALL, o32);
             if (rc != TDBEM_OK) return rc;
         }
         if (split) {
@@ -1058,15 +1156,17 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                 c->prof_pending[pe].flops = (double)n * c->nq * c->nq * kFlopsPerItemPointF32;
             }
         }
-        const int pc = prof_begin(c, TDBEM_K_AUX);
-        CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                              c->d_geom, c->ph, c->d_cterm, c->stream));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o32,
                                     c->stream));
-        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
-                                    c->stream));
-        prof_end(c, pc, 0, 0);
-        c->launches += 3;
+        c->launches += 1;
+        if (split) {
+            inv_thread.join();  // its streams are synchronised when it returns
+            const double DD = (double)D * D;
+            prof_end_on(c, pf, ninv * 2.0 * 4 * DD, ninv * 2.0 * DD * D, c->stream2);
+            c->timings[1] = tf.stop_ms(c->stream2);
+            const int rc = finish_inverses(c, ninv, ir);
+            if (rc != TDBEM_OK) return rc;
+        }
     }
     c->timings[0] = tm.stop_ms(c->stream);
     CUDA_TRY(cudaGetLastError());
@@ -1501,6 +1601,7 @@ int tdbem_export_levels(tdbem_ctx* c, const char* path) {
 
 int tdbem_import_levels(tdbem_ctx* c, const char* path) {
     if (!c || !path) return fail(TDBEM_ERR_ARG, "null argument");
+    c->inv_valid = false;
     FILE* f = std::fopen(path, "rb");
     if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s", path);
     CkptHeader h{};

@@ -400,9 +400,17 @@ struct tdbem_ctx {
     unsigned char* d_is_fbc = nullptr;
     double* d_inv_scratch = nullptr;  // blocked inverse scratch (FP64)
     float* d_inv_scratch32 = nullptr;
-    // mixed: the second FP32 inverse's stream and scratch (the two run concurrently)
+    // mixed: side streams of the FP32 inverses (the two run concurrently, and next to
+    // the far-field assembly when it makes them), the second inverse's scratch, and
+    // the key of the inverses held (alpha, UBC dofs, count; levels 0/1 unchanged)
     cudaStream_t stream2 = nullptr;
+    cudaStream_t stream3 = nullptr;
     cudaEvent_t ev_fork = nullptr;
+    cudaEvent_t ev_fork2 = nullptr;
+    bool inv_valid = false;
+    int inv_n = 0;
+    double inv_a1 = 0, inv_a2 = 0;
+    std::vector<int> inv_ubc;
     float* d_inv_scratch32b = nullptr;
     int* d_perm2 = nullptr;
     int* d_status2 = nullptr;
