@@ -17,9 +17,17 @@
 // After the last panel the columns are permuted back (reverse order of the
 // row swaps).  Step 5 is a rank-bw update with bw-deep dot products, so the
 // whole inversion is 2 n^3 flops in GEMM form.
+//
+// The FP32 inverse (a preconditioner that FP64 refinement corrects) may restrict
+// step 1's search to the panel's diagonal block (k_block_pivots, one CTA: no
+// cluster-wide reduction per column).  On the boundary-element LHS the column
+// maximum lies in that block (diagonal dominance), so the pivots are the same; a
+// zero pivot in the block, or a probe ||A (X v) - v|| / ||v|| above 1e-2 of the
+// finished inverse, sends the inversion back to the full search.
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "tdbem_internal.cuh"
@@ -443,6 +451,99 @@ __global__ void k_permute_cols_t(T* __restrict__ A, int n, const int* __restrict
     }
 }
 
+// Pivot sequence of the panel with the search restricted to its diagonal block:
+// LU with partial pivoting (largest magnitude, lowest row on ties) of the bw x bw
+// block A[k0:k0+bw, k0:k0+bw] in shared memory, one CTA.  Writes perm[k0 + c] as
+// the tall-panel kernels do; a zero pivot sets *status = 2 (the caller retries
+// with the full search).
+template <typename T, int BW>
+__global__ void __launch_bounds__(256) k_block_pivots(const T* __restrict__ A, int n, int k0,
+                                                      int bw, int* __restrict__ perm,
+                                                      int* __restrict__ status) {
+    __shared__ T ws[BW][BW + 1];
+    __shared__ int s_p;
+    for (int idx = threadIdx.x; idx < BW * BW; idx += blockDim.x) {
+        const int r = idx / BW, c = idx % BW;
+        ws[r][c] = (r < bw && c < bw) ? A[(size_t)(k0 + r) * n + k0 + c] : T(0);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int c = 0; c < bw; c++) {
+        if (threadIdx.x < 32) {  // warp 0: argmax of |ws[r][c]|, r in [c, bw)
+            T best = T(-1);
+            int bi = bw;
+            for (int r = c + lane; r < bw; r += 32) {
+                const T v = absv(ws[r][c]);
+                if (v > best) { best = v; bi = r; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const T v2 = __shfl_xor_sync(0xffffffffu, best, o);
+                const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (v2 > best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
+            }
+            if (lane == 0) s_p = (bi < bw && best != T(0)) ? bi : -1;
+        }
+        __syncthreads();
+        const int p = s_p;
+        if (p < 0) {
+            if (threadIdx.x == 0) *status = 2;
+            return;
+        }
+        if (p != c)
+            for (int j = threadIdx.x; j < BW; j += blockDim.x) {
+                const T t = ws[c][j];
+                ws[c][j] = ws[p][j];
+                ws[p][j] = t;
+            }
+        if (threadIdx.x == 0) perm[k0 + c] = k0 + p;
+        __syncthreads();
+        const T inv = T(1) / ws[c][c];
+        const int nr = bw - c - 1, nc = bw - c;  // rows c+1.., columns c.. (column c -> l)
+        for (int idx = threadIdx.x; idx < nr * nc; idx += blockDim.x) {
+            const int r = c + 1 + idx / nc, j = c + idx % nc;
+            const T l = ws[r][c] * inv;
+            if (j > c) ws[r][j] -= l * ws[c][j];
+        }
+        __syncthreads();
+        for (int r = c + 1 + threadIdx.x; r < bw; r += blockDim.x) ws[r][c] *= inv;
+        __syncthreads();
+    }
+}
+
+// Probe of an FP32 inverse X of A64: y = X v, then err = max_i |(A64 y)_i - v_i|
+// (v_i = (i mod 13) - 6.5, max |v| = 6.5), as the float bits of a non-negative
+// value (integer max preserves the order).  Warp per row.
+__device__ __forceinline__ double probe_v(int i) { return (double)(i % 13) - 6.5; }
+
+__global__ void __launch_bounds__(256) k_probe_xv(const float* __restrict__ X, int n,
+                                                  double* __restrict__ y) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const float* row = X + (size_t)w * n;
+    double acc = 0;
+    for (int j = lane; j < n; j += 32) acc += (double)row[j] * probe_v(j);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) y[w] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_probe_ay(const double* __restrict__ A, int n,
+                                                  const double* __restrict__ y,
+                                                  unsigned* __restrict__ err_bits) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const double* row = A + (size_t)w * n;
+    double acc = 0;
+    for (int j = lane; j < n; j += 32) acc += row[j] * y[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+        const float e = (float)fabs(acc - probe_v(w));
+        atomicMax(err_bits, __float_as_uint(e == e ? e : 3.0e38f));  // NaN counts as huge
+    }
+}
+
 __global__ void k_cast_f64_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
@@ -512,7 +613,7 @@ cudaError_t pivot_attributes() {
 
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
-                           bool* singular, cudaStream_t s) {
+                           bool* singular, cudaStream_t s, bool restricted = false) {
     *singular = false;
     {
         const cudaError_t ea = pivot_attributes<T, BW>();
@@ -536,9 +637,14 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         if (smem > kClusterPanelBytes) return cudaErrorInvalidConfiguration;  // panel too tall
         int kk0 = k0, kbw = bw, kn = n;
         const T* cA = A;
-        // the panel in one cluster's distributed shared memory when it fits
         bool done = false;
+        if (restricted) {
+            k_block_pivots<T, BW><<<1, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
+            done = true;
+        }
+        // the panel in one cluster's distributed shared memory when it fits
         for (int cs : {16, 8}) {
+            if (done) break;
             const int crpb = (rows + cs - 1) / cs;
             const size_t csmem = (size_t)crpb * BW * sizeof(T);
             if (csmem > kClusterPanelBytes || !cluster_ok(cs)) continue;
@@ -613,6 +719,32 @@ cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scrat
 
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s) {
+    k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
+    *nlaunch += 1;
+    // first with the pivot search in the panels' diagonal blocks, then checked
+    cudaError_t e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular,
+                                              s, true);
+    if (e != cudaSuccess) return e;
+    bool good = false;
+    if (!*singular) {
+        // the probe's y (n doubles) and error word fit in the panel scratch rows
+        double* y = reinterpret_cast<double*>(scratch);
+        unsigned* err = reinterpret_cast<unsigned*>(y + n);
+        e = cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+        if (e != cudaSuccess) return e;
+        const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+        k_probe_xv<<<g, 256, 0, s>>>(A, n, y);
+        k_probe_ay<<<g, 256, 0, s>>>(A64, n, y, err);
+        *nlaunch += 2;
+        unsigned bits = 0;
+        e = cudaMemcpyAsync(&bits, err, sizeof(bits), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return e;
+        float ef;
+        std::memcpy(&ef, &bits, sizeof(ef));
+        good = ef <= 1e-2f * 6.5f;
+    }
+    if (good) return cudaSuccess;
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
     return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s);
