@@ -465,7 +465,9 @@ def run_ours(args, dist):
     peaks, peak_kind = measured_peaks()
     peaks.update(measure_fp_peaks(torch))
     traffic = ncu_traffic()
-    dom = max(stats, key=lambda k: stats[k]["ms"])
+    # the dominant single kernel: "factor" (the inverses, ~440 kernels each, two running
+    # side by side next to the assembly) and "aux" are composites, not one kernel
+    dom = max((k for k in stats if k not in ("factor", "aux")), key=lambda k: stats[k]["ms"])
     st = stats[dom]
     if dom == "conv_batch":
         # split-BF16 GEMM: 3 BF16 MMA products per useful FP32 product
@@ -496,7 +498,7 @@ def run_ours(args, dist):
             else "fp64_tflops"
         fp64 = peaks.get(key)
         roof = {"bound": "fp32" if key == "fp32_tflops" else "fp64",
-                "kernel": {"assemble": "k_assemble_items", "assemble_f32": "k_assemble_far_f32",
+                "kernel": {"assemble": "k_assemble_items", "assemble_f32": "k_assemble_far_rows",
                            "factor": "blocked Gauss-Jordan", "solve": "solve"}.get(dom, dom),
                 "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                 "frac": (achieved / fp64) if fp64 else None,
