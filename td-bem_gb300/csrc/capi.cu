@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <new>
 #include <string>
@@ -204,8 +205,6 @@ void free_march(tdbem_ctx* c) {
     }
     dfree(c->d_Wt_old);
     dfree(c->d_Wu_old);
-    dfree(c->d_Wt_new);
-    dfree(c->d_Wu_new);
     dfree(c->d_Yold);
     dfree(c->d_pmix);
     dfree(c->d_res);
@@ -510,8 +509,6 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     if (!c->d_Wt_old) {
         CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
         CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
-        CUDA_TRY(dalloc(&c->d_Wt_new, (size_t)(M + 1) * ldw));
-        CUDA_TRY(dalloc(&c->d_Wu_new, (size_t)(M + 1) * ldw));
         CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
         CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
         CUDA_TRY(dalloc(&c->d_res, D));
@@ -525,62 +522,93 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     const size_t lstride = (size_t)D * c->ldf;
     const int last_s = numstep - 1;  // solve steps 1..numstep-1
     const std::vector<const void*> ptrs = {
-        c->d_u,      c->d_t,      c->d_Gf,       c->d_Hf,       c->d_inv32[0], c->d_inv32[1],
-        c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old, c->d_Wu_old,   c->d_Wt_new,   c->d_Wu_new,
-        c->d_Yold,   c->d_pmix,   c->d_rhs,      c->d_x,        c->d_res,      c->d_dx,
-        c->d_load_t, c->d_load_u, c->d_is_ubc,   c->d_ubc_map,  c->d_is_fbc,   c->d_fbc_map};
-    const int lrc = run_march_loop(c, 1, numstep, ptrs, [&]() -> int {
-    for (int S = 1; S <= last_s; S += nb) {
-        const int nbe = std::min(nb, last_s - S + 1);
-        if (S > 1) {
-            const int nlev = std::min(M, S + nbe - 1) + 1;
-            CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, ldw,
-                                        c->d_Wt_old, c->d_Wu_old, s));
-            const int nch = mixed_chunks(nlev, D);
-            int nparts = 0;
-            const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
-            CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
-                                     c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
-                                     mixed_ksplit(nch, D, M + 1), &nparts, s));
-            prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
-                     nlev * 4.0 * nb * (double)DD);
-            CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, nb, D, nullptr, c->d_Yold, s));
-            c->launches += 3;
-        } else {
-            CUDA_TRY(cudaMemsetAsync(c->d_Yold, 0, sizeof(double) * nb * D, s));
-        }
+        c->d_u,       c->d_t,       c->d_Gf,      c->d_Hf,      c->d_inv32[0], c->d_inv32[1],
+        c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old,  c->d_Wu_old,  c->d_Yold,     c->d_pmix,
+        c->d_x,       c->d_res,     c->d_dx,      c->d_load_t,  c->d_load_u,   c->d_is_ubc,
+        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map};
+    // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
+    // Old pass: history before the block and the steps' known-load terms.
+    auto old_pass = [&](int S, int nbe) -> int {
+        const int nlev = (S > 1 ? std::min(M, S + nbe - 1) : std::min(M, 1)) + 1;
+        BlockLoads bl{};
+        bl.nload = nbe;
+        bl.load_t = c->d_load_t;
+        bl.load_u = c->d_load_u;
         for (int j = 0; j < nbe; j++) {
             const int st = S + j;
-            const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
-            const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-            const double amp = c->amp.empty() ? 1.0 : c->amp[st];
-            const int L = std::min(M, std::max(1, st + 1 - S));
-            CUDA_TRY(launch_build_w_new(c->d_u, c->d_t, D, st, S, L + 1, a1, a2, a3, c0, c1, amp,
-                                        c->d_load_t, c->d_load_u, ldw, c->d_Wt_new, c->d_Wu_new,
-                                        s));
-            const int nch = mixed_chunks(L + 1, D);
-            int nparts = 0;
-            int pe = prof_begin(c, TDBEM_K_CONV);
-            CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, L, 1, c->d_Wt_new,
-                                     c->d_Wu_new, ldw, c->d_pmix, nch,
-                                     mixed_ksplit(nch, D, (M + 1) * nb), &nparts, s));
-            prof_end(c, pe, (L + 1) * 2.0 * (double)lstride * 4, (L + 1) * 4.0 * (double)DD);
-            pe = prof_begin(c, TDBEM_K_SOLVE);
-            CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, 1, D, c->d_Yold + (size_t)j * D,
-                                        c->d_rhs, s));
-            const int v = st == 1 ? 0 : 1;
-            // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
-            CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_rhs, c->d_x,
-                                        c->d_res, reinterpret_cast<float*>(c->d_dx), c->n_refine,
-                                        s));
-            CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                         c->d_fbc_map, amp, c->d_u, c->d_t, s));
-            prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine) / 1.0,
-                     2.0 * (double)DD * (1 + 2 * c->n_refine));
-            c->launches += 6 + 2LL * c->n_refine;  // W, conv, reduce, cast, gemv(s), update
+            bl.amp[j] = c->amp.empty() ? 1.0 : c->amp[st];
+            bl.c0[j] = st == 1 ? 1.0 : lhs_c[1][0];
+            bl.c1[j] = st == 1 ? 0.0 : lhs_c[1][1];
         }
-    }
-    return TDBEM_OK;
+        CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, bl, ldw,
+                                    c->d_Wt_old, c->d_Wu_old, s));
+        const int nch = mixed_chunks(nlev, D);
+        int nparts = 0;
+        const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
+        CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
+                                 c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
+                                 mixed_ksplit(nch, D, M + 1), &nparts, s));
+        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
+                 nlev * 4.0 * nb * (double)DD);
+        CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, nb, D, nullptr, c->d_Yold, s));
+        c->launches += 3;
+        return TDBEM_OK;
+    };
+    // The history of steps [a, b) into the right-hand sides of steps [b, e): levels
+    // 0..e-a, e-b columns (padded to a kernel width).
+    auto cross = [&](int S, int a, int b, int e) -> int {
+        const int ncol = e - b;
+        const int nbp = ncol <= 1 ? 1 : ncol <= 2 ? 2 : ncol <= 4 ? 4 : ncol <= 8 ? 8 : 16;
+        const int nlev = std::min(M, e - a) + 1;
+        CUDA_TRY(launch_build_w_cross(c->d_u, c->d_t, D, a, b, ncol, nbp, nlev, a1, a2, a3, ldw,
+                                      c->d_Wt_old, c->d_Wu_old, s));
+        const int nch = mixed_chunks(nlev, D);
+        int nparts = 0;
+        const int pe = prof_begin(c, TDBEM_K_CONV);
+        CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nbp,
+                                 c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
+                                 mixed_ksplit(nch, D, (M + 1) * nb / nbp), &nparts, s));
+        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nbp * ldw * 4,
+                 nlev * 4.0 * ncol * (double)DD);
+        double* y = c->d_Yold + (size_t)(b - S) * D;
+        CUDA_TRY(launch_reduce_cols_n(c->d_pmix, nparts, nbp, ncol, D, y, y, s));
+        c->launches += 3;
+        return TDBEM_OK;
+    };
+    // Step st from its accumulated right-hand side.
+    auto solve = [&](int S, int st) -> int {
+        const int pe = prof_begin(c, TDBEM_K_SOLVE);
+        const int v = st == 1 ? 0 : 1;
+        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
+        // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
+        CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_Yold + (size_t)(st - S) * D,
+                                    c->d_x, c->d_res, reinterpret_cast<float*>(c->d_dx),
+                                    c->n_refine, s));
+        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
+                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
+        prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine),
+                 2.0 * (double)DD * (1 + 2 * c->n_refine));
+        c->launches += 4 + 2LL * c->n_refine;  // cast, gemv(s), residual(s), update
+        return TDBEM_OK;
+    };
+    // Steps [s0, s0 + n) of the block starting at S: first half, its history into
+    // the second half, second half.
+    std::function<int(int, int, int)> rec = [&](int S, int s0, int n) -> int {
+        if (n == 1) return solve(S, s0);
+        const int h = n / 2;
+        int r = rec(S, s0, h);
+        if (r == TDBEM_OK) r = cross(S, s0, s0 + h, s0 + n);
+        if (r == TDBEM_OK) r = rec(S, s0 + h, n - h);
+        return r;
+    };
+    const int lrc = run_march_loop(c, 1, numstep, ptrs, [&]() -> int {
+        for (int S = 1; S <= last_s; S += nb) {
+            const int nbe = std::min(nb, last_s - S + 1);
+            int r = old_pass(S, nbe);
+            if (r == TDBEM_OK) r = rec(S, S, nbe);
+            if (r != TDBEM_OK) return r;
+        }
+        return TDBEM_OK;
     });
     if (lrc != TDBEM_OK) return lrc;
     c->timings[2] = tmr.stop_ms(s);
@@ -2138,8 +2166,6 @@ int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
     if (block_steps != c->nb) {  // scratch sized by the block
         dfree(c->d_Wt_old);
         dfree(c->d_Wu_old);
-        dfree(c->d_Wt_new);
-        dfree(c->d_Wu_new);
         dfree(c->d_Yold);
         dfree(c->d_pmix);
         dfree(c->d_res);

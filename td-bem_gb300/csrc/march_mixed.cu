@@ -9,7 +9,13 @@
 // one pass over the levels with NB right-hand-side columns,
 //     Y_old[:, j] = sum_f X^f W_f^old[:, j],
 // so each level is read once per block instead of once per step.  The part with
-// S <= m < s needs only levels f <= s - S + 1 and is added step by step.
+// S <= m < s (history inside the block) is added by recursive halving: the block's
+// first half is solved, then the first half's history enters every step of the
+// second half in one multi-column pass over levels 0..n (a history step m reaches
+// step s only through levels s-m-1, s-m, s-m+1), then the second half is solved.
+// A block of n steps reads n log2(n) + n - 1 levels for its inner part instead of
+// n (n+3)/2 step by step; the known-load terms of levels 0/1 join the old pass, and
+// the leaves are plain solves.
 #include <algorithm>
 
 #include "tdbem_internal.cuh"
@@ -98,11 +104,13 @@ __global__ void __launch_bounds__(256) k_conv_f32(const float* __restrict__ G,
         }
 }
 
-// W_f^old[:, j] for s = S + j, history indices 1 <= m < S only (no load terms).
+// W_f^old[:, j] for s = S + j: history indices 1 <= m < S, plus the known-load
+// terms of levels 0/1 (c0, c1: the LHS weights of those levels, amp the step's load
+// amplitude; columns j < nload).
 __global__ void k_build_w_old(const double* __restrict__ u_hist,
                               const double* __restrict__ t_hist, int D, int S, int nb, int nlev,
-                              double a1, double a2, double a3, int ldw, float* __restrict__ Wt,
-                              float* __restrict__ Wu) {
+                              double a1, double a2, double a3, BlockLoads bl, int ldw,
+                              float* __restrict__ Wt, float* __restrict__ Wu) {
     const size_t total = (size_t)nlev * nb * ldw;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
          idx += (size_t)gridDim.x * blockDim.x) {
@@ -129,49 +137,49 @@ __global__ void k_build_w_old(const double* __restrict__ u_hist,
                 wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
                 wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
             }
+            if (f <= 1 && j < bl.nload) {
+                const double cf = f == 0 ? bl.c0[j] : bl.c1[j];
+                wt += cf * (bl.amp[j] * bl.load_t[k]);
+                wu += cf * bl.load_u[k];
+            }
         }
         Wt[idx] = (float)wt;
         Wu[idx] = (float)wu;
     }
 }
 
-// w_f^new for step s: history indices S <= m <= s-1, plus the known-load terms
-// of levels 0/1 (c0, c1: the LHS weights of those levels).
-__global__ void k_build_w_new(const double* __restrict__ u_hist,
-                              const double* __restrict__ t_hist, int D, int s, int S, int nlev,
-                              double a1, double a2, double a3, double c0, double c1, double amp,
-                              const double* __restrict__ load_t,
-                              const double* __restrict__ load_u, int ldw,
-                              float* __restrict__ Wt, float* __restrict__ Wu) {
-    const size_t total = (size_t)nlev * ldw;
+// W_f[:, j] of the history steps m in [a, b) for the steps s = b + j, j < ncol
+// (columns ncol..nbp-1 zero): a1 x^m on level s+1-m (>= 2), a3 x^m on level s-m
+// (>= 1), a2 x^m on level s-1-m, and -a1 x^{s-1} on level 0.
+__global__ void k_build_w_cross(const double* __restrict__ u_hist,
+                                const double* __restrict__ t_hist, int D, int a, int b,
+                                int ncol, int nbp, int nlev, double a1, double a2, double a3,
+                                int ldw, float* __restrict__ Wt, float* __restrict__ Wu) {
+    const size_t total = (size_t)nlev * nbp * ldw;
     for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
          idx += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)(idx % ldw), f = (int)(idx / ldw);
+        const int k = (int)(idx % ldw);
+        const int j = (int)((idx / ldw) % nbp);
+        const int f = (int)(idx / ((size_t)ldw * nbp));
+        const int s = b + j;
         double wt = 0, wu = 0;
-        if (k < D) {
+        if (k < D && j < ncol) {
             const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
-            if (f >= 2 && m1 >= S && m1 >= 1) {
+            if (f >= 2 && m1 >= a && m1 < b) {
                 wt += a1 * t_hist[(size_t)m1 * D + k];
                 wu += a1 * u_hist[(size_t)m1 * D + k];
             }
-            if (f >= 1 && m3 >= S && m3 >= 1) {
+            if (f >= 1 && m3 >= a && m3 < b) {
                 wt += a3 * t_hist[(size_t)m3 * D + k];
                 wu += a3 * u_hist[(size_t)m3 * D + k];
             }
-            if (m2 >= S && m2 >= 1) {
+            if (m2 >= a && m2 < b) {
                 wt += a2 * t_hist[(size_t)m2 * D + k];
                 wu += a2 * u_hist[(size_t)m2 * D + k];
             }
-            if (f == 0) {
-                if (s - 1 >= S && s - 1 >= 1) {
-                    wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
-                    wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
-                }
-                wt += c0 * (amp * load_t[k]);
-                wu += c0 * load_u[k];
-            } else if (f == 1) {
-                wt += c1 * (amp * load_t[k]);
-                wu += c1 * load_u[k];
+            if (f == 0 && s - 1 >= a && s - 1 < b) {
+                wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
+                wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
             }
         }
         Wt[idx] = (float)wt;
@@ -179,11 +187,12 @@ __global__ void k_build_w_new(const double* __restrict__ u_hist,
     }
 }
 
-// out[j][row] = sum over chunks of partial[chunk][j][row] (+ add[j][row] if given).
-__global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, int nb, int D,
-                              const double* __restrict__ add, double* __restrict__ out) {
+// out[j][row] = sum over chunks of partial[chunk][j][row] (+ add[j][row] if given),
+// for the first ncol of the nb partial columns.
+__global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, int nb, int ncol,
+                              int D, const double* __restrict__ add, double* __restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb * D) return;
+    if (i >= ncol * D) return;
     double s = add ? add[i] : 0.0;
     for (int c = 0; c < nchunks; c++) s += partial[(size_t)c * nb * D + i];
     out[i] = s;
@@ -277,6 +286,7 @@ cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int 
     const float* wu = Wu - (size_t)f_lo * nb * ldw;
     switch (nb) {
     case 1: k_conv_f32<1><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
+    case 2: k_conv_f32<2><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
     case 4: k_conv_f32<4><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
     case 6: k_conv_f32<6><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
     case 8: k_conv_f32<8><<<grid, 256, 0, s>>>(G, H, lstride, ld, D, f_lo, f_hi, per_chunk, wt, wu, ldw, kspan, partial); break;
@@ -288,28 +298,35 @@ cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int 
 }
 
 cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
-                               int nlev, double a1, double a2, double a3, int ldw, float* Wt,
-                               float* Wu, cudaStream_t s) {
+                               int nlev, double a1, double a2, double a3, const BlockLoads& bl,
+                               int ldw, float* Wt, float* Wu, cudaStream_t s) {
     const size_t total = (size_t)nlev * nb * ldw;
     const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 8192);
-    k_build_w_old<<<grid, 256, 0, s>>>(u_hist, t_hist, D, S, nb, nlev, a1, a2, a3, ldw, Wt, Wu);
+    k_build_w_old<<<grid, 256, 0, s>>>(u_hist, t_hist, D, S, nb, nlev, a1, a2, a3, bl, ldw, Wt,
+                                       Wu);
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_w_new(const double* u_hist, const double* t_hist, int D, int st, int S,
-                               int nlev, double a1, double a2, double a3, double c0, double c1,
-                               double amp, const double* load_t, const double* load_u, int ldw,
-                               float* Wt, float* Wu, cudaStream_t s) {
-    const size_t total = (size_t)nlev * ldw;
-    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 4096);
-    k_build_w_new<<<grid, 256, 0, s>>>(u_hist, t_hist, D, st, S, nlev, a1, a2, a3, c0, c1, amp,
-                                       load_t, load_u, ldw, Wt, Wu);
+cudaError_t launch_build_w_cross(const double* u_hist, const double* t_hist, int D, int a, int b,
+                                 int ncol, int nbp, int nlev, double a1, double a2, double a3,
+                                 int ldw, float* Wt, float* Wu, cudaStream_t s) {
+    const size_t total = (size_t)nlev * nbp * ldw;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 8192);
+    k_build_w_cross<<<grid, 256, 0, s>>>(u_hist, t_hist, D, a, b, ncol, nbp, nlev, a1, a2, a3,
+                                         ldw, Wt, Wu);
     return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
                                const double* add, double* out, cudaStream_t s) {
-    k_reduce_cols<<<(nb * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, D, add, out);
+    k_reduce_cols<<<(nb * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, nb, D, add, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce_cols_n(const double* partial, int nchunks, int nb, int ncol, int D,
+                                 const double* add, double* out, cudaStream_t s) {
+    k_reduce_cols<<<(ncol * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, ncol, D, add,
+                                                         out);
     return cudaGetLastError();
 }
 

@@ -255,13 +255,23 @@ cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int 
                             int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
                             int ldw, double* partial, int nchunks, int ksplit, int* nparts,
                             cudaStream_t s);
+// Per-column load terms of a time block's old pass (steps S + j, j < nload <= 16).
+struct BlockLoads {
+    int nload;
+    double amp[16], c0[16], c1[16];
+    const double* load_t;
+    const double* load_u;
+};
 cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
-                               int nlev, double a1, double a2, double a3, int ldw, float* Wt,
-                               float* Wu, cudaStream_t s);
-cudaError_t launch_build_w_new(const double* u_hist, const double* t_hist, int D, int st, int S,
-                               int nlev, double a1, double a2, double a3, double c0, double c1,
-                               double amp, const double* load_t, const double* load_u, int ldw,
-                               float* Wt, float* Wu, cudaStream_t s);
+                               int nlev, double a1, double a2, double a3, const BlockLoads& bl,
+                               int ldw, float* Wt, float* Wu, cudaStream_t s);
+// History of steps [a, b) into the steps b .. b+ncol-1 (nbp >= ncol padded columns).
+cudaError_t launch_build_w_cross(const double* u_hist, const double* t_hist, int D, int a, int b,
+                                 int ncol, int nbp, int nlev, double a1, double a2, double a3,
+                                 int ldw, float* Wt, float* Wu, cudaStream_t s);
+// The first ncol of nb partial columns (out and add have ncol columns).
+cudaError_t launch_reduce_cols_n(const double* partial, int nchunks, int nb, int ncol, int D,
+                                 const double* add, double* out, cudaStream_t s);
 cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
                                const double* add, double* out, cudaStream_t s);
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
@@ -349,8 +359,6 @@ struct tdbem_ctx {
     double* d_Hc64[2] = {nullptr, nullptr};
     float* d_Wt_old = nullptr;
     float* d_Wu_old = nullptr;
-    float* d_Wt_new = nullptr;
-    float* d_Wu_new = nullptr;
     double* d_Yold = nullptr;
     double* d_pmix = nullptr;       // conv partials, chunks x nb x D
     double* d_res = nullptr;
