@@ -364,7 +364,9 @@ def run_ours(args, dist):
     ctx.set_alpha(*ALPHA)
     engine = lib.ENGINE_TCGEN05 if args.engine == "tcgen05" else lib.ENGINE_MMA_SYNC
     refine = args.refine if args.refine is not None else (0 if cases else 1)
-    ctx.set_march_options(8, refine)
+    march_engine = lib.ENGINE_TCGEN05 if args.march_engine == "tcgen05" else lib.ENGINE_FP32
+    ctx.set_march_options(args.block, refine)
+    ctx.set_march_engine(march_engine)
     ctx.set_batch_options(engine, refine)
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -419,7 +421,8 @@ def run_ours(args, dist):
         t0 = time.perf_counter()
         with lib.Context(model) as c2:
             c2.set_alpha(*ALPHA)
-            c2.set_march_options(8, refine)
+            c2.set_march_options(args.block, refine)
+            c2.set_march_engine(march_engine)
             c2.set_batch_options(engine, refine)
             c2.assemble(precision=prec)
             if cases:
@@ -487,8 +490,9 @@ def run_ours(args, dist):
                     "bf16_mma_tflops": mma_tf}
     elif dom in ("conv", "conv_block"):
         achieved = st["bytes"] / (st["ms"] / 1e3) / 1e9
-        kname = {"conv": "k_conv" if prec == lib.FP64 else "k_conv_f32<1>",
-                 "conv_block": "k_conv_f32<NB>"}[dom]
+        kname = {"conv": "k_conv" if prec == lib.FP64 else "k_conv_f32<NB>",
+                 "conv_block": "k_conv_tc (tcgen05, split-BF16)"
+                 if args.march_engine == "tcgen05" else "k_conv_f32<NB>"}[dom]
         roof = {"bound": "hbm", "kernel": kname, "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "peak_source": f"hbm_gbs of {peak_kind}"}
@@ -505,7 +509,10 @@ def run_ours(args, dist):
                 "peak_source": f"{key}: cuBLAS GEMM measured in this run"}
     roof["launches"] = st["launches"]
     roof["avg_launch_ms"] = st["ms"] / max(1, st["launches"])
-    t = traffic.get(f"{args.workload}:{args.precision}:{dom}")
+    tkey = f"{args.workload}:{args.precision}:{dom}"
+    if dom == "conv_block":
+        tkey += f":{args.march_engine}"
+    t = traffic.get(tkey)
     if isinstance(t, dict) and "ratio_to_algorithmic" in t:
         roof["traffic"] = t["ratio_to_algorithmic"] * st["bytes"] / max(1, st["launches"])
         roof["traffic_source"] = t["source"]
@@ -519,6 +526,8 @@ def run_ours(args, dist):
                        "alpha": list(ALPHA), "precision": args.precision,
                        "parallelism": f"replicas{dist.world}", "load_cases": nc,
                        "refine_sweeps": refine,
+                       "block_steps": args.block,
+                       "march_engine": args.march_engine if prec == lib.MIXED else None,
                        "batch_engine": args.engine if cases else None,
                        "l2": "inputs larger than L2: the level store is "
                              f"{level_gb:.1f} GB"},
@@ -726,6 +735,11 @@ def main():
                          "0 for batched workloads)")
     ap.add_argument("--engine", choices=["tcgen05", "mma_sync"], default="tcgen05",
                     help="tensor-core engine of the batched convolution")
+    ap.add_argument("--march-engine", choices=["tcgen05", "fp32"], default="tcgen05",
+                    help="old-history pass of the mixed march: split-BF16 products on the "
+                         "tensor cores, or FP32 products on the CUDA cores")
+    ap.add_argument("--block", type=int, default=16, choices=[1, 4, 6, 8, 12, 16],
+                    help="time-block steps of the mixed march")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 64-load-case batched measurement beside the headline")

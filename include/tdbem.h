@@ -231,9 +231,19 @@ int tdbem_set_batch_options(tdbem_ctx* ctx, int engine, int refine_sweeps);
  * (on by default; off with on = 0, and off while profiling is on). */
 int tdbem_set_graphs(tdbem_ctx* ctx, int on);
 
+/* Engine of the TDBEM_MIXED marching's per-block pass over the old history (the
+ * largest part of the march): TDBEM_ENGINE_TCGEN05 (default; the FP32 levels as BF16
+ * hi/lo planes, three BF16 tensor-core products per FP32 product, FP32 accumulation
+ * and compensated sums across levels: HBM-bound, history error ~1e-5 of FP64) or
+ * TDBEM_ENGINE_FP32 (FP32 products on the CUDA cores: error ~2e-7 of FP64, slower).
+ * The tcgen05 engine keeps a second level store of the same size (the planes). */
+#define TDBEM_ENGINE_FP32 2
+int tdbem_set_march_engine(tdbem_ctx* ctx, int engine);
+
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
- * history convolution (1, 4, 6, 8, 12 or 16; default 8, the fastest on GB300 for
- * the 4614-DOF sphere), refine_sweeps = FP64 residual-refinement sweeps per solve
+ * history convolution (1, 4, 6, 8, 12 or 16; default 16, the fastest on GB300 for
+ * the 4614-DOF sphere with the tcgen05 engine; 8 is the fastest with the FP32
+ * engine), refine_sweeps = FP64 residual-refinement sweeps per solve
  * (0..4; default 1). */
 int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
 

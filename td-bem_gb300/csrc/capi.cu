@@ -516,6 +516,39 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     }
     const int rc = mixed_inverses(c, numstep, lhs_c);
     if (rc != TDBEM_OK) return rc;
+    // tcgen05 engine: BF16 hi/lo planes of the levels (once per assembly) and of the
+    // old-history vectors, with their tensor maps
+    const bool tc = c->march_engine == TDBEM_ENGINE_TCGEN05;
+    const int Lw = M + 1;
+    if (tc) {
+        if (!c->tc_planes_valid) {
+            if (!c->d_tc_planes) CUDA_TRY(cudaMalloc(&c->d_tc_planes, tc_plane_bytes(D, M + 1)));
+            const int pe = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_split_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_tc_planes, s));
+            prof_end(c, pe, 2.0 * (M + 1) * (double)D * (c->ldf + tc_ldb(D)) * 4, 0);
+            c->launches += 1;
+            c->tc_planes_valid = true;
+        }
+        const size_t wb = tc_w_bytes(D, nb, Lw);
+        if (c->mtc_W_bytes < wb) {
+            if (c->d_mtc_W) cudaFree(c->d_mtc_W);
+            c->d_mtc_W = nullptr;
+            c->mtc_W_bytes = 0;
+            c->mtc_maps_for[0] = c->mtc_maps_for[1] = nullptr;
+            CUDA_TRY(cudaMalloc(&c->d_mtc_W, wb));
+            c->mtc_W_bytes = wb;
+        }
+        if (c->mtc_maps_for[0] != c->d_tc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
+            c->mtc_nb != nb) {
+            if (!make_tc_maps(c->d_tc_planes, D, M + 1, c->d_mtc_W, nb, Lw, &c->mtc_maps))
+                return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the march planes");
+            c->mtc_maps_for[0] = c->d_tc_planes;
+            c->mtc_maps_for[1] = c->d_mtc_W;
+            c->mtc_nb = nb;
+        }
+        if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 1));
+        CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), s));
+    }
 
     EventTimer tmr;
     tmr.start(s);
@@ -525,7 +558,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         c->d_u,       c->d_t,       c->d_Gf,      c->d_Hf,      c->d_inv32[0], c->d_inv32[1],
         c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old,  c->d_Wu_old,  c->d_Yold,     c->d_pmix,
         c->d_x,       c->d_res,     c->d_dx,      c->d_load_t,  c->d_load_u,   c->d_is_ubc,
-        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map};
+        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map, tc ? c->d_tc_planes : nullptr,
+        tc ? c->d_mtc_W : nullptr,  tc ? c->d_tc_err : nullptr};
     // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
     // Old pass: history before the block and the steps' known-load terms.
     auto old_pass = [&](int S, int nbe) -> int {
@@ -539,6 +573,20 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             bl.amp[j] = c->amp.empty() ? 1.0 : c->amp[st];
             bl.c0[j] = st == 1 ? 1.0 : lhs_c[1][0];
             bl.c1[j] = st == 1 ? 0.0 : lhs_c[1][1];
+        }
+        if (tc) {  // split-BF16 products on the tensor cores, FP32 accumulation
+            CUDA_TRY(launch_build_w_old_tc(c->d_u, c->d_t, D, S, nb, nlev, Lw, a1, a2, a3, bl,
+                                           c->d_mtc_W, s));
+            const int splits = tc_conv_splits(nlev, D, nb);
+            const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
+            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, nb, c->d_pmix, splits,
+                                    c->d_tc_err, s));
+            prof_end(c, pe, nlev * 2.0 * (double)D * tc_ldb(D) * 4 +
+                                nlev * 2.0 * tc_cases_pad(nb) * tc_ldb(D) * 4,
+                     nlev * 4.0 * nb * (double)DD);
+            CUDA_TRY(launch_reduce_cols(c->d_pmix, splits, nb, D, nullptr, c->d_Yold, s));
+            c->launches += 3;
+            return TDBEM_OK;
         }
         CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, bl, ldw,
                                     c->d_Wt_old, c->d_Wu_old, s));
@@ -611,6 +659,14 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         return TDBEM_OK;
     });
     if (lrc != TDBEM_OK) return lrc;
+    if (tc) {  // a bounded pipeline wait of the tcgen05 kernel that ran out
+        int err = 0;
+        CUDA_TRY(cudaMemcpyAsync(&err, c->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CUDA_TRY(cudaStreamSynchronize(s));
+        if (err)
+            return fail(TDBEM_ERR_CUDA, "tcgen05 convolution: pipeline wait timed out (code %d)",
+                        err);
+    }
     c->timings[2] = tmr.stop_ms(s);
     return TDBEM_OK;
 }
@@ -2156,6 +2212,14 @@ int tdbem_set_batch_options(tdbem_ctx* c, int engine, int refine_sweeps) {
     return TDBEM_OK;
 }
 
+int tdbem_set_march_engine(tdbem_ctx* c, int engine) {
+    if (!c) return fail(TDBEM_ERR_ARG, "null context");
+    if (engine != TDBEM_ENGINE_TCGEN05 && engine != TDBEM_ENGINE_FP32)
+        return fail(TDBEM_ERR_ARG, "engine must be TDBEM_ENGINE_TCGEN05 or TDBEM_ENGINE_FP32");
+    c->march_engine = engine;
+    return TDBEM_OK;
+}
+
 int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
     if (!c) return fail(TDBEM_ERR_ARG, "null context");
     if (block_steps != 1 && block_steps != 4 && block_steps != 6 && block_steps != 8 &&
@@ -2253,6 +2317,7 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         b += 2 * L * D * ld * 4 + 4 * DD * 8;   // FP32 levels, FP64 levels 0 and 1
         b += 2 * DD * 8 + 2 * DD * 4 + inverse_scratch_elems((int)D) * 4;  // LHS, inverses
         b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
+        b += tc_plane_bytes((int)D, (int)L) + tc_w_bytes((int)D, 8, (int)L);  // tcgen05 planes
     }
     *bytes = b;
     return TDBEM_OK;

@@ -319,22 +319,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // FP32 level store [f][row][ldf] -> BF16 hi/lo planes [(mat*2+plane)*L + f][row][ldb].
-__global__ void k_split_levels(const float* __restrict__ Gf, const float* __restrict__ Hf,
-                               int ldf, int D, int L, int ldb, __nv_bfloat16* __restrict__ P) {
-    const size_t per_mat = (size_t)L * D * ldb;
-    const size_t plane = per_mat;  // one (mat, plane) block = L * D * ldb
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < 2 * per_mat;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int mat = (int)(idx / per_mat);
-        const size_t r = idx % per_mat;
-        const int k = (int)(r % ldb);
-        const size_t fr = r / ldb;  // f * D + row
-        float x = 0.f;
-        if (k < D) x = (mat == 0 ? Gf : Hf)[fr * ldf + k];
-        const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(__fsub_rn(x, __bfloat162float(hi)));
-        P[(size_t)(mat * 2) * plane + r] = hi;
-        P[(size_t)(mat * 2 + 1) * plane + r] = lo;
+__global__ void __launch_bounds__(256) k_split_levels(const float* __restrict__ Gf,
+                                                      const float* __restrict__ Hf, int ldf,
+                                                      int D, int L, int ldb,
+                                                      __nv_bfloat16* __restrict__ P) {
+    // block per row (mat, f, row), 4 columns per thread: a 16-byte load of the FP32
+    // row (ldf is a multiple of 4, its padding zero) and an 8-byte store per plane
+    const size_t rows = (size_t)L * D;  // per matrix
+    const size_t plane = rows * ldb;    // one (mat, plane) block
+    for (size_t rr = blockIdx.x; rr < 2 * rows; rr += gridDim.x) {
+        const int mat = rr >= rows ? 1 : 0;
+        const size_t fr = rr - (size_t)mat * rows;  // f * D + row
+        const float* src = (mat == 0 ? Gf : Hf) + fr * ldf;
+        __nv_bfloat16* hi_row = P + (size_t)(mat * 2) * plane + fr * ldb;
+        __nv_bfloat16* lo_row = P + (size_t)(mat * 2 + 1) * plane + fr * ldb;
+        for (int k = 4 * threadIdx.x; k < ldb; k += 4 * blockDim.x) {
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (k < ldf) x = __ldcs(reinterpret_cast<const float4*>(src + k));
+            const float v[4] = {x.x, x.y, x.z, x.w};
+            __align__(8) __nv_bfloat16 h[4], l[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                h[q] = __float2bfloat16_rn(v[q]);
+                l[q] = __float2bfloat16_rn(__fsub_rn(v[q], __bfloat162float(h[q])));
+            }
+            *reinterpret_cast<uint2*>(hi_row + k) = *reinterpret_cast<const uint2*>(h);
+            *reinterpret_cast<uint2*>(lo_row + k) = *reinterpret_cast<const uint2*>(l);
+        }
     }
 }
 
@@ -396,6 +407,60 @@ __global__ void k_build_w_tc(const double* __restrict__ u_hist, const double* __
     }
 }
 
+// The old-history vectors of a time block (march_mixed.cu's k_build_w_old: history
+// 1 <= m < S for the steps s = S + c, c < nb, and the steps' known-load terms of
+// levels 0/1) as BF16 hi/lo planes [(mat*2+plane)*Lw + f][c][ldb] (c < Cpad, zero
+// beyond nb and D; mat 1 = -Wu).
+__global__ void k_build_w_old_tc(const double* __restrict__ u_hist,
+                                 const double* __restrict__ t_hist, int D, int S, int nb,
+                                 int Cpad, int nlev, int Lw, double a1, double a2, double a3,
+                                 BlockLoads bl, int ldb, __nv_bfloat16* __restrict__ W) {
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const size_t plane = (size_t)Lw * Cpad * ldb;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % ldb);
+        const int c = (int)((idx / ldb) % Cpad);
+        const int f = (int)(idx / ((size_t)ldb * Cpad));
+        const int s = S + c;
+        double wt = 0, wu = 0;
+        if (k < D && c < nb) {
+            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+            if (f >= 2 && m1 >= 1 && m1 < S) {
+                wt += a1 * t_hist[(size_t)m1 * D + k];
+                wu += a1 * u_hist[(size_t)m1 * D + k];
+            }
+            if (f >= 1 && m3 >= 1 && m3 < S) {
+                wt += a3 * t_hist[(size_t)m3 * D + k];
+                wu += a3 * u_hist[(size_t)m3 * D + k];
+            }
+            if (m2 >= 1 && m2 < S) {
+                wt += a2 * t_hist[(size_t)m2 * D + k];
+                wu += a2 * u_hist[(size_t)m2 * D + k];
+            }
+            if (f == 0 && s - 1 >= 1 && s - 1 < S) {
+                wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
+                wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
+            }
+            if (f <= 1 && c < bl.nload) {
+                const double cf = f == 0 ? bl.c0[c] : bl.c1[c];
+                wt += cf * (bl.amp[c] * bl.load_t[k]);
+                wu += cf * bl.load_u[k];
+            }
+        }
+        const double vals[2] = {wt, -wu};
+#pragma unroll
+        for (int mat = 0; mat < 2; mat++) {
+            const float xf = (float)vals[mat];
+            const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
+            const __nv_bfloat16 lo =
+                __float2bfloat16_rn((float)(vals[mat] - (double)__bfloat162float(hi)));
+            W[(size_t)(mat * 2) * plane + idx] = hi;
+            W[(size_t)(mat * 2 + 1) * plane + idx] = lo;
+        }
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -437,8 +502,9 @@ int tc_conv_splits(int nlev, int D, int C) {
 
 cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
                                 void* planes, cudaStream_t s) {
-    const size_t total = 2 * (size_t)L * D * tc_ldb(D);
-    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 152 * 16);
+    if (ldf % 4 != 0 || ldf > tc_ldb(D)) return cudaErrorInvalidValue;
+    const size_t rows = 2 * (size_t)L * D;
+    const unsigned grid = (unsigned)std::min<size_t>(rows, 152 * 8);
     k_split_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, tc_ldb(D),
                                         static_cast<__nv_bfloat16*>(planes));
     return cudaGetLastError();
@@ -455,6 +521,17 @@ cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D,
     k_build_w_tc<<<grid, 256, 0, st>>>(u_hist, t_hist, D, C, Cpad, s, nlev, Lw, a1, a2, a3, c0,
                                        c1, amp, numstep, traction, is_u, ubc_val, ldb,
                                        static_cast<__nv_bfloat16*>(W));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_old_tc(const double* u_hist, const double* t_hist, int D, int S,
+                                  int nb, int nlev, int Lw, double a1, double a2, double a3,
+                                  const BlockLoads& bl, void* W, cudaStream_t st) {
+    const int Cpad = tc_cases_pad(nb), ldb = tc_ldb(D);
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
+    k_build_w_old_tc<<<grid, 256, 0, st>>>(u_hist, t_hist, D, S, nb, Cpad, nlev, Lw, a1, a2, a3,
+                                           bl, ldb, static_cast<__nv_bfloat16*>(W));
     return cudaGetLastError();
 }
 

@@ -219,6 +219,14 @@ cudaError_t launch_update_state(const double* x, int D, int s, const unsigned ch
                                 double* t_hist, cudaStream_t st);
 int conv_chunks(int L, int D);
 
+// Per-column load terms of a time block's old pass (steps S + j, j < nload <= 16).
+struct BlockLoads {
+    int nload;
+    double amp[16], c0[16], c1[16];
+    const double* load_t;
+    const double* load_u;
+};
+
 // Batched convolution on tcgen05 tensor cores (conv_tc.cu).
 constexpr int kTensorMapBytes = 128;
 struct TcMaps {
@@ -237,6 +245,10 @@ cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D,
                               double c1, const double* amp, int numstep, const double* traction,
                               const unsigned char* is_u, const double* ubc_val, void* W,
                               cudaStream_t st);
+// Old-history vectors of a time block of the mixed march as BF16 planes (nb columns).
+cudaError_t launch_build_w_old_tc(const double* u_hist, const double* t_hist, int D, int S,
+                                  int nb, int nlev, int Lw, double a1, double a2, double a3,
+                                  const BlockLoads& bl, void* W, cudaStream_t st);
 bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out);
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
                            double* partial, int splits, int* d_err, cudaStream_t s);
@@ -255,13 +267,6 @@ cudaError_t launch_conv_f32(const float* G, const float* H, size_t lstride, int 
                             int f_lo, int f_hi, int nb, const float* Wt, const float* Wu,
                             int ldw, double* partial, int nchunks, int ksplit, int* nparts,
                             cudaStream_t s);
-// Per-column load terms of a time block's old pass (steps S + j, j < nload <= 16).
-struct BlockLoads {
-    int nload;
-    double amp[16], c0[16], c1[16];
-    const double* load_t;
-    const double* load_u;
-};
 cudaError_t launch_build_w_old(const double* u_hist, const double* t_hist, int D, int S, int nb,
                                int nlev, double a1, double a2, double a3, const BlockLoads& bl,
                                int ldw, float* Wt, float* Wu, cudaStream_t s);
@@ -353,7 +358,7 @@ struct tdbem_ctx {
     double* d_G01 = nullptr;        // mixed: levels 0 and 1 in FP64 (the LHS)
     double* d_H01 = nullptr;
     // mixed marching
-    int nb = 8;                     // steps per time block
+    int nb = 16;                    // steps per time block
     int n_refine = 1;               // FP64 refinement sweeps per solve
     float* d_inv32[2] = {nullptr, nullptr};
     double* d_Hc64[2] = {nullptr, nullptr};
@@ -384,6 +389,14 @@ struct tdbem_ctx {
     size_t tc_W_bytes = 0;
     int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
     tdbem::TcMaps tc_maps{};
+    // mixed march: engine of the time blocks' old-history pass, its BF16 vector planes
+    // and tensor maps (encoded for d_mtc_W and the level planes)
+    int march_engine = TDBEM_ENGINE_TCGEN05;
+    void* d_mtc_W = nullptr;
+    size_t mtc_W_bytes = 0;
+    tdbem::TcMaps mtc_maps{};
+    const void* mtc_maps_for[2] = {nullptr, nullptr};
+    int mtc_nb = 0;
     // stepwise marching (tdbem_march_begin / tdbem_march_step) and host-block levels
     bool use_graphs = true;         // replay the marching loop as a CUDA graph
     MarchGraph graph;

@@ -59,6 +59,7 @@ SIGNATURES = {
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_set_march_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
                                             ctypes.c_int]),
     "tdbem_march_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
@@ -121,7 +122,7 @@ class Request(ctypes.Structure):
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
-ENGINE_TCGEN05, ENGINE_MMA_SYNC = 0, 1
+ENGINE_TCGEN05, ENGINE_MMA_SYNC, ENGINE_FP32 = 0, 1, 2
 
 
 def _ctx_array(ctxs):
@@ -333,8 +334,11 @@ class Context:
     def set_alpha(self, a1: float, a2: float):
         _check(load().tdbem_set_alpha(self.h, a1, a2))
 
-    def set_march_options(self, block_steps: int = 8, refine_sweeps: int = 1):
+    def set_march_options(self, block_steps: int = 16, refine_sweeps: int = 1):
         _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
+
+    def set_march_engine(self, engine: int):
+        _check(load().tdbem_set_march_engine(self.h, engine))
 
     def set_graphs(self, on: bool):
         _check(load().tdbem_set_graphs(self.h, 1 if on else 0))

@@ -26,10 +26,12 @@ def rel_l2(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-def run(lib, m, precision, alpha=(0.25, 0.0), block=12, refine=1, numstep=None):
+def run(lib, m, precision, alpha=(0.25, 0.0), block=12, refine=1, numstep=None, engine=None):
     with lib.Context(m) as ctx:
         ctx.set_alpha(*alpha)
         ctx.set_march_options(block, refine)
+        if engine is not None:
+            ctx.set_march_engine(engine)
         ctx.assemble(precision=precision)
         u, t = ctx.march(numstep)
         lev = (ctx.level(3, 0), ctx.level(3, 1), ctx.level(ctx.M, 1))
@@ -78,10 +80,24 @@ def test_mixed_q8_bar(tdlib):
 
 
 def test_refinement_recovers_fp64_solve(tdlib, sphere8):
+    """With FP32 convolution products the inverse's error dominates; refinement
+    removes it (under split-BF16 products the convolution's ~1e-5 dominates)."""
     m, (u, t, _) = sphere8
-    e0 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=0)[0], u)
-    e2 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=2)[0], u)
+    e0 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=0, engine=tdlib.ENGINE_FP32)[0], u)
+    e2 = rel_l2(run(tdlib, m, tdlib.MIXED, refine=2, engine=tdlib.ENGINE_FP32)[0], u)
     assert e2 <= e0 and e2 <= TOL_L2
+
+
+@pytest.mark.parametrize("block", [8, 16])
+def test_march_engines(tdlib, sphere8, block):
+    """Old-history pass on the tensor cores (split-BF16, the default) and on the CUDA
+    cores (FP32 products): both within the bar, the FP32 one near FP32 round-off."""
+    m, (u, t, _) = sphere8
+    u_tc, t_tc, _ = run(tdlib, m, tdlib.MIXED, block=block, engine=tdlib.ENGINE_TCGEN05)
+    u_32, t_32, _ = run(tdlib, m, tdlib.MIXED, block=block, engine=tdlib.ENGINE_FP32)
+    assert rel_l2(u_tc, u) <= TOL_L2 and rel_l2(t_tc, t) <= TOL_L2
+    assert rel_l2(u_32, u) <= 1e-6
+    assert rel_l2(u_tc, u) > rel_l2(u_32, u)  # the split products are the coarser ones
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
