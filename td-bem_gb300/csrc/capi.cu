@@ -170,7 +170,11 @@ void free_levels(tdbem_ctx* c) {
     c->levels_last = 0;
     if (c->d_tc_planes) cudaFree(c->d_tc_planes);
     c->d_tc_planes = nullptr;
-    c->tc_planes_valid = false;
+    if (c->d_mtc_planes) cudaFree(c->d_mtc_planes);
+    c->d_mtc_planes = nullptr;
+    dfree(c->d_mtc_known);
+    dfree(c->d_mtc_bc);
+    c->tc_planes_valid = c->mtc_planes_valid = false;
 }
 
 void free_batch(tdbem_ctx* c) {
@@ -209,6 +213,13 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_pmix);
     dfree(c->d_res);
     dfree(c->d_dx);
+    if (c->d_mtc_W) cudaFree(c->d_mtc_W);
+    c->d_mtc_W = nullptr;
+    c->mtc_W_bytes = 0;
+    c->mtc_maps_for[0] = c->mtc_maps_for[1] = nullptr;
+    dfree(c->d_mtc_coef);
+    c->mtc_coef_cap = 0;
+    c->mtc_coef_key.clear();
 
     if (c->d_Ainv[1] == c->d_Ainv[0]) c->d_Ainv[1] = nullptr;
     dfree(c->d_Ainv[0]);
@@ -516,20 +527,62 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     }
     const int rc = mixed_inverses(c, numstep, lhs_c);
     if (rc != TDBEM_OK) return rc;
-    // tcgen05 engine: BF16 hi/lo planes of the levels (once per assembly) and of the
-    // old-history vectors, with their tensor maps
+    // tcgen05 engine: the merged level matrix as BF16 hi/lo planes and the known
+    // part's vectors (once per assembly and boundary conditions), the known part's
+    // coefficients (once per load history, weights and step count), the history
+    // vectors' planes and the tensor maps
     const bool tc = c->march_engine == TDBEM_ENGINE_TCGEN05;
     const int Lw = M + 1;
     if (tc) {
-        if (!c->tc_planes_valid) {
-            if (!c->d_tc_planes) CUDA_TRY(cudaMalloc(&c->d_tc_planes, tc_plane_bytes(D, M + 1)));
+        if (!c->mtc_planes_valid) {
+            if (!c->d_mtc_planes)
+                CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, M + 1, 1)));
+            if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
+            if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
+            // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
+            std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
+            std::vector<double> umap(D, 0.0), fmap(D, 0.0);
+            for (size_t i = 0; i < c->ubc.size(); i++) {
+                is_u[c->ubc[i]] = 1;
+                umap[c->ubc[i]] = c->ubc_v[i];
+            }
+            for (size_t i = 0; i < c->fbc.size(); i++) {
+                is_f[c->fbc[i]] = 1;
+                fmap[c->fbc[i]] = c->fbc_v[i];
+            }
+            std::vector<float> bcv((size_t)3 * D, 0.f);
+            for (int j = 0; j < D; j++) {
+                if (is_f[j] && (!is_u[j] || j == D - 1)) bcv[j] = (float)fmap[j];
+                if (is_f[j] && !is_u[j]) bcv[D + j] = (float)fmap[j];
+                if (is_u[j]) bcv[2 * D + j] = (float)umap[j];
+            }
+            CUDA_TRY(cudaMemcpyAsync(c->d_mtc_bc, bcv.data(), sizeof(float) * bcv.size(),
+                                     cudaMemcpyHostToDevice, s));
             const int pe = prof_begin(c, TDBEM_K_AUX);
-            CUDA_TRY(launch_split_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_tc_planes, s));
-            prof_end(c, pe, 2.0 * (M + 1) * (double)D * (c->ldf + tc_ldb(D)) * 4, 0);
+            CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_is_ubc,
+                                         c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
+                                         c->d_mtc_planes, c->d_mtc_known, s));
+            prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
             c->launches += 1;
-            c->tc_planes_valid = true;
+            c->mtc_planes_valid = true;
         }
-        const size_t wb = tc_w_bytes(D, nb, Lw);
+        std::vector<double> key = {(double)numstep, (double)(M + 1), a1, a2,
+                                   lhs_c[1][0], lhs_c[1][1]};
+        key.insert(key.end(), c->amp.begin(), c->amp.end());
+        if (key != c->mtc_coef_key) {
+            std::vector<double> tab;
+            known_coefficients(numstep, M + 1, a1, a2, a3, c->amp, lhs_c[1][0], lhs_c[1][1], tab);
+            if (c->mtc_coef_cap < tab.size()) {
+                dfree(c->d_mtc_coef);
+                c->mtc_coef_cap = 0;
+                CUDA_TRY(dalloc(&c->d_mtc_coef, tab.size()));
+                c->mtc_coef_cap = tab.size();
+            }
+            CUDA_TRY(cudaMemcpyAsync(c->d_mtc_coef, tab.data(), sizeof(double) * tab.size(),
+                                     cudaMemcpyHostToDevice, s));
+            c->mtc_coef_key = key;
+        }
+        const size_t wb = tc_w_bytes(D, nb, Lw, 1);
         if (c->mtc_W_bytes < wb) {
             if (c->d_mtc_W) cudaFree(c->d_mtc_W);
             c->d_mtc_W = nullptr;
@@ -538,11 +591,11 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             CUDA_TRY(cudaMalloc(&c->d_mtc_W, wb));
             c->mtc_W_bytes = wb;
         }
-        if (c->mtc_maps_for[0] != c->d_tc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
+        if (c->mtc_maps_for[0] != c->d_mtc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
             c->mtc_nb != nb) {
-            if (!make_tc_maps(c->d_tc_planes, D, M + 1, c->d_mtc_W, nb, Lw, &c->mtc_maps))
+            if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_mtc_W, nb, Lw, &c->mtc_maps, 1))
                 return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the march planes");
-            c->mtc_maps_for[0] = c->d_tc_planes;
+            c->mtc_maps_for[0] = c->d_mtc_planes;
             c->mtc_maps_for[1] = c->d_mtc_W;
             c->mtc_nb = nb;
         }
@@ -558,8 +611,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         c->d_u,       c->d_t,       c->d_Gf,      c->d_Hf,      c->d_inv32[0], c->d_inv32[1],
         c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old,  c->d_Wu_old,  c->d_Yold,     c->d_pmix,
         c->d_x,       c->d_res,     c->d_dx,      c->d_load_t,  c->d_load_u,   c->d_is_ubc,
-        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map, tc ? c->d_tc_planes : nullptr,
-        tc ? c->d_mtc_W : nullptr,  tc ? c->d_tc_err : nullptr};
+        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map, tc ? c->d_mtc_planes : nullptr,
+        tc ? c->d_mtc_W : nullptr,  tc ? c->d_tc_err : nullptr,  tc ? c->d_mtc_known : nullptr,
+        tc ? c->d_mtc_coef : nullptr};
     // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
     // Old pass: history before the block and the steps' known-load terms.
     auto old_pass = [&](int S, int nbe) -> int {
@@ -574,18 +628,28 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             bl.c0[j] = st == 1 ? 1.0 : lhs_c[1][0];
             bl.c1[j] = st == 1 ? 0.0 : lhs_c[1][1];
         }
-        if (tc) {  // split-BF16 products on the tensor cores, FP32 accumulation
-            CUDA_TRY(launch_build_w_old_tc(c->d_u, c->d_t, D, S, nb, nlev, Lw, a1, a2, a3, bl,
-                                           c->d_mtc_W, s));
-            const int splits = tc_conv_splits(nlev, D, nb);
-            const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
-            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, nb, c->d_pmix, splits,
-                                    c->d_tc_err, s));
-            prof_end(c, pe, nlev * 2.0 * (double)D * tc_ldb(D) * 4 +
-                                nlev * 2.0 * tc_cases_pad(nb) * tc_ldb(D) * 4,
-                     nlev * 4.0 * nb * (double)DD);
-            CUDA_TRY(launch_reduce_cols(c->d_pmix, splits, nb, D, nullptr, c->d_Yold, s));
-            c->launches += 3;
+        if (tc) {  // merged levels, split-BF16 products on the tensor cores
+            double* Y = c->d_Yold;
+            if (S == 1) {  // no unknown history before the first block
+                CUDA_TRY(cudaMemsetAsync(Y, 0, sizeof(double) * nbe * D, s));
+            } else {
+                CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, S, nbe, nb, 1, S,
+                                               nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
+                // d_pmix holds (M+1) x nb x D partial sums
+                const int splits = tc_conv_splits(nlev, D, nbe, (M + 1) * nb / nbe, 1);
+                const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
+                CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, nbe, c->d_pmix, splits,
+                                        c->d_tc_err, s, 1));
+                prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
+                                    nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                         nlev * 2.0 * nbe * (double)DD);
+                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, nullptr, Y, s));
+                c->launches += 3;
+            }
+            const int pk = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_known_terms(c->d_mtc_known, c->d_mtc_coef, D, M + 1, S, nbe, Y, s));
+            prof_end(c, pk, 3.0 * (std::min(M, S + nbe - 1) + 1) * D * 8, 0);
+            c->launches += 1;
             return TDBEM_OK;
         }
         CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, bl, ldw,
@@ -608,6 +672,21 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         const int ncol = e - b;
         const int nbp = ncol <= 1 ? 1 : ncol <= 2 ? 2 : ncol <= 4 ? 4 : ncol <= 8 ? 8 : 16;
         const int nlev = std::min(M, e - a) + 1;
+        double* y = c->d_Yold + (size_t)(b - S) * D;
+        if (tc) {
+            CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, b, ncol, nb, a, b,
+                                           nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
+            const int splits = tc_conv_splits(nlev, D, ncol, (M + 1) * nb / ncol, 1);
+            const int pe = prof_begin(c, TDBEM_K_CONV);
+            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, ncol, c->d_pmix, splits,
+                                    c->d_tc_err, s, 1));
+            prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
+                                nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                     nlev * 2.0 * ncol * (double)DD);
+            CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s));
+            c->launches += 3;
+            return TDBEM_OK;
+        }
         CUDA_TRY(launch_build_w_cross(c->d_u, c->d_t, D, a, b, ncol, nbp, nlev, a1, a2, a3, ldw,
                                       c->d_Wt_old, c->d_Wu_old, s));
         const int nch = mixed_chunks(nlev, D);
@@ -618,7 +697,6 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                                  mixed_ksplit(nch, D, (M + 1) * nb / nbp), &nparts, s));
         prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nbp * ldw * 4,
                  nlev * 4.0 * ncol * (double)DD);
-        double* y = c->d_Yold + (size_t)(b - S) * D;
         CUDA_TRY(launch_reduce_cols_n(c->d_pmix, nparts, nbp, ncol, D, y, y, s));
         c->launches += 3;
         return TDBEM_OK;
@@ -1256,7 +1334,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
     CUDA_TRY(cudaGetLastError());
     prof_flush(c);
     c->levels_last = last;
-    c->tc_planes_valid = false;  // the BF16 planes follow the levels
+    c->tc_planes_valid = c->mtc_planes_valid = false;  // the BF16 planes follow the levels
     return TDBEM_OK;
 }
 
@@ -1298,6 +1376,7 @@ int tdbem_set_bc(tdbem_ctx* c, const int* ubc_dofs, const double* ubc_vals, int 
     c->ubc_v.assign(ubc_vals, ubc_vals + n_u);
     c->fbc.assign(fbc_dofs, fbc_dofs + n_f);
     c->fbc_v.assign(fbc_vals, fbc_vals + n_f);
+    c->mtc_planes_valid = false;  // the merged levels follow the BC types and values
     return TDBEM_OK;
 }
 
@@ -1546,7 +1625,7 @@ int tdbem_update_gh_linear(tdbem_ctx* c, int step, int node_lo, int node_hi, con
         CUDA_TRY(cudaStreamSynchronize(s));  // the temporary is reused for H
     }
     c->levels_last = std::max(c->levels_last, step);
-    c->tc_planes_valid = false;
+    c->tc_planes_valid = c->mtc_planes_valid = false;
     c->step_inv_ready[0] = c->step_inv_ready[1] = false;
     return TDBEM_OK;
 }
@@ -1740,7 +1819,7 @@ int tdbem_import_levels(tdbem_ctx* c, const char* path) {
         return fail(TDBEM_ERR_ARG, "%s is truncated or the copy failed", path);
     }
     c->levels_last = h.levels_last;
-    c->tc_planes_valid = false;
+    c->tc_planes_valid = c->mtc_planes_valid = false;
     c->step_inv_ready[0] = c->step_inv_ready[1] = false;
     return TDBEM_OK;
 }
@@ -1931,7 +2010,7 @@ int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int p
     for (int i = 0; i < n; i++) {
         tdbem_ctx* c = ctxs[i];
         c->levels_last = std::min(c->M, nsteps[i]);
-        c->tc_planes_valid = false;
+        c->tc_planes_valid = c->mtc_planes_valid = false;
         c->step_inv_ready[0] = c->step_inv_ready[1] = false;
         c->timings[0] = ms;
     }
@@ -2317,7 +2396,9 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         b += 2 * L * D * ld * 4 + 4 * DD * 8;   // FP32 levels, FP64 levels 0 and 1
         b += 2 * DD * 8 + 2 * DD * 4 + inverse_scratch_elems((int)D) * 4;  // LHS, inverses
         b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
-        b += tc_plane_bytes((int)D, (int)L) + tc_w_bytes((int)D, 8, (int)L);  // tcgen05 planes
+        // tcgen05 march: merged planes, history planes, known part and its coefficients
+        b += tc_plane_bytes((int)D, (int)L, 1) + tc_w_bytes((int)D, 16, (int)L, 1) +
+             3 * L * D * 8 + (numstep + 1) * L * 3 * 8 + 3 * D * 4;
     }
     *bytes = b;
     return TDBEM_OK;

@@ -8,7 +8,10 @@
 //   vector planes [(mat*2 + plane)*Lw + f][case][ldb]  mat 1 holds -Wu
 // with ldb = D rounded up to 64 (zero-padded K).
 //
-// One CTA owns a 128-row tile of all (<= 64) cases for a range of levels:
+// One CTA owns a 128-row tile of (<= 64) cases and an equal share of the tile's
+// (level, G/H, 64-wide K chunk) iterations, taken in that order, so a share may
+// start and end inside a level (every CTA of the grid streams the same number of
+// level bytes, whatever the level count):
 //   warp 0      TMA producer: per stage a 128 x 64 tile of the hi and lo level
 //               planes and a 64 x 64 tile of the hi and lo vector planes
 //               (128-byte swizzle), completion counted on an mbarrier;
@@ -16,7 +19,7 @@
 //               (kind::f16, BF16 x BF16 -> FP32, M = 128, N = 64, K = 16):
 //               lo*hi + hi*lo + hi*hi per K step into the accumulator of the
 //               current level; tcgen05.commit frees the stage / hands the
-//               finished level to the epilogue;
+//               finished level (its part in this share) to the epilogue;
 //   warps 2..5  epilogue: tcgen05.ld of a finished level's accumulator (double
 //               buffered in TMEM, columns 0-63 / 64-127), compensated (Kahan)
 //               FP32 sum over the levels, FP64 partial sums at the end.
@@ -161,7 +164,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-              int D, int L, int Lw, int nlev, int per_split, int nk, int C,
+              int D, int L, int Lw, int nlev, int nk, int nmat, int C,
               double* __restrict__ partial, int* __restrict__ err) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
@@ -176,9 +179,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = blockIdx.x * TC_BM;
-    const int f0 = blockIdx.y * per_split;
-    const int nlv = max(0, min(nlev, f0 + per_split) - f0);
     const int c0 = blockIdx.z * TC_BN;
+    // this CTA's iterations [i0, i1) of nlev x nmat x nk; level f = i / per_lev
+    const int per_lev = nmat * nk;
+    const long long T = (long long)nlev * per_lev;
+    const int i0 = (int)(T * blockIdx.y / gridDim.y), i1 = (int)(T * (blockIdx.y + 1) / gridDim.y);
+    const int f0 = i0 / per_lev;
+    const int nseg = i1 > i0 ? (i1 - 1) / per_lev - f0 + 1 : 0;  // levels touched
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -208,27 +215,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {  // ---------------- TMA producer
             int it = 0;
-            bool ok = true;
-            for (int j = 0; j < nlv && ok; j++) {
-                const int f = f0 + j;
-                for (int mat = 0; mat < 2 && ok; mat++)
-                    for (int kc = 0; kc < nk && ok; kc++, it++) {
-                        const int s = it % TC_STAGES, n = it / TC_STAGES;
-                        if (n >= 1 && !mbar_wait(bar(EMPTY + s), (n - 1) & 1, abort_flag, err, 1)) {
-                            ok = false;
-                            break;
-                        }
-                        const uint32_t st = sbase + s * TC_STAGE_BYTES;
-                        mbar_expect_tx(bar(FULL + s), TC_STAGE_BYTES);
-                        const int x = kc * TC_BK;
-                        tma_load_3d(st, &tmA, x, row0, (mat * 2 + 0) * L + f, bar(FULL + s));
-                        tma_load_3d(st + TC_A_BYTES, &tmA, x, row0, (mat * 2 + 1) * L + f,
-                                    bar(FULL + s));
-                        tma_load_3d(st + 2 * TC_A_BYTES, &tmB, x, c0, (mat * 2 + 0) * Lw + f,
-                                    bar(FULL + s));
-                        tma_load_3d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, x, c0,
-                                    (mat * 2 + 1) * Lw + f, bar(FULL + s));
-                    }
+            for (int i = i0; i < i1; i++, it++) {
+                const int f = i / per_lev, r = i - f * per_lev;
+                const int mat = r / nk, kc = r - mat * nk;
+                const int s = it % TC_STAGES, n = it / TC_STAGES;
+                if (n >= 1 && !mbar_wait(bar(EMPTY + s), (n - 1) & 1, abort_flag, err, 1)) break;
+                const uint32_t st = sbase + s * TC_STAGE_BYTES;
+                mbar_expect_tx(bar(FULL + s), TC_STAGE_BYTES);
+                const int x = kc * TC_BK;
+                tma_load_3d(st, &tmA, x, row0, (mat * 2 + 0) * L + f, bar(FULL + s));
+                tma_load_3d(st + TC_A_BYTES, &tmA, x, row0, (mat * 2 + 1) * L + f, bar(FULL + s));
+                tma_load_3d(st + 2 * TC_A_BYTES, &tmB, x, c0, (mat * 2 + 0) * Lw + f,
+                            bar(FULL + s));
+                tma_load_3d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, x, c0, (mat * 2 + 1) * Lw + f,
+                            bar(FULL + s));
             }
             // every issued copy has landed before the CTA can exit
             for (int k = std::max(0, it - TC_STAGES); k < it; k++)
@@ -239,32 +239,33 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) {  // ---------------- MMA issuer
             int it = 0;
             bool ok = true;
-            for (int j = 0; j < nlv && ok; j++) {
+            for (int j = 0; j < nseg && ok; j++) {
                 const int b = j & 1, u = j >> 1;
                 if (u >= 1 && !mbar_wait(bar(TEMPTY + b), (u - 1) & 1, abort_flag, err, 2)) break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(b * TC_BN);
+                const int f = f0 + j;
+                const int ia = max(i0, f * per_lev), ib = min(i1, (f + 1) * per_lev);
                 uint32_t acc = 0;
-                for (int mat = 0; mat < 2 && ok; mat++)
-                    for (int kc = 0; kc < nk; kc++, it++) {
-                        const int s = it % TC_STAGES, n = it / TC_STAGES;
-                        if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3)) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint32_t ah = sbase + s * TC_STAGE_BYTES, al = ah + TC_A_BYTES;
-                        const uint32_t bh = ah + 2 * TC_A_BYTES, bl = bh + TC_B_BYTES;
-#pragma unroll
-                        for (int kk = 0; kk < TC_BK / 16; kk++) {
-                            const uint32_t o = kk * 32;  // 16 BF16 along K inside the swizzle atom
-                            umma_bf16(d_tmem, sw128_desc(al + o), sw128_desc(bh + o), acc);
-                            umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bl + o), 1);
-                            umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bh + o), 1);
-                            acc = 1;
-                        }
-                        umma_commit(bar(EMPTY + s));
+                for (int i = ia; i < ib; i++, it++) {
+                    const int s = it % TC_STAGES, n = it / TC_STAGES;
+                    if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3)) {
+                        ok = false;
+                        break;
                     }
+                    tc_fence_after();
+                    const uint32_t ah = sbase + s * TC_STAGE_BYTES, al = ah + TC_A_BYTES;
+                    const uint32_t bh = ah + 2 * TC_A_BYTES, bl = bh + TC_B_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < TC_BK / 16; kk++) {
+                        const uint32_t o = kk * 32;  // 16 BF16 along K inside the swizzle atom
+                        umma_bf16(d_tmem, sw128_desc(al + o), sw128_desc(bh + o), acc);
+                        umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bl + o), 1);
+                        umma_bf16(d_tmem, sw128_desc(ah + o), sw128_desc(bh + o), 1);
+                        acc = 1;
+                    }
+                    umma_commit(bar(EMPTY + s));
+                }
                 if (ok) umma_commit(bar(TFULL + b));
             }
             // all MMAs of this thread complete before TMEM is released
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float sum[TC_BN], cmp[TC_BN];
 #pragma unroll
         for (int i = 0; i < TC_BN; i++) sum[i] = cmp[i] = 0.f;
-        for (int j = 0; j < nlv; j++) {
+        for (int j = 0; j < nseg; j++) {
             const int b = j & 1, u = j >> 1;
             if (!mbar_wait(bar(TFULL + b), u & 1, abort_flag, err, 4)) break;
             tc_fence_after();
@@ -407,60 +408,6 @@ __global__ void k_build_w_tc(const double* __restrict__ u_hist, const double* __
     }
 }
 
-// The old-history vectors of a time block (march_mixed.cu's k_build_w_old: history
-// 1 <= m < S for the steps s = S + c, c < nb, and the steps' known-load terms of
-// levels 0/1) as BF16 hi/lo planes [(mat*2+plane)*Lw + f][c][ldb] (c < Cpad, zero
-// beyond nb and D; mat 1 = -Wu).
-__global__ void k_build_w_old_tc(const double* __restrict__ u_hist,
-                                 const double* __restrict__ t_hist, int D, int S, int nb,
-                                 int Cpad, int nlev, int Lw, double a1, double a2, double a3,
-                                 BlockLoads bl, int ldb, __nv_bfloat16* __restrict__ W) {
-    const size_t total = (size_t)nlev * Cpad * ldb;
-    const size_t plane = (size_t)Lw * Cpad * ldb;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)(idx % ldb);
-        const int c = (int)((idx / ldb) % Cpad);
-        const int f = (int)(idx / ((size_t)ldb * Cpad));
-        const int s = S + c;
-        double wt = 0, wu = 0;
-        if (k < D && c < nb) {
-            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
-            if (f >= 2 && m1 >= 1 && m1 < S) {
-                wt += a1 * t_hist[(size_t)m1 * D + k];
-                wu += a1 * u_hist[(size_t)m1 * D + k];
-            }
-            if (f >= 1 && m3 >= 1 && m3 < S) {
-                wt += a3 * t_hist[(size_t)m3 * D + k];
-                wu += a3 * u_hist[(size_t)m3 * D + k];
-            }
-            if (m2 >= 1 && m2 < S) {
-                wt += a2 * t_hist[(size_t)m2 * D + k];
-                wu += a2 * u_hist[(size_t)m2 * D + k];
-            }
-            if (f == 0 && s - 1 >= 1 && s - 1 < S) {
-                wt -= a1 * t_hist[(size_t)(s - 1) * D + k];
-                wu -= a1 * u_hist[(size_t)(s - 1) * D + k];
-            }
-            if (f <= 1 && c < bl.nload) {
-                const double cf = f == 0 ? bl.c0[c] : bl.c1[c];
-                wt += cf * (bl.amp[c] * bl.load_t[k]);
-                wu += cf * bl.load_u[k];
-            }
-        }
-        const double vals[2] = {wt, -wu};
-#pragma unroll
-        for (int mat = 0; mat < 2; mat++) {
-            const float xf = (float)vals[mat];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-            const __nv_bfloat16 lo =
-                __float2bfloat16_rn((float)(vals[mat] - (double)__bfloat162float(hi)));
-            W[(size_t)(mat * 2) * plane + idx] = hi;
-            W[(size_t)(mat * 2 + 1) * plane + idx] = lo;
-        }
-    }
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -495,9 +442,13 @@ static_assert(sizeof(CUtensorMap) == kTensorMapBytes, "tensor map size");
 int tc_ldb(int D) { return (D + TC_BK - 1) / TC_BK * TC_BK; }
 int tc_cases_pad(int C) { return (C + TC_BN - 1) / TC_BN * TC_BN; }
 
-int tc_conv_splits(int nlev, int D, int C) {
+int tc_conv_splits(int nlev, int D, int C, int max_splits, int nmat) {
+    // one CTA per SM (197 KB of shared memory each), and at least 16 iterations
+    // (16 x 48 KB) per CTA so the pipeline's fill and drain stay small
     const int tiles = (D + TC_BM - 1) / TC_BM * ((C + TC_BN - 1) / TC_BN);
-    return std::max(1, std::min(nlev, 152 / std::max(1, tiles)));
+    const long long iters = (long long)nlev * nmat * (tc_ldb(D) / TC_BK);
+    const long long s = std::min<long long>(152 / std::max(1, tiles), iters / 16);
+    return (int)std::max<long long>(1, std::min<long long>(s, max_splits));
 }
 
 cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
@@ -524,25 +475,14 @@ cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D,
     return cudaGetLastError();
 }
 
-cudaError_t launch_build_w_old_tc(const double* u_hist, const double* t_hist, int D, int S,
-                                  int nb, int nlev, int Lw, double a1, double a2, double a3,
-                                  const BlockLoads& bl, void* W, cudaStream_t st) {
-    const int Cpad = tc_cases_pad(nb), ldb = tc_ldb(D);
-    const size_t total = (size_t)nlev * Cpad * ldb;
-    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
-    k_build_w_old_tc<<<grid, 256, 0, st>>>(u_hist, t_hist, D, S, nb, Cpad, nlev, Lw, a1, a2, a3,
-                                           bl, ldb, static_cast<__nv_bfloat16*>(W));
-    return cudaGetLastError();
-}
-
-bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out) {
+bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out, int nmat) {
     const int ldb = tc_ldb(D);
-    return encode_map(out->a, planes, ldb, D, 4 * L, TC_BM) &&
-           encode_map(out->b, W, ldb, tc_cases_pad(C), 4 * Lw, TC_BN);
+    return encode_map(out->a, planes, ldb, D, 2 * nmat * L, TC_BM) &&
+           encode_map(out->b, W, ldb, tc_cases_pad(C), 2 * nmat * Lw, TC_BN);
 }
 
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
-                           double* partial, int splits, int* d_err, cudaStream_t s) {
+                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat) {
     static unsigned long long attr_set = 0;  // devices with the shared-memory attribute set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -553,18 +493,20 @@ cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, i
         if (e != cudaSuccess) return e;
         attr_set |= 1ull << dev;
     }
-    if (splits < 1 || nlev < 1) return cudaErrorInvalidValue;
+    if (splits < 1 || nlev < 1 || nlev > L || nlev > Lw || (nmat != 1 && nmat != 2))
+        return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
     std::memcpy(&ma, maps.a, sizeof(ma));
     std::memcpy(&mb, maps.b, sizeof(mb));
-    const int per = (nlev + splits - 1) / splits;
     dim3 grid((D + TC_BM - 1) / TC_BM, splits, (C + TC_BN - 1) / TC_BN);
-    k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, per, tc_ldb(D) / TC_BK, C,
-                                                partial, d_err);
+    k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, tc_ldb(D) / TC_BK, nmat,
+                                                C, partial, d_err);
     return cudaGetLastError();
 }
 
-size_t tc_plane_bytes(int D, int L) { return 4 * (size_t)L * D * tc_ldb(D) * 2; }
-size_t tc_w_bytes(int D, int C, int Lw) { return 4 * (size_t)Lw * tc_cases_pad(C) * tc_ldb(D) * 2; }
+size_t tc_plane_bytes(int D, int L, int nmat) { return 2 * nmat * (size_t)L * D * tc_ldb(D) * 2; }
+size_t tc_w_bytes(int D, int C, int Lw, int nmat) {
+    return 2 * nmat * (size_t)Lw * tc_cases_pad(C) * tc_ldb(D) * 2;
+}
 
 }  // namespace tdbem

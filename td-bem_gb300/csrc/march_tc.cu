@@ -1,0 +1,238 @@
+// Mixed march on the tcgen05 tensor cores: one merged level matrix per level.
+//
+// At every dof one of (u_j, t_j) is prescribed and the other is the unknown
+// x_j of the step's solve; the state update (march.cu: k_update_state) writes
+//   u_j = ubc_j,            t_j = x_j                 dof with a prescribed
+//                                                      displacement, j < D-1
+//   u_j = x_j,              t_j = fbc_j amp(m) or 0   every other dof
+// and, for the last dof with a prescribed displacement, u = ubc and t = fbc amp
+// or 0 (the reference's ExtractField leaves it out of its loop).  A history term
+// G^f wt - H^f wu of the march therefore splits, column by column, into
+//   A^f w   with A^f[:, j] = G^f[:, j] (t_j unknown), -H^f[:, j] (u_j unknown),
+//           0 (the last dof above), and w the same combination of x's history,
+// plus the known values' part, a scalar times one of three vectors per level:
+//   pt_f = G^f kt   kt_j = fbc_j where t_j is known and prescribed (history),
+//   pl_f = G^f lt   lt_j = fbc_j at the dofs without a prescribed displacement
+//                   (the step's own load, the known-load terms of levels 0/1),
+//   pu_f = H^f lu   lu_j = ubc_j.
+// The convolution streams A^f (BF16 hi/lo planes, half the bytes of G^f and
+// H^f); the known part is a sum over levels of those vectors with coefficients
+// tabulated per step from the load history.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "tdbem_internal.cuh"
+
+namespace tdbem {
+
+namespace {
+
+// Column selector of A^f: 1 = G (t unknown), 2 = -H (u unknown), 0 = none.
+__device__ __forceinline__ int col_sel(const unsigned char* __restrict__ is_u, int k, int D) {
+    if (k >= D) return 0;
+    if (is_u[k]) return k < D - 1 ? 1 : 0;
+    return 2;
+}
+
+// FP32 levels [f][row][ldf] -> merged planes [plane*L + f][row][ldb] and the known
+// part's vectors known[(v*L + f)*D + row], v = 0 pt, 1 pl, 2 pu.  Block per
+// (f, row), 4 columns per thread (16-byte loads of G and H, 8-byte stores per
+// plane); FP32 products, FP64 block sums.
+__global__ void __launch_bounds__(256) k_merge_levels(
+    const float* __restrict__ Gf, const float* __restrict__ Hf, int ldf, int D, int L, int ldb,
+    const unsigned char* __restrict__ is_u, const float* __restrict__ kt,
+    const float* __restrict__ lt, const float* __restrict__ lu, __nv_bfloat16* __restrict__ P,
+    double* __restrict__ known) {
+    __shared__ double red[3][8];
+    const size_t rows = (size_t)L * D;
+    const size_t plane = rows * ldb;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (size_t fr = blockIdx.x; fr < rows; fr += gridDim.x) {
+        const float* g = Gf + fr * ldf;
+        const float* h = Hf + fr * ldf;
+        __nv_bfloat16* hi_row = P + fr * ldb;
+        __nv_bfloat16* lo_row = P + plane + fr * ldb;
+        float st = 0.f, sl = 0.f, su = 0.f;
+        for (int k = 4 * threadIdx.x; k < ldb; k += 4 * blockDim.x) {
+            float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
+            if (k < ldf) {
+                x = __ldcs(reinterpret_cast<const float4*>(g + k));
+                y = __ldcs(reinterpret_cast<const float4*>(h + k));
+            }
+            const float gv[4] = {x.x, x.y, x.z, x.w}, hv[4] = {y.x, y.y, y.z, y.w};
+            __align__(8) __nv_bfloat16 hb[4], lb[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int c = k + q;
+                const int sel = col_sel(is_u, c, D);
+                const float a = sel == 1 ? gv[q] : sel == 2 ? -hv[q] : 0.f;
+                hb[q] = __float2bfloat16_rn(a);
+                lb[q] = __float2bfloat16_rn(__fsub_rn(a, __bfloat162float(hb[q])));
+                if (c < D) {
+                    st = fmaf(gv[q], kt[c], st);
+                    sl = fmaf(gv[q], lt[c], sl);
+                    su = fmaf(hv[q], lu[c], su);
+                }
+            }
+            *reinterpret_cast<uint2*>(hi_row + k) = *reinterpret_cast<const uint2*>(hb);
+            *reinterpret_cast<uint2*>(lo_row + k) = *reinterpret_cast<const uint2*>(lb);
+        }
+        double v[3] = {st, sl, su};
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+            for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+        if (lane == 0)
+            for (int i = 0; i < 3; i++) red[i][warp] = v[i];
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double s = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+            const size_t f = fr / D, row = fr - f * D;
+            known[((size_t)threadIdx.x * L + f) * D + row] = s;
+        }
+        __syncthreads();
+    }
+}
+
+// x's history combination of level f for step s over history steps [lo, hi)
+// (the W terms of march_mixed.cu's k_build_w_old / k_build_w_cross).
+__device__ __forceinline__ double w_of(const double* __restrict__ hist, int D, int k, int s,
+                                       int f, int lo, int hi, double a1, double a2, double a3) {
+    double w = 0;
+    const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
+    if (f >= 2 && m1 >= lo && m1 < hi) w += a1 * hist[(size_t)m1 * D + k];
+    if (f >= 1 && m3 >= lo && m3 < hi) w += a3 * hist[(size_t)m3 * D + k];
+    if (m2 >= lo && m2 < hi) w += a2 * hist[(size_t)m2 * D + k];
+    if (f == 0 && s - 1 >= lo && s - 1 < hi) w -= a1 * hist[(size_t)(s - 1) * D + k];
+    return w;
+}
+
+// Merged history vectors [plane*Lw + f][j][ldb] (j < Cpad, zero beyond ncol and D)
+// of the steps s0 + j over history steps [lo, hi).
+__global__ void k_build_w_merged(const double* __restrict__ u_hist,
+                                 const double* __restrict__ t_hist,
+                                 const unsigned char* __restrict__ is_u, int D, int s0, int ncol,
+                                 int Cpad, int lo, int hi, int nlev, int Lw, double a1, double a2,
+                                 double a3, int ldb, __nv_bfloat16* __restrict__ W) {
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const size_t plane = (size_t)Lw * Cpad * ldb;
+    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(idx % ldb);
+        const int j = (int)((idx / ldb) % Cpad);
+        const int f = (int)(idx / ((size_t)ldb * Cpad));
+        double w = 0;
+        if (j < ncol) {
+            const int sel = col_sel(is_u, k, D);
+            if (sel)
+                w = w_of(sel == 1 ? t_hist : u_hist, D, k, s0 + j, f, lo, hi, a1, a2, a3);
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn((float)w);
+        W[idx] = h;
+        W[plane + idx] = __float2bfloat16_rn((float)(w - (double)__bfloat162float(h)));
+    }
+}
+
+// Y[j][row] += sum_f ( ct pt_f + cl pl_f - cu pu_f )[row] for the steps S + j,
+// j < nbe, with (ct, cl, cu) = coef[(S + j) * L + f] (zero where the level has no
+// term).  Thread per row.
+constexpr int kKnownMaxSteps = 16;
+__global__ void __launch_bounds__(128) k_known_terms(const double* __restrict__ known,
+                                                     const double3* __restrict__ coef, int D,
+                                                     int L, int S, int nbe,
+                                                     double* __restrict__ Y) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= D) return;
+    double acc[kKnownMaxSteps];
+#pragma unroll
+    for (int j = 0; j < kKnownMaxSteps; j++) acc[j] = 0;
+    const int flast = min(L - 1, S + nbe - 1);
+    for (int f = 0; f <= flast; f++) {
+        const double pt = known[(size_t)f * D + row];
+        const double pl = known[((size_t)L + f) * D + row];
+        const double pu = known[((size_t)2 * L + f) * D + row];
+#pragma unroll
+        for (int j = 0; j < kKnownMaxSteps; j++)
+            if (j < nbe) {
+                const double3 c = coef[(size_t)(S + j) * L + f];
+                acc[j] += c.x * pt + c.y * pl - c.z * pu;
+            }
+    }
+#pragma unroll
+    for (int j = 0; j < kKnownMaxSteps; j++)
+        if (j < nbe) Y[(size_t)j * D + row] += acc[j];
+}
+
+}  // namespace
+
+cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
+                                const unsigned char* is_u, const float* kt, const float* lt,
+                                const float* lu, void* planes, double* known, cudaStream_t s) {
+    const int ldb = tc_ldb(D);
+    if (ldf % 4 != 0 || ldf > ldb) return cudaErrorInvalidValue;  // float4 rows inside ldb
+    const size_t rows = (size_t)L * D;
+    const unsigned grid = (unsigned)std::min<size_t>(rows, 152 * 8);
+    k_merge_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, ldb, is_u, kt, lt, lu,
+                                        static_cast<__nv_bfloat16*>(planes), known);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
+                                  const unsigned char* is_u, int D, int s0, int ncol, int Cmax,
+                                  int lo, int hi, int nlev, int Lw, double a1, double a2,
+                                  double a3, void* W, cudaStream_t st) {
+    if (ncol < 1 || ncol > Cmax || nlev < 1 || nlev > Lw) return cudaErrorInvalidValue;
+    const int Cpad = tc_cases_pad(Cmax), ldb = tc_ldb(D);
+    const size_t total = (size_t)nlev * Cpad * ldb;
+    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
+    k_build_w_merged<<<grid, 256, 0, st>>>(u_hist, t_hist, is_u, D, s0, ncol, Cpad, lo, hi, nlev,
+                                           Lw, a1, a2, a3, ldb, static_cast<__nv_bfloat16*>(W));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int S,
+                               int nbe, double* Y, cudaStream_t s) {
+    if (nbe < 1 || nbe > kKnownMaxSteps) return cudaErrorInvalidValue;
+    k_known_terms<<<(D + 127) / 128, 128, 0, s>>>(known, static_cast<const double3*>(coef), D, L,
+                                                  S, nbe, Y);
+    return cudaGetLastError();
+}
+
+// Coefficients (ct, cl, cu) of the known part for the steps 0..numstep and levels
+// 0..L-1 (see the header): the history terms of the W combination with m >= 1,
+// amp(m) on the prescribed tractions, 1 on the prescribed displacements, and the
+// step's own load with lhs_c0/lhs_c1 at levels 0/1 (step 1: 1 and 0).
+void known_coefficients(int numstep, int L, double a1, double a2, double a3,
+                        const std::vector<double>& amp, double c0, double c1,
+                        std::vector<double>& out) {
+    out.assign((size_t)(numstep + 1) * L * 3, 0.0);
+    auto A = [&](int m) { return amp.empty() ? 1.0 : amp[m]; };
+    for (int s = 1; s <= numstep; s++)
+        for (int f = 0; f < L && f <= s; f++) {
+            double ct = 0, cu = 0;
+            auto term = [&](int m, double w) {
+                if (m >= 1 && m <= s - 1) {
+                    ct += w * A(m);
+                    cu += w;
+                }
+            };
+            if (f >= 2) term(s + 1 - f, a1);
+            if (f >= 1) term(s - f, a3);
+            term(s - 1 - f, a2);
+            if (f == 0) term(s - 1, -a1);
+            double cl = 0;
+            if (f <= 1) {
+                const double cf = f == 0 ? (s == 1 ? 1.0 : c0) : (s == 1 ? 0.0 : c1);
+                cl = cf * A(s);
+                cu += cf;
+            }
+            double* o = &out[((size_t)s * L + f) * 3];
+            o[0] = ct;
+            o[1] = cl;
+            o[2] = cu;
+        }
+}
+
+}  // namespace tdbem

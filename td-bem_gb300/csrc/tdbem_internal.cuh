@@ -235,9 +235,13 @@ struct TcMaps {
 };
 int tc_ldb(int D);
 int tc_cases_pad(int C);
-int tc_conv_splits(int nlev, int D, int C);
-size_t tc_plane_bytes(int D, int L);
-size_t tc_w_bytes(int D, int C, int Lw);
+// Grid splits of a k_conv_tc launch (each writes its own partial sums: at most
+// max_splits of them fit the caller's buffer).
+// nmat = 2: G and H planes (batched convolution); 1: the mixed march's merged
+// level matrix (march_tc.cu).
+int tc_conv_splits(int nlev, int D, int C, int max_splits = 1 << 30, int nmat = 2);
+size_t tc_plane_bytes(int D, int L, int nmat = 2);
+size_t tc_w_bytes(int D, int C, int Lw, int nmat = 2);
 cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
                                 void* planes, cudaStream_t s);
 cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D, int C, int s,
@@ -245,13 +249,25 @@ cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D,
                               double c1, const double* amp, int numstep, const double* traction,
                               const unsigned char* is_u, const double* ubc_val, void* W,
                               cudaStream_t st);
-// Old-history vectors of a time block of the mixed march as BF16 planes (nb columns).
-cudaError_t launch_build_w_old_tc(const double* u_hist, const double* t_hist, int D, int S,
-                                  int nb, int nlev, int Lw, double a1, double a2, double a3,
-                                  const BlockLoads& bl, void* W, cudaStream_t st);
-bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out);
+bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out,
+                  int nmat = 2);
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
-                           double* partial, int splits, int* d_err, cudaStream_t s);
+                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 2);
+
+// Mixed march with merged levels on tcgen05 (march_tc.cu).
+cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
+                                const unsigned char* is_u, const float* kt, const float* lt,
+                                const float* lu, void* planes, double* known, cudaStream_t s);
+cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
+                                  const unsigned char* is_u, int D, int s0, int ncol, int Cmax,
+                                  int lo, int hi, int nlev, int Lw, double a1, double a2,
+                                  double a3, void* W, cudaStream_t st);
+cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int S,
+                               int nbe, double* Y, cudaStream_t s);
+void known_coefficients(int numstep, int L, double a1, double a2, double a3,
+                        const std::vector<double>& amp, double c0, double c1,
+                        std::vector<double>& out);
+
 
 // Sets the calling thread's tdbem_last_error() message (capi.cu).
 void note_error(const char* msg);
@@ -397,6 +413,16 @@ struct tdbem_ctx {
     tdbem::TcMaps mtc_maps{};
     const void* mtc_maps_for[2] = {nullptr, nullptr};
     int mtc_nb = 0;
+    // merged level planes of the tcgen05 march (march_tc.cu), the known part's
+    // vectors (pt, pl, pu per level), the BC vectors they come from (kt, lt, lu)
+    // and the per-step coefficients with the key they were built for
+    void* d_mtc_planes = nullptr;
+    double* d_mtc_known = nullptr;
+    bool mtc_planes_valid = false;
+    float* d_mtc_bc = nullptr;
+    double* d_mtc_coef = nullptr;
+    size_t mtc_coef_cap = 0;
+    std::vector<double> mtc_coef_key;
     // stepwise marching (tdbem_march_begin / tdbem_march_step) and host-block levels
     bool use_graphs = true;         // replay the marching loop as a CUDA graph
     MarchGraph graph;

@@ -26,12 +26,15 @@ def rel_l2(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
-def run(lib, m, precision, alpha=(0.25, 0.0), block=12, refine=1, numstep=None, engine=None):
+def run(lib, m, precision, alpha=(0.25, 0.0), block=12, refine=1, numstep=None, engine=None,
+        amp=None):
     with lib.Context(m) as ctx:
         ctx.set_alpha(*alpha)
         ctx.set_march_options(block, refine)
         if engine is not None:
             ctx.set_march_engine(engine)
+        if amp is not None:
+            ctx.set_load_history(amp)
         ctx.assemble(precision=precision)
         u, t = ctx.march(numstep)
         lev = (ctx.level(3, 0), ctx.level(3, 1), ctx.level(ctx.M, 1))
@@ -66,6 +69,53 @@ def test_mixed_bar_with_prescribed_displacements(tdlib):
     u, t, _ = run(tdlib, m, tdlib.FP64, alpha=(0.25, 0.1))
     u32, t32, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1))
     assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
+
+
+def bar_with_prescribed_values(seed=3):
+    """The alpha bar with nonzero prescribed displacements, and its last dof both
+    displacement- and traction-prescribed (the state update keeps the prescribed
+    traction in that dof's history)."""
+    import copy
+    _, m = load_golden("bar_1x1x4_q2_alpha")
+    m = copy.copy(m)
+    D = 3 * m.nnd
+    rng = np.random.default_rng(seed)
+    m.ubc_dofs = np.unique(np.append(m.ubc_dofs, D - 1)).astype(np.int32)
+    m.ubc_vals = 1e-3 * rng.standard_normal(len(m.ubc_dofs))
+    m.fbc_dofs = np.append(m.fbc_dofs, D - 1).astype(np.int32)
+    m.fbc_vals = np.append(m.fbc_vals, 0.5 * np.abs(m.fbc_vals).max())
+    return m
+
+
+@pytest.mark.parametrize("engine", ["tcgen05", "fp32"])
+def test_mixed_prescribed_values_and_load_history(tdlib, engine):
+    """Known values in every history term: nonzero prescribed displacements, a
+    prescribed traction on a displacement-prescribed last dof, and a ramped load
+    history, in both march engines against the plain FP64 march."""
+    m = bar_with_prescribed_values()
+    amp = np.minimum(1.0, np.arange(m.numstep + 1) / 20.0)
+    eng = tdlib.ENGINE_TCGEN05 if engine == "tcgen05" else tdlib.ENGINE_FP32
+    u, t, _ = run(tdlib, m, tdlib.FP64, alpha=(0.25, 0.1), amp=amp)
+    for block in (4, 16):
+        u32, t32, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1), amp=amp, engine=eng,
+                          block=block)
+        assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
+
+
+def test_new_boundary_values_reach_the_merged_levels(tdlib):
+    """tdbem_set_bc between two marches of one assembly: the second march uses the
+    new values (the merged levels and their known part are rebuilt)."""
+    _, m0 = load_golden("bar_1x1x4_q2_alpha")
+    m1 = bar_with_prescribed_values()
+    ref, _, _ = run(tdlib, m1, tdlib.MIXED, alpha=(0.25, 0.1))
+    with tdlib.Context(m0) as ctx:
+        ctx.set_alpha(0.25, 0.1)
+        ctx.set_march_options(12, 1)
+        ctx.assemble(precision=tdlib.MIXED)
+        ctx.march()
+        ctx.set_bc(m1.ubc_dofs, m1.ubc_vals, m1.fbc_dofs, m1.fbc_vals)
+        u, _ = ctx.march()
+    assert np.array_equal(u, ref)
 
 
 def test_mixed_q8_bar(tdlib):
