@@ -968,8 +968,11 @@ __global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
 // surface, with the reference's regular / Duffy quadrature per element.  One
 // block per node, fixed-order tree reduction; the result goes to cbuf[c][9].
 // C term of node c, computed by the whole block (256 threads), into dst[9].  A
-// singular 8-node element contributes through its 4-node sub-elements.
-template <int ENND = 4>
+// singular 8-node element contributes through its 4-node sub-elements.  FAST (the
+// mixed-precision assembly): a regular element's points in FP32 from their FP64
+// offsets to the node, summed in FP32 per element and in FP64 across elements
+// (relative error ~1e-7 of C); singular elements as in the FP64 form.
+template <int ENND = 4, bool FAST = false>
 __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const int* __restrict__ ien, int nel, int c, int nq,
                                            const double* __restrict__ gx,
@@ -995,6 +998,31 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
         int nsub = 1;
         if (ENND == 8 && sing >= 0) nsub = q8_subelements(sing, ids, cid);
         const int npts = sing < 0 ? nq2 : nsub * 2 * nq2;
+        if (FAST && sing < 0) {
+            const float onem2nu_f = (float)onem2nu, kscale_f = (float)kscale;
+            float a32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for (int qq = 0; qq < nq2; qq++) {
+                const double* g = geom + ((size_t)e * nq2 + qq) * stride;
+                const float d0 = (float)(g[0] - xc[0]), d1 = (float)(g[1] - xc[1]),
+                            d2 = (float)(g[2] - xc[2]);
+                const float nv[3] = {(float)g[3], (float)g[4], (float)g[5]};
+                const float inv_r = rsqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+                const float rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
+                const float w = (float)g[6] * (kscale_f * inv_r * inv_r);
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int kk = 0; kk < 3; kk++) {
+                        const float Kki = ((kk == i ? onem2nu_f : 0.f) + 3.f * rv[kk] * rv[i]) * rdn -
+                                          onem2nu_f * (rv[i] * nv[kk] - rv[kk] * nv[i]);
+                        a32[i * 3 + kk] -= w * Kki;
+                    }
+            }
+#pragma unroll
+            for (int m = 0; m < 9; m++) acc[m] += (double)a32[m];
+            continue;
+        }
         double cn[12];
         int cur = -1;
         for (int qq = 0; qq < npts; qq++) {
@@ -1043,7 +1071,7 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
     if (threadIdx.x < 9) dst[threadIdx.x] = red[threadIdx.x][0];
 }
 
-template <int ENND>
+template <int ENND, bool FAST>
 __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords,
                                                const int* __restrict__ ien, int nel,
                                                int node_lo, int nq,
@@ -1051,8 +1079,8 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
                                                const double* __restrict__ gw,
                                                const double* __restrict__ geom, Phys ph,
                                                double* __restrict__ cbuf) {
-    cterm_node<ENND>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
-                     cbuf + (size_t)blockIdx.x * 9);
+    cterm_node<ENND, FAST>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
+                           cbuf + (size_t)blockIdx.x * 9);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -1230,12 +1258,24 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
 
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
-                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s) {
+                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
+                         bool fast) {
     if (nnodes == 0) return cudaSuccess;
-    if (ennd == 8)
-        k_cterm<8><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
-    else
-        k_cterm<4><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph, cbuf);
+    if (ennd == 8) {
+        if (fast)
+            k_cterm<8, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
+                                                    cbuf);
+        else
+            k_cterm<8, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
+                                                     ph, cbuf);
+    } else {
+        if (fast)
+            k_cterm<4, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
+                                                    cbuf);
+        else
+            k_cterm<4, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
+                                                     ph, cbuf);
+    }
     return cudaGetLastError();
 }
 

@@ -1241,10 +1241,10 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, o64);
             if (rc != TDBEM_OK) return rc;
         }
-        // the C term (the FP32 store takes it after the far field)
+        // the C term, regular elements in FP32 (the FP32 store takes it after the far field)
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
-                              c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream));
+                              c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
                                     c->stream));
         prof_end(c, pc, 0, 0);

@@ -37,25 +37,26 @@ __device__ __forceinline__ int col_sel(const unsigned char* __restrict__ is_u, i
 }
 
 // FP32 levels [f][row][ldf] -> merged planes [plane*L + f][row][ldb] and the known
-// part's vectors known[(v*L + f)*D + row], v = 0 pt, 1 pl, 2 pu.  Block per
-// (f, row), 4 columns per thread (16-byte loads of G and H, 8-byte stores per
-// plane); FP32 products, FP64 block sums.
+// part's vectors known[(v*L + f)*D + row], v = 0 pt, 1 pl, 2 pu.  Warp per
+// (f, row), 4 columns per lane (16-byte loads of G and H, 8-byte stores per
+// plane); FP32 products, FP64 warp sums.
 __global__ void __launch_bounds__(256) k_merge_levels(
     const float* __restrict__ Gf, const float* __restrict__ Hf, int ldf, int D, int L, int ldb,
     const unsigned char* __restrict__ is_u, const float* __restrict__ kt,
     const float* __restrict__ lt, const float* __restrict__ lu, __nv_bfloat16* __restrict__ P,
     double* __restrict__ known) {
-    __shared__ double red[3][8];
     const size_t rows = (size_t)L * D;
     const size_t plane = rows * ldb;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (size_t fr = blockIdx.x; fr < rows; fr += gridDim.x) {
+    const int lane = threadIdx.x & 31;
+    const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
+    for (size_t fr = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); fr < rows;
+         fr += nwarps) {
         const float* g = Gf + fr * ldf;
         const float* h = Hf + fr * ldf;
         __nv_bfloat16* hi_row = P + fr * ldb;
         __nv_bfloat16* lo_row = P + plane + fr * ldb;
         float st = 0.f, sl = 0.f, su = 0.f;
-        for (int k = 4 * threadIdx.x; k < ldb; k += 4 * blockDim.x) {
+        for (int k = 4 * lane; k < ldb; k += 128) {
             float4 x = make_float4(0.f, 0.f, 0.f, 0.f), y = x;
             if (k < ldf) {
                 x = __ldcs(reinterpret_cast<const float4*>(g + k));
@@ -83,16 +84,10 @@ __global__ void __launch_bounds__(256) k_merge_levels(
 #pragma unroll
         for (int i = 0; i < 3; i++)
             for (int o = 16; o > 0; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
-        if (lane == 0)
-            for (int i = 0; i < 3; i++) red[i][warp] = v[i];
-        __syncthreads();
-        if (threadIdx.x < 3) {
-            double s = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[threadIdx.x][w];
+        if (lane < 3) {
             const size_t f = fr / D, row = fr - f * D;
-            known[((size_t)threadIdx.x * L + f) * D + row] = s;
+            known[((size_t)lane * L + f) * D + row] = lane == 0 ? v[0] : lane == 1 ? v[1] : v[2];
         }
-        __syncthreads();
     }
 }
 
@@ -173,7 +168,7 @@ cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D
     const int ldb = tc_ldb(D);
     if (ldf % 4 != 0 || ldf > ldb) return cudaErrorInvalidValue;  // float4 rows inside ldb
     const size_t rows = (size_t)L * D;
-    const unsigned grid = (unsigned)std::min<size_t>(rows, 152 * 8);
+    const unsigned grid = (unsigned)std::min<size_t>((rows + 7) / 8, 152 * 8);
     k_merge_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, ldb, is_u, kt, lt, lu,
                                         static_cast<__nv_bfloat16*>(planes), known);
     return cudaGetLastError();

@@ -89,7 +89,8 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      unsigned long long* nitems, cudaStream_t s);
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
-                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s);
+                         const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
+                         bool fast = false);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
                                int if_ext, int mode, const AsmOut& out, cudaStream_t s);
 size_t scan_temp_bytes(unsigned n);

@@ -55,6 +55,23 @@ def test_mixed_levels_close_to_fp64(tdlib, sphere8):
         assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
 
 
+def test_mixed_c_term_close_to_fp64(tdlib):
+    """Levels 0 and 1 of the mixed form (the LHS of its solves) hold the C term,
+    its regular elements in FP32: the diagonal blocks stay within 1e-6 of FP64."""
+    from tdbem import meshes
+    m = meshes.cubed_sphere(4, numstep=20)
+    out = {}
+    for prec in (tdlib.FP64, tdlib.MIXED):
+        with tdlib.Context(m) as ctx:
+            ctx.assemble(precision=prec)
+            out[prec] = [ctx.level(k, 1) for k in (0, 1)]
+    n = 3 * m.nnd
+    blk = np.kron(np.eye(m.nnd), np.ones((3, 3))) > 0
+    for a, b in zip(out[tdlib.MIXED], out[tdlib.FP64]):
+        assert a.shape == (n, n)
+        assert np.abs(a - b)[blk].max() <= 1e-6 * np.abs(b[blk]).max()
+
+
 @pytest.mark.parametrize("block", [1, 8, 12, 16])
 def test_mixed_histories_within_1e4(tdlib, sphere8, block):
     m, (u, t, _) = sphere8
