@@ -363,7 +363,7 @@ def run_ours(args, dist):
     ctx = lib.Context(model)
     ctx.set_alpha(*ALPHA)
     engine = lib.ENGINE_TCGEN05 if args.engine == "tcgen05" else lib.ENGINE_MMA_SYNC
-    refine = args.refine if args.refine is not None else (0 if cases else 1)
+    refine = args.refine if args.refine is not None else 0
     march_engine = lib.ENGINE_TCGEN05 if args.march_engine == "tcgen05" else lib.ENGINE_FP32
     ctx.set_march_options(args.block, refine)
     ctx.set_march_engine(march_engine)
@@ -731,8 +731,7 @@ def main():
                     help="skip the plain FP64 run that measures the mixed form's error")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--refine", type=int, default=None,
-                    help="refinement sweeps of the mixed-precision solves (0..4; default 1, "
-                         "0 for batched workloads)")
+                    help="FP64 refinement sweeps of the mixed-precision solves (0..4; default 0)")
     ap.add_argument("--engine", choices=["tcgen05", "mma_sync"], default="tcgen05",
                     help="tensor-core engine of the batched convolution")
     ap.add_argument("--march-engine", choices=["tcgen05", "fp32"], default="tcgen05",

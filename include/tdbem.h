@@ -244,7 +244,9 @@ int tdbem_set_march_engine(tdbem_ctx* ctx, int engine);
  * history convolution (1, 4, 6, 8, 12 or 16; default 16, the fastest on GB300 for
  * the 4614-DOF sphere with the tcgen05 engine; 8 is the fastest with the FP32
  * engine), refine_sweeps = FP64 residual-refinement sweeps per solve
- * (0..4; default 1). */
+ * (0..4; default 0: on the 4614-DOF sphere the FP32 inverse alone is within
+ * 2.4e-7 of FP64, below the tcgen05 engine's convolution error of ~1e-5; the
+ * sweeps are for LHS matrices whose FP32 inverse is less accurate). */
 int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
 
 /* Device pointers of the histories of the last tdbem_march (FP64,

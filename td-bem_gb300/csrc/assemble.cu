@@ -969,16 +969,20 @@ __global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
 // block per node, fixed-order tree reduction; the result goes to cbuf[c][9].
 // C term of node c, computed by the whole block (256 threads), into dst[9].  A
 // singular 8-node element contributes through its 4-node sub-elements.  FAST (the
-// mixed-precision assembly): a regular element's points in FP32 from their FP64
-// offsets to the node, summed in FP32 per element and in FP64 across elements
-// (relative error ~1e-7 of C); singular elements as in the FP64 form.
+// mixed-precision assembly): a regular element's points in FP32, summed in FP32
+// per element and in FP64 across elements (relative error ~1e-7 of C); for 4-node
+// elements from the FP32 geometry table (points relative to the element's first
+// node, so the only FP64 arithmetic is the node's offset to that node, once per
+// element), for 8-node elements from the FP64 points' offsets to the node;
+// singular elements as in the FP64 form.
 template <int ENND = 4, bool FAST = false>
 __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const int* __restrict__ ien, int nel, int c, int nq,
                                            const double* __restrict__ gx,
                                            const double* __restrict__ gw,
                                            const double* __restrict__ geom, const Phys& ph,
-                                           double* __restrict__ dst) {
+                                           double* __restrict__ dst,
+                                           const float* __restrict__ geomf = nullptr) {
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int nq2 = nq * nq;
@@ -1001,15 +1005,36 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
         if (FAST && sing < 0) {
             const float onem2nu_f = (float)onem2nu, kscale_f = (float)kscale;
             float a32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            // the node relative to the element's first node (4-node FP32 table)
+            const float xr[3] = {(float)(xc[0] - en[0]), (float)(xc[1] - en[1]),
+                                 (float)(xc[2] - en[2])};
             for (int qq = 0; qq < nq2; qq++) {
-                const double* g = geom + ((size_t)e * nq2 + qq) * stride;
-                const float d0 = (float)(g[0] - xc[0]), d1 = (float)(g[1] - xc[1]),
-                            d2 = (float)(g[2] - xc[2]);
-                const float nv[3] = {(float)g[3], (float)g[4], (float)g[5]};
+                float d0, d1, d2, nv[3], wJf;
+                if (ENND == 4 && geomf) {
+                    const float4* g4 =
+                        reinterpret_cast<const float4*>(geomf + ((size_t)e * nq2 + qq) * 12);
+                    const float4 p0 = __ldg(g4), p1 = __ldg(g4 + 1);
+                    d0 = p0.x - xr[0];
+                    d1 = p0.y - xr[1];
+                    d2 = p0.z - xr[2];
+                    nv[0] = p0.w;
+                    nv[1] = p1.x;
+                    nv[2] = p1.y;
+                    wJf = p1.z;
+                } else {
+                    const double* g = geom + ((size_t)e * nq2 + qq) * stride;
+                    d0 = (float)(g[0] - xc[0]);
+                    d1 = (float)(g[1] - xc[1]);
+                    d2 = (float)(g[2] - xc[2]);
+                    nv[0] = (float)g[3];
+                    nv[1] = (float)g[4];
+                    nv[2] = (float)g[5];
+                    wJf = (float)g[6];
+                }
                 const float inv_r = rsqrtf(d0 * d0 + d1 * d1 + d2 * d2);
                 const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
                 const float rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
-                const float w = (float)g[6] * (kscale_f * inv_r * inv_r);
+                const float w = wJf * (kscale_f * inv_r * inv_r);
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -1078,9 +1103,10 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
                                                const double* __restrict__ gx,
                                                const double* __restrict__ gw,
                                                const double* __restrict__ geom, Phys ph,
-                                               double* __restrict__ cbuf) {
+                                               double* __restrict__ cbuf,
+                                               const float* __restrict__ geomf) {
     cterm_node<ENND, FAST>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
-                           cbuf + (size_t)blockIdx.x * 9);
+                           cbuf + (size_t)blockIdx.x * 9, geomf);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -1259,22 +1285,22 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
-                         bool fast) {
+                         bool fast, const float* geomf) {
     if (nnodes == 0) return cudaSuccess;
     if (ennd == 8) {
         if (fast)
             k_cterm<8, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
-                                                    cbuf);
+                                                    cbuf, nullptr);
         else
             k_cterm<8, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf);
+                                                     ph, cbuf, nullptr);
     } else {
         if (fast)
             k_cterm<4, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
-                                                    cbuf);
+                                                    cbuf, geomf);
         else
             k_cterm<4, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf);
+                                                     ph, cbuf, nullptr);
     }
     return cudaGetLastError();
 }

@@ -220,6 +220,8 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_mtc_coef);
     c->mtc_coef_cap = 0;
     c->mtc_coef_key.clear();
+    dfree(c->d_mtc_yk);
+    c->mtc_yk_cap = 0;
 
     if (c->d_Ainv[1] == c->d_Ainv[0]) c->d_Ainv[1] = nullptr;
     dfree(c->d_Ainv[0]);
@@ -582,6 +584,13 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                                      cudaMemcpyHostToDevice, s));
             c->mtc_coef_key = key;
         }
+        const size_t yk = (size_t)(numstep + 1) * D;
+        if (c->mtc_yk_cap < yk) {
+            dfree(c->d_mtc_yk);
+            c->mtc_yk_cap = 0;
+            CUDA_TRY(dalloc(&c->d_mtc_yk, yk));
+            c->mtc_yk_cap = yk;
+        }
         const size_t wb = tc_w_bytes(D, nb, Lw, 1);
         if (c->mtc_W_bytes < wb) {
             if (c->d_mtc_W) cudaFree(c->d_mtc_W);
@@ -613,7 +622,7 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         c->d_x,       c->d_res,     c->d_dx,      c->d_load_t,  c->d_load_u,   c->d_is_ubc,
         c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map, tc ? c->d_mtc_planes : nullptr,
         tc ? c->d_mtc_W : nullptr,  tc ? c->d_tc_err : nullptr,  tc ? c->d_mtc_known : nullptr,
-        tc ? c->d_mtc_coef : nullptr};
+        tc ? c->d_mtc_coef : nullptr, tc ? c->d_mtc_yk : nullptr};
     // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
     // Old pass: history before the block and the steps' known-load terms.
     auto old_pass = [&](int S, int nbe) -> int {
@@ -630,8 +639,10 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         }
         if (tc) {  // merged levels, split-BF16 products on the tensor cores
             double* Y = c->d_Yold;
+            const double* yk = c->d_mtc_yk + (size_t)S * D;  // the steps' known part
             if (S == 1) {  // no unknown history before the first block
-                CUDA_TRY(cudaMemsetAsync(Y, 0, sizeof(double) * nbe * D, s));
+                CUDA_TRY(cudaMemcpyAsync(Y, yk, sizeof(double) * nbe * D,
+                                         cudaMemcpyDeviceToDevice, s));
             } else {
                 CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, S, nbe, nb, 1, S,
                                                nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
@@ -643,13 +654,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                 prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                     nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                          nlev * 2.0 * nbe * (double)DD);
-                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, nullptr, Y, s));
+                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, yk, Y, s));
                 c->launches += 3;
             }
-            const int pk = prof_begin(c, TDBEM_K_AUX);
-            CUDA_TRY(launch_known_terms(c->d_mtc_known, c->d_mtc_coef, D, M + 1, S, nbe, Y, s));
-            prof_end(c, pk, 3.0 * (std::min(M, S + nbe - 1) + 1) * D * 8, 0);
-            c->launches += 1;
             return TDBEM_OK;
         }
         CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, bl, ldw,
@@ -728,6 +735,13 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         return r;
     };
     const int lrc = run_march_loop(c, 1, numstep, ptrs, [&]() -> int {
+        if (tc) {  // the known part of every step's right-hand side
+            const int pk = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_known_terms(c->d_mtc_known, c->d_mtc_coef, D, M + 1, last_s,
+                                        c->d_mtc_yk, s));
+            prof_end(c, pk, 3.0 * (M + 1) * D * 8 * ((last_s + 15) / 16) + 8.0 * last_s * D, 0);
+            c->launches += 1;
+        }
         for (int S = 1; S <= last_s; S += nb) {
             const int nbe = std::min(nb, last_s - S + 1);
             int r = old_pass(S, nbe);
@@ -1244,7 +1258,8 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         // the C term, regular elements in FP32 (the FP32 store takes it after the far field)
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
-                              c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true));
+                              c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true,
+                              c->d_geomf));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
                                     c->stream));
         prof_end(c, pc, 0, 0);
@@ -2398,7 +2413,7 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
         // tcgen05 march: merged planes, history planes, known part and its coefficients
         b += tc_plane_bytes((int)D, (int)L, 1) + tc_w_bytes((int)D, 16, (int)L, 1) +
-             3 * L * D * 8 + (numstep + 1) * L * 3 * 8 + 3 * D * 4;
+             3 * L * D * 8 + (numstep + 1) * (L * 3 + D) * 8 + 3 * D * 4;
     }
     *bytes = b;
     return TDBEM_OK;

@@ -104,42 +104,40 @@ __device__ __forceinline__ double w_of(const double* __restrict__ hist, int D, i
     return w;
 }
 
-// Merged history vectors [plane*Lw + f][j][ldb] (j < Cpad, zero beyond ncol and D)
-// of the steps s0 + j over history steps [lo, hi).
-__global__ void k_build_w_merged(const double* __restrict__ u_hist,
-                                 const double* __restrict__ t_hist,
-                                 const unsigned char* __restrict__ is_u, int D, int s0, int ncol,
-                                 int Cpad, int lo, int hi, int nlev, int Lw, double a1, double a2,
-                                 double a3, int ldb, __nv_bfloat16* __restrict__ W) {
-    const size_t total = (size_t)nlev * Cpad * ldb;
+// Merged history vectors [plane*Lw + f][j][ldb] of the steps s0 + j (j < ncol,
+// zero beyond D) over history steps [lo, hi).  Columns ncol..Cpad-1 are left as
+// they are: the product's output columns are independent and those are not read.
+// Grid (K tiles, ncol, nlev).
+__global__ void __launch_bounds__(256) k_build_w_merged(
+    const double* __restrict__ u_hist, const double* __restrict__ t_hist,
+    const unsigned char* __restrict__ is_u, int D, int s0, int Cpad, int lo, int hi, int Lw,
+    double a1, double a2, double a3, int ldb, __nv_bfloat16* __restrict__ W) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, f = blockIdx.z;
+    if (k >= ldb) return;
+    double w = 0;
+    const int sel = col_sel(is_u, k, D);
+    if (sel) w = w_of(sel == 1 ? t_hist : u_hist, D, k, s0 + j, f, lo, hi, a1, a2, a3);
+    const size_t idx = ((size_t)f * Cpad + j) * ldb + k;
     const size_t plane = (size_t)Lw * Cpad * ldb;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)(idx % ldb);
-        const int j = (int)((idx / ldb) % Cpad);
-        const int f = (int)(idx / ((size_t)ldb * Cpad));
-        double w = 0;
-        if (j < ncol) {
-            const int sel = col_sel(is_u, k, D);
-            if (sel)
-                w = w_of(sel == 1 ? t_hist : u_hist, D, k, s0 + j, f, lo, hi, a1, a2, a3);
-        }
-        const __nv_bfloat16 h = __float2bfloat16_rn((float)w);
-        W[idx] = h;
-        W[plane + idx] = __float2bfloat16_rn((float)(w - (double)__bfloat162float(h)));
-    }
+    const __nv_bfloat16 h = __float2bfloat16_rn((float)w);
+    W[idx] = h;
+    W[plane + idx] = __float2bfloat16_rn((float)(w - (double)__bfloat162float(h)));
 }
 
-// Y[j][row] += sum_f ( ct pt_f + cl pl_f - cu pu_f )[row] for the steps S + j,
-// j < nbe, with (ct, cl, cu) = coef[(S + j) * L + f] (zero where the level has no
-// term).  Thread per row.
+// Known part of the right-hand sides of every solve step, once per march:
+// Yk[s][row] = sum_f ( ct pt_f + cl pl_f - cu pu_f )[row] with (ct, cl, cu) =
+// coef[s * L + f], for the steps s = 1 + blockIdx.y * nbs + j (j < nbs, s <= last).
+// Thread per row.
 constexpr int kKnownMaxSteps = 16;
 __global__ void __launch_bounds__(128) k_known_terms(const double* __restrict__ known,
                                                      const double3* __restrict__ coef, int D,
-                                                     int L, int S, int nbe,
-                                                     double* __restrict__ Y) {
+                                                     int L, int nbs, int last,
+                                                     double* __restrict__ Yk) {
     const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= D) return;
+    const int S = 1 + blockIdx.y * nbs;
+    const int nbe = min(nbs, last - S + 1);
+    if (row >= D || nbe < 1) return;
     double acc[kKnownMaxSteps];
 #pragma unroll
     for (int j = 0; j < kKnownMaxSteps; j++) acc[j] = 0;
@@ -157,7 +155,7 @@ __global__ void __launch_bounds__(128) k_known_terms(const double* __restrict__ 
     }
 #pragma unroll
     for (int j = 0; j < kKnownMaxSteps; j++)
-        if (j < nbe) Y[(size_t)j * D + row] += acc[j];
+        if (j < nbe) Yk[(size_t)(S + j) * D + row] = acc[j];
 }
 
 }  // namespace
@@ -180,18 +178,19 @@ cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
                                   double a3, void* W, cudaStream_t st) {
     if (ncol < 1 || ncol > Cmax || nlev < 1 || nlev > Lw) return cudaErrorInvalidValue;
     const int Cpad = tc_cases_pad(Cmax), ldb = tc_ldb(D);
-    const size_t total = (size_t)nlev * Cpad * ldb;
-    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
-    k_build_w_merged<<<grid, 256, 0, st>>>(u_hist, t_hist, is_u, D, s0, ncol, Cpad, lo, hi, nlev,
-                                           Lw, a1, a2, a3, ldb, static_cast<__nv_bfloat16*>(W));
+    const dim3 grid((ldb + 255) / 256, ncol, nlev);
+    k_build_w_merged<<<grid, 256, 0, st>>>(u_hist, t_hist, is_u, D, s0, Cpad, lo, hi, Lw, a1, a2,
+                                           a3, ldb, static_cast<__nv_bfloat16*>(W));
     return cudaGetLastError();
 }
 
-cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int S,
-                               int nbe, double* Y, cudaStream_t s) {
-    if (nbe < 1 || nbe > kKnownMaxSteps) return cudaErrorInvalidValue;
-    k_known_terms<<<(D + 127) / 128, 128, 0, s>>>(known, static_cast<const double3*>(coef), D, L,
-                                                  S, nbe, Y);
+cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int last,
+                               double* Yk, cudaStream_t s) {
+    if (last < 1) return cudaSuccess;
+    const int nbs = kKnownMaxSteps;
+    const dim3 grid((D + 127) / 128, (last + nbs - 1) / nbs);
+    k_known_terms<<<grid, 128, 0, s>>>(known, static_cast<const double3*>(coef), D, L, nbs, last,
+                                       Yk);
     return cudaGetLastError();
 }
 

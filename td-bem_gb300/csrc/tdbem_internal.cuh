@@ -90,7 +90,7 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
-                         bool fast = false);
+                         bool fast = false, const float* geomf = nullptr);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
                                int if_ext, int mode, const AsmOut& out, cudaStream_t s);
 size_t scan_temp_bytes(unsigned n);
@@ -263,8 +263,9 @@ cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
                                   const unsigned char* is_u, int D, int s0, int ncol, int Cmax,
                                   int lo, int hi, int nlev, int Lw, double a1, double a2,
                                   double a3, void* W, cudaStream_t st);
-cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int S,
-                               int nbe, double* Y, cudaStream_t s);
+// Known part of the right-hand sides of the solve steps 1..last into Yk[step][D].
+cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int last,
+                               double* Yk, cudaStream_t s);
 void known_coefficients(int numstep, int L, double a1, double a2, double a3,
                         const std::vector<double>& amp, double c0, double c1,
                         std::vector<double>& out);
@@ -376,7 +377,7 @@ struct tdbem_ctx {
     double* d_H01 = nullptr;
     // mixed marching
     int nb = 16;                    // steps per time block
-    int n_refine = 1;               // FP64 refinement sweeps per solve
+    int n_refine = 0;               // FP64 refinement sweeps per solve
     float* d_inv32[2] = {nullptr, nullptr};
     double* d_Hc64[2] = {nullptr, nullptr};
     float* d_Wt_old = nullptr;
@@ -423,6 +424,8 @@ struct tdbem_ctx {
     float* d_mtc_bc = nullptr;
     double* d_mtc_coef = nullptr;
     size_t mtc_coef_cap = 0;
+    double* d_mtc_yk = nullptr;      // known part of every step's right-hand side
+    size_t mtc_yk_cap = 0;
     std::vector<double> mtc_coef_key;
     // stepwise marching (tdbem_march_begin / tdbem_march_step) and host-block levels
     bool use_graphs = true;         // replay the marching loop as a CUDA graph

@@ -120,6 +120,7 @@ def test_group_mixed_within_1e4_of_fp64(tdlib):
     try:
         for ctx, m, (alpha, ak) in zip(ctxs, ms, setup):
             configure(ctx, m, alpha, ak)
+            ctx.set_march_options(refine_sweeps=1)
         tdlib.assemble_group(ctxs, precision=tdlib.MIXED)
         out = tdlib.march_group(ctxs)
         for (u, _), ur in zip(out, ref):

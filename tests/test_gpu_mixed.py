@@ -135,6 +135,26 @@ def test_new_boundary_values_reach_the_merged_levels(tdlib):
     assert np.array_equal(u, ref)
 
 
+@pytest.mark.parametrize("case", ["alpha_bar", "prescribed", "q8"])
+def test_default_options_within_1e4(tdlib, case):
+    """The library's default march options (tcgen05 engine, 16-step blocks, no
+    refinement sweep) on the bars with prescribed displacements, known values in
+    every history term, and 8-node elements."""
+    if case == "q8":
+        z, m = load_golden("ref_bar2_alpha")
+        a = (float(z["a1"]), float(z["a2"]))
+    else:
+        m = bar_with_prescribed_values() if case == "prescribed" else \
+            load_golden("bar_1x1x4_q2_alpha")[1]
+        a = (0.25, 0.1)
+    u, t, _ = run(tdlib, m, tdlib.FP64, alpha=a)
+    with tdlib.Context(m) as ctx:
+        ctx.set_alpha(*a)
+        ctx.assemble(precision=tdlib.MIXED)
+        u32, t32 = ctx.march()
+    assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
+
+
 def test_mixed_q8_bar(tdlib):
     """8-node elements in mixed precision: every pair through the FP64 quadrature
     into the FP32 store, FP32 convolution and FP32 inverse with refinement."""
