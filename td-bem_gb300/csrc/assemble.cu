@@ -843,6 +843,18 @@ __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool d
 // level store.  Gauss-point geometry comes from the FP32 table (points relative to
 // the element's first node); no FP64 arithmetic in the point loop, which on GB300
 // would run on the narrow FP64 pipe.
+template <typename T>
+__device__ __forceinline__ T* far_out(const AsmOut& o, int which);
+template <>
+__device__ __forceinline__ float* far_out<float>(const AsmOut& o, int which) {
+    return which == 0 ? o.G0f : o.H0f;
+}
+template <>
+__device__ __forceinline__ double* far_out<double>(const AsmOut& o, int which) {
+    return which == 0 ? o.G0 : o.H0;
+}
+
+template <typename T>
 __device__ __forceinline__ void far_item(const double* __restrict__ coords,
                                          const int* __restrict__ ien, int c, int e, int k,
                                          int nq2, const float* __restrict__ geomf,
@@ -875,6 +887,8 @@ __device__ __forceinline__ void far_item(const double* __restrict__ coords,
     const size_t D = (size_t)out.ld;
     const size_t rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
     constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+    T* G = far_out<T>(out, 0);
+    T* H = far_out<T>(out, 1);
 #pragma unroll
     for (int a = 0; a < 4; a++)
 #pragma unroll
@@ -882,8 +896,8 @@ __device__ __forceinline__ void far_item(const double* __restrict__ coords,
 #pragma unroll
             for (int j = 0; j < 3; j++) {
                 const size_t idx = rowbase + (size_t)i * D + 3 * (size_t)nid[a] + j;
-                out.G0f[idx] += acc.g[a][sym[i * 3 + j]];
-                out.H0f[idx] += acc.h[a][i * 3 + j];
+                G[idx] += (T)acc.g[a][sym[i * 3 + j]];
+                H[idx] += (T)acc.h[a][i * 3 + j];
             }
 }
 
@@ -922,6 +936,7 @@ __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
 // level) of a batch of kFarBlock elements are compacted with a block scan and
 // spread over the threads.  pairs[c * nel + j] is the window of node c and the
 // j-th element in colour order.
+template <typename T>
 __global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
@@ -952,8 +967,8 @@ __global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
             for (int i = threadIdx.x; i < total; i += kFarBlock) {
                 const int code = s_items[i];
                 const int k = k0 + (code & 15);
-                far_item(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, f,
-                         (float)k * f.dt, level_last, out);
+                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, f,
+                            (float)k * f.dt, level_last, out);
             }
             count += total;
             // s_items is rebuilt next; this batch's adds come before the next colour's
@@ -1274,11 +1289,22 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
                                      int nnd, int nel, int nq, const float* geomf, const Phys& ph,
                                      int level_last, const PairInfo* pairs, const AsmOut& out,
-                                     unsigned long long* nitems, cudaStream_t s) {
-    const dim3 grid(nnd, (level_last + kFarChunk) / kFarChunk);
-    k_assemble_far_rows<<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems, color_start, ncolor,
-                                                    nel, nq * nq, geomf, ph, level_last, pairs,
-                                                    out, nitems);
+                                     unsigned long long* nitems, cudaStream_t s, int level_cap,
+                                     bool fp64_out) {
+    // the pairs' windows are capped at level_cap already; the grid covers its chunks
+    const int top = std::min(level_last, level_cap);
+    if (top < 0) return cudaSuccess;
+    const dim3 grid(nnd, (top + kFarChunk) / kFarChunk);
+    if (fp64_out)
+        k_assemble_far_rows<double><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
+                                                               color_start, ncolor, nel, nq * nq,
+                                                               geomf, ph, level_last, pairs, out,
+                                                               nitems);
+    else
+        k_assemble_far_rows<float><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
+                                                              color_start, ncolor, nel, nq * nq,
+                                                              geomf, ph, level_last, pairs, out,
+                                                              nitems);
     return cudaGetLastError();
 }
 

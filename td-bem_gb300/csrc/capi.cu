@@ -1250,10 +1250,38 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         // is written for 4-node elements)
         const bool split = c->ennd == 4;
         // FP64 levels 0/1 first: with the C term they are final, and the inverses can
-        // start next to the rest of the assembly
+        // start next to the rest of the assembly.  Singular pairs through the FP64
+        // quadrature, the others through the FP32 far form (FP64 sums): the store's
+        // FP32 inverses and levels carry FP32 accuracy either way.
+        const size_t np = (size_t)c->nnd * c->nel;
+        if (split && c->far_pairs_cap < np) {
+            dfree(c->d_far_pairs);
+            c->far_pairs_cap = 0;
+            CUDA_TRY(dalloc(&c->d_far_pairs, np));
+            c->far_pairs_cap = np;
+        }
         for (int col = 0; col < ncol; col++) {
-            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0, SEL_ALL, o64);
+            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, 1, 0,
+                                          split ? SEL_NEAR : SEL_ALL, o64);
             if (rc != TDBEM_OK) return rc;
+        }
+        const bool count = c->prof;  // the far item count feeds the profile's byte/flop totals
+        if (count)
+            CUDA_TRY(cudaMemsetAsync(c->d_far_items, 0, sizeof(unsigned long long), c->stream));
+        if (split) {
+            const int pw = prof_begin(c, TDBEM_K_AUX);
+            CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
+                                        c->nnd, c->ph, ASM_LEVELS, last, 1, 0, SEL_FAR,
+                                        c->d_far_pairs, nullptr, c->stream));
+            prof_end(c, pw, 0, 0);
+            const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
+            CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
+                                              c->d_color_start, ncol, c->nnd, c->nel, c->nq,
+                                              c->d_geomf, c->ph, last, c->d_far_pairs, o64,
+                                              count ? c->d_far_items : nullptr, c->stream, 1,
+                                              true));
+            prof_end(c, pe, 0, 0);
+            c->launches += 2;
         }
         // the C term, regular elements in FP32 (the FP32 store takes it after the far field)
         const int pc = prof_begin(c, TDBEM_K_AUX);
@@ -1302,21 +1330,11 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         if (split) {
             // far pairs: windows of every (node, element) pair, elements in colour order,
             // then one row-local FP32 launch
-            const size_t np = (size_t)c->nnd * c->nel;
-            if (c->far_pairs_cap < np) {
-                dfree(c->d_far_pairs);
-                c->far_pairs_cap = 0;
-                CUDA_TRY(dalloc(&c->d_far_pairs, np));
-                c->far_pairs_cap = np;
-            }
             const int pw = prof_begin(c, TDBEM_K_AUX);
             CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
                                         c->nnd, c->ph, ASM_LEVELS, last, c->M, 0, SEL_FAR,
                                         c->d_far_pairs, nullptr, c->stream));
             prof_end(c, pw, 0, 0);
-            const bool count = c->prof;  // the item count feeds the profile's byte/flop totals
-            if (count)
-                CUDA_TRY(cudaMemsetAsync(c->d_far_items, 0, sizeof(unsigned long long), c->stream));
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
                                               c->d_color_start, ncol, c->nnd, c->nel, c->nq,

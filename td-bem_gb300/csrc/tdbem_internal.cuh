@@ -36,10 +36,12 @@ struct PairInfo {
 // pairs in FP32 and the rest in FP64).
 enum PairSelect : int {
     SEL_ALL = 0,   // every pair
-    SEL_NEAR = 1,  // singular pairs and pairs closer than kFarRatio element radii
+    SEL_NEAR = 1,  // singular pairs and pairs within kFarRatio element radii
     SEL_FAR = 2,   // the others
 };
-constexpr double kFarRatio = 2.0;  // far: distance to the element's bounding sphere > 2 radii
+// far: a non-singular pair whose node lies outside the element's bounding sphere
+// (the FP32 form keeps level entries within ~1e-6 of FP64 down to that distance)
+constexpr double kFarRatio = 0.0;
 
 // Assembly output selection.
 enum AsmMode : int {
@@ -86,7 +88,8 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
                                      int nnd, int nel, int nq, const float* geomf, const Phys& ph,
                                      int level_last, const PairInfo* pairs, const AsmOut& out,
-                                     unsigned long long* nitems, cudaStream_t s);
+                                     unsigned long long* nitems, cudaStream_t s,
+                                     int level_cap = 1 << 30, bool fp64_out = false);
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
