@@ -81,7 +81,9 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         for _, log in results:
             sys.stderr.write(log)
     if _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + \
+            ["-lcublas", "-lcudart", "-lpthread", "-Xlinker", "-rpath=" + cuda_lib]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -448,11 +448,15 @@ void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t
     const int D = c->D;
     const size_t DD = (size_t)D * D;
     auto invert = [&](int v, cudaStream_t st, int* perm, int* status, float* scratch) {
+        // a cuBLAS handle of the device's pool for the trailing updates (without one
+        // the inverse uses its own update kernel)
+        void* blas = blas_checkout(c->device);
         r.e[v] = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
                                   lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
         if (r.e[v] == cudaSuccess)
             r.e[v] = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
-                                &r.launches[v], &r.singular[v], st);
+                                &r.launches[v], &r.singular[v], st, blas);
+        blas_return(c->device, blas);  // invert_f32 synchronises its stream before returning
         r.launches[v] += 1;
     };
     if (ninv == 2) {
@@ -1018,6 +1022,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
         }                                                                                    \
     } while (0)
     CTX_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    blas_pool_init(c->device);  // before any march of this device can capture a graph
     CTX_TRY(dalloc(&c->d_coords, c->h_coords.size()));
     CTX_TRY(dalloc(&c->d_ien, c->h_ien.size()));
     CTX_TRY(dalloc(&c->d_gx, nq));

@@ -16,7 +16,10 @@
 //      A[i, C1] = -A[i, C1] Ainv11       for rows i not in R1.
 // After the last panel the columns are permuted back (reverse order of the
 // row swaps).  Step 5 is a rank-bw update with bw-deep dot products, so the
-// whole inversion is 2 n^3 flops in GEMM form.
+// whole inversion is 2 n^3 flops in GEMM form.  With a cuBLAS handle (the FP32
+// inverse) step 5 is two plain GEMMs over the columns left and right of C1 and
+// every row: rows R1 are rewritten by step 6 whatever step 5 leaves there, and
+// step 6 reads only columns C1, which the GEMMs do not write.
 //
 // The FP32 inverse (a preconditioner that FP64 refinement corrects) may restrict
 // step 1's search to the panel's diagonal block (k_block_pivots, one CTA: no
@@ -25,9 +28,13 @@
 // zero pivot in the block, or a probe ||A (X v) - v|| / ||v|| above 1e-2 of the
 // finished inverse, sends the inversion back to the full search.
 #include <cooperative_groups.h>
+#include <cublas_v2.h>
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
+#include <type_traits>
 #include <vector>
 
 #include "tdbem_internal.cuh"
@@ -611,9 +618,14 @@ cudaError_t pivot_attributes() {
     return e;
 }
 
+// FP32 GEMM on the tensor cores with FP32 accuracy (each input as three BF16
+// terms), where this cuBLAS offers it.
+cublasComputeType_t blas_compute() { return CUBLAS_COMPUTE_32F_EMULATED_16BFX9; }
+
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
-                           bool* singular, cudaStream_t s, bool restricted = false) {
+                           bool* singular, cudaStream_t s, bool restricted = false,
+                           void* blas = nullptr) {
     *singular = false;
     {
         const cudaError_t ea = pivot_attributes<T, BW>();
@@ -675,10 +687,43 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         k_apply_swaps<T><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
         k_panel_inv<T, BW><<<1, 1024, 0, s>>>(A, n, k0, bw, Ainv, d_status);
         k_panel_t12<T, BW><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, Ainv, T12, d_status);
-        k_panel_update<T, BW><<<ugrid, 256, 0, s>>>(A, n, k0, bw, T12, d_status);
+        bool updated = false;
+        if constexpr (std::is_same<T, float>::value) {
+            if (blas) {  // A[:, J] -= A[:, C1] T12[:, J] for J left and right of C1
+                cublasHandle_t h = static_cast<cublasHandle_t>(blas);
+                if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+                const float alpha = -1.f, beta = 1.f;
+                const int spans[2][2] = {{0, k0}, {k0 + bw, n - k0 - bw}};
+                for (const auto& sp : spans) {
+                    if (sp[1] <= 0) continue;
+                    // column-major views of the row-major arrays: C^T -= T12_J^T A_C1^T;
+                    // plain FP32 where the emulated form does not take the shape
+                    // (rows of an odd n are not 16-byte aligned)
+                    auto gemm = [&](cublasComputeType_t ct) {
+                        return cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, sp[1], n, bw, &alpha,
+                                            T12 + sp[0], CUDA_R_32F, n, A + k0, CUDA_R_32F, n,
+                                            &beta, A + sp[0], CUDA_R_32F, n, ct,
+                                            CUBLAS_GEMM_DEFAULT);
+                    };
+                    cublasStatus_t st = gemm(blas_compute());
+                    if (st == CUBLAS_STATUS_NOT_SUPPORTED) st = gemm(CUBLAS_COMPUTE_32F);
+                    if (st != CUBLAS_STATUS_SUCCESS) {
+                        note_error(("cuBLAS trailing update: " +
+                                    std::string(cublasGetStatusString(st))).c_str());
+                        return cudaErrorUnknown;
+                    }
+                    *nlaunch += 1;
+                }
+                updated = true;
+            }
+        }
+        if (!updated) {
+            k_panel_update<T, BW><<<ugrid, 256, 0, s>>>(A, n, k0, bw, T12, d_status);
+            *nlaunch += 1;
+        }
         k_panel_finish<T, BW><<<std::max(1, (n + 255) / 256), 256, 0, s>>>(A, n, k0, bw, T12,
                                                                            Ainv, d_status);
-        *nlaunch += 6;
+        *nlaunch += 5;
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -717,13 +762,64 @@ cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scrat
     return invert_blocked<double, 16>(A, n, perm, d_status, scratch, nlaunch, singular, s);
 }
 
+// cuBLAS handles, a fixed pool per device.  Creating (or destroying) a handle
+// invalidates a stream capture that another thread has in progress (measured on
+// GB300: a loop creating and destroying handles next to 200 thread-local
+// captures broke 45 of them; GEMM calls broke none), so the pool is made when the
+// first context of a device is created, before any of its marches can capture,
+// and lives as long as the process.
+namespace {
+constexpr int kBlasPool = 8;
+constexpr int kBlasDevices = 64;
+struct BlasPool {
+    std::mutex m;
+    bool made = false;
+    std::vector<cublasHandle_t> free_handles;
+};
+BlasPool& blas_pool(int dev) {
+    static BlasPool pools[kBlasDevices];
+    return pools[dev];
+}
+}  // namespace
+
+void blas_pool_init(int dev) {
+    if (dev < 0 || dev >= kBlasDevices) return;
+    BlasPool& p = blas_pool(dev);
+    std::lock_guard<std::mutex> lk(p.m);
+    if (p.made) return;
+    p.made = true;
+    for (int i = 0; i < kBlasPool; i++) {
+        cublasHandle_t h = nullptr;
+        if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) break;
+        p.free_handles.push_back(h);
+    }
+}
+
+void* blas_checkout(int dev) {
+    if (dev < 0 || dev >= kBlasDevices) return nullptr;
+    BlasPool& p = blas_pool(dev);
+    std::lock_guard<std::mutex> lk(p.m);
+    if (p.free_handles.empty()) return nullptr;
+    cublasHandle_t h = p.free_handles.back();
+    p.free_handles.pop_back();
+    return h;
+}
+
+void blas_return(int dev, void* h) {
+    if (!h || dev < 0 || dev >= kBlasDevices) return;
+    BlasPool& p = blas_pool(dev);
+    std::lock_guard<std::mutex> lk(p.m);
+    p.free_handles.push_back(static_cast<cublasHandle_t>(h));
+}
+
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
-                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s) {
+                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
+                       void* blas) {
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
     // first with the pivot search in the panels' diagonal blocks, then checked
     cudaError_t e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular,
-                                              s, true);
+                                              s, true, blas);
     if (e != cudaSuccess) return e;
     bool good = false;
     if (!*singular) {
@@ -747,7 +843,8 @@ cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_sta
     if (good) return cudaSuccess;
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
-    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s);
+    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s, false,
+                                     blas);
 }
 
 }  // namespace tdbem

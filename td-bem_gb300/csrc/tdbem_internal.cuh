@@ -199,8 +199,16 @@ size_t inverse_scratch_elems(int n);
 // *singular is set (and cudaSuccess returned) when a pivot is exactly zero.
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
                        long long* nlaunch, bool* singular, cudaStream_t s);
+// blas: a cuBLAS handle (blas_checkout) for the trailing updates, or nullptr for
+// the built-in update kernel.
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
-                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s);
+                       float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
+                       void* blas = nullptr);
+// The device's cuBLAS handle pool (made once, with the device's first context);
+// a handle is used by one thread at a time; nullptr when none is free.
+void blas_pool_init(int dev);
+void* blas_checkout(int dev);
+void blas_return(int dev, void* h);
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
                                    int L, double a1, double a2, double a3, double c0,
                                    double c1, double amp, const double* load_t,
