@@ -526,7 +526,7 @@ def run_ours(args, dist):
                        "alpha": list(ALPHA), "precision": args.precision,
                        "parallelism": f"replicas{dist.world}", "load_cases": nc,
                        "refine_sweeps": refine,
-                       "block_steps": args.block,
+                       "block_steps": args.block or (32 if args.march_engine == "tcgen05" else 8),
                        "march_engine": args.march_engine if prec == lib.MIXED else None,
                        "batch_engine": args.engine if cases else None,
                        "l2": "inputs larger than L2: the level store is "
@@ -737,8 +737,8 @@ def main():
     ap.add_argument("--march-engine", choices=["tcgen05", "fp32"], default="tcgen05",
                     help="old-history pass of the mixed march: split-BF16 products on the "
                          "tensor cores, or FP32 products on the CUDA cores")
-    ap.add_argument("--block", type=int, default=16, choices=[1, 4, 6, 8, 12, 16],
-                    help="time-block steps of the mixed march")
+    ap.add_argument("--block", type=int, default=0, choices=[0, 1, 4, 6, 8, 12, 16, 24, 32],
+                    help="time-block steps of the mixed march (0: the engine's default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 64-load-case batched measurement beside the headline")

@@ -241,9 +241,9 @@ int tdbem_set_graphs(tdbem_ctx* ctx, int on);
 int tdbem_set_march_engine(tdbem_ctx* ctx, int engine);
 
 /* Options of the TDBEM_MIXED marching: block_steps = time steps per block of the
- * history convolution (1, 4, 6, 8, 12 or 16; default 16, the fastest on GB300 for
- * the 4614-DOF sphere with the tcgen05 engine; 8 is the fastest with the FP32
- * engine), refine_sweeps = FP64 residual-refinement sweeps per solve
+ * history convolution (1, 4, 6, 8, 12 or 16, and 24 or 32 with the tcgen05 engine;
+ * 0 = each engine's default, the fastest on GB300 for the 4614-DOF sphere: 32 with
+ * tcgen05, 8 with FP32), refine_sweeps = FP64 residual-refinement sweeps per solve
  * (0..4; default 0: on the 4614-DOF sphere the FP32 inverse alone is within
  * 2.4e-7 of FP64, below the tcgen05 engine's convolution error of ~1e-5; the
  * sweeps are for LHS matrices whose FP32 inverse is less accurate). */

@@ -506,8 +506,8 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
     if (sing >= 0) n_lo = 0;
     PairInfo pi;
     pi.sing = sing;
-    if (mode == ASM_LEVELS) {
-        const int klo = max(0, n_lo);
+    if (mode == ASM_LEVELS) {  // step_n: the lowest level wanted
+        const int klo = max(step_n, n_lo);
         const int khi = min(min(level_last, (int)ceil(rmax * ph.inv_cs * ph.inv_dt) + 1),
                             level_cap);
         pi.klo = klo;
@@ -1328,6 +1328,25 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel
             k_cterm<4, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
                                                      ph, cbuf, nullptr);
     }
+    return cudaGetLastError();
+}
+
+// FP32 store levels 0/1 from the finished FP64 levels 0/1 (ld D -> ldf).
+__global__ void k_cast_levels01(const double* __restrict__ G01, const double* __restrict__ H01,
+                                int D, int ldf, float* __restrict__ Gf, float* __restrict__ Hf) {
+    const size_t n = (size_t)2 * D * D;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t kr = i / D, col = i - kr * D;  // kr = level * D + row
+        Gf[kr * ldf + col] = (float)G01[i];
+        Hf[kr * ldf + col] = (float)H01[i];
+    }
+}
+
+cudaError_t launch_cast_levels01(const double* G01, const double* H01, int D, int ldf, float* Gf,
+                                 float* Hf, cudaStream_t s) {
+    if (ldf < D) return cudaErrorInvalidValue;
+    k_cast_levels01<<<152 * 8, 256, 0, s>>>(G01, H01, D, ldf, Gf, Hf);
     return cudaGetLastError();
 }
 

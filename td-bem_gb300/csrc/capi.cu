@@ -359,7 +359,7 @@ int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const 
     if (c->prof || !c->use_graphs) return loop();
     MarchGraph& g = c->graph;
     cudaStream_t s = c->stream;
-    const bool same = g.exec && g.kind == kind && g.numstep == numstep && g.nb == c->nb &&
+    const bool same = g.exec && g.kind == kind && g.numstep == numstep && g.nb == c->nb_eff &&
                       g.refine == c->n_refine && g.a1 == c->a1 && g.a2 == c->a2 &&
                       g.amp == c->amp && g.ptrs == ptrs;
     if (!same) {
@@ -382,7 +382,7 @@ int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const 
         c->launches = l0;
         g.kind = kind;
         g.numstep = numstep;
-        g.nb = c->nb;
+        g.nb = c->nb_eff;
         g.refine = c->n_refine;
         g.a1 = c->a1;
         g.a2 = c->a2;
@@ -518,12 +518,27 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
 // Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
 // inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
 int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
-    const int D = c->D, M = c->M, nb = c->nb;
+    // block steps: the setting, or each engine's measured optimum on the 4614-DOF sphere
+    const int nb = c->nb ? c->nb : (c->march_engine == TDBEM_ENGINE_TCGEN05 ? 32 : 8);
+    const int D = c->D, M = c->M;
     const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
     const size_t DD = (size_t)D * D;
     const int ldw = mixed_ldw(D);
     cudaStream_t s = c->stream;
+    if (nb > 16 && c->march_engine != TDBEM_ENGINE_TCGEN05)
+        return fail(TDBEM_ERR_ARG, "block_steps %d needs the tcgen05 march engine (FP32: <= 16)",
+                    nb);
+    c->nb_eff = nb;
+    if (c->d_Wt_old && c->nb_alloc != nb) {  // scratch sized by the block
+        dfree(c->d_Wt_old);
+        dfree(c->d_Wu_old);
+        dfree(c->d_Yold);
+        dfree(c->d_pmix);
+        dfree(c->d_res);
+        dfree(c->d_dx);
+    }
     if (!c->d_Wt_old) {
+        c->nb_alloc = nb;
         CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
         CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
         CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
@@ -631,11 +646,11 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     // Old pass: history before the block and the steps' known-load terms.
     auto old_pass = [&](int S, int nbe) -> int {
         const int nlev = (S > 1 ? std::min(M, S + nbe - 1) : std::min(M, 1)) + 1;
-        BlockLoads bl{};
-        bl.nload = nbe;
+        BlockLoads bl{};  // the FP32 engine's known-load terms (its blocks: <= 16 steps)
+        bl.nload = tc ? 0 : nbe;
         bl.load_t = c->d_load_t;
         bl.load_u = c->d_load_u;
-        for (int j = 0; j < nbe; j++) {
+        for (int j = 0; j < bl.nload; j++) {
             const int st = S + j;
             bl.amp[j] = c->amp.empty() ? 1.0 : c->amp[st];
             bl.c0[j] = st == 1 ? 1.0 : lhs_c[1][0];
@@ -1326,9 +1341,10 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                 run_inverses(c, ninv, lhs_c, c->stream2, c->stream3, ir);
             });
         }
-        // near pairs (FP64 quadrature into the FP32 store), colour by colour
+        // near pairs (FP64 quadrature into the FP32 store), colour by colour, from level
+        // 2 on: levels 0/1 are the FP64 ones, cast at the end
         for (int col = 0; col < ncol; col++) {
-            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 0,
+            const int rc = assemble_color(c, col, 0, c->nnd, ASM_LEVELS, last, c->M, 2,
                                           split ? SEL_NEAR : SEL_ALL, o32);
             if (rc != TDBEM_OK) return rc;
         }
@@ -1337,7 +1353,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             // then one row-local FP32 launch
             const int pw = prof_begin(c, TDBEM_K_AUX);
             CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
-                                        c->nnd, c->ph, ASM_LEVELS, last, c->M, 0, SEL_FAR,
+                                        c->nnd, c->ph, ASM_LEVELS, last, c->M, 2, SEL_FAR,
                                         c->d_far_pairs, nullptr, c->stream));
             prof_end(c, pw, 0, 0);
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
@@ -1356,8 +1372,9 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                 c->prof_pending[pe].flops = (double)n * c->nq * c->nq * kFlopsPerItemPointF32;
             }
         }
-        CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o32,
-                                    c->stream));
+        // levels 0/1 (with the C term) from the FP64 pair
+        CUDA_TRY(launch_cast_levels01(c->d_G01, c->d_H01, D, (int)ldf, c->d_Gf, c->d_Hf,
+                                      c->stream));
         c->launches += 1;
         if (split) {
             inv_thread.join();  // its streams are synchronised when it returns
@@ -2339,20 +2356,13 @@ int tdbem_set_march_engine(tdbem_ctx* c, int engine) {
 
 int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
     if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (block_steps != 1 && block_steps != 4 && block_steps != 6 && block_steps != 8 &&
-        block_steps != 12 && block_steps != 16)
-        return fail(TDBEM_ERR_ARG, "block_steps must be 1, 4, 6, 8, 12 or 16");
+    if (block_steps != 0 && block_steps != 1 && block_steps != 4 && block_steps != 6 &&
+        block_steps != 8 && block_steps != 12 && block_steps != 16 && block_steps != 24 &&
+        block_steps != 32)
+        return fail(TDBEM_ERR_ARG, "block_steps must be 0 (auto), 1, 4, 6, 8, 12, 16, 24 or 32");
     if (refine_sweeps < 0 || refine_sweeps > 4)
         return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
-    if (block_steps != c->nb) {  // scratch sized by the block
-        dfree(c->d_Wt_old);
-        dfree(c->d_Wu_old);
-        dfree(c->d_Yold);
-        dfree(c->d_pmix);
-        dfree(c->d_res);
-        dfree(c->d_dx);
-    }
-    c->nb = block_steps;
+    c->nb = block_steps;  // the march resizes its scratch when the block changes
     c->n_refine = refine_sweeps;
     return TDBEM_OK;
 }
@@ -2430,12 +2440,12 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         b += 2 * L * DD * 8;                    // levels
         b += 2 * DD * 8 + inverse_scratch_elems((int)D) * 8;  // inverses
     } else {
-        const size_t ld = mixed_ld((int)D), ldw = mixed_ldw((int)D), nb = 16;
+        const size_t ld = mixed_ld((int)D), ldw = mixed_ldw((int)D), nb = 32;
         b += 2 * L * D * ld * 4 + 4 * DD * 8;   // FP32 levels, FP64 levels 0 and 1
         b += 2 * DD * 8 + 2 * DD * 4 + inverse_scratch_elems((int)D) * 4;  // LHS, inverses
         b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
         // tcgen05 march: merged planes, history planes, known part and its coefficients
-        b += tc_plane_bytes((int)D, (int)L, 1) + tc_w_bytes((int)D, 16, (int)L, 1) +
+        b += tc_plane_bytes((int)D, (int)L, 1) + tc_w_bytes((int)D, 32, (int)L, 1) +
              3 * L * D * 8 + (numstep + 1) * (L * 3 + D) * 8 + 3 * D * 4;
     }
     *bytes = b;

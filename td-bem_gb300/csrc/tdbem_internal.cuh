@@ -94,6 +94,8 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
                          bool fast = false, const float* geomf = nullptr);
+cudaError_t launch_cast_levels01(const double* G01, const double* H01, int D, int ldf, float* Gf,
+                                 float* Hf, cudaStream_t s);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
                                int if_ext, int mode, const AsmOut& out, cudaStream_t s);
 size_t scan_temp_bytes(unsigned n);
@@ -387,7 +389,9 @@ struct tdbem_ctx {
     double* d_G01 = nullptr;        // mixed: levels 0 and 1 in FP64 (the LHS)
     double* d_H01 = nullptr;
     // mixed marching
-    int nb = 16;                    // steps per time block
+    int nb = 0;                     // steps per time block (0: the engine's default)
+    int nb_eff = 0;                 // the block of the last mixed march
+    int nb_alloc = 0;               // the block its scratch is sized for
     int n_refine = 0;               // FP64 refinement sweeps per solve
     float* d_inv32[2] = {nullptr, nullptr};
     double* d_Hc64[2] = {nullptr, nullptr};

@@ -334,7 +334,7 @@ class Context:
     def set_alpha(self, a1: float, a2: float):
         _check(load().tdbem_set_alpha(self.h, a1, a2))
 
-    def set_march_options(self, block_steps: int = 16, refine_sweeps: int = 0):
+    def set_march_options(self, block_steps: int = 0, refine_sweeps: int = 0):
         _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
 
     def set_march_engine(self, engine: int):

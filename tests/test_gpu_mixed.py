@@ -72,7 +72,7 @@ def test_mixed_c_term_close_to_fp64(tdlib):
         assert np.abs(a - b)[blk].max() <= 1e-6 * np.abs(b[blk]).max()
 
 
-@pytest.mark.parametrize("block", [1, 8, 12, 16])
+@pytest.mark.parametrize("block", [1, 8, 12, 16, 24, 32])
 def test_mixed_histories_within_1e4(tdlib, sphere8, block):
     m, (u, t, _) = sphere8
     u32, t32, _ = run(tdlib, m, tdlib.MIXED, block=block)
@@ -117,6 +117,19 @@ def test_mixed_prescribed_values_and_load_history(tdlib, engine):
         u32, t32, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1), amp=amp, engine=eng,
                           block=block)
         assert rel_l2(u32, u) <= TOL_L2 and rel_l2(t32, t) <= TOL_L2
+
+
+def test_long_blocks_need_the_tcgen05_engine(tdlib):
+    _, m = load_golden("bar_1x1x4_q2_alpha")
+    with tdlib.Context(m) as ctx:
+        ctx.set_march_options(32, 0)
+        ctx.set_march_engine(tdlib.ENGINE_FP32)
+        ctx.assemble(precision=tdlib.MIXED)
+        with pytest.raises(tdlib.TdbemError) as e:
+            ctx.march()
+        assert e.value.code == -1 and "tcgen05" in str(e.value)
+        with pytest.raises(tdlib.TdbemError):
+            ctx.set_march_options(20, 0)
 
 
 def test_new_boundary_values_reach_the_merged_levels(tdlib):

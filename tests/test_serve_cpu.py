@@ -38,8 +38,8 @@ def test_footprint_counts_the_level_store(tdlib):
     f32 = tdlib.footprint(m, tdlib.MIXED)
     levels64 = 2 * (M + 1) * D * D * 8
     assert levels64 < f64 < 1.3 * levels64
-    # FP32 levels and, for the tcgen05 march, their BF16 hi/lo planes
-    assert levels64 < f32 < 1.3 * levels64
+    # FP32 levels and, for the tcgen05 march, the merged BF16 hi/lo planes (half of them)
+    assert 2 * (M + 1) * D * D * 4 < f32 < f64
     # more steps: longer histories, same levels
     assert tdlib.footprint(m, tdlib.MIXED, numstep=400) > f32
 
