@@ -709,7 +709,15 @@ __global__ void __launch_bounds__(128) k_assemble_items(
 struct PhysF {
     float dt, inv_dt, inv_cp, inv_cs, inv_cp2, inv_cs2, cs2, ratio2, ratio3, inv_4pi_rho,
         inv_4pi, c4;  // c4 = 1 - 2 (cs/cp)^2
+    float dt_below;   // the largest float below dt
 };
+
+// A point's FP32 tau = T - r/c is off by at most ~8 eps (T + r/c) (T = k dt and r/c
+// each rounded, r from FP32 offsets); within 64 eps (T + dt + r/c_p) of a threshold
+// of the time integrals' regimes (tau of some evaluation time at 0 or dt, where the
+// step terms I5/J5 jump and the exact-zero skips switch) the regimes are decided in
+// FP64 as the FP64 quadrature decides them.
+constexpr float kTauMargin = 64.f / 16777216.f;
 
 __device__ __forceinline__ PhysF to_f(const Phys& p) {
     PhysF f;
@@ -725,7 +733,41 @@ __device__ __forceinline__ PhysF to_f(const Phys& p) {
     f.inv_4pi_rho = (float)p.inv_4pi_rho;
     f.inv_4pi = (float)p.inv_4pi;
     f.c4 = (float)(1 - 2 * p.ratio2);
+    f.dt_below = nextafterf(f.dt, 0.f);
     return f;
+}
+
+// FP32 tau in the regime that FP64 gives tr (wave_I / wave_J: dt <= tr, 0 <= tr < dt,
+// tr < 0).
+__device__ __forceinline__ float snap_tau(double tr, double dt, const PhysF& f) {
+    const float t = (float)tr;
+    if (dt <= tr) return fmaxf(t, f.dt);
+    if (0 <= tr) return fminf(fmaxf(t, 0.f), f.dt_below);
+    return t < 0.f ? t : -1e-30f;
+}
+
+struct FrontTaus {
+    float p[4], s[4];
+};
+
+// The taus of both waves at TI = k dt, TI - dt, TJ = (k+1) dt, TJ - dt from the FP64
+// point, node and times of the FP64 quadrature (point_kernels, time_consts), snapped
+// into its regimes.  Kept out of line: it runs for the few points near a front, and
+// inlined its FP64 temporaries would cost the FP32 point loop registers.
+__device__ __noinline__ FrontTaus front_taus(const double* xq64, const double* xc64, int k,
+                                             const Phys& ph, const PhysF& f) {
+    const double e0 = xq64[0] - xc64[0], e1 = xq64[1] - xc64[1], e2 = xq64[2] - xc64[2];
+    const double r64 = sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+    const double rp = r64 * ph.inv_cp, rs = r64 * ph.inv_cs;
+    const double TI0 = k * ph.dt, TJ0 = (k + 1) * ph.dt;
+    const double T4[4] = {TI0, TI0 - ph.dt, TJ0, TJ0 - ph.dt};
+    FrontTaus t;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        t.p[i] = snap_tau(T4[i] - rp, ph.dt, f);
+        t.s[i] = snap_tau(T4[i] - rs, ph.dt, f);
+    }
+    return t;
 }
 
 // One wave at local time tau: F_I = rho Q1 + Q0, I3, I5 and F_J = rho R1 + R0, J3, J5.
@@ -761,10 +803,13 @@ struct ItemAccF {
 };
 
 // One Gauss point of a far item in FP32: TI = k dt (I part), TJ = (k+1) dt (J part).
+// xq64, xc64, k, ph: the point, the node and the level in FP64, for the regime
+// decisions of points near a wave front.
 __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool doJ0, float TI,
                                                 const PhysF& f, const float xc[3],
                                                 const float xq[3], const float nq[3], float wJ,
-                                                const float N[4]) {
+                                                const float N[4], const double* xq64,
+                                                const double* xc64, int k, const Phys& ph) {
     const float d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
     const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
     const float inv_r = rsqrtf(r2);
@@ -773,28 +818,46 @@ __device__ __forceinline__ void gauss_point_f32(ItemAccF& acc, bool doI0, bool d
     const float rdn = rv[0] * nq[0] + rv[1] * nq[1] + rv[2] * nq[2];
     const float rho_p = r * f.inv_cp, rho_s = r * f.inv_cs;
     const float tp = TI - rho_p, ts = TI - rho_s;  // tau of each wave at T = TI
+    // tau of each wave at the part's times: [0] TI, [1] TI - dt (I part), [2] TI + dt,
+    // [3] TI (J part)
+    float tP[4] = {tp, tp - f.dt, tp + f.dt, tp}, tS[4] = {ts, ts - f.dt, ts + f.dt, ts};
+    {
+        const float m = kTauMargin * (TI + f.dt + rho_p);
+        auto near = [&](float t) {
+            return fminf(fminf(fabsf(t + f.dt), fabsf(t)), fminf(fabsf(t - f.dt),
+                                                                 fabsf(t - 2.f * f.dt))) < m;
+        };
+        if (near(tp) || near(ts)) {  // regimes from FP64, as the FP64 quadrature has them
+            const FrontTaus t = front_taus(xq64, xc64, k, ph, f);
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                tP[i] = t.p[i];
+                tS[i] = t.s[i];
+            }
+        }
+    }
     // exact zero once the S front has passed at both times of a part, and before the
     // P front arrives (b = 0 and no I5/J5 step at both times of the part: every term
     // of the part is then exactly zero)
-    const bool doI = doI0 && !(ts - f.dt >= f.dt) && !(tp < 0.f);
-    const bool doJ = doJ0 && !(ts >= f.dt) && !(tp + f.dt < 0.f);
+    const bool doI = doI0 && !(tS[1] >= f.dt) && !(tP[0] < 0.f);
+    const bool doJ = doJ0 && !(tS[3] >= f.dt) && !(tP[2] < 0.f);
     if (!doI && !doJ) return;
     float P1 = 0.f, P3 = 0.f, P5 = 0.f, S2 = 0.f, S4 = 0.f, S6 = 0.f;
     float a1, a3, a5, b1, b3, b5;
     if (doI) {
-        wave_tau_I(tp, rho_p, f, a1, a3, a5);
-        wave_tau_I(tp - f.dt, rho_p, f, b1, b3, b5);
+        wave_tau_I(tP[0], rho_p, f, a1, a3, a5);
+        wave_tau_I(tP[1], rho_p, f, b1, b3, b5);
         P1 = a1 - b1; P3 = a3 - b3; P5 = a5 - b5;
-        wave_tau_I(ts, rho_s, f, a1, a3, a5);
-        wave_tau_I(ts - f.dt, rho_s, f, b1, b3, b5);
+        wave_tau_I(tS[0], rho_s, f, a1, a3, a5);
+        wave_tau_I(tS[1], rho_s, f, b1, b3, b5);
         S2 = a1 - b1; S4 = a3 - b3; S6 = a5 - b5;
     }
     if (doJ) {
-        wave_tau_J(tp + f.dt, rho_p, f, a1, a3, a5);
-        wave_tau_J(tp, rho_p, f, b1, b3, b5);
+        wave_tau_J(tP[2], rho_p, f, a1, a3, a5);
+        wave_tau_J(tP[3], rho_p, f, b1, b3, b5);
         P1 += a1 - b1; P3 += a3 - b3; P5 += a5 - b5;
-        wave_tau_J(ts + f.dt, rho_s, f, a1, a3, a5);
-        wave_tau_J(ts, rho_s, f, b1, b3, b5);
+        wave_tau_J(tS[2], rho_s, f, a1, a3, a5);
+        wave_tau_J(tS[3], rho_s, f, b1, b3, b5);
         S2 += a1 - b1; S4 += a3 - b3; S6 += a5 - b5;
     }
     const float inv_r2 = inv_r * inv_r;
@@ -858,7 +921,8 @@ template <typename T>
 __device__ __forceinline__ void far_item(const double* __restrict__ coords,
                                          const int* __restrict__ ien, int c, int e, int k,
                                          int nq2, const float* __restrict__ geomf,
-                                         const PhysF& f, float TI, int level_last,
+                                         const double* __restrict__ geom, const PhysF& f,
+                                         const Phys& ph, float TI, int level_last,
                                          const AsmOut& out) {
     int nid[4];
 #pragma unroll
@@ -882,7 +946,8 @@ __device__ __forceinline__ void far_item(const double* __restrict__ coords,
         const float xq[3] = {p0.x, p0.y, p0.z};
         const float nqv[3] = {p0.w, p1.x, p1.y};
         const float N[4] = {p1.w, p2.x, p2.y, p2.z};
-        gauss_point_f32(acc, doI, doJ, TI, f, xc, xq, nqv, p1.z, N);
+        gauss_point_f32(acc, doI, doJ, TI, f, xc, xq, nqv, p1.z, N,
+                        geom + ((size_t)e * nq2 + q) * kGeomStride, coords + 3 * c, k, ph);
     }
     const size_t D = (size_t)out.ld;
     const size_t rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
@@ -937,11 +1002,12 @@ __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
 // spread over the threads.  pairs[c * nel + j] is the window of node c and the
 // j-th element in colour order.
 template <typename T>
-__global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
+__global__ void __launch_bounds__(kFarBlock, 4) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
-    int nel, int nq2, const float* __restrict__ geomf, Phys ph, int level_last,
-    const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
+    int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom, Phys ph,
+    int level_last, const PairInfo* __restrict__ pairs, AsmOut out,
+    unsigned long long* __restrict__ nitems) {
     __shared__ int s_warp[kFarBlock / 32];
     __shared__ int s_items[kFarBlock * kFarChunk];
     const int c = blockIdx.x;
@@ -967,8 +1033,8 @@ __global__ void __launch_bounds__(kFarBlock) k_assemble_far_rows(
             for (int i = threadIdx.x; i < total; i += kFarBlock) {
                 const int code = s_items[i];
                 const int k = k0 + (code & 15);
-                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, f,
-                            (float)k * f.dt, level_last, out);
+                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, geom, f,
+                            ph, (float)k * f.dt, level_last, out);
             }
             count += total;
             // s_items is rebuilt next; this batch's adds come before the next colour's
@@ -1287,8 +1353,9 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
 
 cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
-                                     int nnd, int nel, int nq, const float* geomf, const Phys& ph,
-                                     int level_last, const PairInfo* pairs, const AsmOut& out,
+                                     int nnd, int nel, int nq, const float* geomf,
+                                     const double* geom, const Phys& ph, int level_last,
+                                     const PairInfo* pairs, const AsmOut& out,
                                      unsigned long long* nitems, cudaStream_t s, int level_cap,
                                      bool fp64_out) {
     // the pairs' windows are capped at level_cap already; the grid covers its chunks
@@ -1298,13 +1365,13 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
     if (fp64_out)
         k_assemble_far_rows<double><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                                color_start, ncolor, nel, nq * nq,
-                                                               geomf, ph, level_last, pairs, out,
-                                                               nitems);
+                                                               geomf, geom, ph, level_last, pairs,
+                                                               out, nitems);
     else
         k_assemble_far_rows<float><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                               color_start, ncolor, nel, nq * nq,
-                                                              geomf, ph, level_last, pairs, out,
-                                                              nitems);
+                                                              geomf, geom, ph, level_last, pairs,
+                                                              out, nitems);
     return cudaGetLastError();
 }
 

@@ -1297,7 +1297,8 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
                                               c->d_color_start, ncol, c->nnd, c->nel, c->nq,
-                                              c->d_geomf, c->ph, last, c->d_far_pairs, o64,
+                                              c->d_geomf, c->d_geom, c->ph, last,
+                                              c->d_far_pairs, o64,
                                               count ? c->d_far_items : nullptr, c->stream, 1,
                                               true));
             prof_end(c, pe, 0, 0);
@@ -1359,7 +1360,8 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
                                               c->d_color_start, ncol, c->nnd, c->nel, c->nq,
-                                              c->d_geomf, c->ph, last, c->d_far_pairs, o32,
+                                              c->d_geomf, c->d_geom, c->ph, last,
+                                              c->d_far_pairs, o32,
                                               count ? c->d_far_items : nullptr, c->stream));
             prof_end(c, pe, 0, 0);
             c->launches += 2;

@@ -86,8 +86,9 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
 // not null) receives the item count.  4-node elements only.
 cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
-                                     int nnd, int nel, int nq, const float* geomf, const Phys& ph,
-                                     int level_last, const PairInfo* pairs, const AsmOut& out,
+                                     int nnd, int nel, int nq, const float* geomf,
+                                     const double* geom, const Phys& ph, int level_last,
+                                     const PairInfo* pairs, const AsmOut& out,
                                      unsigned long long* nitems, cudaStream_t s,
                                      int level_cap = 1 << 30, bool fp64_out = false);
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
