@@ -516,7 +516,10 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
         pi.klo = step_n;
         pi.cnt = (step_n >= n_lo && step_n <= n_hi) ? 1 : 0;
     }
-    const bool far = sing < 0 && rmin > kFarRatio * rad;
+    // FP32 far form: non-singular, and every point at least c_s dt / 8 from the node.
+    // Closer, the dynamic kernel nears the static one through the cancellation of
+    // terms ~(c_s dt / r)^2 larger, which FP32 would amplify by as much.
+    const bool far = sing < 0 && rmin > kFarRatio * rad && 8.0 * rmin * ph.inv_cs >= ph.dt;
     if ((select == SEL_NEAR && far) || (select == SEL_FAR && !far)) pi.cnt = 0;
     return pi;
 }
