@@ -924,16 +924,20 @@ template <typename T>
 __device__ __forceinline__ void far_item(const double* __restrict__ coords,
                                          const int* __restrict__ ien, int c, int e, int k,
                                          int nq2, const float* __restrict__ geomf,
-                                         const double* __restrict__ geom, const PhysF& f,
+                                         const double* __restrict__ geom,
+                                         const float* __restrict__ coordf, const PhysF& f,
                                          const Phys& ph, float TI, int level_last,
                                          const AsmOut& out) {
     int nid[4];
 #pragma unroll
     for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
-    // collocation point relative to the element's first node, rounded once
-    const float xc[3] = {(float)(coords[c * 3] - coords[nid[0] * 3]),
-                         (float)(coords[c * 3 + 1] - coords[nid[0] * 3 + 1]),
-                         (float)(coords[c * 3 + 2] - coords[nid[0] * 3 + 2])};
+    // collocation point relative to the element's first node from the coordinates'
+    // FP32 pairs, (hi - hi) + (lo - lo): ~1.5 eps relative, no FP64 arithmetic
+    const float4* cf4 = reinterpret_cast<const float4*>(coordf);
+    const float4 ch = __ldg(cf4 + 2 * c), cl = __ldg(cf4 + 2 * c + 1);
+    const float4 eh = __ldg(cf4 + 2 * nid[0]), el = __ldg(cf4 + 2 * nid[0] + 1);
+    const float xc[3] = {(ch.x - eh.x) + (cl.x - el.x), (ch.y - eh.y) + (cl.y - el.y),
+                         (ch.z - eh.z) + (cl.z - el.z)};
     const bool doI = (k >= 1), doJ = (k + 1 <= level_last);
     ItemAccF acc;
 #pragma unroll
@@ -1008,9 +1012,9 @@ template <typename T>
 __global__ void __launch_bounds__(kFarBlock, 4) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
-    int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom, Phys ph,
-    int level_last, const PairInfo* __restrict__ pairs, AsmOut out,
-    unsigned long long* __restrict__ nitems) {
+    int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom,
+    const float* __restrict__ coordf, Phys ph, int level_last,
+    const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
     __shared__ int s_warp[kFarBlock / 32];
     __shared__ int s_items[kFarBlock * kFarChunk];
     const int c = blockIdx.x;
@@ -1036,8 +1040,8 @@ __global__ void __launch_bounds__(kFarBlock, 4) k_assemble_far_rows(
             for (int i = threadIdx.x; i < total; i += kFarBlock) {
                 const int code = s_items[i];
                 const int k = k0 + (code & 15);
-                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, geom, f,
-                            ph, (float)k * f.dt, level_last, out);
+                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, geom,
+                            coordf, f, ph, (float)k * f.dt, level_last, out);
             }
             count += total;
             // s_items is rebuilt next; this batch's adds come before the next colour's
@@ -1357,8 +1361,8 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
 cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
                                      int nnd, int nel, int nq, const float* geomf,
-                                     const double* geom, const Phys& ph, int level_last,
-                                     const PairInfo* pairs, const AsmOut& out,
+                                     const double* geom, const float* coordf, const Phys& ph,
+                                     int level_last, const PairInfo* pairs, const AsmOut& out,
                                      unsigned long long* nitems, cudaStream_t s, int level_cap,
                                      bool fp64_out) {
     // the pairs' windows are capped at level_cap already; the grid covers its chunks
@@ -1368,13 +1372,13 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
     if (fp64_out)
         k_assemble_far_rows<double><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                                color_start, ncolor, nel, nq * nq,
-                                                               geomf, geom, ph, level_last, pairs,
-                                                               out, nitems);
+                                                               geomf, geom, coordf, ph,
+                                                               level_last, pairs, out, nitems);
     else
         k_assemble_far_rows<float><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                               color_start, ncolor, nel, nq * nq,
-                                                              geomf, geom, ph, level_last, pairs,
-                                                              out, nitems);
+                                                              geomf, geom, coordf, ph,
+                                                              level_last, pairs, out, nitems);
     return cudaGetLastError();
 }
 

@@ -1050,6 +1050,19 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_far_items, 1));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
+    {  // node coordinates as FP32 pairs x = hi + lo for the FP32 far form
+        std::vector<float> cf((size_t)8 * c->nnd, 0.f);
+        for (int i = 0; i < c->nnd; i++)
+            for (int d = 0; d < 3; d++) {
+                const double x = c->h_coords[(size_t)3 * i + d];
+                const float hi = (float)x;
+                cf[(size_t)8 * i + d] = hi;
+                cf[(size_t)8 * i + 4 + d] = (float)(x - (double)hi);
+            }
+        CTX_TRY(dalloc(&c->d_coordf, cf.size()));
+        CTX_TRY(cudaMemcpyAsync(c->d_coordf, cf.data(), sizeof(float) * cf.size(),
+                                cudaMemcpyHostToDevice, c->stream));
+    }
     CTX_TRY(cudaMemcpyAsync(c->d_ien, c->h_ien.data(), sizeof(int) * c->h_ien.size(),
                             cudaMemcpyHostToDevice, c->stream));
     CTX_TRY(cudaMemcpyAsync(c->d_gx, gx.data(), sizeof(double) * nq, cudaMemcpyHostToDevice,
@@ -1093,6 +1106,7 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_geom);
     dfree(c->d_cterm);
     dfree(c->d_geomf);
+    dfree(c->d_coordf);
     dfree(c->d_color_elems);
     dfree(c->d_color_start);
     dfree(c->d_far_items);
@@ -1297,7 +1311,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
                                               c->d_color_start, ncol, c->nnd, c->nel, c->nq,
-                                              c->d_geomf, c->d_geom, c->ph, last,
+                                              c->d_geomf, c->d_geom, c->d_coordf, c->ph, last,
                                               c->d_far_pairs, o64,
                                               count ? c->d_far_items : nullptr, c->stream, 1,
                                               true));
@@ -1360,7 +1374,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
                                               c->d_color_start, ncol, c->nnd, c->nel, c->nq,
-                                              c->d_geomf, c->d_geom, c->ph, last,
+                                              c->d_geomf, c->d_geom, c->d_coordf, c->ph, last,
                                               c->d_far_pairs, o32,
                                               count ? c->d_far_items : nullptr, c->stream));
             prof_end(c, pe, 0, 0);

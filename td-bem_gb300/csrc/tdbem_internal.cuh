@@ -87,8 +87,8 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
 cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
                                      int nnd, int nel, int nq, const float* geomf,
-                                     const double* geom, const Phys& ph, int level_last,
-                                     const PairInfo* pairs, const AsmOut& out,
+                                     const double* geom, const float* coordf, const Phys& ph,
+                                     int level_last, const PairInfo* pairs, const AsmOut& out,
                                      unsigned long long* nitems, cudaStream_t s,
                                      int level_cap = 1 << 30, bool fp64_out = false);
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
@@ -365,6 +365,7 @@ struct tdbem_ctx {
     double* d_geom = nullptr;        // regular Gauss-point geometry, nel x nq^2 x 12
     double* d_cterm = nullptr;       // C term of every node, nnd x 9
     float* d_geomf = nullptr;        // FP32 copy of the geometry (element-relative points)
+    float* d_coordf = nullptr;       // node coordinates as FP32 pairs: hi[3], 0, lo[3], 0
     // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
     std::vector<int> color_start;
     int* d_color_elems = nullptr;
