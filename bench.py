@@ -490,9 +490,9 @@ def run_ours(args, dist):
                     "bf16_mma_tflops": mma_tf}
     elif dom in ("conv", "conv_block"):
         achieved = st["bytes"] / (st["ms"] / 1e3) / 1e9
-        kname = {"conv": "k_conv" if prec == lib.FP64 else "k_conv_f32<NB>",
-                 "conv_block": "k_conv_tc (tcgen05, split-BF16)"
-                 if args.march_engine == "tcgen05" else "k_conv_f32<NB>"}[dom]
+        tc_march = prec != lib.FP64 and args.march_engine == "tcgen05"
+        kname = "k_conv" if prec == lib.FP64 else \
+            "k_conv_tc (tcgen05, split-BF16)" if tc_march else "k_conv_f32<NB>"
         roof = {"bound": "hbm", "kernel": kname, "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "peak_source": f"hbm_gbs of {peak_kind}"}
@@ -510,7 +510,7 @@ def run_ours(args, dist):
     roof["launches"] = st["launches"]
     roof["avg_launch_ms"] = st["ms"] / max(1, st["launches"])
     tkey = f"{args.workload}:{args.precision}:{dom}"
-    if dom == "conv_block":
+    if dom in ("conv", "conv_block") and prec != lib.FP64:
         tkey += f":{args.march_engine}"
     t = traffic.get(tkey)
     if isinstance(t, dict) and "ratio_to_algorithmic" in t:
