@@ -442,6 +442,7 @@ def run_ours(args, dist):
         compare = compare_batch(lib, torch, ctx, model, trac, amp, ms_step)
     elif prec == lib.MIXED and not args.no_compare:
         u32, t32 = ctx.march()  # histories of the mixed form (levels already assembled)
+        ctx.close()  # its level stores make room for the FP64 ones (6x24x24: 125 + 158 GB)
         with lib.Context(model) as c64:
             c64.set_alpha(*ALPHA)
             c64.assemble(precision=lib.FP64)

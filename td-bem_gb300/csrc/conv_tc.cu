@@ -443,12 +443,24 @@ int tc_ldb(int D) { return (D + TC_BK - 1) / TC_BK * TC_BK; }
 int tc_cases_pad(int C) { return (C + TC_BN - 1) / TC_BN * TC_BN; }
 
 int tc_conv_splits(int nlev, int D, int C, int max_splits, int nmat) {
-    // one CTA per SM (197 KB of shared memory each), and at least 16 iterations
-    // (16 x 48 KB) per CTA so the pipeline's fill and drain stay small
-    const int tiles = (D + TC_BM - 1) / TC_BM * ((C + TC_BN - 1) / TC_BN);
+    // One CTA per SM (197 KB of shared memory each) and at least 16 iterations
+    // (16 x 48 KB) per CTA so the pipeline's fill and drain stay small.  The split
+    // count fills the waves best: tiles x splits CTAs in ceil(tiles x splits / 152)
+    // waves of 152 (37 row tiles: 4 splits, 148 CTAs; 82: 11 splits, 902 CTAs in 6
+    // waves), the smallest count within 3 % of the best fill.
+    const int tiles = std::max(1, (D + TC_BM - 1) / TC_BM * ((C + TC_BN - 1) / TC_BN));
     const long long iters = (long long)nlev * nmat * (tc_ldb(D) / TC_BK);
-    const long long s = std::min<long long>(152 / std::max(1, tiles), iters / 16);
-    return (int)std::max<long long>(1, std::min<long long>(s, max_splits));
+    const long long smax =
+        std::max<long long>(1, std::min<long long>({(long long)max_splits, iters / 16, 64}));
+    auto fill = [&](long long s) {
+        const long long ctas = tiles * s, waves = (ctas + 151) / 152;
+        return (double)ctas / (double)(waves * 152);
+    };
+    double best = 0;
+    for (long long s = 1; s <= smax; s++) best = std::max(best, fill(s));
+    for (long long s = 1; s <= smax; s++)
+        if (fill(s) >= best - 0.03) return (int)s;
+    return 1;
 }
 
 cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
