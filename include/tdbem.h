@@ -231,12 +231,13 @@ int tdbem_set_batch_options(tdbem_ctx* ctx, int engine, int refine_sweeps);
  * (on by default; off with on = 0, and off while profiling is on). */
 int tdbem_set_graphs(tdbem_ctx* ctx, int on);
 
-/* Engine of the TDBEM_MIXED marching's per-block pass over the old history (the
- * largest part of the march): TDBEM_ENGINE_TCGEN05 (default; the FP32 levels as BF16
- * hi/lo planes, three BF16 tensor-core products per FP32 product, FP32 accumulation
- * and compensated sums across levels: HBM-bound, history error ~1e-5 of FP64) or
- * TDBEM_ENGINE_FP32 (FP32 products on the CUDA cores: error ~2e-7 of FP64, slower).
- * The tcgen05 engine keeps a second level store of the same size (the planes). */
+/* Engine of the TDBEM_MIXED march's history convolution: TDBEM_ENGINE_TCGEN05
+ * (default; per level one merged matrix, each column the unknown's column of G or -H,
+ * as BF16 hi/lo planes, with the prescribed values' part from three vectors per level;
+ * three BF16 tensor-core products per FP32 product, FP32 accumulation and compensated
+ * sums across levels: HBM-bound, history error ~1e-5 of FP64) or TDBEM_ENGINE_FP32
+ * (G and H with FP32 products on the CUDA cores: error ~2e-7 of FP64, slower).  The
+ * tcgen05 engine keeps the merged planes beside the FP32 levels: half their size. */
 #define TDBEM_ENGINE_FP32 2
 int tdbem_set_march_engine(tdbem_ctx* ctx, int engine);
 
