@@ -1318,7 +1318,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             prof_end(c, pe, 0, 0);
             c->launches += 2;
         }
-        // the C term, regular elements in FP32 (the FP32 store takes it after the far field)
+        // the C term, regular elements in FP32 (the FP32 store gets it with levels 0/1)
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
                               c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true,

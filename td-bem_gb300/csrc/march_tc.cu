@@ -194,16 +194,17 @@ cudaError_t launch_known_terms(const double* known, const void* coef, int D, int
     return cudaGetLastError();
 }
 
-// Coefficients (ct, cl, cu) of the known part for the steps 0..numstep and levels
-// 0..L-1 (see the header): the history terms of the W combination with m >= 1,
-// amp(m) on the prescribed tractions, 1 on the prescribed displacements, and the
-// step's own load with lhs_c0/lhs_c1 at levels 0/1 (step 1: 1 and 0).
+// Coefficients (ct, cl, cu) of the known part for the solve steps 1..numstep-1 and
+// levels 0..L-1 (zero for step 0 and numstep; see the header): the history terms of
+// the W combination with m >= 1, amp(m) on the prescribed tractions, 1 on the
+// prescribed displacements, and the step's own load with lhs_c0/lhs_c1 at levels 0/1
+// (step 1: 1 and 0).  amp: empty (unit load) or at least numstep values.
 void known_coefficients(int numstep, int L, double a1, double a2, double a3,
                         const std::vector<double>& amp, double c0, double c1,
                         std::vector<double>& out) {
     out.assign((size_t)(numstep + 1) * L * 3, 0.0);
     auto A = [&](int m) { return amp.empty() ? 1.0 : amp[m]; };
-    for (int s = 1; s <= numstep; s++)
+    for (int s = 1; s <= numstep - 1; s++)
         for (int f = 0; f < L && f <= s; f++) {
             double ct = 0, cu = 0;
             auto term = [&](int m, double w) {

@@ -132,6 +132,18 @@ def test_long_blocks_need_the_tcgen05_engine(tdlib):
             ctx.set_march_options(20, 0)
 
 
+def test_load_history_of_exactly_numstep_values(tdlib):
+    """A load history with one value per step (the shortest accepted) marches like the
+    same history with an extra trailing value, in both engines."""
+    m = bar_with_prescribed_values()
+    amp = np.minimum(1.0, np.arange(m.numstep) / 20.0)
+    for engine in (tdlib.ENGINE_TCGEN05, tdlib.ENGINE_FP32):
+        u1, t1, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1), amp=amp, engine=engine)
+        u2, t2, _ = run(tdlib, m, tdlib.MIXED, alpha=(0.25, 0.1), engine=engine,
+                        amp=np.append(amp, 7.0))
+        assert np.array_equal(u1, u2) and np.array_equal(t1, t2)
+
+
 def test_new_boundary_values_reach_the_merged_levels(tdlib):
     """tdbem_set_bc between two marches of one assembly: the second march uses the
     new values (the merged levels and their known part are rebuilt)."""
