@@ -335,9 +335,13 @@ class Context:
         _check(load().tdbem_set_alpha(self.h, a1, a2))
 
     def set_march_options(self, block_steps: int = 0, refine_sweeps: int = 0):
+        """Time-block steps of the mixed march (0: the engine's default, 32 with
+        ENGINE_TCGEN05 and 8 with ENGINE_FP32) and FP64 refinement sweeps per solve."""
         _check(load().tdbem_set_march_options(self.h, block_steps, refine_sweeps))
 
     def set_march_engine(self, engine: int):
+        """ENGINE_TCGEN05 (default: merged levels, split-BF16 tensor-core products, ~1e-5
+        of FP64) or ENGINE_FP32 (FP32 products on the CUDA cores, ~2e-7)."""
         _check(load().tdbem_set_march_engine(self.h, engine))
 
     def set_graphs(self, on: bool):
