@@ -195,6 +195,9 @@ void free_batch(tdbem_ctx* c) {
     c->d_tc_W = nullptr;
     c->tc_W_bytes = 0;
     dfree(c->d_tc_err);
+    dfree(c->d_bkt);
+    dfree(c->d_bGK);
+    dfree(c->d_bGL);
 }
 
 void free_march(tdbem_ctx* c) {
@@ -515,6 +518,45 @@ int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     return rc2;
 }
 
+// The merged level planes of the tcgen05 march and the known part's vectors (once
+// per assembly and boundary conditions; march_tc.cu), from the FP32 levels.
+int ensure_merged_levels(tdbem_ctx* c) {
+    const int D = c->D, M = c->M;
+    cudaStream_t s = c->stream;
+    if (c->mtc_planes_valid) return TDBEM_OK;
+    if (!c->d_mtc_planes)
+        CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, M + 1, 1)));
+    if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
+    if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
+    // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
+    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
+    std::vector<double> umap(D, 0.0), fmap(D, 0.0);
+    for (size_t i = 0; i < c->ubc.size(); i++) {
+        is_u[c->ubc[i]] = 1;
+        umap[c->ubc[i]] = c->ubc_v[i];
+    }
+    for (size_t i = 0; i < c->fbc.size(); i++) {
+        is_f[c->fbc[i]] = 1;
+        fmap[c->fbc[i]] = c->fbc_v[i];
+    }
+    std::vector<float> bcv((size_t)3 * D, 0.f);
+    for (int j = 0; j < D; j++) {
+        if (is_f[j] && (!is_u[j] || j == D - 1)) bcv[j] = (float)fmap[j];
+        if (is_f[j] && !is_u[j]) bcv[D + j] = (float)fmap[j];
+        if (is_u[j]) bcv[2 * D + j] = (float)umap[j];
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->d_mtc_bc, bcv.data(), sizeof(float) * bcv.size(),
+                             cudaMemcpyHostToDevice, s));
+    const int pe = prof_begin(c, TDBEM_K_AUX);
+    CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_is_ubc,
+                                 c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
+                                 c->d_mtc_planes, c->d_mtc_known, s));
+    prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
+    c->launches += 1;
+    c->mtc_planes_valid = true;
+    return TDBEM_OK;
+}
+
 // Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
 // inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
 int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
@@ -555,38 +597,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     const bool tc = c->march_engine == TDBEM_ENGINE_TCGEN05;
     const int Lw = M + 1;
     if (tc) {
-        if (!c->mtc_planes_valid) {
-            if (!c->d_mtc_planes)
-                CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, M + 1, 1)));
-            if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
-            if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
-            // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
-            std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
-            std::vector<double> umap(D, 0.0), fmap(D, 0.0);
-            for (size_t i = 0; i < c->ubc.size(); i++) {
-                is_u[c->ubc[i]] = 1;
-                umap[c->ubc[i]] = c->ubc_v[i];
-            }
-            for (size_t i = 0; i < c->fbc.size(); i++) {
-                is_f[c->fbc[i]] = 1;
-                fmap[c->fbc[i]] = c->fbc_v[i];
-            }
-            std::vector<float> bcv((size_t)3 * D, 0.f);
-            for (int j = 0; j < D; j++) {
-                if (is_f[j] && (!is_u[j] || j == D - 1)) bcv[j] = (float)fmap[j];
-                if (is_f[j] && !is_u[j]) bcv[D + j] = (float)fmap[j];
-                if (is_u[j]) bcv[2 * D + j] = (float)umap[j];
-            }
-            CUDA_TRY(cudaMemcpyAsync(c->d_mtc_bc, bcv.data(), sizeof(float) * bcv.size(),
-                                     cudaMemcpyHostToDevice, s));
-            const int pe = prof_begin(c, TDBEM_K_AUX);
-            CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_is_ubc,
-                                         c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
-                                         c->d_mtc_planes, c->d_mtc_known, s));
-            prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
-            c->launches += 1;
-            c->mtc_planes_valid = true;
-        }
+        const int rm = ensure_merged_levels(c);
+        if (rm != TDBEM_OK) return rm;
         std::vector<double> key = {(double)numstep, (double)(M + 1), a1, a2,
                                    lhs_c[1][0], lhs_c[1][1]};
         key.insert(key.end(), c->amp.begin(), c->amp.end());
@@ -1540,8 +1552,8 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         CUDA_TRY(dalloc(&c->d_bWu, (size_t)(M + 1) * C * ldw));
         int smax = batch_apply_splits(D, C);
         for (int nlev = 2; nlev <= M + 1; nlev++)
-            smax = std::max(smax, std::max(batch_conv_splits(nlev, D, C),
-                                           tc_conv_splits(nlev, D, C)));
+            smax = std::max({smax, batch_conv_splits(nlev, D, C),
+                             tc_conv_splits(nlev, D, C, 1 << 30, 1)});
         c->bpart_cap = (size_t)smax * CD;
         CUDA_TRY(dalloc(&c->d_bpart, c->bpart_cap));
         CUDA_TRY(dalloc(&c->d_brhs, CD));
@@ -1563,20 +1575,16 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
     const int rc = mixed_inverses(c, numstep, lhs_c);
     if (rc != TDBEM_OK) return rc;
 
+    // tcgen05 engine: the merged level planes of the single march (the cases share the
+    // boundary-condition types) and, per case, its known tractions times every level
     const bool tc = c->batch_engine == TDBEM_ENGINE_TCGEN05;
     const int Lw = M + 1;
     if (tc) {
         if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 1));
         CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), s));
-        if (!c->tc_planes_valid) {
-            if (!c->d_tc_planes) CUDA_TRY(cudaMalloc(&c->d_tc_planes, tc_plane_bytes(D, M + 1)));
-            const int pe = prof_begin(c, TDBEM_K_AUX);
-            CUDA_TRY(launch_split_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_tc_planes, s));
-            prof_end(c, pe, 2.0 * (M + 1) * (double)D * (c->ldf + tc_ldb(D)) * 4, 0);
-            c->launches += 1;
-            c->tc_planes_valid = true;
-        }
-        const size_t wb = tc_w_bytes(D, C, Lw);
+        const int rm = ensure_merged_levels(c);
+        if (rm != TDBEM_OK) return rm;
+        const size_t wb = tc_w_bytes(D, C, Lw, 1);
         if (c->tc_W_bytes < wb) {
             if (c->d_tc_W) cudaFree(c->d_tc_W);
             c->d_tc_W = nullptr;
@@ -1584,8 +1592,22 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
             CUDA_TRY(cudaMalloc(&c->d_tc_W, wb));
             c->tc_W_bytes = wb;
         }
-        if (!make_tc_maps(c->d_tc_planes, D, M + 1, c->d_tc_W, C, Lw, &c->tc_maps))
+        if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_tc_W, C, Lw, &c->tc_maps, 1))
             return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched planes");
+        if (!c->d_bkt) {
+            CUDA_TRY(dalloc(&c->d_bkt, 2 * CD));
+            CUDA_TRY(dalloc(&c->d_bGK, (size_t)(M + 1) * CD));
+            CUDA_TRY(dalloc(&c->d_bGL, 2 * CD));
+        }
+        const int pk = prof_begin(c, TDBEM_K_AUX);
+        CUDA_TRY(launch_batch_known_tractions(c->d_btrac, c->d_is_ubc, D, C, c->d_bkt,
+                                              c->d_bkt + CD, s));
+        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, M + 1, c->d_bkt, C, c->d_bGK,
+                                      c->device, s));
+        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, std::min(2, M + 1), c->d_bkt + CD, C,
+                                      c->d_bGL, c->device, s));
+        prof_end(c, pk, (M + 3) * (double)D * c->ldf * 4, 2.0 * (M + 3) * (double)D * D * C);
+        c->launches += 3;
     }
 
     EventTimer tmr;
@@ -1599,18 +1621,21 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
         const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
         int pe;
-        if (tc) {
-            CUDA_TRY(launch_build_w_tc(c->d_bu, c->d_bt, D, C, st, nlev, Lw, a1, a2, a3, c0, c1,
-                                       d_amp, numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map,
-                                       c->d_tc_W, s));
-            const int splits = tc_conv_splits(nlev, D, C);
+        if (tc) {  // merged levels: the unknowns' history, then the known values' part
+            CUDA_TRY(launch_build_w_batch_merged(c->d_bu, c->d_bt, c->d_is_ubc, D, C, st, nlev,
+                                                 Lw, a1, a2, a3, c->d_tc_W, s));
+            const int splits = tc_conv_splits(nlev, D, C, 1 << 30, 1);
             const double ldb = tc_ldb(D), cp = tc_cases_pad(C);
             pe = prof_begin(c, TDBEM_K_CONV_BATCH);
             CUDA_TRY(launch_conv_tc(c->tc_maps, D, M + 1, Lw, nlev, C, c->d_bpart, splits,
-                                    c->d_tc_err, s));
-            prof_end(c, pe, nlev * 2.0 * (double)D * ldb * 4 + nlev * 2.0 * cp * ldb * 4,
-                     nlev * 4.0 * DD * C);
+                                    c->d_tc_err, s, 1));
+            prof_end(c, pe, nlev * (double)D * ldb * 4 + nlev * cp * ldb * 4,
+                     nlev * 2.0 * DD * C);
             CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
+            const double* hu = c->d_mtc_known + (size_t)2 * (M + 1) * D;  // H^f ubc
+            CUDA_TRY(launch_known_batch(c->d_bGK, c->d_bGL, hu, D, C, M + 1, st, a1, a2, a3, c0,
+                                        c1, d_amp, numstep, c->d_brhs, s));
+            c->launches += 1;
         } else {
             CUDA_TRY(launch_build_w_batch(c->d_bu, c->d_bt, D, C, st, nlev, a1, a2, a3, c0, c1,
                                           d_amp, numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map,

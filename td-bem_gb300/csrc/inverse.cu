@@ -812,6 +812,25 @@ void blas_return(int dev, void* h) {
     p.free_handles.push_back(static_cast<cublasHandle_t>(h));
 }
 
+cudaError_t levels_times_columns(const float* Gf, int ldf, int D, int nlev, const float* K,
+                                 int C, float* out, int device, cudaStream_t s) {
+    // column-major views: out_f (D x C, ld D) = G_f (row-major, ld ldf: op T) K (D x C)
+    void* h = blas_checkout(device);
+    if (!h) return cudaErrorNotReady;
+    cublasHandle_t hb = static_cast<cublasHandle_t>(h);
+    const float one = 1.f, zero = 0.f;
+    cublasStatus_t st = cublasSetStream(hb, s);
+    if (st == CUBLAS_STATUS_SUCCESS)
+        st = cublasSgemmStridedBatched(hb, CUBLAS_OP_T, CUBLAS_OP_N, D, C, D, &one, Gf, ldf,
+                                       (long long)D * ldf, K, D, 0, &zero, out, D,
+                                       (long long)C * D, nlev);
+    // the handle (and any workspace of its) goes back only after the products ran
+    const cudaError_t e = cudaStreamSynchronize(s);
+    blas_return(device, h);
+    if (e != cudaSuccess) return e;
+    return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
+}
+
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
                        void* blas) {

@@ -158,7 +158,111 @@ __global__ void __launch_bounds__(128) k_known_terms(const double* __restrict__ 
         if (j < nbe) Yk[(size_t)(S + j) * D + row] = acc[j];
 }
 
+// Batched form ([step][case][dof] histories): the merged history vectors of all
+// cases for step s over history steps [1, s), planes [plane*Lw + f][c][ldb].
+__global__ void __launch_bounds__(256) k_build_w_batch_merged(
+    const double* __restrict__ u_hist, const double* __restrict__ t_hist,
+    const unsigned char* __restrict__ is_u, int D, int C, int Cpad, int s, int Lw, double a1,
+    double a2, double a3, int ldb, __nv_bfloat16* __restrict__ W) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y, f = blockIdx.z;
+    if (k >= ldb) return;
+    double w = 0;
+    const int sel = col_sel(is_u, k, D);
+    if (sel) {
+        const double* h = (sel == 1 ? t_hist : u_hist) + (size_t)c * D;  // [m][c][k]
+        w = w_of(h, C * D, k, s, f, 1, s, a1, a2, a3);
+    }
+    const size_t idx = ((size_t)f * Cpad + c) * ldb + k;
+    const size_t plane = (size_t)Lw * Cpad * ldb;
+    const __nv_bfloat16 hb = __float2bfloat16_rn((float)w);
+    W[idx] = hb;
+    W[plane + idx] = __float2bfloat16_rn((float)(w - (double)__bfloat162float(hb)));
+}
+
+// Known tractions of the batched cases as FP32 columns [c][D]: kt (history: every dof
+// but a prescribed-displacement dof below D-1) and lt (the step's own load: the dofs
+// without a prescribed displacement).
+__global__ void k_batch_known_tractions(const double* __restrict__ trac,
+                                        const unsigned char* __restrict__ is_u, int D, int C,
+                                        float* __restrict__ kt, float* __restrict__ lt) {
+    const size_t n = (size_t)C * D;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i % D);
+        const float v = (float)trac[i];
+        kt[i] = (is_u[j] && j < D - 1) ? 0.f : v;
+        lt[i] = is_u[j] ? 0.f : v;
+    }
+}
+
+// Batched right-hand sides of step s, Y[c][row] += the known values' part:
+// sum_f ( ct_c GK[f][c][row] + cl_c GL[f][c][row] (f <= 1) - cu HU[f][row] ) with the
+// coefficients of known_coefficients, case c's amplitude amp[c][m] (or 1).
+__global__ void __launch_bounds__(128) k_known_batch(const float* __restrict__ GK,
+                                                     const float* __restrict__ GL,
+                                                     const double* __restrict__ HU, int D, int C,
+                                                     int L, int s, double a1, double a2,
+                                                     double a3, double c0, double c1,
+                                                     const double* __restrict__ amp,
+                                                     int numstep, double* __restrict__ Y) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    if (row >= D) return;
+    auto A = [&](int m) { return amp ? amp[(size_t)c * numstep + m] : 1.0; };
+    double acc = 0;
+    const int flast = min(L - 1, s);
+    for (int f = 0; f <= flast; f++) {
+        double ct = 0, cu = 0;
+        auto term = [&](int m, double w) {
+            if (m >= 1 && m <= s - 1) {
+                ct += w * A(m);
+                cu += w;
+            }
+        };
+        if (f >= 2) term(s + 1 - f, a1);
+        if (f >= 1) term(s - f, a3);
+        term(s - 1 - f, a2);
+        if (f == 0) term(s - 1, -a1);
+        double v = ct * (double)GK[((size_t)f * C + c) * D + row];
+        if (f <= 1) {
+            const double cf = f == 0 ? c0 : c1;
+            v += cf * A(s) * (double)GL[((size_t)f * C + c) * D + row];
+            cu += cf;
+        }
+        acc += v - cu * HU[(size_t)f * D + row];
+    }
+    Y[(size_t)c * D + row] += acc;
+}
+
 }  // namespace
+
+cudaError_t launch_build_w_batch_merged(const double* u_hist, const double* t_hist,
+                                        const unsigned char* is_u, int D, int C, int s,
+                                        int nlev, int Lw, double a1, double a2, double a3,
+                                        void* W, cudaStream_t st) {
+    if (C < 1 || nlev < 1 || nlev > Lw) return cudaErrorInvalidValue;
+    const int Cpad = tc_cases_pad(C), ldb = tc_ldb(D);
+    const dim3 grid((ldb + 255) / 256, C, nlev);
+    k_build_w_batch_merged<<<grid, 256, 0, st>>>(u_hist, t_hist, is_u, D, C, Cpad, s, Lw, a1,
+                                                 a2, a3, ldb, static_cast<__nv_bfloat16*>(W));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_known_tractions(const double* trac, const unsigned char* is_u, int D,
+                                         int C, float* kt, float* lt, cudaStream_t s) {
+    k_batch_known_tractions<<<1216, 256, 0, s>>>(trac, is_u, D, C, kt, lt);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_known_batch(const float* GK, const float* GL, const double* HU, int D, int C,
+                               int L, int s, double a1, double a2, double a3, double c0,
+                               double c1, const double* amp, int numstep, double* Y,
+                               cudaStream_t st) {
+    const dim3 grid((D + 127) / 128, C);
+    k_known_batch<<<grid, 128, 0, st>>>(GK, GL, HU, D, C, L, s, a1, a2, a3, c0, c1, amp,
+                                        numstep, Y);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
                                 const unsigned char* is_u, const float* kt, const float* lt,

@@ -280,6 +280,22 @@ cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
 // Known part of the right-hand sides of the solve steps 1..last into Yk[step][D].
 cudaError_t launch_known_terms(const double* known, const void* coef, int D, int L, int last,
                                double* Yk, cudaStream_t s);
+// Batched form of the merged march: history planes of all cases, the cases' known
+// tractions as FP32 columns, and the known part of step s added into Y[c][D].
+cudaError_t launch_build_w_batch_merged(const double* u_hist, const double* t_hist,
+                                        const unsigned char* is_u, int D, int C, int s,
+                                        int nlev, int Lw, double a1, double a2, double a3,
+                                        void* W, cudaStream_t st);
+cudaError_t launch_batch_known_tractions(const double* trac, const unsigned char* is_u, int D,
+                                         int C, float* kt, float* lt, cudaStream_t s);
+cudaError_t launch_known_batch(const float* GK, const float* GL, const double* HU, int D, int C,
+                               int L, int s, double a1, double a2, double a3, double c0,
+                               double c1, const double* amp, int numstep, double* Y,
+                               cudaStream_t st);
+// G^f K for levels f < nlev (FP32 levels, ld ldf) and the columns K [c][D]: out
+// [f][c][D] (cuBLAS strided-batched SGEMM with a pooled handle; inverse.cu).
+cudaError_t levels_times_columns(const float* Gf, int ldf, int D, int nlev, const float* K,
+                                 int C, float* out, int device, cudaStream_t s);
 void known_coefficients(int numstep, int L, double a1, double a2, double a3,
                         const std::vector<double>& amp, double c0, double c1,
                         std::vector<double>& out);
@@ -421,6 +437,9 @@ struct tdbem_ctx {
     void* d_tc_planes = nullptr;    // BF16 hi/lo planes of the FP32 levels
     bool tc_planes_valid = false;
     void* d_tc_W = nullptr;         // BF16 hi/lo planes of the batched history vectors
+    float* d_bkt = nullptr;         // batched known tractions as FP32 columns: kt, lt (2 C D)
+    float* d_bGK = nullptr;         // G^f kt of every level and case [f][c][D]
+    float* d_bGL = nullptr;         // G^f lt of levels 0/1 [f][c][D]
     size_t tc_W_bytes = 0;
     int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
     tdbem::TcMaps tc_maps{};

@@ -5,7 +5,7 @@ that case's traction list and load history.  Tolerances: relative L2 error
 <= 1e-4 against the plain FP64 GPU form (itself parity-tested against the
 oracle at 1e-10) over all steps and dofs of the case; duplicated cases in
 different column blocks are bitwise equal; the batch is linear in its loads to
-1e-4 of the history norm; the tcgen05 and mma.sync engines agree to 1e-5."""
+1e-4 of the history norm; the tcgen05 and mma.sync engines agree to 3e-5."""
 import numpy as np
 import pytest
 
@@ -97,17 +97,18 @@ def test_batch_gaussian_patches_sphere(tdlib, engine):
 
 
 def test_batch_engines_agree(tdlib):
-    """tcgen05 and mma.sync compute the same split-BF16 products in different
-    orders: the histories agree to 1e-5 of their norm; rows past a 128-row
-    tile edge (D = 1158) and 70 cases (two column blocks) included."""
+    """tcgen05 (merged levels: the unknowns' history in split-BF16 products, the
+    known tractions' part in FP32) and mma.sync (G and H in split-BF16 products) are
+    each within ~1e-5 of FP64: the histories agree to 3e-5 of their norm; rows past
+    a 128-row tile edge (D = 1158) and 70 cases (two column blocks) included."""
     from tdbem import loads, meshes
     m = meshes.cubed_sphere(8, numstep=60)
     trac, amp = loads.gaussian_patch_cases(m, 70, seed=4, numstep=60)
     u0, _ = batch(tdlib, m, trac, amp, (0.25, 0.0), engine=0)
     u1, _ = batch(tdlib, m, trac, amp, (0.25, 0.0), engine=1)
-    assert np.linalg.norm(u0 - u1) <= 1e-5 * np.linalg.norm(u1)
+    assert np.linalg.norm(u0 - u1) <= 3e-5 * np.linalg.norm(u1)
     for c in (0, 63, 64, 69):
-        assert np.linalg.norm(u0[:, c] - u1[:, c]) <= 1e-5 * np.linalg.norm(u1[:, c])
+        assert np.linalg.norm(u0[:, c] - u1[:, c]) <= 3e-5 * np.linalg.norm(u1[:, c])
 
 
 @pytest.mark.parametrize("engine", [0, 1], ids=["tcgen05", "mma_sync"])
