@@ -168,13 +168,11 @@ void free_levels(tdbem_ctx* c) {
     dfree(c->d_H01);
     c->level_precision = -1;
     c->levels_last = 0;
-    if (c->d_tc_planes) cudaFree(c->d_tc_planes);
-    c->d_tc_planes = nullptr;
     if (c->d_mtc_planes) cudaFree(c->d_mtc_planes);
     c->d_mtc_planes = nullptr;
     dfree(c->d_mtc_known);
     dfree(c->d_mtc_bc);
-    c->tc_planes_valid = c->mtc_planes_valid = false;
+    c->mtc_planes_valid = false;
 }
 
 void free_batch(tdbem_ctx* c) {
@@ -1417,7 +1415,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
     CUDA_TRY(cudaGetLastError());
     prof_flush(c);
     c->levels_last = last;
-    c->tc_planes_valid = c->mtc_planes_valid = false;  // the BF16 planes follow the levels
+    c->mtc_planes_valid = false;  // the merged planes follow the levels
     return TDBEM_OK;
 }
 
@@ -1721,7 +1719,7 @@ int tdbem_update_gh_linear(tdbem_ctx* c, int step, int node_lo, int node_hi, con
         CUDA_TRY(cudaStreamSynchronize(s));  // the temporary is reused for H
     }
     c->levels_last = std::max(c->levels_last, step);
-    c->tc_planes_valid = c->mtc_planes_valid = false;
+    c->mtc_planes_valid = false;
     c->step_inv_ready[0] = c->step_inv_ready[1] = false;
     return TDBEM_OK;
 }
@@ -1915,7 +1913,7 @@ int tdbem_import_levels(tdbem_ctx* c, const char* path) {
         return fail(TDBEM_ERR_ARG, "%s is truncated or the copy failed", path);
     }
     c->levels_last = h.levels_last;
-    c->tc_planes_valid = c->mtc_planes_valid = false;
+    c->mtc_planes_valid = false;
     c->step_inv_ready[0] = c->step_inv_ready[1] = false;
     return TDBEM_OK;
 }
@@ -2106,7 +2104,7 @@ int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int p
     for (int i = 0; i < n; i++) {
         tdbem_ctx* c = ctxs[i];
         c->levels_last = std::min(c->M, nsteps[i]);
-        c->tc_planes_valid = c->mtc_planes_valid = false;
+        c->mtc_planes_valid = false;
         c->step_inv_ready[0] = c->step_inv_ready[1] = false;
         c->timings[0] = ms;
     }

@@ -1,15 +1,16 @@
-// Batched history convolution on the 5th-generation tensor cores (tcgen05).
-//
-// Same product as k_conv_mma (batch.cu),
-//     partial[split][c][row] = sum_f ( G^f[row,:] . Wt[f][c] - H^f[row,:] . Wu[f][c] ),
+// History convolution on the 5th-generation tensor cores (tcgen05), for the single
+// and the batched mixed marches:
+//     partial[split][c][row] = sum_f sum_mat A_mat^f[row,:] . W_mat[f][c]
+// over nmat matrices per level (1: the merged level matrix of march_tc.cu; 2: a G
+// and an H plane pair, W_1 holding -Wu, as k_conv_mma of batch.cu multiplies them),
 // with both operands pre-split into BF16 planes (x = hi + lo, hi = bf16(x),
 // lo = bf16(x - hi)) so that no conversion runs in the product kernel:
-//   level planes  [(mat*2 + plane)*L  + f][row][ldb]   mat 0 = G, 1 = H
-//   vector planes [(mat*2 + plane)*Lw + f][case][ldb]  mat 1 holds -Wu
+//   level planes  [(mat*2 + plane)*L  + f][row][ldb]
+//   vector planes [(mat*2 + plane)*Lw + f][column][ldb]
 // with ldb = D rounded up to 64 (zero-padded K).
 //
-// One CTA owns a 128-row tile of (<= 64) cases and an equal share of the tile's
-// (level, G/H, 64-wide K chunk) iterations, taken in that order, so a share may
+// One CTA owns a 128-row tile of (<= 64) columns and an equal share of the tile's
+// (level, matrix, 64-wide K chunk) iterations, taken in that order, so a share may
 // start and end inside a level (every CTA of the grid streams the same number of
 // level bytes, whatever the level count):
 //   warp 0      TMA producer: per stage a 128 x 64 tile of the hi and lo level
@@ -319,95 +320,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
 }
 
-// FP32 level store [f][row][ldf] -> BF16 hi/lo planes [(mat*2+plane)*L + f][row][ldb].
-__global__ void __launch_bounds__(256) k_split_levels(const float* __restrict__ Gf,
-                                                      const float* __restrict__ Hf, int ldf,
-                                                      int D, int L, int ldb,
-                                                      __nv_bfloat16* __restrict__ P) {
-    // block per row (mat, f, row), 4 columns per thread: a 16-byte load of the FP32
-    // row (ldf is a multiple of 4, its padding zero) and an 8-byte store per plane
-    const size_t rows = (size_t)L * D;  // per matrix
-    const size_t plane = rows * ldb;    // one (mat, plane) block
-    for (size_t rr = blockIdx.x; rr < 2 * rows; rr += gridDim.x) {
-        const int mat = rr >= rows ? 1 : 0;
-        const size_t fr = rr - (size_t)mat * rows;  // f * D + row
-        const float* src = (mat == 0 ? Gf : Hf) + fr * ldf;
-        __nv_bfloat16* hi_row = P + (size_t)(mat * 2) * plane + fr * ldb;
-        __nv_bfloat16* lo_row = P + (size_t)(mat * 2 + 1) * plane + fr * ldb;
-        for (int k = 4 * threadIdx.x; k < ldb; k += 4 * blockDim.x) {
-            float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k < ldf) x = __ldcs(reinterpret_cast<const float4*>(src + k));
-            const float v[4] = {x.x, x.y, x.z, x.w};
-            __align__(8) __nv_bfloat16 h[4], l[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                h[q] = __float2bfloat16_rn(v[q]);
-                l[q] = __float2bfloat16_rn(__fsub_rn(v[q], __bfloat162float(h[q])));
-            }
-            *reinterpret_cast<uint2*>(hi_row + k) = *reinterpret_cast<const uint2*>(h);
-            *reinterpret_cast<uint2*>(lo_row + k) = *reinterpret_cast<const uint2*>(l);
-        }
-    }
-}
-
-// Batched history vectors of step s as BF16 hi/lo planes
-// [(mat*2+plane)*Lw + f][c][ldb] (c < Cpad, zero beyond C and D; mat 1 = -Wu).
-// The combination is that of k_build_w_batch (batch.cu).
-__global__ void k_build_w_tc(const double* __restrict__ u_hist, const double* __restrict__ t_hist,
-                             int D, int C, int Cpad, int s, int nlev, int Lw, double a1, double a2,
-                             double a3, double c0, double c1, const double* __restrict__ amp,
-                             int numstep, const double* __restrict__ traction,
-                             const unsigned char* __restrict__ is_u,
-                             const double* __restrict__ ubc_val, int ldb,
-                             __nv_bfloat16* __restrict__ W) {
-    const size_t total = (size_t)nlev * Cpad * ldb;
-    const size_t plane = (size_t)Lw * Cpad * ldb;
-    const size_t cs = (size_t)C * D;
-    for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const int k = (int)(idx % ldb);
-        const int c = (int)((idx / ldb) % Cpad);
-        const int f = (int)(idx / ((size_t)ldb * Cpad));
-        double wt = 0, wu = 0;
-        if (k < D && c < C) {
-            const size_t o = (size_t)c * D + k;
-            const int m1 = s + 1 - f, m3 = s - f, m2 = s - 1 - f;
-            if (f >= 2 && m1 >= 1) {
-                wt += a1 * t_hist[m1 * cs + o];
-                wu += a1 * u_hist[m1 * cs + o];
-            }
-            if (f >= 1 && m3 >= 1) {
-                wt += a3 * t_hist[m3 * cs + o];
-                wu += a3 * u_hist[m3 * cs + o];
-            }
-            if (m2 >= 1) {
-                wt += a2 * t_hist[m2 * cs + o];
-                wu += a2 * u_hist[m2 * cs + o];
-            }
-            if (f <= 1) {
-                const double cf = f == 0 ? c0 : c1;
-                if (f == 0 && s - 1 >= 1) {
-                    wt -= a1 * t_hist[(size_t)(s - 1) * cs + o];
-                    wu -= a1 * u_hist[(size_t)(s - 1) * cs + o];
-                }
-                const double a = amp ? amp[(size_t)c * numstep + s] : 1.0;
-                if (is_u[k]) wu += cf * ubc_val[k];
-                else wt += cf * (a * traction[o]);
-            }
-        }
-        const double vals[2] = {wt, -wu};
-#pragma unroll
-        for (int mat = 0; mat < 2; mat++) {
-            const float xf = (float)vals[mat];
-            const __nv_bfloat16 hi = __float2bfloat16_rn(xf);
-            const __nv_bfloat16 lo =
-                __float2bfloat16_rn((float)(vals[mat] - (double)__bfloat162float(hi)));
-            W[(size_t)(mat * 2) * plane + idx] = hi;
-            W[(size_t)(mat * 2 + 1) * plane + idx] = lo;
-        }
-    }
-}
-
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
@@ -461,30 +373,6 @@ int tc_conv_splits(int nlev, int D, int C, int max_splits, int nmat) {
     for (long long s = 1; s <= smax; s++)
         if (fill(s) >= best - 0.03) return (int)s;
     return 1;
-}
-
-cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
-                                void* planes, cudaStream_t s) {
-    if (ldf % 4 != 0 || ldf > tc_ldb(D)) return cudaErrorInvalidValue;
-    const size_t rows = 2 * (size_t)L * D;
-    const unsigned grid = (unsigned)std::min<size_t>(rows, 152 * 8);
-    k_split_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, tc_ldb(D),
-                                        static_cast<__nv_bfloat16*>(planes));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D, int C, int s,
-                              int nlev, int Lw, double a1, double a2, double a3, double c0,
-                              double c1, const double* amp, int numstep, const double* traction,
-                              const unsigned char* is_u, const double* ubc_val, void* W,
-                              cudaStream_t st) {
-    const int Cpad = tc_cases_pad(C), ldb = tc_ldb(D);
-    const size_t total = (size_t)nlev * Cpad * ldb;
-    const unsigned grid = (unsigned)std::min<size_t>((total + 255) / 256, 16384);
-    k_build_w_tc<<<grid, 256, 0, st>>>(u_hist, t_hist, D, C, Cpad, s, nlev, Lw, a1, a2, a3, c0,
-                                       c1, amp, numstep, traction, is_u, ubc_val, ldb,
-                                       static_cast<__nv_bfloat16*>(W));
-    return cudaGetLastError();
 }
 
 bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out, int nmat) {

@@ -252,22 +252,15 @@ int tc_ldb(int D);
 int tc_cases_pad(int C);
 // Grid splits of a k_conv_tc launch (each writes its own partial sums: at most
 // max_splits of them fit the caller's buffer).
-// nmat = 2: G and H planes (batched convolution); 1: the mixed march's merged
-// level matrix (march_tc.cu).
-int tc_conv_splits(int nlev, int D, int C, int max_splits = 1 << 30, int nmat = 2);
-size_t tc_plane_bytes(int D, int L, int nmat = 2);
-size_t tc_w_bytes(int D, int C, int Lw, int nmat = 2);
-cudaError_t launch_split_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
-                                void* planes, cudaStream_t s);
-cudaError_t launch_build_w_tc(const double* u_hist, const double* t_hist, int D, int C, int s,
-                              int nlev, int Lw, double a1, double a2, double a3, double c0,
-                              double c1, const double* amp, int numstep, const double* traction,
-                              const unsigned char* is_u, const double* ubc_val, void* W,
-                              cudaStream_t st);
+// nmat: matrices per level in the planes (1: the merged level matrix of the single
+// and batched marches, march_tc.cu; 2: a G and an H plane pair per level).
+int tc_conv_splits(int nlev, int D, int C, int max_splits = 1 << 30, int nmat = 1);
+size_t tc_plane_bytes(int D, int L, int nmat = 1);
+size_t tc_w_bytes(int D, int C, int Lw, int nmat = 1);
 bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out,
-                  int nmat = 2);
+                  int nmat = 1);
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
-                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 2);
+                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 1);
 
 // Mixed march with merged levels on tcgen05 (march_tc.cu).
 cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
@@ -434,8 +427,6 @@ struct tdbem_ctx {
     double* d_br = nullptr;
     int batch_engine = TDBEM_ENGINE_TCGEN05;
     int batch_refine = 0;           // refinement sweeps of the batched solve
-    void* d_tc_planes = nullptr;    // BF16 hi/lo planes of the FP32 levels
-    bool tc_planes_valid = false;
     void* d_tc_W = nullptr;         // BF16 hi/lo planes of the batched history vectors
     float* d_bkt = nullptr;         // batched known tractions as FP32 columns: kt, lt (2 C D)
     float* d_bGK = nullptr;         // G^f kt of every level and case [f][c][D]
