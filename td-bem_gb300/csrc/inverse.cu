@@ -32,6 +32,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <condition_variable>
 #include <mutex>
 #include <string>
 #include <type_traits>
@@ -773,7 +774,9 @@ constexpr int kBlasPool = 8;
 constexpr int kBlasDevices = 64;
 struct BlasPool {
     std::mutex m;
+    std::condition_variable cv;
     bool made = false;
+    int total = 0;
     std::vector<cublasHandle_t> free_handles;
 };
 BlasPool& blas_pool(int dev) {
@@ -792,13 +795,17 @@ void blas_pool_init(int dev) {
         cublasHandle_t h = nullptr;
         if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) break;
         p.free_handles.push_back(h);
+        p.total++;
     }
 }
 
-void* blas_checkout(int dev) {
+// wait: block until a handle is free (each user returns it once its work on the
+// stream has finished); otherwise nullptr when none is free.
+void* blas_checkout(int dev, bool wait) {
     if (dev < 0 || dev >= kBlasDevices) return nullptr;
     BlasPool& p = blas_pool(dev);
-    std::lock_guard<std::mutex> lk(p.m);
+    std::unique_lock<std::mutex> lk(p.m);
+    if (wait && p.total > 0) p.cv.wait(lk, [&] { return !p.free_handles.empty(); });
     if (p.free_handles.empty()) return nullptr;
     cublasHandle_t h = p.free_handles.back();
     p.free_handles.pop_back();
@@ -808,15 +815,18 @@ void* blas_checkout(int dev) {
 void blas_return(int dev, void* h) {
     if (!h || dev < 0 || dev >= kBlasDevices) return;
     BlasPool& p = blas_pool(dev);
-    std::lock_guard<std::mutex> lk(p.m);
-    p.free_handles.push_back(static_cast<cublasHandle_t>(h));
+    {
+        std::lock_guard<std::mutex> lk(p.m);
+        p.free_handles.push_back(static_cast<cublasHandle_t>(h));
+    }
+    p.cv.notify_one();
 }
 
 cudaError_t levels_times_columns(const float* Gf, int ldf, int D, int nlev, const float* K,
                                  int C, float* out, int device, cudaStream_t s) {
     // column-major views: out_f (D x C, ld D) = G_f (row-major, ld ldf: op T) K (D x C)
-    void* h = blas_checkout(device);
-    if (!h) return cudaErrorNotReady;
+    void* h = blas_checkout(device, true);
+    if (!h) return cudaErrorNotReady;  // no handle could be made on this device
     cublasHandle_t hb = static_cast<cublasHandle_t>(h);
     const float one = 1.f, zero = 0.f;
     cublasStatus_t st = cublasSetStream(hb, s);

@@ -208,9 +208,10 @@ cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_sta
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
                        void* blas = nullptr);
 // The device's cuBLAS handle pool (made once, with the device's first context);
-// a handle is used by one thread at a time; nullptr when none is free.
+// a handle is used by one thread at a time.  blas_checkout: nullptr when none is
+// free, or with wait, blocks until one is returned (nullptr if none could be made).
 void blas_pool_init(int dev);
-void* blas_checkout(int dev);
+void* blas_checkout(int dev, bool wait = false);
 void blas_return(int dev, void* h);
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
                                    int L, double a1, double a2, double a3, double c0,
