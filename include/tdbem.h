@@ -215,11 +215,12 @@ int tdbem_march_batch(tdbem_ctx* ctx, int numstep, int nrhs, const double* tract
                       const double* amp, double* u_hist, double* t_hist);
 
 /* Options of tdbem_march_batch.  engine: TDBEM_ENGINE_TCGEN05 (default;
- * tcgen05.mma with TMEM accumulators, TMA-loaded BF16 hi/lo planes of the
- * levels, which take as much device memory again as the FP32 levels) or
- * TDBEM_ENGINE_MMA_SYNC (warp-level mma.sync splitting the FP32 levels on the
- * fly, no extra memory).  refine_sweeps (0..4, default 0): refinement sweeps of
- * the batched solve; the split-BF16 convolution, not the FP32 inverse, sets the
+ * tcgen05.mma with TMEM accumulators over the merged levels of the mixed march
+ * (BF16 hi/lo planes, half the size of the FP32 levels, shared with tdbem_march)
+ * and, per case, its known tractions times every level in FP32) or
+ * TDBEM_ENGINE_MMA_SYNC (warp-level mma.sync on G and H, splitting the FP32 levels
+ * on the fly, no extra memory).  refine_sweeps (0..4, default 0): refinement sweeps
+ * of the batched solve; the split-BF16 convolution, not the FP32 inverse, sets the
  * batched form's error, so the default skips them. */
 #define TDBEM_ENGINE_TCGEN05 0
 #define TDBEM_ENGINE_MMA_SYNC 1
