@@ -251,6 +251,16 @@ int tdbem_set_march_engine(tdbem_ctx* ctx, int engine);
  * sweeps are for LHS matrices whose FP32 inverse is less accurate). */
 int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
 
+/* Limit of each pipeline wait (an mbarrier wait for a TMA copy, an MMA or the
+ * epilogue) in the tcgen05 convolution kernel, in seconds of the GPU's global
+ * timer (0 = the default, 2 s; at most 60).  A wait that runs out makes the kernel
+ * stop its producer, MMA and epilogue roles, wait (2 s at most) for its copies and
+ * MMAs in flight, free its tensor memory and return; the march then fails with
+ * TDBEM_ERR_CUDA naming the wait, and the context stays usable.  The reference has
+ * no device code; this bounds the wait a GPU kernel of this library may spend on a
+ * pipeline stage. */
+int tdbem_set_pipeline_wait(tdbem_ctx* ctx, double seconds);
+
 /* Device pointers of the histories of the last tdbem_march (FP64,
  * (numstep+1) x D each); valid until the next march or destroy. */
 int tdbem_history_device(const tdbem_ctx* ctx, const double** u_hist, const double** t_hist);

@@ -1,24 +1,19 @@
-// C ABI of tdbem-gb300 (include/tdbem.h): context lifetime, element colouring,
-// and the host-side sequencing of the assembly and marching kernels.
-#include <algorithm>
-#include <cmath>
-#include <cstdarg>
-#include <cstdio>
-#include <cstring>
-#include <functional>
-#include <mutex>
-#include <new>
-#include <string>
-#include <thread>
-#include <vector>
-
-#include "tdbem_internal.cuh"
+// C ABI of tdbem-gb300 (include/tdbem.h), context and levels: context lifetime,
+// element colouring, the single-step driver, the level assembly, boundary
+// conditions and weights, the stepwise level placement, profiling counters.
+// The march engines are in capi_march.cu, the batched march in capi_batch.cu,
+// checkpoints in capi_ckpt.cu and the many-mesh calls in capi_group.cu.
+#include "capi_common.cuh"
 
 using namespace tdbem;
+using namespace tdbem::capi;
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace tdbem {
+namespace capi {
 
 int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -28,30 +23,6 @@ int fail(int code, const char* fmt, ...) {
     va_end(ap);
     g_last_error = buf;
     return code;
-}
-
-#define CUDA_TRY(expr)                                                                   \
-    do {                                                                                 \
-        cudaError_t e_ = (expr);                                                         \
-        if (e_ != cudaSuccess) {                                                         \
-            const int code_ = (e_ == cudaErrorMemoryAllocation) ? TDBEM_ERR_NOMEM        \
-                                                                : TDBEM_ERR_CUDA;        \
-            return fail(code_, "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, \
-                        __LINE__);                                                       \
-        }                                                                                \
-    } while (0)
-
-template <typename T>
-cudaError_t dalloc(T** p, size_t count) {
-    *p = nullptr;
-    if (count == 0) count = 1;
-    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
-}
-
-template <typename T>
-void dfree(T*& p) {
-    if (p) cudaFree(p);
-    p = nullptr;
 }
 
 // Gauss tables of ShapeFunctionT::SetNQ (ShapeFunctionT.cpp:71-169); the
@@ -233,15 +204,6 @@ void free_march(tdbem_ctx* c) {
     free_batch(c);
 }
 
-// Algorithmic FP64 operations of one (item, Gauss point) of the level quadrature
-// with both the I and the J part (FMA = 2): geometry 22, four I-part and four
-// J-part wave integrals with their differences 150, kernel scalars 37, the two
-// 3x3 kernels 65, accumulation into the 4 node blocks 124.
-constexpr double kFlopsPerItemPoint = 398.0;
-// The FP32 far-field form (tau variables): geometry 20, wave polynomials and
-// differences 176, scalars 40, kernels 65, accumulation 124.
-constexpr double kFlopsPerItemPointF32 = 425.0;
-
 int prof_begin_on(tdbem_ctx* c, int cls, cudaStream_t s) {
     if (!c->prof) return -1;
     tdbem_ctx::ProfEvent ev{cls, nullptr, nullptr, 0, 0};
@@ -328,637 +290,8 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
     return TDBEM_OK;
 }
 
-struct EventTimer {
-    cudaEvent_t a = nullptr, b = nullptr;
-    EventTimer() {
-        cudaEventCreate(&a);
-        cudaEventCreate(&b);
-    }
-    ~EventTimer() {
-        if (a) cudaEventDestroy(a);
-        if (b) cudaEventDestroy(b);
-    }
-    void start(cudaStream_t s) { cudaEventRecord(a, s); }
-    double stop_ms(cudaStream_t s) {
-        cudaEventRecord(b, s);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        return ms;
-    }
-};
-
-
-// Runs a marching loop (kernel launches only, no host synchronisation) through a
-// CUDA graph: captured on the context's stream the first time and whenever a
-// captured value changes (kind of loop, step count, block size, refinement
-// sweeps, weights, load history, buffer addresses), replayed otherwise.  With
-// profiling on (per-launch events) or graphs off the loop runs directly.
-template <typename F>
-int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const void*>& ptrs,
-                   F loop) {
-    if (c->prof || !c->use_graphs) return loop();
-    MarchGraph& g = c->graph;
-    cudaStream_t s = c->stream;
-    const bool same = g.exec && g.kind == kind && g.numstep == numstep && g.nb == c->nb_eff &&
-                      g.refine == c->n_refine && g.a1 == c->a1 && g.a2 == c->a2 &&
-                      g.amp == c->amp && g.ptrs == ptrs;
-    if (!same) {
-        if (g.exec) cudaGraphExecDestroy(g.exec);
-        g.exec = nullptr;
-        const long long l0 = c->launches;
-        CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        const int rc = loop();
-        cudaGraph_t graph = nullptr;
-        const cudaError_t e = cudaStreamEndCapture(s, &graph);
-        if (rc != TDBEM_OK) {
-            if (graph) cudaGraphDestroy(graph);
-            return rc;
-        }
-        CUDA_TRY(e);
-        const cudaError_t ei = cudaGraphInstantiate(&g.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        CUDA_TRY(ei);
-        g.launches = c->launches - l0;
-        c->launches = l0;
-        g.kind = kind;
-        g.numstep = numstep;
-        g.nb = c->nb_eff;
-        g.refine = c->n_refine;
-        g.a1 = c->a1;
-        g.a2 = c->a2;
-        g.amp = c->amp;
-        g.ptrs = ptrs;
-    }
-    CUDA_TRY(cudaGraphLaunch(g.exec, s));
-    c->launches += g.launches;
-    return TDBEM_OK;
-}
-
-// FP64 column-exchanged LHS and its FP32 inverse for each distinct LHS of the
-// mixed form (step 2 and steps >= 3).  The inverses depend on alpha, the UBC dofs
-// (the column exchange) and levels 0/1; they are kept with that key and reused
-// while it holds (an assembly may have made them already, next to its far field).
-int mixed_ninv(int numstep, const double lhs_c[2][2]) {
-    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-    return (numstep >= 3 && !same) ? 2 : 1;
-}
-
-bool inverses_current(const tdbem_ctx* c, int ninv) {
-    return c->inv_valid && c->inv_n == ninv && c->inv_a1 == c->a1 && c->inv_a2 == c->a2 &&
-           c->inv_ubc == c->ubc;
-}
-
-int prepare_inverses(tdbem_ctx* c, int ninv) {
-    const size_t DD = (size_t)c->D * c->D;
-    for (int v = 0; v < 2; v++) {
-        if (c->d_inv32[1] == c->d_inv32[0]) c->d_inv32[1] = nullptr;
-        if (c->d_Hc64[1] == c->d_Hc64[0]) c->d_Hc64[1] = nullptr;
-    }
-    for (int v = 0; v < ninv; v++) {
-        if (!c->d_Hc64[v]) CUDA_TRY(dalloc(&c->d_Hc64[v], DD));
-        if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
-    }
-    if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(c->D)));
-    for (cudaStream_t* st : {&c->stream2, &c->stream3})
-        if (!*st) CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
-    if (!c->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-    if (!c->ev_fork2) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming));
-    if (ninv == 2) {
-        if (!c->d_inv_scratch32b)
-            CUDA_TRY(dalloc(&c->d_inv_scratch32b, inverse_scratch_elems(c->D)));
-        if (!c->d_perm2) CUDA_TRY(dalloc(&c->d_perm2, (size_t)c->D + 2 * kMaxPivotBlocks));
-        if (!c->d_status2) CUDA_TRY(dalloc(&c->d_status2, 1));
-    }
-    return TDBEM_OK;
-}
-
-struct InvResult {
-    cudaError_t e[2] = {cudaSuccess, cudaSuccess};
-    bool singular[2] = {false, false};
-    long long launches[2] = {0, 0};
-};
-
-// The inverses on streams s0 and s1 (s1 after s0's prior work): the second from a
-// second host thread, as each inverse leaves most SMs idle during its pivot
-// searches (one cluster of 16 CTAs) and the two overlap.  Touches no profiling
-// state or shared counter, so it may run on a helper thread; returns after both
-// streams have finished.
-void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t s0,
-                  cudaStream_t s1, InvResult& r) {
-    const int D = c->D;
-    const size_t DD = (size_t)D * D;
-    auto invert = [&](int v, cudaStream_t st, int* perm, int* status, float* scratch) {
-        // a cuBLAS handle of the device's pool for the trailing updates (without one
-        // the inverse uses its own update kernel)
-        void* blas = blas_checkout(c->device);
-        r.e[v] = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
-                                  lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
-        if (r.e[v] == cudaSuccess)
-            r.e[v] = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
-                                &r.launches[v], &r.singular[v], st, blas);
-        blas_return(c->device, blas);  // invert_f32 synchronises its stream before returning
-        r.launches[v] += 1;
-    };
-    if (ninv == 2) {
-        r.e[1] = cudaEventRecord(c->ev_fork2, s0);  // levels 0/1 and the maps are ready
-        if (r.e[1] == cudaSuccess) r.e[1] = cudaStreamWaitEvent(s1, c->ev_fork2, 0);
-        if (r.e[1] != cudaSuccess) return;
-        std::thread second([&] {
-            cudaSetDevice(c->device);
-            invert(1, s1, c->d_perm2, c->d_status2, c->d_inv_scratch32b);
-        });
-        invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
-        second.join();  // both inverses end with a synchronisation of their stream
-    } else {
-        invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
-    }
-}
-
-int finish_inverses(tdbem_ctx* c, int ninv, const InvResult& r) {
-    for (int v = 0; v < ninv; v++) {
-        c->launches += r.launches[v];
-        CUDA_TRY(r.e[v]);
-        if (r.singular[v])
-            return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
-    }
-    if (ninv == 1) {
-        if (c->d_inv32[1] && c->d_inv32[1] != c->d_inv32[0]) dfree(c->d_inv32[1]);
-        if (c->d_Hc64[1] && c->d_Hc64[1] != c->d_Hc64[0]) dfree(c->d_Hc64[1]);
-        c->d_inv32[1] = c->d_inv32[0];
-        c->d_Hc64[1] = c->d_Hc64[0];
-    }
-    c->inv_valid = true;
-    c->inv_n = ninv;
-    c->inv_a1 = c->a1;
-    c->inv_a2 = c->a2;
-    c->inv_ubc = c->ubc;
-    return TDBEM_OK;
-}
-
-// The inverses for a march of numstep steps, unless current; c->timings[1] gets
-// the time taken (left as it is when they are reused).
-int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
-    const int ninv = mixed_ninv(numstep, lhs_c);
-    if (inverses_current(c, ninv)) return TDBEM_OK;
-    const int rc = prepare_inverses(c, ninv);
-    if (rc != TDBEM_OK) return rc;
-    cudaStream_t s = c->stream;
-    EventTimer tf;
-    tf.start(s);
-    const int pe = prof_begin(c, TDBEM_K_FACTOR);
-    InvResult r;
-    run_inverses(c, ninv, lhs_c, s, c->stream2, r);
-    const double DD = (double)c->D * c->D;
-    prof_end(c, pe, ninv * 2.0 * 4 * DD, ninv * 2.0 * DD * c->D);
-    const int rc2 = finish_inverses(c, ninv, r);
-    c->timings[1] = tf.stop_ms(s);
-    return rc2;
-}
-
-// The merged level planes of the tcgen05 march and the known part's vectors (once
-// per assembly and boundary conditions; march_tc.cu), from the FP32 levels.
-int ensure_merged_levels(tdbem_ctx* c) {
-    const int D = c->D, M = c->M;
-    cudaStream_t s = c->stream;
-    if (c->mtc_planes_valid) return TDBEM_OK;
-    if (!c->d_mtc_planes)
-        CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, M + 1, 1)));
-    if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
-    if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
-    // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
-    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
-    std::vector<double> umap(D, 0.0), fmap(D, 0.0);
-    for (size_t i = 0; i < c->ubc.size(); i++) {
-        is_u[c->ubc[i]] = 1;
-        umap[c->ubc[i]] = c->ubc_v[i];
-    }
-    for (size_t i = 0; i < c->fbc.size(); i++) {
-        is_f[c->fbc[i]] = 1;
-        fmap[c->fbc[i]] = c->fbc_v[i];
-    }
-    std::vector<float> bcv((size_t)3 * D, 0.f);
-    for (int j = 0; j < D; j++) {
-        if (is_f[j] && (!is_u[j] || j == D - 1)) bcv[j] = (float)fmap[j];
-        if (is_f[j] && !is_u[j]) bcv[D + j] = (float)fmap[j];
-        if (is_u[j]) bcv[2 * D + j] = (float)umap[j];
-    }
-    CUDA_TRY(cudaMemcpyAsync(c->d_mtc_bc, bcv.data(), sizeof(float) * bcv.size(),
-                             cudaMemcpyHostToDevice, s));
-    const int pe = prof_begin(c, TDBEM_K_AUX);
-    CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_is_ubc,
-                                 c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
-                                 c->d_mtc_planes, c->d_mtc_known, s));
-    prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
-    c->launches += 1;
-    c->mtc_planes_valid = true;
-    return TDBEM_OK;
-}
-
-// Mixed-precision marching: FP32 levels with time blocks of c->nb steps, FP32
-// inverse of each distinct LHS, FP64 residual refinement against the FP64 LHS.
-int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
-    // block steps: the setting, or each engine's measured optimum on the 4614-DOF sphere
-    const int nb = c->nb ? c->nb : (c->march_engine == TDBEM_ENGINE_TCGEN05 ? 32 : 8);
-    const int D = c->D, M = c->M;
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    const size_t DD = (size_t)D * D;
-    const int ldw = mixed_ldw(D);
-    cudaStream_t s = c->stream;
-    if (nb > 16 && c->march_engine != TDBEM_ENGINE_TCGEN05)
-        return fail(TDBEM_ERR_ARG, "block_steps %d needs the tcgen05 march engine (FP32: <= 16)",
-                    nb);
-    c->nb_eff = nb;
-    if (c->d_Wt_old && c->nb_alloc != nb) {  // scratch sized by the block
-        dfree(c->d_Wt_old);
-        dfree(c->d_Wu_old);
-        dfree(c->d_Yold);
-        dfree(c->d_pmix);
-        dfree(c->d_res);
-        dfree(c->d_dx);
-    }
-    if (!c->d_Wt_old) {
-        c->nb_alloc = nb;
-        CUDA_TRY(dalloc(&c->d_Wt_old, (size_t)(M + 1) * nb * ldw));
-        CUDA_TRY(dalloc(&c->d_Wu_old, (size_t)(M + 1) * nb * ldw));
-        CUDA_TRY(dalloc(&c->d_Yold, (size_t)nb * D));
-        CUDA_TRY(dalloc(&c->d_pmix, (size_t)(M + 1) * nb * D));
-        CUDA_TRY(dalloc(&c->d_res, D));
-        CUDA_TRY(dalloc(&c->d_dx, D));
-    }
-    const int rc = mixed_inverses(c, numstep, lhs_c);
-    if (rc != TDBEM_OK) return rc;
-    // tcgen05 engine: the merged level matrix as BF16 hi/lo planes and the known
-    // part's vectors (once per assembly and boundary conditions), the known part's
-    // coefficients (once per load history, weights and step count), the history
-    // vectors' planes and the tensor maps
-    const bool tc = c->march_engine == TDBEM_ENGINE_TCGEN05;
-    const int Lw = M + 1;
-    if (tc) {
-        const int rm = ensure_merged_levels(c);
-        if (rm != TDBEM_OK) return rm;
-        std::vector<double> key = {(double)numstep, (double)(M + 1), a1, a2,
-                                   lhs_c[1][0], lhs_c[1][1]};
-        key.insert(key.end(), c->amp.begin(), c->amp.end());
-        if (key != c->mtc_coef_key) {
-            std::vector<double> tab;
-            known_coefficients(numstep, M + 1, a1, a2, a3, c->amp, lhs_c[1][0], lhs_c[1][1], tab);
-            if (c->mtc_coef_cap < tab.size()) {
-                dfree(c->d_mtc_coef);
-                c->mtc_coef_cap = 0;
-                CUDA_TRY(dalloc(&c->d_mtc_coef, tab.size()));
-                c->mtc_coef_cap = tab.size();
-            }
-            CUDA_TRY(cudaMemcpyAsync(c->d_mtc_coef, tab.data(), sizeof(double) * tab.size(),
-                                     cudaMemcpyHostToDevice, s));
-            c->mtc_coef_key = key;
-        }
-        const size_t yk = (size_t)(numstep + 1) * D;
-        if (c->mtc_yk_cap < yk) {
-            dfree(c->d_mtc_yk);
-            c->mtc_yk_cap = 0;
-            CUDA_TRY(dalloc(&c->d_mtc_yk, yk));
-            c->mtc_yk_cap = yk;
-        }
-        const size_t wb = tc_w_bytes(D, nb, Lw, 1);
-        if (c->mtc_W_bytes < wb) {
-            if (c->d_mtc_W) cudaFree(c->d_mtc_W);
-            c->d_mtc_W = nullptr;
-            c->mtc_W_bytes = 0;
-            c->mtc_maps_for[0] = c->mtc_maps_for[1] = nullptr;
-            CUDA_TRY(cudaMalloc(&c->d_mtc_W, wb));
-            c->mtc_W_bytes = wb;
-        }
-        if (c->mtc_maps_for[0] != c->d_mtc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
-            c->mtc_nb != nb) {
-            if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_mtc_W, nb, Lw, &c->mtc_maps, 1))
-                return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the march planes");
-            c->mtc_maps_for[0] = c->d_mtc_planes;
-            c->mtc_maps_for[1] = c->d_mtc_W;
-            c->mtc_nb = nb;
-        }
-        if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 1));
-        CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), s));
-    }
-
-    EventTimer tmr;
-    tmr.start(s);
-    const size_t lstride = (size_t)D * c->ldf;
-    const int last_s = numstep - 1;  // solve steps 1..numstep-1
-    const std::vector<const void*> ptrs = {
-        c->d_u,       c->d_t,       c->d_Gf,      c->d_Hf,      c->d_inv32[0], c->d_inv32[1],
-        c->d_Hc64[0], c->d_Hc64[1], c->d_Wt_old,  c->d_Wu_old,  c->d_Yold,     c->d_pmix,
-        c->d_x,       c->d_res,     c->d_dx,      c->d_load_t,  c->d_load_u,   c->d_is_ubc,
-        c->d_ubc_map, c->d_is_fbc,  c->d_fbc_map, tc ? c->d_mtc_planes : nullptr,
-        tc ? c->d_mtc_W : nullptr,  tc ? c->d_tc_err : nullptr,  tc ? c->d_mtc_known : nullptr,
-        tc ? c->d_mtc_coef : nullptr, tc ? c->d_mtc_yk : nullptr};
-    // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
-    // Old pass: history before the block and the steps' known-load terms.
-    auto old_pass = [&](int S, int nbe) -> int {
-        const int nlev = (S > 1 ? std::min(M, S + nbe - 1) : std::min(M, 1)) + 1;
-        BlockLoads bl{};  // the FP32 engine's known-load terms (its blocks: <= 16 steps)
-        bl.nload = tc ? 0 : nbe;
-        bl.load_t = c->d_load_t;
-        bl.load_u = c->d_load_u;
-        for (int j = 0; j < bl.nload; j++) {
-            const int st = S + j;
-            bl.amp[j] = c->amp.empty() ? 1.0 : c->amp[st];
-            bl.c0[j] = st == 1 ? 1.0 : lhs_c[1][0];
-            bl.c1[j] = st == 1 ? 0.0 : lhs_c[1][1];
-        }
-        if (tc) {  // merged levels, split-BF16 products on the tensor cores
-            double* Y = c->d_Yold;
-            const double* yk = c->d_mtc_yk + (size_t)S * D;  // the steps' known part
-            if (S == 1) {  // no unknown history before the first block
-                CUDA_TRY(cudaMemcpyAsync(Y, yk, sizeof(double) * nbe * D,
-                                         cudaMemcpyDeviceToDevice, s));
-            } else {
-                CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, S, nbe, nb, 1, S,
-                                               nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
-                // d_pmix holds (M+1) x nb x D partial sums
-                const int splits = tc_conv_splits(nlev, D, nbe, (M + 1) * nb / nbe, 1);
-                const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
-                CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, nbe, c->d_pmix, splits,
-                                        c->d_tc_err, s, 1));
-                prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
-                                    nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
-                         nlev * 2.0 * nbe * (double)DD);
-                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, yk, Y, s));
-                c->launches += 3;
-            }
-            return TDBEM_OK;
-        }
-        CUDA_TRY(launch_build_w_old(c->d_u, c->d_t, D, S, nb, nlev, a1, a2, a3, bl, ldw,
-                                    c->d_Wt_old, c->d_Wu_old, s));
-        const int nch = mixed_chunks(nlev, D);
-        int nparts = 0;
-        const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
-        CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nb,
-                                 c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
-                                 mixed_ksplit(nch, D, M + 1), &nparts, s));
-        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nb * ldw * 4,
-                 nlev * 4.0 * nb * (double)DD);
-        CUDA_TRY(launch_reduce_cols(c->d_pmix, nparts, nb, D, nullptr, c->d_Yold, s));
-        c->launches += 3;
-        return TDBEM_OK;
-    };
-    // The history of steps [a, b) into the right-hand sides of steps [b, e): levels
-    // 0..e-a, e-b columns (padded to a kernel width).
-    auto cross = [&](int S, int a, int b, int e) -> int {
-        const int ncol = e - b;
-        const int nbp = ncol <= 1 ? 1 : ncol <= 2 ? 2 : ncol <= 4 ? 4 : ncol <= 8 ? 8 : 16;
-        const int nlev = std::min(M, e - a) + 1;
-        double* y = c->d_Yold + (size_t)(b - S) * D;
-        if (tc) {
-            CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, b, ncol, nb, a, b,
-                                           nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
-            const int splits = tc_conv_splits(nlev, D, ncol, (M + 1) * nb / ncol, 1);
-            const int pe = prof_begin(c, TDBEM_K_CONV);
-            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, ncol, c->d_pmix, splits,
-                                    c->d_tc_err, s, 1));
-            prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
-                                nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
-                     nlev * 2.0 * ncol * (double)DD);
-            CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s));
-            c->launches += 3;
-            return TDBEM_OK;
-        }
-        CUDA_TRY(launch_build_w_cross(c->d_u, c->d_t, D, a, b, ncol, nbp, nlev, a1, a2, a3, ldw,
-                                      c->d_Wt_old, c->d_Wu_old, s));
-        const int nch = mixed_chunks(nlev, D);
-        int nparts = 0;
-        const int pe = prof_begin(c, TDBEM_K_CONV);
-        CUDA_TRY(launch_conv_f32(c->d_Gf, c->d_Hf, lstride, c->ldf, D, 0, nlev - 1, nbp,
-                                 c->d_Wt_old, c->d_Wu_old, ldw, c->d_pmix, nch,
-                                 mixed_ksplit(nch, D, (M + 1) * nb / nbp), &nparts, s));
-        prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * nbp * ldw * 4,
-                 nlev * 4.0 * ncol * (double)DD);
-        CUDA_TRY(launch_reduce_cols_n(c->d_pmix, nparts, nbp, ncol, D, y, y, s));
-        c->launches += 3;
-        return TDBEM_OK;
-    };
-    // Step st from its accumulated right-hand side.
-    auto solve = [&](int S, int st) -> int {
-        const int pe = prof_begin(c, TDBEM_K_SOLVE);
-        const int v = st == 1 ? 0 : 1;
-        const double amp = c->amp.empty() ? 1.0 : c->amp[st];
-        // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
-        CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_Yold + (size_t)(st - S) * D,
-                                    c->d_x, c->d_res, reinterpret_cast<float*>(c->d_dx),
-                                    c->n_refine, s));
-        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
-        prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine),
-                 2.0 * (double)DD * (1 + 2 * c->n_refine));
-        c->launches += 4 + 2LL * c->n_refine;  // cast, gemv(s), residual(s), update
-        return TDBEM_OK;
-    };
-    // Steps [s0, s0 + n) of the block starting at S: first half, its history into
-    // the second half, second half.
-    std::function<int(int, int, int)> rec = [&](int S, int s0, int n) -> int {
-        if (n == 1) return solve(S, s0);
-        const int h = n / 2;
-        int r = rec(S, s0, h);
-        if (r == TDBEM_OK) r = cross(S, s0, s0 + h, s0 + n);
-        if (r == TDBEM_OK) r = rec(S, s0 + h, n - h);
-        return r;
-    };
-    const int lrc = run_march_loop(c, 1, numstep, ptrs, [&]() -> int {
-        if (tc) {  // the known part of every step's right-hand side
-            const int pk = prof_begin(c, TDBEM_K_AUX);
-            CUDA_TRY(launch_known_terms(c->d_mtc_known, c->d_mtc_coef, D, M + 1, last_s,
-                                        c->d_mtc_yk, s));
-            prof_end(c, pk, 3.0 * (M + 1) * D * 8 * ((last_s + 15) / 16) + 8.0 * last_s * D, 0);
-            c->launches += 1;
-        }
-        for (int S = 1; S <= last_s; S += nb) {
-            const int nbe = std::min(nb, last_s - S + 1);
-            int r = old_pass(S, nbe);
-            if (r == TDBEM_OK) r = rec(S, S, nbe);
-            if (r != TDBEM_OK) return r;
-        }
-        return TDBEM_OK;
-    });
-    if (lrc != TDBEM_OK) return lrc;
-    if (tc) {  // a bounded pipeline wait of the tcgen05 kernel that ran out
-        int err = 0;
-        CUDA_TRY(cudaMemcpyAsync(&err, c->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaStreamSynchronize(s));
-        if (err)
-            return fail(TDBEM_ERR_CUDA, "tcgen05 convolution: pipeline wait timed out (code %d)",
-                        err);
-    }
-    c->timings[2] = tmr.stop_ms(s);
-    return TDBEM_OK;
-}
-
-
-// Per-dof boundary-condition maps and the marching scratch shared by every
-// marching form.
-int upload_bc(tdbem_ctx* c) {
-    const int D = c->D;
-    // per-dof boundary-condition maps; the last list entry of a dof wins (VecSetValues)
-    std::vector<unsigned char> is_u(D, 0), is_f(D, 0);
-    std::vector<double> umap(D, 0.0), fmap(D, 0.0), load_t(D, 0.0), load_u(D, 0.0);
-    for (size_t i = 0; i < c->ubc.size(); i++) {
-        is_u[c->ubc[i]] = 1;
-        umap[c->ubc[i]] = c->ubc_v[i];
-    }
-    for (size_t i = 0; i < c->fbc.size(); i++) {
-        is_f[c->fbc[i]] = 1;
-        fmap[c->fbc[i]] = c->fbc_v[i];
-    }
-    for (int j = 0; j < D; j++) {
-        if (is_u[j]) load_u[j] = umap[j];
-        else if (is_f[j]) load_t[j] = fmap[j];
-    }
-    if (!c->d_ubc_map) {
-        CUDA_TRY(dalloc(&c->d_ubc_map, D));
-        CUDA_TRY(dalloc(&c->d_fbc_map, D));
-        CUDA_TRY(dalloc(&c->d_is_ubc, D));
-        CUDA_TRY(dalloc(&c->d_is_fbc, D));
-        CUDA_TRY(dalloc(&c->d_load_t, D));
-        CUDA_TRY(dalloc(&c->d_load_u, D));
-        CUDA_TRY(dalloc(&c->d_Wt, (size_t)(c->M + 1) * D));
-        CUDA_TRY(dalloc(&c->d_Wu, (size_t)(c->M + 1) * D));
-        CUDA_TRY(dalloc(&c->d_rhs, D));
-        CUDA_TRY(dalloc(&c->d_x, D));
-        CUDA_TRY(dalloc(&c->d_perm, D + 2 * kMaxPivotBlocks));
-        CUDA_TRY(dalloc(&c->d_status, 1));
-        c->partial_cap = (size_t)(c->M + 1) * D;
-        CUDA_TRY(dalloc(&c->d_partial, c->partial_cap));
-    }
-    cudaStream_t s = c->stream;
-    CUDA_TRY(cudaMemcpyAsync(c->d_ubc_map, umap.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_fbc_map, fmap.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_is_ubc, is_u.data(), D, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_is_fbc, is_f.data(), D, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_load_t, load_t.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    CUDA_TRY(cudaMemcpyAsync(c->d_load_u, load_u.data(), sizeof(double) * D,
-                             cudaMemcpyHostToDevice, s));
-    // the host vectors above are pageable: finish the copies before they go
-    CUDA_TRY(cudaStreamSynchronize(s));
-    return TDBEM_OK;
-}
-
-// FP64 inverse of the column-exchanged LHS v (0: step 2's, 1: steps >= 3) into
-// c->d_Ainv[v] (SolverStepLinearT.cpp:357-393, KSPSolve as an explicit inverse).
-int fp64_inverse(tdbem_ctx* c, int v, const double lhs_c[2][2]) {
-    const int D = c->D;
-    const size_t stride = (size_t)D * D;
-    cudaStream_t s = c->stream;
-    if (c->d_Ainv[1 - v] == c->d_Ainv[v]) c->d_Ainv[v] = nullptr;  // was an alias of the other
-    if (!c->d_Ainv[v]) CUDA_TRY(dalloc(&c->d_Ainv[v], stride));
-    CUDA_TRY(launch_build_lhs(c->d_G, c->d_H, c->d_Gf, c->d_Hf, stride, D, lhs_c[v][0],
-                              lhs_c[v][1], c->d_is_ubc, c->d_Ainv[v], s));
-    if (!c->d_inv_scratch) CUDA_TRY(dalloc(&c->d_inv_scratch, inverse_scratch_elems(D)));
-    const int pe = prof_begin(c, TDBEM_K_FACTOR);
-    bool singular = false;
-    cudaError_t e = invert_f64(c->d_Ainv[v], D, c->d_perm, c->d_status, c->d_inv_scratch,
-                               &c->launches, &singular, s);
-    prof_end(c, pe, 2.0 * 8 * stride, 2.0 * (double)D * D * D);
-    c->launches += 1;  // LHS build
-    CUDA_TRY(e);
-    if (singular)
-        return fail(TDBEM_ERR_SINGULAR, "zero pivot in the H^0 factorisation (LHS %d)", v);
-    return TDBEM_OK;
-}
-
-// One FP64 Solve_Averaging step: solve step st (history st) from histories < st.
-int fp64_step(tdbem_ctx* c, int st, const double lhs_c[2][2]) {
-    const int D = c->D;
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    const size_t stride = (size_t)D * D;
-    cudaStream_t s = c->stream;
-    MarchDev md{D, c->M, c->d_G, c->d_H, c->d_Gf, c->d_Hf};
-    const int L = std::min(std::max(st, 1), c->M);
-    const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
-    const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-    const double amp = c->amp.empty() ? 1.0 : c->amp[st];
-    CUDA_TRY(launch_history_combine(c->d_u, c->d_t, D, st, L, a1, a2, a3, c0, c1, amp,
-                                    c->d_load_t, c->d_load_u, c->d_Wt, c->d_Wu, s));
-    const int nch = conv_chunks(L, D);
-    const double esz = c->d_G ? 8.0 : 4.0;
-    int pe = prof_begin(c, TDBEM_K_CONV);
-    CUDA_TRY(launch_conv(md, L, c->d_Wt, c->d_Wu, c->d_partial, nch, s));
-    prof_end(c, pe, (L + 1) * 2.0 * (double)stride * esz + (L + 1) * 2.0 * D * 8,
-             (L + 1) * 4.0 * (double)stride);
-    pe = prof_begin(c, TDBEM_K_SOLVE);
-    CUDA_TRY(launch_reduce_solve(c->d_partial, nch, D, c->d_Ainv[st == 1 ? 0 : 1], c->d_rhs,
-                                 c->d_x, s));
-    CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                 c->d_fbc_map, amp, c->d_u, c->d_t, s));
-    prof_end(c, pe, 8.0 * (double)stride, 2.0 * (double)stride);
-    c->launches += 5;  // combine, conv, reduce, gemv, update
-    return TDBEM_OK;
-}
-
-// Plain FP64 marching: one level-streamed convolution and one FP64 inverse
-// product per step.
-int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hist,
-               double* t_hist) {
-    const int D = c->D;
-    cudaStream_t s = c->stream;
-    const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-    EventTimer tf;
-    tf.start(s);
-    const int ninv = (numstep >= 3 && !same) ? 2 : 1;
-    for (int v = 0; v < ninv; v++) {
-        const int rc = fp64_inverse(c, v, lhs_c);
-        if (rc != TDBEM_OK) return rc;
-    }
-    if (ninv == 1) {
-        if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
-        c->d_Ainv[1] = c->d_Ainv[0];
-    }
-    c->timings[1] = tf.stop_ms(s);
-
-    EventTimer tmr;
-    tmr.start(s);
-    const std::vector<const void*> ptrs = {
-        c->d_u,     c->d_t,   c->d_G,       c->d_H,      c->d_Gf,       c->d_Hf,
-        c->d_Ainv[0], c->d_Ainv[1], c->d_Wt, c->d_Wu,    c->d_partial,  c->d_rhs,
-        c->d_x,     c->d_load_t, c->d_load_u, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-        c->d_fbc_map};
-    const int lrc = run_march_loop(c, 0, numstep, ptrs, [&]() -> int {
-        for (int st = 1; st <= numstep - 1; st++) {
-            const int rc = fp64_step(c, st, lhs_c);
-            if (rc != TDBEM_OK) return rc;
-        }
-        return TDBEM_OK;
-    });
-    if (lrc != TDBEM_OK) return lrc;
-    c->timings[2] = tmr.stop_ms(s);
-    if (u_hist)
-        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
-                                 cudaMemcpyDeviceToHost, s));
-    if (t_hist)
-        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
-                                 cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    prof_flush(c);
-    return TDBEM_OK;
-}
-
-// FP64 level store of (M+1) levels, zeroed, for levels fed from host row blocks
-// or a checkpoint.
-int ensure_fp64_store(tdbem_ctx* c) {
-    if (c->level_precision == TDBEM_FP64 && c->d_G) return TDBEM_OK;
-    free_levels(c);
-    const size_t n = (size_t)(c->M + 1) * c->D * c->D;
-    CUDA_TRY(dalloc(&c->d_G, n));
-    CUDA_TRY(dalloc(&c->d_H, n));
-    CUDA_TRY(cudaMemsetAsync(c->d_G, 0, sizeof(double) * n, c->stream));
-    CUDA_TRY(cudaMemsetAsync(c->d_H, 0, sizeof(double) * n, c->stream));
-    c->level_precision = TDBEM_FP64;
-    c->levels_last = 0;
-    return TDBEM_OK;
-}
-
-}  // namespace
+}  // namespace capi
+}  // namespace tdbem
 
 void tdbem::note_error(const char* msg) { g_last_error = msg; }
 
@@ -1477,211 +810,6 @@ int tdbem_set_load_history(tdbem_ctx* c, const double* amp, int nsteps) {
     return TDBEM_OK;
 }
 
-int tdbem_march(tdbem_ctx* c, int numstep, double* u_hist, double* t_hist) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (numstep < 1) return fail(TDBEM_ERR_ARG, "numstep must be >= 1");
-    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
-    if (c->levels_last < std::min(c->M, numstep))
-        return fail(TDBEM_ERR_STATE, "levels assembled for %d steps, %d needed", c->levels_last,
-                    std::min(c->M, numstep));
-    if (!c->amp.empty() && (int)c->amp.size() < numstep)
-        return fail(TDBEM_ERR_ARG, "load history has %zu values, %d steps", c->amp.size(),
-                    numstep);
-    const int D = c->D;
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    const int rc0 = upload_bc(c);
-    if (rc0 != TDBEM_OK) return rc0;
-    cudaStream_t s = c->stream;
-    if (c->hist_steps != numstep) {
-        dfree(c->d_u);
-        dfree(c->d_t);
-        CUDA_TRY(dalloc(&c->d_u, (size_t)(numstep + 1) * D));
-        CUDA_TRY(dalloc(&c->d_t, (size_t)(numstep + 1) * D));
-        c->hist_steps = numstep;
-    }
-    CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (numstep + 1) * D, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (numstep + 1) * D, s));
-
-    // LHS of step 2 (SolverStepLinearT.cpp:357-371) and of steps >= 3 (381-393)
-    const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-    if (c->level_precision == TDBEM_MIXED) {
-        const int rc = march_mixed(c, numstep, lhs_c);
-        if (rc != TDBEM_OK) return rc;
-        if (u_hist)
-            CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_u, sizeof(double) * (numstep + 1) * D,
-                                     cudaMemcpyDeviceToHost, s));
-        if (t_hist)
-            CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_t, sizeof(double) * (numstep + 1) * D,
-                                     cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaStreamSynchronize(s));
-        prof_flush(c);
-        return TDBEM_OK;
-    }
-    return march_fp64(c, numstep, lhs_c, u_hist, t_hist);
-}
-
-int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* traction,
-                      const double* amp, double* u_hist, double* t_hist) {
-    if (!c || !traction) return fail(TDBEM_ERR_ARG, "null argument");
-    if (numstep < 1 || nrhs < 1) return fail(TDBEM_ERR_ARG, "numstep and nrhs must be >= 1");
-    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
-    if (c->level_precision != TDBEM_MIXED)
-        return fail(TDBEM_ERR_UNSUPPORTED,
-                    "batched marching runs on FP32 levels: assemble with TDBEM_MIXED");
-    if (c->levels_last < std::min(c->M, numstep))
-        return fail(TDBEM_ERR_STATE, "levels assembled for %d steps, %d needed", c->levels_last,
-                    std::min(c->M, numstep));
-    const int D = c->D, M = c->M, C = nrhs;
-    if ((size_t)C * D > (size_t)INT32_MAX / 2)
-        return fail(TDBEM_ERR_ARG, "nrhs x D = %zu is too large", (size_t)C * D);
-    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-    const int rc0 = upload_bc(c);
-    if (rc0 != TDBEM_OK) return rc0;
-    cudaStream_t s = c->stream;
-    const size_t CD = (size_t)C * D;
-    const int ldw = batch_ldw(D);
-    if (c->batch_C != C || c->batch_steps != numstep) {
-        free_batch(c);
-        CUDA_TRY(dalloc(&c->d_bu, (size_t)(numstep + 1) * CD));
-        CUDA_TRY(dalloc(&c->d_bt, (size_t)(numstep + 1) * CD));
-        CUDA_TRY(dalloc(&c->d_btrac, CD));
-        CUDA_TRY(dalloc(&c->d_bamp, (size_t)C * numstep));
-        CUDA_TRY(dalloc(&c->d_bWt, (size_t)(M + 1) * C * ldw));
-        CUDA_TRY(dalloc(&c->d_bWu, (size_t)(M + 1) * C * ldw));
-        int smax = batch_apply_splits(D, C);
-        for (int nlev = 2; nlev <= M + 1; nlev++)
-            smax = std::max({smax, batch_conv_splits(nlev, D, C),
-                             tc_conv_splits(nlev, D, C, 1 << 30, 1)});
-        c->bpart_cap = (size_t)smax * CD;
-        CUDA_TRY(dalloc(&c->d_bpart, c->bpart_cap));
-        CUDA_TRY(dalloc(&c->d_brhs, CD));
-        CUDA_TRY(dalloc(&c->d_bx, CD));
-        CUDA_TRY(dalloc(&c->d_br, CD));
-        c->batch_C = C;
-        c->batch_steps = numstep;
-    }
-    CUDA_TRY(cudaMemcpyAsync(c->d_btrac, traction, sizeof(double) * CD, cudaMemcpyHostToDevice, s));
-    if (amp)
-        CUDA_TRY(cudaMemcpyAsync(c->d_bamp, amp, sizeof(double) * C * numstep,
-                                 cudaMemcpyHostToDevice, s));
-    const double* d_amp = amp ? c->d_bamp : nullptr;
-    CUDA_TRY(cudaMemsetAsync(c->d_bu, 0, sizeof(double) * (numstep + 1) * CD, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_bt, 0, sizeof(double) * (numstep + 1) * CD, s));
-    c->launches += 0;
-
-    const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-    const int rc = mixed_inverses(c, numstep, lhs_c);
-    if (rc != TDBEM_OK) return rc;
-
-    // tcgen05 engine: the merged level planes of the single march (the cases share the
-    // boundary-condition types) and, per case, its known tractions times every level
-    const bool tc = c->batch_engine == TDBEM_ENGINE_TCGEN05;
-    const int Lw = M + 1;
-    if (tc) {
-        if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 1));
-        CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), s));
-        const int rm = ensure_merged_levels(c);
-        if (rm != TDBEM_OK) return rm;
-        const size_t wb = tc_w_bytes(D, C, Lw, 1);
-        if (c->tc_W_bytes < wb) {
-            if (c->d_tc_W) cudaFree(c->d_tc_W);
-            c->d_tc_W = nullptr;
-            c->tc_W_bytes = 0;
-            CUDA_TRY(cudaMalloc(&c->d_tc_W, wb));
-            c->tc_W_bytes = wb;
-        }
-        if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_tc_W, C, Lw, &c->tc_maps, 1))
-            return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched planes");
-        if (!c->d_bkt) {
-            CUDA_TRY(dalloc(&c->d_bkt, 2 * CD));
-            CUDA_TRY(dalloc(&c->d_bGK, (size_t)(M + 1) * CD));
-            CUDA_TRY(dalloc(&c->d_bGL, 2 * CD));
-        }
-        const int pk = prof_begin(c, TDBEM_K_AUX);
-        CUDA_TRY(launch_batch_known_tractions(c->d_btrac, c->d_is_ubc, D, C, c->d_bkt,
-                                              c->d_bkt + CD, s));
-        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, M + 1, c->d_bkt, C, c->d_bGK,
-                                      c->device, s));
-        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, std::min(2, M + 1), c->d_bkt + CD, C,
-                                      c->d_bGL, c->device, s));
-        prof_end(c, pk, (M + 3) * (double)D * c->ldf * 4, 2.0 * (M + 3) * (double)D * D * C);
-        c->launches += 3;
-    }
-
-    EventTimer tmr;
-    tmr.start(s);
-    const size_t lstride = (size_t)D * c->ldf;
-    const double DD = (double)D * D;
-    const int sp = batch_apply_splits(D, C);
-    for (int st = 1; st <= numstep - 1; st++) {
-        const int L = std::min(M, std::max(1, st));
-        const int nlev = L + 1;
-        const double c0 = st == 1 ? 1.0 : lhs_c[1][0];
-        const double c1 = st == 1 ? 0.0 : lhs_c[1][1];
-        int pe;
-        if (tc) {  // merged levels: the unknowns' history, then the known values' part
-            CUDA_TRY(launch_build_w_batch_merged(c->d_bu, c->d_bt, c->d_is_ubc, D, C, st, nlev,
-                                                 Lw, a1, a2, a3, c->d_tc_W, s));
-            const int splits = tc_conv_splits(nlev, D, C, 1 << 30, 1);
-            const double ldb = tc_ldb(D), cp = tc_cases_pad(C);
-            pe = prof_begin(c, TDBEM_K_CONV_BATCH);
-            CUDA_TRY(launch_conv_tc(c->tc_maps, D, M + 1, Lw, nlev, C, c->d_bpart, splits,
-                                    c->d_tc_err, s, 1));
-            prof_end(c, pe, nlev * (double)D * ldb * 4 + nlev * cp * ldb * 4,
-                     nlev * 2.0 * DD * C);
-            CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
-            const double* hu = c->d_mtc_known + (size_t)2 * (M + 1) * D;  // H^f ubc
-            CUDA_TRY(launch_known_batch(c->d_bGK, c->d_bGL, hu, D, C, M + 1, st, a1, a2, a3, c0,
-                                        c1, d_amp, numstep, c->d_brhs, s));
-            c->launches += 1;
-        } else {
-            CUDA_TRY(launch_build_w_batch(c->d_bu, c->d_bt, D, C, st, nlev, a1, a2, a3, c0, c1,
-                                          d_amp, numstep, c->d_btrac, c->d_is_ubc, c->d_ubc_map,
-                                          ldw, c->d_bWt, c->d_bWu, s));
-            const int splits = batch_conv_splits(nlev, D, C);
-            pe = prof_begin(c, TDBEM_K_CONV_BATCH);
-            CUDA_TRY(launch_conv_mma(c->d_Gf, c->d_Hf, lstride, c->ldf, D, nlev, c->d_bWt,
-                                     c->d_bWu, ldw, C, c->d_bpart, splits, s));
-            prof_end(c, pe, nlev * 2.0 * (double)lstride * 4 + nlev * 2.0 * C * ldw * 4,
-                     nlev * 4.0 * DD * C);
-            CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
-        }
-        pe = prof_begin(c, TDBEM_K_SOLVE_BATCH);
-        const int v = st == 1 ? 0 : 1;
-        CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_brhs, C, c->d_bpart, sp, s));
-        CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, nullptr, c->d_bx, s));
-        for (int it = 0; it < c->batch_refine; it++) {
-            CUDA_TRY(launch_apply_cols(c->d_Hc64[v], 1, D, c->d_bx, C, c->d_bpart, sp, s));
-            CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_brhs, c->d_br, s));
-            CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_br, C, c->d_bpart, sp, s));
-            CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_bx, c->d_bx, s));
-        }
-        CUDA_TRY(launch_update_batch(c->d_bx, D, C, st, c->d_is_ubc, c->d_ubc_map, c->d_btrac,
-                                     d_amp, numstep, c->d_bu, c->d_bt, s));
-        prof_end(c, pe, DD * 4 * (1 + c->batch_refine) + DD * 8 * c->batch_refine,
-                 2.0 * DD * C * (1 + 2 * c->batch_refine));
-        c->launches += 6 + 4LL * c->batch_refine;
-    }
-    c->timings[2] = tmr.stop_ms(s);
-    if (tc) {
-        int code = 0;
-        CUDA_TRY(cudaMemcpyAsync(&code, c->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaStreamSynchronize(s));
-        if (code)
-            return fail(TDBEM_ERR_CUDA,
-                        "tensor-core convolution: a pipeline wait timed out (code %d)", code);
-    }
-    if (u_hist)
-        CUDA_TRY(cudaMemcpyAsync(u_hist, c->d_bu, sizeof(double) * (numstep + 1) * CD,
-                                 cudaMemcpyDeviceToHost, s));
-    if (t_hist)
-        CUDA_TRY(cudaMemcpyAsync(t_hist, c->d_bt, sizeof(double) * (numstep + 1) * CD,
-                                 cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    prof_flush(c);
-    return TDBEM_OK;
-}
-
 int tdbem_update_gh_linear(tdbem_ctx* c, int step, int node_lo, int node_hi, const double* G_I,
                            const double* G_J, const double* H_I, const double* H_J) {
     if (!c || !G_I || !G_J || !H_I || !H_J) return fail(TDBEM_ERR_ARG, "null argument");
@@ -1721,696 +849,6 @@ int tdbem_update_gh_linear(tdbem_ctx* c, int step, int node_lo, int node_hi, con
     c->levels_last = std::max(c->levels_last, step);
     c->mtc_planes_valid = false;
     c->step_inv_ready[0] = c->step_inv_ready[1] = false;
-    return TDBEM_OK;
-}
-
-int tdbem_march_begin(tdbem_ctx* c, int numstep) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (numstep < 1) return fail(TDBEM_ERR_ARG, "numstep must be >= 1");
-    if (!c->amp.empty() && (int)c->amp.size() < numstep)
-        return fail(TDBEM_ERR_ARG, "load history has %zu values, %d steps", c->amp.size(),
-                    numstep);
-    const int rc = upload_bc(c);
-    if (rc != TDBEM_OK) return rc;
-    const int D = c->D;
-    cudaStream_t s = c->stream;
-    if (c->hist_steps != numstep) {
-        dfree(c->d_u);
-        dfree(c->d_t);
-        CUDA_TRY(dalloc(&c->d_u, (size_t)(numstep + 1) * D));
-        CUDA_TRY(dalloc(&c->d_t, (size_t)(numstep + 1) * D));
-        c->hist_steps = numstep;
-    }
-    CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (numstep + 1) * D, s));
-    CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (numstep + 1) * D, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    c->step_numstep = numstep;
-    c->step_inv_ready[0] = c->step_inv_ready[1] = false;
-    return TDBEM_OK;
-}
-
-int tdbem_march_step(tdbem_ctx* c, int curr_step, double* u, double* t) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (c->step_numstep < 1) return fail(TDBEM_ERR_STATE, "tdbem_march_begin has not run");
-    if (curr_step < 1 || curr_step > c->step_numstep)
-        return fail(TDBEM_ERR_ARG, "step %d outside 1..%d", curr_step, c->step_numstep);
-    const int D = c->D, st = curr_step - 1;
-    cudaStream_t s = c->stream;
-    if (st >= 1) {
-        if (c->level_precision != TDBEM_FP64)
-            return fail(TDBEM_ERR_UNSUPPORTED, "stepwise marching runs on FP64 levels");
-        if (c->levels_last < std::min(c->M, curr_step))
-            return fail(TDBEM_ERR_STATE, "levels hold %d steps, step %d needs %d", c->levels_last,
-                        curr_step, std::min(c->M, curr_step));
-        const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-        const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-        const int v = st == 1 ? 0 : 1;
-        if (!c->step_inv_ready[v]) {
-            const int rc = fp64_inverse(c, v, lhs_c);
-            if (rc != TDBEM_OK) return rc;
-            c->step_inv_ready[v] = true;
-        }
-        const int rc = fp64_step(c, st, lhs_c);
-        if (rc != TDBEM_OK) return rc;
-    }
-    if (u)
-        CUDA_TRY(cudaMemcpyAsync(u, c->d_u + (size_t)st * D, sizeof(double) * D,
-                                 cudaMemcpyDeviceToHost, s));
-    if (t)
-        CUDA_TRY(cudaMemcpyAsync(t, c->d_t + (size_t)st * D, sizeof(double) * D,
-                                 cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    prof_flush(c);
-    return TDBEM_OK;
-}
-
-// Level checkpoint: a 64-byte header (magic, version, D, M, precision, levels held,
-// row stride) followed by the raw level store (FP64: G then H, (M+1) x D x D;
-// mixed: FP32 G then H, (M+1) x D x ld, then FP64 levels 0-1 of G and H).
-namespace {
-constexpr char kCkptMagic[8] = {'T', 'D', 'B', 'E', 'M', 'L', 'V', 'L'};
-struct CkptHeader {
-    char magic[8];
-    int32_t version, D, M, precision, levels_last, ld;
-    int32_t pad[8];
-};
-static_assert(sizeof(CkptHeader) == 64, "checkpoint header is 64 bytes");
-
-struct LevelArrays {
-    void* dev[4];
-    size_t bytes[4];
-    int n;
-};
-
-LevelArrays level_arrays(tdbem_ctx* c) {
-    LevelArrays a{};
-    const size_t L = (size_t)c->M + 1, D = c->D;
-    if (c->level_precision == TDBEM_FP64) {
-        a.n = 2;
-        a.dev[0] = c->d_G;
-        a.dev[1] = c->d_H;
-        a.bytes[0] = a.bytes[1] = L * D * D * 8;
-    } else {
-        a.n = 4;
-        a.dev[0] = c->d_Gf;
-        a.dev[1] = c->d_Hf;
-        a.bytes[0] = a.bytes[1] = L * D * c->ldf * 4;
-        a.dev[2] = c->d_G01;
-        a.dev[3] = c->d_H01;
-        a.bytes[2] = a.bytes[3] = 2 * D * D * 8;
-    }
-    return a;
-}
-}  // namespace
-
-int tdbem_export_levels(tdbem_ctx* c, const char* path) {
-    if (!c || !path) return fail(TDBEM_ERR_ARG, "null argument");
-    if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "levels not assembled");
-    FILE* f = std::fopen(path, "wb");
-    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s for writing", path);
-    CkptHeader h{};
-    std::memcpy(h.magic, kCkptMagic, 8);
-    h.version = 1;
-    h.D = c->D;
-    h.M = c->M;
-    h.precision = c->level_precision;
-    h.levels_last = c->levels_last;
-    h.ld = c->level_precision == TDBEM_FP64 ? c->D : c->ldf;
-    bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1;
-    const LevelArrays a = level_arrays(c);
-    std::vector<unsigned char> buf;
-    const size_t chunk = (size_t)64 << 20;
-    for (int k = 0; k < a.n && ok; k++)
-        for (size_t o = 0; o < a.bytes[k] && ok; o += chunk) {
-            const size_t b = std::min(chunk, a.bytes[k] - o);
-            buf.resize(b);
-            if (cudaMemcpy(buf.data(), static_cast<unsigned char*>(a.dev[k]) + o, b,
-                           cudaMemcpyDeviceToHost) != cudaSuccess) {
-                std::fclose(f);
-                return fail(TDBEM_ERR_CUDA, "level copy to host failed");
-            }
-            ok = std::fwrite(buf.data(), 1, b, f) == b;
-        }
-    ok = (std::fclose(f) == 0) && ok;
-    if (!ok) return fail(TDBEM_ERR_ARG, "write to %s failed", path);
-    return TDBEM_OK;
-}
-
-int tdbem_import_levels(tdbem_ctx* c, const char* path) {
-    if (!c || !path) return fail(TDBEM_ERR_ARG, "null argument");
-    c->inv_valid = false;
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s", path);
-    CkptHeader h{};
-    if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 ||
-        h.version != 1) {
-        std::fclose(f);
-        return fail(TDBEM_ERR_ARG, "%s is not a level checkpoint", path);
-    }
-    if (h.D != c->D || h.M != c->M) {
-        std::fclose(f);
-        return fail(TDBEM_ERR_ARG, "checkpoint is for D=%d, M=%d; this mesh has D=%d, M=%d", h.D,
-                    h.M, c->D, c->M);
-    }
-    int rc = TDBEM_OK;
-    if (h.precision == TDBEM_FP64) {
-        rc = ensure_fp64_store(c);
-    } else if (h.precision == TDBEM_MIXED && h.ld == mixed_ld(c->D)) {
-        if (c->level_precision != TDBEM_MIXED || !c->d_Gf) {
-            free_levels(c);
-            const size_t n = (size_t)(c->M + 1) * c->D * mixed_ld(c->D);
-            cudaError_t e = dalloc(&c->d_Gf, n);
-            if (e == cudaSuccess) e = dalloc(&c->d_Hf, n);
-            if (e == cudaSuccess) e = dalloc(&c->d_G01, 2 * (size_t)c->D * c->D);
-            if (e == cudaSuccess) e = dalloc(&c->d_H01, 2 * (size_t)c->D * c->D);
-            if (e != cudaSuccess) rc = fail(TDBEM_ERR_NOMEM, "level allocation failed");
-            c->ldf = mixed_ld(c->D);
-            c->level_precision = TDBEM_MIXED;
-        }
-    } else {
-        rc = fail(TDBEM_ERR_ARG, "checkpoint precision %d / row stride %d not supported",
-                  h.precision, h.ld);
-    }
-    if (rc != TDBEM_OK) {
-        std::fclose(f);
-        return rc;
-    }
-    const LevelArrays a = level_arrays(c);
-    std::vector<unsigned char> buf;
-    const size_t chunk = (size_t)64 << 20;
-    bool ok = true;
-    for (int k = 0; k < a.n && ok; k++)
-        for (size_t o = 0; o < a.bytes[k] && ok; o += chunk) {
-            const size_t b = std::min(chunk, a.bytes[k] - o);
-            buf.resize(b);
-            ok = std::fread(buf.data(), 1, b, f) == b &&
-                 cudaMemcpy(static_cast<unsigned char*>(a.dev[k]) + o, buf.data(), b,
-                            cudaMemcpyHostToDevice) == cudaSuccess;
-        }
-    std::fclose(f);
-    if (!ok) {
-        free_levels(c);
-        return fail(TDBEM_ERR_ARG, "%s is truncated or the copy failed", path);
-    }
-    c->levels_last = h.levels_last;
-    c->mtc_planes_valid = false;
-    c->step_inv_ready[0] = c->step_inv_ready[1] = false;
-    return TDBEM_OK;
-}
-
-int tdbem_write_gh(const char* name_prefix, int step, int num_row, int num_column,
-                   const double* data) {
-    if (!name_prefix || !data || num_row < 0 || num_column < 0)
-        return fail(TDBEM_ERR_ARG, "invalid arguments");
-    char path[4096];
-    std::snprintf(path, sizeof(path), "%s%d.txt", name_prefix, step);
-    FILE* f = std::fopen(path, "w");
-    if (!f) return fail(TDBEM_ERR_ARG, "cannot open %s", path);
-    bool ok = true;
-    for (int i = 0; i < num_row && ok; i++) {
-        for (int j = 0; j < num_column && ok; j++)
-            ok = std::fprintf(f, "%15.5e", data[(size_t)i * num_column + j]) > 0;
-        ok = ok && std::fputc('\n', f) != EOF;
-    }
-    ok = (std::fclose(f) == 0) && ok;
-    return ok ? TDBEM_OK : fail(TDBEM_ERR_ARG, "write to %s failed", path);
-}
-
-}  // extern "C"
-
-namespace {
-// Runs fn(i) for i < n on n host threads (each sets the context's device) and
-// returns the first failure with its message.
-template <typename F>
-int parallel_contexts(tdbem_ctx* const* ctxs, int n, F fn) {
-    std::vector<int> rc(n, TDBEM_OK);
-    std::vector<std::string> msg(n);
-    std::vector<std::thread> th;
-    th.reserve(n);
-    for (int i = 0; i < n; i++)
-        th.emplace_back([&, i] {
-            cudaSetDevice(ctxs[i]->device);
-            rc[i] = fn(i);
-            if (rc[i] != TDBEM_OK) msg[i] = tdbem_last_error();
-        });
-    for (auto& t : th) t.join();
-    for (int i = 0; i < n; i++)
-        if (rc[i] != TDBEM_OK) return fail(rc[i], "mesh %d: %s", i, msg[i].c_str());
-    return TDBEM_OK;
-}
-}  // namespace
-
-extern "C" {
-
-int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int precision) {
-    if (!ctxs || !nsteps || n < 1) return fail(TDBEM_ERR_ARG, "invalid group");
-    if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
-        return fail(TDBEM_ERR_ARG, "unknown precision %d", precision);
-    for (int i = 0; i < n; i++) {
-        if (!ctxs[i]) return fail(TDBEM_ERR_ARG, "null context %d", i);
-        if (ctxs[i]->device != ctxs[0]->device)
-            return fail(TDBEM_ERR_ARG, "the group's contexts are on different devices");
-        if (nsteps[i] < 1) return fail(TDBEM_ERR_ARG, "nsteps[%d] must be >= 1", i);
-        for (int j = 0; j < i; j++)
-            if (ctxs[j] == ctxs[i]) return fail(TDBEM_ERR_ARG, "context %d appears twice", i);
-    }
-    bool any_q8 = false;
-    for (int i = 0; i < n; i++) any_q8 = any_q8 || ctxs[i]->ennd == 8;
-    // mixed: near/far split per mesh; 8-node meshes: the single-mesh launches (the
-    // grouped kernels are written for 4-node elements).  The meshes' streams overlap.
-    if (precision == TDBEM_MIXED || any_q8)
-        return parallel_contexts(ctxs, n, [&](int i) {
-            return tdbem_assemble_levels(ctxs[i], nsteps[i], precision);
-        });
-    tdbem_ctx* c0 = ctxs[0];
-    cudaStream_t s = c0->stream;
-    EventTimer tm;
-    int ncol = 0;
-    for (int i = 0; i < n; i++) {
-        tdbem_ctx* c = ctxs[i];
-        CUDA_TRY(cudaStreamSynchronize(c->stream));
-        if (c->level_precision != TDBEM_FP64 || !c->d_G) {
-            free_levels(c);
-            const size_t nn = (size_t)(c->M + 1) * c->D * c->D;
-            CUDA_TRY(dalloc(&c->d_G, nn));
-            CUDA_TRY(dalloc(&c->d_H, nn));
-            c->level_precision = TDBEM_FP64;
-        }
-        const size_t total = (size_t)(c->M + 1) * c->D * c->D;
-        CUDA_TRY(cudaMemsetAsync(c->d_G, 0, 8 * total, s));
-        CUDA_TRY(cudaMemsetAsync(c->d_H, 0, 8 * total, s));
-        ncol = std::max(ncol, (int)c->color_start.size() - 1);
-    }
-    tm.start(s);
-    // descriptors of every mesh; per colour only the meshes that have it
-    std::vector<GroupAsm> all(n);
-    unsigned node_total = 0;
-    size_t pair_max = 0;
-    for (int i = 0; i < n; i++) {
-        tdbem_ctx* c = ctxs[i];
-        GroupAsm& g = all[i];
-        g = GroupAsm{};
-        g.coords = c->d_coords;
-        g.ien = c->d_ien;
-        g.nnd = c->nnd;
-        g.nel = c->nel;
-        g.nq = c->nq;
-        g.gx = c->d_gx;
-        g.gw = c->d_gw;
-        g.geom = c->d_geom;
-        g.ph = c->ph;
-        g.level_last = std::min(c->M, nsteps[i]);
-        g.level_cap = c->M;
-        g.if_ext = c->if_ext;
-        g.out.G0 = c->d_G;
-        g.out.H0 = c->d_H;
-        g.out.level_stride = (size_t)c->D * c->D;
-        g.out.D = c->D;
-        g.out.ld = c->D;
-        g.node_begin = node_total;
-        g.cbuf = c->d_cterm;
-        node_total += (unsigned)c->nnd;
-    }
-    for (int col = 0; col < ncol; col++) {
-        size_t np = 0;
-        for (int i = 0; i < n; i++) {
-            const tdbem_ctx* c = ctxs[i];
-            if (col + 1 < (int)c->color_start.size())
-                np += (size_t)c->nnd * (c->color_start[col + 1] - c->color_start[col]);
-        }
-        pair_max = std::max(pair_max, np);
-    }
-    if (pair_max >= ((size_t)1 << 31)) return fail(TDBEM_ERR_UNSUPPORTED, "group too large");
-    PairInfo* d_pairs = nullptr;
-    unsigned *d_counts = nullptr, *d_offsets = nullptr;
-    GroupAsm* d_gm = nullptr;
-    void* d_tmp = nullptr;
-    const size_t tmp_bytes = std::max<size_t>(scan_temp_bytes((unsigned)std::max<size_t>(pair_max, 1)), 16);
-    struct Free {
-        PairInfo*& a;
-        unsigned*& b;
-        unsigned*& c;
-        GroupAsm*& d;
-        void*& e;
-        ~Free() {
-            dfree(a);
-            dfree(b);
-            dfree(c);
-            dfree(d);
-            if (e) cudaFree(e);
-        }
-    } guard{d_pairs, d_counts, d_offsets, d_gm, d_tmp};
-    CUDA_TRY(dalloc(&d_pairs, std::max<size_t>(pair_max, 1)));
-    CUDA_TRY(dalloc(&d_counts, std::max<size_t>(pair_max, 1)));
-    CUDA_TRY(dalloc(&d_offsets, std::max<size_t>(pair_max, 1)));
-    CUDA_TRY(dalloc(&d_gm, (size_t)n));
-    CUDA_TRY(cudaMalloc(&d_tmp, tmp_bytes));
-    long long launches = 0;
-    for (int col = 0; col < ncol; col++) {
-        std::vector<GroupAsm> gl;
-        unsigned np = 0;
-        for (int i = 0; i < n; i++) {
-            const tdbem_ctx* c = ctxs[i];
-            if (col + 1 >= (int)c->color_start.size()) continue;
-            const int e0 = c->color_start[col], ne = c->color_start[col + 1] - e0;
-            if (ne == 0) continue;
-            GroupAsm g = all[i];
-            g.elems = c->d_color_elems + e0;
-            g.ne = ne;
-            g.pair_begin = np;
-            np += (unsigned)(c->nnd * ne);
-            gl.push_back(g);
-        }
-        if (gl.empty()) continue;
-        CUDA_TRY(cudaMemcpyAsync(d_gm, gl.data(), sizeof(GroupAsm) * gl.size(),
-                                 cudaMemcpyHostToDevice, s));
-        CUDA_TRY(launch_pair_window_group(d_gm, (int)gl.size(), np, d_pairs, d_counts, s));
-        CUDA_TRY(exclusive_scan(d_counts, d_offsets, np, d_tmp, tmp_bytes, s));
-        unsigned last[2];
-        CUDA_TRY(cudaMemcpyAsync(&last[0], d_offsets + np - 1, sizeof(unsigned),
-                                 cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaMemcpyAsync(&last[1], d_counts + np - 1, sizeof(unsigned),
-                                 cudaMemcpyDeviceToHost, s));
-        CUDA_TRY(cudaStreamSynchronize(s));  // also keeps d_gm alive until its launches ran
-        const unsigned nitems = last[0] + last[1];
-        CUDA_TRY(launch_assemble_group(d_gm, (int)gl.size(), d_pairs, d_offsets, np, nitems, s));
-        CUDA_TRY(cudaStreamSynchronize(s));  // d_gm is rewritten for the next colour
-        launches += 4;
-    }
-    CUDA_TRY(cudaMemcpyAsync(d_gm, all.data(), sizeof(GroupAsm) * n, cudaMemcpyHostToDevice, s));
-    CUDA_TRY(launch_cterm_group(d_gm, n, node_total, s));
-    launches += 1;
-    const double ms = tm.stop_ms(s);
-    for (int i = 0; i < n; i++) {
-        tdbem_ctx* c = ctxs[i];
-        c->levels_last = std::min(c->M, nsteps[i]);
-        c->mtc_planes_valid = false;
-        c->step_inv_ready[0] = c->step_inv_ready[1] = false;
-        c->timings[0] = ms;
-    }
-    c0->launches += launches;
-    return TDBEM_OK;
-}
-
-namespace {
-struct ShapeKey {
-    int nmesh;
-    unsigned nrows, nw;
-    bool operator==(const ShapeKey& o) const {
-        return nmesh == o.nmesh && nrows == o.nrows && nw == o.nw;
-    }
-};
-std::mutex g_shape_mu;
-std::vector<std::pair<ShapeKey, GroupShape>> g_shapes;  // autotuned launch shapes
-}  // namespace
-
-int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double* const* u_hist,
-                      double* const* t_hist) {
-    if (!ctxs || !numsteps || n < 1) return fail(TDBEM_ERR_ARG, "invalid group");
-    int max_steps = 0;
-    for (int i = 0; i < n; i++) {
-        tdbem_ctx* c = ctxs[i];
-        if (!c) return fail(TDBEM_ERR_ARG, "null context %d", i);
-        if (c->device != ctxs[0]->device)
-            return fail(TDBEM_ERR_ARG, "the group's contexts are on different devices");
-        for (int j = 0; j < i; j++)
-            if (ctxs[j] == c) return fail(TDBEM_ERR_ARG, "context %d appears twice", i);
-        if (numsteps[i] < 1) return fail(TDBEM_ERR_ARG, "numsteps[%d] must be >= 1", i);
-        if (c->level_precision < 0) return fail(TDBEM_ERR_STATE, "mesh %d: levels not assembled", i);
-        if (c->level_precision != ctxs[0]->level_precision)
-            return fail(TDBEM_ERR_UNSUPPORTED,
-                        "a group marches FP64 levels or TDBEM_MIXED levels, not both (mesh %d)", i);
-        if (c->levels_last < std::min(c->M, numsteps[i]))
-            return fail(TDBEM_ERR_STATE, "mesh %d: levels hold %d steps, %d needed", i,
-                        c->levels_last, std::min(c->M, numsteps[i]));
-        if (!c->amp.empty() && (int)c->amp.size() < numsteps[i])
-            return fail(TDBEM_ERR_ARG, "mesh %d: load history shorter than its steps", i);
-        max_steps = std::max(max_steps, numsteps[i]);
-    }
-    const bool mixed = ctxs[0]->level_precision == TDBEM_MIXED;
-    cudaStream_t s = ctxs[0]->stream;
-    std::vector<GroupMarch> gm(n);
-    std::vector<double*> d_amp(n, nullptr);
-    struct FreeAmp {
-        std::vector<double*>& v;
-        ~FreeAmp() {
-            for (auto& p : v) dfree(p);
-        }
-    } amp_guard{d_amp};
-    unsigned nrows = 0, nw = 0;
-    EventTimer tf;
-    tf.start(s);
-    // per mesh: boundary conditions, histories, inverses, load history -- on the
-    // mesh's own stream from its own host thread, so the meshes overlap
-    int rc = parallel_contexts(ctxs, n, [&](int i) -> int {
-        tdbem_ctx* c = ctxs[i];
-        const int D = c->D, ns = numsteps[i];
-        int r = upload_bc(c);
-        if (r != TDBEM_OK) return r;
-        if (c->hist_steps != ns) {
-            dfree(c->d_u);
-            dfree(c->d_t);
-            CUDA_TRY(dalloc(&c->d_u, (size_t)(ns + 1) * D));
-            CUDA_TRY(dalloc(&c->d_t, (size_t)(ns + 1) * D));
-            c->hist_steps = ns;
-        }
-        CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (ns + 1) * D, c->stream));
-        CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (ns + 1) * D, c->stream));
-        const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-        const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-        if (mixed) {
-            if (!c->d_res) CUDA_TRY(dalloc(&c->d_res, D));
-            r = mixed_inverses(c, ns, lhs_c);
-            if (r != TDBEM_OK) return r;
-        } else {
-            const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-            const int ninv = (ns >= 3 && !same) ? 2 : 1;
-            for (int v = 0; v < ninv; v++) {
-                r = fp64_inverse(c, v, lhs_c);
-                if (r != TDBEM_OK) return r;
-            }
-            if (ninv == 1) {
-                if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
-                c->d_Ainv[1] = c->d_Ainv[0];
-            }
-        }
-        if (!c->amp.empty()) {
-            CUDA_TRY(dalloc(&d_amp[i], (size_t)ns));
-            CUDA_TRY(cudaMemcpyAsync(d_amp[i], c->amp.data(), sizeof(double) * ns,
-                                     cudaMemcpyHostToDevice, c->stream));
-        }
-        CUDA_TRY(cudaStreamSynchronize(c->stream));
-        GroupMarch& g = gm[i];
-        g = GroupMarch{};
-        g.D = D;
-        g.M = c->M;
-        g.numstep = ns;
-        g.G = c->d_G;
-        g.H = c->d_H;
-        g.Ainv0 = c->d_Ainv[0];
-        g.Ainv1 = c->d_Ainv[1];
-        g.u = c->d_u;
-        g.t = c->d_t;
-        g.is_u = c->d_is_ubc;
-        g.is_f = c->d_is_fbc;
-        g.ubc = c->d_ubc_map;
-        g.fbc = c->d_fbc_map;
-        g.load_t = c->d_load_t;
-        g.load_u = c->d_load_u;
-        g.amp = d_amp[i];
-        g.a1 = a1;
-        g.a2 = a2;
-        g.a3 = a3;
-        g.c0 = lhs_c[1][0];
-        g.c1 = lhs_c[1][1];
-        g.Wt = c->d_Wt;
-        g.Wu = c->d_Wu;
-        g.rhs = c->d_rhs;
-        g.Gf = c->d_Gf;
-        g.Hf = c->d_Hf;
-        g.ldf = c->ldf;
-        g.inv32_0 = c->d_inv32[0];
-        g.inv32_1 = c->d_inv32[1];
-        g.Hc0 = c->d_Hc64[0];
-        g.Hc1 = c->d_Hc64[1];
-        g.x = c->d_x;
-        g.r = c->d_res;
-        g.refine = c->n_refine > 0 ? 1 : 0;
-        return TDBEM_OK;
-    });
-    if (rc != TDBEM_OK) return rc;
-    unsigned nquads = 0, nwold = 0;
-    size_t nwf = 0, nwoldf = 0, nyold = 0;  // FP32 scratch (row stride ldf) and Y_old sizes
-    for (int i = 0; i < n; i++) {
-        const tdbem_ctx* c = ctxs[i];
-        gm[i].row_begin = nrows;
-        gm[i].w_begin = nw;
-        gm[i].quad_begin = nquads;
-        gm[i].wold_begin = nwold;
-        nrows += (unsigned)c->D;
-        nw += (unsigned)((c->M + 1) * c->D);
-        nquads += (unsigned)((c->D + 3) / 4);
-        nwold += (unsigned)((c->M + 1) * kGroupNB * c->D);
-        nwf += (size_t)(c->M + 1) * c->ldf;
-        nwoldf += (size_t)(c->M + 1) * kGroupNB * c->ldf;
-        nyold += (size_t)kGroupNB * c->D;
-    }
-    float* d_wf = nullptr;    // FP32 history vectors of every mesh (mixed)
-    double* d_yold = nullptr;
-    struct FreeWf {
-        float*& p;
-        double*& q;
-        ~FreeWf() {
-            dfree(p);
-            dfree(q);
-        }
-    } wf_guard{d_wf, d_yold};
-    if (mixed) {
-        // new-W (2 x nwf) and old-W (2 x nwoldf) planes, zeroed: the padding columns
-        // ldf > D are read by the 16-byte loads and must stay zero
-        const size_t tot = 2 * nwf + 2 * nwoldf;
-        CUDA_TRY(dalloc(&d_wf, tot));
-        CUDA_TRY(cudaMemsetAsync(d_wf, 0, sizeof(float) * tot, s));
-        CUDA_TRY(dalloc(&d_yold, nyold));
-        size_t ow = 0, oo = 0, oy = 0;
-        for (int i = 0; i < n; i++) {
-            const tdbem_ctx* c = ctxs[i];
-            gm[i].Wtf = d_wf + ow;
-            gm[i].Wuf = d_wf + nwf + ow;
-            gm[i].Wold_t = d_wf + 2 * nwf + oo;
-            gm[i].Wold_u = d_wf + 2 * nwf + nwoldf + oo;
-            gm[i].Yold = d_yold + oy;
-            ow += (size_t)(c->M + 1) * c->ldf;
-            oo += (size_t)(c->M + 1) * kGroupNB * c->ldf;
-            oy += (size_t)kGroupNB * c->D;
-        }
-    }
-    const double factor_ms = tf.stop_ms(s);
-    GroupMarch* d_gm = nullptr;
-    CUDA_TRY(dalloc(&d_gm, (size_t)n));
-    struct FreeGm {
-        GroupMarch*& p;
-        ~FreeGm() { dfree(p); }
-    } gm_guard{d_gm};
-    CUDA_TRY(cudaMemcpyAsync(d_gm, gm.data(), sizeof(GroupMarch) * n, cudaMemcpyHostToDevice, s));
-
-    // launch shape: the fastest of the candidates on the first steps, remembered per
-    // group size (the march is deterministic: every step is recomputed by the full run)
-    const ShapeKey key{n * (mixed ? -1 : 1), nrows, nw};
-    GroupShape shape{0, 0, 0};
-    {
-        std::lock_guard<std::mutex> lock(g_shape_mu);
-        for (auto& kv : g_shapes)
-            if (kv.first == key) shape = kv.second;
-    }
-    if (shape.lanes == 0) {
-        // the probe covers one old-history pass of the time-blocked form
-        const int probe_hi = std::min(max_steps, mixed ? 2 * kGroupNB + 1 : 8);
-        float best = 1e30f;
-        GroupShape best_shape{32, 256, 1};
-        for (int lanes : {8, 16, 32})
-            for (int block : {128, 256, 512})
-                for (int bps : {1, 2, 4}) {
-                    if (block * bps > 2048) continue;
-                    const GroupShape cand{lanes, block, bps};
-                    if (probe_hi <= 1) break;
-                    EventTimer t;
-                    t.start(s);
-                    const cudaError_t e = launch_march_group(d_gm, n, nrows, nw, nquads, nwold, 1,
-                                                             probe_hi, cand, mixed, s);
-                    if (e == cudaErrorInvalidConfiguration || e == cudaErrorCooperativeLaunchTooLarge) {
-                        cudaGetLastError();
-                        t.stop_ms(s);
-                        continue;
-                    }
-                    CUDA_TRY(e);
-                    const float ms = (float)t.stop_ms(s);
-                    if (ms < best) {
-                        best = ms;
-                        best_shape = cand;
-                    }
-                }
-        shape = best_shape;
-        std::lock_guard<std::mutex> lock(g_shape_mu);
-        g_shapes.push_back({key, shape});
-    }
-    EventTimer tmr;
-    tmr.start(s);
-    CUDA_TRY(launch_march_group(d_gm, n, nrows, nw, nquads, nwold, 1, max_steps, shape, mixed, s));
-    ctxs[0]->launches += 1;
-    const double march_ms = tmr.stop_ms(s);
-    for (int i = 0; i < n; i++) {
-        tdbem_ctx* c = ctxs[i];
-        const size_t bytes = sizeof(double) * (numsteps[i] + 1) * c->D;
-        if (u_hist && u_hist[i])
-            CUDA_TRY(cudaMemcpyAsync(u_hist[i], c->d_u, bytes, cudaMemcpyDeviceToHost, s));
-        if (t_hist && t_hist[i])
-            CUDA_TRY(cudaMemcpyAsync(t_hist[i], c->d_t, bytes, cudaMemcpyDeviceToHost, s));
-        c->timings[1] = factor_ms;
-        c->timings[2] = march_ms;
-    }
-    CUDA_TRY(cudaStreamSynchronize(s));
-    return TDBEM_OK;
-}
-
-int tdbem_group_shape(int* lanes, int* block, int* blocks_per_sm) {
-    std::lock_guard<std::mutex> lock(g_shape_mu);
-    if (g_shapes.empty()) return fail(TDBEM_ERR_STATE, "no grouped march has run");
-    const GroupShape& sh = g_shapes.back().second;
-    if (lanes) *lanes = sh.lanes;
-    if (block) *block = sh.block;
-    if (blocks_per_sm) *blocks_per_sm = sh.blocks_per_sm;
-    return TDBEM_OK;
-}
-
-int tdbem_set_graphs(tdbem_ctx* c, int on) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    c->use_graphs = on != 0;
-    if (!c->use_graphs && c->graph.exec) {
-        cudaStreamSynchronize(c->stream);
-        cudaGraphExecDestroy(c->graph.exec);
-        c->graph.exec = nullptr;
-    }
-    return TDBEM_OK;
-}
-
-int tdbem_set_batch_options(tdbem_ctx* c, int engine, int refine_sweeps) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (engine != TDBEM_ENGINE_TCGEN05 && engine != TDBEM_ENGINE_MMA_SYNC)
-        return fail(TDBEM_ERR_ARG, "unknown batch engine %d", engine);
-    if (refine_sweeps < 0 || refine_sweeps > 4)
-        return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
-    c->batch_engine = engine;
-    c->batch_refine = refine_sweeps;
-    return TDBEM_OK;
-}
-
-int tdbem_set_march_engine(tdbem_ctx* c, int engine) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (engine != TDBEM_ENGINE_TCGEN05 && engine != TDBEM_ENGINE_FP32)
-        return fail(TDBEM_ERR_ARG, "engine must be TDBEM_ENGINE_TCGEN05 or TDBEM_ENGINE_FP32");
-    c->march_engine = engine;
-    return TDBEM_OK;
-}
-
-int tdbem_set_march_options(tdbem_ctx* c, int block_steps, int refine_sweeps) {
-    if (!c) return fail(TDBEM_ERR_ARG, "null context");
-    if (block_steps != 0 && block_steps != 1 && block_steps != 4 && block_steps != 6 &&
-        block_steps != 8 && block_steps != 12 && block_steps != 16 && block_steps != 24 &&
-        block_steps != 32)
-        return fail(TDBEM_ERR_ARG, "block_steps must be 0 (auto), 1, 4, 6, 8, 12, 16, 24 or 32");
-    if (refine_sweeps < 0 || refine_sweeps > 4)
-        return fail(TDBEM_ERR_ARG, "refine_sweeps must be in 0..4");
-    c->nb = block_steps;  // the march resizes its scratch when the block changes
-    c->n_refine = refine_sweeps;
-    return TDBEM_OK;
-}
-
-int tdbem_history_device(const tdbem_ctx* c, const double** u_hist, const double** t_hist) {
-    if (!c || !u_hist || !t_hist) return fail(TDBEM_ERR_ARG, "null argument");
-    if (c->hist_steps < 0) return fail(TDBEM_ERR_STATE, "no march has run");
-    *u_hist = c->d_u;
-    *t_hist = c->d_t;
     return TDBEM_OK;
 }
 

@@ -24,9 +24,12 @@
 //   warps 2..5  epilogue: tcgen05.ld of a finished level's accumulator (double
 //               buffered in TMEM, columns 0-63 / 64-127), compensated (Kahan)
 //               FP32 sum over the levels, FP64 partial sums at the end.
-// Every mbarrier wait is bounded (%globaltimer); a wait that runs out sets an
-// error code, makes every role stop, and the CTA still drains its MMAs before
-// it frees TMEM.
+// Every mbarrier wait is bounded (%globaltimer); a wait of the pipeline that runs
+// out of its limit (a kernel argument, 2 s by default) sets an error code and
+// makes every role stop; the CTA then still waits (2 s at most per wait) for its
+// copies in flight and its MMAs before it frees TMEM.  err[1] counts the CTAs
+// holding TMEM: +1 after the allocation, -1 after the release, so it returns to 0
+// once every CTA has freed its columns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -49,7 +52,7 @@ constexpr int TC_THREADS = 192;
 constexpr int TC_TMEM_COLS = 128;
 constexpr int TC_NBAR = 2 * TC_STAGES + 5;  // full, empty, tmem full x2, tmem empty x2, done
 constexpr int TC_SMEM = 1024 + TC_STAGES * TC_STAGE_BYTES + TC_NBAR * 8 + 16;
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kDrainWaitNs = 2000000000ull;  // 2 s per drain wait
 
 // Instruction descriptor, kind::f16: D FP32 (bits 4-5 = 1), A and B BF16
 // (bits 7-9 = 1, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
@@ -92,16 +95,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase of `parity`: false when it runs out (error code
-// recorded, every role told to stop) or when another role has stopped.
+// Bounded wait for the phase of `parity`: false when it runs out of limit_ns
+// (error code recorded, every role told to stop) or when another role has stopped
+// (honour_abort).
 __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, int* err,
-                          int code, bool honour_abort = true) {
+                          int code, unsigned long long limit_ns, bool honour_abort = true) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = gtimer();
     while (true) {
         if (honour_abort && *abort_flag) return false;
         if (mbar_try(bar, parity)) return true;
-        if (gtimer() - t0 > kWaitNs) {
+        if (gtimer() - t0 > limit_ns) {
             *abort_flag = 1;
             atomicExch(err, code);
             return false;
@@ -166,7 +170,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               int D, int L, int Lw, int nlev, int nk, int nmat, int C,
-              double* __restrict__ partial, int* __restrict__ err) {
+              double* __restrict__ partial, int* __restrict__ err, unsigned long long wait_ns) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
@@ -212,6 +216,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
+    if (threadIdx.x == 0) atomicAdd(err + 1, 1);  // this CTA holds TMEM
 
     if (warp == 0) {
         if (lane == 0) {  // ---------------- TMA producer
@@ -220,7 +225,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const int f = i / per_lev, r = i - f * per_lev;
                 const int mat = r / nk, kc = r - mat * nk;
                 const int s = it % TC_STAGES, n = it / TC_STAGES;
-                if (n >= 1 && !mbar_wait(bar(EMPTY + s), (n - 1) & 1, abort_flag, err, 1)) break;
+                if (n >= 1 && !mbar_wait(bar(EMPTY + s), (n - 1) & 1, abort_flag, err, 1, wait_ns))
+                    break;
                 const uint32_t st = sbase + s * TC_STAGE_BYTES;
                 mbar_expect_tx(bar(FULL + s), TC_STAGE_BYTES);
                 const int x = kc * TC_BK;
@@ -234,7 +240,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             // every issued copy has landed before the CTA can exit
             for (int k = std::max(0, it - TC_STAGES); k < it; k++)
                 mbar_wait(bar(FULL + k % TC_STAGES), (k / TC_STAGES) & 1, abort_flag, err, 5,
-                          false);
+                          kDrainWaitNs, false);
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---------------- MMA issuer
@@ -242,7 +248,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             bool ok = true;
             for (int j = 0; j < nseg && ok; j++) {
                 const int b = j & 1, u = j >> 1;
-                if (u >= 1 && !mbar_wait(bar(TEMPTY + b), (u - 1) & 1, abort_flag, err, 2)) break;
+                if (u >= 1 && !mbar_wait(bar(TEMPTY + b), (u - 1) & 1, abort_flag, err, 2, wait_ns))
+                    break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(b * TC_BN);
                 const int f = f0 + j;
@@ -250,7 +257,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 uint32_t acc = 0;
                 for (int i = ia; i < ib; i++, it++) {
                     const int s = it % TC_STAGES, n = it / TC_STAGES;
-                    if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3)) {
+                    if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3, wait_ns)) {
                         ok = false;
                         break;
                     }
@@ -271,7 +278,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
             // all MMAs of this thread complete before TMEM is released
             umma_commit(bar(DONE));
-            mbar_wait(bar(DONE), 0, abort_flag, err, 6, false);
+            mbar_wait(bar(DONE), 0, abort_flag, err, 6, kDrainWaitNs, false);
         }
     } else {  // ---------------- epilogue, warps 2..5 -> TMEM lanes 32 * (warp % 4)
         const int q = warp & 3;
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int i = 0; i < TC_BN; i++) sum[i] = cmp[i] = 0.f;
         for (int j = 0; j < nseg; j++) {
             const int b = j & 1, u = j >> 1;
-            if (!mbar_wait(bar(TFULL + b), u & 1, abort_flag, err, 4)) break;
+            if (!mbar_wait(bar(TFULL + b), u & 1, abort_flag, err, 4, wait_ns)) break;
             tc_fence_after();
 #pragma unroll
             for (int ch = 0; ch < TC_BN / 16; ch++) {
@@ -317,6 +324,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                      "r"(TC_TMEM_COLS)
                      : "memory");
+        if (lane == 0) atomicSub(err + 1, 1);  // released
     }
 }
 
@@ -382,7 +390,8 @@ bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* ou
 }
 
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
-                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat) {
+                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat,
+                           unsigned long long wait_ns) {
     static unsigned long long attr_set = 0;  // devices with the shared-memory attribute set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -393,14 +402,15 @@ cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, i
         if (e != cudaSuccess) return e;
         attr_set |= 1ull << dev;
     }
-    if (splits < 1 || nlev < 1 || nlev > L || nlev > Lw || (nmat != 1 && nmat != 2))
+    if (splits < 1 || nlev < 1 || nlev > L || nlev > Lw || (nmat != 1 && nmat != 2) ||
+        wait_ns == 0)
         return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
     std::memcpy(&ma, maps.a, sizeof(ma));
     std::memcpy(&mb, maps.b, sizeof(mb));
     dim3 grid((D + TC_BM - 1) / TC_BM, splits, (C + TC_BN - 1) / TC_BN);
     k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, tc_ldb(D) / TC_BK, nmat,
-                                                C, partial, d_err);
+                                                C, partial, d_err, wait_ns);
     return cudaGetLastError();
 }
 

@@ -260,8 +260,11 @@ size_t tc_plane_bytes(int D, int L, int nmat = 1);
 size_t tc_w_bytes(int D, int C, int Lw, int nmat = 1);
 bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* out,
                   int nmat = 1);
+// Default limit of each pipeline wait of k_conv_tc (2 s of %globaltimer).
+constexpr unsigned long long kTcWaitNsDefault = 2000000000ull;
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
-                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 1);
+                           double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 1,
+                           unsigned long long wait_ns = kTcWaitNsDefault);
 
 // Mixed march with merged levels on tcgen05 (march_tc.cu).
 cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
@@ -354,6 +357,7 @@ struct MarchGraph {
     double a1 = 0, a2 = 0;
     std::vector<double> amp;
     std::vector<const void*> ptrs;
+    unsigned long long wait_ns = 0;  // pipeline wait limit of the tcgen05 kernels
     long long launches = 0;  // kernels in the graph
 };
 
@@ -433,7 +437,8 @@ struct tdbem_ctx {
     float* d_bGK = nullptr;         // G^f kt of every level and case [f][c][D]
     float* d_bGL = nullptr;         // G^f lt of levels 0/1 [f][c][D]
     size_t tc_W_bytes = 0;
-    int* d_tc_err = nullptr;        // pipeline wait time-out code of the tcgen05 kernel
+    int* d_tc_err = nullptr;        // tcgen05 kernel: [0] wait time-out code, [1] CTAs holding TMEM
+    unsigned long long tc_wait_ns = tdbem::kTcWaitNsDefault;  // its pipeline wait limit
     tdbem::TcMaps tc_maps{};
     // mixed march: engine of the time blocks' old-history pass, its BF16 vector planes
     // and tensor maps (encoded for d_mtc_W and the level planes)

@@ -59,6 +59,7 @@ SIGNATURES = {
     "tdbem_set_march_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tdbem_set_pipeline_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "tdbem_set_march_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
                                             ctypes.c_int]),
@@ -346,6 +347,10 @@ class Context:
 
     def set_graphs(self, on: bool):
         _check(load().tdbem_set_graphs(self.h, 1 if on else 0))
+
+    def set_pipeline_wait(self, seconds: float):
+        """Limit of each pipeline wait of the tcgen05 convolution (0: the default, 2 s)."""
+        _check(load().tdbem_set_pipeline_wait(self.h, seconds))
 
     def set_batch_options(self, engine: int = 0, refine_sweeps: int = 0):
         _check(load().tdbem_set_batch_options(self.h, engine, refine_sweeps))
