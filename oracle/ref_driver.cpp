@@ -16,6 +16,10 @@
  *   ref_driver <input.txt> <a1> <a2> <out_prefix> [nolevels]
  *   ref_driver <input.txt> --assemble <node_lo> <node_hi> <nsteps>
  *       (times G_H_Driver alone on a node range, the reference's MPI row split)
+ *   ref_driver <input.txt> --rows <node_lo> <node_hi> <step> <out_prefix>
+ *       (one G_H_Driver(step*dt, dt) on a node range; writes the four row blocks
+ *       GetGHLinear returns, G_1 G_2 H_1 H_2, as <out_prefix>.rows: 4 x
+ *       3*(node_hi-node_lo+1) x 3*nnd float64)
  */
 #include <chrono>
 #include <cstdio>
@@ -122,8 +126,29 @@ static int run_assemble(const char* input, int lo, int hi, int nsteps) {
     return 0;
 }
 
+static int run_rows(const char* input, int lo, int hi, int step, const char* prefix) {
+    ModelManagerT* model = new ModelManagerT;
+    model->ReadInput(input);
+    ElastoDynamicsT* ED = new ElastoDynamicsT(model);
+    ED->SetLowerUpper(lo, hi);
+    const double dt = model->GetDT();
+    ED->G_H_Driver(step * dt, dt);
+    double* blocks[4];
+    ED->GetGHLinear(&blocks[0], &blocks[1], &blocks[2], &blocks[3]);
+    const size_t n = (size_t)3 * (hi - lo + 1) * 3 * model->GetNND();
+    FILE* f = std::fopen((std::string(prefix) + ".rows").c_str(), "wb");
+    for (int b = 0; b < 4; b++) std::fwrite(blocks[b], sizeof(double), n, f);
+    std::fclose(f);
+    delete ED;
+    delete model;
+    return 0;
+}
+
 int main(int argc, char** argv) {
     try {
+        if (argc >= 7 && std::strcmp(argv[2], "--rows") == 0)
+            return run_rows(argv[1], std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]),
+                            argv[6]);
         if (argc >= 6 && std::strcmp(argv[2], "--assemble") == 0)
             return run_assemble(argv[1], std::atoi(argv[3]), std::atoi(argv[4]),
                                 std::atoi(argv[5]));

@@ -17,10 +17,11 @@ def pytest_configure(config):
 
 
 def golden_cases():
-    """Single-region cases (the two-region ones are named mrt_*)."""
+    """Single-region full-march cases (two-region ones are named mrt_*, row-block
+    ones rows_*)."""
     return sorted(n for n in (os.path.basename(p)[:-4]
                               for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
-                  if not n.startswith("mrt_"))
+                  if not n.startswith(("mrt_", "rows_")))
 
 
 def mrt_golden_cases():

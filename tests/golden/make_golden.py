@@ -24,7 +24,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, os.path.join(ROOT, "td-bem_gb300"))
 from tdbem import inputfile, meshes  # noqa: E402
 
-REF_ROOT = os.environ.get("TDBEM_REFERENCE", "/root/reference")
+# the reference checkout: $TDBEM_REFERENCE, else a checkout beside this repository
+REF_ROOT = os.environ.get("TDBEM_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 OUT = os.path.join(ROOT, "tests", "golden")
 SEED = 20151022
 
@@ -62,6 +63,33 @@ def run_case(driver, name, text, a1=0.0, a2=0.0, full_levels=False, dof_stride=1
         rec.update(G=G, H=H)
     np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **rec)
     print(f"{name}: D={D} M={M} steps={ns}")
+
+
+def run_rows_case(driver, name, text, blocks, steps):
+    """G_H_Driver row blocks of a mesh too large for a full level dump: for each
+    (node block, step) the reference's four row blocks (G_1, G_2, H_1, H_2) projected
+    on the seeded vector (rows @ w) plus each block's max-norm."""
+    m = inputfile.parse(text)
+    D = 3 * m.nnd
+    w = projection_vector(D)
+    proj, amax = [], []
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "input.txt")
+        with open(path, "w") as f:
+            f.write(text)
+        prefix = os.path.join(tmp, "out")
+        for lo, hi in blocks:
+            for st in steps:
+                subprocess.run([driver, path, "--rows", str(lo), str(hi), str(st), prefix],
+                               cwd=tmp, check=True, stdout=subprocess.DEVNULL)
+                r = np.fromfile(prefix + ".rows").reshape(4, 3 * (hi - lo + 1), D)
+                proj.append(r @ w)
+                amax.append(np.abs(r).max(axis=(1, 2)))
+    np.savez_compressed(os.path.join(OUT, f"{name}.npz"), input_text=np.array(text),
+                        seed=SEED, blocks=np.array(blocks, np.int32),
+                        steps=np.array(steps, np.int32), rows_w=np.array(proj),
+                        rows_absmax=np.array(amax))
+    print(f"{name}: D={D} blocks={blocks} steps={steps}")
 
 
 def run_mrt_case(name, text1, text2, max_step):
@@ -124,6 +152,14 @@ def main():
     bar2 = open(os.path.join(geo, "Bar_2.txt")).read()
     run_case(driver, "ref_bar2", bar2)
     run_case(driver, "ref_bar2_alpha", bar2, a1=0.25, a2=0.1)
+    # Row blocks (start, middle, end of the node list) of the benchmark's 6x16x16
+    # cubed-sphere cavity (D = 4614), too large for a full level dump.
+    sph16 = meshes.cubed_sphere(16)
+    nnd = sph16.nnd
+    rows_blocks = [(0, 3), (nnd // 2, nnd // 2 + 3), (nnd - 4, nnd - 1)]
+    if not only or "rows_sphere_6x16x16" in only:
+        run_rows_case(driver, "rows_sphere_6x16x16", inputfile.dumps(sph16), rows_blocks,
+                      [1, 2, 30, 60])
     # Two-region solver (SolverMRT): the reference's layer pair, and a bar split into
     # two materials with the history truncated (max_step 10 < MaxStep of region 1) or
     # longer than both regions' MaxStep.

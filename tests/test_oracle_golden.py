@@ -79,3 +79,20 @@ def test_reference_roundoff_floor(name, oracle_mod):
     for k in range(len(G)):
         assert rel_max(Gc[k], G[k]) < 1e-7 and rel_max(Hc[k], H[k]) < 1e-7
     assert np.array_equal(G[:2], Gc[:2]) and np.array_equal(H[:2], Hc[:2])
+
+
+def test_oracle_matches_reference_rows_at_benchmark_size(oracle_mod):
+    """G_H_Driver row blocks of the 6x16x16 cubed-sphere cavity (D = 4614): the
+    reference's own rows (projected on the fixture's seeded vector) at steps 1, 2,
+    M/2 and M, for node blocks at the start, middle and end of the node list."""
+    z, m = load_golden("rows_sphere_6x16x16")
+    o = oracle_mod.Oracle(m)
+    w = np.random.default_rng(int(z["seed"])).standard_normal(o.D)
+    i = 0
+    for lo, hi in z["blocks"]:
+        for st in z["steps"]:
+            got = o.gh_driver(int(st) * m.dt, m.dt, int(lo), int(hi))
+            for b in range(4):
+                assert rel_max(got[b] @ w, z["rows_w"][i][b]) <= TOL, f"rows {lo} step {st}"
+                assert np.abs(got[b]).max() == z["rows_absmax"][i][b]
+            i += 1
