@@ -105,17 +105,36 @@ int tdbem_gh_driver(tdbem_ctx* ctx, int step, int node_lo, int node_hi, double* 
  * their implicit synchronisation).  No counterpart in the reference.  Same
  * result as tdbem_gh_driver, written into caller-owned DEVICE buffers
  * (3*(node_hi-node_lo+1) x D doubles each, zeroed by the call), with work
- * ordered on `stream` (a cudaStream_t; NULL = the context's stream) and not
- * waited for.  Its kernels' scratch is one fixed 8 MiB array in device memory
- * that every GPU loading the library holds until exit; meshes whose largest
- * element colour exceeds 262144 elements are rejected (TDBEM_ERR_UNSUPPORTED).
- * All calls share that array: calls that overlap on the GPU race, so serialise
- * them.  The first call on a device looks the array up with that device
- * current (the context's device must be current); make it before any stream
- * capture.  Calls no cudaMalloc, cudaFree or allocating library routine. */
+ * ordered on `stream` (a cudaStream_t; NULL = the context's stream); the call
+ * never waits for the device.  Its kernels' scratch is one fixed 8 MiB array in
+ * device memory that every GPU loading the library holds until exit; meshes whose
+ * largest element colour exceeds 262144 elements are rejected
+ * (TDBEM_ERR_UNSUPPORTED).  All calls share that array: calls that overlap on the
+ * GPU race, so serialise them.  The array's device address is looked up on every
+ * call made outside a stream capture, with the context's device current (it must
+ * be); the first call on a device must come before any stream capture.  Calls no
+ * cudaMalloc, cudaFree or allocating library routine. */
 int tdbem_gh_driver_noalloc(const tdbem_ctx* ctx, int step, int node_lo, int node_hi,
                             double* d_G_I, double* d_G_J, double* d_H_I, double* d_H_J,
                             void* stream);
+
+/* Element interface: TDElementStepLinearT::FormGH_Regular (singular[i] = -1) or
+ * FormGH_Singular(singular[i]) followed by GetGHLinear (TDElementT.h:16-115,
+ * TDElementStepLinearT.cpp:28-626, TDElementT.cpp:148-157) for n independent
+ * (collocation point, element) pairs, evaluated together in one launch on the
+ * current device.  etype 1 (4 nodes) or 2 (8 nodes), nq Gauss points per direction,
+ * material (E, nu, rho) and t_1 (TDElementT::SetTime's second argument, the time
+ * step) are shared by the batch; per pair: colloc[i] (3 doubles, SetCollocation),
+ * coords[i] (ennd x 3 doubles, SetCoords), t[i] (SetTime's t) and singular[i] (the
+ * element's local node at the collocation point, or -1).  Outputs (host buffers):
+ * GE_1, GE_2, HE_1, HE_2 of n x 3 x 3*ennd doubles ([i][3a + j] of each pair's
+ * block, the reference's fGE_1 ... layout) and C_1, C_2 of n x 9 doubles (the
+ * Kelvin term at t[i] == t_1, zeros otherwise).  FP64, with exact zeros where both
+ * wave fronts have passed a quadrature point at both evaluation times. */
+int tdbem_element_gh(int etype, int nq, double E, double nu, double rho, double t_1, int n,
+                     const double* colloc, const double* coords, const double* t,
+                     const int* singular, double* GE_1, double* GE_2, double* HE_1,
+                     double* HE_2, double* C_1, double* C_2);
 
 /* Assemble the device-resident level store G^k, H^k for k = 0..M: the result
  * of main()'s steps 1..min(M, nsteps) of G_H_Driver + UpdateGHLinear
@@ -260,6 +279,23 @@ int tdbem_set_march_options(tdbem_ctx* ctx, int block_steps, int refine_sweeps);
  * no device code; this bounds the wait a GPU kernel of this library may spend on a
  * pipeline stage. */
 int tdbem_set_pipeline_wait(tdbem_ctx* ctx, double seconds);
+
+/* The FP32 inverses of the TDBEM_MIXED march's LHS (the step-2 LHS and the later
+ * one): probe[v] = max |A (X v) - v| / max |v| of inverse X of A (v a fixed vector)
+ * and full_search[v] = 1 when the pivot search of the panels left their diagonal
+ * blocks (a zero pivot there or a probe above 1e-5 made the inversion start again
+ * with the full partial-pivoting search). */
+int tdbem_inverse_report(const tdbem_ctx* ctx, double probe[2], int full_search[2]);
+
+/* The H^0 inverse alone, on the current device: X = A^-1 for a row-major n x n
+ * host matrix A (blocked Gauss-Jordan with partial pivoting; precision TDBEM_FP64,
+ * or TDBEM_MIXED for the FP32 inverse the mixed march uses, widened to double in
+ * X), with the FP32 inverse's probe residual and pivot-search fallback (probe 0 and
+ * full_search 1 for FP64).  Replaces the factorisation inside KSPSolve
+ * (SolverStepLinearT.cpp:503-504) for callers that solve with the inverse; a zero
+ * pivot gives TDBEM_ERR_SINGULAR. */
+int tdbem_invert(int n, const double* A, int precision, double* X, double* probe,
+                 int* full_search);
 
 /* Device pointers of the histories of the last tdbem_march (FP64,
  * (numstep+1) x D each); valid until the next march or destroy. */

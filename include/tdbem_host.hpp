@@ -3,6 +3,9 @@
 // They mirror the classes main.cpp drives (src/main.cpp:42-130) so that its
 // sequence runs unchanged on the GPU:
 //   ModelManagerT        ModelManagerT.h:16-196 (input reading and getters)
+//   TDElementGpuT        TDElementT.h:16-115 / TDElementStepLinearT (one element's
+//                        G/H blocks: SetCollocation, SetCoords, SetTime, SetNQ,
+//                        SetMaterial, FormGH_Regular, FormGH_Singular, GetGHLinear)
 //   ElastoDynamicsGpuT   ElastoDynamicsT.h:22-39 (G_H_Driver, GetGHLinear)
 //   SolverStepLinearGpuT SolverT.h:22-128 / SolverStepLinearT (SetTimeControl,
 //                        Initialize, GetMaxStep, UpdateGHLinear, SetLoad,
@@ -95,6 +98,49 @@ class ModelManagerT {
     std::vector<int> ien_, ien_aux_;
     std::vector<int> ubc_dof_, fbc_dof_, interface_;
     std::vector<double> ubc_val_, fbc_val_;
+};
+
+// TDElementT / TDElementStepLinearT (TDElementT.h:16-115): the element-level
+// quadrature of one (collocation point, element) pair, with the reference's call
+// sequence.  FormGH_Regular / FormGH_Singular take a copy of the current
+// collocation point, coordinates and time and queue the pair; GetGHLinear
+// evaluates every queued pair in one launch (tdbem_element_gh) and returns the
+// blocks of the pair formed last, as the reference's element returns its own.
+// GetGHLinear(k, ...) returns pair k of that evaluation (0 = the first formed
+// since the previous evaluation), so a caller that forms many elements before
+// reading them gets one launch for all of them.  Material, quadrature order and
+// t_1 are shared by a launch: changing one evaluates the queued pairs first.
+// The returned pointers stay valid until the next evaluation.
+class TDElementGpuT {
+   public:
+    // type: 1 = 4-node quad, 2 = 8-node quad (TDElementT(int type)).
+    explicit TDElementGpuT(int type);
+    void SetCollocation(double* collocation);
+    void SetCoords(double* coords);
+    virtual void SetTime(double t, double t_1);
+    void SetNQ(int nq);
+    void SetMaterial(double E, double nu, double density);
+    virtual void FormGH_Regular();
+    virtual void FormGH_Singular(int singular);
+    void GetGHLinear(const double** GE_1, const double** GE_2, const double** HE_1,
+                     const double** HE_2, const double** C_1, const double** C_2);
+    void GetGHLinear(int k, const double** GE_1, const double** GE_2, const double** HE_1,
+                     const double** HE_2, const double** C_1, const double** C_2);
+    // Pairs of the last evaluation.
+    int NumEvaluated() const { return evaluated_; }
+    virtual ~TDElementGpuT() = default;
+
+   private:
+    void Queue(int singular);
+    void Evaluate();
+    int type_, ennd_, nq_ = 6;
+    double E_ = 0, nu_ = 0, rho_ = 0, t_ = 0, t_1_ = 0;
+    const double* colloc_ = nullptr;
+    const double* coords_ = nullptr;
+    std::vector<double> q_colloc_, q_coords_, q_t_;
+    std::vector<int> q_sing_;
+    std::vector<double> ge1_, ge2_, he1_, he2_, c1_, c2_;
+    int evaluated_ = 0;
 };
 
 class SolverStepLinearGpuT;

@@ -83,7 +83,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     if _stale(LIB, objs):
         cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + \
-            ["-lcublas", "-lcudart", "-lpthread", "-Xlinker", "-rpath=" + cuda_lib]
+            ["-lcudart", "-lpthread", "-Xlinker", "-rpath=" + cuda_lib]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -694,6 +694,193 @@ __global__ void __launch_bounds__(128) k_assemble_items(
                               step_n, part, pi, p, k, out, (int)(gid & SH));
 }
 
+// One step (ASM_STEP) without compaction: one thread per pair (two for an 8-node
+// element), the pairs outside the step's window returning at once.  A pair holds
+// at most one item of a step, so this needs neither a scan of the counts nor the
+// item total on the host; the allocation-free driver (noalloc.cu) uses it so that
+// a call never waits for the device.  Same items, same arithmetic and the same
+// colour-ordered scatter as k_assemble_items, so the same results bit for bit.
+template <int ENND>
+__global__ void __launch_bounds__(128) k_assemble_step_pairs(
+    const double* __restrict__ coords, const int* __restrict__ ien,
+    const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
+    const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int step_n,
+    int part, const PairInfo* __restrict__ pairs, unsigned npairs, AsmOut out) {
+    constexpr int SH = ENND == 8 ? 1 : 0;
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned p = gid >> SH;
+    if (p >= npairs) return;
+    const PairInfo pi = pairs[p];
+    if (pi.cnt == 0) return;
+    assemble_item<ASM_STEP, ENND>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, step_n,
+                                  step_n, part, pi, p, pi.klo, out, (int)(gid & SH));
+}
+
+// ---------------------------------------------------------------------------
+// Element interface (TDElementT / TDElementStepLinearT): a batch of independent
+// (collocation point, element) pairs, each with its own node coordinates, time and
+// singular node, integrated as FormGH_Regular / FormGH_Singular(singular)
+// integrate one element (TDElementStepLinearT.cpp:28-626) and written as the
+// element blocks GetGHLinear returns: GE_1/HE_1 (I part) and GE_2/HE_2 (J part),
+// 3 x 3 ennd row-major each, [i][3a + j].  The points, Duffy rules, sub-elements
+// and kernels are the mesh path's (q4_eval / q8_eval, duffy_point,
+// q8_subelements, gauss_point); the geometry is evaluated per point instead of
+// read from a per-mesh table.
+// ---------------------------------------------------------------------------
+
+// Kelvin part of one element (C_1 = C_2 = -sum wJ DT_Kelvin^T at t == t_1,
+// TDElementStepLinearT.cpp:110-116 and its singular counterpart), from the same
+// points as the element's quadrature.
+template <int ENND>
+__device__ void element_cterm(const double* en, const double xc[3], int sing, int nq,
+                              const double* __restrict__ gx, const double* __restrict__ gw,
+                              const Phys& ph, double acc[9]) {
+    const double onem2nu = 1 - 2 * ph.nu;
+    const double kscale = (0.5 * ph.dt) / (-(8 * M_PI) * (1 - ph.nu));
+    for (int m = 0; m < 9; m++) acc[m] = 0;
+    int ids[2][4] = {{0, 1, 2, 3}, {0, 1, 2, 3}}, cid[2] = {sing, sing};
+    int nsub = 1;
+    if (ENND == 8 && sing >= 0) nsub = q8_subelements(sing, ids, cid);
+    const int nq2 = nq * nq;
+    const int npts = sing < 0 ? nq2 : nsub * 2 * nq2;
+    double cn[12];
+    int cur = -1;
+    for (int qq = 0; qq < npts; qq++) {
+        double xq[3], nv[3], wJ;
+        if (sing < 0) {
+            const int q1 = qq / nq, q2 = qq % nq;
+            double N[ENND], J;
+            if constexpr (ENND == 8) q8_eval(en, gx[q1], gx[q2], N, xq, nv, J);
+            else q4_eval(en, gx[q1], gx[q2], N, xq, nv, J);
+            wJ = (gw[q1] * gw[q2]) * J;
+        } else {
+            const int se = qq / (2 * nq2), r = qq % (2 * nq2);
+            if (se != cur) {
+                for (int i = 0; i < 4; i++)
+                    for (int d = 0; d < 3; d++) cn[i * 3 + d] = en[ids[se][i] * 3 + d];
+                cur = se;
+            }
+            const int tri = r / nq2, q = r % nq2, q1 = q / nq, q2 = q % nq;
+            double N[4];
+            duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
+        }
+        const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
+        const double inv_r = 1.0 / sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const double rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+        const double rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
+        const double w = wJ * (kscale * inv_r * inv_r);
+        for (int i = 0; i < 3; i++)
+            for (int kk = 0; kk < 3; kk++) {
+                const double Kki = ((kk == i ? onem2nu : 0.0) + 3 * rv[kk] * rv[i]) * rdn -
+                                   onem2nu * (rv[i] * nv[kk] - rv[kk] * nv[i]);
+                acc[i * 3 + kk] -= w * Kki;
+            }
+    }
+}
+
+// One thread per pair (two adjacent threads for an 8-node element, one per half of
+// its nodes); part 0 writes GE_1 / HE_1 (and C at t == t_1), part 1 GE_2 / HE_2.
+template <int ENND>
+__global__ void __launch_bounds__(128) k_element_gh(
+    int n, int nq, const double* __restrict__ gx, const double* __restrict__ gw, Phys ph,
+    const double* __restrict__ colloc, const double* __restrict__ ecoords,
+    const double* __restrict__ times, const int* __restrict__ sing_in, int part,
+    double* __restrict__ GE, double* __restrict__ HE, double* __restrict__ C1,
+    double* __restrict__ C2) {
+    constexpr int SH = ENND == 8 ? 1 : 0;
+    const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned item = gid >> SH;
+    const int half = (int)(gid & SH);
+    if (item >= (unsigned)n) return;
+    const double xc[3] = {colloc[item * 3], colloc[item * 3 + 1], colloc[item * 3 + 2]};
+    double en[3 * ENND];
+    for (int m = 0; m < 3 * ENND; m++) en[m] = ecoords[(size_t)item * 3 * ENND + m];
+    const double t = times[item];
+    const int sing = sing_in[item];
+    TimeConsts tc;
+    tc.doI = (part == 0);
+    tc.doJ = (part == 1);
+    time_consts(tc, t, t, ph.dt);
+    ItemAcc acc;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] = 0;
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] = 0;
+    }
+    const int nq2 = nq * nq;
+    if (sing < 0) {
+        for (int q = 0; q < nq2; q++) {
+            const int q1 = q / nq, q2 = q % nq;
+            double Nf[ENND], xq[3], nqv[3], J;
+            if constexpr (ENND == 8) q8_eval(en, gx[q1], gx[q2], Nf, xq, nqv, J);
+            else q4_eval(en, gx[q1], gx[q2], Nf, xq, nqv, J);
+            const double N[4] = {Nf[4 * half], Nf[4 * half + 1], Nf[4 * half + 2],
+                                 Nf[4 * half + 3]};
+            gauss_point(acc, tc, ph, xc, xq, nqv, (gw[q1] * gw[q2]) * J, N);
+        }
+    } else if (ENND == 8) {
+        int ids[2][4], cid[2];
+        const int nsub = q8_subelements(sing, ids, cid);
+        for (int se = 0; se < nsub; se++) {
+            double cn[12];
+            int slot[4];
+            for (int i = 0; i < 4; i++) {
+                slot[i] = ids[se][i] - 4 * half;
+                for (int d = 0; d < 3; d++) cn[i * 3 + d] = en[ids[se][i] * 3 + d];
+            }
+            for (int qq = 0; qq < 2 * nq2; qq++) {
+                const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+                double N4[4], xq[3], nqv[3], wJ;
+                duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N4, xq, nqv,
+                            wJ);
+                double N[4] = {0, 0, 0, 0};
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+                        if (slot[i] == a) N[a] = N4[i];
+                gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
+            }
+        }
+    } else {
+        for (int qq = 0; qq < 2 * nq2; qq++) {
+            const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+            double N[4], xq[3], nqv[3], wJ;
+            duffy_point(en, sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nqv, wJ);
+            gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
+        }
+    }
+    constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+    const size_t row = 3 * (size_t)ENND;  // 3 ennd entries per row of an element block
+    double* G = GE + (size_t)item * 3 * row;
+    double* H = HE + (size_t)item * 3 * row;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const size_t idx = (size_t)i * row + 3 * (size_t)(a + 4 * half) + j;
+                G[idx] = acc.g[a][sym[i * 3 + j]];
+                H[idx] = acc.h[a][i * 3 + j];
+            }
+    if (part == 0 && half == 0) {
+        double c[9];
+        if (t == ph.dt) {
+            element_cterm<ENND>(en, xc, sing, nq, gx, gw, ph, c);
+        } else {
+            for (int m = 0; m < 9; m++) c[m] = 0;
+        }
+        for (int m = 0; m < 9; m++) {
+            C1[item * 9 + m] = c[m];
+            C2[item * 9 + m] = c[m];
+        }
+    }
+}
+
+
 // ---------------------------------------------------------------------------
 // FP32 far-field quadrature (mixed precision).
 //
@@ -1354,6 +1541,49 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
     } else {
         launch_items_fp64<4>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
                              level_last, step_n, pairs, offsets, npairs, nitems, out, s);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_step_pairs(const double* coords, const int* ien, int ennd,
+                                       const int* elems, int nelem_color, int node_lo, int nq,
+                                       const double* gx, const double* gw, const double* geom,
+                                       const Phys& ph, int step_n, const PairInfo* pairs,
+                                       unsigned npairs, const AsmOut& out, cudaStream_t s) {
+    if (npairs == 0) return cudaSuccess;
+    const int bs = 128;
+    const unsigned long long threads = (unsigned long long)npairs << (ennd == 8 ? 1 : 0);
+    const unsigned grid = (unsigned)((threads + bs - 1) / bs);
+    for (int part = 0; part < 2; part++) {
+        if (ennd == 8)
+            k_assemble_step_pairs<8><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo,
+                                                         nq, gx, gw, geom, ph, step_n, part,
+                                                         pairs, npairs, out);
+        else
+            k_assemble_step_pairs<4><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo,
+                                                         nq, gx, gw, geom, ph, step_n, part,
+                                                         pairs, npairs, out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_element_gh(int ennd, int n, int nq, const double* gx, const double* gw,
+                              const Phys& ph, const double* colloc, const double* ecoords,
+                              const double* times, const int* sing, double* GE1, double* GE2,
+                              double* HE1, double* HE2, double* C1, double* C2, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    const int bs = 128;
+    const unsigned long long threads = (unsigned long long)n << (ennd == 8 ? 1 : 0);
+    const unsigned grid = (unsigned)((threads + bs - 1) / bs);
+    for (int part = 0; part < 2; part++) {
+        double* G = part == 0 ? GE1 : GE2;
+        double* H = part == 0 ? HE1 : HE2;
+        if (ennd == 8)
+            k_element_gh<8><<<grid, bs, 0, s>>>(n, nq, gx, gw, ph, colloc, ecoords, times, sing,
+                                                part, G, H, C1, C2);
+        else
+            k_element_gh<4><<<grid, bs, 0, s>>>(n, nq, gx, gw, ph, colloc, ecoords, times, sing,
+                                                part, G, H, C1, C2);
     }
     return cudaGetLastError();
 }

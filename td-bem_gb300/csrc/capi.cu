@@ -295,6 +295,28 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
 
 void tdbem::note_error(const char* msg) { g_last_error = msg; }
 
+tdbem::Phys tdbem::make_phys(double E, double nu, double rho, double dt) {
+    // GreenFunctionT::WaveSpeed (GreenFunctionT.cpp:76-84)
+    const double mu = E / (2 * (1 + nu));
+    const double lam = E * nu / ((1 + nu) * (1 - 2 * nu));
+    Phys ph;
+    ph.dt = dt;
+    ph.inv_dt = 1.0 / dt;
+    ph.cp = std::sqrt((lam + 2 * mu) / rho);
+    ph.cs = std::sqrt(mu / rho);
+    ph.inv_cp = 1.0 / ph.cp;
+    ph.inv_cs = 1.0 / ph.cs;
+    ph.inv_cp2 = 1.0 / (ph.cp * ph.cp);
+    ph.inv_cs2 = 1.0 / (ph.cs * ph.cs);
+    ph.cs2 = ph.cs * ph.cs;
+    ph.ratio2 = (ph.cs / ph.cp) * (ph.cs / ph.cp);
+    ph.ratio3 = ph.ratio2 * (ph.cs / ph.cp);
+    ph.inv_4pi_rho = 1.0 / (4 * M_PI * rho);
+    ph.inv_4pi = 1.0 / (4 * M_PI);
+    ph.nu = nu;
+    return ph;
+}
+
 extern "C" {
 
 const char* tdbem_last_error(void) { return g_last_error.c_str(); }
@@ -342,24 +364,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     c->h_coords.assign(mesh->coords, mesh->coords + 3 * (size_t)mesh->nnd);
     c->h_ien.assign(mesh->ien, mesh->ien + ennd * (size_t)mesh->nel);
     c->M = compute_max_step(c->h_coords, c->nnd, c->E, c->nu, c->rho, dt);
-    // GreenFunctionT::WaveSpeed (GreenFunctionT.cpp:76-84)
-    const double mu = c->E / (2 * (1 + c->nu));
-    const double lam = c->E * c->nu / ((1 + c->nu) * (1 - 2 * c->nu));
-    Phys& ph = c->ph;
-    ph.dt = dt;
-    ph.inv_dt = 1.0 / dt;
-    ph.cp = std::sqrt((lam + 2 * mu) / c->rho);
-    ph.cs = std::sqrt(mu / c->rho);
-    ph.inv_cp = 1.0 / ph.cp;
-    ph.inv_cs = 1.0 / ph.cs;
-    ph.inv_cp2 = 1.0 / (ph.cp * ph.cp);
-    ph.inv_cs2 = 1.0 / (ph.cs * ph.cs);
-    ph.cs2 = ph.cs * ph.cs;
-    ph.ratio2 = (ph.cs / ph.cp) * (ph.cs / ph.cp);
-    ph.ratio3 = ph.ratio2 * (ph.cs / ph.cp);
-    ph.inv_4pi_rho = 1.0 / (4 * M_PI * c->rho);
-    ph.inv_4pi = 1.0 / (4 * M_PI);
-    ph.nu = c->nu;
+    c->ph = make_phys(c->E, c->nu, c->rho, dt);
     std::vector<int> order;
     color_elements(c->h_ien, c->nel, c->ennd, c->nnd, order, c->color_start);
     int max_color = 0;
@@ -380,7 +385,6 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
         }                                                                                    \
     } while (0)
     CTX_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    blas_pool_init(c->device);  // before any march of this device can capture a graph
     CTX_TRY(dalloc(&c->d_coords, c->h_coords.size()));
     CTX_TRY(dalloc(&c->d_ien, c->h_ien.size()));
     CTX_TRY(dalloc(&c->d_gx, nq));

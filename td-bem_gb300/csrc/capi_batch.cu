@@ -87,10 +87,9 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         const int pk = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_batch_known_tractions(c->d_btrac, c->d_is_ubc, D, C, c->d_bkt,
                                               c->d_bkt + CD, s));
-        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, M + 1, c->d_bkt, C, c->d_bGK,
-                                      c->device, s));
+        CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, M + 1, c->d_bkt, C, c->d_bGK, s));
         CUDA_TRY(levels_times_columns(c->d_Gf, c->ldf, D, std::min(2, M + 1), c->d_bkt + CD, C,
-                                      c->d_bGL, c->device, s));
+                                      c->d_bGL, s));
         prof_end(c, pk, (M + 3) * (double)D * c->ldf * 4, 2.0 * (M + 3) * (double)D * D * C);
         c->launches += 3;
     }

@@ -152,6 +152,7 @@ struct InvResult {
     cudaError_t e[2] = {cudaSuccess, cudaSuccess};
     bool singular[2] = {false, false};
     long long launches[2] = {0, 0};
+    InverseReport report[2];
 };
 
 void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t s0,

@@ -50,8 +50,15 @@ int prepare_inverses(tdbem_ctx* c, int ninv) {
         if (!c->d_inv32[v]) CUDA_TRY(dalloc(&c->d_inv32[v], DD));
     }
     if (!c->d_inv_scratch32) CUDA_TRY(dalloc(&c->d_inv_scratch32, inverse_scratch_elems(c->D)));
+    // The inverses are chains of short dependent launches that run beside the
+    // assembly's long quadrature launches: their streams take the device's highest
+    // priority, so each of their blocks is scheduled as soon as an SM has room
+    // instead of queueing behind the quadrature's pending blocks.
+    int prio_least = 0, prio_greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
     for (cudaStream_t* st : {&c->stream2, &c->stream3})
-        if (!*st) CUDA_TRY(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking));
+        if (!*st)
+            CUDA_TRY(cudaStreamCreateWithPriority(st, cudaStreamNonBlocking, prio_greatest));
     if (!c->ev_fork) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
     if (!c->ev_fork2) CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming));
     if (ninv == 2) {
@@ -74,16 +81,12 @@ void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t
     const int D = c->D;
     const size_t DD = (size_t)D * D;
     auto invert = [&](int v, cudaStream_t st, int* perm, int* status, float* scratch) {
-        // a cuBLAS handle of the device's pool for the trailing updates (without one
-        // the inverse uses its own update kernel)
-        void* blas = blas_checkout(c->device);
         r.e[v] = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[v][0],
                                   lhs_c[v][1], c->d_is_ubc, c->d_Hc64[v], st);
         if (r.e[v] == cudaSuccess)
             r.e[v] = invert_f32(c->d_Hc64[v], c->d_inv32[v], D, perm, status, scratch,
-                                &r.launches[v], &r.singular[v], st, blas);
-        blas_return(c->device, blas);  // invert_f32 synchronises its stream before returning
-        r.launches[v] += 1;
+                                &r.launches[v], &r.singular[v], st, &r.report[v]);
+        r.launches[v] += 1;  // invert_f32 synchronises its stream before returning
     };
     if (ninv == 2) {
         r.e[1] = cudaEventRecord(c->ev_fork2, s0);  // levels 0/1 and the maps are ready
@@ -113,6 +116,7 @@ int finish_inverses(tdbem_ctx* c, int ninv, const InvResult& r) {
         c->d_inv32[1] = c->d_inv32[0];
         c->d_Hc64[1] = c->d_Hc64[0];
     }
+    for (int v = 0; v < 2; v++) c->inv_report[v] = r.report[v < ninv ? v : 0];
     c->inv_valid = true;
     c->inv_n = ninv;
     c->inv_a1 = c->a1;
@@ -727,6 +731,75 @@ int tdbem_set_pipeline_wait(tdbem_ctx* c, double seconds) {
     if (!(seconds >= 0) || seconds > 60) return fail(TDBEM_ERR_ARG, "wait limit %g s", seconds);
     const unsigned long long ns = (unsigned long long)(seconds * 1e9);
     c->tc_wait_ns = seconds == 0 ? kTcWaitNsDefault : std::max(1ull, ns);
+    return TDBEM_OK;
+}
+
+int tdbem_inverse_report(const tdbem_ctx* c, double probe[2], int full_search[2]) {
+    if (!c || !probe || !full_search) return fail(TDBEM_ERR_ARG, "null argument");
+    if (!c->inv_valid) return fail(TDBEM_ERR_STATE, "no FP32 inverse made yet");
+    for (int v = 0; v < 2; v++) {
+        probe[v] = c->inv_report[v].probe_rel;
+        full_search[v] = c->inv_report[v].full_search;
+    }
+    return TDBEM_OK;
+}
+
+int tdbem_invert(int n, const double* A, int precision, double* X, double* probe,
+                 int* full_search) {
+    if (n < 1 || !A || !X) return fail(TDBEM_ERR_ARG, "invalid matrix");
+    if (precision != TDBEM_FP64 && precision != TDBEM_MIXED)
+        return fail(TDBEM_ERR_ARG, "unknown precision %d", precision);
+    const size_t nn = (size_t)n * n;
+    cudaStream_t s = cudaStreamPerThread;
+    double* dA = nullptr;
+    double* dA64 = nullptr;
+    float* dX = nullptr;
+    int* perm = nullptr;
+    int* status = nullptr;
+    void* scratch = nullptr;
+    auto release = [&] {
+        dfree(dA);
+        dfree(dA64);
+        dfree(dX);
+        dfree(perm);
+        dfree(status);
+        if (scratch) cudaFree(scratch);
+    };
+    const size_t scratch_bytes = inverse_scratch_elems(n) * sizeof(double);
+    cudaError_t e = dalloc(&dA, nn);
+    if (e == cudaSuccess) e = dalloc(&perm, (size_t)n + 2 * kMaxPivotBlocks);
+    if (e == cudaSuccess) e = dalloc(&status, 1);
+    if (e == cudaSuccess) e = cudaMalloc(&scratch, scratch_bytes);
+    if (e == cudaSuccess && precision == TDBEM_MIXED) e = dalloc(&dX, nn);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dA, A, sizeof(double) * nn, cudaMemcpyHostToDevice, s);
+    long long nl = 0;
+    bool singular = false;
+    InverseReport rep;
+    if (e == cudaSuccess) {
+        if (precision == TDBEM_FP64)
+            e = invert_f64(dA, n, perm, status, static_cast<double*>(scratch), &nl, &singular, s);
+        else
+            e = invert_f32(dA, dX, n, perm, status, static_cast<float*>(scratch), &nl, &singular,
+                           s, &rep);
+    }
+    std::vector<float> hx;
+    if (e == cudaSuccess && !singular) {
+        if (precision == TDBEM_FP64) {
+            e = cudaMemcpyAsync(X, dA, sizeof(double) * nn, cudaMemcpyDeviceToHost, s);
+        } else {
+            hx.resize(nn);
+            e = cudaMemcpyAsync(hx.data(), dX, sizeof(float) * nn, cudaMemcpyDeviceToHost, s);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    release();
+    if (e != cudaSuccess)
+        return fail(e == cudaErrorMemoryAllocation ? TDBEM_ERR_NOMEM : TDBEM_ERR_CUDA,
+                    "tdbem_invert: %s", cudaGetErrorString(e));
+    if (singular) return fail(TDBEM_ERR_SINGULAR, "zero pivot in the inversion");
+    for (size_t i = 0; i < hx.size(); i++) X[i] = hx[i];
+    if (probe) *probe = precision == TDBEM_MIXED ? rep.probe_rel : 0.0;
+    if (full_search) *full_search = precision == TDBEM_MIXED ? rep.full_search : 1;
     return TDBEM_OK;
 }
 

@@ -16,19 +16,17 @@
 //      A[i, C1] = -A[i, C1] Ainv11       for rows i not in R1.
 // After the last panel the columns are permuted back (reverse order of the
 // row swaps).  Step 5 is a rank-bw update with bw-deep dot products, so the
-// whole inversion is 2 n^3 flops in GEMM form.  With a cuBLAS handle (the FP32
-// inverse) step 5 is two plain GEMMs over the columns left and right of C1 and
-// every row: rows R1 are rewritten by step 6 whatever step 5 leaves there, and
-// step 6 reads only columns C1, which the GEMMs do not write.
+// whole inversion is 2 n^3 flops in GEMM form; the FP32 inverse runs step 5 on
+// 128 x 128 tiles (k_panel_update_f32), the FP64 one on 64 x 64 tiles.
 //
 // The FP32 inverse (a preconditioner that FP64 refinement corrects) may restrict
 // step 1's search to the panel's diagonal block (k_block_pivots, one CTA: no
 // cluster-wide reduction per column).  On the boundary-element LHS the column
 // maximum lies in that block (diagonal dominance), so the pivots are the same; a
-// zero pivot in the block, or a probe ||A (X v) - v|| / ||v|| above 1e-2 of the
-// finished inverse, sends the inversion back to the full search.
+// zero pivot in the block, or a probe max |A (X v) - v| / max |v| of the finished
+// inverse above kInverseProbeBar (1e-5), sends the inversion back to the full
+// search.
 #include <cooperative_groups.h>
-#include <cublas_v2.h>
 
 #include <algorithm>
 #include <cstring>
@@ -411,6 +409,109 @@ __global__ void __launch_bounds__(256) k_panel_update(T* __restrict__ A, int n, 
     }
 }
 
+// The FP32 inverse's rank-64 trailing update, A[i][j] -= sum_c A[i][k0+c] T12[c][j]
+// for i not in R1, j not in C1, on 128 x 128 tiles: the panel columns (transposed)
+// and the T12 rows in shared memory, 8 x 8 outputs per thread (two 4-wide groups in
+// rows and columns, 64 apart, so that a warp's shared-memory reads are conflict
+// free), 64 FMAs per four 16-byte shared loads.  FP32 products and sums, as a
+// plain SGEMM; the reads and writes of A are scalar (rows of an n not divisible by
+// 4 are not 16-byte aligned).
+constexpr int kUpdTile = 128, kUpdBW = 64, kUpdPad = 4;
+
+// 4-byte asynchronous global-to-shared copy (cp.async, completion awaited with
+// cp.async.wait_all by the issuing thread).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src)
+                 : "memory");
+}
+constexpr int kUpdSmem = 2 * kUpdBW * (kUpdTile + kUpdPad) * (int)sizeof(float);
+
+__global__ void __launch_bounds__(256) k_panel_update_f32(float* __restrict__ A, int n, int k0,
+                                                          int bw, const float* __restrict__ T12,
+                                                          const int* __restrict__ status) {
+    if (*status) return;
+    extern __shared__ float usm[];
+    float* sP = usm;                                 // [c][r], row stride kUpdTile + kUpdPad
+    float* sT = usm + kUpdBW * (kUpdTile + kUpdPad);  // [c][q]
+    constexpr int LD = kUpdTile + kUpdPad;
+    const int i0 = blockIdx.y * kUpdTile, j0 = blockIdx.x * kUpdTile;
+    const int tid = threadIdx.x;
+    // panel tile sP[c][r] = A[i0 + r][k0 + c] (a warp reads 32 consecutive c of one
+    // row) and T12 tile sT[c][q] = T12[c][j0 + q]: every element an asynchronous
+    // 4-byte copy, all in flight together; zeros outside the matrix
+#pragma unroll
+    for (int it = 0; it < kUpdTile * kUpdBW / 256; it++) {
+        const int idx = tid + it * 256;
+        const int r = idx / kUpdBW, c = idx % kUpdBW;
+        const int i = i0 + r;
+        float* dst = sP + c * LD + r;
+        if (i < n && c < bw) cp_async4(dst, A + (size_t)i * n + k0 + c);
+        else *dst = 0.f;
+    }
+#pragma unroll
+    for (int it = 0; it < kUpdTile * kUpdBW / 256; it++) {
+        const int idx = tid + it * 256;
+        const int c = idx / kUpdTile, q = idx % kUpdTile;
+        const int j = j0 + q;
+        float* dst = sT + c * LD + q;
+        if (j < n && c < bw) cp_async4(dst, T12 + (size_t)c * n + j);
+        else *dst = 0.f;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    const int tx = tid % 16, ty = tid / 16;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) acc[a][b] = 0.f;
+#pragma unroll 4
+    for (int c = 0; c < kUpdBW; c++) {
+        const float4 p0 = *reinterpret_cast<const float4*>(sP + c * LD + ty * 4);
+        const float4 p1 = *reinterpret_cast<const float4*>(sP + c * LD + ty * 4 + 64);
+        const float4 t0 = *reinterpret_cast<const float4*>(sT + c * LD + tx * 4);
+        const float4 t1 = *reinterpret_cast<const float4*>(sT + c * LD + tx * 4 + 64);
+        const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+        const float tb[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+#pragma unroll
+        for (int a = 0; a < 8; a++)
+#pragma unroll
+            for (int b = 0; b < 8; b++) acc[a][b] = fmaf(pa[a], tb[b], acc[a][b]);
+    }
+    // read-modify-write of the C tile, two of the thread's rows at a time: their 16
+    // reads are issued together before any write (a store to A between two reads
+    // of A would otherwise serialise every read's DRAM latency)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float cv[2][8];
+        bool ok[2][8];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int a = 2 * q + h;
+            const int i = i0 + ty * 4 + (a & 3) + (a >> 2) * 64;
+            const bool row_ok = i < n && !(i >= k0 && i < k0 + bw);
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int j = j0 + tx * 4 + (b & 3) + (b >> 2) * 64;
+                ok[h][b] = row_ok && j < n && !(j >= k0 && j < k0 + bw);
+                cv[h][b] = ok[h][b] ? A[(size_t)i * n + j] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int a = 2 * q + h;
+            const int i = i0 + ty * 4 + (a & 3) + (a >> 2) * 64;
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int j = j0 + tx * 4 + (b & 3) + (b >> 2) * 64;
+                if (ok[h][b]) A[(size_t)i * n + j] = cv[h][b] - acc[a][b];
+            }
+        }
+    }
+}
+
 // Rows R1 <- [T12 | Ainv11]; other rows' C1 block <- -A[i, C1] Ainv11.
 template <typename T, int BW>
 __global__ void __launch_bounds__(256) k_panel_finish(T* __restrict__ A, int n, int k0, int bw,
@@ -519,6 +620,86 @@ __global__ void __launch_bounds__(256) k_block_pivots(const T* __restrict__ A, i
     }
 }
 
+// The same pivot sequence (largest magnitude, lowest row on ties) from one warp:
+// the block is copied into shared memory by four warps (asynchronous copies, all in
+// flight together), then warp 0 factors it without block barriers, each lane owning
+// rows lane and lane + 32 (BW = 64).  Each column costs a warp reduction and the
+// lane-parallel row updates instead of four block barriers.
+template <int BW>
+__global__ void __launch_bounds__(128) k_block_pivots_warp(const float* __restrict__ A, int n,
+                                                           int k0, int bw, int* __restrict__ perm,
+                                                           int* __restrict__ status) {
+    static_assert(BW % 32 == 0, "rows per lane");
+    constexpr int RPL = BW / 32;
+    __shared__ float ws[BW][BW + 1];
+#pragma unroll 8
+    for (int idx = threadIdx.x; idx < BW * BW; idx += 128) {
+        const int r = idx / BW, c = idx % BW;
+        if (r < bw && c < bw)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                             (unsigned)__cvta_generic_to_shared(&ws[r][c])),
+                         "l"(A + (size_t)(k0 + r) * n + k0 + c)
+                         : "memory");
+        else
+            ws[r][c] = 0.f;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    for (int c = 0; c < bw; c++) {
+        float best = -1.f;
+        int bi = bw;
+#pragma unroll
+        for (int k = 0; k < RPL; k++) {
+            const int r = lane + 32 * k;
+            if (r >= c && r < bw) {
+                const float v = fabsf(ws[r][c]);
+                if (v > best) {
+                    best = v;
+                    bi = r;
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+            const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (v2 > best || (v2 == best && i2 < bi)) {
+                best = v2;
+                bi = i2;
+            }
+        }
+        const int p = (bi < bw && best != 0.f) ? bi : -1;  // the same on every lane
+        if (p < 0) {
+            if (lane == 0) *status = 2;
+            return;
+        }
+        if (p != c) {
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                const int j = lane + 32 * k;
+                const float t = ws[c][j];
+                ws[c][j] = ws[p][j];
+                ws[p][j] = t;
+            }
+        }
+        if (lane == 0) perm[k0 + c] = k0 + p;
+        __syncwarp();
+        const float inv = 1.f / ws[c][c];
+#pragma unroll
+        for (int k = 0; k < RPL; k++) {
+            const int r = lane + 32 * k;
+            if (r > c && r < bw) {
+                const float l = ws[r][c] * inv;
+                for (int j = c + 1; j < BW; j++) ws[r][j] -= l * ws[c][j];
+                ws[r][c] = l;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Probe of an FP32 inverse X of A64: y = X v, then err = max_i |(A64 y)_i - v_i|
 // (v_i = (i mod 13) - 6.5, max |v| = 6.5), as the float bits of a non-negative
 // value (integer max preserves the order).  Warp per row.
@@ -614,19 +795,18 @@ cudaError_t pivot_attributes() {
             r = cudaFuncSetAttribute((const void*)k_panel_pivots_cluster<T, BW>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kClusterPanelBytes);
+        if (r == cudaSuccess && std::is_same<T, float>::value && BW == kUpdBW)
+            r = cudaFuncSetAttribute((const void*)k_panel_update_f32,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kUpdSmem);
         return r;
     }();
     return e;
 }
 
-// FP32 GEMM on the tensor cores with FP32 accuracy (each input as three BF16
-// terms), where this cuBLAS offers it.
-cublasComputeType_t blas_compute() { return CUBLAS_COMPUTE_32F_EMULATED_16BFX9; }
 
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
-                           bool* singular, cudaStream_t s, bool restricted = false,
-                           void* blas = nullptr) {
+                           bool* singular, cudaStream_t s, bool restricted = false) {
     *singular = false;
     {
         const cudaError_t ea = pivot_attributes<T, BW>();
@@ -652,7 +832,10 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         const T* cA = A;
         bool done = false;
         if (restricted) {
-            k_block_pivots<T, BW><<<1, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
+            if constexpr (std::is_same<T, float>::value && BW == 64)
+                k_block_pivots_warp<BW><<<1, 128, 0, s>>>(A, n, k0, bw, perm, d_status);
+            else
+                k_block_pivots<T, BW><<<1, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
             done = true;
         }
         // the panel in one cluster's distributed shared memory when it fits
@@ -689,34 +872,11 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         k_panel_inv<T, BW><<<1, 1024, 0, s>>>(A, n, k0, bw, Ainv, d_status);
         k_panel_t12<T, BW><<<(n + 255) / 256, 256, 0, s>>>(A, n, k0, bw, Ainv, T12, d_status);
         bool updated = false;
-        if constexpr (std::is_same<T, float>::value) {
-            if (blas) {  // A[:, J] -= A[:, C1] T12[:, J] for J left and right of C1
-                cublasHandle_t h = static_cast<cublasHandle_t>(blas);
-                if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-                const float alpha = -1.f, beta = 1.f;
-                const int spans[2][2] = {{0, k0}, {k0 + bw, n - k0 - bw}};
-                for (const auto& sp : spans) {
-                    if (sp[1] <= 0) continue;
-                    // column-major views of the row-major arrays: C^T -= T12_J^T A_C1^T;
-                    // plain FP32 where the emulated form does not take the shape
-                    // (rows of an odd n are not 16-byte aligned)
-                    auto gemm = [&](cublasComputeType_t ct) {
-                        return cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, sp[1], n, bw, &alpha,
-                                            T12 + sp[0], CUDA_R_32F, n, A + k0, CUDA_R_32F, n,
-                                            &beta, A + sp[0], CUDA_R_32F, n, ct,
-                                            CUBLAS_GEMM_DEFAULT);
-                    };
-                    cublasStatus_t st = gemm(blas_compute());
-                    if (st == CUBLAS_STATUS_NOT_SUPPORTED) st = gemm(CUBLAS_COMPUTE_32F);
-                    if (st != CUBLAS_STATUS_SUCCESS) {
-                        note_error(("cuBLAS trailing update: " +
-                                    std::string(cublasGetStatusString(st))).c_str());
-                        return cudaErrorUnknown;
-                    }
-                    *nlaunch += 1;
-                }
-                updated = true;
-            }
+        if constexpr (std::is_same<T, float>::value && BW == kUpdBW) {
+            const dim3 wgrid((n + kUpdTile - 1) / kUpdTile, (n + kUpdTile - 1) / kUpdTile);
+            k_panel_update_f32<<<wgrid, 256, kUpdSmem, s>>>(A, n, k0, bw, T12, d_status);
+            *nlaunch += 1;
+            updated = true;
         }
         if (!updated) {
             k_panel_update<T, BW><<<ugrid, 256, 0, s>>>(A, n, k0, bw, T12, d_status);
@@ -763,117 +923,134 @@ cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scrat
     return invert_blocked<double, 16>(A, n, perm, d_status, scratch, nlaunch, singular, s);
 }
 
-// cuBLAS handles, a fixed pool per device.  Creating (or destroying) a handle
-// invalidates a stream capture that another thread has in progress (measured on
-// GB300: a loop creating and destroying handles next to 200 thread-local
-// captures broke 45 of them; GEMM calls broke none), so the pool is made when the
-// first context of a device is created, before any of its marches can capture,
-// and lives as long as the process.
 namespace {
-constexpr int kBlasPool = 8;
-constexpr int kBlasDevices = 64;
-struct BlasPool {
-    std::mutex m;
-    std::condition_variable cv;
-    bool made = false;
-    int total = 0;
-    std::vector<cublasHandle_t> free_handles;
-};
-BlasPool& blas_pool(int dev) {
-    static BlasPool pools[kBlasDevices];
-    return pools[dev];
+
+// out[f][c][row] = sum_col Gf[f][row][col] K[c][col] for levels f < nlev: every
+// level of the FP32 store times the C columns of K (the batched march's known
+// tractions), in FP32 as an SGEMM per level.  A CTA takes 128 rows x 64 columns of
+// one level, 32-wide K chunks staged in shared memory (the level rows transposed),
+// 8 x 4 outputs per thread.
+constexpr int kLtcRows = 128, kLtcCols = 64, kLtcK = 32;
+
+__global__ void __launch_bounds__(256) k_levels_times_columns(const float* __restrict__ Gf,
+                                                              int ldf, int D,
+                                                              const float* __restrict__ K,
+                                                              int C, float* __restrict__ out) {
+    __shared__ __align__(16) float sG[kLtcK][kLtcRows + 4];
+    __shared__ __align__(16) float sK[kLtcK][kLtcCols + 4];
+    const int f = blockIdx.z;
+    const int r0 = blockIdx.x * kLtcRows, c0 = blockIdx.y * kLtcCols;
+    const float* G = Gf + (size_t)f * D * ldf;
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    float acc[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+    for (int k0 = 0; k0 < D; k0 += kLtcK) {
+#pragma unroll
+        for (int it = 0; it < kLtcRows * kLtcK / 256; it++) {
+            const int idx = tid + it * 256;
+            const int r = idx / kLtcK, k = idx % kLtcK;
+            const int row = r0 + r, col = k0 + k;
+            if (row < D && col < D) cp_async4(&sG[k][r], G + (size_t)row * ldf + col);
+            else sG[k][r] = 0.f;
+        }
+#pragma unroll
+        for (int it = 0; it < kLtcCols * kLtcK / 256; it++) {
+            const int idx = tid + it * 256;
+            const int c = idx / kLtcK, k = idx % kLtcK;
+            const int cc = c0 + c, col = k0 + k;
+            if (cc < C && col < D) cp_async4(&sK[k][c], K + (size_t)cc * D + col);
+            else sK[k][c] = 0.f;
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < kLtcK; k++) {
+            const float4 g0 = *reinterpret_cast<const float4*>(&sG[k][ty * 4]);
+            const float4 g1 = *reinterpret_cast<const float4*>(&sG[k][ty * 4 + 64]);
+            const float4 kv = *reinterpret_cast<const float4*>(&sK[k][tx * 4]);
+            const float ga[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+            const float kb[4] = {kv.x, kv.y, kv.z, kv.w};
+#pragma unroll
+            for (int a = 0; a < 8; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = fmaf(ga[a], kb[b], acc[a][b]);
+        }
+        __syncthreads();
+    }
+    float* o = out + (size_t)f * C * D;
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+        const int row = r0 + ty * 4 + (a & 3) + (a >> 2) * 64;
+        if (row >= D) continue;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int cc = c0 + tx * 4 + b;
+            if (cc < C) o[(size_t)cc * D + row] = acc[a][b];
+        }
+    }
 }
+
 }  // namespace
 
-void blas_pool_init(int dev) {
-    if (dev < 0 || dev >= kBlasDevices) return;
-    BlasPool& p = blas_pool(dev);
-    std::lock_guard<std::mutex> lk(p.m);
-    if (p.made) return;
-    p.made = true;
-    for (int i = 0; i < kBlasPool; i++) {
-        cublasHandle_t h = nullptr;
-        if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) break;
-        p.free_handles.push_back(h);
-        p.total++;
-    }
-}
-
-// wait: block until a handle is free (each user returns it once its work on the
-// stream has finished); otherwise nullptr when none is free.
-void* blas_checkout(int dev, bool wait) {
-    if (dev < 0 || dev >= kBlasDevices) return nullptr;
-    BlasPool& p = blas_pool(dev);
-    std::unique_lock<std::mutex> lk(p.m);
-    if (wait && p.total > 0) p.cv.wait(lk, [&] { return !p.free_handles.empty(); });
-    if (p.free_handles.empty()) return nullptr;
-    cublasHandle_t h = p.free_handles.back();
-    p.free_handles.pop_back();
-    return h;
-}
-
-void blas_return(int dev, void* h) {
-    if (!h || dev < 0 || dev >= kBlasDevices) return;
-    BlasPool& p = blas_pool(dev);
-    {
-        std::lock_guard<std::mutex> lk(p.m);
-        p.free_handles.push_back(static_cast<cublasHandle_t>(h));
-    }
-    p.cv.notify_one();
-}
-
 cudaError_t levels_times_columns(const float* Gf, int ldf, int D, int nlev, const float* K,
-                                 int C, float* out, int device, cudaStream_t s) {
-    // column-major views: out_f (D x C, ld D) = G_f (row-major, ld ldf: op T) K (D x C)
-    void* h = blas_checkout(device, true);
-    if (!h) return cudaErrorNotReady;  // no handle could be made on this device
-    cublasHandle_t hb = static_cast<cublasHandle_t>(h);
-    const float one = 1.f, zero = 0.f;
-    cublasStatus_t st = cublasSetStream(hb, s);
-    if (st == CUBLAS_STATUS_SUCCESS)
-        st = cublasSgemmStridedBatched(hb, CUBLAS_OP_T, CUBLAS_OP_N, D, C, D, &one, Gf, ldf,
-                                       (long long)D * ldf, K, D, 0, &zero, out, D,
-                                       (long long)C * D, nlev);
-    // the handle (and any workspace of its) goes back only after the products ran
-    const cudaError_t e = cudaStreamSynchronize(s);
-    blas_return(device, h);
+                                 int C, float* out, cudaStream_t s) {
+    if (nlev <= 0 || C <= 0) return cudaSuccess;
+    const dim3 grid((D + kLtcRows - 1) / kLtcRows, (C + kLtcCols - 1) / kLtcCols, nlev);
+    k_levels_times_columns<<<grid, 256, 0, s>>>(Gf, ldf, D, K, C, out);
+    return cudaGetLastError();
+}
+
+// The probe's relative residual max |A64 (X v) - v| / max |v| (max |v| = 6.5).
+cudaError_t probe_inverse(const double* A64, const float* X, int n, float* scratch, float* rel,
+                          long long* nlaunch, cudaStream_t s) {
+    // the probe's y (n doubles) and error word fit in the panel scratch rows
+    double* y = reinterpret_cast<double*>(scratch);
+    unsigned* err = reinterpret_cast<unsigned*>(y + n);
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
-    return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
+    const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+    k_probe_xv<<<g, 256, 0, s>>>(X, n, y);
+    k_probe_ay<<<g, 256, 0, s>>>(A64, n, y, err);
+    *nlaunch += 2;
+    unsigned bits = 0;
+    e = cudaMemcpyAsync(&bits, err, sizeof(bits), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    float ef;
+    std::memcpy(&ef, &bits, sizeof(ef));
+    *rel = ef / 6.5f;
+    return cudaSuccess;
 }
 
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
-                       void* blas) {
+                       InverseReport* report) {
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
     // first with the pivot search in the panels' diagonal blocks, then checked
     cudaError_t e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular,
-                                              s, true, blas);
+                                              s, true);
     if (e != cudaSuccess) return e;
-    bool good = false;
+    float rel = 3.0e38f;
     if (!*singular) {
-        // the probe's y (n doubles) and error word fit in the panel scratch rows
-        double* y = reinterpret_cast<double*>(scratch);
-        unsigned* err = reinterpret_cast<unsigned*>(y + n);
-        e = cudaMemsetAsync(err, 0, sizeof(unsigned), s);
+        e = probe_inverse(A64, A, n, scratch, &rel, nlaunch, s);
         if (e != cudaSuccess) return e;
-        const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
-        k_probe_xv<<<g, 256, 0, s>>>(A, n, y);
-        k_probe_ay<<<g, 256, 0, s>>>(A64, n, y, err);
-        *nlaunch += 2;
-        unsigned bits = 0;
-        e = cudaMemcpyAsync(&bits, err, sizeof(bits), cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) return e;
-        float ef;
-        std::memcpy(&ef, &bits, sizeof(ef));
-        good = ef <= 1e-2f * 6.5f;
     }
-    if (good) return cudaSuccess;
+    if (report) {
+        report->probe_rel = rel;
+        report->full_search = 0;
+    }
+    if (rel <= kInverseProbeBar) return cudaSuccess;
+    // a zero pivot in a diagonal block or a residual above the bar: the full search
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
-    return invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s, false,
-                                     blas);
+    e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s, false);
+    if (e != cudaSuccess || *singular || !report) return e;
+    report->full_search = 1;
+    return probe_inverse(A64, A, n, scratch, &report->probe_rel, nlaunch, s);
 }
 
 }  // namespace tdbem

@@ -7,22 +7,28 @@
 // the implicit device synchronisation of cudaMalloc / cudaFree is not
 // acceptable).  tdbem_gh_driver allocates a device staging buffer on every call;
 // this variant writes into device buffers the caller already owns and keeps the
-// per-call scratch of the kernels (pair windows, item counts and offsets, the
-// scan's temporaries, the C term) in one fixed-size array in device memory that
-// is part of the library image (kNoAllocScratchBytes; every GPU that loads the
-// library holds it until the process exits).
+// per-call scratch of the kernels (pair windows, the C term) in one fixed-size
+// array in device memory that is part of the library image (kNoAllocScratchBytes;
+// every GPU that loads the library holds it until the process exits).  The call
+// never waits for the device: a step has at most one item per (node, element)
+// pair, so the quadrature runs one thread per pair of a window pass
+// (k_assemble_step_pairs) instead of compacting the items with a scan whose total
+// the host would have to read back.
 //
 // Every call shares that array and it keeps the last call's contents; each call
-// overwrites what it reads (counts, offsets and the C term are recomputed,
-// outputs are zeroed first), but calls whose work overlaps on the GPU (other
-// streams, other host threads) race on it and must be serialised by the caller.
-// The first call on a device looks up the array's device address with that
-// device current; make that first call before any stream capture.
+// overwrites what it reads (windows and the C term are recomputed, outputs are
+// zeroed first), but calls whose work overlaps on the GPU (other streams, other
+// host threads) race on it and must be serialised by the caller.  The array's
+// device address is looked up with the context's device current on every call made
+// outside a stream capture (so a device reset that reloads the module is seen) and
+// taken from the last lookup during a capture; make the first call on a device
+// before any capture.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "tdbem_internal.cuh"
@@ -34,18 +40,24 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 8u << 20;  // 8 MiB
 constexpr size_t kMaxPairs = 1u << 18;             // pairs per launch chunk
 constexpr size_t kMaxNodes = 1u << 14;             // collocation nodes per chunk (C term)
-constexpr size_t kScanBytes = 64u << 10;           // scan temporaries
 constexpr int kMaxDevices = 64;
 
-// Layout: PairInfo[kMaxPairs] | counts[kMaxPairs] | offsets[kMaxPairs] |
-//         C term[kMaxNodes * 9] | scan temporaries.
+// Layout: PairInfo[kMaxPairs] | C term[kMaxNodes * 9].
 constexpr size_t kOffPairs = 0;
-constexpr size_t kOffCounts = kOffPairs + kMaxPairs * sizeof(PairInfo);
-constexpr size_t kOffOffsets = kOffCounts + kMaxPairs * sizeof(unsigned);
-constexpr size_t kOffCterm = kOffOffsets + kMaxPairs * sizeof(unsigned);
-constexpr size_t kOffScan = kOffCterm + kMaxNodes * 9 * sizeof(double);
-static_assert(kOffScan + kScanBytes <= kNoAllocScratchBytes, "scratch layout exceeds the array");
-static_assert(kOffCterm % 256 == 0 && kOffScan % 256 == 0, "scratch regions stay 256-byte aligned");
+constexpr size_t kOffCterm = kOffPairs + kMaxPairs * sizeof(PairInfo);
+static_assert(kOffCterm + kMaxNodes * 9 * sizeof(double) <= kNoAllocScratchBytes,
+              "scratch layout exceeds the array");
+static_assert(kOffCterm % 256 == 0, "scratch regions stay 256-byte aligned");
+
+// Per-launch chunk limits: the maxima above, or smaller ones from the environment
+// (TDBEM_NOALLOC_CHUNK_PAIRS / TDBEM_NOALLOC_CHUNK_NODES) so that a test can make a
+// small mesh run several chunks.
+size_t chunk_limit(const char* name, size_t max) {
+    const char* v = std::getenv(name);
+    if (!v || !*v) return max;
+    const long long n = std::atoll(v);
+    return n >= 1 ? std::min<size_t>((size_t)n, max) : max;
+}
 
 std::mutex g_mu;
 void* g_scratch[kMaxDevices] = {};
@@ -67,12 +79,20 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 
-// Device address of the scratch array on the current device, looked up once per
-// device with that device current.
-int scratch_address(int dev, unsigned char** out) {
+// Device address of the scratch array on the current device: looked up with that
+// device current whenever the stream is not being captured (a reset device may have
+// reloaded the module at another address), the last lookup otherwise.
+int scratch_address(int dev, cudaStream_t s, unsigned char** out) {
     if (dev < 0 || dev >= kMaxDevices) return nfail(TDBEM_ERR_UNSUPPORTED, "device %d", dev);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t ec = cudaStreamIsCapturing(s, &cap);
+    if (ec != cudaSuccess)
+        return nfail(TDBEM_ERR_CUDA, "cudaStreamIsCapturing: %s", cudaGetErrorString(ec));
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev]) {
+    if (!g_scratch[dev] && cap != cudaStreamCaptureStatusNone)
+        return nfail(TDBEM_ERR_STATE,
+                     "first allocation-free call on device %d made during a stream capture", dev);
+    if (cap == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
@@ -114,17 +134,14 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
                      "an element colour of %d elements exceeds the allocation-free maximum of "
                      "%zu pairs per launch (8 MiB scratch)",
                      max_color, kMaxPairs);
-    if (scan_temp_bytes((unsigned)kMaxPairs) > kScanBytes)
-        return nfail(TDBEM_ERR_UNSUPPORTED, "scan temporaries exceed the scratch reserve");
+    const size_t max_pairs = chunk_limit("TDBEM_NOALLOC_CHUNK_PAIRS", kMaxPairs);
+    const int max_nodes = (int)chunk_limit("TDBEM_NOALLOC_CHUNK_NODES", kMaxNodes);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
     unsigned char* base = nullptr;
-    const int rc0 = scratch_address(dev, &base);
+    const int rc0 = scratch_address(dev, s, &base);
     if (rc0 != TDBEM_OK) return rc0;
     PairInfo* pairs = reinterpret_cast<PairInfo*>(base + kOffPairs);
-    unsigned* counts = reinterpret_cast<unsigned*>(base + kOffCounts);
-    unsigned* offsets = reinterpret_cast<unsigned*>(base + kOffOffsets);
     double* cbuf = reinterpret_cast<double*>(base + kOffCterm);
-    void* scan_tmp = base + kOffScan;
-    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
 
     const int nn = node_hi - node_lo + 1;
     const size_t n = (size_t)3 * nn * c->D;
@@ -140,34 +157,26 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
     out.D = c->D;
     out.ld = c->D;
     out.row_node_lo = node_lo;
-    // Same window / scan / item sequence as tdbem_gh_driver, in node chunks that
-    // fit the fixed scratch.
+    // The pair windows of tdbem_gh_driver, colour by colour in node chunks that fit
+    // the fixed scratch, each followed by the uncompacted step kernel.
     for (size_t col = 0; col + 1 < c->color_start.size(); col++) {
         const int e0 = c->color_start[col], ne = c->color_start[col + 1] - e0;
         if (ne == 0) continue;
         const int* elems = c->d_color_elems + e0;
-        const int chunk = (int)std::max<size_t>(1, kMaxPairs / (size_t)ne);
+        const int chunk = (int)std::max<size_t>(1, max_pairs / (size_t)ne);
         for (int n0 = node_lo; n0 <= node_hi; n0 += chunk) {
             const int cn = std::min(chunk, node_hi - n0 + 1);
             const unsigned npairs = (unsigned)((size_t)cn * ne);
-            NA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, cn, c->ph, ASM_STEP,
-                                      step, 1 << 30, step, SEL_ALL, pairs, counts, s));
-            NA_TRY(exclusive_scan(counts, offsets, npairs, scan_tmp, kScanBytes, s));
-            unsigned last[2];
-            NA_TRY(cudaMemcpyAsync(&last[0], offsets + npairs - 1, sizeof(unsigned),
-                                   cudaMemcpyDeviceToHost, s));
-            NA_TRY(cudaMemcpyAsync(&last[1], counts + npairs - 1, sizeof(unsigned),
-                                   cudaMemcpyDeviceToHost, s));
-            NA_TRY(cudaStreamSynchronize(s));
-            NA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
-                                         c->d_gx, c->d_gw, c->d_geom, c->ph, ASM_STEP, step,
-                                         step, pairs, offsets, npairs, last[0] + last[1], out,
-                                         s));
+            NA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, cn, c->ph,
+                                      ASM_STEP, step, 1 << 30, step, SEL_ALL, pairs, nullptr, s));
+            NA_TRY(launch_assemble_step_pairs(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
+                                              c->d_gx, c->d_gw, c->d_geom, c->ph, step, pairs,
+                                              npairs, out, s));
         }
     }
     if (step == 1) {
-        for (int n0 = node_lo; n0 <= node_hi; n0 += (int)kMaxNodes) {
-            const int cn = std::min((int)kMaxNodes, node_hi - n0 + 1);
+        for (int n0 = node_lo; n0 <= node_hi; n0 += max_nodes) {
+            const int cn = std::min(max_nodes, node_hi - n0 + 1);
             NA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, n0, cn, c->nq, c->d_gx, c->d_gw,
                                 c->d_geom, c->ph, cbuf, s));
             AsmOut o2 = out;

@@ -80,6 +80,24 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
                                   cudaStream_t s);
+// Element interface: n independent (collocation point, element) pairs, element
+// node coordinates ecoords[n][ennd][3], time times[n], singular local node sing[n]
+// (-1: FormGH_Regular); GE1/HE1 (I part), GE2/HE2 (J part) [n][3][3 ennd] and C1 / C2
+// [n][9] (the Kelvin part when times[i] == ph.dt, zeros otherwise).
+cudaError_t launch_element_gh(int ennd, int n, int nq, const double* gx, const double* gw,
+                              const Phys& ph, const double* colloc, const double* ecoords,
+                              const double* times, const int* sing, double* GE1, double* GE2,
+                              double* HE1, double* HE2, double* C1, double* C2, cudaStream_t s);
+// Material and time-step constants of the kernels (GreenFunctionT::WaveSpeed,
+// GreenFunctionT.cpp:76-84).
+Phys make_phys(double E, double nu, double rho, double dt);
+// One step (ASM_STEP) over the pairs of a window pass without compaction: one thread
+// per pair (two for 8-node elements), no scan and no item total on the host.
+cudaError_t launch_assemble_step_pairs(const double* coords, const int* ien, int ennd,
+                                       const int* elems, int nelem_color, int node_lo, int nq,
+                                       const double* gx, const double* gw, const double* geom,
+                                       const Phys& ph, int step_n, const PairInfo* pairs,
+                                       unsigned npairs, const AsmOut& out, cudaStream_t s);
 // Far (well-separated) items of every node in FP32, ASM_LEVELS, into the FP32 store:
 // one launch over (node, chunk of levels) blocks, colours walked inside each block.
 // pairs holds nnd x nel windows (SEL_FAR), elements in colour order; *nitems (if
@@ -202,17 +220,17 @@ size_t inverse_scratch_elems(int n);
 // *singular is set (and cudaSuccess returned) when a pivot is exactly zero.
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
                        long long* nlaunch, bool* singular, cudaStream_t s);
-// blas: a cuBLAS handle (blas_checkout) for the trailing updates, or nullptr for
-// the built-in update kernel.
+// Outcome of an FP32 inverse: the probe's relative residual max |A (X v) - v| /
+// max |v| and whether the pivot search fell back from the panels' diagonal blocks
+// to the full panel (a zero pivot there, or a probe above kInverseProbeBar).
+struct InverseReport {
+    float probe_rel = 0;
+    int full_search = 0;
+};
+constexpr float kInverseProbeBar = 1e-5f;
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
-                       void* blas = nullptr);
-// The device's cuBLAS handle pool (made once, with the device's first context);
-// a handle is used by one thread at a time.  blas_checkout: nullptr when none is
-// free, or with wait, blocks until one is returned (nullptr if none could be made).
-void blas_pool_init(int dev);
-void* blas_checkout(int dev, bool wait = false);
-void blas_return(int dev, void* h);
+                       InverseReport* report = nullptr);
 cudaError_t launch_history_combine(const double* u_hist, const double* t_hist, int D, int s,
                                    int L, double a1, double a2, double a3, double c0,
                                    double c1, double amp, const double* load_t,
@@ -290,9 +308,9 @@ cudaError_t launch_known_batch(const float* GK, const float* GL, const double* H
                                double c1, const double* amp, int numstep, double* Y,
                                cudaStream_t st);
 // G^f K for levels f < nlev (FP32 levels, ld ldf) and the columns K [c][D]: out
-// [f][c][D] (cuBLAS strided-batched SGEMM with a pooled handle; inverse.cu).
+// [f][c][D], FP32 (k_levels_times_columns, inverse.cu).
 cudaError_t levels_times_columns(const float* Gf, int ldf, int D, int nlev, const float* K,
-                                 int C, float* out, int device, cudaStream_t s);
+                                 int C, float* out, cudaStream_t s);
 void known_coefficients(int numstep, int L, double a1, double a2, double a3,
                         const std::vector<double>& amp, double c0, double c1,
                         std::vector<double>& out);
@@ -439,6 +457,7 @@ struct tdbem_ctx {
     size_t tc_W_bytes = 0;
     int* d_tc_err = nullptr;        // tcgen05 kernel: [0] wait time-out code, [1] CTAs holding TMEM
     unsigned long long tc_wait_ns = tdbem::kTcWaitNsDefault;  // its pipeline wait limit
+    tdbem::InverseReport inv_report[2];  // probe and pivot search of the FP32 inverses
     tdbem::TcMaps tc_maps{};
     // mixed march: engine of the time blocks' old-history pass, its BF16 vector planes
     // and tensor maps (encoded for d_mtc_W and the level planes)

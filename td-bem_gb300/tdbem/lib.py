@@ -29,6 +29,10 @@ SIGNATURES = {
                                         ctypes.c_int, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     "tdbem_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tdbem_element_gh": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_int, _dp, _dp, _dp, _ip, _dp, _dp, _dp, _dp,
+                                        _dp, _dp]),
     "tdbem_max_step": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "tdbem_num_dof": (ctypes.c_int, [ctypes.c_void_p, _ip]),
     "tdbem_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
@@ -60,6 +64,8 @@ SIGNATURES = {
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_set_pipeline_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "tdbem_inverse_report": (ctypes.c_int, [ctypes.c_void_p, _dp, _ip]),
+    "tdbem_invert": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _ip]),
     "tdbem_set_march_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
                                             ctypes.c_int]),
@@ -158,6 +164,37 @@ def group_shape():
     a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _check(load().tdbem_group_shape(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
     return {"lanes": a.value, "block": b.value, "blocks_per_sm": c.value}
+
+
+def element_gh(etype: int, nq: int, E: float, nu: float, rho: float, t_1: float, colloc,
+               coords, t, singular):
+    """TDElementStepLinearT's element blocks of n (collocation point, element) pairs
+    in one launch (tdbem_element_gh).  colloc (n, 3), coords (n, ennd, 3), t (n,),
+    singular (n,) (-1: FormGH_Regular).  Returns GE_1, GE_2, HE_1, HE_2 of shape
+    (n, 3, 3 ennd) and C_1, C_2 of shape (n, 3, 3)."""
+    ennd = 4 if etype == 1 else 8
+    xc = np.ascontiguousarray(colloc, np.float64).reshape(-1, 3)
+    n = xc.shape[0]
+    en = np.ascontiguousarray(coords, np.float64).reshape(n, ennd, 3)
+    tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, np.float64), (n,)))
+    sg = np.ascontiguousarray(np.broadcast_to(np.asarray(singular, np.int32), (n,)))
+    outs = [np.empty((n, 3, 3 * ennd)) for _ in range(4)] + [np.empty((n, 3, 3)) for _ in range(2)]
+    _check(load().tdbem_element_gh(etype, nq, E, nu, rho, t_1, n, _d(xc), _d(en), _d(tt), _i(sg),
+                                   *[_d(o) for o in outs]))
+    return outs
+
+
+def invert(A, precision: int = FP64):
+    """X = A^-1 on the device (tdbem_invert): returns X, the FP32 inverse's probe
+    residual and whether its pivot search fell back to the full panel."""
+    a = np.ascontiguousarray(A, np.float64)
+    n = a.shape[0]
+    x = np.empty_like(a)
+    probe = ctypes.c_double()
+    full = ctypes.c_int()
+    _check(load().tdbem_invert(n, _d(a), precision, _d(x), ctypes.byref(probe),
+                               ctypes.byref(full)))
+    return x, probe.value, full.value
 
 
 def write_gh(prefix: str, step: int, data) -> None:
@@ -351,6 +388,13 @@ class Context:
     def set_pipeline_wait(self, seconds: float):
         """Limit of each pipeline wait of the tcgen05 convolution (0: the default, 2 s)."""
         _check(load().tdbem_set_pipeline_wait(self.h, seconds))
+
+    def inverse_report(self):
+        """(probe residuals, full-search flags) of the two FP32 inverses of the mixed march."""
+        p = (ctypes.c_double * 2)()
+        f = (ctypes.c_int * 2)()
+        _check(load().tdbem_inverse_report(self.h, p, f))
+        return list(p), list(f)
 
     def set_batch_options(self, engine: int = 0, refine_sweeps: int = 0):
         _check(load().tdbem_set_batch_options(self.h, engine, refine_sweeps))
