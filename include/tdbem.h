@@ -357,10 +357,14 @@ int tdbem_launch_count(const tdbem_ctx* ctx, long long* n);
 
 /* ---- serving: continuous batching of transient solves ---------------- */
 /* The reference runs one solve per process (main.cpp); it has no server.  The
- * server below accepts whole solves as they arrive, admits them by device
- * footprint into a fixed number of slots, and runs the admitted solves'
- * kernels concurrently, each on its own stream with its levels and histories
- * resident on the device until it completes. */
+ * server below accepts whole solves as they arrive and admits them by device
+ * footprint into a fixed number of slots.  A slot assembles its solve's levels
+ * and prepares its march on the solve's own stream; the time steps of all
+ * prepared solves are then batched: one march thread advances every resident
+ * solve by a time block of steps in ONE persistent launch (each solve at its own
+ * step), retires finished solves and lets newly prepared ones join at the next
+ * block boundary.  Levels and histories stay on the device until a solve
+ * completes; a result is bitwise the same served alone and in any mix. */
 
 /* Device bytes a solve needs: the level store (levels x D x D x bytes x 2)
  * plus the assembly and marching state of tdbem_assemble_levels + tdbem_march
@@ -411,6 +415,11 @@ int tdbem_server_result(tdbem_server* srv, long long id, double* u_hist, double*
                         double* times);
 int tdbem_server_stats(tdbem_server* srv, size_t* used_bytes, size_t* budget_bytes, int* active,
                        int* queued, long long* completed);
+/* The batched march so far: grouped launches (time blocks), solve-steps they
+ * advanced (each resident solve's steps summed) and the mean number of resident
+ * solves per launch. */
+int tdbem_server_march_stats(tdbem_server* srv, long long* launches, long long* solve_steps,
+                             double* mean_resident);
 /* Finish every queued and running request, then stop. */
 int tdbem_server_destroy(tdbem_server* srv);
 

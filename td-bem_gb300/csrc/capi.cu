@@ -201,6 +201,9 @@ void free_march(tdbem_ctx* c) {
     c->hist_steps = -1;
     dfree(c->d_upd_tmp);
     c->upd_tmp_cap = 0;
+    dfree(c->d_group_amp);
+    dfree(c->d_group_wf);
+    dfree(c->d_group_yold);
     free_batch(c);
 }
 
@@ -928,7 +931,10 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         // tcgen05 march: merged planes, history planes, known part and its coefficients
         b += tc_plane_bytes((int)D, (int)L, 1) + tc_w_bytes((int)D, 32, (int)L, 1) +
              3 * L * D * 8 + (numstep + 1) * (L * 3 + D) * 8 + 3 * D * 4;
+        // grouped march (the server's batched steps): FP32 time-block vectors
+        b += (2 + 2 * (size_t)kGroupNB) * L * ld * 4 + (size_t)kGroupNB * D * 8;
     }
+    b += (size_t)numstep * 8;  // the load history on the device
     *bytes = b;
     return TDBEM_OK;
 }

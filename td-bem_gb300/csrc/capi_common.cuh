@@ -168,6 +168,18 @@ int march_fp64(tdbem_ctx* c, int numstep, const double lhs_c[2][2], double* u_hi
                double* t_hist);
 int ensure_fp64_store(tdbem_ctx* c);
 
+// ---- grouped marching (capi_group.cu)
+
+// Per-mesh preparation of a grouped march of ns steps: boundary conditions, zeroed
+// histories, the LHS inverses (FP64, or the mixed form's FP32 pair), the load
+// history and the FP32 block scratch on the device (owned by the context), and the
+// mesh's GroupMarch entry with off = 0 (the list offsets are group_layout's).
+// Synchronises the context's stream.
+int group_prepare(tdbem_ctx* c, int ns, bool mixed, GroupMarch& g);
+// Row / W / quad / old-W list offsets of the meshes in order, and the totals.
+void group_layout(GroupMarch* gm, int n, unsigned* nrows, unsigned* nw, unsigned* nquads,
+                  unsigned* nwold);
+
 // Error of the tcgen05 convolution launches since d_tc_err was cleared (the stream
 // synchronised by the caller's copy): TDBEM_OK, or TDBEM_ERR_CUDA naming the wait
 // that ran out and the CTAs still holding TMEM.

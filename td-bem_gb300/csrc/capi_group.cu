@@ -27,6 +27,125 @@ int parallel_contexts(tdbem_ctx* const* ctxs, int n, F fn) {
 }
 }  // namespace
 
+namespace tdbem {
+namespace capi {
+
+int group_prepare(tdbem_ctx* c, int ns, bool mixed, GroupMarch& g) {
+    const int D = c->D;
+    int r = upload_bc(c);
+    if (r != TDBEM_OK) return r;
+    if (c->hist_steps != ns) {
+        dfree(c->d_u);
+        dfree(c->d_t);
+        CUDA_TRY(dalloc(&c->d_u, (size_t)(ns + 1) * D));
+        CUDA_TRY(dalloc(&c->d_t, (size_t)(ns + 1) * D));
+        c->hist_steps = ns;
+    }
+    CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (ns + 1) * D, c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (ns + 1) * D, c->stream));
+    const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
+    const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
+    if (mixed) {
+        if (!c->d_res) CUDA_TRY(dalloc(&c->d_res, D));
+        r = mixed_inverses(c, ns, lhs_c);
+        if (r != TDBEM_OK) return r;
+        // FP32 history vectors of the time blocks: new W (2 x (M+1) x ldf), old W
+        // (2 x (M+1) x kGroupNB x ldf), zeroed once (the padding columns ldf > D are
+        // read by 16-byte loads and never written), and Y_old (kGroupNB x D)
+        const size_t nwf = (size_t)(c->M + 1) * c->ldf, nwold = nwf * kGroupNB;
+        if (!c->d_group_wf) {
+            CUDA_TRY(dalloc(&c->d_group_wf, 2 * nwf + 2 * nwold));
+            CUDA_TRY(cudaMemsetAsync(c->d_group_wf, 0, sizeof(float) * (2 * nwf + 2 * nwold),
+                                     c->stream));
+            CUDA_TRY(dalloc(&c->d_group_yold, (size_t)kGroupNB * D));
+        }
+    } else {
+        const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
+        const int ninv = (ns >= 3 && !same) ? 2 : 1;
+        for (int v = 0; v < ninv; v++) {
+            r = fp64_inverse(c, v, lhs_c);
+            if (r != TDBEM_OK) return r;
+        }
+        if (ninv == 1) {
+            if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
+            c->d_Ainv[1] = c->d_Ainv[0];
+        }
+    }
+    dfree(c->d_group_amp);
+    if (!c->amp.empty()) {
+        CUDA_TRY(dalloc(&c->d_group_amp, (size_t)ns));
+        CUDA_TRY(cudaMemcpyAsync(c->d_group_amp, c->amp.data(), sizeof(double) * ns,
+                                 cudaMemcpyHostToDevice, c->stream));
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    g = GroupMarch{};
+    g.D = D;
+    g.M = c->M;
+    g.numstep = ns;
+    g.G = c->d_G;
+    g.H = c->d_H;
+    g.Ainv0 = c->d_Ainv[0];
+    g.Ainv1 = c->d_Ainv[1];
+    g.u = c->d_u;
+    g.t = c->d_t;
+    g.is_u = c->d_is_ubc;
+    g.is_f = c->d_is_fbc;
+    g.ubc = c->d_ubc_map;
+    g.fbc = c->d_fbc_map;
+    g.load_t = c->d_load_t;
+    g.load_u = c->d_load_u;
+    g.amp = c->d_group_amp;
+    g.a1 = a1;
+    g.a2 = a2;
+    g.a3 = a3;
+    g.c0 = lhs_c[1][0];
+    g.c1 = lhs_c[1][1];
+    g.Wt = c->d_Wt;
+    g.Wu = c->d_Wu;
+    g.rhs = c->d_rhs;
+    g.Gf = c->d_Gf;
+    g.Hf = c->d_Hf;
+    g.ldf = c->ldf;
+    g.inv32_0 = c->d_inv32[0];
+    g.inv32_1 = c->d_inv32[1];
+    g.Hc0 = c->d_Hc64[0];
+    g.Hc1 = c->d_Hc64[1];
+    g.x = c->d_x;
+    g.r = c->d_res;
+    g.refine = c->n_refine > 0 ? 1 : 0;
+    if (mixed) {
+        const size_t nwf = (size_t)(c->M + 1) * c->ldf, nwold = nwf * kGroupNB;
+        g.Wtf = c->d_group_wf;
+        g.Wuf = c->d_group_wf + nwf;
+        g.Wold_t = c->d_group_wf + 2 * nwf;
+        g.Wold_u = c->d_group_wf + 2 * nwf + nwold;
+        g.Yold = c->d_group_yold;
+    }
+    return TDBEM_OK;
+}
+
+void group_layout(GroupMarch* gm, int n, unsigned* nrows, unsigned* nw, unsigned* nquads,
+                  unsigned* nwold) {
+    unsigned r = 0, w = 0, q = 0, wo = 0;
+    for (int i = 0; i < n; i++) {
+        gm[i].row_begin = r;
+        gm[i].w_begin = w;
+        gm[i].quad_begin = q;
+        gm[i].wold_begin = wo;
+        r += (unsigned)gm[i].D;
+        w += (unsigned)((gm[i].M + 1) * gm[i].D);
+        q += (unsigned)((gm[i].D + 3) / 4);
+        wo += (unsigned)((gm[i].M + 1) * kGroupNB * gm[i].D);
+    }
+    *nrows = r;
+    *nw = w;
+    *nquads = q;
+    *nwold = wo;
+}
+
+}  // namespace capi
+}  // namespace tdbem
+
 extern "C" {
 
 int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int precision) {
@@ -217,141 +336,16 @@ int tdbem_march_group(tdbem_ctx* const* ctxs, int n, const int* numsteps, double
     const bool mixed = ctxs[0]->level_precision == TDBEM_MIXED;
     cudaStream_t s = ctxs[0]->stream;
     std::vector<GroupMarch> gm(n);
-    std::vector<double*> d_amp(n, nullptr);
-    struct FreeAmp {
-        std::vector<double*>& v;
-        ~FreeAmp() {
-            for (auto& p : v) dfree(p);
-        }
-    } amp_guard{d_amp};
-    unsigned nrows = 0, nw = 0;
     EventTimer tf;
     tf.start(s);
     // per mesh: boundary conditions, histories, inverses, load history -- on the
     // mesh's own stream from its own host thread, so the meshes overlap
     int rc = parallel_contexts(ctxs, n, [&](int i) -> int {
-        tdbem_ctx* c = ctxs[i];
-        const int D = c->D, ns = numsteps[i];
-        int r = upload_bc(c);
-        if (r != TDBEM_OK) return r;
-        if (c->hist_steps != ns) {
-            dfree(c->d_u);
-            dfree(c->d_t);
-            CUDA_TRY(dalloc(&c->d_u, (size_t)(ns + 1) * D));
-            CUDA_TRY(dalloc(&c->d_t, (size_t)(ns + 1) * D));
-            c->hist_steps = ns;
-        }
-        CUDA_TRY(cudaMemsetAsync(c->d_u, 0, sizeof(double) * (ns + 1) * D, c->stream));
-        CUDA_TRY(cudaMemsetAsync(c->d_t, 0, sizeof(double) * (ns + 1) * D, c->stream));
-        const double a1 = c->a1, a2 = c->a2, a3 = 1 - a1 - a2;
-        const double lhs_c[2][2] = {{1.0, 0.0}, {2 * a1 + a3, a1}};
-        if (mixed) {
-            if (!c->d_res) CUDA_TRY(dalloc(&c->d_res, D));
-            r = mixed_inverses(c, ns, lhs_c);
-            if (r != TDBEM_OK) return r;
-        } else {
-            const bool same = (lhs_c[1][0] == 1.0 && lhs_c[1][1] == 0.0);
-            const int ninv = (ns >= 3 && !same) ? 2 : 1;
-            for (int v = 0; v < ninv; v++) {
-                r = fp64_inverse(c, v, lhs_c);
-                if (r != TDBEM_OK) return r;
-            }
-            if (ninv == 1) {
-                if (c->d_Ainv[1] && c->d_Ainv[1] != c->d_Ainv[0]) dfree(c->d_Ainv[1]);
-                c->d_Ainv[1] = c->d_Ainv[0];
-            }
-        }
-        if (!c->amp.empty()) {
-            CUDA_TRY(dalloc(&d_amp[i], (size_t)ns));
-            CUDA_TRY(cudaMemcpyAsync(d_amp[i], c->amp.data(), sizeof(double) * ns,
-                                     cudaMemcpyHostToDevice, c->stream));
-        }
-        CUDA_TRY(cudaStreamSynchronize(c->stream));
-        GroupMarch& g = gm[i];
-        g = GroupMarch{};
-        g.D = D;
-        g.M = c->M;
-        g.numstep = ns;
-        g.G = c->d_G;
-        g.H = c->d_H;
-        g.Ainv0 = c->d_Ainv[0];
-        g.Ainv1 = c->d_Ainv[1];
-        g.u = c->d_u;
-        g.t = c->d_t;
-        g.is_u = c->d_is_ubc;
-        g.is_f = c->d_is_fbc;
-        g.ubc = c->d_ubc_map;
-        g.fbc = c->d_fbc_map;
-        g.load_t = c->d_load_t;
-        g.load_u = c->d_load_u;
-        g.amp = d_amp[i];
-        g.a1 = a1;
-        g.a2 = a2;
-        g.a3 = a3;
-        g.c0 = lhs_c[1][0];
-        g.c1 = lhs_c[1][1];
-        g.Wt = c->d_Wt;
-        g.Wu = c->d_Wu;
-        g.rhs = c->d_rhs;
-        g.Gf = c->d_Gf;
-        g.Hf = c->d_Hf;
-        g.ldf = c->ldf;
-        g.inv32_0 = c->d_inv32[0];
-        g.inv32_1 = c->d_inv32[1];
-        g.Hc0 = c->d_Hc64[0];
-        g.Hc1 = c->d_Hc64[1];
-        g.x = c->d_x;
-        g.r = c->d_res;
-        g.refine = c->n_refine > 0 ? 1 : 0;
-        return TDBEM_OK;
+        return group_prepare(ctxs[i], numsteps[i], mixed, gm[i]);
     });
     if (rc != TDBEM_OK) return rc;
-    unsigned nquads = 0, nwold = 0;
-    size_t nwf = 0, nwoldf = 0, nyold = 0;  // FP32 scratch (row stride ldf) and Y_old sizes
-    for (int i = 0; i < n; i++) {
-        const tdbem_ctx* c = ctxs[i];
-        gm[i].row_begin = nrows;
-        gm[i].w_begin = nw;
-        gm[i].quad_begin = nquads;
-        gm[i].wold_begin = nwold;
-        nrows += (unsigned)c->D;
-        nw += (unsigned)((c->M + 1) * c->D);
-        nquads += (unsigned)((c->D + 3) / 4);
-        nwold += (unsigned)((c->M + 1) * kGroupNB * c->D);
-        nwf += (size_t)(c->M + 1) * c->ldf;
-        nwoldf += (size_t)(c->M + 1) * kGroupNB * c->ldf;
-        nyold += (size_t)kGroupNB * c->D;
-    }
-    float* d_wf = nullptr;    // FP32 history vectors of every mesh (mixed)
-    double* d_yold = nullptr;
-    struct FreeWf {
-        float*& p;
-        double*& q;
-        ~FreeWf() {
-            dfree(p);
-            dfree(q);
-        }
-    } wf_guard{d_wf, d_yold};
-    if (mixed) {
-        // new-W (2 x nwf) and old-W (2 x nwoldf) planes, zeroed: the padding columns
-        // ldf > D are read by the 16-byte loads and must stay zero
-        const size_t tot = 2 * nwf + 2 * nwoldf;
-        CUDA_TRY(dalloc(&d_wf, tot));
-        CUDA_TRY(cudaMemsetAsync(d_wf, 0, sizeof(float) * tot, s));
-        CUDA_TRY(dalloc(&d_yold, nyold));
-        size_t ow = 0, oo = 0, oy = 0;
-        for (int i = 0; i < n; i++) {
-            const tdbem_ctx* c = ctxs[i];
-            gm[i].Wtf = d_wf + ow;
-            gm[i].Wuf = d_wf + nwf + ow;
-            gm[i].Wold_t = d_wf + 2 * nwf + oo;
-            gm[i].Wold_u = d_wf + 2 * nwf + nwoldf + oo;
-            gm[i].Yold = d_yold + oy;
-            ow += (size_t)(c->M + 1) * c->ldf;
-            oo += (size_t)(c->M + 1) * kGroupNB * c->ldf;
-            oy += (size_t)kGroupNB * c->D;
-        }
-    }
+    unsigned nrows = 0, nw = 0, nquads = 0, nwold = 0;
+    group_layout(gm.data(), n, &nrows, &nw, &nquads, &nwold);
     const double factor_ms = tf.stop_ms(s);
     GroupMarch* d_gm = nullptr;
     CUDA_TRY(dalloc(&d_gm, (size_t)n));

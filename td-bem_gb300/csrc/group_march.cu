@@ -136,12 +136,13 @@ __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restric
         // ---- A: combined history vectors (levels f <= L of each mesh)
         for (unsigned idx = tid; idx < nw; idx += nthreads) {
             const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WBegin{})];
-            if (st >= g.numstep) continue;
+            const int ls = st - g.off;  // the mesh's own step
+            if (ls < 1 || ls >= g.numstep) continue;
             const unsigned loc = idx - g.w_begin;
             const int f = (int)(loc / g.D), j = (int)(loc % g.D);
-            if (f > min(max(st, 1), g.M)) continue;
+            if (f > min(max(ls, 1), g.M)) continue;
             double wt, wu;
-            combine(g, st, f, j, 1, st, true, wt, wu);
+            combine(g, ls, f, j, 1, ls, true, wt, wu);
             g.Wt[loc] = wt;
             g.Wu[loc] = wu;
         }
@@ -150,11 +151,12 @@ __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restric
         for (unsigned base = warp_group0; base < nrows; base += ngroups) {
             const unsigned r = base + sub;
             const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
-            const bool live = g && st < g->numstep;
+            const int ls = g ? st - g->off : 0;
+            const bool live = g && ls >= 1 && ls < g->numstep;
             double acc = 0;
             if (live) {
                 const int row = (int)(r - g->row_begin), D = g->D;
-                const int L = min(max(st, 1), g->M);
+                const int L = min(max(ls, 1), g->M);
                 for (int f = 0; f <= L; f++) {
                     const double* Gr = g->G + ((size_t)f * D + row) * D;
                     const double* Hr = g->H + ((size_t)f * D + row) * D;
@@ -172,16 +174,17 @@ __global__ void __launch_bounds__(512) k_march_group(const GroupMarch* __restric
         for (unsigned base = warp_group0; base < nrows; base += ngroups) {
             const unsigned r = base + sub;
             const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
-            const bool live = g && st < g->numstep;
+            const int ls = g ? st - g->off : 0;
+            const bool live = g && ls >= 1 && ls < g->numstep;
             double acc = 0;
             int j = 0;
             if (live) {
                 j = (int)(r - g->row_begin);
-                const double* Ar = (st == 1 ? g->Ainv0 : g->Ainv1) + (size_t)j * g->D;
+                const double* Ar = (ls == 1 ? g->Ainv0 : g->Ainv1) + (size_t)j * g->D;
                 for (int k = lane; k < g->D; k += LANES) acc += Ar[k] * g->rhs[k];
             }
             acc = group_sum<LANES>(acc);
-            if (live && lane == 0) update_dof(*g, st, j, acc);
+            if (live && lane == 0) update_dof(*g, ls, j, acc);
         }
         grid.sync();
     }
@@ -192,7 +195,7 @@ template <int LANES>
 __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __restrict__ gm,
                                                         int nmesh, unsigned nrows, unsigned nw,
                                                         unsigned nquads, unsigned nwold,
-                                                        int st_lo, int st_hi) {
+                                                        int st_lo, int st_hi, int has_offsets) {
     constexpr int NB = kGroupNB, RQ = 4;
     cg::grid_group grid = cg::this_grid();
     const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,19 +205,22 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
     const unsigned warp_group0 = (tid / 32) * (32 / LANES);
     const unsigned sub = (threadIdx.x % 32) / LANES;
     for (int S = st_lo; S < st_hi; S += NB) {
-        if (S > 1) {
-            // ---- old-history vectors of the block: W_f^old[:, j], s = S + j, m < S
+        // meshes join at block starts: a mesh's own block start lS = S - off is 1 or a
+        // later block start of its march
+        if (S > 1 || has_offsets) {
+            // ---- old-history vectors of the block: W_f^old[:, j], s = lS + j, m < lS
             for (unsigned idx = tid; idx < nwold; idx += nthreads) {
                 const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WoldBegin{})];
-                if (S >= g.numstep) continue;
+                const int lS = S - g.off;
+                if (lS <= 1 || lS >= g.numstep) continue;
                 const unsigned loc = idx - g.wold_begin;
                 const int k = (int)(loc % g.D);
                 const int j = (int)((loc / g.D) % NB);
                 const int f = (int)(loc / ((unsigned)g.D * NB));
-                const int nbe = min(NB, g.numstep - S);
-                if (f > min(g.M, S + nbe - 1)) continue;
+                const int nbe = min(NB, g.numstep - lS);
+                if (f > min(g.M, lS + nbe - 1)) continue;
                 double wt, wu;
-                combine(g, S + j, f, k, 1, S, false, wt, wu);
+                combine(g, lS + j, f, k, 1, lS, false, wt, wu);
                 const size_t o = ((size_t)f * NB + j) * g.ldf + k;
                 g.Wold_t[o] = (float)wt;
                 g.Wold_u[o] = (float)wu;
@@ -225,7 +231,8 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                 const unsigned q = base + sub;
                 const GroupMarch* g =
                     q < nquads ? &gm[mesh_of(gm, nmesh, q, QuadBegin{})] : nullptr;
-                const bool live = g && S < g->numstep;
+                const int lS = g ? S - g->off : 0;
+                const bool live = g && lS > 1 && lS < g->numstep;
                 float acc[RQ][NB];
 #pragma unroll
                 for (int r = 0; r < RQ; r++)
@@ -235,8 +242,8 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                 if (live) {
                     const int D = g->D, ld4 = g->ldf / 4;
                     row0 = (int)(q - g->quad_begin) * RQ;
-                    const int nbe = min(NB, g->numstep - S);
-                    const int nlev = min(g->M, S + nbe - 1) + 1;
+                    const int nbe = min(NB, g->numstep - lS);
+                    const int nlev = min(g->M, lS + nbe - 1) + 1;
                     size_t rowoff[RQ];
 #pragma unroll
                     for (int r = 0; r < RQ; r++) rowoff[r] = (size_t)min(row0 + r, D - 1) * ld4;
@@ -283,12 +290,13 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
             // ---- new-history vectors: m >= S, and the known loads, levels f <= s - S + 1
             for (unsigned idx = tid; idx < nw; idx += nthreads) {
                 const GroupMarch& g = gm[mesh_of(gm, nmesh, idx, WBegin{})];
-                if (st >= g.numstep) continue;
+                const int ls = st - g.off, lS = S - g.off;
+                if (ls < 1 || ls >= g.numstep) continue;
                 const unsigned loc = idx - g.w_begin;
                 const int f = (int)(loc / g.D), k = (int)(loc % g.D);
                 if (f > min(g.M, max(1, st + 1 - S))) continue;
                 double wt, wu;
-                combine(g, st, f, k, S, st, true, wt, wu);
+                combine(g, ls, f, k, lS, ls, true, wt, wu);
                 g.Wtf[(size_t)f * g.ldf + k] = (float)wt;
                 g.Wuf[(size_t)f * g.ldf + k] = (float)wu;
             }
@@ -297,7 +305,8 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
             for (unsigned base = warp_group0; base < nrows; base += ngroups) {
                 const unsigned r = base + sub;
                 const GroupMarch* g = r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
-                const bool live = g && st < g->numstep;
+                const int ls = g ? st - g->off : 0, lS = g ? S - g->off : 0;
+                const bool live = g && ls >= 1 && ls < g->numstep;
                 double acc = 0;
                 int row = 0;
                 if (live) {
@@ -319,7 +328,7 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                 }
                 acc = group_sum<LANES>(acc);
                 if (live && lane == 0)
-                    g->rhs[row] = acc + (S > 1 ? g->Yold[(size_t)jb * g->D + row] : 0.0);
+                    g->rhs[row] = acc + (lS > 1 ? g->Yold[(size_t)jb * g->D + row] : 0.0);
             }
             grid.sync();
             // ---- x0 = inv32 rhs | r = rhs - A64 x0 | x = x0 + inv32 r, state update
@@ -328,17 +337,19 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                     const unsigned r = base + sub;
                     const GroupMarch* g =
                         r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
-                    const bool live = g && st < g->numstep && (sweep == 0 || g->refine > 0);
+                    const int ls = g ? st - g->off : 0;
+                    const bool live =
+                        g && ls >= 1 && ls < g->numstep && (sweep == 0 || g->refine > 0);
                     double acc = 0;
                     int j = 0;
                     if (live) {
                         j = (int)(r - g->row_begin);
                         const int D = g->D;
                         if (sweep == 1) {
-                            const double* Ar = (st == 1 ? g->Hc0 : g->Hc1) + (size_t)j * D;
+                            const double* Ar = (ls == 1 ? g->Hc0 : g->Hc1) + (size_t)j * D;
                             for (int k = lane; k < D; k += LANES) acc += Ar[k] * g->x[k];
                         } else {
-                            const float* Ar = (st == 1 ? g->inv32_0 : g->inv32_1) + (size_t)j * D;
+                            const float* Ar = (ls == 1 ? g->inv32_0 : g->inv32_1) + (size_t)j * D;
                             const double* v = sweep == 0 ? g->rhs : g->r;
                             float a32 = 0.f;
                             for (int k = lane; k < D; k += LANES) a32 += Ar[k] * (float)v[k];
@@ -349,11 +360,11 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                     if (live && lane == 0) {
                         if (sweep == 0) {
                             g->x[j] = acc;
-                            if (g->refine == 0) update_dof(*g, st, j, acc);
+                            if (g->refine == 0) update_dof(*g, ls, j, acc);
                         } else if (sweep == 1) {
                             g->r[j] = g->rhs[j] - acc;
                         } else {
-                            update_dof(*g, st, j, g->x[j] + acc);
+                            update_dof(*g, ls, j, g->x[j] + acc);
                         }
                     }
                 }
@@ -366,7 +377,7 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
 template <int LANES>
 cudaError_t launch_lanes(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
                          unsigned nquads, unsigned nwold, int st_lo, int st_hi, int block,
-                         int blocks_per_sm, bool mixed, cudaStream_t s) {
+                         int blocks_per_sm, bool mixed, int has_offsets, cudaStream_t s) {
     int dev = 0, nsm = 0, occ = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -378,7 +389,8 @@ cudaError_t launch_lanes(const GroupMarch* gm, int nmesh, unsigned nrows, unsign
     const int grid = nsm * std::min(occ, blocks_per_sm);  // every block resident: grid.sync is safe
     if (mixed) {
         void* args[] = {(void*)&gm,     (void*)&nmesh, (void*)&nrows, (void*)&nw,
-                        (void*)&nquads, (void*)&nwold, (void*)&st_lo, (void*)&st_hi};
+                        (void*)&nquads, (void*)&nwold, (void*)&st_lo, (void*)&st_hi,
+                        (void*)&has_offsets};
         return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, 0, s);
     }
     void* args[] = {(void*)&gm, (void*)&nmesh, (void*)&nrows, (void*)&nw, (void*)&st_lo,
@@ -390,19 +402,20 @@ cudaError_t launch_lanes(const GroupMarch* gm, int nmesh, unsigned nrows, unsign
 
 cudaError_t launch_march_group(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
                                unsigned nquads, unsigned nwold, int st_lo, int st_hi,
-                               const GroupShape& shape, bool mixed, cudaStream_t s) {
+                               const GroupShape& shape, bool mixed, cudaStream_t s,
+                               bool has_offsets) {
     if (shape.block < 32 || shape.block > 512 || shape.block % 32 || shape.blocks_per_sm < 1)
         return cudaErrorInvalidValue;
     switch (shape.lanes) {
     case 8:
         return launch_lanes<8>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
-                               shape.blocks_per_sm, mixed, s);
+                               shape.blocks_per_sm, mixed, has_offsets ? 1 : 0, s);
     case 16:
         return launch_lanes<16>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
-                                shape.blocks_per_sm, mixed, s);
+                                shape.blocks_per_sm, mixed, has_offsets ? 1 : 0, s);
     case 32:
         return launch_lanes<32>(gm, nmesh, nrows, nw, nquads, nwold, st_lo, st_hi, shape.block,
-                                shape.blocks_per_sm, mixed, s);
+                                shape.blocks_per_sm, mixed, has_offsets ? 1 : 0, s);
     default:
         return cudaErrorInvalidValue;
     }

@@ -148,6 +148,7 @@ cudaError_t launch_cterm_group(const GroupAsm* gm, int nmesh, unsigned nnodes, c
 // One mesh of a persistent grouped march (group_march.cu): FP64 levels and inverses.
 struct GroupMarch {
     int D, M, numstep;
+    int off;               // the mesh's step s runs at the launch's global step s + off
     const double* G;       // (M+1) x D x D
     const double* H;
     const double* Ainv0;   // inverse of step 2's LHS
@@ -194,9 +195,13 @@ struct GroupShape {
     int blocks_per_sm;     // at most the occupancy limit
 };
 // nquads / nwold: 4-row blocks and old-W entries of all meshes (mixed form only).
+// st_lo..st_hi: global steps; mesh i runs its own steps st - gm[i].off (only those
+// in 1..numstep-1).  has_offsets: some mesh has off != 0 (they join at block starts
+// of the mixed form's time blocks: off is a multiple of kGroupNB).
 cudaError_t launch_march_group(const GroupMarch* gm, int nmesh, unsigned nrows, unsigned nw,
                                unsigned nquads, unsigned nwold, int st_lo, int st_hi,
-                               const GroupShape& shape, bool mixed, cudaStream_t s);
+                               const GroupShape& shape, bool mixed, cudaStream_t s,
+                               bool has_offsets = false);
 cudaError_t exclusive_scan(const unsigned* in, unsigned* out, unsigned n, void* tmp,
                            size_t tmp_bytes, cudaStream_t s);
 
@@ -458,6 +463,10 @@ struct tdbem_ctx {
     int* d_tc_err = nullptr;        // tcgen05 kernel: [0] wait time-out code, [1] CTAs holding TMEM
     unsigned long long tc_wait_ns = tdbem::kTcWaitNsDefault;  // its pipeline wait limit
     tdbem::InverseReport inv_report[2];  // probe and pivot search of the FP32 inverses
+    // grouped marching: the load history on the device, the FP32 time-block scratch
+    double* d_group_amp = nullptr;
+    float* d_group_wf = nullptr;
+    double* d_group_yold = nullptr;
     tdbem::TcMaps tc_maps{};
     // mixed march: engine of the time blocks' old-history pass, its BF16 vector planes
     // and tensor maps (encoded for d_mtc_W and the level planes)

@@ -93,6 +93,9 @@ SIGNATURES = {
     "tdbem_server_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t),
                                           ctypes.POINTER(ctypes.c_size_t), _ip, _ip,
                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "tdbem_server_march_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                                 ctypes.POINTER(ctypes.c_longlong),
+                                                 ctypes.POINTER(ctypes.c_double)]),
     "tdbem_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tdbem_mrt_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _ip, _ip, ctypes.c_int,
                                         ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
@@ -266,6 +269,13 @@ class Server:
                                          ctypes.byref(act), ctypes.byref(q), ctypes.byref(done)))
         return {"used_bytes": used.value, "budget_bytes": budget.value, "active": act.value,
                 "queued": q.value, "completed": done.value}
+
+    def march_stats(self):
+        """Grouped march launches, solve-steps they advanced, mean resident solves."""
+        n, st, mr = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_double()
+        _check(load().tdbem_server_march_stats(self.h, ctypes.byref(n), ctypes.byref(st),
+                                               ctypes.byref(mr)))
+        return {"launches": n.value, "solve_steps": st.value, "mean_resident": mr.value}
 
     def close(self):
         if self.h:

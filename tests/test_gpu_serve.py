@@ -1,10 +1,17 @@
 """Serving (tdbem_server_*): continuous batching of transient solves.
 
-Each result must be the same alone and in the mix: the histories of a request
-served among others equal, bitwise, those of the same solve run alone through
-tdbem_march (the kernels are deterministic and contexts share no device data).
+The server batches the time steps of its resident solves: every prepared solve
+advances by a time block in one grouped launch, each at its own step, and solves
+join and leave at block boundaries.  Each result must be the same alone and in
+the mix: the histories of a request served among others equal, bitwise, those
+of the same request served alone (the grouped kernels reduce each row in a fixed
+order whatever else is resident).  They also match the solve run alone through
+tdbem_march: FP64 at 1e-10 per step (max-norm relative, another summation
+order), the mixed form at 1e-4 relative L2 (the server marches FP32 levels on
+the CUDA cores, tdbem_march split-BF16 products on the tensor cores).
 Admission keeps the resident footprint within the budget; a failing request
-fails alone."""
+fails alone; with requests arriving while others march, grouped launches carry
+several solves at once."""
 import copy
 import threading
 import time
@@ -50,19 +57,52 @@ def alone(lib, m, amp, precision):
         return ctx.march()
 
 
+def served(lib, reqs, prec, slots=4):
+    with lib.Server(0, 0, slots=slots) as srv:
+        ids = [srv.submit(m, amp=a, precision=prec) for m, a in reqs]
+        out = []
+        for rid in ids:
+            assert srv.wait(rid) == lib.REQ_DONE
+            out.append(srv.result(rid))
+        stats = srv.march_stats()
+    return out, stats
+
+
+def rel_step_max(u, ur):
+    return max((np.abs(u[s] - ur[s]).max() / np.abs(ur[s]).max()) if np.abs(ur[s]).max() else
+               np.abs(u[s]).max() for s in range(ur.shape[0]))
+
+
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_results_same_alone_and_in_mix(tdlib, mix, precision):
     prec = tdlib.MIXED if precision == "mixed" else tdlib.FP64
-    ref = [alone(tdlib, m, a, prec) for m, a in mix]
-    with tdlib.Server(0, 0, slots=4) as srv:
-        ids = [srv.submit(m, amp=a, precision=prec) for m, a in mix]
-        out = []
-        for rid in ids:
-            assert srv.wait(rid) == tdlib.REQ_DONE
-            out.append(srv.result(rid))
-    for (u, t), (us, ts, times) in zip(ref, out):
-        assert np.array_equal(u, us) and np.array_equal(t, ts)
+    solo = [served(tdlib, [(m, a)], prec, slots=1)[0][0] for m, a in mix]
+    out, stats = served(tdlib, mix, prec)
+    assert stats["launches"] > 0 and stats["solve_steps"] > 0
+    for (u1, t1, _), (us, ts, times), (m, a) in zip(solo, out, mix):
+        assert np.array_equal(u1, us) and np.array_equal(t1, ts)
         assert times["latency_s"] >= times["run_s"] > 0 and times["queued_s"] >= 0
+        u, t = alone(tdlib, m, a, prec)
+        if prec == tdlib.FP64:
+            assert rel_step_max(us, u) <= 1e-10 and rel_step_max(ts, t) <= 1e-10
+        else:
+            assert np.linalg.norm(us - u) / np.linalg.norm(u) <= 1e-4
+
+
+def test_co_resident_steps_share_launches(tdlib):
+    """Six solves of 300 steps submitted together: their marches overlap, so the
+    grouped launches carry more than one resident solve on average and there are
+    fewer launches than the solves' time blocks."""
+    from tdbem import meshes
+    reqs = [(meshes.cubed_sphere(n, numstep=300), None) for n in (4, 5, 6, 6)]
+    reqs += [(meshes.bar(1, 1, L, per_unit=2, numstep=300), None) for L in (3, 5)]
+    out, stats = served(tdlib, reqs, tdlib.MIXED, slots=6)
+    assert len(out) == 6
+    blocks = sum(-(-(m.numstep - 1) // 12) for m, _ in reqs)
+    print(f"launches {stats['launches']}, solve blocks {blocks}, "
+          f"mean resident {stats['mean_resident']:.2f}")
+    assert stats["mean_resident"] > 1.5
+    assert stats["launches"] < blocks
 
 
 def test_admission_keeps_within_budget(tdlib, mix):
@@ -108,7 +148,9 @@ def test_failing_request_fails_alone(tdlib, mix):
         assert ei.value.code == -1 and "out of range" in str(ei.value)
         assert srv.wait(r_ok) == tdlib.REQ_DONE
         u, _, _ = srv.result(r_ok)
-    assert np.array_equal(u, u_ref)
+    (u_solo, _, _), = served(tdlib, [(m, a)], tdlib.MIXED, slots=1)[0]
+    assert np.array_equal(u, u_solo)
+    assert np.linalg.norm(u - u_ref) / np.linalg.norm(u_ref) <= 1e-4
 
 
 def test_request_larger_than_budget_is_refused(tdlib, mix):
