@@ -61,6 +61,17 @@ def group_models(count, numstep, seed=0):
 METRIC = "DOF*steps/s"
 
 
+def workload_config(name, model, M, world):
+    """The workload's identity, the same in both arms (method details go elsewhere)."""
+    cases = WORKLOADS[name].get("cases", 0)
+    D = model.ndof
+    fp64_gb = 2 * (M + 1) * D * D * 8 / 1e9
+    return {"workload": name, "dof": D, "steps": model.numstep, "max_step": M,
+            "alpha": list(ALPHA), "load_cases": max(1, cases), "parallelism": f"replicas{world}",
+            "l2": f"inputs larger than L2: the FP64 level store is {fp64_gb:.1f} GB "
+                  "(the mixed form's FP32 store and merged BF16 planes: 3/4 of it)"}
+
+
 def make_model(name):
     from tdbem import meshes
     w = WORKLOADS[name]
@@ -264,6 +275,10 @@ def cpu_sample(model, M, numstep, a1, a2, nthreads, cases=0):
     total = t_asm + nc * t_march + t_lu
     return {"seconds": total, "assembly_s": t_asm, "march_s": nc * t_march, "lu_s": t_lu,
             "value": nc * D * numstep / total,
+            "sample_fractions": {"assembly_rows": R / model.nnd, "assembly_levels": 1.0 / M,
+                                 "march": "4 short marches on 2- and 5-level stores at full D "
+                                          "(per-term cost fitted, not the workload's levels)",
+                                 "lu_size": 2000.0 / D},
             "sample": (f"G_H_Driver on {R} of {model.nnd} rows at one step scaled to all rows "
                        f"x {M} steps; Solve_Averaging steps at D={D} on synthetic {m_a}- and "
                        f"{m_b}-level stores fitted to c0+c1*terms and summed over {numstep} "
@@ -292,11 +307,12 @@ def run_reference(args, dist):
             "ms_per_step": 1000.0 * max(1, cases) * model.ndof * model.numstep / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": args.workload, "dof": model.ndof, "steps": model.numstep,
-                       "max_step": M, "alpha": list(ALPHA), "precision": "fp64",
-                       "load_cases": max(1, cases)},
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
-                             "sample": last["sample"]},
+            "config": workload_config(args.workload, model, M, args.gpus),
+            "method": {"precision": "fp64", "solver": "the oracle port of the reference's "
+                       "G_H_Driver, Solve_Averaging and dense LU, on the host cores"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads,
+                             "kind": "port, extrapolated", "sample": last["sample"],
+                             "sample_fractions": last["sample_fractions"]},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "estimate_seconds": {k: last[k] for k in ("assembly_s", "march_s", "lu_s")}}
@@ -523,15 +539,17 @@ def run_ours(args, dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == lib.FP64 else "f32+f64", "data": "synthetic",
-            "config": {"workload": args.workload, "dof": D, "steps": nsteps, "max_step": M,
-                       "alpha": list(ALPHA), "precision": args.precision,
-                       "parallelism": f"replicas{dist.world}", "load_cases": nc,
-                       "refine_sweeps": refine,
+            "config": workload_config(args.workload, model, M, dist.world),
+            "method": {"precision": args.precision, "refine_sweeps": refine,
                        "block_steps": args.block or (32 if args.march_engine == "tcgen05" else 8),
                        "march_engine": args.march_engine if prec == lib.MIXED else None,
                        "batch_engine": args.engine if cases else None,
-                       "l2": "inputs larger than L2: the level store is "
-                             f"{level_gb:.1f} GB"},
+                       "level_store_gb": round(level_gb, 2),
+                       "parity": "plain FP64 form: 1e-10 per level and per step against the "
+                                 "oracle in exact-zero mode (the step response of a point both "
+                                 "wave fronts have passed is exactly 0); against the "
+                                 "reference's raw outputs 1e-10 plus twice their round-off "
+                                 "floor (up to ~6e-8 of a level's max-norm)"},
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -548,12 +566,15 @@ def run_ours(args, dist):
         line["vs_plain_fp64"] = compare
     if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_batched:
         line["batched"] = run_batched(lib, torch, args)
+    if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_precision_config:
+        line["precision_config"] = run_precision_config(lib, torch, args, peaks, peak_kind)
     if args.serve_requests > 0:
         line["serve"] = run_serve(lib, args, dev)
     if dist.world == 1 and not args.no_cpu_baseline:
         r = cpu_sample(model, M, nsteps, *ALPHA, os.cpu_count() or 1, cases)
         line["cpu_baseline"] = {"value": r["value"], "unit": METRIC, "cores": os.cpu_count(),
-                                "kind": "port", "sample": r["sample"]}
+                                "kind": "port, extrapolated", "sample": r["sample"],
+                                "sample_fractions": r["sample_fractions"]}
     print(json.dumps(line))
     return 0
 
@@ -602,6 +623,76 @@ def run_batched(lib, torch, args, workload="sphere_6x16x16_batch64"):
     if not args.no_compare:
         out["vs_plain_fp64"] = compare_batch(lib, torch, ctx, model, trac, amp, ms)
     ctx.close()
+    return out
+
+
+def run_precision_config(lib, torch, args, peaks, peak_kind, workload="sphere_6x24x24"):
+    """The precision configuration: the 6x24x24 cubed-sphere cavity (10374 DOF, 500
+    steps, 91 levels) in the mixed form, timed like the headline (W warm-up and K
+    timed solves between CUDA events), its dominant kernel's roofline, and its error
+    against the plain FP64 form of the same solve (the FP64 level store, 157 GB, is
+    made after the mixed context is released)."""
+    model = make_model(workload)
+    D, n = model.ndof, model.numstep
+    ctx = lib.Context(model)
+    ctx.set_alpha(*ALPHA)
+    M = ctx.M
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def job():
+        ctx.assemble(precision=lib.MIXED)
+        ctx.march(to_host=False)
+
+    for _ in range(args.warmup):
+        job()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        job()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    ctx.set_profiling(True)
+    job()
+    stats = ctx.kernel_stats()
+    ctx.set_profiling(False)
+    phases = ctx.timings()
+    far = stats["assemble_f32"]
+    tf = far["flops"] / max(1e-9, far["ms"] / 1e3) / 1e12
+    out = {"workload": workload, "value": D * n / (ms / 1e3), "unit": METRIC, "ms_per_step": ms,
+           "config": workload_config(workload, model, M, 1), "phases_ms": phases,
+           "roofline": {"bound": "fp32", "kernel": "k_assemble_far_rows", "achieved": tf,
+                        "peak": peaks.get("fp32_tflops"), "unit": "TFLOP/s",
+                        "frac": tf / peaks["fp32_tflops"] if peaks.get("fp32_tflops") else None,
+                        "launches": far["launches"],
+                        "share": far["ms"] / max(1e-9, sum(v["ms"] for v in stats.values())),
+                        "peak_source": "fp32_tflops: cuBLAS GEMM measured in this run"},
+           "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3)}
+                       for k, v in stats.items() if v["launches"]}}
+    if not args.no_compare:
+        u32, t32 = ctx.march()
+        ctx.close()
+        with lib.Context(model) as c64:
+            c64.set_alpha(*ALPHA)
+            s64 = torch.cuda.ExternalStream(c64.stream)
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(s64)
+            c64.assemble(precision=lib.FP64)
+            u64, t64 = c64.march()
+            a1.record(s64)
+            a1.synchronize()
+            ms64 = a0.elapsed_time(a1)
+        out["vs_plain_fp64"] = {
+            "plain_fp64_value": D * n / (ms64 / 1e3), "plain_fp64_ms_per_step": ms64,
+            "speedup_vs_plain_fp64": ms64 / ms,
+            "u_rel_l2_err": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+            "t_rel_l2_err": float(np.linalg.norm(t32 - t64) / max(1e-300, np.linalg.norm(t64))),
+            "note": "the cavity's tractions are all prescribed, so t matches exactly"}
+    else:
+        ctx.close()
     return out
 
 
@@ -700,24 +791,39 @@ def run_group(lib, torch, args, dist):
 
 
 def run_serve(lib, args, dev):
-    """Seeded Poisson stream of mixed transient solves through the server
-    (continuous batching, admission by HBM footprint): latency percentiles and
-    throughput.  Not part of the timed region of the headline number."""
+    """Seeded Poisson streams of mixed transient solves through the server
+    (continuous batching: slots assemble, one grouped launch per time block advances
+    every resident solve; admission by HBM footprint) at several arrival rates:
+    latency percentiles, throughput and how many solves each grouped launch carried.
+    Not part of the timed region of the headline number."""
     from tdbem import serve
-    reqs = serve.request_mix(args.serve_requests, args.serve_rate, seed=0)
-    with lib.Server(dev, 0, slots=args.serve_slots) as srv:
-        res = serve.run_stream(srv, reqs, alpha=ALPHA)
-    mix = {}
-    for r in res["records"]:
-        k = r["name"].split("_")[0]
-        mix[k] = mix.get(k, 0) + 1
-    return {"requests": len(reqs), "rate_hz": args.serve_rate, "slots": args.serve_slots,
-            "precision": "mixed", "p50_s": res["p50_s"], "p99_s": res["p99_s"],
-            "mean_queued_s": res["mean_queued_s"], "wall_s": res["wall_s"],
-            "dof_steps_per_s": res["dof_steps_per_s"], "mix": mix,
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    curves = []
+    for i, rate in enumerate(rates):
+        reqs = serve.request_mix(args.serve_requests, rate, seed=i)
+        with lib.Server(dev, 0, slots=args.serve_slots) as srv:
+            res = serve.run_stream(srv, reqs, alpha=ALPHA)
+            ms = srv.march_stats()
+        mix = {}
+        for r in res["records"]:
+            k = r["name"].split("_")[0]
+            mix[k] = mix.get(k, 0) + 1
+        done_hz = len(reqs) / res["wall_s"]
+        curves.append({
+            "rate_hz": rate, "requests": len(reqs), "p50_s": res["p50_s"],
+            "p99_s": res["p99_s"], "mean_queued_s": res["mean_queued_s"],
+            "wall_s": res["wall_s"], "completed_per_s": done_hz,
+            "saturated": done_hz < 0.9 * rate,
+            "dof_steps_per_s": res["dof_steps_per_s"],
+            "grouped_launches": ms["launches"], "solve_steps": ms["solve_steps"],
+            "mean_resident_per_launch": ms["mean_resident"],
+            "launches_per_solve_step": ms["launches"] / max(1, ms["solve_steps"]),
+            "mix": mix,
             "dof_range": [min(r["dof"] for r in reqs), max(r["dof"] for r in reqs)],
             "steps_range": [min(r["steps"] for r in reqs), max(r["steps"] for r in reqs)],
-            "seed": 0}
+            "seed": i})
+    return {"slots": args.serve_slots, "precision": "mixed", "curves": curves,
+            "note": "each grouped launch advances every resident solve by a 12-step block"}
 
 
 def main():
@@ -743,10 +849,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the 64-load-case batched measurement beside the headline")
-    ap.add_argument("--serve-requests", type=int, default=16,
-                    help="requests of the serving stream reported beside the headline (0: off)")
-    ap.add_argument("--serve-rate", type=float, default=2.0, help="Poisson arrival rate, 1/s")
-    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-requests", type=int, default=200,
+                    help="requests of each serving stream reported beside the headline (0: off)")
+    ap.add_argument("--serve-rates", default="4,12,40",
+                    help="Poisson arrival rates of the serving streams, 1/s, comma-separated")
+    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--no-precision-config", action="store_true",
+                    help="skip the 6x24x24 precision configuration beside the headline")
     args = ap.parse_args()
     dist = Dist()
     try:
