@@ -851,7 +851,7 @@ def main():
                     help="skip the 64-load-case batched measurement beside the headline")
     ap.add_argument("--serve-requests", type=int, default=200,
                     help="requests of each serving stream reported beside the headline (0: off)")
-    ap.add_argument("--serve-rates", default="4,12,40",
+    ap.add_argument("--serve-rates", default="2,4,8",
                     help="Poisson arrival rates of the serving streams, 1/s, comma-separated")
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--no-precision-config", action="store_true",
