@@ -1161,7 +1161,15 @@ __device__ __forceinline__ void far_item(const double* __restrict__ coords,
 }
 
 constexpr int kFarBlock = 128;  // threads of a far-field block
-constexpr int kFarChunk = 8;    // levels of a far-field block (the item code keeps 4 bits)
+#ifndef TDBEM_FAR_CHUNK
+#define TDBEM_FAR_CHUNK 8
+#endif
+#ifndef TDBEM_FAR_MIN_BLOCKS
+#define TDBEM_FAR_MIN_BLOCKS 4
+#endif
+constexpr int kFarChunk = TDBEM_FAR_CHUNK;  // levels of a far-field block (at most 256)
+constexpr int kFarCodeBits = 8;             // level offset bits of a compacted item code
+static_assert(kFarChunk >= 1 && kFarChunk <= (1 << kFarCodeBits), "far-field level chunk");
 
 // Exclusive scan of one value per thread over the block; returns the block total.
 __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
@@ -1196,7 +1204,7 @@ __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
 // spread over the threads.  pairs[c * nel + j] is the window of node c and the
 // j-th element in colour order.
 template <typename T>
-__global__ void __launch_bounds__(kFarBlock, 4) k_assemble_far_rows(
+__global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
     int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom,
@@ -1222,12 +1230,14 @@ __global__ void __launch_bounds__(kFarBlock, 4) k_assemble_far_rows(
             }
             int off;
             const int total = far_block_scan(na, off, s_warp);
-            for (int t = 0; t < na; t++) s_items[off + t] = ((j - j0) << 4) | (lo + t - k0);
+            for (int t = 0; t < na; t++)
+                s_items[off + t] = ((j - j0) << kFarCodeBits) | (lo + t - k0);
             __syncthreads();
             for (int i = threadIdx.x; i < total; i += kFarBlock) {
                 const int code = s_items[i];
-                const int k = k0 + (code & 15);
-                far_item<T>(coords, ien, c, color_elems[j0 + (code >> 4)], k, nq2, geomf, geom,
+                const int k = k0 + (code & ((1 << kFarCodeBits) - 1));
+                far_item<T>(coords, ien, c, color_elems[j0 + (code >> kFarCodeBits)], k, nq2,
+                            geomf, geom,
                             coordf, f, ph, (float)k * f.dt, level_last, out);
             }
             count += total;
