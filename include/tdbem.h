@@ -284,8 +284,13 @@ int tdbem_set_pipeline_wait(tdbem_ctx* ctx, double seconds);
  * one): probe[v] = max |A (X v) - v| / max |v| of inverse X of A (v a fixed vector)
  * and full_search[v] = 1 when the pivot search of the panels left their diagonal
  * blocks (a zero pivot there or a probe above 1e-5 made the inversion start again
- * with the full partial-pivoting search). */
-int tdbem_inverse_report(const tdbem_ctx* ctx, double probe[2], int full_search[2]);
+ * with the full partial-pivoting search).  *step2_sweeps (may be NULL) > 0 when the
+ * step-2 LHS, which serves a single solve, gets no inverse of its own: that solve
+ * then runs this many Richardson sweeps x <- x + X (b - A x) with the later LHS's
+ * inverse X against its FP64 LHS A (chosen when they reach 1e-7 on a probe problem;
+ * entry 0 of probe / full_search then repeats entry 1). */
+int tdbem_inverse_report(const tdbem_ctx* ctx, double probe[2], int full_search[2],
+                         int* step2_sweeps);
 
 /* The H^0 inverse alone, on the current device: X = A^-1 for a row-major n x n
  * host matrix A (blocked Gauss-Jordan with partial pivoting; precision TDBEM_FP64,

@@ -136,7 +136,10 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         const int v = st == 1 ? 0 : 1;
         CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_brhs, C, c->d_bpart, sp, s));
         CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, nullptr, c->d_bx, s));
-        for (int it = 0; it < c->batch_refine; it++) {
+        const int sweeps =
+            (st == 1 && c->step2_sweeps > 0) ? std::max(c->step2_sweeps, c->batch_refine)
+                                             : c->batch_refine;
+        for (int it = 0; it < sweeps; it++) {
             CUDA_TRY(launch_apply_cols(c->d_Hc64[v], 1, D, c->d_bx, C, c->d_bpart, sp, s));
             CUDA_TRY(launch_reduce_cols(c->d_bpart, sp, C, D, c->d_brhs, c->d_br, s));
             CUDA_TRY(launch_apply_cols(c->d_inv32[v], 0, D, c->d_br, C, c->d_bpart, sp, s));
@@ -144,9 +147,8 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         }
         CUDA_TRY(launch_update_batch(c->d_bx, D, C, st, c->d_is_ubc, c->d_ubc_map, c->d_btrac,
                                      d_amp, numstep, c->d_bu, c->d_bt, s));
-        prof_end(c, pe, DD * 4 * (1 + c->batch_refine) + DD * 8 * c->batch_refine,
-                 2.0 * DD * C * (1 + 2 * c->batch_refine));
-        c->launches += 6 + 4LL * c->batch_refine;
+        prof_end(c, pe, DD * 4 * (1 + sweeps) + DD * 8 * sweeps, 2.0 * DD * C * (1 + 2 * sweeps));
+        c->launches += 6 + 4LL * sweeps;
     }
     c->timings[2] = tmr.stop_ms(s);
     if (tc) {

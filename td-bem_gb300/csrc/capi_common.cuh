@@ -108,7 +108,8 @@ int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const 
     cudaStream_t s = c->stream;
     const bool same = g.exec && g.kind == kind && g.numstep == numstep && g.nb == c->nb_eff &&
                       g.refine == c->n_refine && g.a1 == c->a1 && g.a2 == c->a2 &&
-                      g.amp == c->amp && g.ptrs == ptrs && g.wait_ns == c->tc_wait_ns;
+                      g.amp == c->amp && g.ptrs == ptrs && g.wait_ns == c->tc_wait_ns &&
+                      g.step2_sweeps == c->step2_sweeps;
     if (!same) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         g.exec = nullptr;
@@ -136,6 +137,7 @@ int run_march_loop(tdbem_ctx* c, int kind, int numstep, const std::vector<const 
         g.amp = c->amp;
         g.ptrs = ptrs;
         g.wait_ns = c->tc_wait_ns;
+        g.step2_sweeps = c->step2_sweeps;
     }
     CUDA_TRY(cudaGraphLaunch(g.exec, s));
     c->launches += g.launches;
@@ -153,6 +155,7 @@ struct InvResult {
     bool singular[2] = {false, false};
     long long launches[2] = {0, 0};
     InverseReport report[2];
+    int step2_sweeps = 0;  // > 0: step 2 by Richardson sweeps with the later inverse
 };
 
 void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t s0,

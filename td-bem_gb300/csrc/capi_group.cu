@@ -113,6 +113,7 @@ int group_prepare(tdbem_ctx* c, int ns, bool mixed, GroupMarch& g) {
     g.x = c->d_x;
     g.r = c->d_res;
     g.refine = c->n_refine > 0 ? 1 : 0;
+    g.step2_sweeps = mixed ? c->step2_sweeps : 0;
     if (mixed) {
         const size_t nwf = (size_t)(c->M + 1) * c->ldf, nwold = nwf * kGroupNB;
         g.Wtf = c->d_group_wf;

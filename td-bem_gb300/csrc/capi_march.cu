@@ -89,15 +89,28 @@ void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t
         r.launches[v] += 1;  // invert_f32 synchronises its stream before returning
     };
     if (ninv == 2) {
-        r.e[1] = cudaEventRecord(c->ev_fork2, s0);  // levels 0/1 and the maps are ready
-        if (r.e[1] == cudaSuccess) r.e[1] = cudaStreamWaitEvent(s1, c->ev_fork2, 0);
-        if (r.e[1] != cudaSuccess) return;
-        std::thread second([&] {
-            cudaSetDevice(c->device);
-            invert(1, s1, c->d_perm2, c->d_status2, c->d_inv_scratch32b);
-        });
-        invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
-        second.join();  // both inverses end with a synchronisation of their stream
+        // The step-2 LHS serves one solve: it is solved by Richardson sweeps
+        // x <- x + X (b - A2 x) with the later steps' inverse X and the FP64 step-2 LHS
+        // A2 when they converge on a probe problem (their contraction is ~0.35 on the
+        // sphere, ~0.6 on a bar with a fixed end), which spares its own inverse; it
+        // gets its own inverse otherwise.
+        invert(1, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
+        if (r.e[1] != cudaSuccess || r.singular[1]) return;
+        r.e[0] = launch_build_lhs(c->d_G01, c->d_H01, nullptr, nullptr, DD, D, lhs_c[0][0],
+                                  lhs_c[0][1], c->d_is_ubc, c->d_Hc64[0], s0);
+        int k = 0;
+        if (r.e[0] == cudaSuccess)
+            r.e[0] = richardson_probe(c->d_Hc64[0], c->d_inv32[1], D,
+                                      reinterpret_cast<double*>(c->d_inv_scratch32),
+                                      kStep2MaxSweeps, kStep2Tol, &k, &r.launches[0], s0);
+        r.launches[0] += 1;
+        if (r.e[0] != cudaSuccess) return;
+        if (k > 0) {
+            r.step2_sweeps = k + kStep2Margin;
+            r.report[0] = r.report[1];
+        } else {
+            invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
+        }
     } else {
         invert(0, s0, c->d_perm, c->d_status, c->d_inv_scratch32);
     }
@@ -116,6 +129,12 @@ int finish_inverses(tdbem_ctx* c, int ninv, const InvResult& r) {
         c->d_inv32[1] = c->d_inv32[0];
         c->d_Hc64[1] = c->d_Hc64[0];
     }
+    // the step-2 solve by Richardson sweeps: its inverse slot is the later LHS's inverse
+    if (ninv == 2 && r.step2_sweeps > 0 && c->d_inv32[0] != c->d_inv32[1]) {
+        dfree(c->d_inv32[0]);
+        c->d_inv32[0] = c->d_inv32[1];
+    }
+    c->step2_sweeps = ninv == 2 ? r.step2_sweeps : 0;
     for (int v = 0; v < 2; v++) c->inv_report[v] = r.report[v < ninv ? v : 0];
     c->inv_valid = true;
     c->inv_n = ninv;
@@ -372,14 +391,15 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         const int v = st == 1 ? 0 : 1;
         const double amp = c->amp.empty() ? 1.0 : c->amp[st];
         // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
+        const int sweeps = (st == 1 && c->step2_sweeps > 0) ? std::max(c->step2_sweeps, c->n_refine)
+                                                            : c->n_refine;
         CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_Yold + (size_t)(st - S) * D,
                                     c->d_x, c->d_res, reinterpret_cast<float*>(c->d_dx),
-                                    c->n_refine, s));
+                                    sweeps, s));
         CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
                                      c->d_fbc_map, amp, c->d_u, c->d_t, s));
-        prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * c->n_refine),
-                 2.0 * (double)DD * (1 + 2 * c->n_refine));
-        c->launches += 4 + 2LL * c->n_refine;  // cast, gemv(s), residual(s), update
+        prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * sweeps), 2.0 * (double)DD * (1 + 2 * sweeps));
+        c->launches += 4 + 2LL * sweeps;  // cast, gemv(s), residual(s), update
         return TDBEM_OK;
     };
     // Steps [s0, s0 + n) of the block starting at S: first half, its history into
@@ -734,13 +754,15 @@ int tdbem_set_pipeline_wait(tdbem_ctx* c, double seconds) {
     return TDBEM_OK;
 }
 
-int tdbem_inverse_report(const tdbem_ctx* c, double probe[2], int full_search[2]) {
+int tdbem_inverse_report(const tdbem_ctx* c, double probe[2], int full_search[2],
+                         int* step2_sweeps) {
     if (!c || !probe || !full_search) return fail(TDBEM_ERR_ARG, "null argument");
     if (!c->inv_valid) return fail(TDBEM_ERR_STATE, "no FP32 inverse made yet");
     for (int v = 0; v < 2; v++) {
         probe[v] = c->inv_report[v].probe_rel;
         full_search[v] = c->inv_report[v].full_search;
     }
+    if (step2_sweeps) *step2_sweeps = c->step2_sweeps;
     return TDBEM_OK;
 }
 

@@ -331,21 +331,31 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                     g->rhs[row] = acc + (lS > 1 ? g->Yold[(size_t)jb * g->D + row] : 0.0);
             }
             grid.sync();
-            // ---- x0 = inv32 rhs | r = rhs - A64 x0 | x = x0 + inv32 r, state update
-            for (int sweep = 0; sweep < 3; sweep++) {
+            // ---- x0 = inv32 rhs | r = rhs - A64 x0 | x = x0 + inv32 r, state update; a mesh
+            // at its step 1 whose step-2 LHS has no inverse of its own repeats the last two
+            // (Richardson sweeps with the later inverse).  The sweep count is the same for
+            // every thread: the largest any mesh needs at this step.
+            int nsw = 3;
+            for (int i = 0; i < nmesh; i++)
+                if (st - gm[i].off == 1 && gm[i].step2_sweeps > 0)
+                    nsw = max(nsw, 1 + 2 * gm[i].step2_sweeps);
+            for (int sweep = 0; sweep < nsw; sweep++) {
                 for (unsigned base = warp_group0; base < nrows; base += ngroups) {
                     const unsigned r = base + sub;
                     const GroupMarch* g =
                         r < nrows ? &gm[mesh_of(gm, nmesh, r, RowBegin{})] : nullptr;
                     const int ls = g ? st - g->off : 0;
-                    const bool live =
-                        g && ls >= 1 && ls < g->numstep && (sweep == 0 || g->refine > 0);
+                    const int msw = !g ? 0
+                                    : (ls == 1 && g->step2_sweeps > 0) ? 1 + 2 * g->step2_sweeps
+                                    : g->refine > 0                    ? 3
+                                                                       : 1;
+                    const bool live = g && ls >= 1 && ls < g->numstep && sweep < msw;
                     double acc = 0;
                     int j = 0;
                     if (live) {
                         j = (int)(r - g->row_begin);
                         const int D = g->D;
-                        if (sweep == 1) {
+                        if (sweep & 1) {
                             const double* Ar = (ls == 1 ? g->Hc0 : g->Hc1) + (size_t)j * D;
                             for (int k = lane; k < D; k += LANES) acc += Ar[k] * g->x[k];
                         } else {
@@ -360,11 +370,13 @@ __global__ void __launch_bounds__(512) k_march_group_tb(const GroupMarch* __rest
                     if (live && lane == 0) {
                         if (sweep == 0) {
                             g->x[j] = acc;
-                            if (g->refine == 0) update_dof(*g, ls, j, acc);
-                        } else if (sweep == 1) {
+                            if (msw == 1) update_dof(*g, ls, j, acc);
+                        } else if (sweep & 1) {
                             g->r[j] = g->rhs[j] - acc;
                         } else {
-                            update_dof(*g, ls, j, g->x[j] + acc);
+                            const double xv = g->x[j] + acc;
+                            g->x[j] = xv;
+                            if (sweep == msw - 1) update_dof(*g, ls, j, xv);
                         }
                     }
                 }

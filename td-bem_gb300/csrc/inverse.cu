@@ -733,6 +733,62 @@ __global__ void __launch_bounds__(256) k_probe_ay(const double* __restrict__ A, 
     }
 }
 
+// Richardson iteration x <- x + X (b - A x) (FP64 residual, FP32 X) on the probe
+// problem b = A v: the kernels of richardson_probe.
+__global__ void __launch_bounds__(256) k_rich_b(const double* __restrict__ A, int n,
+                                                double* __restrict__ b, float* __restrict__ b32) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const double* row = A + (size_t)w * n;
+    double acc = 0;
+    for (int j = lane; j < n; j += 32) acc += row[j] * probe_v(j);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+        b[w] = acc;
+        b32[w] = (float)acc;
+    }
+}
+
+// x = X r32 (accumulate = 0) or x += X r32; err_bits (if set) receives
+// max_i |x_i - v_i| as float bits.
+__global__ void __launch_bounds__(256) k_rich_x(const float* __restrict__ X, int n,
+                                                const float* __restrict__ r32,
+                                                double* __restrict__ x, int accumulate,
+                                                unsigned* __restrict__ err_bits) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const float* row = X + (size_t)w * n;
+    float acc = 0.f;
+    for (int j = lane; j < n; j += 32) acc += row[j] * r32[j];
+    double a = acc;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+        const double xv = accumulate ? x[w] + a : a;
+        x[w] = xv;
+        if (err_bits) {
+            const float e = (float)fabs(xv - probe_v(w));
+            atomicMax(err_bits, __float_as_uint(e == e ? e : 3.0e38f));  // NaN counts as huge
+        }
+    }
+}
+
+// r32 = b - A x
+__global__ void __launch_bounds__(256) k_rich_r(const double* __restrict__ A, int n,
+                                                const double* __restrict__ x,
+                                                const double* __restrict__ b,
+                                                float* __restrict__ r32) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const double* row = A + (size_t)w * n;
+    double acc = 0;
+    for (int j = lane; j < n; j += 32) acc += row[j] * x[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) r32[w] = (float)(b[w] - acc);
+}
+
 __global__ void k_cast_f64_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x)
@@ -1022,6 +1078,40 @@ cudaError_t probe_inverse(const double* A64, const float* X, int n, float* scrat
     float ef;
     std::memcpy(&ef, &bits, sizeof(ef));
     *rel = ef / 6.5f;
+    return cudaSuccess;
+}
+
+cudaError_t richardson_probe(const double* A, const float* X, int n, double* work, int max_sweeps,
+                             double tol, int* sweeps, long long* nlaunch, cudaStream_t s) {
+    *sweeps = 0;
+    if (max_sweeps < 1) return cudaSuccess;
+    double* b = work;
+    double* x = work + n;
+    float* r32 = reinterpret_cast<float*>(work + 2 * (size_t)n);
+    unsigned* err = reinterpret_cast<unsigned*>(r32 + n + (n & 1));  // max_sweeps + 1 words
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned) * (max_sweeps + 1), s);
+    if (e != cudaSuccess) return e;
+    const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+    k_rich_b<<<g, 256, 0, s>>>(A, n, b, r32);
+    k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 0, err);
+    for (int it = 1; it <= max_sweeps; it++) {
+        k_rich_r<<<g, 256, 0, s>>>(A, n, x, b, r32);
+        k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 1, err + it);
+    }
+    *nlaunch += 2 + 2LL * max_sweeps;
+    std::vector<unsigned> bits(max_sweeps + 1);
+    e = cudaMemcpyAsync(bits.data(), err, sizeof(unsigned) * bits.size(), cudaMemcpyDeviceToHost,
+                        s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    for (int it = 1; it <= max_sweeps; it++) {
+        float ef;
+        std::memcpy(&ef, &bits[it], sizeof(ef));
+        if (ef / 6.5 <= tol) {
+            *sweeps = it;
+            break;
+        }
+    }
     return cudaSuccess;
 }
 

@@ -181,6 +181,8 @@ struct GroupMarch {
     double* x;             // D: first solution, then the refined one
     double* r;             // D: residual
     int refine;            // refinement sweeps (0 or 1)
+    int step2_sweeps;      // > 0: step 1's solve by this many Richardson sweeps (inv32_0 =
+                           // inv32_1, Hc0 the step's own FP64 LHS)
     // time blocks of kGroupNB steps (mixed): old-history vectors and their product
     float* Wold_t;         // (M+1) x kGroupNB x ldf
     float* Wold_u;
@@ -233,6 +235,15 @@ struct InverseReport {
     int full_search = 0;
 };
 constexpr float kInverseProbeBar = 1e-5f;
+// Sweeps of the Richardson iteration x <- x + X (b - A x) (x0 = X b, FP64 residual,
+// FP32 X) that bring the probe problem b = A v within tol (max |x - v| / max |v|);
+// *sweeps = 0 when max_sweeps do not.  work: 3 n + max_sweeps + 2 doubles of scratch.
+cudaError_t richardson_probe(const double* A, const float* X, int n, double* work, int max_sweeps,
+                             double tol, int* sweeps, long long* nlaunch, cudaStream_t s);
+// The step-2 solve by Richardson sweeps with the later steps' inverse: the iteration's
+// tolerance on the probe problem, the most sweeps tried, and the margin added.
+constexpr double kStep2Tol = 1e-7;
+constexpr int kStep2MaxSweeps = 48, kStep2Margin = 2;
 cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_status,
                        float* scratch, long long* nlaunch, bool* singular, cudaStream_t s,
                        InverseReport* report = nullptr);
@@ -381,6 +392,7 @@ struct MarchGraph {
     std::vector<double> amp;
     std::vector<const void*> ptrs;
     unsigned long long wait_ns = 0;  // pipeline wait limit of the tcgen05 kernels
+    int step2_sweeps = 0;            // Richardson sweeps of the step-2 solve
     long long launches = 0;  // kernels in the graph
 };
 
@@ -463,6 +475,9 @@ struct tdbem_ctx {
     int* d_tc_err = nullptr;        // tcgen05 kernel: [0] wait time-out code, [1] CTAs holding TMEM
     unsigned long long tc_wait_ns = tdbem::kTcWaitNsDefault;  // its pipeline wait limit
     tdbem::InverseReport inv_report[2];  // probe and pivot search of the FP32 inverses
+    // mixed form: > 0 when step 2's LHS is solved by this many Richardson sweeps with the
+    // later steps' FP32 inverse (d_inv32[0] then aliases d_inv32[1]), 0 with its own
+    int step2_sweeps = 0;
     // grouped marching: the load history on the device, the FP32 time-block scratch
     double* d_group_amp = nullptr;
     float* d_group_wf = nullptr;

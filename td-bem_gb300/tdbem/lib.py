@@ -64,7 +64,7 @@ SIGNATURES = {
     "tdbem_set_batch_options": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tdbem_set_graphs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_set_pipeline_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
-    "tdbem_inverse_report": (ctypes.c_int, [ctypes.c_void_p, _dp, _ip]),
+    "tdbem_inverse_report": (ctypes.c_int, [ctypes.c_void_p, _dp, _ip, _ip]),
     "tdbem_invert": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _ip]),
     "tdbem_set_march_engine": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tdbem_assemble_group": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip,
@@ -400,11 +400,13 @@ class Context:
         _check(load().tdbem_set_pipeline_wait(self.h, seconds))
 
     def inverse_report(self):
-        """(probe residuals, full-search flags) of the two FP32 inverses of the mixed march."""
+        """(probe residuals, full-search flags, step-2 Richardson sweeps) of the FP32
+        inverses of the mixed march."""
         p = (ctypes.c_double * 2)()
         f = (ctypes.c_int * 2)()
-        _check(load().tdbem_inverse_report(self.h, p, f))
-        return list(p), list(f)
+        k = ctypes.c_int()
+        _check(load().tdbem_inverse_report(self.h, p, f, ctypes.byref(k)))
+        return list(p), list(f), k.value
 
     def set_batch_options(self, engine: int = 0, refine_sweeps: int = 0):
         _check(load().tdbem_set_batch_options(self.h, engine, refine_sweeps))

@@ -91,8 +91,30 @@ def test_march_inverses_pass_the_probe(tdlib, case):
         ctx.set_alpha(0.25, 0.1)
         ctx.assemble(precision=tdlib.MIXED)
         ctx.march(20)
-        probe, full = ctx.inverse_report()
-    print(f"{case}: probe {probe}, full search {full}")
+        probe, full, k2 = ctx.inverse_report()
+    print(f"{case}: probe {probe}, full search {full}, step-2 Richardson sweeps {k2}")
     assert max(probe) <= 1e-5
+    # alpha_1 = 0.25: the step-2 LHS differs from the later one and is solved with
+    # Richardson sweeps (contraction ~0.35 on the sphere, ~0.6 on the bar)
+    assert 0 < k2 <= 50
     if case == "sphere":
         assert full == [0, 0]
+
+
+def test_step2_richardson_matches_fp64(tdlib):
+    """The mixed march with the step-2 solve by Richardson sweeps stays within 1e-4
+    (relative L2) of the plain FP64 march, and its first solved step within 1e-5."""
+    from tdbem import meshes
+    m = meshes.cubed_sphere(8, numstep=60)
+    out = {}
+    for prec in (tdlib.FP64, tdlib.MIXED):
+        with tdlib.Context(m) as ctx:
+            ctx.set_alpha(0.25, 0.1)
+            ctx.set_march_engine(tdlib.ENGINE_FP32)
+            ctx.assemble(precision=prec)
+            out[prec] = ctx.march()
+            if prec == tdlib.MIXED:
+                assert ctx.inverse_report()[2] > 0
+    u64, u32 = out[tdlib.FP64][0], out[tdlib.MIXED][0]
+    assert np.linalg.norm(u32 - u64) / np.linalg.norm(u64) <= 1e-4
+    assert np.abs(u32[1] - u64[1]).max() / np.abs(u64[1]).max() <= 1e-5
