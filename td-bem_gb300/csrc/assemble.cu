@@ -656,21 +656,40 @@ __device__ __forceinline__ void assemble_item(
         rowbase = (size_t)(3 * (c - out.row_node_lo)) * D;
     }
     constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+    // read-modify-write of the item's entries, a node block at a time, reads before
+    // writes (as in far_item)
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++) {
+        if (Gf) {
+            float og[9], oh[9];
 #pragma unroll
-        for (int i = 0; i < 3; i++)
-#pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const size_t idx = rowbase + (size_t)i * D + 3 * (size_t)nid[a] + j;
-                if (Gf) {
-                    Gf[idx] += (float)acc.g[a][sym[i * 3 + j]];
-                    Hf[idx] += (float)acc.h[a][i * 3 + j];
-                } else {
-                    G[idx] += acc.g[a][sym[i * 3 + j]];
-                    H[idx] += acc.h[a][i * 3 + j];
-                }
+            for (int m = 0; m < 9; m++) {
+                const size_t idx = rowbase + (size_t)(m / 3) * D + 3 * (size_t)nid[a] + m % 3;
+                og[m] = Gf[idx];
+                oh[m] = Hf[idx];
             }
+#pragma unroll
+            for (int m = 0; m < 9; m++) {
+                const size_t idx = rowbase + (size_t)(m / 3) * D + 3 * (size_t)nid[a] + m % 3;
+                Gf[idx] = og[m] + (float)acc.g[a][sym[m]];
+                Hf[idx] = oh[m] + (float)acc.h[a][m];
+            }
+        } else {
+            double og[9], oh[9];
+#pragma unroll
+            for (int m = 0; m < 9; m++) {
+                const size_t idx = rowbase + (size_t)(m / 3) * D + 3 * (size_t)nid[a] + m % 3;
+                og[m] = G[idx];
+                oh[m] = H[idx];
+            }
+#pragma unroll
+            for (int m = 0; m < 9; m++) {
+                const size_t idx = rowbase + (size_t)(m / 3) * D + 3 * (size_t)nid[a] + m % 3;
+                G[idx] = og[m] + acc.g[a][sym[m]];
+                H[idx] = oh[m] + acc.h[a][m];
+            }
+        }
+    }
 }
 
 
