@@ -84,16 +84,22 @@ def make_model(name):
 # distributed plumbing (replicas only)
 # --------------------------------------------------------------------------
 class Dist:
+    """Replicas of the workload, one process per GPU (torchrun): a barrier around the
+    timed region and the slowest rank's time.  NCCL on GPUs, gloo on CPU-only hosts."""
+
     def __init__(self):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.pg = None
+        self.device = "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+                self.device = "cuda"
+            dist.init_process_group("nccl" if self.device == "cuda" else "gloo")
             self.pg = dist
 
     def barrier(self):
@@ -104,8 +110,16 @@ class Dist:
         if not self.pg:
             return x
         import torch
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
         self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
         return float(t.item())
 
     def close(self):
@@ -355,6 +369,32 @@ def compare_batch(lib, torch, ctx, model, trac, amp, ms_step, check=(0, 1, 2)):
             "u_rel_l2_err": max(errs_u), "t_rel_l2_err": max(errs_t)}
 
 
+def compare_fixed_cap(lib, model):
+    """The traction-unknown path of the mixed march at the workload's size: the same
+    cavity with the displacement of its nodes above z = 0.7 prescribed (zero) and the
+    pressure elsewhere, so that the march solves for tractions at the cap's dofs;
+    the mixed form's u and t errors against the plain FP64 form."""
+    import dataclasses
+    cap = np.flatnonzero(model.coords[:, 2] > 0.7)
+    udofs = (3 * cap[:, None] + np.arange(3)).reshape(-1).astype(np.int32)
+    keep = ~np.isin(model.fbc_dofs, udofs)
+    m = dataclasses.replace(model, ubc_dofs=udofs, ubc_vals=np.zeros(len(udofs)),
+                            fbc_dofs=np.ascontiguousarray(model.fbc_dofs[keep]),
+                            fbc_vals=np.ascontiguousarray(model.fbc_vals[keep]))
+    out = {}
+    for prec in (lib.FP64, lib.MIXED):
+        with lib.Context(m) as c:
+            c.set_alpha(*ALPHA)
+            c.assemble(precision=prec)
+            out[prec] = c.march()
+    (u64, t64), (u32, t32) = out[lib.FP64], out[lib.MIXED]
+    return {"prescribed_displacement_dofs": int(len(udofs)),
+            "u_rel_l2_err": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+            "t_rel_l2_err": float(np.linalg.norm(t32 - t64) / np.linalg.norm(t64)),
+            "t_rel_l2_err_at_cap": float(np.linalg.norm((t32 - t64)[:, udofs]) /
+                                         np.linalg.norm(t64[:, udofs]))}
+
+
 def run_ours(args, dist):
     import torch
     from tdbem import lib
@@ -479,6 +519,8 @@ def run_ours(args, dist):
                    "u_rel_l2_err": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
                    "t_rel_l2_err": float(np.linalg.norm(t32 - t64) / np.linalg.norm(t64))}
     ctx.close()
+    if compare is not None and not cases and WORKLOADS[args.workload]["kind"] == "sphere":
+        compare["fixed_cap"] = compare_fixed_cap(lib, model)
 
     if dist.rank != 0:
         return 0
