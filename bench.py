@@ -608,6 +608,10 @@ def run_ours(args, dist):
         line["vs_plain_fp64"] = compare
     if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_batched:
         line["batched"] = run_batched(lib, torch, args)
+    if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_batched:
+        g = group_measure(lib, torch, args, dist, "bars32_group")
+        line["grouped"] = {k: g[k] for k in ("value", "unit", "ms_per_step", "config", "e2e",
+                                              "autotuned_shape", "vs_plain_fp64") if k in g}
     if dist.world == 1 and not cases and prec == lib.MIXED and not args.no_precision_config:
         line["precision_config"] = run_precision_config(lib, torch, args, peaks, peak_kind)
     if args.serve_requests > 0:
@@ -739,10 +743,18 @@ def run_precision_config(lib, torch, args, peaks, peak_kind, workload="sphere_6x
 
 
 def run_group(lib, torch, args, dist):
+    """Many meshes at once (the --workload bars32_group line)."""
+    line = group_measure(lib, torch, args, dist, args.workload)
+    if dist.rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def group_measure(lib, torch, args, dist, workload):
     """Many meshes at once: grouped assembly + one persistent launch for every step
     of every mesh, against the same meshes solved one after another (plain FP64
     both ways)."""
-    w = WORKLOADS[args.workload]
+    w = WORKLOADS[workload]
     models = group_models(w["count"], w["numstep"])
     dofs = [m.ndof for m in models]
     units = sum(d * m.numstep for d, m in zip(dofs, models))
@@ -808,13 +820,11 @@ def run_group(lib, torch, args, dist):
             "u_rel_l2_err_max_over_meshes": err}}
     for c in ctxs:
         c.close()
-    if dist.rank != 0:
-        return 0
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == lib.FP64 else "f32+f64", "data": "synthetic",
-            "config": {"workload": args.workload, "meshes": len(models),
+            "config": {"workload": workload, "meshes": len(models),
                        "dof_range": [min(dofs), max(dofs)], "dof_total": sum(dofs),
                        "steps": w["numstep"], "alpha": list(ALPHA), "precision": args.precision,
                        "parallelism": f"replicas{dist.world}",
@@ -828,8 +838,7 @@ def run_group(lib, torch, args, dist):
             "gpu_launches": int(launches), "phases_ms": timing, "autotuned_shape": shape,
             "clocks": clk}
     line.update(line_extra)
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 def run_serve(lib, args, dev):
