@@ -1126,6 +1126,33 @@ __device__ __forceinline__ double* far_out<double>(const AsmOut& o, int which) {
     return which == 0 ? o.G0 : o.H0;
 }
 
+// Adds s times an item's 4 node blocks (G as symmetric 6-vectors, H as 3x3) into the
+// 3 rows at rowbase of a level store with leading dimension D, as reductions
+// (red.global.add): none waits for a read of the store, where a read-modify-write
+// would wait for every read in turn (as far as the compiler knows G and H, and two
+// nodes' columns, may alias).  The order of the adds into one entry is still fixed:
+// all of an entry's adds come from one block (the block owns its node's rows), at
+// most one per colour, and a barrier separates the colours, so each add is performed
+// before the next colour's (bitwise reproducible).  The FP32 reduction flushes
+// subnormal values to zero (below 1.2e-38, far under the store's resolution).
+template <typename T>
+__device__ __forceinline__ void add_node_blocks(T* G, T* H, size_t rowbase, size_t D,
+                                                const int nid[4], const ItemAccF& acc,
+                                                float s) {
+    constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+        const size_t col = rowbase + 3 * (size_t)nid[a];
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                atomicAdd(G + col + (size_t)i * D + j, (T)(s * acc.g[a][sym[i * 3 + j]]));
+                atomicAdd(H + col + (size_t)i * D + j, (T)(s * acc.h[a][i * 3 + j]));
+            }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void far_item(const double* __restrict__ coords,
                                          const int* __restrict__ ien, int c, int e, int k,
@@ -1163,20 +1190,123 @@ __device__ __forceinline__ void far_item(const double* __restrict__ coords,
                         geom + ((size_t)e * nq2 + q) * kGeomStride, coords + 3 * c, k, ph);
     }
     const size_t D = (size_t)out.ld;
-    const size_t rowbase = (size_t)k * out.level_stride + (size_t)(3 * c) * D;
-    constexpr int sym[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
-    T* G = far_out<T>(out, 0);
-    T* H = far_out<T>(out, 1);
+    add_node_blocks<T>(far_out<T>(out, 0), far_out<T>(out, 1),
+                       (size_t)k * out.level_stride + (size_t)(3 * c) * D, D, nid, acc, 1.f);
+}
+
+// Settled far items.  At level k the P front has passed every Gauss point of the
+// element at all four evaluation times of the level (TI - dt - r/c_p >= dt) and the S
+// front reaches none of them (TJ - r/c_s < 0, TJ = TI + dt).  Every tau of the P wave
+// is then >= dt (b = dt, no I5/J5 step, I3 and J3 constant) and the S wave's terms are
+// all zero, so the differences of the tau polynomials reduce to
+//   Q1(tau) - Q1(tau - dt) + R1(tau + dt) - R1(tau) = 24 dt^3,
+//   Q0(tau) - Q0(tau - dt) + R0(tau + dt) - R0(tau) = 24 tau dt^3 - 12 dt^4,
+// and with rho + tau = TI: P1 = 2 dt^2 (TI - dt/2) / r^2, It1 = dt^2 (TI - dt/2) / r^2,
+// every other time integral zero.  The level's blocks are (TI - dt/2) times one
+// time-independent block of the pair (the quasi-static kernel):
+//   G: dt^2 / (4 pi rho r^3) (3 r r^T - I)
+//   H: 6 c_s^2 dt^2 / (4 pi r^4) (-5 (r.n) r r^T + r n^T + n r^T + (r.n) I)
+// (GreenFunctionT.cpp:241-446 and TDElementStepLinearT.cpp:28-125 evaluated in that
+// regime), so a pair's settled levels take one pass over its Gauss points and one
+// scaled add per level.  The range is decided from FP32 distances with margins that
+// only narrow it (a level at a regime threshold takes the general quadrature).
+constexpr float kSettledRel = 1e-5f;  // relative margin on FP32 point distances
+constexpr float kSettledAbs = 1e-3f;  // margin in levels
+
+// Levels slo..shi at which pair (c, e) is settled (empty if slo > shi).
+__device__ __forceinline__ void settled_range(const int* __restrict__ ien, int c, int e,
+                                              int nq2, const float* __restrict__ geomf,
+                                              const float* __restrict__ coordf,
+                                              const PhysF& f, int& slo, int& shi) {
+    const int n0 = ien[e * 4];
+    const float4* cf4 = reinterpret_cast<const float4*>(coordf);
+    const float4 ch = __ldg(cf4 + 2 * c), cl = __ldg(cf4 + 2 * c + 1);
+    const float4 eh = __ldg(cf4 + 2 * n0), el = __ldg(cf4 + 2 * n0 + 1);
+    const float x0 = (ch.x - eh.x) + (cl.x - el.x), x1 = (ch.y - eh.y) + (cl.y - el.y),
+                x2 = (ch.z - eh.z) + (cl.z - el.z);
+    const float4* g4 = reinterpret_cast<const float4*>(geomf + (size_t)e * nq2 * kGeomStride);
+    float r2min = 3.4e38f, r2max = 0.f;
+#pragma unroll 4
+    for (int q = 0; q < nq2; q++) {
+        const float4 p = __ldg(g4 + 3 * q);
+        const float d0 = p.x - x0, d1 = p.y - x1, d2 = p.z - x2;
+        const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        r2min = fminf(r2min, r2);
+        r2max = fmaxf(r2max, r2);
+    }
+    const float rmax = sqrtf(r2max) * (1.f + kSettledRel);
+    const float rmin = sqrtf(r2min) * (1.f - kSettledRel);
+    // P passed at TI - dt: k >= 2 + r/(c_p dt) at the farthest point
+    slo = (int)ceilf(2.f + rmax * f.inv_cp * f.inv_dt + kSettledAbs);
+    // S short of the nearest point at TJ: k + 1 < r/(c_s dt), i.e. k <= ceil(y) - 2
+    shi = (int)ceilf(rmin * f.inv_cs * f.inv_dt - kSettledAbs) - 2;
+}
+
+// A settled job: pair (c, e) at levels ks .. ks + ns - 1, all settled.
+template <typename T>
+__device__ __forceinline__ void settled_job(const int* __restrict__ ien, int c, int e, int ks,
+                                            int ns, int nq2, const float* __restrict__ geomf,
+                                            const float* __restrict__ coordf, const PhysF& f,
+                                            const AsmOut& out) {
+    int nid[4];
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+    for (int a = 0; a < 4; a++) nid[a] = ien[e * 4 + a];
+    const float4* cf4 = reinterpret_cast<const float4*>(coordf);
+    const float4 ch = __ldg(cf4 + 2 * c), cl = __ldg(cf4 + 2 * c + 1);
+    const float4 eh = __ldg(cf4 + 2 * nid[0]), el = __ldg(cf4 + 2 * nid[0] + 1);
+    const float xc[3] = {(ch.x - eh.x) + (cl.x - el.x), (ch.y - eh.y) + (cl.y - el.y),
+                         (ch.z - eh.z) + (cl.z - el.z)};
+    ItemAccF acc;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+#pragma unroll
+        for (int m = 0; m < 6; m++) acc.g[a][m] = 0.f;
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc.h[a][m] = 0.f;
+    }
+    const float dt2 = f.dt * f.dt;
+    const float h6 = 6.f * f.cs2 * f.inv_4pi;
+    const float4* g4 = reinterpret_cast<const float4*>(geomf + (size_t)e * nq2 * kGeomStride);
+    for (int q = 0; q < nq2; q++) {
+        const float4 p0 = __ldg(g4 + 3 * q), p1 = __ldg(g4 + 3 * q + 1), p2 = __ldg(g4 + 3 * q + 2);
+        const float nq[3] = {p0.w, p1.x, p1.y};
+        const float N[4] = {p1.w, p2.x, p2.y, p2.z};
+        const float d0 = p0.x - xc[0], d1 = p0.y - xc[1], d2 = p0.z - xc[2];
+        const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        const float inv_r = rsqrtf(r2);
+        const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+        const float rdn = rv[0] * nq[0] + rv[1] * nq[1] + rv[2] * nq[2];
+        const float u = dt2 * inv_r * inv_r;       // It1 / (TI - dt/2)
+        const float ga = u * inv_r * f.inv_4pi_rho;  // A = 3 ga, B = -ga
+        const float hb = h6 * u * inv_r * inv_r;     // beta = gamma = hb, alpha = -5 hb
+        const float ga3 = 3.f * ga;
+        const float rr00 = rv[0] * rv[0], rr01 = rv[0] * rv[1], rr02 = rv[0] * rv[2];
+        const float rr11 = rv[1] * rv[1], rr12 = rv[1] * rv[2], rr22 = rv[2] * rv[2];
+        const float sg[6] = {ga3 * rr00 - ga, ga3 * rr01, ga3 * rr02,
+                             ga3 * rr11 - ga, ga3 * rr12, ga3 * rr22 - ga};
+        const float ar = -5.f * hb * rdn, gd = hb * rdn;
+        const float rrm[9] = {rr00, rr01, rr02, rr01, rr11, rr12, rr02, rr12, rr22};
+        float th[9];
 #pragma unroll
         for (int i = 0; i < 3; i++)
 #pragma unroll
-            for (int j = 0; j < 3; j++) {
-                const size_t idx = rowbase + (size_t)i * D + 3 * (size_t)nid[a] + j;
-                G[idx] += (T)acc.g[a][sym[i * 3 + j]];
-                H[idx] += (T)acc.h[a][i * 3 + j];
-            }
+            for (int j = 0; j < 3; j++)
+                th[i * 3 + j] = ar * rrm[i * 3 + j] + hb * (nq[j] * rv[i] + nq[i] * rv[j]) +
+                                (i == j ? gd : 0.f);
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            const float w = p1.z * N[a];
+#pragma unroll
+            for (int m = 0; m < 6; m++) acc.g[a][m] += w * sg[m];
+#pragma unroll
+            for (int m = 0; m < 9; m++) acc.h[a][m] += w * th[m];
+        }
+    }
+    const size_t D = (size_t)out.ld;
+    for (int k = ks; k < ks + ns; k++)  // scaled by TI - dt/2
+        add_node_blocks<T>(far_out<T>(out, 0), far_out<T>(out, 1),
+                           (size_t)k * out.level_stride + (size_t)(3 * c) * D, D, nid, acc,
+                           ((float)k - 0.5f) * f.dt);
 }
 
 constexpr int kFarBlock = 128;  // threads of a far-field block
@@ -1221,50 +1351,85 @@ __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
 // reproducible), and one launch covers all colours.  Candidate items (element,
 // level) of a batch of kFarBlock elements are compacted with a block scan and
 // spread over the threads.  pairs[c * nel + j] is the window of node c and the
-// j-th element in colour order.
+// j-th element in colour order.  A pair's settled levels (settled_range) leave its
+// item list and go to one settled job; the batch's items come first in the thread
+// order and its jobs after them, so most warps hold one kind of work.  level_top:
+// the highest level any window reaches.  nitems (if not null) receives the item,
+// job and settled-level counts.
 template <typename T>
 __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
     int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom,
-    const float* __restrict__ coordf, Phys ph, int level_last,
+    const float* __restrict__ coordf, Phys ph, int level_last, int level_top,
     const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
     __shared__ int s_warp[kFarBlock / 32];
     __shared__ int s_items[kFarBlock * kFarChunk];
+    __shared__ int s_jobs[kFarBlock];
     const int c = blockIdx.x;
     const int k0 = blockIdx.y * kFarChunk;
-    const int k1 = min(k0 + kFarChunk, level_last + 1);
+    const int k1 = min(k0 + kFarChunk, level_top + 1);
+    // settled levels need both parts (1 <= k <= level_last - 1) and k >= 2
+    const bool settle = k1 - 1 >= 2 && level_last >= 3;
     const PhysF f = to_f(ph);
     const PairInfo* pc = pairs + (size_t)c * nel;
-    unsigned long long count = 0;
+    unsigned long long count = 0, njobs = 0, nsettled = 0;
     for (int col = 0; col < ncolor; col++) {
         const int j0 = color_start[col], j1 = color_start[col + 1];
         for (int base = j0; base < j1; base += kFarBlock) {  // uniform over the block
             const int j = base + (int)threadIdx.x;
-            int na = 0, lo = 0;
+            int na = 0, lo = 0, ss = 0, sn = 0;
             if (j < j1) {
                 const PairInfo pi = pc[j];
                 lo = max(k0, pi.klo);
                 na = max(0, min(k1, pi.klo + pi.cnt) - lo);
+                if (settle && na > 0) {
+                    int slo, shi;
+                    settled_range(ien, c, color_elems[j], nq2, geomf, coordf, f, slo, shi);
+                    slo = max(slo, lo);
+                    shi = min(shi, min(lo + na - 1, level_last - 1));
+                    if (shi >= slo) {
+                        ss = slo;
+                        sn = shi - slo + 1;
+                    }
+                }
             }
-            int off;
-            const int total = far_block_scan(na, off, s_warp);
-            for (int t = 0; t < na; t++)
-                s_items[off + t] = ((j - j0) << kFarCodeBits) | (lo + t - k0);
+            int off, offj;
+            const int total = far_block_scan(na - sn, off, s_warp);
+            const int jobs = far_block_scan(sn > 0 ? 1 : 0, offj, s_warp);
+            for (int k = lo; k < lo + na; k++)
+                if (k < ss || k >= ss + sn)
+                    s_items[off++] = ((int)threadIdx.x << kFarCodeBits) | (k - k0);
+            if (sn > 0)
+                s_jobs[offj] = ((int)threadIdx.x << 16) | ((ss - k0) << 8) | (sn - 1);
             __syncthreads();
-            for (int i = threadIdx.x; i < total; i += kFarBlock) {
-                const int code = s_items[i];
-                const int k = k0 + (code & ((1 << kFarCodeBits) - 1));
-                far_item<T>(coords, ien, c, color_elems[j0 + (code >> kFarCodeBits)], k, nq2,
-                            geomf, geom,
-                            coordf, f, ph, (float)k * f.dt, level_last, out);
+            for (int i = threadIdx.x; i < total + jobs; i += kFarBlock) {
+                if (i < total) {
+                    const int code = s_items[i];
+                    const int k = k0 + (code & ((1 << kFarCodeBits) - 1));
+                    far_item<T>(coords, ien, c, color_elems[base + (code >> kFarCodeBits)], k,
+                                nq2, geomf, geom, coordf, f, ph, (float)k * f.dt, level_last,
+                                out);
+                } else {
+                    const int job = s_jobs[i - total];
+                    settled_job<T>(ien, c, color_elems[base + (job >> 16)],
+                                   k0 + ((job >> 8) & 0xff), (job & 0xff) + 1, nq2, geomf,
+                                   coordf, f, out);
+                }
             }
             count += total;
+            njobs += jobs;
+            nsettled += sn;
             // s_items is rebuilt next; this batch's adds come before the next colour's
             __syncthreads();
         }
     }
-    if (nitems && threadIdx.x == 0 && count) atomicAdd(nitems, count);
+    if (nitems) {
+        if (threadIdx.x == 0 && count) atomicAdd(nitems, count);
+        if (threadIdx.x == 0 && njobs) atomicAdd(nitems + 1, njobs);
+        const unsigned w = __reduce_add_sync(0xffffffffu, (unsigned)nsettled);
+        if ((threadIdx.x & 31) == 0 && w) atomicAdd(nitems + 2, (unsigned long long)w);
+    }
 }
 
 // C term (TDElementStepLinearT.cpp:103-109, 501-508, 577-584 with AssembleC,
@@ -1632,12 +1797,14 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
         k_assemble_far_rows<double><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                                color_start, ncolor, nel, nq * nq,
                                                                geomf, geom, coordf, ph,
-                                                               level_last, pairs, out, nitems);
+                                                               level_last, top, pairs, out,
+                                                               nitems);
     else
         k_assemble_far_rows<float><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                               color_start, ncolor, nel, nq * nq,
                                                               geomf, geom, coordf, ph,
-                                                              level_last, pairs, out, nitems);
+                                                              level_last, top, pairs, out,
+                                                              nitems);
     return cudaGetLastError();
 }
 

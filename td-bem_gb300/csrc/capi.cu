@@ -397,7 +397,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     if (ennd == 4) CTX_TRY(dalloc(&c->d_geomf, (size_t)c->nel * nq * nq * 12));
     CTX_TRY(dalloc(&c->d_color_elems, order.size()));
     CTX_TRY(dalloc(&c->d_color_start, c->color_start.size()));
-    CTX_TRY(dalloc(&c->d_far_items, 1));
+    CTX_TRY(dalloc(&c->d_far_items, 3));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
     {  // node coordinates as FP32 pairs x = hi + lo for the FP32 far form
@@ -651,7 +651,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         }
         const bool count = c->prof;  // the far item count feeds the profile's byte/flop totals
         if (count)
-            CUDA_TRY(cudaMemsetAsync(c->d_far_items, 0, sizeof(unsigned long long), c->stream));
+            CUDA_TRY(cudaMemsetAsync(c->d_far_items, 0, 3 * sizeof(unsigned long long), c->stream));
         if (split) {
             const int pw = prof_begin(c, TDBEM_K_AUX);
             CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
@@ -730,12 +730,14 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             prof_end(c, pe, 0, 0);
             c->launches += 2;
             if (count && pe >= 0) {
-                unsigned long long n = 0;
-                CUDA_TRY(cudaMemcpyAsync(&n, c->d_far_items, sizeof(n), cudaMemcpyDeviceToHost,
+                unsigned long long n[3] = {0, 0, 0};
+                CUDA_TRY(cudaMemcpyAsync(n, c->d_far_items, sizeof(n), cudaMemcpyDeviceToHost,
                                          c->stream));
                 CUDA_TRY(cudaStreamSynchronize(c->stream));
-                c->prof_pending[pe].bytes = (double)n * 4 * 45 * 4.0 * 2;
-                c->prof_pending[pe].flops = (double)n * c->nq * c->nq * kFlopsPerItemPointF32;
+                c->prof_pending[pe].bytes = (double)(n[0] + n[2]) * 4 * 45 * 4.0 * 2;
+                c->prof_pending[pe].flops = (double)n[0] * c->nq * c->nq * kFlopsPerItemPointF32 +
+                                            (double)n[1] * c->nq * c->nq * kFlopsSettledPoint +
+                                            (double)n[2] * kFlopsSettledLevel;
             }
         }
         // levels 0/1 (with the C term) from the FP64 pair

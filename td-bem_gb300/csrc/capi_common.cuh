@@ -65,6 +65,10 @@ constexpr double kFlopsPerItemPoint = 398.0;
 // The FP32 far-field form (tau variables): geometry 20, wave polynomials and
 // differences 176, scalars 40, kernels 65, accumulation 124.
 constexpr double kFlopsPerItemPointF32 = 425.0;
+// A settled job's point (the quasi-static kernel): geometry 18, scalars 8, kernels
+// 51, accumulation 124; a settled level: a scaled add per entry of the 4 node blocks.
+constexpr double kFlopsSettledPoint = 201.0;
+constexpr double kFlopsSettledLevel = 144.0;
 
 int prof_begin_on(tdbem_ctx* c, int cls, cudaStream_t s);
 int prof_begin(tdbem_ctx* c, int cls);

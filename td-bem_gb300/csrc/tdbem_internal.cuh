@@ -100,8 +100,9 @@ cudaError_t launch_assemble_step_pairs(const double* coords, const int* ien, int
                                        unsigned npairs, const AsmOut& out, cudaStream_t s);
 // Far (well-separated) items of every node in FP32, ASM_LEVELS, into the FP32 store:
 // one launch over (node, chunk of levels) blocks, colours walked inside each block.
-// pairs holds nnd x nel windows (SEL_FAR), elements in colour order; *nitems (if
-// not null) receives the item count.  4-node elements only.
+// pairs holds nnd x nel windows (SEL_FAR), elements in colour order; nitems[0..2]
+// (if not null) receive the counts of items through the quadrature, of settled jobs
+// and of settled levels.  4-node elements only.
 cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
                                      const int* color_elems, const int* color_start, int ncolor,
                                      int nnd, int nel, int nq, const float* geomf,
@@ -421,7 +422,7 @@ struct tdbem_ctx {
     int* d_color_start = nullptr;    // color_start on the device
     tdbem::PairInfo* d_far_pairs = nullptr;  // mixed: windows of all nnd x nel pairs (SEL_FAR)
     size_t far_pairs_cap = 0;
-    unsigned long long* d_far_items = nullptr;  // far item count (profiling)
+    unsigned long long* d_far_items = nullptr;  // far items, settled jobs, settled levels (profiling)
     // pair/item scratch
     tdbem::PairInfo* d_pairs = nullptr;
     unsigned* d_counts = nullptr;

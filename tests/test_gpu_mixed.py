@@ -55,6 +55,32 @@ def test_mixed_levels_close_to_fp64(tdlib, sphere8):
         assert np.abs(a - b).max() <= 2e-5 * np.abs(b).max()
 
 
+def test_mixed_every_level_close_to_fp64(tdlib):
+    """Every level of the FP32 store against the FP64 levels (oracle-pinned), 2e-5 of
+    the level's max-norm: the far pairs' settled levels (P front passed at every
+    Gauss point, S front at none: one quasi-static block per pair scaled by
+    (k - 1/2) dt) and the levels at both fronts (the tau form) alike."""
+    from tdbem import meshes
+    m = meshes.cubed_sphere(8, numstep=60)
+    levels = {}
+    for prec in (tdlib.FP64, tdlib.MIXED):
+        with tdlib.Context(m) as ctx:
+            ctx.assemble(precision=prec)
+            M = ctx.M
+            levels[prec] = [(ctx.level(k, 0), ctx.level(k, 1)) for k in range(2, M + 1)]
+    assert M > 20
+    worst = 0.0
+    for k, (a, b) in enumerate(zip(levels[tdlib.MIXED], levels[tdlib.FP64]), start=2):
+        for x, y, nm in zip(a, b, "GH"):
+            if np.abs(y).max() == 0:
+                assert np.abs(x).max() == 0, f"level {k} {nm}"
+                continue
+            e = np.abs(x - y).max() / np.abs(y).max()
+            worst = max(worst, e)
+            assert e <= 2e-5, f"level {k} {nm}: {e:.2e}"
+    print(f"worst level error {worst:.2e} over levels 2..{M}")
+
+
 def test_mixed_c_term_close_to_fp64(tdlib):
     """Levels 0 and 1 of the mixed form (the LHS of its solves) hold the C term,
     its regular elements in FP32: the diagonal blocks stay within 1e-6 of FP64."""
