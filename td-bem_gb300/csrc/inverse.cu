@@ -19,13 +19,13 @@
 // whole inversion is 2 n^3 flops in GEMM form; the FP32 inverse runs step 5 on
 // 128 x 128 tiles (k_panel_update_f32), the FP64 one on 64 x 64 tiles.
 //
-// The FP32 inverse (a preconditioner that FP64 refinement corrects) may restrict
-// step 1's search to the panel's diagonal block (k_block_pivots, one CTA: no
-// cluster-wide reduction per column).  On the boundary-element LHS the column
-// maximum lies in that block (diagonal dominance), so the pivots are the same; a
-// zero pivot in the block, or a probe max |A (X v) - v| / max |v| of the finished
-// inverse above kInverseProbeBar (1e-5), sends the inversion back to the full
-// search.
+// The FP32 inverse (a preconditioner that FP64 refinement corrects) first restricts
+// step 1's search to the panel's diagonal block, which needs no row swaps outside the
+// panel and fits in three launches per panel (invert_blockpiv_f32).  On the
+// boundary-element LHS the column maximum lies in that block (diagonal dominance), so
+// the pivots are the same; a zero pivot in the block, or a probe
+// max |A (X v) - v| / max |v| of the finished inverse above kInverseProbeBar (1e-5),
+// sends the inversion back to the full search.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -560,146 +560,6 @@ __global__ void k_permute_cols_t(T* __restrict__ A, int n, const int* __restrict
     }
 }
 
-// Pivot sequence of the panel with the search restricted to its diagonal block:
-// LU with partial pivoting (largest magnitude, lowest row on ties) of the bw x bw
-// block A[k0:k0+bw, k0:k0+bw] in shared memory, one CTA.  Writes perm[k0 + c] as
-// the tall-panel kernels do; a zero pivot sets *status = 2 (the caller retries
-// with the full search).
-template <typename T, int BW>
-__global__ void __launch_bounds__(256) k_block_pivots(const T* __restrict__ A, int n, int k0,
-                                                      int bw, int* __restrict__ perm,
-                                                      int* __restrict__ status) {
-    __shared__ T ws[BW][BW + 1];
-    __shared__ int s_p;
-    for (int idx = threadIdx.x; idx < BW * BW; idx += blockDim.x) {
-        const int r = idx / BW, c = idx % BW;
-        ws[r][c] = (r < bw && c < bw) ? A[(size_t)(k0 + r) * n + k0 + c] : T(0);
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    for (int c = 0; c < bw; c++) {
-        if (threadIdx.x < 32) {  // warp 0: argmax of |ws[r][c]|, r in [c, bw)
-            T best = T(-1);
-            int bi = bw;
-            for (int r = c + lane; r < bw; r += 32) {
-                const T v = absv(ws[r][c]);
-                if (v > best) { best = v; bi = r; }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const T v2 = __shfl_xor_sync(0xffffffffu, best, o);
-                const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (v2 > best || (v2 == best && i2 < bi)) { best = v2; bi = i2; }
-            }
-            if (lane == 0) s_p = (bi < bw && best != T(0)) ? bi : -1;
-        }
-        __syncthreads();
-        const int p = s_p;
-        if (p < 0) {
-            if (threadIdx.x == 0) *status = 2;
-            return;
-        }
-        if (p != c)
-            for (int j = threadIdx.x; j < BW; j += blockDim.x) {
-                const T t = ws[c][j];
-                ws[c][j] = ws[p][j];
-                ws[p][j] = t;
-            }
-        if (threadIdx.x == 0) perm[k0 + c] = k0 + p;
-        __syncthreads();
-        const T inv = T(1) / ws[c][c];
-        const int nr = bw - c - 1, nc = bw - c;  // rows c+1.., columns c.. (column c -> l)
-        for (int idx = threadIdx.x; idx < nr * nc; idx += blockDim.x) {
-            const int r = c + 1 + idx / nc, j = c + idx % nc;
-            const T l = ws[r][c] * inv;
-            if (j > c) ws[r][j] -= l * ws[c][j];
-        }
-        __syncthreads();
-        for (int r = c + 1 + threadIdx.x; r < bw; r += blockDim.x) ws[r][c] *= inv;
-        __syncthreads();
-    }
-}
-
-// The same pivot sequence (largest magnitude, lowest row on ties) from one warp:
-// the block is copied into shared memory by four warps (asynchronous copies, all in
-// flight together), then warp 0 factors it without block barriers, each lane owning
-// rows lane and lane + 32 (BW = 64).  Each column costs a warp reduction and the
-// lane-parallel row updates instead of four block barriers.
-template <int BW>
-__global__ void __launch_bounds__(128) k_block_pivots_warp(const float* __restrict__ A, int n,
-                                                           int k0, int bw, int* __restrict__ perm,
-                                                           int* __restrict__ status) {
-    static_assert(BW % 32 == 0, "rows per lane");
-    constexpr int RPL = BW / 32;
-    __shared__ float ws[BW][BW + 1];
-#pragma unroll 8
-    for (int idx = threadIdx.x; idx < BW * BW; idx += 128) {
-        const int r = idx / BW, c = idx % BW;
-        if (r < bw && c < bw)
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                             (unsigned)__cvta_generic_to_shared(&ws[r][c])),
-                         "l"(A + (size_t)(k0 + r) * n + k0 + c)
-                         : "memory");
-        else
-            ws[r][c] = 0.f;
-    }
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
-    for (int c = 0; c < bw; c++) {
-        float best = -1.f;
-        int bi = bw;
-#pragma unroll
-        for (int k = 0; k < RPL; k++) {
-            const int r = lane + 32 * k;
-            if (r >= c && r < bw) {
-                const float v = fabsf(ws[r][c]);
-                if (v > best) {
-                    best = v;
-                    bi = r;
-                }
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-            const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (v2 > best || (v2 == best && i2 < bi)) {
-                best = v2;
-                bi = i2;
-            }
-        }
-        const int p = (bi < bw && best != 0.f) ? bi : -1;  // the same on every lane
-        if (p < 0) {
-            if (lane == 0) *status = 2;
-            return;
-        }
-        if (p != c) {
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                const int j = lane + 32 * k;
-                const float t = ws[c][j];
-                ws[c][j] = ws[p][j];
-                ws[p][j] = t;
-            }
-        }
-        if (lane == 0) perm[k0 + c] = k0 + p;
-        __syncwarp();
-        const float inv = 1.f / ws[c][c];
-#pragma unroll
-        for (int k = 0; k < RPL; k++) {
-            const int r = lane + 32 * k;
-            if (r > c && r < bw) {
-                const float l = ws[r][c] * inv;
-                for (int j = c + 1; j < BW; j++) ws[r][j] -= l * ws[c][j];
-                ws[r][c] = l;
-            }
-        }
-        __syncwarp();
-    }
-}
-
 // Probe of an FP32 inverse X of A64: y = X v, then err = max_i |(A64 y)_i - v_i|
 // (v_i = (i mod 13) - 6.5, max |v| = 6.5), as the float bits of a non-negative
 // value (integer max preserves the order).  Warp per row.
@@ -862,7 +722,7 @@ cudaError_t pivot_attributes() {
 
 template <typename T, int BW>
 cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, long long* nlaunch,
-                           bool* singular, cudaStream_t s, bool restricted = false) {
+                           bool* singular, cudaStream_t s) {
     *singular = false;
     {
         const cudaError_t ea = pivot_attributes<T, BW>();
@@ -887,13 +747,6 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
         int kk0 = k0, kbw = bw, kn = n;
         const T* cA = A;
         bool done = false;
-        if (restricted) {
-            if constexpr (std::is_same<T, float>::value && BW == 64)
-                k_block_pivots_warp<BW><<<1, 128, 0, s>>>(A, n, k0, bw, perm, d_status);
-            else
-                k_block_pivots<T, BW><<<1, 256, 0, s>>>(A, n, k0, bw, perm, d_status);
-            done = true;
-        }
         // the panel in one cluster's distributed shared memory when it fits
         for (int cs : {16, 8}) {
             if (done) break;
@@ -968,10 +821,285 @@ cudaError_t invert_blocked(T* A, int n, int* perm, int* d_status, T* scratch, lo
     return e;
 }
 
+// ---------------------------------------------------------------------------
+// The FP32 inverse with the pivot search restricted to the panels' diagonal blocks,
+// in three launches per 64-column panel.  With the swaps confined to the panel's own
+// rows R1, and those rows overwritten by the panel step, the step needs only the
+// inverse of the unpermuted diagonal block A11 (with P the block's row permutation,
+// (P A11)^-1 P A[R1, :] = A11^-1 A[R1, :], and the column exchange the swaps imply
+// on A[:, C1] cancels against the permutation of the finished inverse's columns):
+//   T12 = A11^-1 A[R1, :],    A[i, j] -= A[i, C1] T12[:, j]   (i not in R1, j not in C1)
+//   A[R1, :] = T12 with A[R1, C1] = A11^-1,   A[i, C1] = -A[i, C1] A11^-1  (i not in R1)
+// which is block Gauss-Jordan without swaps between panels: the finished matrix is
+// A^-1 with no column permutation.  Per panel:
+//   k_block_inverse_f32  (one CTA) A11^-1, Gauss-Jordan with partial pivoting;
+//   k_panel_b_f32        B = [T12 | A11^-1] (64 x n) and Pc = A[:, C1]^T (64 x n);
+//   k_panel_step_f32     every 128 x 64 tile of A from Pc^T B: the trailing update,
+//                        the pivot rows and the panel columns in one pass.
+// Each block fits in a fourth of an SM (16K registers, <= 34 KB of shared memory), so
+// that beside the assembly's kernels it waits for one block of theirs to retire.
+// ---------------------------------------------------------------------------
+constexpr int kGjThreads = 256;
+
+// A11^-1 of the panel's diagonal block (bw x bw, padded to 64 x 64 with the
+// identity) by in-place Gauss-Jordan with partial pivoting among the rows not yet
+// pivoted (largest magnitude, lowest row on ties), rows left in place: at step c the
+// pivot row p_c is scaled and column c eliminated from every other row, and column
+// c's storage then holds the transformed identity column p_c.  The result S gives
+// A11^-1[c][j] = S[p_c][q] with p_q = j.  Double-buffered in shared memory (two
+// barriers per column); thread t updates 16 entries of row t / 4.  A zero pivot sets
+// *status = 2.
+__global__ void __launch_bounds__(kGjThreads) k_block_inverse_f32(const float* __restrict__ A,
+                                                                  int n, int k0, int bw,
+                                                                  float* __restrict__ Ainv,
+                                                                  int* __restrict__ status) {
+    if (*status) return;
+    __shared__ float sm[2][64][65];
+    __shared__ int s_p[64], s_pinv[64], s_used[64];
+    __shared__ float s_piv;
+    const int t = threadIdx.x;
+    for (int idx = t; idx < 64 * 64; idx += kGjThreads) {
+        const int r = idx >> 6, c = idx & 63;
+        sm[0][r][c] = (r < bw && c < bw) ? A[(size_t)(k0 + r) * n + k0 + c]
+                                         : (r == c ? 1.f : 0.f);
+    }
+    if (t < 64) s_used[t] = 0;
+    __syncthreads();
+    const int r = t >> 2, q0 = (t & 3) * 16;
+    int cur = 0;
+    for (int c = 0; c < 64; c++) {
+        float(*X)[65] = sm[cur];
+        float(*Y)[65] = sm[cur ^ 1];
+        if (t < 32) {
+            const float v0 = s_used[t] ? -1.f : fabsf(X[t][c]);
+            const float v1 = s_used[t + 32] ? -1.f : fabsf(X[t + 32][c]);
+            float best = v0;
+            int bi = t;
+            if (v1 > best) {
+                best = v1;
+                bi = t + 32;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+                const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (v2 > best || (v2 == best && i2 < bi)) {
+                    best = v2;
+                    bi = i2;
+                }
+            }
+            if (t == 0) {
+                s_p[c] = best > 0.f ? bi : -1;
+                if (best > 0.f) {
+                    s_used[bi] = 1;
+                    s_piv = 1.f / X[bi][c];
+                }
+            }
+        }
+        __syncthreads();
+        const int p = s_p[c];
+        if (p < 0) {  // the same on every thread
+            if (t == 0) *status = 2;
+            return;
+        }
+        const float piv = s_piv;
+        const float f = X[r][c];
+#pragma unroll
+        for (int jj = 0; jj < 16; jj++) {
+            const int j = q0 + jj;
+            const float rp = (j == c ? 1.f : X[p][j]) * piv;
+            Y[r][j] = r == p ? rp : (j == c ? 0.f : X[r][j]) - f * rp;
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (t < 64) s_pinv[s_p[t]] = t;
+    __syncthreads();
+#pragma unroll
+    for (int jj = 0; jj < 16; jj++) {
+        const int q = q0 + jj;
+        Ainv[s_pinv[r] * 64 + s_p[q]] = sm[cur][r][q];
+    }
+}
+
+// B[c][j] = sum_d Ainv[c][d] A[k0 + d][j] (T12) for j outside the panel columns and
+// Ainv[c][j - k0] inside them; Pc[c][i] = A[i][k0 + c].  Thread per column j (and
+// per row i = j for Pc); rows c >= bw of B and Pc come out zero (Ainv is the
+// identity there and the panel's columns beyond bw are zero).  ld: the leading
+// dimension of B and Pc.
+__global__ void __launch_bounds__(128) k_panel_b_f32(const float* __restrict__ A, int n, int k0,
+                                                     int bw, const float* __restrict__ Ainv,
+                                                     float* __restrict__ B,
+                                                     float* __restrict__ Pc, int ld,
+                                                     const int* __restrict__ status) {
+    if (*status) return;
+    __shared__ float sa[64 * 64];
+    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) sa[i] = Ainv[i];
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+#pragma unroll 16
+    for (int c = 0; c < 64; c++) Pc[(size_t)c * ld + j] = c < bw ? A[(size_t)j * n + k0 + c] : 0.f;
+    if (j >= k0 && j < k0 + bw) {
+        for (int c = 0; c < 64; c++) B[(size_t)c * ld + j] = sa[c * 64 + (j - k0)];
+        return;
+    }
+    float a[64];
+#pragma unroll
+    for (int d = 0; d < 64; d++) a[d] = d < bw ? A[(size_t)(k0 + d) * n + j] : 0.f;
+    for (int c = 0; c < 64; c++) {
+        float acc = 0.f;
+#pragma unroll
+        for (int d = 0; d < 64; d++) acc = fmaf(sa[c * 64 + d], a[d], acc);
+        B[(size_t)c * ld + j] = acc;
+    }
+}
+
+// One tile of the panel step, 128 rows x 64 columns, 128 threads (8 x 8 outputs
+// each): acc = Pc[:, i0..]^T B[:, j0..] over the 64 panel columns in two halves of 32
+// (25.6 KB of shared memory), then per entry (i, j): a pivot row i takes
+// B[i - k0][j]; a panel column j (other rows) takes -acc; the rest A[i][j] - acc
+// (their reads issued two rows at a time before the writes).  16K registers and
+// 25.6 KB of shared memory per block.
+constexpr int kStepTM = 128, kStepTN = 64, kStepKH = 32;
+constexpr int kStepLP = kStepTM + 4, kStepLT = kStepTN + 4;
+constexpr int kStepSmem = kStepKH * (kStepLP + kStepLT) * (int)sizeof(float);
+
+__global__ void __launch_bounds__(128) k_panel_step_f32(float* __restrict__ A, int n, int k0,
+                                                        int bw, const float* __restrict__ B,
+                                                        const float* __restrict__ Pc, int ld,
+                                                        const int* __restrict__ status) {
+    if (*status) return;
+    __shared__ __align__(16) float sP[kStepKH * kStepLP];  // [c][r]
+    __shared__ __align__(16) float sT[kStepKH * kStepLT];  // [c][q]
+    const int i0 = blockIdx.y * kStepTM, j0 = blockIdx.x * kStepTN;
+    const int tid = threadIdx.x;
+    const int tx = tid % 8, ty = tid / 8;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 8; b++) acc[a][b] = 0.f;
+    for (int h0 = 0; h0 < 64; h0 += kStepKH) {
+        if (h0) __syncthreads();  // the first half's reads are done
+#pragma unroll
+        for (int it = 0; it < kStepKH * kStepTM / 128; it++) {
+            const int idx = tid + it * 128;
+            const int c = idx / kStepTM, q = idx % kStepTM;
+            if (i0 + q < n) cp_async4(sP + c * kStepLP + q, Pc + (size_t)(h0 + c) * ld + i0 + q);
+            else sP[c * kStepLP + q] = 0.f;
+        }
+#pragma unroll
+        for (int it = 0; it < kStepKH * kStepTN / 128; it++) {
+            const int idx = tid + it * 128;
+            const int c = idx / kStepTN, q = idx % kStepTN;
+            if (j0 + q < n) cp_async4(sT + c * kStepLT + q, B + (size_t)(h0 + c) * ld + j0 + q);
+            else sT[c * kStepLT + q] = 0.f;
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();
+#pragma unroll 4
+        for (int c = 0; c < kStepKH; c++) {
+            const float4 p0 = *reinterpret_cast<const float4*>(sP + c * kStepLP + ty * 4);
+            const float4 p1 = *reinterpret_cast<const float4*>(sP + c * kStepLP + ty * 4 + 64);
+            const float4 t0 = *reinterpret_cast<const float4*>(sT + c * kStepLT + tx * 4);
+            const float4 t1 = *reinterpret_cast<const float4*>(sT + c * kStepLT + tx * 4 + 32);
+            const float pa[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+            const float tb[8] = {t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z, t1.w};
+#pragma unroll
+            for (int a = 0; a < 8; a++)
+#pragma unroll
+                for (int b = 0; b < 8; b++) acc[a][b] = fmaf(pa[a], tb[b], acc[a][b]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float cv[2][8];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int a = 2 * q + h;
+            const int i = i0 + ty * 4 + (a & 3) + (a >> 2) * 64;
+            const bool rest_row = i < n && !(i >= k0 && i < k0 + bw);
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int j = j0 + tx * 4 + (b & 3) + (b >> 2) * 32;
+                const bool rest = rest_row && j < n && !(j >= k0 && j < k0 + bw);
+                cv[h][b] = rest ? A[(size_t)i * n + j] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int a = 2 * q + h;
+            const int i = i0 + ty * 4 + (a & 3) + (a >> 2) * 64;
+            if (i >= n) continue;
+            const bool pivot_row = i >= k0 && i < k0 + bw;
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int j = j0 + tx * 4 + (b & 3) + (b >> 2) * 32;
+                if (j >= n) continue;
+                float v;
+                if (pivot_row) v = B[(size_t)(i - k0) * ld + j];
+                else if (j >= k0 && j < k0 + bw) v = -acc[a][b];
+                else v = cv[h][b] - acc[a][b];
+                A[(size_t)i * n + j] = v;
+            }
+        }
+    }
+}
+
+// The three-launch FP32 inversion (above) in place; *singular on a zero pivot in a
+// diagonal block.  scratch holds B and Pc (64 x ld each, ld = n rounded up to 4) and
+// the block inverse (64 x 64).
+cudaError_t invert_blockpiv_f32(float* A, int n, int* d_status, float* scratch,
+                                long long* nlaunch, bool* singular, cudaStream_t s) {
+    *singular = false;
+    const int ld = (n + 3) & ~3;
+    float* B = scratch;
+    float* Pc = B + (size_t)64 * ld;
+    float* Ainv = Pc + (size_t)64 * ld;
+    // prefer the largest shared-memory carveout, so that these blocks fit beside the
+    // assembly's blocks on an SM
+    static const cudaError_t ea = [] {
+        const void* fns[3] = {(const void*)k_block_inverse_f32, (const void*)k_panel_b_f32,
+                              (const void*)k_panel_step_f32};
+        for (const void* fn : fns) {
+            const cudaError_t r = cudaFuncSetAttribute(
+                fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+            if (r != cudaSuccess) return r;
+        }
+        return cudaSuccess;
+    }();
+    if (ea != cudaSuccess) return ea;
+    cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    for (int k0 = 0; k0 < n; k0 += 64) {
+        const int bw = std::min(64, n - k0);
+        k_block_inverse_f32<<<1, kGjThreads, 0, s>>>(A, n, k0, bw, Ainv, d_status);
+        k_panel_b_f32<<<(n + 127) / 128, 128, 0, s>>>(A, n, k0, bw, Ainv, B, Pc, ld, d_status);
+        k_panel_step_f32<<<dim3((n + kStepTN - 1) / kStepTN, (n + kStepTM - 1) / kStepTM), 128, 0,
+                           s>>>(A, n, k0, bw, B, Pc, ld, d_status);
+        *nlaunch += 3;
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int status = 0;
+    e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    *singular = status != 0;
+    return cudaSuccess;
+}
+
 }  // namespace
 
 size_t inverse_scratch_elems(int n) {
-    return (size_t)2 * 64 * n + 64 * 64 + 2 * kMaxPivotBlocks + 2 * (kMaxPivotBlocks + 1) * 64;
+    // the panel kernels' T12 and permutation rows, the diagonal-block inverse and the
+    // pivot candidates; the three-launch FP32 form's B and Pc (64 x ld each, ld = n
+    // rounded up to 4) and block inverse
+    const size_t blocked =
+        (size_t)2 * 64 * n + 64 * 64 + 2 * kMaxPivotBlocks + 2 * (kMaxPivotBlocks + 1) * 64;
+    const size_t blockpiv = (size_t)2 * 64 * (size_t)((n + 3) & ~3) + 64 * 64;
+    return std::max(blocked, blockpiv);
 }
 
 cudaError_t invert_f64(double* A, int n, int* perm, int* d_status, double* scratch,
@@ -1121,8 +1249,7 @@ cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_sta
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
     // first with the pivot search in the panels' diagonal blocks, then checked
-    cudaError_t e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular,
-                                              s, true);
+    cudaError_t e = invert_blockpiv_f32(A, n, d_status, scratch, nlaunch, singular, s);
     if (e != cudaSuccess) return e;
     float rel = 3.0e38f;
     if (!*singular) {
@@ -1137,7 +1264,7 @@ cudaError_t invert_f32(const double* A64, float* A, int n, int* perm, int* d_sta
     // a zero pivot in a diagonal block or a residual above the bar: the full search
     k_cast_f64_f32<<<1216, 256, 0, s>>>(A64, A, (size_t)n * n);
     *nlaunch += 1;
-    e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s, false);
+    e = invert_blocked<float, 64>(A, n, perm, d_status, scratch, nlaunch, singular, s);
     if (e != cudaSuccess || *singular || !report) return e;
     report->full_search = 1;
     return probe_inverse(A64, A, n, scratch, &report->probe_rel, nlaunch, s);
