@@ -77,7 +77,7 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
             CUDA_TRY(cudaMalloc(&c->d_tc_W, wb));
             c->tc_W_bytes = wb;
         }
-        if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_tc_W, C, Lw, &c->tc_maps, 1))
+        if (!make_tc_maps(c->d_mtc_planes, D, mtc_slabs(M), c->d_tc_W, C, Lw, &c->tc_maps, 1))
             return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the batched planes");
         if (!c->d_bkt) {
             CUDA_TRY(dalloc(&c->d_bkt, 2 * CD));
@@ -111,7 +111,7 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
             const int splits = tc_conv_splits(nlev, D, C, 1 << 30, 1);
             const double ldb = tc_ldb(D), cp = tc_cases_pad(C);
             pe = prof_begin(c, TDBEM_K_CONV_BATCH);
-            CUDA_TRY(launch_conv_tc(c->tc_maps, D, M + 1, Lw, nlev, C, c->d_bpart, splits,
+            CUDA_TRY(launch_conv_tc(c->tc_maps, D, mtc_slabs(M), Lw, nlev, C, c->d_bpart, splits,
                                     c->d_tc_err, s, 1, c->tc_wait_ns));
             prof_end(c, pe, nlev * (double)D * ldb * 4 + nlev * cp * ldb * 4,
                      nlev * 2.0 * DD * C);

@@ -171,7 +171,7 @@ int ensure_merged_levels(tdbem_ctx* c) {
     cudaStream_t s = c->stream;
     if (c->mtc_planes_valid) return TDBEM_OK;
     if (!c->d_mtc_planes)
-        CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, M + 1, 1)));
+        CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, mtc_slabs(M), 1)));
     if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
     if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
     // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
@@ -194,12 +194,32 @@ int ensure_merged_levels(tdbem_ctx* c) {
     CUDA_TRY(cudaMemcpyAsync(c->d_mtc_bc, bcv.data(), sizeof(float) * bcv.size(),
                              cudaMemcpyHostToDevice, s));
     const int pe = prof_begin(c, TDBEM_K_AUX);
-    CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, c->d_is_ubc,
-                                 c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
+    CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, mtc_slabs(M),
+                                 c->d_is_ubc, c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
                                  c->d_mtc_planes, c->d_mtc_known, s));
     prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
     c->launches += 1;
     c->mtc_planes_valid = true;
+    c->mtc_steps_valid = false;  // the step-distance matrices follow the levels
+    return TDBEM_OK;
+}
+
+// The planes' step-distance matrices B_1 .. B_kStepMats for the weights (a1, a2):
+// after every merge and when the weights change.
+int ensure_step_mats(tdbem_ctx* c, double a1, double a2) {
+    if (c->mtc_steps_valid && c->mtc_step_key[0] == a1 && c->mtc_step_key[1] == a2)
+        return TDBEM_OK;
+    const int pe = prof_begin(c, TDBEM_K_AUX);
+    CUDA_TRY(launch_step_mats(c->d_Gf, c->d_Hf, c->ldf, c->D, c->M, mtc_slabs(c->M), c->d_is_ubc,
+                              a1, a2, 1 - a1 - a2, c->d_mtc_planes, c->stream));
+    prof_end(c, pe,
+             std::min(c->M + 1, kStepMats + 2) * (double)c->D * 2.0 * c->ldf * 4 +
+                 kStepMats * (double)c->D * tc_ldb(c->D) * 4,
+             0);
+    c->launches += 1;
+    c->mtc_step_key[0] = a1;
+    c->mtc_step_key[1] = a2;
+    c->mtc_steps_valid = true;
     return TDBEM_OK;
 }
 
@@ -243,7 +263,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     const bool tc = c->march_engine == TDBEM_ENGINE_TCGEN05;
     const int Lw = M + 1;
     if (tc) {
-        const int rm = ensure_merged_levels(c);
+        int rm = ensure_merged_levels(c);
+        if (rm == TDBEM_OK) rm = ensure_step_mats(c, a1, a2);
         if (rm != TDBEM_OK) return rm;
         std::vector<double> key = {(double)numstep, (double)(M + 1), a1, a2,
                                    lhs_c[1][0], lhs_c[1][1]};
@@ -279,7 +300,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         }
         if (c->mtc_maps_for[0] != c->d_mtc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
             c->mtc_nb != nb) {
-            if (!make_tc_maps(c->d_mtc_planes, D, M + 1, c->d_mtc_W, nb, Lw, &c->mtc_maps, 1))
+            if (!make_tc_maps(c->d_mtc_planes, D, mtc_slabs(M), c->d_mtc_W, nb, Lw, &c->mtc_maps,
+                              1))
                 return fail(TDBEM_ERR_CUDA, "cuTensorMapEncodeTiled failed for the march planes");
             c->mtc_maps_for[0] = c->d_mtc_planes;
             c->mtc_maps_for[1] = c->d_mtc_W;
@@ -326,8 +348,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                 // d_pmix holds (M+1) x nb x D partial sums
                 const int splits = tc_conv_splits(nlev, D, nbe, (M + 1) * nb / nbe, 1);
                 const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
-                CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, nbe, c->d_pmix, splits,
-                                        c->d_tc_err, s, 1, c->tc_wait_ns));
+                CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, nbe, c->d_pmix,
+                                        splits, c->d_tc_err, s, 1, c->tc_wait_ns));
                 prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                     nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                          nlev * 2.0 * nbe * (double)DD);
@@ -357,13 +379,28 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         const int nbp = ncol <= 1 ? 1 : ncol <= 2 ? 2 : ncol <= 4 ? 4 : ncol <= 8 ? 8 : 16;
         const int nlev = std::min(M, e - a) + 1;
         double* y = c->d_Yold + (size_t)(b - S) * D;
+        const int nm = e - a - 1;  // step-distance matrices B_1 .. B_(e-a-1)
+        if (tc && nm <= std::min(kStepMats, Lw)) {
+            CUDA_TRY(launch_build_w_steps(c->d_u, c->d_t, c->d_is_ubc, D, a, b, ncol, nb, nm, Lw,
+                                          c->d_mtc_W, s));
+            const int splits = tc_conv_splits(nm, D, ncol, (M + 1) * nb / ncol, 1);
+            const int pe = prof_begin(c, TDBEM_K_CONV);
+            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nm, ncol, c->d_pmix, splits,
+                                    c->d_tc_err, s, 1, c->tc_wait_ns, M + 1));
+            prof_end(c, pe, nm * (double)D * tc_ldb(D) * 4 +
+                                nm * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                     nm * 2.0 * ncol * (double)DD);
+            CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s));
+            c->launches += 3;
+            return TDBEM_OK;
+        }
         if (tc) {
             CUDA_TRY(launch_build_w_merged(c->d_u, c->d_t, c->d_is_ubc, D, b, ncol, nb, a, b,
                                            nlev, Lw, a1, a2, a3, c->d_mtc_W, s));
             const int splits = tc_conv_splits(nlev, D, ncol, (M + 1) * nb / ncol, 1);
             const int pe = prof_begin(c, TDBEM_K_CONV);
-            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, M + 1, Lw, nlev, ncol, c->d_pmix, splits,
-                                    c->d_tc_err, s, 1, c->tc_wait_ns));
+            CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, ncol, c->d_pmix,
+                                    splits, c->d_tc_err, s, 1, c->tc_wait_ns));
             prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                 nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                      nlev * 2.0 * ncol * (double)DD);

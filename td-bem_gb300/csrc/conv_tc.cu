@@ -170,7 +170,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               int D, int L, int Lw, int nlev, int nk, int nmat, int C,
-              double* __restrict__ partial, int* __restrict__ err, unsigned long long wait_ns) {
+              double* __restrict__ partial, int* __restrict__ err, unsigned long long wait_ns,
+              int lev0) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
@@ -230,8 +231,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 const uint32_t st = sbase + s * TC_STAGE_BYTES;
                 mbar_expect_tx(bar(FULL + s), TC_STAGE_BYTES);
                 const int x = kc * TC_BK;
-                tma_load_3d(st, &tmA, x, row0, (mat * 2 + 0) * L + f, bar(FULL + s));
-                tma_load_3d(st + TC_A_BYTES, &tmA, x, row0, (mat * 2 + 1) * L + f, bar(FULL + s));
+                tma_load_3d(st, &tmA, x, row0, (mat * 2 + 0) * L + lev0 + f, bar(FULL + s));
+                tma_load_3d(st + TC_A_BYTES, &tmA, x, row0, (mat * 2 + 1) * L + lev0 + f,
+                            bar(FULL + s));
                 tma_load_3d(st + 2 * TC_A_BYTES, &tmB, x, c0, (mat * 2 + 0) * Lw + f,
                             bar(FULL + s));
                 tma_load_3d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, x, c0, (mat * 2 + 1) * Lw + f,
@@ -391,7 +393,7 @@ bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* ou
 
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
                            double* partial, int splits, int* d_err, cudaStream_t s, int nmat,
-                           unsigned long long wait_ns) {
+                           unsigned long long wait_ns, int lev0) {
     static unsigned long long attr_set = 0;  // devices with the shared-memory attribute set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -402,15 +404,15 @@ cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, i
         if (e != cudaSuccess) return e;
         attr_set |= 1ull << dev;
     }
-    if (splits < 1 || nlev < 1 || nlev > L || nlev > Lw || (nmat != 1 && nmat != 2) ||
-        wait_ns == 0)
+    if (splits < 1 || nlev < 1 || lev0 < 0 || lev0 + nlev > L || nlev > Lw ||
+        (nmat != 1 && nmat != 2) || wait_ns == 0)
         return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
     std::memcpy(&ma, maps.a, sizeof(ma));
     std::memcpy(&mb, maps.b, sizeof(mb));
     dim3 grid((D + TC_BM - 1) / TC_BM, splits, (C + TC_BN - 1) / TC_BN);
     k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, tc_ldb(D) / TC_BK, nmat,
-                                                C, partial, d_err, wait_ns);
+                                                C, partial, d_err, wait_ns, lev0);
     return cudaGetLastError();
 }
 

@@ -36,17 +36,17 @@ __device__ __forceinline__ int col_sel(const unsigned char* __restrict__ is_u, i
     return 2;
 }
 
-// FP32 levels [f][row][ldf] -> merged planes [plane*L + f][row][ldb] and the known
-// part's vectors known[(v*L + f)*D + row], v = 0 pt, 1 pl, 2 pu.  Warp per
+// FP32 levels [f][row][ldf] -> merged planes [plane*slabs + f][row][ldb] and the
+// known part's vectors known[(v*L + f)*D + row], v = 0 pt, 1 pl, 2 pu.  Warp per
 // (f, row), 4 columns per lane (16-byte loads of G and H, 8-byte stores per
 // plane); FP32 products, FP64 warp sums.
 __global__ void __launch_bounds__(256) k_merge_levels(
-    const float* __restrict__ Gf, const float* __restrict__ Hf, int ldf, int D, int L, int ldb,
-    const unsigned char* __restrict__ is_u, const float* __restrict__ kt,
+    const float* __restrict__ Gf, const float* __restrict__ Hf, int ldf, int D, int L, int slabs,
+    int ldb, const unsigned char* __restrict__ is_u, const float* __restrict__ kt,
     const float* __restrict__ lt, const float* __restrict__ lu, __nv_bfloat16* __restrict__ P,
     double* __restrict__ known) {
     const size_t rows = (size_t)L * D;
-    const size_t plane = rows * ldb;
+    const size_t plane = (size_t)slabs * D * ldb;
     const int lane = threadIdx.x & 31;
     const size_t nwarps = (size_t)gridDim.x * (blockDim.x >> 5);
     for (size_t fr = (size_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); fr < rows;
@@ -89,6 +89,82 @@ __global__ void __launch_bounds__(256) k_merge_levels(
             known[((size_t)lane * L + f) * D + row] = lane == 0 ? v[0] : lane == 1 ? v[1] : v[2];
         }
     }
+}
+
+// Step-distance matrices B_d (d = 1 .. kStepMats) into slabs M + d of the planes:
+//   B_1 = (a2 - a1) A^0 + a3 A^1 + a1 A^2,   B_d = a2 A^(d-1) + a3 A^d + a1 A^(d+1)
+// (A^f = 0 beyond level M), the weights with which w_of combines the history of
+// step m into level f of step m + d.  Warp per row, 4 columns per lane: the lane
+// walks levels 0 .. kStepMats + 1 with the last two merged values kept, so every
+// level is read once; FP32 sums of the FP32 levels, then the BF16 hi/lo split.
+__global__ void __launch_bounds__(256) k_step_mats(
+    const float* __restrict__ Gf, const float* __restrict__ Hf, int ldf, int D, int M, int slabs,
+    int ldb, const unsigned char* __restrict__ is_u, float a1, float a2, float a3,
+    __nv_bfloat16* __restrict__ P) {
+    const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (row >= D) return;
+    const size_t plane = (size_t)slabs * D * ldb;
+    const size_t lstride = (size_t)D * ldf;
+    for (int k = 4 * lane; k < ldb; k += 128) {
+        int sel[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) sel[q] = col_sel(is_u, k + q, D);
+        float am2[4] = {0.f, 0.f, 0.f, 0.f}, am1[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int f = 0; f <= kStepMats + 1; f++) {
+            float a[4] = {0.f, 0.f, 0.f, 0.f};
+            if (f <= M && k < ldf) {
+                const float4 x =
+                    __ldcs(reinterpret_cast<const float4*>(Gf + f * lstride + (size_t)row * ldf + k));
+                const float4 y =
+                    __ldcs(reinterpret_cast<const float4*>(Hf + f * lstride + (size_t)row * ldf + k));
+                const float gv[4] = {x.x, x.y, x.z, x.w}, hv[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    a[q] = sel[q] == 1 ? gv[q] : sel[q] == 2 ? -hv[q] : 0.f;
+            }
+            if (f >= 2) {  // B_(f-1) from levels f - 2, f - 1, f
+                const int d = f - 1;
+                const float c0 = d == 1 ? a2 - a1 : a2;
+                __align__(8) __nv_bfloat16 hb[4], lb[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const float b = fmaf(c0, am2[q], fmaf(a3, am1[q], a1 * a[q]));
+                    hb[q] = __float2bfloat16_rn(b);
+                    lb[q] = __float2bfloat16_rn(__fsub_rn(b, __bfloat162float(hb[q])));
+                }
+                const size_t off = ((size_t)(M + d) * D + row) * ldb + k;
+                *reinterpret_cast<uint2*>(P + off) = *reinterpret_cast<const uint2*>(hb);
+                *reinterpret_cast<uint2*>(P + plane + off) = *reinterpret_cast<const uint2*>(lb);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                am2[q] = am1[q];
+                am1[q] = a[q];
+            }
+        }
+    }
+}
+
+// History planes of the step-distance matrices for the steps b + j (j < ncol) from
+// the history steps [a, b): slab d - 1, column j holds the unknowns' history
+// x_(b + j - d) (t where t is the unknown, u where u is; zero beyond D and outside
+// [a, b)).  Columns ncol..Cpad-1 are left as they are.  Grid (K tiles, ncol, nmats).
+__global__ void __launch_bounds__(256) k_build_w_steps(
+    const double* __restrict__ u_hist, const double* __restrict__ t_hist,
+    const unsigned char* __restrict__ is_u, int D, int a, int b, int Cpad, int Lw, int ldb,
+    __nv_bfloat16* __restrict__ W) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, d = blockIdx.z + 1;
+    if (k >= ldb) return;
+    const int m = b + j - d;
+    double w = 0;
+    const int sel = col_sel(is_u, k, D);
+    if (sel && m >= a && m < b) w = (sel == 1 ? t_hist : u_hist)[(size_t)m * D + k];
+    const size_t idx = ((size_t)(d - 1) * Cpad + j) * ldb + k;
+    const size_t plane = (size_t)Lw * Cpad * ldb;
+    const __nv_bfloat16 h = __float2bfloat16_rn((float)w);
+    W[idx] = h;
+    W[plane + idx] = __float2bfloat16_rn((float)(w - (double)__bfloat162float(h)));
 }
 
 // x's history combination of level f for step s over history steps [lo, hi)
@@ -265,14 +341,38 @@ cudaError_t launch_known_batch(const float* GK, const float* GL, const double* H
 }
 
 cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
-                                const unsigned char* is_u, const float* kt, const float* lt,
-                                const float* lu, void* planes, double* known, cudaStream_t s) {
+                                int slabs, const unsigned char* is_u, const float* kt,
+                                const float* lt, const float* lu, void* planes, double* known,
+                                cudaStream_t s) {
     const int ldb = tc_ldb(D);
-    if (ldf % 4 != 0 || ldf > ldb) return cudaErrorInvalidValue;  // float4 rows inside ldb
+    if (ldf % 4 != 0 || ldf > ldb || slabs < L) return cudaErrorInvalidValue;
     const size_t rows = (size_t)L * D;
     const unsigned grid = (unsigned)std::min<size_t>((rows + 7) / 8, 152 * 8);
-    k_merge_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, ldb, is_u, kt, lt, lu,
+    k_merge_levels<<<grid, 256, 0, s>>>(Gf, Hf, ldf, D, L, slabs, ldb, is_u, kt, lt, lu,
                                         static_cast<__nv_bfloat16*>(planes), known);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_mats(const float* Gf, const float* Hf, int ldf, int D, int M, int slabs,
+                             const unsigned char* is_u, double a1, double a2, double a3,
+                             void* planes, cudaStream_t s) {
+    const int ldb = tc_ldb(D);
+    if (ldf % 4 != 0 || ldf > ldb || slabs < M + 1 + kStepMats) return cudaErrorInvalidValue;
+    k_step_mats<<<(D + 7) / 8, 256, 0, s>>>(Gf, Hf, ldf, D, M, slabs, ldb, is_u, (float)a1,
+                                            (float)a2, (float)a3,
+                                            static_cast<__nv_bfloat16*>(planes));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_build_w_steps(const double* u_hist, const double* t_hist,
+                                 const unsigned char* is_u, int D, int a, int b, int ncol,
+                                 int Cmax, int nmats, int Lw, void* W, cudaStream_t st) {
+    if (ncol < 1 || ncol > Cmax || nmats < 1 || nmats > Lw || nmats > kStepMats)
+        return cudaErrorInvalidValue;
+    const int Cpad = tc_cases_pad(Cmax), ldb = tc_ldb(D);
+    const dim3 grid((ldb + 255) / 256, ncol, nmats);
+    k_build_w_steps<<<grid, 256, 0, st>>>(u_hist, t_hist, is_u, D, a, b, Cpad, Lw, ldb,
+                                          static_cast<__nv_bfloat16*>(W));
     return cudaGetLastError();
 }
 

@@ -297,14 +297,34 @@ bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* ou
                   int nmat = 1);
 // Default limit of each pipeline wait of k_conv_tc (2 s of %globaltimer).
 constexpr unsigned long long kTcWaitNsDefault = 2000000000ull;
+// The product reads level slabs lev0 .. lev0 + nlev - 1 of the planes (L slabs per
+// plane) with the vector slabs 0 .. nlev - 1.
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
                            double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 1,
-                           unsigned long long wait_ns = kTcWaitNsDefault);
+                           unsigned long long wait_ns = kTcWaitNsDefault, int lev0 = 0);
 
 // Mixed march with merged levels on tcgen05 (march_tc.cu).
+// The merged planes hold, per plane, the M + 1 level matrices A^f and after them the
+// kStepMats step-distance matrices B_d (d = 1 .. kStepMats): the weight of the
+// history of step m in the right-hand side of step m + d,
+//   B_1 = (a2 - a1) A^0 + a3 A^1 + a1 A^2,   B_d = a2 A^(d-1) + a3 A^d + a1 A^(d+1),
+// which the in-block cross terms of time blocks of up to kStepMats + 1 steps read
+// instead of the levels (two matrices fewer per cross term).
+constexpr int kStepMats = 31;
+inline int mtc_slabs(int M) { return M + 1 + kStepMats; }
 cudaError_t launch_merge_levels(const float* Gf, const float* Hf, int ldf, int D, int L,
-                                const unsigned char* is_u, const float* kt, const float* lt,
-                                const float* lu, void* planes, double* known, cudaStream_t s);
+                                int slabs, const unsigned char* is_u, const float* kt,
+                                const float* lt, const float* lu, void* planes, double* known,
+                                cudaStream_t s);
+// B_1 .. B_kStepMats from the FP32 levels into slabs M + 1 .. of the planes.
+cudaError_t launch_step_mats(const float* Gf, const float* Hf, int ldf, int D, int M, int slabs,
+                             const unsigned char* is_u, double a1, double a2, double a3,
+                             void* planes, cudaStream_t s);
+// History planes of B_1 .. B_nmats for the steps b .. b + ncol - 1 from the history
+// steps [a, b): slab d - 1, column j holds x_(b + j - d) where a <= b + j - d < b.
+cudaError_t launch_build_w_steps(const double* u_hist, const double* t_hist,
+                                 const unsigned char* is_u, int D, int a, int b, int ncol,
+                                 int Cmax, int nmats, int Lw, void* W, cudaStream_t st);
 cudaError_t launch_build_w_merged(const double* u_hist, const double* t_hist,
                                   const unsigned char* is_u, int D, int s0, int ncol, int Cmax,
                                   int lo, int hi, int nlev, int Lw, double a1, double a2,
@@ -498,6 +518,8 @@ struct tdbem_ctx {
     void* d_mtc_planes = nullptr;
     double* d_mtc_known = nullptr;
     bool mtc_planes_valid = false;
+    double mtc_step_key[2] = {-1.0, -1.0};  // (a1, a2) of the planes' step matrices
+    bool mtc_steps_valid = false;
     float* d_mtc_bc = nullptr;
     double* d_mtc_coef = nullptr;
     size_t mtc_coef_cap = 0;

@@ -261,3 +261,22 @@ def test_graph_replay_is_bitwise_the_direct_loop(tdlib, precision):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(out[True][0][0], out[True][1][0])
     assert not np.array_equal(out[True][0][0], out[True][2][0])
+
+
+def test_step_matrices_follow_the_weights(tdlib):
+    """The step-distance matrices of the tcgen05 march (B_d, combinations of three
+    levels with the averaging weights) are rebuilt when the weights change between
+    two marches of one assembly: the second march equals a fresh context's."""
+    from tdbem import meshes
+    m = meshes.cubed_sphere(4, numstep=90)
+    with tdlib.Context(m) as ctx:
+        ctx.set_alpha(0.25, 0.1)
+        ctx.assemble(precision=tdlib.MIXED)
+        ctx.march()
+        ctx.set_alpha(0.3, 0.05)
+        u1, t1 = ctx.march()
+    with tdlib.Context(m) as ctx:
+        ctx.set_alpha(0.3, 0.05)
+        ctx.assemble(precision=tdlib.MIXED)
+        u2, t2 = ctx.march()
+    assert np.array_equal(u1, u2) and np.array_equal(t1, t2)

@@ -99,3 +99,54 @@ def test_merged_levels_equal_the_g_h_form(seed):
             ct, cl, cu = known_coefficients(s, f, a1, a2, a3, amp, c0, c1)
             merged += ct * pt[f] + cl * pl[f] - cu * pu[f]
         np.testing.assert_allclose(merged, direct, rtol=0, atol=1e-11 * np.abs(direct).max())
+
+
+def step_mats(A, nd, a1, a2, a3):
+    """B_1 .. B_nd (k_step_mats in march_tc.cu): the weight of the history of step m
+    in the right-hand side of step m + d; levels beyond the last are zero."""
+    L = A.shape[0]
+    lev = lambda f: A[f] if f < L else np.zeros_like(A[0])
+    B = [(a2 - a1) * lev(0) + a3 * lev(1) + a1 * lev(2)]
+    for d in range(2, nd + 1):
+        B.append(a2 * lev(d - 1) + a3 * lev(d) + a1 * lev(d + 1))
+    return B
+
+
+@pytest.mark.parametrize("L", [4, 40])
+def test_cross_terms_from_step_distance_matrices(L):
+    """The in-block cross terms of the tcgen05 march: the history of steps [a, b)
+    into the right-hand sides of steps b .. e - 1, as levels 0 .. e - a with the
+    w_of combinations (launch_build_w_merged) and as B_1 .. B_(e-a-1) times the raw
+    history (launch_build_w_steps), for every (a, b, e) of the recursive halving of
+    32-step blocks; a short level list (L = 4) checks the zero levels past the
+    last."""
+    rng = np.random.default_rng(7)
+    D = 9
+    a1, a2 = 0.25, 0.1
+    a3 = 1 - a1 - a2
+    A = rng.standard_normal((L, D, D))
+    x = rng.standard_normal((40, D))
+    B = step_mats(A, 31, a1, a2, a3)
+
+    def halves(s0, n, out):
+        if n == 1:
+            return
+        h = n // 2
+        halves(s0, h, out)
+        out.append((s0, s0 + h, s0 + n))
+        halves(s0 + h, n - h, out)
+
+    crosses = []
+    halves(1, 32, crosses)
+    assert len(crosses) == 31
+    for a, b, e in crosses:
+        for s in range(b, e):
+            levels = np.zeros(D)
+            for f in range(min(L - 1, e - a) + 1):
+                levels += A[f] @ combine(x, s, f, a, b, a1, a2, a3)
+            steps = np.zeros(D)
+            for d in range(1, e - a):
+                if a <= s - d < b:
+                    steps += B[d - 1] @ x[s - d]
+            np.testing.assert_allclose(steps, levels, rtol=0,
+                                       atol=1e-12 * max(1.0, np.abs(levels).max()))
