@@ -141,6 +141,7 @@ void free_levels(tdbem_ctx* c) {
     c->levels_last = 0;
     if (c->d_mtc_planes) cudaFree(c->d_mtc_planes);
     c->d_mtc_planes = nullptr;
+    dfree(c->d_mtc_occ);
     dfree(c->d_mtc_known);
     dfree(c->d_mtc_bc);
     c->mtc_planes_valid = false;
@@ -932,6 +933,7 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
         b += 2 * L * (nb + 1) * ldw * 4 + L * nb * D * 8 + (nb + 2) * D * 8;  // time blocks
         // tcgen05 march: merged planes, history planes, known part and its coefficients
         b += tc_plane_bytes((int)D, (int)L + kStepMats, 1) + tc_w_bytes((int)D, 32, (int)L, 1) +
+             tc_occ_bytes((int)D, (int)L + kStepMats) +
              3 * L * D * 8 + (numstep + 1) * (L * 3 + D) * 8 + 3 * D * 4;
         // grouped march (the server's batched steps): FP32 time-block vectors
         b += (2 + 2 * (size_t)kGroupNB) * L * ld * 4 + (size_t)kGroupNB * D * 8;

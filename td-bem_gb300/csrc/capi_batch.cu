@@ -112,7 +112,7 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
             const double ldb = tc_ldb(D), cp = tc_cases_pad(C);
             pe = prof_begin(c, TDBEM_K_CONV_BATCH);
             CUDA_TRY(launch_conv_tc(c->tc_maps, D, mtc_slabs(M), Lw, nlev, C, c->d_bpart, splits,
-                                    c->d_tc_err, s, 1, c->tc_wait_ns));
+                                    c->d_tc_err, s, 1, c->tc_wait_ns, 0, c->d_mtc_occ));
             prof_end(c, pe, nlev * (double)D * ldb * 4 + nlev * cp * ldb * 4,
                      nlev * 2.0 * DD * C);
             CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));

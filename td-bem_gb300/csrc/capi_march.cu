@@ -197,8 +197,13 @@ int ensure_merged_levels(tdbem_ctx* c) {
     CUDA_TRY(launch_merge_levels(c->d_Gf, c->d_Hf, c->ldf, D, M + 1, mtc_slabs(M),
                                  c->d_is_ubc, c->d_mtc_bc, c->d_mtc_bc + D, c->d_mtc_bc + 2 * D,
                                  c->d_mtc_planes, c->d_mtc_known, s));
-    prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4, 0);
-    c->launches += 1;
+    // which 128 x 64 tiles of the levels are all zero (the convolution skips them)
+    if (!c->d_mtc_occ) CUDA_TRY(dalloc(&c->d_mtc_occ, tc_occ_bytes(D, mtc_slabs(M))));
+    CUDA_TRY(launch_tile_occupancy(c->d_mtc_planes, D, 0, M + 1, c->d_mtc_occ, s));
+    prof_end(c, pe, (M + 1) * (double)D * (2.0 * c->ldf + tc_ldb(D)) * 4 +
+                        (M + 1) * (double)D * tc_ldb(D) * 2,
+             0);
+    c->launches += 2;
     c->mtc_planes_valid = true;
     c->mtc_steps_valid = false;  // the step-distance matrices follow the levels
     return TDBEM_OK;
@@ -212,11 +217,13 @@ int ensure_step_mats(tdbem_ctx* c, double a1, double a2) {
     const int pe = prof_begin(c, TDBEM_K_AUX);
     CUDA_TRY(launch_step_mats(c->d_Gf, c->d_Hf, c->ldf, c->D, c->M, mtc_slabs(c->M), c->d_is_ubc,
                               a1, a2, 1 - a1 - a2, c->d_mtc_planes, c->stream));
+    CUDA_TRY(launch_tile_occupancy(c->d_mtc_planes, c->D, c->M + 1, mtc_slabs(c->M), c->d_mtc_occ,
+                                   c->stream));
     prof_end(c, pe,
              std::min(c->M + 1, kStepMats + 2) * (double)c->D * 2.0 * c->ldf * 4 +
-                 kStepMats * (double)c->D * tc_ldb(c->D) * 4,
+                 kStepMats * (double)c->D * tc_ldb(c->D) * 6,
              0);
-    c->launches += 1;
+    c->launches += 2;
     c->mtc_step_key[0] = a1;
     c->mtc_step_key[1] = a2;
     c->mtc_steps_valid = true;
@@ -349,7 +356,8 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                 const int splits = tc_conv_splits(nlev, D, nbe, (M + 1) * nb / nbe, 1);
                 const int pe = prof_begin(c, TDBEM_K_CONV_BLOCK);
                 CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, nbe, c->d_pmix,
-                                        splits, c->d_tc_err, s, 1, c->tc_wait_ns));
+                                        splits, c->d_tc_err, s, 1, c->tc_wait_ns, 0,
+                                        c->d_mtc_occ));
                 prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                     nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                          nlev * 2.0 * nbe * (double)DD);
@@ -386,7 +394,7 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             const int splits = tc_conv_splits(nm, D, ncol, (M + 1) * nb / ncol, 1);
             const int pe = prof_begin(c, TDBEM_K_CONV);
             CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nm, ncol, c->d_pmix, splits,
-                                    c->d_tc_err, s, 1, c->tc_wait_ns, M + 1));
+                                    c->d_tc_err, s, 1, c->tc_wait_ns, M + 1, c->d_mtc_occ));
             prof_end(c, pe, nm * (double)D * tc_ldb(D) * 4 +
                                 nm * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                      nm * 2.0 * ncol * (double)DD);
@@ -400,7 +408,7 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             const int splits = tc_conv_splits(nlev, D, ncol, (M + 1) * nb / ncol, 1);
             const int pe = prof_begin(c, TDBEM_K_CONV);
             CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, ncol, c->d_pmix,
-                                    splits, c->d_tc_err, s, 1, c->tc_wait_ns));
+                                    splits, c->d_tc_err, s, 1, c->tc_wait_ns, 0, c->d_mtc_occ));
             prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                 nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                      nlev * 2.0 * ncol * (double)DD);

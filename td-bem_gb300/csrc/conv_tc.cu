@@ -167,11 +167,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// Tile occupancy (optional, one matrix per level): occ[(slab * nrt + rt) * nk + kc] is
+// zero where the 128-row x 64-column tile (row tile rt, K chunk kc) of level slab
+// `slab` holds only zeros.  Such an iteration adds nothing to the product: every role
+// skips it (the producer loads no stage, the MMA thread issues nothing, and a level
+// whose tiles in the share are all zero hands no accumulator to the epilogue), each
+// role evaluating the same predicate.
+__device__ __forceinline__ bool tile_live(const unsigned char* __restrict__ occ, int slab,
+                                          int nrt, int rt, int nk, int kc) {
+    return !occ || occ[((size_t)slab * nrt + rt) * nk + kc] != 0;
+}
+
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               int D, int L, int Lw, int nlev, int nk, int nmat, int C,
               double* __restrict__ partial, int* __restrict__ err, unsigned long long wait_ns,
-              int lev0) {
+              int lev0, const unsigned char* __restrict__ occ, int nrt) {
     extern __shared__ unsigned char smem_raw[];
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
@@ -192,6 +203,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int i0 = (int)(T * blockIdx.y / gridDim.y), i1 = (int)(T * (blockIdx.y + 1) / gridDim.y);
     const int f0 = i0 / per_lev;
     const int nseg = i1 > i0 ? (i1 - 1) / per_lev - f0 + 1 : 0;  // levels touched
+    // iteration i reads a nonzero tile (occupancy maps come with nmat == 1)
+    auto live = [&](int i) {
+        const int f = i / per_lev;
+        return tile_live(occ, lev0 + f, nrt, blockIdx.x, nk, i - f * per_lev);
+    };
+    // level segment j of the share: iterations [ia, ib), and whether any is live
+    auto seg_live = [&](int j, int& ia, int& ib) {
+        const int f = f0 + j;
+        ia = max(i0, f * per_lev);
+        ib = min(i1, (f + 1) * per_lev);
+        if (!occ) return ia < ib;
+        for (int i = ia; i < ib; i++)
+            if (live(i)) return true;
+        return false;
+    };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; s++) {
@@ -222,7 +248,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (warp == 0) {
         if (lane == 0) {  // ---------------- TMA producer
             int it = 0;
-            for (int i = i0; i < i1; i++, it++) {
+            for (int i = i0; i < i1; i++) {
+                if (!live(i)) continue;
                 const int f = i / per_lev, r = i - f * per_lev;
                 const int mat = r / nk, kc = r - mat * nk;
                 const int s = it % TC_STAGES, n = it / TC_STAGES;
@@ -238,6 +265,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                             bar(FULL + s));
                 tma_load_3d(st + 2 * TC_A_BYTES + TC_B_BYTES, &tmB, x, c0, (mat * 2 + 1) * Lw + f,
                             bar(FULL + s));
+                it++;  // issued (the drain below waits for exactly these)
             }
             // every issued copy has landed before the CTA can exit
             for (int k = std::max(0, it - TC_STAGES); k < it; k++)
@@ -246,18 +274,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {  // ---------------- MMA issuer
-            int it = 0;
+            int it = 0, jj = 0;  // stages used, levels handed over
             bool ok = true;
             for (int j = 0; j < nseg && ok; j++) {
-                const int b = j & 1, u = j >> 1;
+                int ia, ib;
+                if (!seg_live(j, ia, ib)) continue;
+                const int b = jj & 1, u = jj >> 1;
+                jj++;
                 if (u >= 1 && !mbar_wait(bar(TEMPTY + b), (u - 1) & 1, abort_flag, err, 2, wait_ns))
                     break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(b * TC_BN);
-                const int f = f0 + j;
-                const int ia = max(i0, f * per_lev), ib = min(i1, (f + 1) * per_lev);
                 uint32_t acc = 0;
-                for (int i = ia; i < ib; i++, it++) {
+                for (int i = ia; i < ib; i++) {
+                    if (!live(i)) continue;
                     const int s = it % TC_STAGES, n = it / TC_STAGES;
                     if (!mbar_wait(bar(FULL + s), n & 1, abort_flag, err, 3, wait_ns)) {
                         ok = false;
@@ -275,6 +305,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                         acc = 1;
                     }
                     umma_commit(bar(EMPTY + s));
+                    it++;
                 }
                 if (ok) umma_commit(bar(TFULL + b));
             }
@@ -287,8 +318,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         float sum[TC_BN], cmp[TC_BN];
 #pragma unroll
         for (int i = 0; i < TC_BN; i++) sum[i] = cmp[i] = 0.f;
+        int jj = 0;
         for (int j = 0; j < nseg; j++) {
-            const int b = j & 1, u = j >> 1;
+            int ia, ib;
+            if (!seg_live(j, ia, ib)) continue;
+            const int b = jj & 1, u = jj >> 1;
+            jj++;
             if (!mbar_wait(bar(TFULL + b), u & 1, abort_flag, err, 4, wait_ns)) break;
             tc_fence_after();
 #pragma unroll
@@ -393,7 +428,7 @@ bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* ou
 
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
                            double* partial, int splits, int* d_err, cudaStream_t s, int nmat,
-                           unsigned long long wait_ns, int lev0) {
+                           unsigned long long wait_ns, int lev0, const unsigned char* occ) {
     static unsigned long long attr_set = 0;  // devices with the shared-memory attribute set
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -405,14 +440,64 @@ cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, i
         attr_set |= 1ull << dev;
     }
     if (splits < 1 || nlev < 1 || lev0 < 0 || lev0 + nlev > L || nlev > Lw ||
-        (nmat != 1 && nmat != 2) || wait_ns == 0)
+        (nmat != 1 && nmat != 2) || wait_ns == 0 || (occ && nmat != 1))
         return cudaErrorInvalidValue;
     CUtensorMap ma, mb;
     std::memcpy(&ma, maps.a, sizeof(ma));
     std::memcpy(&mb, maps.b, sizeof(mb));
     dim3 grid((D + TC_BM - 1) / TC_BM, splits, (C + TC_BN - 1) / TC_BN);
     k_conv_tc<<<grid, TC_THREADS, TC_SMEM, s>>>(ma, mb, D, L, Lw, nlev, tc_ldb(D) / TC_BK, nmat,
-                                                C, partial, d_err, wait_ns, lev0);
+                                                C, partial, d_err, wait_ns, lev0, occ,
+                                                (D + TC_BM - 1) / TC_BM);
+    return cudaGetLastError();
+}
+
+namespace {
+
+// occ[(slab * nrt + rt) * nk + kc] = 1 where the hi plane's tile (rows rt*128..,
+// columns kc*64..) of a slab in [slab_lo, slab_hi) holds a nonzero: warp per tile,
+// 16-byte loads (a zero hi part means a zero lo part: hi = bf16(a) is zero only for
+// |a| below half the smallest BF16 subnormal, and lo = bf16(a - hi) is then zero).
+__global__ void __launch_bounds__(256) k_tile_occupancy(const __nv_bfloat16* __restrict__ hi,
+                                                        int D, int ldb, int slab_lo,
+                                                        int slab_hi, unsigned char* occ) {
+    const int nrt = (D + TC_BM - 1) / TC_BM, nk = ldb / TC_BK;
+    const long long tiles = (long long)(slab_hi - slab_lo) * nrt * nk;
+    const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (t >= tiles) return;
+    const int kc = (int)(t % nk);
+    const int rt = (int)((t / nk) % nrt);
+    const int slab = slab_lo + (int)(t / ((long long)nk * nrt));
+    unsigned any = 0;
+    // 128 rows x 8 16-byte pieces: lane takes piece lane % 8 of rows lane / 8 + 4 q
+    for (int q = 0; q < TC_BM / 4; q++) {
+        const int r = rt * TC_BM + lane / 8 + 4 * q;
+        if (r >= D) break;
+        const uint4 v = __ldcs(reinterpret_cast<const uint4*>(
+            hi + ((size_t)slab * D + r) * ldb + (size_t)kc * TC_BK) + (lane & 7));
+        any |= v.x | v.y | v.z | v.w;
+    }
+    // BF16 -0 is 0x8000: not a nonzero value
+    any &= 0x7fff7fffu;
+    const unsigned w = __ballot_sync(0xffffffffu, any != 0);
+    if (lane == 0) occ[((size_t)slab * nrt + rt) * nk + kc] = w != 0;
+}
+
+}  // namespace
+
+size_t tc_occ_bytes(int D, int slabs) {
+    return (size_t)slabs * ((D + TC_BM - 1) / TC_BM) * (tc_ldb(D) / TC_BK);
+}
+
+cudaError_t launch_tile_occupancy(const void* planes, int D, int slab_lo, int slab_hi,
+                                  unsigned char* occ, cudaStream_t s) {
+    const int ldb = tc_ldb(D);
+    const long long tiles =
+        (long long)(slab_hi - slab_lo) * ((D + TC_BM - 1) / TC_BM) * (ldb / TC_BK);
+    if (tiles <= 0) return cudaSuccess;
+    k_tile_occupancy<<<(unsigned)((tiles * 32 + 255) / 256), 256, 0, s>>>(
+        static_cast<const __nv_bfloat16*>(planes), D, ldb, slab_lo, slab_hi, occ);
     return cudaGetLastError();
 }
 

@@ -299,9 +299,17 @@ bool make_tc_maps(void* planes, int D, int L, void* W, int C, int Lw, TcMaps* ou
 constexpr unsigned long long kTcWaitNsDefault = 2000000000ull;
 // The product reads level slabs lev0 .. lev0 + nlev - 1 of the planes (L slabs per
 // plane) with the vector slabs 0 .. nlev - 1.
+// occ (optional, nmat == 1): the tile occupancy of the planes' slabs (tc_occ_bytes);
+// all-zero tiles are skipped.
 cudaError_t launch_conv_tc(const TcMaps& maps, int D, int L, int Lw, int nlev, int C,
                            double* partial, int splits, int* d_err, cudaStream_t s, int nmat = 1,
-                           unsigned long long wait_ns = kTcWaitNsDefault, int lev0 = 0);
+                           unsigned long long wait_ns = kTcWaitNsDefault, int lev0 = 0,
+                           const unsigned char* occ = nullptr);
+// Tile occupancy of the merged planes' slabs [slab_lo, slab_hi) (one byte per
+// 128-row x 64-column tile of each slab; tc_occ_bytes(D, slabs) for all slabs).
+size_t tc_occ_bytes(int D, int slabs);
+cudaError_t launch_tile_occupancy(const void* planes, int D, int slab_lo, int slab_hi,
+                                  unsigned char* occ, cudaStream_t s);
 
 // Mixed march with merged levels on tcgen05 (march_tc.cu).
 // The merged planes hold, per plane, the M + 1 level matrices A^f and after them the
@@ -520,6 +528,7 @@ struct tdbem_ctx {
     bool mtc_planes_valid = false;
     double mtc_step_key[2] = {-1.0, -1.0};  // (a1, a2) of the planes' step matrices
     bool mtc_steps_valid = false;
+    unsigned char* d_mtc_occ = nullptr;  // tile occupancy of the planes' slabs
     float* d_mtc_bc = nullptr;
     double* d_mtc_coef = nullptr;
     size_t mtc_coef_cap = 0;
