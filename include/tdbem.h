@@ -302,6 +302,16 @@ int tdbem_inverse_report(const tdbem_ctx* ctx, double probe[2], int full_search[
 int tdbem_invert(int n, const double* A, int precision, double* X, double* probe,
                  int* full_search);
 
+/* Device memory the library keeps for reuse.  Buffers a destroyed context releases
+ * stay allocated, keyed by device and size (at most half of the device's memory),
+ * and the next allocation of the same size takes them: creating a context for a mesh
+ * of the same size again allocates and frees nothing.  An allocation that fails
+ * releases the device's kept buffers and tries again.  device -1: all devices.
+ * tdbem_cached_memory reports the kept bytes; tdbem_release_cached_memory frees
+ * them (*released, may be NULL: the bytes freed). */
+int tdbem_cached_memory(int device, size_t* bytes);
+int tdbem_release_cached_memory(int device, size_t* released);
+
 /* Device pointers of the histories of the last tdbem_march (FP64,
  * (numstep+1) x D each); valid until the next march or destroy. */
 int tdbem_history_device(const tdbem_ctx* ctx, const double** u_hist, const double** t_hist);

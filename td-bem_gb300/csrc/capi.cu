@@ -139,7 +139,7 @@ void free_levels(tdbem_ctx* c) {
     dfree(c->d_H01);
     c->level_precision = -1;
     c->levels_last = 0;
-    if (c->d_mtc_planes) cudaFree(c->d_mtc_planes);
+    mem_free(c->d_mtc_planes);
     c->d_mtc_planes = nullptr;
     dfree(c->d_mtc_occ);
     dfree(c->d_mtc_known);
@@ -161,7 +161,7 @@ void free_batch(tdbem_ctx* c) {
     c->bpart_cap = 0;
     c->batch_C = 0;
     c->batch_steps = -1;
-    if (c->d_tc_W) cudaFree(c->d_tc_W);
+    mem_free(c->d_tc_W);
     c->d_tc_W = nullptr;
     c->tc_W_bytes = 0;
     dfree(c->d_tc_err);
@@ -186,7 +186,7 @@ void free_march(tdbem_ctx* c) {
     dfree(c->d_pmix);
     dfree(c->d_res);
     dfree(c->d_dx);
-    if (c->d_mtc_W) cudaFree(c->d_mtc_W);
+    mem_free(c->d_mtc_W);
     c->d_mtc_W = nullptr;
     c->mtc_W_bytes = 0;
     c->mtc_maps_for[0] = c->mtc_maps_for[1] = nullptr;
@@ -433,7 +433,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_counts, c->pair_cap));
     CTX_TRY(dalloc(&c->d_offsets, c->pair_cap));
     c->scan_tmp_bytes = scan_temp_bytes((unsigned)c->pair_cap);
-    CTX_TRY(cudaMalloc(&c->d_scan_tmp, std::max<size_t>(c->scan_tmp_bytes, 16)));
+    CTX_TRY(mem_alloc(&c->d_scan_tmp, std::max<size_t>(c->scan_tmp_bytes, 16)));
     CTX_TRY(cudaStreamSynchronize(c->stream));
 #undef CTX_TRY
     *out = c;
@@ -465,7 +465,7 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_pairs);
     dfree(c->d_counts);
     dfree(c->d_offsets);
-    if (c->d_scan_tmp) cudaFree(c->d_scan_tmp);
+    mem_free(c->d_scan_tmp);
     dfree(c->d_ubc_map);
     dfree(c->d_fbc_map);
     dfree(c->d_is_ubc);
@@ -559,7 +559,7 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
     e = cudaStreamSynchronize(c->stream);
     if (rc == TDBEM_OK && e != cudaSuccess)
         rc = fail(TDBEM_ERR_CUDA, "gh_driver: %s", cudaGetErrorString(e));
-    cudaFree(buf);
+    mem_free(buf);
     return rc;
 }
 

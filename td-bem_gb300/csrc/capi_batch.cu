@@ -71,10 +71,10 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
         if (rm != TDBEM_OK) return rm;
         const size_t wb = tc_w_bytes(D, C, Lw, 1);
         if (c->tc_W_bytes < wb) {
-            if (c->d_tc_W) cudaFree(c->d_tc_W);
+            mem_free(c->d_tc_W);
             c->d_tc_W = nullptr;
             c->tc_W_bytes = 0;
-            CUDA_TRY(cudaMalloc(&c->d_tc_W, wb));
+            CUDA_TRY(mem_alloc(&c->d_tc_W, wb));
             c->tc_W_bytes = wb;
         }
         if (!make_tc_maps(c->d_mtc_planes, D, mtc_slabs(M), c->d_tc_W, C, Lw, &c->tc_maps, 1))

@@ -19,6 +19,14 @@
 #include "tdbem_internal.cuh"
 
 namespace tdbem {
+
+// Device buffers of the library (devmem.cu): freed blocks are kept and handed to the
+// next allocation of the same rounded size on the same device.
+cudaError_t mem_alloc(void** p, size_t bytes);
+void mem_free(void* p);
+size_t mem_release(int device);       // the kept blocks of a device (all: -1); bytes
+size_t mem_cached_bytes(int device);  // bytes kept (all devices: -1)
+
 namespace capi {
 
 // Records the message of a failed call (tdbem_last_error) and returns code.
@@ -39,12 +47,12 @@ template <typename T>
 cudaError_t dalloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
-    return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+    return mem_alloc(reinterpret_cast<void**>(p), sizeof(T) * count);
 }
 
 template <typename T>
 void dfree(T*& p) {
-    if (p) cudaFree(p);
+    if (p) mem_free(p);
     p = nullptr;
 }
 

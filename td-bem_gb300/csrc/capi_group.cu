@@ -244,14 +244,14 @@ int tdbem_assemble_group(tdbem_ctx* const* ctxs, int n, const int* nsteps, int p
             dfree(b);
             dfree(c);
             dfree(d);
-            if (e) cudaFree(e);
+            mem_free(e);
         }
     } guard{d_pairs, d_counts, d_offsets, d_gm, d_tmp};
     CUDA_TRY(dalloc(&d_pairs, std::max<size_t>(pair_max, 1)));
     CUDA_TRY(dalloc(&d_counts, std::max<size_t>(pair_max, 1)));
     CUDA_TRY(dalloc(&d_offsets, std::max<size_t>(pair_max, 1)));
     CUDA_TRY(dalloc(&d_gm, (size_t)n));
-    CUDA_TRY(cudaMalloc(&d_tmp, tmp_bytes));
+    CUDA_TRY(mem_alloc(&d_tmp, tmp_bytes));
     long long launches = 0;
     for (int col = 0; col < ncol; col++) {
         std::vector<GroupAsm> gl;

@@ -171,7 +171,7 @@ int ensure_merged_levels(tdbem_ctx* c) {
     cudaStream_t s = c->stream;
     if (c->mtc_planes_valid) return TDBEM_OK;
     if (!c->d_mtc_planes)
-        CUDA_TRY(cudaMalloc(&c->d_mtc_planes, tc_plane_bytes(D, mtc_slabs(M), 1)));
+        CUDA_TRY(mem_alloc(&c->d_mtc_planes, tc_plane_bytes(D, mtc_slabs(M), 1)));
     if (!c->d_mtc_known) CUDA_TRY(dalloc(&c->d_mtc_known, (size_t)3 * (M + 1) * D));
     if (!c->d_mtc_bc) CUDA_TRY(dalloc(&c->d_mtc_bc, (size_t)3 * D));
     // kt, lt, lu (the last list entry of a dof wins, as in upload_bc)
@@ -298,11 +298,11 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         }
         const size_t wb = tc_w_bytes(D, nb, Lw, 1);
         if (c->mtc_W_bytes < wb) {
-            if (c->d_mtc_W) cudaFree(c->d_mtc_W);
+            mem_free(c->d_mtc_W);
             c->d_mtc_W = nullptr;
             c->mtc_W_bytes = 0;
             c->mtc_maps_for[0] = c->mtc_maps_for[1] = nullptr;
-            CUDA_TRY(cudaMalloc(&c->d_mtc_W, wb));
+            CUDA_TRY(mem_alloc(&c->d_mtc_W, wb));
             c->mtc_W_bytes = wb;
         }
         if (c->mtc_maps_for[0] != c->d_mtc_planes || c->mtc_maps_for[1] != c->d_mtc_W ||
@@ -830,13 +830,13 @@ int tdbem_invert(int n, const double* A, int precision, double* X, double* probe
         dfree(dX);
         dfree(perm);
         dfree(status);
-        if (scratch) cudaFree(scratch);
+        mem_free(scratch);
     };
     const size_t scratch_bytes = inverse_scratch_elems(n) * sizeof(double);
     cudaError_t e = dalloc(&dA, nn);
     if (e == cudaSuccess) e = dalloc(&perm, (size_t)n + 2 * kMaxPivotBlocks);
     if (e == cudaSuccess) e = dalloc(&status, 1);
-    if (e == cudaSuccess) e = cudaMalloc(&scratch, scratch_bytes);
+    if (e == cudaSuccess) e = mem_alloc(&scratch, scratch_bytes);
     if (e == cudaSuccess && precision == TDBEM_MIXED) e = dalloc(&dX, nn);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dA, A, sizeof(double) * nn, cudaMemcpyHostToDevice, s);
     long long nl = 0;

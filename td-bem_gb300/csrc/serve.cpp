@@ -312,7 +312,10 @@ int tdbem_server_create(int device, size_t hbm_budget, int slots, tdbem_server**
     auto* s = new (std::nothrow) tdbem_server();
     if (!s) return sfail(TDBEM_ERR_NOMEM, "server allocation");
     s->device = device;
-    s->budget = hbm_budget ? hbm_budget : free_b / 10 * 9;
+    // memory the library keeps for reuse counts as free: contexts take it first
+    size_t kept = 0;
+    tdbem_cached_memory(device, &kept);
+    s->budget = hbm_budget ? hbm_budget : (free_b + kept) / 10 * 9;
     s->slots = slots;
     s->t0 = std::chrono::steady_clock::now();
     if (cudaStreamCreateWithFlags(&s->mstream, cudaStreamNonBlocking) != cudaSuccess) {

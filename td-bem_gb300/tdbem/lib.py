@@ -97,6 +97,9 @@ SIGNATURES = {
                                                  ctypes.POINTER(ctypes.c_longlong),
                                                  ctypes.POINTER(ctypes.c_double)]),
     "tdbem_server_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tdbem_cached_memory": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)]),
+    "tdbem_release_cached_memory": (ctypes.c_int, [ctypes.c_int,
+                                                    ctypes.POINTER(ctypes.c_size_t)]),
     "tdbem_mrt_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, _ip, _ip, ctypes.c_int,
                                         ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "tdbem_mrt_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -198,6 +201,20 @@ def invert(A, precision: int = FP64):
     _check(load().tdbem_invert(n, _d(a), precision, _d(x), ctypes.byref(probe),
                                ctypes.byref(full)))
     return x, probe.value, full.value
+
+
+def cached_memory(device: int = -1) -> int:
+    """Device bytes the library keeps for reuse (tdbem_cached_memory)."""
+    b = ctypes.c_size_t()
+    _check(load().tdbem_cached_memory(device, ctypes.byref(b)))
+    return b.value
+
+
+def release_cached_memory(device: int = -1) -> int:
+    """Free the device memory the library keeps for reuse; returns the bytes freed."""
+    b = ctypes.c_size_t()
+    _check(load().tdbem_release_cached_memory(device, ctypes.byref(b)))
+    return b.value
 
 
 def write_gh(prefix: str, step: int, data) -> None:

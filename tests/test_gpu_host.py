@@ -193,3 +193,27 @@ def test_tdbem_run_two_regions_matches_oracle(tdlib, oracle_mod, name, mode, tmp
     assert rows.shape == (n, 2)
     assert np.allclose(rows[:, 0], m1.dt * np.arange(n), rtol=1e-5, atol=1e-15)
     assert np.allclose(rows[:, 1], u2o[:n, dof], rtol=1e-5, atol=1e-12 * np.abs(u2o).max())
+
+
+def test_device_memory_kept_for_the_next_context(tdlib):
+    """Buffers of a destroyed context stay allocated for the next one (devmem.cu): a
+    second context of the same mesh takes them (nothing new kept afterwards beyond
+    what the first left) and gives bitwise the same solve; releasing frees them."""
+    from tdbem import meshes
+    m = meshes.cubed_sphere(4, numstep=40)
+    tdlib.release_cached_memory()
+    assert tdlib.cached_memory() == 0
+    outs = []
+    kept = []
+    for _ in range(2):
+        with tdlib.Context(m) as ctx:
+            ctx.set_alpha(0.25, 0.0)
+            ctx.assemble(precision=tdlib.MIXED)
+            outs.append(ctx.march())
+            if kept:  # the second context runs on the blocks the first one left
+                assert tdlib.cached_memory() < kept[0]
+        kept.append(tdlib.cached_memory())
+    assert kept[0] > 0 and kept[1] == kept[0]
+    assert all(np.array_equal(a, b) for a, b in zip(outs[0], outs[1]))
+    assert tdlib.release_cached_memory() == kept[1]
+    assert tdlib.cached_memory() == 0

@@ -38,8 +38,12 @@ def test_footprint_counts_the_level_store(tdlib):
     f32 = tdlib.footprint(m, tdlib.MIXED)
     levels64 = 2 * (M + 1) * D * D * 8
     assert levels64 < f64 < 1.3 * levels64
-    # FP32 levels and, for the tcgen05 march, the merged BF16 hi/lo planes (half of them)
-    assert 2 * (M + 1) * D * D * 4 < f32 < f64
+    # FP32 levels and, for the tcgen05 march, the merged BF16 hi/lo planes of the levels
+    # and of the 31 step-distance matrices (rows of D rounded up to 64)
+    ldb = (D + 63) // 64 * 64
+    store32 = 2 * (M + 1) * D * D * 4
+    planes = (M + 1 + 31) * D * ldb * 4
+    assert store32 + planes < f32 < 1.3 * (store32 + planes)
     # more steps: longer histories, same levels
     assert tdlib.footprint(m, tdlib.MIXED, numstep=400) > f32
 
