@@ -1343,19 +1343,25 @@ __device__ __forceinline__ int far_block_scan(int v, int& excl, int* s_warp) {
     return total;
 }
 
+// Capacity of a far-field block's item and settled-job lists (one colour's worth
+// at a time; flushed earlier when a colour's elements hold more).
+constexpr int kFarItemCap = 2 * kFarBlock * kFarChunk;
+constexpr int kFarJobCap = 4 * kFarBlock;
+
 // All far items of collocation node c = blockIdx.x at levels [k0, k0 + kFarChunk),
 // k0 = blockIdx.y * kFarChunk.  The block owns those rows of those levels, so it
 // walks the element colours in order (elements of one colour share no node:
 // their items write distinct entries) with a barrier between colours: every add
 // to a row lands while the rows are resident in L2, in a fixed order (bitwise
-// reproducible), and one launch covers all colours.  Candidate items (element,
-// level) of a batch of kFarBlock elements are compacted with a block scan and
-// spread over the threads.  pairs[c * nel + j] is the window of node c and the
-// j-th element in colour order.  A pair's settled levels (settled_range) leave its
-// item list and go to one settled job; the batch's items come first in the thread
-// order and its jobs after them, so most warps hold one kind of work.  level_top:
-// the highest level any window reaches.  nitems (if not null) receives the item,
-// job and settled-level counts.
+// reproducible), and one launch covers all colours.  The candidate items (element,
+// level) of a colour's elements, kFarBlock elements at a time, are compacted with
+// one block scan per chunk into the colour's list, which the threads then work
+// through in one pass (a list about to overflow is worked through first).
+// pairs[c * nel + j] is the window of node c and the j-th element in colour order.
+// A pair's settled levels (settled_range) leave its item list and go to one settled
+// job; the items come first in the thread order and the jobs after them, so most
+// warps hold one kind of work.  level_top: the highest level any window reaches.
+// nitems (if not null) receives the item, job and settled-level counts.
 template <typename T>
 __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
@@ -1364,8 +1370,9 @@ __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_fa
     const float* __restrict__ coordf, Phys ph, int level_last, int level_top,
     const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
     __shared__ int s_warp[kFarBlock / 32];
-    __shared__ int s_items[kFarBlock * kFarChunk];
-    __shared__ int s_jobs[kFarBlock];
+    __shared__ int s_items[kFarItemCap];          // (element in colour) << bits | level
+    __shared__ int s_jobs[kFarJobCap];            // element in colour
+    __shared__ unsigned short s_jobl[kFarJobCap];  // first level << 8 | levels - 1
     const int c = blockIdx.x;
     const int k0 = blockIdx.y * kFarChunk;
     const int k1 = min(k0 + kFarChunk, level_top + 1);
@@ -1376,7 +1383,24 @@ __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_fa
     unsigned long long count = 0, njobs = 0, nsettled = 0;
     for (int col = 0; col < ncolor; col++) {
         const int j0 = color_start[col], j1 = color_start[col + 1];
-        for (int base = j0; base < j1; base += kFarBlock) {  // uniform over the block
+        // work through the list: items [0, ni), then jobs [0, nj)
+        auto work = [&](int ni, int nj) {
+            for (int i = threadIdx.x; i < ni + nj; i += kFarBlock) {
+                if (i < ni) {
+                    const int code = s_items[i];
+                    const int k = k0 + (code & ((1 << kFarCodeBits) - 1));
+                    far_item<T>(coords, ien, c, color_elems[j0 + (code >> kFarCodeBits)], k,
+                                nq2, geomf, geom, coordf, f, ph, (float)k * f.dt, level_last,
+                                out);
+                } else {
+                    const int jl = s_jobl[i - ni];
+                    settled_job<T>(ien, c, color_elems[j0 + s_jobs[i - ni]], k0 + (jl >> 8),
+                                   (jl & 0xff) + 1, nq2, geomf, coordf, f, out);
+                }
+            }
+        };
+        int ni = 0, nj = 0;  // the colour's list so far (uniform over the block)
+        for (int base = j0; base < j1; base += kFarBlock) {
             const int j = base + (int)threadIdx.x;
             int na = 0, lo = 0, ss = 0, sn = 0;
             if (j < j1) {
@@ -1394,35 +1418,35 @@ __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_fa
                     }
                 }
             }
-            int off, offj;
-            const int total = far_block_scan(na - sn, off, s_warp);
-            const int jobs = far_block_scan(sn > 0 ? 1 : 0, offj, s_warp);
+            // items in the low 16 bits, the job in the high ones (chunk totals < 2^16)
+            int off;
+            const int tot = far_block_scan((na - sn) | ((sn > 0 ? 1 : 0) << 16), off, s_warp);
+            const int ti = tot & 0xffff, tj = tot >> 16;
+            if (ni + ti > kFarItemCap || nj + tj > kFarJobCap) {
+                // the chunks so far are written (the scan's barriers follow them)
+                work(ni, nj);
+                __syncthreads();  // the list is rewritten next
+                ni = nj = 0;
+            }
+            int oi = ni + (off & 0xffff);
             for (int k = lo; k < lo + na; k++)
                 if (k < ss || k >= ss + sn)
-                    s_items[off++] = ((int)threadIdx.x << kFarCodeBits) | (k - k0);
-            if (sn > 0)
-                s_jobs[offj] = ((int)threadIdx.x << 16) | ((ss - k0) << 8) | (sn - 1);
-            __syncthreads();
-            for (int i = threadIdx.x; i < total + jobs; i += kFarBlock) {
-                if (i < total) {
-                    const int code = s_items[i];
-                    const int k = k0 + (code & ((1 << kFarCodeBits) - 1));
-                    far_item<T>(coords, ien, c, color_elems[base + (code >> kFarCodeBits)], k,
-                                nq2, geomf, geom, coordf, f, ph, (float)k * f.dt, level_last,
-                                out);
-                } else {
-                    const int job = s_jobs[i - total];
-                    settled_job<T>(ien, c, color_elems[base + (job >> 16)],
-                                   k0 + ((job >> 8) & 0xff), (job & 0xff) + 1, nq2, geomf,
-                                   coordf, f, out);
-                }
+                    s_items[oi++] = ((j - j0) << kFarCodeBits) | (k - k0);
+            if (sn > 0) {
+                const int oj = nj + (off >> 16);
+                s_jobs[oj] = j - j0;
+                s_jobl[oj] = (unsigned short)(((ss - k0) << 8) | (sn - 1));
             }
-            count += total;
-            njobs += jobs;
+            ni += ti;
+            nj += tj;
+            count += ti;
+            njobs += tj;
             nsettled += sn;
-            // s_items is rebuilt next; this batch's adds come before the next colour's
-            __syncthreads();
         }
+        __syncthreads();
+        work(ni, nj);
+        // the list is rebuilt next; this colour's adds come before the next colour's
+        __syncthreads();
     }
     if (nitems) {
         if (threadIdx.x == 0 && count) atomicAdd(nitems, count);

