@@ -331,6 +331,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         tc ? c->d_mtc_coef : nullptr, tc ? c->d_mtc_yk : nullptr};
     // d_Yold[j] accumulates the right-hand side of step S + j of the current block.
     // Old pass: history before the block and the steps' known-load terms.
+    // set when the reduction that finished the right-hand side of the step solved next
+    // also wrote its FP32 copy (the solve's first product reads it)
+    bool v32_ready = false;
     auto old_pass = [&](int S, int nbe) -> int {
         const int nlev = (S > 1 ? std::min(M, S + nbe - 1) : std::min(M, 1)) + 1;
         BlockLoads bl{};  // the FP32 engine's known-load terms (its blocks: <= 16 steps)
@@ -361,7 +364,10 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                 prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
                                     nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                          nlev * 2.0 * nbe * (double)DD);
-                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, yk, Y, s));
+                // column 0 (step S, solved next) also in FP32 for its solve
+                CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, yk, Y, s,
+                                              reinterpret_cast<float*>(c->d_dx)));
+                v32_ready = true;
                 c->launches += 3;
             }
             return TDBEM_OK;
@@ -398,7 +404,10 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             prof_end(c, pe, nm * (double)D * tc_ldb(D) * 4 +
                                 nm * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
                      nm * 2.0 * ncol * (double)DD);
-            CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s));
+            // column 0 (step b, solved next) also in FP32 for its solve
+            CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s,
+                                          reinterpret_cast<float*>(c->d_dx)));
+            v32_ready = true;
             c->launches += 3;
             return TDBEM_OK;
         }
@@ -438,13 +447,22 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
         // d_dx (D doubles) holds the D-float FP32 vector of the solve's products
         const int sweeps = (st == 1 && c->step2_sweeps > 0) ? std::max(c->step2_sweeps, c->n_refine)
                                                             : c->n_refine;
+        // the step's state update rides on its last product
+        StateUpdate upd;
+        upd.is_u = c->d_is_ubc;
+        upd.ubc = c->d_ubc_map;
+        upd.is_f = c->d_is_fbc;
+        upd.fbc = c->d_fbc_map;
+        upd.amp = amp;
+        upd.u_hist = c->d_u;
+        upd.t_hist = c->d_t;
+        upd.s = st;
         CUDA_TRY(launch_solve_mixed(c->d_inv32[v], c->d_Hc64[v], D, c->d_Yold + (size_t)(st - S) * D,
                                     c->d_x, c->d_res, reinterpret_cast<float*>(c->d_dx),
-                                    sweeps, s));
-        CUDA_TRY(launch_update_state(c->d_x, D, st, c->d_is_ubc, c->d_ubc_map, c->d_is_fbc,
-                                     c->d_fbc_map, amp, c->d_u, c->d_t, s));
+                                    sweeps, s, v32_ready, upd));
         prof_end(c, pe, 4.0 * (double)DD * (1 + 2 * sweeps), 2.0 * (double)DD * (1 + 2 * sweeps));
-        c->launches += 4 + 2LL * sweeps;  // cast, gemv(s), residual(s), update
+        c->launches += (v32_ready ? 1 : 2) + 2LL * sweeps;  // cast, gemv(s), residual(s)
+        v32_ready = false;
         return TDBEM_OK;
     };
     // Steps [s0, s0 + n) of the block starting at S: first half, its history into

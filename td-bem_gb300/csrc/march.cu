@@ -14,6 +14,7 @@
 // SolverT.cpp:265-342), computed once per distinct LHS (inverse.cu).
 #include <algorithm>
 
+#include "state_update.cuh"
 #include "tdbem_internal.cuh"
 
 namespace tdbem {
@@ -174,11 +175,16 @@ __global__ void k_update_state(const double* __restrict__ x, int D, int s,
                                double* __restrict__ u_hist, double* __restrict__ t_hist) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= D) return;
-    const bool u = is_u[j] != 0, f = is_f[j] != 0;
-    u_hist[(size_t)s * D + j] = u ? ubc_val[j] : x[j];
-    double tv = f ? fbc_val[j] * amp : 0.0;
-    if (u && j < D - 1) tv = x[j];
-    t_hist[(size_t)s * D + j] = tv;
+    StateUpdate p;
+    p.is_u = is_u;
+    p.ubc = ubc_val;
+    p.is_f = is_f;
+    p.fbc = fbc_val;
+    p.amp = amp;
+    p.u_hist = u_hist;
+    p.t_hist = t_hist;
+    p.s = s;
+    update_state_dof(p, D, j, x[j]);
 }
 
 __global__ void k_add_inplace(double* __restrict__ y, const double* __restrict__ x, size_t n) {

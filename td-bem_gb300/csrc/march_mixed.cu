@@ -18,6 +18,7 @@
 // the leaves are plain solves.
 #include <algorithm>
 
+#include "state_update.cuh"
 #include "tdbem_internal.cuh"
 
 namespace tdbem {
@@ -190,12 +191,14 @@ __global__ void k_build_w_cross(const double* __restrict__ u_hist,
 // out[j][row] = sum over chunks of partial[chunk][j][row] (+ add[j][row] if given),
 // for the first ncol of the nb partial columns.
 __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, int nb, int ncol,
-                              int D, const double* __restrict__ add, double* __restrict__ out) {
+                              int D, const double* __restrict__ add, double* __restrict__ out,
+                              float* __restrict__ v32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= ncol * D) return;
     double s = add ? add[i] : 0.0;
     for (int c = 0; c < nchunks; c++) s += partial[(size_t)c * nb * D + i];
     out[i] = s;
+    if (v32 && i < D) v32[i] = (float)s;
 }
 
 // y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
@@ -203,7 +206,8 @@ __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, i
 // vector in every row would put D^2 conversions on GB300's narrow FP64 pipe.
 __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, int D,
                                                   const float* __restrict__ v,
-                                                  double* __restrict__ y, int accumulate) {
+                                                  double* __restrict__ y, int accumulate,
+                                                  StateUpdate upd) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= D) return;
     const float* a = A + (size_t)row * D;
@@ -239,7 +243,11 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
     double s = acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) y[row] = accumulate ? y[row] + s : s;
+    if (lane == 0) {
+        const double xr = accumulate ? y[row] + s : s;
+        y[row] = xr;
+        if (upd.u_hist) update_state_dof(upd, D, row, xr);  // the step's last product
+    }
 }
 
 // r = b - A64 x, FP64, warp per row; also r in FP32 for the correction product.
@@ -336,27 +344,30 @@ cudaError_t launch_build_w_cross(const double* u_hist, const double* t_hist, int
 
 cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
                                const double* add, double* out, cudaStream_t s) {
-    k_reduce_cols<<<(nb * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, nb, D, add, out);
+    k_reduce_cols<<<(nb * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, nb, D, add, out,
+                                                       nullptr);
     return cudaGetLastError();
 }
 
 cudaError_t launch_reduce_cols_n(const double* partial, int nchunks, int nb, int ncol, int D,
-                                 const double* add, double* out, cudaStream_t s) {
+                                 const double* add, double* out, cudaStream_t s, float* v32) {
     k_reduce_cols<<<(ncol * D + 255) / 256, 256, 0, s>>>(partial, nchunks, nb, ncol, D, add,
-                                                         out);
+                                                         out, v32);
     return cudaGetLastError();
 }
 
 // x = inv32 rhs, then n_refine times: r = rhs - A64 x; x += inv32 r.  v32 is D
 // floats of scratch (the FP32 copy of the vector each product reads).
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
-                               double* x, double* r, float* v32, int n_refine, cudaStream_t s) {
+                               double* x, double* r, float* v32, int n_refine, cudaStream_t s,
+                               bool v32_ready, const StateUpdate& upd) {
     const unsigned g = (D * 32 + 255) / 256;
-    k_to_f32<<<(D + 255) / 256, 256, 0, s>>>(rhs, v32, D);
-    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 0);
+    const StateUpdate none;
+    if (!v32_ready) k_to_f32<<<(D + 255) / 256, 256, 0, s>>>(rhs, v32, D);
+    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 0, n_refine == 0 ? upd : none);
     for (int it = 0; it < n_refine; it++) {
         k_residual_f64<<<g, 256, 0, s>>>(A64, D, x, rhs, r, v32);
-        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 1);
+        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 1, it == n_refine - 1 ? upd : none);
     }
     return cudaGetLastError();
 }

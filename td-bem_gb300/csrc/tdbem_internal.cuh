@@ -383,12 +383,29 @@ cudaError_t launch_build_w_cross(const double* u_hist, const double* t_hist, int
                                  int ncol, int nbp, int nlev, double a1, double a2, double a3,
                                  int ldw, float* Wt, float* Wu, cudaStream_t s);
 // The first ncol of nb partial columns (out and add have ncol columns).
+// v32 (optional): column 0 of out also in FP32 (the vector the next solve multiplies).
 cudaError_t launch_reduce_cols_n(const double* partial, int nchunks, int nb, int ncol, int D,
-                                 const double* add, double* out, cudaStream_t s);
+                                 const double* add, double* out, cudaStream_t s,
+                                 float* v32 = nullptr);
 cudaError_t launch_reduce_cols(const double* partial, int nchunks, int nb, int D,
                                const double* add, double* out, cudaStream_t s);
+// The histories' update of solve step s from its unknowns (state_update.cuh); a null
+// u_hist means none.
+struct StateUpdate {
+    const unsigned char* is_u = nullptr;
+    const double* ubc = nullptr;
+    const unsigned char* is_f = nullptr;
+    const double* fbc = nullptr;
+    double amp = 1.0;
+    double* u_hist = nullptr;
+    double* t_hist = nullptr;
+    int s = 0;
+};
+// v32_ready: v32 already holds rhs in FP32 (the reduction that finished rhs wrote it);
+// upd (if its u_hist is set): the step's state update, done by the last product.
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
-                               double* x, double* r, float* v32, int n_refine, cudaStream_t s);
+                               double* x, double* r, float* v32, int n_refine, cudaStream_t s,
+                               bool v32_ready = false, const StateUpdate& upd = StateUpdate());
 
 // Batched marching of many load cases (batch.cu).
 int batch_block_cases();            // cases per tensor-core column block
