@@ -67,7 +67,9 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
     if (tc) {
         if (!c->d_tc_err) CUDA_TRY(dalloc(&c->d_tc_err, 2));
         CUDA_TRY(cudaMemsetAsync(c->d_tc_err, 0, 2 * sizeof(int), s));
-        const int rm = ensure_merged_levels(c);
+        int rm = ensure_merged_levels(c);
+        // profiling: the level slabs' live tiles (the product's bytes)
+        if (rm == TDBEM_OK && c->prof) rm = count_live_tiles(c);
         if (rm != TDBEM_OK) return rm;
         const size_t wb = tc_w_bytes(D, C, Lw, 1);
         if (c->tc_W_bytes < wb) {
@@ -113,8 +115,8 @@ int tdbem_march_batch(tdbem_ctx* c, int numstep, int nrhs, const double* tractio
             pe = prof_begin(c, TDBEM_K_CONV_BATCH);
             CUDA_TRY(launch_conv_tc(c->tc_maps, D, mtc_slabs(M), Lw, nlev, C, c->d_bpart, splits,
                                     c->d_tc_err, s, 1, c->tc_wait_ns, 0, c->d_mtc_occ));
-            prof_end(c, pe, nlev * (double)D * ldb * 4 + nlev * cp * ldb * 4,
-                     nlev * 2.0 * DD * C);
+            const double pb = conv_plane_bytes(c, 0, nlev);
+            prof_end(c, pe, pb + nlev * cp * ldb * 4, pb / 4 * 2.0 * C);
             CUDA_TRY(launch_reduce_cols(c->d_bpart, splits, C, D, nullptr, c->d_brhs, s));
             const double* hu = c->d_mtc_known + (size_t)2 * (M + 1) * D;  // H^f ubc
             CUDA_TRY(launch_known_batch(c->d_bGK, c->d_bGL, hu, D, C, M + 1, st, a1, a2, a3, c0,

@@ -175,6 +175,10 @@ void run_inverses(tdbem_ctx* c, int ninv, const double lhs_c[2][2], cudaStream_t
 int finish_inverses(tdbem_ctx* c, int ninv, const InvResult& r);
 int mixed_inverses(tdbem_ctx* c, int numstep, const double lhs_c[2][2]);
 int ensure_merged_levels(tdbem_ctx* c);
+// Profiling: the live tiles of every slab from the occupancy map (one copy to the
+// host), and the merged-plane bytes a convolution over slabs [lev0, lev0 + nlev) reads.
+int count_live_tiles(tdbem_ctx* c);
+double conv_plane_bytes(const tdbem_ctx* c, int lev0, int nlev);
 int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]);
 int upload_bc(tdbem_ctx* c);
 int fp64_inverse(tdbem_ctx* c, int v, const double lhs_c[2][2]);

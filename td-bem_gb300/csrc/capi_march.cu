@@ -209,6 +209,28 @@ int ensure_merged_levels(tdbem_ctx* c) {
     return TDBEM_OK;
 }
 
+int count_live_tiles(tdbem_ctx* c) {
+    const int D = c->D, slabs = mtc_slabs(c->M);
+    const size_t n = tc_occ_bytes(D, slabs);
+    std::vector<unsigned char> occ(n);
+    CUDA_TRY(cudaMemcpyAsync(occ.data(), c->d_mtc_occ, n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const size_t per_slab = n / slabs;
+    c->h_occ_live.assign(slabs, 0);
+    for (int sl = 0; sl < slabs; sl++)
+        for (size_t i = 0; i < per_slab; i++) c->h_occ_live[sl] += occ[sl * per_slab + i] != 0;
+    return TDBEM_OK;
+}
+
+double conv_plane_bytes(const tdbem_ctx* c, int lev0, int nlev) {
+    const double tile = 128.0 * 64 * 2 * 2;  // hi + lo BF16
+    if ((int)c->h_occ_live.size() < lev0 + nlev)  // not counted: every tile
+        return nlev * (double)c->D * tc_ldb(c->D) * 4;
+    double live = 0;
+    for (int sl = lev0; sl < lev0 + nlev; sl++) live += (double)c->h_occ_live[sl];
+    return live * tile;
+}
+
 // The planes' step-distance matrices B_1 .. B_kStepMats for the weights (a1, a2):
 // after every merge and when the weights change.
 int ensure_step_mats(tdbem_ctx* c, double a1, double a2) {
@@ -272,6 +294,7 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
     if (tc) {
         int rm = ensure_merged_levels(c);
         if (rm == TDBEM_OK) rm = ensure_step_mats(c, a1, a2);
+        if (rm == TDBEM_OK && c->prof) rm = count_live_tiles(c);
         if (rm != TDBEM_OK) return rm;
         std::vector<double> key = {(double)numstep, (double)(M + 1), a1, a2,
                                    lhs_c[1][0], lhs_c[1][1]};
@@ -361,9 +384,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
                 CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, nbe, c->d_pmix,
                                         splits, c->d_tc_err, s, 1, c->tc_wait_ns, 0,
                                         c->d_mtc_occ));
-                prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
-                                    nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
-                         nlev * 2.0 * nbe * (double)DD);
+                const double pb = conv_plane_bytes(c, 0, nlev);
+                prof_end(c, pe, pb + nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                         pb / 4 * 2.0 * nbe);
                 // column 0 (step S, solved next) also in FP32 for its solve
                 CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, nbe, nbe, D, yk, Y, s,
                                               reinterpret_cast<float*>(c->d_dx)));
@@ -401,9 +424,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             const int pe = prof_begin(c, TDBEM_K_CONV);
             CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nm, ncol, c->d_pmix, splits,
                                     c->d_tc_err, s, 1, c->tc_wait_ns, M + 1, c->d_mtc_occ));
-            prof_end(c, pe, nm * (double)D * tc_ldb(D) * 4 +
-                                nm * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
-                     nm * 2.0 * ncol * (double)DD);
+            const double pb = conv_plane_bytes(c, M + 1, nm);
+            prof_end(c, pe, pb + nm * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                     pb / 4 * 2.0 * ncol);
             // column 0 (step b, solved next) also in FP32 for its solve
             CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s,
                                           reinterpret_cast<float*>(c->d_dx)));
@@ -418,9 +441,9 @@ int march_mixed(tdbem_ctx* c, int numstep, const double lhs_c[2][2]) {
             const int pe = prof_begin(c, TDBEM_K_CONV);
             CUDA_TRY(launch_conv_tc(c->mtc_maps, D, mtc_slabs(M), Lw, nlev, ncol, c->d_pmix,
                                     splits, c->d_tc_err, s, 1, c->tc_wait_ns, 0, c->d_mtc_occ));
-            prof_end(c, pe, nlev * (double)D * tc_ldb(D) * 4 +
-                                nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
-                     nlev * 2.0 * ncol * (double)DD);
+            const double pb = conv_plane_bytes(c, 0, nlev);
+            prof_end(c, pe, pb + nlev * (double)tc_cases_pad(nb) * tc_ldb(D) * 4,
+                     pb / 4 * 2.0 * ncol);
             CUDA_TRY(launch_reduce_cols_n(c->d_pmix, splits, ncol, ncol, D, y, y, s));
             c->launches += 3;
             return TDBEM_OK;

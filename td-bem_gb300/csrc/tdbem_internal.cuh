@@ -546,6 +546,9 @@ struct tdbem_ctx {
     double mtc_step_key[2] = {-1.0, -1.0};  // (a1, a2) of the planes' step matrices
     bool mtc_steps_valid = false;
     unsigned char* d_mtc_occ = nullptr;  // tile occupancy of the planes' slabs
+    // profiling: live 128 x 64 tiles per slab (summed over the row tiles), so that the
+    // convolution's bytes count the tiles it reads
+    std::vector<long long> h_occ_live;
     float* d_mtc_bc = nullptr;
     double* d_mtc_coef = nullptr;
     size_t mtc_coef_cap = 0;
