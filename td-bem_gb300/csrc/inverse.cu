@@ -846,80 +846,90 @@ constexpr int kGjThreads = 256;
 // pivoted (largest magnitude, lowest row on ties), rows left in place: at step c the
 // pivot row p_c is scaled and column c eliminated from every other row, and column
 // c's storage then holds the transformed identity column p_c.  The result S gives
-// A11^-1[c][j] = S[p_c][q] with p_q = j.  Double-buffered in shared memory (two
-// barriers per column); thread t updates 16 entries of row t / 4.  A zero pivot sets
-// *status = 2.
+// A11^-1[c][j] = S[p_c][q] with p_q = j.  Thread t keeps entries q0 .. q0 + 15 of row
+// t / 4 (q0 = 16 (t % 4)) in registers; per column the owners of column c publish it,
+// warp 0 picks the pivot, the pivot row's owners publish it scaled, and every thread
+// updates its entries (three barriers, 64 + 64 shared values per column).  The column
+// loop runs in blocks of 16 so that the owned entry of column c is a fixed register.
+// A zero pivot sets *status = 2.
 __global__ void __launch_bounds__(kGjThreads) k_block_inverse_f32(const float* __restrict__ A,
                                                                   int n, int k0, int bw,
                                                                   float* __restrict__ Ainv,
                                                                   int* __restrict__ status) {
     if (*status) return;
-    __shared__ float sm[2][64][65];
+    __shared__ float s_col[64], s_row[64];
     __shared__ int s_p[64], s_pinv[64], s_used[64];
     __shared__ float s_piv;
+    __shared__ int s_pc;
     const int t = threadIdx.x;
-    for (int idx = t; idx < 64 * 64; idx += kGjThreads) {
-        const int r = idx >> 6, c = idx & 63;
-        sm[0][r][c] = (r < bw && c < bw) ? A[(size_t)(k0 + r) * n + k0 + c]
-                                         : (r == c ? 1.f : 0.f);
+    const int r = t >> 2, q0 = (t & 3) * 16;
+    float a[16];
+#pragma unroll
+    for (int jj = 0; jj < 16; jj++) {
+        const int j = q0 + jj;
+        a[jj] = (r < bw && j < bw) ? A[(size_t)(k0 + r) * n + k0 + j] : (r == j ? 1.f : 0.f);
     }
     if (t < 64) s_used[t] = 0;
-    __syncthreads();
-    const int r = t >> 2, q0 = (t & 3) * 16;
-    int cur = 0;
-    for (int c = 0; c < 64; c++) {
-        float(*X)[65] = sm[cur];
-        float(*Y)[65] = sm[cur ^ 1];
-        if (t < 32) {
-            const float v0 = s_used[t] ? -1.f : fabsf(X[t][c]);
-            const float v1 = s_used[t + 32] ? -1.f : fabsf(X[t + 32][c]);
-            float best = v0;
-            int bi = t;
-            if (v1 > best) {
-                best = v1;
-                bi = t + 32;
-            }
+    for (int cb = 0; cb < 64; cb += 16) {
+        const bool own = q0 == cb;  // this thread holds columns cb .. cb + 15 of its row
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
-                const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (v2 > best || (v2 == best && i2 < bi)) {
-                    best = v2;
-                    bi = i2;
+        for (int ci = 0; ci < 16; ci++) {
+            const int c = cb + ci;
+            if (own) s_col[r] = a[ci];
+            __syncthreads();
+            if (t < 32) {
+                const float v0 = s_used[t] ? -1.f : fabsf(s_col[t]);
+                const float v1 = s_used[t + 32] ? -1.f : fabsf(s_col[t + 32]);
+                float best = v0;
+                int bi = t;
+                if (v1 > best) {
+                    best = v1;
+                    bi = t + 32;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float v2 = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (v2 > best || (v2 == best && i2 < bi)) {
+                        best = v2;
+                        bi = i2;
+                    }
+                }
+                if (t == 0) {
+                    s_pc = best > 0.f ? bi : -1;
+                    s_p[c] = bi;
+                    if (best > 0.f) {
+                        s_used[bi] = 1;
+                        s_piv = 1.f / s_col[bi];
+                    }
                 }
             }
-            if (t == 0) {
-                s_p[c] = best > 0.f ? bi : -1;
-                if (best > 0.f) {
-                    s_used[bi] = 1;
-                    s_piv = 1.f / X[bi][c];
-                }
+            __syncthreads();
+            const int p = s_pc;
+            if (p < 0) {  // the same on every thread
+                if (t == 0) *status = 2;
+                return;
+            }
+            const float piv = s_piv;
+            if (r == p) {  // the pivot row, scaled (its column c becomes piv)
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++)
+                    s_row[q0 + jj] = (own && jj == ci ? 1.f : a[jj]) * piv;
+            }
+            const float f = s_col[r];
+            __syncthreads();
+#pragma unroll
+            for (int jj = 0; jj < 16; jj++) {
+                const float rp = s_row[q0 + jj];
+                a[jj] = r == p ? rp : (own && jj == ci ? 0.f : a[jj]) - f * rp;
             }
         }
-        __syncthreads();
-        const int p = s_p[c];
-        if (p < 0) {  // the same on every thread
-            if (t == 0) *status = 2;
-            return;
-        }
-        const float piv = s_piv;
-        const float f = X[r][c];
-#pragma unroll
-        for (int jj = 0; jj < 16; jj++) {
-            const int j = q0 + jj;
-            const float rp = (j == c ? 1.f : X[p][j]) * piv;
-            Y[r][j] = r == p ? rp : (j == c ? 0.f : X[r][j]) - f * rp;
-        }
-        __syncthreads();
-        cur ^= 1;
     }
+    __syncthreads();
     if (t < 64) s_pinv[s_p[t]] = t;
     __syncthreads();
 #pragma unroll
-    for (int jj = 0; jj < 16; jj++) {
-        const int q = q0 + jj;
-        Ainv[s_pinv[r] * 64 + s_p[q]] = sm[cur][r][q];
-    }
+    for (int jj = 0; jj < 16; jj++) Ainv[s_pinv[r] * 64 + s_p[q0 + jj]] = a[jj];
 }
 
 // B[c][j] = sum_d Ainv[c][d] A[k0 + d][j] (T12) for j outside the panel columns and
