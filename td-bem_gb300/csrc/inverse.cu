@@ -610,14 +610,22 @@ __global__ void __launch_bounds__(256) k_rich_b(const double* __restrict__ A, in
     }
 }
 
+// Whether the previous sweep (its error word prev, null for the first) has already
+// reached the tolerance: the sweeps after it do nothing.
+__device__ __forceinline__ bool rich_done(const unsigned* prev, unsigned tol_bits) {
+    return prev && *prev <= tol_bits;
+}
+
 // x = X r32 (accumulate = 0) or x += X r32; err_bits (if set) receives
 // max_i |x_i - v_i| as float bits.
 __global__ void __launch_bounds__(256) k_rich_x(const float* __restrict__ X, int n,
                                                 const float* __restrict__ r32,
                                                 double* __restrict__ x, int accumulate,
-                                                unsigned* __restrict__ err_bits) {
+                                                unsigned* __restrict__ err_bits,
+                                                const unsigned* __restrict__ prev,
+                                                unsigned tol_bits) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= n) return;
+    if (w >= n || rich_done(prev, tol_bits)) return;
     const float* row = X + (size_t)w * n;
     float acc = 0.f;
     for (int j = lane; j < n; j += 32) acc += row[j] * r32[j];
@@ -638,9 +646,11 @@ __global__ void __launch_bounds__(256) k_rich_x(const float* __restrict__ X, int
 __global__ void __launch_bounds__(256) k_rich_r(const double* __restrict__ A, int n,
                                                 const double* __restrict__ x,
                                                 const double* __restrict__ b,
-                                                float* __restrict__ r32) {
+                                                float* __restrict__ r32,
+                                                const unsigned* __restrict__ prev,
+                                                unsigned tol_bits) {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= n) return;
+    if (w >= n || rich_done(prev, tol_bits)) return;
     const double* row = A + (size_t)w * n;
     double acc = 0;
     for (int j = lane; j < n; j += 32) acc += row[j] * x[j];
@@ -1230,11 +1240,17 @@ cudaError_t richardson_probe(const double* A, const float* X, int n, double* wor
     cudaError_t e = cudaMemsetAsync(err, 0, sizeof(unsigned) * (max_sweeps + 1), s);
     if (e != cudaSuccess) return e;
     const unsigned g = (unsigned)(((size_t)n * 32 + 255) / 256);
+    // a sweep after the first that reaches the tolerance returns at once (the count is
+    // all that is kept; the later error words stay 0)
+    const float tol_err = (float)(tol * 6.5);
+    unsigned tol_bits = 0;
+    std::memcpy(&tol_bits, &tol_err, sizeof(tol_bits));
     k_rich_b<<<g, 256, 0, s>>>(A, n, b, r32);
-    k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 0, err);
+    k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 0, err, nullptr, tol_bits);
     for (int it = 1; it <= max_sweeps; it++) {
-        k_rich_r<<<g, 256, 0, s>>>(A, n, x, b, r32);
-        k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 1, err + it);
+        const unsigned* prev = it >= 2 ? err + it - 1 : nullptr;
+        k_rich_r<<<g, 256, 0, s>>>(A, n, x, b, r32, prev, tol_bits);
+        k_rich_x<<<g, 256, 0, s>>>(X, n, r32, x, 1, err + it, prev, tol_bits);
     }
     *nlaunch += 2 + 2LL * max_sweeps;
     std::vector<unsigned> bits(max_sweeps + 1);
@@ -1242,10 +1258,10 @@ cudaError_t richardson_probe(const double* A, const float* X, int n, double* wor
                         s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return e;
+    // the test the sweeps applied on the device (max |x - v| <= tol max |v|, as float
+    // bits): the first sweep that passes it
     for (int it = 1; it <= max_sweeps; it++) {
-        float ef;
-        std::memcpy(&ef, &bits[it], sizeof(ef));
-        if (ef / 6.5 <= tol) {
+        if (bits[it] <= tol_bits) {
             *sweeps = it;
             break;
         }
