@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
     const float* a = A + (size_t)row * D;
     float acc = 0.f;
     if ((D & 1) == 0) {
-        // eight independent 8-byte loads per lane in flight (a warp per row leaves
+        // sixteen independent 8-byte loads per lane in flight (a warp per row leaves
         // too few bytes in flight to cover HBM latency with fewer: four measured
         // 3.7 TB/s at D = 4614)
         const float2* a2 = reinterpret_cast<const float2*>(a);
@@ -221,6 +221,16 @@ __global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, i
         const int n2 = D / 2;
         float c[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         int j = lane;
+        for (; j + 480 < n2; j += 512) {
+            float2 x[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) x[u] = __ldcs(a2 + j + 32 * u);
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const float2 w = v2[j + 32 * u];
+                c[u & 7] += x[u].x * w.x + x[u].y * w.y;
+            }
+        }
         for (; j + 224 < n2; j += 256) {
             float2 x[8];
 #pragma unroll
