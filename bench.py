@@ -566,6 +566,13 @@ def run_ours(args, dist):
                 "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
                 "frac": (achieved / fp64) if fp64 else None,
                 "peak_source": f"{key}: cuBLAS GEMM measured in this run"}
+        if dom == "assemble_f32":
+            roof["flops_counted"] = (
+                "algorithmic: every far (node, element, level) item x its Gauss points x 425 "
+                "flops, settled levels included; about half the items are settled levels, "
+                "which the kernel produces from one quasi-static pass per pair (201 flops "
+                "per point) and one scaled add per level, so it executes fewer flops than "
+                "it is credited with")
     roof["launches"] = st["launches"]
     roof["avg_launch_ms"] = st["ms"] / max(1, st["launches"])
     tkey = f"{args.workload}:{args.precision}:{dom}"

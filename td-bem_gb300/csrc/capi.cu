@@ -736,9 +736,12 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
                                          c->stream));
                 CUDA_TRY(cudaStreamSynchronize(c->stream));
                 c->prof_pending[pe].bytes = (double)(n[0] + n[2]) * 4 * 45 * 4.0 * 2;
-                c->prof_pending[pe].flops = (double)n[0] * c->nq * c->nq * kFlopsPerItemPointF32 +
-                                            (double)n[1] * c->nq * c->nq * kFlopsSettledPoint +
-                                            (double)n[2] * kFlopsSettledLevel;
+                // algorithmic flops: every far (node, element, level) item's Gauss points at
+                // the per-point count, settled levels included (a settled job produces
+                // them from one quasi-static pass per pair: kFlopsSettledPoint per point
+                // and kFlopsSettledLevel per level executed)
+                c->prof_pending[pe].flops =
+                    (double)(n[0] + n[2]) * c->nq * c->nq * kFlopsPerItemPointF32;
             }
         }
         // levels 0/1 (with the C term) from the FP64 pair
