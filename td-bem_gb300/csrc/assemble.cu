@@ -928,7 +928,7 @@ struct PhysF {
 // FP64 as the FP64 quadrature decides them.
 constexpr float kTauMargin = 64.f / 16777216.f;
 
-__device__ __forceinline__ PhysF to_f(const Phys& p) {
+__host__ __device__ __forceinline__ PhysF to_f(const Phys& p) {
     PhysF f;
     f.dt = (float)p.dt;
     f.inv_dt = (float)p.inv_dt;
@@ -1361,13 +1361,17 @@ constexpr int kFarJobCap = 4 * kFarBlock;
 // A pair's settled levels (settled_range) leave its item list and go to one settled
 // job; the items come first in the thread order and the jobs after them, so most
 // warps hold one kind of work.  level_top: the highest level any window reaches.
+// f: ph's FP32 constants, converted on the host.  Kernel parameters are operands of
+// the FP32 instructions as they stand; converted in the kernel, they were re-derived
+// from ph at their uses (one FP64-to-FP32 conversion each, ~14 per Gauss point) to
+// save registers, and GB300 runs conversions on its narrow FP64 pipe.
 // nitems (if not null) receives the item, job and settled-level counts.
 template <typename T>
 __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_far_rows(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ color_elems, const int* __restrict__ color_start, int ncolor,
     int nel, int nq2, const float* __restrict__ geomf, const double* __restrict__ geom,
-    const float* __restrict__ coordf, Phys ph, int level_last, int level_top,
+    const float* __restrict__ coordf, Phys ph, PhysF f, int level_last, int level_top,
     const PairInfo* __restrict__ pairs, AsmOut out, unsigned long long* __restrict__ nitems) {
     __shared__ int s_warp[kFarBlock / 32];
     __shared__ int s_items[kFarItemCap];          // (element in colour) << bits | level
@@ -1378,7 +1382,6 @@ __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_fa
     const int k1 = min(k0 + kFarChunk, level_top + 1);
     // settled levels need both parts (1 <= k <= level_last - 1) and k >= 2
     const bool settle = k1 - 1 >= 2 && level_last >= 3;
-    const PhysF f = to_f(ph);
     const PairInfo* pc = pairs + (size_t)c * nel;
     unsigned long long count = 0, njobs = 0, nsettled = 0;
     for (int col = 0; col < ncolor; col++) {
@@ -1817,16 +1820,17 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
     const int top = std::min(level_last, level_cap);
     if (top < 0) return cudaSuccess;
     const dim3 grid(nnd, (top + kFarChunk) / kFarChunk);
+    const PhysF f = to_f(ph);
     if (fp64_out)
         k_assemble_far_rows<double><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                                color_start, ncolor, nel, nq * nq,
-                                                               geomf, geom, coordf, ph,
+                                                               geomf, geom, coordf, ph, f,
                                                                level_last, top, pairs, out,
                                                                nitems);
     else
         k_assemble_far_rows<float><<<grid, kFarBlock, 0, s>>>(coords, ien, color_elems,
                                                               color_start, ncolor, nel, nq * nq,
-                                                              geomf, geom, coordf, ph,
+                                                              geomf, geom, coordf, ph, f,
                                                               level_last, top, pairs, out,
                                                               nitems);
     return cudaGetLastError();
