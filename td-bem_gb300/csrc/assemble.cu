@@ -428,21 +428,20 @@ __device__ __forceinline__ unsigned find_pair(const unsigned* __restrict__ offse
     return lo;
 }
 
-// The pair of this thread's item (item = global thread index >> SH): one full
+// The pair of this thread's item (item = global thread index >> sh): one full
 // search per block for its first and last items, then a short search inside that
 // range.  Call with all threads of the block (it synchronises); returns false
 // for threads past the last item.
-template <int SH = 0>
 __device__ __forceinline__ bool item_pair(const unsigned* __restrict__ offsets, unsigned npairs,
-                                          unsigned nitems, unsigned& p) {
+                                          unsigned nitems, unsigned& p, int sh = 0) {
     __shared__ unsigned s_lo, s_hi;
-    const unsigned first = (blockIdx.x * blockDim.x) >> SH;
+    const unsigned first = (blockIdx.x * blockDim.x) >> sh;
     if (first >= nitems) return false;  // uniform over the block
-    const unsigned last = min(first + (blockDim.x >> SH), nitems) - 1;
+    const unsigned last = min(first + (blockDim.x >> sh), nitems) - 1;
     if (threadIdx.x == 0) s_lo = find_pair(offsets, 0, npairs - 1, first);
     if (threadIdx.x == 32) s_hi = find_pair(offsets, 0, npairs - 1, last);
     __syncthreads();
-    const unsigned item = first + (threadIdx.x >> SH);
+    const unsigned item = first + (threadIdx.x >> sh);
     if (item >= nitems) return false;
     p = find_pair(offsets, s_lo, s_hi, item);
     return true;
@@ -546,13 +545,18 @@ __global__ void k_pair_window(const double* __restrict__ coords, const int* __re
 // level (or step) k; accumulates its Gauss points and scatters into out.  An
 // 8-node element's item is split over two threads, half 0 holding the blocks of
 // nodes 0-3 and half 1 those of nodes 4-7 (each evaluates every point's kernels).
+// L > 1 (a power of two, at most 32): L aligned lanes of a warp share the item (or
+// half), lane sub taking every L-th Gauss point; an xor butterfly of shuffles then
+// gives every lane the item's sums (bitwise the same on all lanes: each addition
+// has the same two operands on both lanes of a pair), and the lanes split the
+// scatter by node.  L = 1 is one thread's sequential sum.
 template <int MODE, int ENND = 4>
 __device__ __forceinline__ void assemble_item(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
     const double* __restrict__ gw, const double* __restrict__ geom, const Phys& ph,
     int level_last, int step_n, int part, const PairInfo& pi, unsigned p, int k,
-    const AsmOut& out, int half = 0) {
+    const AsmOut& out, int half = 0, int sub = 0, int L = 1) {
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
@@ -582,9 +586,10 @@ __device__ __forceinline__ void assemble_item(
     const int nq2 = nq * nq;
     constexpr int stride = ENND == 8 ? kGeomStride8 : kGeomStride;
     if (pi.sing < 0) {
-        const double* g = geom + (size_t)e * nq2 * stride;
+        const double* g0 = geom + (size_t)e * nq2 * stride;
         const int n0 = 7 + 4 * half;
-        for (int q = 0; q < nq2; q++, g += stride) {
+        for (int q = sub; q < nq2; q += L) {
+            const double* g = g0 + (size_t)q * stride;
             const double xq[3] = {__ldg(g), __ldg(g + 1), __ldg(g + 2)};
             const double nqv[3] = {__ldg(g + 3), __ldg(g + 4), __ldg(g + 5)};
             const double N[4] = {__ldg(g + n0), __ldg(g + n0 + 1), __ldg(g + n0 + 2),
@@ -609,7 +614,7 @@ __device__ __forceinline__ void assemble_item(
 #pragma unroll
                 for (int d = 0; d < 3; d++) cn[i * 3 + d] = coords[n * 3 + d];
             }
-            for (int qq = 0; qq < 2 * nq2; qq++) {
+            for (int qq = sub; qq < 2 * nq2; qq += L) {
                 const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
                 double N4[4], xq[3], nqv[3], wJ;
                 duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N4, xq, nqv,
@@ -629,13 +634,30 @@ __device__ __forceinline__ void assemble_item(
         for (int a = 0; a < 4; a++)
 #pragma unroll
             for (int d = 0; d < 3; d++) cn[a * 3 + d] = coords[nid[a] * 3 + d];
-        for (int qq = 0; qq < 2 * nq2; qq++) {
+        for (int qq = sub; qq < 2 * nq2; qq += L) {
             const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
             double N[4], xq[3], nqv[3], wJ;
             duffy_point(cn, pi.sing, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nqv, wJ);
             gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
         }
     }
+
+    if (L > 1) {
+        const unsigned lane = threadIdx.x & 31;
+        const unsigned mask =
+            L == 32 ? 0xffffffffu : ((1u << L) - 1) << (lane & ~(unsigned)(L - 1));
+        for (int o = 1; o < L; o <<= 1) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+#pragma unroll
+                for (int m = 0; m < 6; m++) acc.g[a][m] += __shfl_xor_sync(mask, acc.g[a][m], o);
+#pragma unroll
+                for (int m = 0; m < 9; m++) acc.h[a][m] += __shfl_xor_sync(mask, acc.h[a][m], o);
+            }
+        }
+    }
+    // lane sub writes the blocks of the nodes a with (a & own) == sub
+    const int own = min(L, 4) - 1;
 
     // scatter: rows 3c+i, columns 3*nid[a]+j
     const size_t D = (size_t)out.ld;
@@ -660,6 +682,7 @@ __device__ __forceinline__ void assemble_item(
     // writes (as in far_item)
 #pragma unroll
     for (int a = 0; a < 4; a++) {
+        if ((a & own) != sub) continue;
         if (Gf) {
             float og[9], oh[9];
 #pragma unroll
@@ -694,23 +717,26 @@ __device__ __forceinline__ void assemble_item(
 
 
 
-// One thread per item (4-node elements) or two adjacent threads per item (8-node
-// elements, one per half of the element's nodes).
+// 2^lg adjacent lanes per item (4-node elements) or per half of an item (8-node
+// elements, one half per group of the element's nodes).
 template <int MODE, int ENND>
 __global__ void __launch_bounds__(128) k_assemble_items(
     const double* __restrict__ coords, const int* __restrict__ ien,
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
     const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
     int step_n, int part, const PairInfo* __restrict__ pairs,
-    const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out) {
+    const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out,
+    int lg) {
     constexpr int SH = ENND == 8 ? 1 : 0;
     unsigned p;
-    if (!item_pair<SH>(offsets, npairs, nitems, p)) return;
+    if (!item_pair(offsets, npairs, nitems, p, SH + lg)) return;
     const unsigned gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned unit = gid >> lg;
     const PairInfo pi = pairs[p];
-    const int k = pi.klo + (int)((gid >> SH) - __ldg(offsets + p));
+    const int k = pi.klo + (int)((unit >> SH) - __ldg(offsets + p));
     assemble_item<MODE, ENND>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, level_last,
-                              step_n, part, pi, p, k, out, (int)(gid & SH));
+                              step_n, part, pi, p, k, out, (int)(unit & SH),
+                              (int)(gid & ((1u << lg) - 1)), 1 << lg);
 }
 
 // One step (ASM_STEP) without compaction: one thread per pair (two for an 8-node
@@ -718,7 +744,10 @@ __global__ void __launch_bounds__(128) k_assemble_items(
 // at most one item of a step, so this needs neither a scan of the counts nor the
 // item total on the host; the allocation-free driver (noalloc.cu) uses it so that
 // a call never waits for the device.  Same items, same arithmetic and the same
-// colour-ordered scatter as k_assemble_items, so the same results bit for bit.
+// colour-ordered scatter as k_assemble_items with one lane per item, so the same
+// results bit for bit as that; where k_assemble_items splits an item's points over
+// lanes (launches of few items) its sums are formed in another order (~1e-16
+// relative).
 template <int ENND>
 __global__ void __launch_bounds__(128) k_assemble_step_pairs(
     const double* __restrict__ coords, const int* __restrict__ ien,
@@ -1734,17 +1763,31 @@ static void launch_items_fp64(const double* coords, const int* ien, const int* e
                               const unsigned* offsets, unsigned npairs, unsigned nitems,
                               const AsmOut& out, cudaStream_t s) {
     const int bs = 128;
-    const unsigned long long threads = (unsigned long long)nitems << (ENND == 8 ? 1 : 0);
+    // Lanes per item: a launch of few items (the near field of one colour: a few
+    // thousand) would hold a handful of blocks, each thread summing 36-72 FP64 Gauss
+    // points in turn on the few SMs it lands on; split the points over up to 32 lanes
+    // until the launch fills two residencies of the GPU (two 128-thread blocks of 255
+    // registers per SM).
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms <= 0)
+        sms = 1;
+    const unsigned long long want = (unsigned long long)sms * 2 * 2 * bs;
+    const int sh = ENND == 8 ? 1 : 0;
+    int lg = 0;
+    while (lg < 5 && ((unsigned long long)nitems << (sh + lg)) < want) lg++;
+    const unsigned long long threads = (unsigned long long)nitems << (sh + lg);
     const unsigned grid = (unsigned)((threads + bs - 1) / bs);
     if (mode == ASM_LEVELS) {
         k_assemble_items<ASM_LEVELS, ENND><<<grid, bs, 0, s>>>(
             coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last, step_n, 0,
-            pairs, offsets, npairs, nitems, out);
+            pairs, offsets, npairs, nitems, out, lg);
     } else {
         for (int part = 0; part < 2; part++)
             k_assemble_items<ASM_STEP, ENND><<<grid, bs, 0, s>>>(
                 coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last,
-                step_n, part, pairs, offsets, npairs, nitems, out);
+                step_n, part, pairs, offsets, npairs, nitems, out, lg);
     }
 }
 
