@@ -461,20 +461,13 @@ __device__ __forceinline__ int singular_corner(const double* c, const double xc[
     return s;
 }
 
-// Level window (or step membership) and singular corner of pair p (collocation
-// node node_lo + p / ne, element elems[p % ne]).
-template <int ENND = 4>
-__device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ coords,
-                                                     const int* __restrict__ ien,
-                                                     const int* __restrict__ elems, int ne,
-                                                     int node_lo, const Phys& ph, int mode,
-                                                     int level_last, int level_cap, int step_n,
-                                                     int select, long long p) {
-    const int c = node_lo + (int)(p / ne);
-    const int e = elems[p % ne];
-    const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
-    double nd[3 * ENND];
-    double ctr[3] = {0, 0, 0};
+// Node coordinates (nd), node centroid (ctr) and the largest node distance from it
+// (the return value) of element e.
+template <int ENND>
+__device__ __forceinline__ double element_box(const double* __restrict__ coords,
+                                              const int* __restrict__ ien, int e,
+                                              double nd[3 * ENND], double ctr[3]) {
+    ctr[0] = ctr[1] = ctr[2] = 0;
     for (int a = 0; a < ENND; a++) {
         const int nid = ien[e * ENND + a];
         for (int d = 0; d < 3; d++) {
@@ -487,6 +480,42 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
         const double dx = nd[a * 3] - ctr[0], dy = nd[a * 3 + 1] - ctr[1], dz = nd[a * 3 + 2] - ctr[2];
         rad = fmax(rad, sqrt(dx * dx + dy * dy + dz * dz));
     }
+    return rad;
+}
+
+// Distance from a node beyond which no node of the element passes the singular test
+// (r^2 < 1e-9, r < 3.2e-5): every node lies within rad of the centroid.
+constexpr double kSingularClear = 1e-4;
+
+// Level window (or step membership) and singular corner of pair p (collocation
+// node node_lo + p / ne, element elems[p % ne]).  ebox (may be null): per element
+// the centroid and node radius of element_box, made once per mesh (k_element_box);
+// with it a pair takes one FP64 square root instead of five, and reads the element's
+// nodes only when the node is within kSingularClear of the element's node radius.
+template <int ENND = 4>
+__device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ coords,
+                                                     const int* __restrict__ ien,
+                                                     const int* __restrict__ elems, int ne,
+                                                     int node_lo, const Phys& ph, int mode,
+                                                     int level_last, int level_cap, int step_n,
+                                                     int select, long long p,
+                                                     const ElemBox* __restrict__ ebox = nullptr) {
+    const int c = node_lo + (int)(p / ne);
+    const int e = elems[p % ne];
+    const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
+    double nd[3 * ENND];
+    double ctr[3];
+    double rad;
+    if (ebox) {
+        const ElemBox b = ebox[e];
+        ctr[0] = b.x;
+        ctr[1] = b.y;
+        ctr[2] = b.z;
+        rad = b.rad;
+    } else {
+        rad = element_box<ENND>(coords, ien, e, nd, ctr);
+    }
+    const double rad_nodes = rad;
     // An 8-node element's surface x = sum N_a x_a is no convex combination of its
     // nodes; sum |N_a| <= 3 on the reference square (at its centre), so the surface
     // lies within 3 rad of the node centroid.
@@ -495,7 +524,16 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
     const double dist = sqrt(dx * dx + dy * dy + dz * dz);
     const double margin = 1e-3 * rad + 1e-12;
     const double rmin = fmax(0.0, dist - rad - margin), rmax = dist + rad + margin;
-    const int sing = singular_corner<ENND>(nd, xc);
+    int sing = -1;
+    if (!ebox) {
+        sing = singular_corner<ENND>(nd, xc);
+    } else if (dist <= rad_nodes + kSingularClear) {
+        for (int a = 0; a < ENND; a++) {
+            const int nid = ien[e * ENND + a];
+            for (int d = 0; d < 3; d++) nd[a * 3 + d] = coords[nid * 3 + d];
+        }
+        sing = singular_corner<ENND>(nd, xc);
+    }
     // The step response at time n dt is exactly zero unless r/c_p <= n dt and
     // n < r/(c_s dt) + 2; level k takes n = k (I part) and n = k + 1 (J part), so it
     // can be non-zero only for r_min/(c_p dt) - 1 <= k < r_max/(c_s dt) + 1 (one level
@@ -524,15 +562,25 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
 }
 
 template <int ENND>
+__global__ void k_element_box(const double* __restrict__ coords, const int* __restrict__ ien,
+                              int nel, ElemBox* __restrict__ ebox) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nel) return;
+    double nd[3 * ENND], ctr[3];
+    const double rad = element_box<ENND>(coords, ien, e, nd, ctr);
+    ebox[e] = ElemBox{ctr[0], ctr[1], ctr[2], rad};
+}
+
+template <int ENND>
 __global__ void k_pair_window(const double* __restrict__ coords, const int* __restrict__ ien,
                               const int* __restrict__ elems, int ne, int node_lo, int nnodes,
                               Phys ph, int mode, int level_last, int level_cap, int step_n,
                               int select, PairInfo* __restrict__ pairs,
-                              unsigned* __restrict__ counts) {
+                              unsigned* __restrict__ counts, const ElemBox* __restrict__ ebox) {
     const long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= (long long)nnodes * ne) return;
     const PairInfo pi = pair_window_info<ENND>(coords, ien, elems, ne, node_lo, ph, mode,
-                                               level_last, level_cap, step_n, select, p);
+                                               level_last, level_cap, step_n, select, p, ebox);
     pairs[p] = pi;
     if (counts) counts[p] = (unsigned)pi.cnt;
 }
@@ -1495,11 +1543,17 @@ __global__ void __launch_bounds__(kFarBlock, TDBEM_FAR_MIN_BLOCKS) k_assemble_fa
 // C term of node c, computed by the whole block (256 threads), into dst[9].  A
 // singular 8-node element contributes through its 4-node sub-elements.  FAST (the
 // mixed-precision assembly): a regular element's points in FP32, summed in FP32
-// per element and in FP64 across elements (relative error ~1e-7 of C); for 4-node
-// elements from the FP32 geometry table (points relative to the element's first
-// node, so the only FP64 arithmetic is the node's offset to that node, once per
-// element), for 8-node elements from the FP64 points' offsets to the node;
-// singular elements as in the FP64 form.
+// per element and across a thread's elements with a TwoSum compensation term
+// (Knuth's error-free addition: the pair (sum, compensation) carries the sum to
+// ~1e-14), in FP64 across threads; relative error ~1e-7 of C.  For 4-node elements
+// from the FP32 geometry table (points relative to the element's first node) and
+// the node's offset to that node from the coordinates' FP32 pairs (coordf), so no
+// FP64 arithmetic per regular element but the singular filter; for 8-node elements
+// from the FP64 points' offsets to the node.  Singular elements as in the FP64
+// form.  ebox (may be null): the mesh's element boxes; an element whose node
+// radius the node is kSingularClear beyond skips the singular test (and the loads
+// of its nodes).  onem2nu_f, kscale_f: the FAST path's FP32 constants, converted
+// on the host.
 template <int ENND = 4, bool FAST = false>
 __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const int* __restrict__ ien, int nel, int c, int nq,
@@ -1507,108 +1561,166 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const double* __restrict__ gw,
                                            const double* __restrict__ geom, const Phys& ph,
                                            double* __restrict__ dst,
-                                           const float* __restrict__ geomf = nullptr) {
+                                           const float* __restrict__ geomf = nullptr,
+                                           const float* __restrict__ coordf = nullptr,
+                                           const ElemBox* __restrict__ ebox = nullptr,
+                                           float onem2nu_f = 0.f, float kscale_f = 0.f) {
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float s32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, e32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int nq2 = nq * nq;
     const double onem2nu = 1 - 2 * ph.nu;
     // Kelvin_Linear (GreenFunctionT.cpp:205-231): K = [..] / (-8 pi (1-nu) r^2) * 0.5 dt
     const double kscale = (0.5 * ph.dt) / (-(8 * M_PI) * (1 - ph.nu));
     constexpr int stride = ENND == 8 ? kGeomStride8 : kGeomStride;
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-        double en[3 * ENND];
-        for (int a = 0; a < ENND; a++) {
-            const int nid = ien[e * ENND + a];
-            for (int d = 0; d < 3; d++) en[a * 3 + d] = coords[nid * 3 + d];
-        }
-        const int sing = singular_corner<ENND>(en, xc);
-        // singular: sub-elements (one for a 4-node element: itself) x 2 triangles
-        int ids[2][4] = {{0, 1, 2, 3}, {0, 1, 2, 3}}, cid[2] = {sing, sing};
-        int nsub = 1;
-        if (ENND == 8 && sing >= 0) nsub = q8_subelements(sing, ids, cid);
-        const int npts = sing < 0 ? nq2 : nsub * 2 * nq2;
-        if (FAST && sing < 0) {
-            const float onem2nu_f = (float)onem2nu, kscale_f = (float)kscale;
-            float a32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-            // the node relative to the element's first node (4-node FP32 table)
-            const float xr[3] = {(float)(xc[0] - en[0]), (float)(xc[1] - en[1]),
-                                 (float)(xc[2] - en[2])};
-            for (int qq = 0; qq < nq2; qq++) {
-                float d0, d1, d2, nv[3], wJf;
-                if (ENND == 4 && geomf) {
-                    const float4* g4 =
-                        reinterpret_cast<const float4*>(geomf + ((size_t)e * nq2 + qq) * 12);
-                    const float4 p0 = __ldg(g4), p1 = __ldg(g4 + 1);
-                    d0 = p0.x - xr[0];
-                    d1 = p0.y - xr[1];
-                    d2 = p0.z - xr[2];
-                    nv[0] = p0.w;
-                    nv[1] = p1.x;
-                    nv[2] = p1.y;
-                    wJf = p1.z;
-                } else {
-                    const double* g = geom + ((size_t)e * nq2 + qq) * stride;
-                    d0 = (float)(g[0] - xc[0]);
-                    d1 = (float)(g[1] - xc[1]);
-                    d2 = (float)(g[2] - xc[2]);
-                    nv[0] = (float)g[3];
-                    nv[1] = (float)g[4];
-                    nv[2] = (float)g[5];
-                    wJf = (float)g[6];
+    const bool pairs4 = FAST && ENND == 4 && geomf && coordf;
+    // C[i][k] -= wJ K[k][i] at an FP64 point
+    auto kelvin64 = [&](const double xq[3], const double nv[3], double wJ) {
+        const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
+        const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
+        const double inv_r = 1.0 / sqrt(r2);
+        const double rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+        const double rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
+        const double w = wJ * (kscale * inv_r * inv_r);
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int kk = 0; kk < 3; kk++) {
+                const double Kki = ((kk == i ? onem2nu : 0.0) + 3 * rv[kk] * rv[i]) * rdn -
+                                   onem2nu * (rv[i] * nv[kk] - rv[kk] * nv[i]);
+                acc[i * 3 + kk] -= w * Kki;
+            }
+    };
+    // Rounds of one element per thread (blockDim.x = 256).  A regular element is summed
+    // by its thread.  The round's singular elements (the node's few) are listed in
+    // thread order and their Duffy points spread over the block: summed by their own
+    // threads, 2 nq^2 FP64 points per sub-element would keep single lanes busy on the
+    // FP64 pipe while the rest of their warps wait.
+    __shared__ int s_sing[256];  // element << 3 | singular corner
+    __shared__ int s_wcnt[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int base = 0; base < nel; base += blockDim.x) {
+        const int e = base + threadIdx.x;
+        int sing = -1;
+        if (e < nel) {
+            bool near = true;
+            if (ebox) {
+                const ElemBox b = ebox[e];
+                const double dx = xc[0] - b.x, dy = xc[1] - b.y, dz = xc[2] - b.z;
+                const double lim = b.rad + kSingularClear;
+                near = dx * dx + dy * dy + dz * dz <= lim * lim;
+            }
+            if (near) {
+                double en[3 * ENND];
+                for (int a = 0; a < ENND; a++) {
+                    const int nid = ien[e * ENND + a];
+                    for (int d = 0; d < 3; d++) en[a * 3 + d] = coords[nid * 3 + d];
                 }
-                const float inv_r = rsqrtf(d0 * d0 + d1 * d1 + d2 * d2);
-                const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
-                const float rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
-                const float w = wJf * (kscale_f * inv_r * inv_r);
-#pragma unroll
-                for (int i = 0; i < 3; i++)
-#pragma unroll
-                    for (int kk = 0; kk < 3; kk++) {
-                        const float Kki = ((kk == i ? onem2nu_f : 0.f) + 3.f * rv[kk] * rv[i]) * rdn -
-                                          onem2nu_f * (rv[i] * nv[kk] - rv[kk] * nv[i]);
-                        a32[i * 3 + kk] -= w * Kki;
+                sing = singular_corner<ENND>(en, xc);
+            }
+            if (FAST && sing < 0) {
+                float a32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                // the node relative to the element's first node (4-node FP32 table), from
+                // the FP32 pairs (hi - hi) + (lo - lo): ~1.5 eps relative
+                float xr[3] = {0.f, 0.f, 0.f};
+                if (pairs4) {
+                    const float4* cf4 = reinterpret_cast<const float4*>(coordf);
+                    const int n0 = ien[e * 4];
+                    const float4 ch = __ldg(cf4 + 2 * c), cl = __ldg(cf4 + 2 * c + 1);
+                    const float4 eh = __ldg(cf4 + 2 * n0), el = __ldg(cf4 + 2 * n0 + 1);
+                    xr[0] = (ch.x - eh.x) + (cl.x - el.x);
+                    xr[1] = (ch.y - eh.y) + (cl.y - el.y);
+                    xr[2] = (ch.z - eh.z) + (cl.z - el.z);
+                }
+                for (int qq = 0; qq < nq2; qq++) {
+                    float d0, d1, d2, nv[3], wJf;
+                    if (pairs4) {
+                        const float4* g4 =
+                            reinterpret_cast<const float4*>(geomf + ((size_t)e * nq2 + qq) * 12);
+                        const float4 p0 = __ldg(g4), p1 = __ldg(g4 + 1);
+                        d0 = p0.x - xr[0];
+                        d1 = p0.y - xr[1];
+                        d2 = p0.z - xr[2];
+                        nv[0] = p0.w;
+                        nv[1] = p1.x;
+                        nv[2] = p1.y;
+                        wJf = p1.z;
+                    } else {
+                        const double* g = geom + ((size_t)e * nq2 + qq) * stride;
+                        d0 = (float)(g[0] - xc[0]);
+                        d1 = (float)(g[1] - xc[1]);
+                        d2 = (float)(g[2] - xc[2]);
+                        nv[0] = (float)g[3];
+                        nv[1] = (float)g[4];
+                        nv[2] = (float)g[5];
+                        wJf = (float)g[6];
                     }
-            }
+                    const float inv_r = rsqrtf(d0 * d0 + d1 * d1 + d2 * d2);
+                    const float rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
+                    const float rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
+                    const float w = wJf * (kscale_f * inv_r * inv_r);
 #pragma unroll
-            for (int m = 0; m < 9; m++) acc[m] += (double)a32[m];
-            continue;
-        }
-        double cn[12];
-        int cur = -1;
-        for (int qq = 0; qq < npts; qq++) {
-            double xq[3], nv[3], wJ;
-            if (sing < 0) {
-                const double* g = geom + ((size_t)e * nq2 + qq) * stride;
-                xq[0] = g[0]; xq[1] = g[1]; xq[2] = g[2];
-                nv[0] = g[3]; nv[1] = g[4]; nv[2] = g[5];
-                wJ = g[6];
-            } else {
-                const int se = qq / (2 * nq2), r = qq % (2 * nq2);
-                if (se != cur) {
-                    for (int i = 0; i < 4; i++)
-                        for (int d = 0; d < 3; d++) cn[i * 3 + d] = en[ids[se][i] * 3 + d];
-                    cur = se;
+                    for (int i = 0; i < 3; i++)
+#pragma unroll
+                        for (int kk = 0; kk < 3; kk++) {
+                            const float Kki = ((kk == i ? onem2nu_f : 0.f) + 3.f * rv[kk] * rv[i]) * rdn -
+                                              onem2nu_f * (rv[i] * nv[kk] - rv[kk] * nv[i]);
+                            a32[i * 3 + kk] -= w * Kki;
+                        }
                 }
-                const int tri = r / nq2, q = r % nq2, q1 = q / nq, q2 = q % nq;
-                double N[4];
-                duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
-            }
-            const double d0 = xq[0] - xc[0], d1 = xq[1] - xc[1], d2 = xq[2] - xc[2];
-            const double r2 = d0 * d0 + d1 * d1 + d2 * d2;
-            const double inv_r = 1.0 / sqrt(r2);
-            const double rv[3] = {d0 * inv_r, d1 * inv_r, d2 * inv_r};
-            const double rdn = rv[0] * nv[0] + rv[1] * nv[1] + rv[2] * nv[2];
-            const double w = wJ * (kscale * inv_r * inv_r);
-            // C[i][k] -= wJ K[k][i]
+                // TwoSum: t = s + a exactly as t + err
 #pragma unroll
-            for (int i = 0; i < 3; i++)
-#pragma unroll
-                for (int kk = 0; kk < 3; kk++) {
-                    const double Kki = ((kk == i ? onem2nu : 0.0) + 3 * rv[kk] * rv[i]) * rdn -
-                                       onem2nu * (rv[i] * nv[kk] - rv[kk] * nv[i]);
-                    acc[i * 3 + kk] -= w * Kki;
+                for (int m = 0; m < 9; m++) {
+                    const float t = s32[m] + a32[m];
+                    const float z = t - s32[m];
+                    e32[m] += (s32[m] - (t - z)) + (a32[m] - z);
+                    s32[m] = t;
                 }
+            } else if (sing < 0) {
+                for (int qq = 0; qq < nq2; qq++) {
+                    const double* g = geom + ((size_t)e * nq2 + qq) * stride;
+                    const double xq[3] = {g[0], g[1], g[2]}, nv[3] = {g[3], g[4], g[5]};
+                    kelvin64(xq, nv, g[6]);
+                }
+            }
         }
+        const unsigned bal = __ballot_sync(0xffffffffu, sing >= 0);
+        if (lane == 0) s_wcnt[warp] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < nwarp; w++) {
+            const int n = s_wcnt[w];
+            before += w < warp ? n : 0;
+            total += n;
+        }
+        if (sing >= 0) s_sing[before + __popc(bal & ((1u << lane) - 1))] = (e << 3) | sing;
+        __syncthreads();
+        // point slots of a singular element: sub-elements (up to 2 for an 8-node element,
+        // the element itself for a 4-node one) x 2 triangles x nq^2
+        const int slots = (ENND == 8 ? 4 : 2) * nq2;
+        for (int t = threadIdx.x; t < total * slots; t += blockDim.x) {
+            const int code = s_sing[t / slots], qq = t % slots;
+            const int es = code >> 3, sg = code & 7;
+            int ids[2][4] = {{0, 1, 2, 3}, {0, 1, 2, 3}}, cid[2] = {sg, sg};
+            int nsub = 1;
+            if (ENND == 8) nsub = q8_subelements(sg, ids, cid);
+            const int se = qq / (2 * nq2), r = qq % (2 * nq2);
+            if (se >= nsub) continue;
+            double cn[12];
+            for (int i = 0; i < 4; i++) {
+                const int nid = ien[es * ENND + ids[se][i]];
+                for (int d = 0; d < 3; d++) cn[i * 3 + d] = coords[nid * 3 + d];
+            }
+            const int tri = r / nq2, q = r % nq2, q1 = q / nq, q2 = q % nq;
+            double N[4], xq[3], nv[3], wJ;
+            duffy_point(cn, cid[se], tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
+            kelvin64(xq, nv, wJ);
+        }
+        __syncthreads();  // s_sing and s_wcnt are rewritten in the next round
+    }
+    if (FAST) {
+#pragma unroll
+        for (int m = 0; m < 9; m++) acc[m] += (double)s32[m] + (double)e32[m];
     }
     __shared__ double red[9][256];
     for (int m = 0; m < 9; m++) red[m][threadIdx.x] = acc[m];
@@ -1629,9 +1741,13 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
                                                const double* __restrict__ gw,
                                                const double* __restrict__ geom, Phys ph,
                                                double* __restrict__ cbuf,
-                                               const float* __restrict__ geomf) {
+                                               const float* __restrict__ geomf,
+                                               const float* __restrict__ coordf,
+                                               const ElemBox* __restrict__ ebox,
+                                               float onem2nu_f, float kscale_f) {
     cterm_node<ENND, FAST>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
-                           cbuf + (size_t)blockIdx.x * 9, geomf);
+                           cbuf + (size_t)blockIdx.x * 9, geomf, coordf, ebox, onem2nu_f,
+                           kscale_f);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -1736,10 +1852,23 @@ cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int
     return cudaGetLastError();
 }
 
+cudaError_t launch_element_box(const double* coords, const int* ien, int ennd, int nel,
+                               ElemBox* ebox, cudaStream_t s) {
+    if (nel == 0) return cudaSuccess;
+    const int bs = 128;
+    const unsigned grid = (unsigned)((nel + bs - 1) / bs);
+    if (ennd == 8)
+        k_element_box<8><<<grid, bs, 0, s>>>(coords, ien, nel, ebox);
+    else
+        k_element_box<4><<<grid, bs, 0, s>>>(coords, ien, nel, ebox);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
                                int mode, int level_last, int level_cap, int step_n, int select,
-                               PairInfo* pairs, unsigned* counts, cudaStream_t s) {
+                               PairInfo* pairs, unsigned* counts, cudaStream_t s,
+                               const ElemBox* ebox) {
     const long long n = (long long)nnodes * nelem_color;
     if (n == 0) return cudaSuccess;
     const int bs = 256;
@@ -1747,11 +1876,11 @@ cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, c
     if (ennd == 8)
         k_pair_window<8><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo, nnodes, ph,
                                              mode, level_last, level_cap, step_n, select, pairs,
-                                             counts);
+                                             counts, ebox);
     else
         k_pair_window<4><<<grid, bs, 0, s>>>(coords, ien, elems, nelem_color, node_lo, nnodes, ph,
                                              mode, level_last, level_cap, step_n, select, pairs,
-                                             counts);
+                                             counts, ebox);
     return cudaGetLastError();
 }
 
@@ -1882,22 +2011,28 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
-                         bool fast, const float* geomf) {
+                         bool fast, const float* geomf, const float* coordf,
+                         const ElemBox* ebox) {
     if (nnodes == 0) return cudaSuccess;
+    // the FP32 path's constants, as cterm_node's FP64 ones rounded once
+    const float onem2nu_f = (float)(1 - 2 * ph.nu);
+    const float kscale_f = (float)((0.5 * ph.dt) / (-(8 * M_PI) * (1 - ph.nu)));
     if (ennd == 8) {
         if (fast)
             k_cterm<8, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
-                                                    cbuf, nullptr);
+                                                    cbuf, nullptr, nullptr, ebox, onem2nu_f,
+                                                    kscale_f);
         else
             k_cterm<8, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf, nullptr);
+                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f);
     } else {
         if (fast)
             k_cterm<4, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
-                                                    cbuf, geomf);
+                                                    cbuf, geomf, coordf, ebox, onem2nu_f,
+                                                    kscale_f);
         else
             k_cterm<4, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf, nullptr);
+                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f);
     }
     return cudaGetLastError();
 }

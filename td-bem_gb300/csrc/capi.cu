@@ -268,7 +268,7 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
         const int pw = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, nn, c->ph, mode,
                                     level_last, level_cap, step_n, select, c->d_pairs,
-                                    c->d_counts, c->stream));
+                                    c->d_counts, c->stream, c->d_ebox));
         CUDA_TRY(exclusive_scan(c->d_counts, c->d_offsets, npairs, c->d_scan_tmp,
                                 c->scan_tmp_bytes, c->stream));
         prof_end(c, pw, 0, 0);
@@ -399,6 +399,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(dalloc(&c->d_color_elems, order.size()));
     CTX_TRY(dalloc(&c->d_color_start, c->color_start.size()));
     CTX_TRY(dalloc(&c->d_far_items, 3));
+    CTX_TRY(dalloc(&c->d_ebox, c->nel));
     CTX_TRY(cudaMemcpyAsync(c->d_coords, c->h_coords.data(), sizeof(double) * c->h_coords.size(),
                             cudaMemcpyHostToDevice, c->stream));
     {  // node coordinates as FP32 pairs x = hi + lo for the FP32 far form
@@ -427,6 +428,7 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
                             cudaMemcpyHostToDevice, c->stream));
     CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, ennd, nq, c->d_gx, c->d_gw,
                               c->d_geom, c->d_geomf, c->stream));
+    CTX_TRY(launch_element_box(c->d_coords, c->d_ien, ennd, c->nel, c->d_ebox, c->stream));
     c->pair_cap = std::min<size_t>((size_t)c->nnd * max_color, (size_t)1 << 26);
     c->pair_cap = std::max<size_t>(c->pair_cap, (size_t)max_color);
     CTX_TRY(dalloc(&c->d_pairs, c->pair_cap));
@@ -458,6 +460,7 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_cterm);
     dfree(c->d_geomf);
     dfree(c->d_coordf);
+    dfree(c->d_ebox);
     dfree(c->d_color_elems);
     dfree(c->d_color_start);
     dfree(c->d_far_items);
@@ -544,7 +547,8 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
         rc = assemble_color(c, (int)col, node_lo, nn, ASM_STEP, step, 1 << 30, step, SEL_ALL, out);
     if (rc == TDBEM_OK && step == 1) {
         e = launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
-                         c->d_geom, c->ph, c->d_cterm, c->stream);
+                         c->d_geom, c->ph, c->d_cterm, c->stream, false, nullptr, nullptr,
+                         c->d_ebox);
         if (e == cudaSuccess)
             e = launch_cterm_apply(c->d_cterm, node_lo, nn, c->dt, c->if_ext, ASM_STEP, out,
                                    c->stream);
@@ -606,7 +610,8 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         }
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
-                              c->d_geom, c->ph, c->d_cterm, c->stream));
+                              c->d_geom, c->ph, c->d_cterm, c->stream, false, nullptr, nullptr,
+                              c->d_ebox));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, out,
                                     c->stream));
         prof_end(c, pc, 0, 0);
@@ -657,7 +662,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pw = prof_begin(c, TDBEM_K_AUX);
             CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
                                         c->nnd, c->ph, ASM_LEVELS, last, 1, 0, SEL_FAR,
-                                        c->d_far_pairs, nullptr, c->stream));
+                                        c->d_far_pairs, nullptr, c->stream, c->d_ebox));
             prof_end(c, pw, 0, 0);
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,
@@ -673,7 +678,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
                               c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true,
-                              c->d_geomf));
+                              c->d_geomf, c->d_coordf, c->d_ebox));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
                                     c->stream));
         prof_end(c, pc, 0, 0);
@@ -720,7 +725,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
             const int pw = prof_begin(c, TDBEM_K_AUX);
             CUDA_TRY(launch_pair_window(c->d_coords, c->d_ien, 4, c->d_color_elems, c->nel, 0,
                                         c->nnd, c->ph, ASM_LEVELS, last, c->M, 2, SEL_FAR,
-                                        c->d_far_pairs, nullptr, c->stream));
+                                        c->d_far_pairs, nullptr, c->stream, c->d_ebox));
             prof_end(c, pw, 0, 0);
             const int pe = prof_begin(c, TDBEM_K_ASSEMBLE_F32);
             CUDA_TRY(launch_assemble_far_rows(c->d_coords, c->d_ien, c->d_color_elems,

@@ -168,7 +168,8 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
             const int cn = std::min(chunk, node_hi - n0 + 1);
             const unsigned npairs = (unsigned)((size_t)cn * ne);
             NA_TRY(launch_pair_window(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, cn, c->ph,
-                                      ASM_STEP, step, 1 << 30, step, SEL_ALL, pairs, nullptr, s));
+                                      ASM_STEP, step, 1 << 30, step, SEL_ALL, pairs, nullptr, s,
+                                      c->d_ebox));
             NA_TRY(launch_assemble_step_pairs(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
                                               c->d_gx, c->d_gw, c->d_geom, c->ph, step, pairs,
                                               npairs, out, s));
@@ -178,7 +179,7 @@ extern "C" int tdbem_gh_driver_noalloc(const tdbem_ctx* c, int step, int node_lo
         for (int n0 = node_lo; n0 <= node_hi; n0 += max_nodes) {
             const int cn = std::min(max_nodes, node_hi - n0 + 1);
             NA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, n0, cn, c->nq, c->d_gx, c->d_gw,
-                                c->d_geom, c->ph, cbuf, s));
+                                c->d_geom, c->ph, cbuf, s, false, nullptr, nullptr, c->d_ebox));
             AsmOut o2 = out;
             // rows of this chunk inside the caller's row block
             const size_t shift = (size_t)3 * (n0 - node_lo) * c->D;

@@ -26,6 +26,11 @@ struct Phys {
 };
 
 // Level-window bounds of one (collocation node, element) pair.
+// An element's node centroid and largest node distance from it (launch_element_box).
+struct alignas(32) ElemBox {
+    double x, y, z, rad;
+};
+
 struct PairInfo {
     int klo;    // first level with a possibly non-zero contribution
     int cnt;    // number of levels (0 = pair contributes nothing)
@@ -69,10 +74,15 @@ struct AsmOut {
 cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int ennd, int nq,
                               const double* gx, const double* gw, double* geom, float* geomf,
                               cudaStream_t s);
+// Per element: node centroid and largest node distance from it (x, y, z, radius).
+cudaError_t launch_element_box(const double* coords, const int* ien, int ennd, int nel,
+                               ElemBox* ebox, cudaStream_t s);
+// ebox: launch_element_box's table of the mesh (or null: computed per pair).
 cudaError_t launch_pair_window(const double* coords, const int* ien, int ennd, const int* elems,
                                int nelem_color, int node_lo, int nnodes, const Phys& ph,
                                int mode, int level_last, int level_cap, int step_n, int select,
-                               PairInfo* pairs, unsigned* counts, cudaStream_t s);
+                               PairInfo* pairs, unsigned* counts, cudaStream_t s,
+                               const ElemBox* ebox = nullptr);
 cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd,
                                   const int* elems, int nelem_color, int node_lo, int nq,
                                   const double* gx, const double* gw, const double* geom,
@@ -113,7 +123,8 @@ cudaError_t launch_assemble_far_rows(const double* coords, const int* ien,
 cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel, int node_lo,
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
-                         bool fast = false, const float* geomf = nullptr);
+                         bool fast = false, const float* geomf = nullptr,
+                         const float* coordf = nullptr, const ElemBox* ebox = nullptr);
 cudaError_t launch_cast_levels01(const double* G01, const double* H01, int D, int ldf, float* Gf,
                                  float* Hf, cudaStream_t s);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
@@ -461,6 +472,7 @@ struct tdbem_ctx {
     double* d_cterm = nullptr;       // C term of every node, nnd x 9
     float* d_geomf = nullptr;        // FP32 copy of the geometry (element-relative points)
     float* d_coordf = nullptr;       // node coordinates as FP32 pairs: hi[3], 0, lo[3], 0
+    tdbem::ElemBox* d_ebox = nullptr;      // per element: node centroid, node radius (launch_element_box)
     // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
     std::vector<int> color_start;
     int* d_color_elems = nullptr;
