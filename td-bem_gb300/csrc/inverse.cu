@@ -985,7 +985,7 @@ constexpr int kStepTM = 128, kStepTN = 64, kStepKH = 32;
 constexpr int kStepLP = kStepTM + 4, kStepLT = kStepTN + 4;
 constexpr int kStepSmem = kStepKH * (kStepLP + kStepLT) * (int)sizeof(float);
 
-__global__ void __launch_bounds__(128) k_panel_step_f32(float* __restrict__ A, int n, int k0,
+__global__ void __launch_bounds__(128, 4) k_panel_step_f32(float* __restrict__ A, int n, int k0,
                                                         int bw, const float* __restrict__ B,
                                                         const float* __restrict__ Pc, int ld,
                                                         const int* __restrict__ status) {
@@ -1031,6 +1031,37 @@ __global__ void __launch_bounds__(128) k_panel_step_f32(float* __restrict__ A, i
 #pragma unroll
                 for (int b = 0; b < 8; b++) acc[a][b] = fmaf(pa[a], tb[b], acc[a][b]);
         }
+    }
+    // A tile inside the matrix that meets neither the pivot rows nor the pivot columns
+    // (most tiles): every entry is A - acc, read and written as float pairs (n even:
+    // a row's pairs start on 8-byte boundaries), four rows' reads before their writes.
+    const bool interior = (n % 2 == 0) && i0 + kStepTM <= n && j0 + kStepTN <= n &&
+                          (i0 >= k0 + bw || i0 + kStepTM <= k0) &&
+                          (j0 >= k0 + bw || j0 + kStepTN <= k0);
+    if (interior) {
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+            float2 cv[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const float* row = A + (size_t)(i0 + ty * 4 + r + g * 64) * n + j0 + tx * 4;
+#pragma unroll
+                for (int h = 0; h < 4; h++)
+                    cv[r][h] = *reinterpret_cast<const float2*>(row + (h >> 1) * 32 + (h & 1) * 2);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int a = r + 4 * g;
+                float* row = A + (size_t)(i0 + ty * 4 + r + g * 64) * n + j0 + tx * 4;
+#pragma unroll
+                for (int h = 0; h < 4; h++) {
+                    const int b = (h >> 1) * 4 + (h & 1) * 2;
+                    *reinterpret_cast<float2*>(row + (h >> 1) * 32 + (h & 1) * 2) =
+                        make_float2(cv[r][h].x - acc[a][b], cv[r][h].y - acc[a][b + 1]);
+                }
+            }
+        }
+        return;
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
