@@ -204,49 +204,52 @@ __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, i
 // y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
 // row, pairs of columns per load when D is even.  v is FP32: converting an FP64
 // vector in every row would put D^2 conversions on GB300's narrow FP64 pipe.
-__global__ void __launch_bounds__(256) k_gemv_f32(const float* __restrict__ A, int D,
-                                                  const float* __restrict__ v,
-                                                  double* __restrict__ y, int accumulate,
-                                                  StateUpdate upd) {
+// A load of the step's FP32 inverse, with an L2 evict-last policy: every step's
+// solve reads the whole inverse (85 MB at D = 4614, under GB300's 129 MB L2), and
+// streaming loads (evict-first) would give its lines up first.  Measured on the
+// 4614-DOF march: 41.3 ms with streaming loads, 41.1 ms with these.
+__device__ __forceinline__ float2 ld_keep(const float2* p, unsigned long long pol) {
+    float2 v;
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+
+// y = A v (accumulate: y += A v), a warp per row.  A row's loads go out in batches of
+// kGemvBatch 8-byte loads per lane, all in flight together: at D = 4614 (2307 pairs
+// a row) three batches, three round trips to memory per warp.  128-thread blocks of
+// at most 64 registers keep 32 warps on every SM: the 4614 rows' warps are resident
+// at once.
+constexpr int kGemvBatch = 26;
+__global__ void __launch_bounds__(128, 8) k_gemv_f32(const float* __restrict__ A, int D,
+                                                     const float* __restrict__ v,
+                                                     double* __restrict__ y, int accumulate,
+                                                     StateUpdate upd) {
     const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (row >= D) return;
     const float* a = A + (size_t)row * D;
     float acc = 0.f;
     if ((D & 1) == 0) {
-        // sixteen independent 8-byte loads per lane in flight (a warp per row leaves
-        // too few bytes in flight to cover HBM latency with fewer: four measured
-        // 3.7 TB/s at D = 4614)
         const float2* a2 = reinterpret_cast<const float2*>(a);
         const float2* v2 = reinterpret_cast<const float2*>(v);
         const int n2 = D / 2;
-        float c[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        int j = lane;
-        for (; j + 480 < n2; j += 512) {
-            float2 x[16];
+        unsigned long long pol;
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int base = lane; base < n2; base += 32 * kGemvBatch) {
+            float2 x[kGemvBatch];
 #pragma unroll
-            for (int u = 0; u < 16; u++) x[u] = __ldcs(a2 + j + 32 * u);
+            for (int u = 0; u < kGemvBatch; u++) {
+                const int j = base + 32 * u;
+                x[u] = j < n2 ? ld_keep(a2 + j, pol) : make_float2(0.f, 0.f);
+            }
 #pragma unroll
-            for (int u = 0; u < 16; u++) {
-                const float2 w = v2[j + 32 * u];
-                c[u & 7] += x[u].x * w.x + x[u].y * w.y;
+            for (int u = 0; u < kGemvBatch; u++) {
+                const int j = base + 32 * u;
+                const float2 w = j < n2 ? v2[j] : make_float2(0.f, 0.f);
+                c[u & 3] += x[u].x * w.x + x[u].y * w.y;
             }
         }
-        for (; j + 224 < n2; j += 256) {
-            float2 x[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) x[u] = __ldcs(a2 + j + 32 * u);
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const float2 w = v2[j + 32 * u];
-                c[u] += x[u].x * w.x + x[u].y * w.y;
-            }
-        }
-        for (; j < n2; j += 32) {
-            const float2 x = __ldcs(a2 + j);
-            const float2 w = v2[j];
-            c[0] += x.x * w.x + x.y * w.y;
-        }
-        acc = ((c[0] + c[1]) + (c[2] + c[3])) + ((c[4] + c[5]) + (c[6] + c[7]));
+        acc = (c[0] + c[1]) + (c[2] + c[3]);
     } else {
         for (int j = lane; j < D; j += 32) acc += __ldcs(a + j) * v[j];
     }
@@ -371,13 +374,13 @@ cudaError_t launch_reduce_cols_n(const double* partial, int nchunks, int nb, int
 cudaError_t launch_solve_mixed(const float* inv32, const double* A64, int D, const double* rhs,
                                double* x, double* r, float* v32, int n_refine, cudaStream_t s,
                                bool v32_ready, const StateUpdate& upd) {
-    const unsigned g = (D * 32 + 255) / 256;
+    const unsigned g = (D * 32 + 255) / 256, gv = (D * 32 + 127) / 128;
     const StateUpdate none;
     if (!v32_ready) k_to_f32<<<(D + 255) / 256, 256, 0, s>>>(rhs, v32, D);
-    k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 0, n_refine == 0 ? upd : none);
+    k_gemv_f32<<<gv, 128, 0, s>>>(inv32, D, v32, x, 0, n_refine == 0 ? upd : none);
     for (int it = 0; it < n_refine; it++) {
         k_residual_f64<<<g, 256, 0, s>>>(A64, D, x, rhs, r, v32);
-        k_gemv_f32<<<g, 256, 0, s>>>(inv32, D, v32, x, 1, it == n_refine - 1 ? upd : none);
+        k_gemv_f32<<<gv, 128, 0, s>>>(inv32, D, v32, x, 1, it == n_refine - 1 ? upd : none);
     }
     return cudaGetLastError();
 }
