@@ -561,6 +561,37 @@ __device__ __forceinline__ PairInfo pair_window_info(const double* __restrict__ 
     return pi;
 }
 
+// The Duffy points of every (element, corner) of a 4-node mesh, as duffy_point gives
+// them (x, n, wJ, N in the geometry table's layout): t = ((e * 4 + corner) * 2 nq^2 +
+// point).  The singular pairs' quadrature (near field at every level, C term) reads
+// them instead of mapping each point again in FP64.
+__global__ void k_duffy_table(const double* __restrict__ coords, const int* __restrict__ ien,
+                              int nel, int nq, const double* __restrict__ gx,
+                              const double* __restrict__ gw, double* __restrict__ duffy) {
+    const int nq2 = nq * nq, per = 2 * nq2;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)nel * 4 * per) return;
+    const int qq = (int)(t % per);
+    const long long ec = t / per;
+    const int corner = (int)(ec % 4), e = (int)(ec / 4);
+    double cn[12];
+    for (int a = 0; a < 4; a++) {
+        const int nid = ien[e * 4 + a];
+        for (int d = 0; d < 3; d++) cn[a * 3 + d] = coords[nid * 3 + d];
+    }
+    const int tri = qq / nq2, q = qq % nq2, q1 = q / nq, q2 = q % nq;
+    double N[4], xq[3], nv[3], wJ;
+    duffy_point(cn, corner, tri, gx[q1], gx[q2], gw[q1] * gw[q2], N, xq, nv, wJ);
+    double* g = duffy + t * kGeomStride;
+    for (int d = 0; d < 3; d++) {
+        g[d] = xq[d];
+        g[3 + d] = nv[d];
+    }
+    g[6] = wJ;
+    for (int a = 0; a < 4; a++) g[7 + a] = N[a];
+    g[11] = 0;
+}
+
 template <int ENND>
 __global__ void k_element_box(const double* __restrict__ coords, const int* __restrict__ ien,
                               int nel, ElemBox* __restrict__ ebox) {
@@ -604,7 +635,8 @@ __device__ __forceinline__ void assemble_item(
     const int* __restrict__ elems, int ne, int node_lo, int nq, const double* __restrict__ gx,
     const double* __restrict__ gw, const double* __restrict__ geom, const Phys& ph,
     int level_last, int step_n, int part, const PairInfo& pi, unsigned p, int k,
-    const AsmOut& out, int half = 0, int sub = 0, int L = 1) {
+    const AsmOut& out, int half = 0, int sub = 0, int L = 1,
+    const double* __restrict__ duffy = nullptr) {
     const int c = node_lo + (int)(p / ne);
     const int e = elems[p % ne];
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
@@ -675,6 +707,16 @@ __device__ __forceinline__ void assemble_item(
                         if (slot[i] == a) N[a] = N4[i];
                 gauss_point(acc, tc, ph, xc, xq, nqv, wJ, N);
             }
+        }
+    } else if (duffy) {
+        // the element's Duffy points from this corner, made once per mesh
+        const double* g0 = duffy + ((size_t)e * 4 + pi.sing) * 2 * nq2 * kGeomStride;
+        for (int qq = sub; qq < 2 * nq2; qq += L) {
+            const double* g = g0 + (size_t)qq * kGeomStride;
+            const double xq[3] = {__ldg(g), __ldg(g + 1), __ldg(g + 2)};
+            const double nqv[3] = {__ldg(g + 3), __ldg(g + 4), __ldg(g + 5)};
+            const double N[4] = {__ldg(g + 7), __ldg(g + 8), __ldg(g + 9), __ldg(g + 10)};
+            gauss_point(acc, tc, ph, xc, xq, nqv, __ldg(g + 6), N);
         }
     } else {
         double cn[12];
@@ -774,7 +816,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(
     const double* __restrict__ gw, const double* __restrict__ geom, Phys ph, int level_last,
     int step_n, int part, const PairInfo* __restrict__ pairs,
     const unsigned* __restrict__ offsets, unsigned npairs, unsigned nitems, AsmOut out,
-    int lg) {
+    int lg, const double* __restrict__ duffy) {
     constexpr int SH = ENND == 8 ? 1 : 0;
     unsigned p;
     if (!item_pair(offsets, npairs, nitems, p, SH + lg)) return;
@@ -784,7 +826,7 @@ __global__ void __launch_bounds__(128) k_assemble_items(
     const int k = pi.klo + (int)((unit >> SH) - __ldg(offsets + p));
     assemble_item<MODE, ENND>(coords, ien, elems, ne, node_lo, nq, gx, gw, geom, ph, level_last,
                               step_n, part, pi, p, k, out, (int)(unit & SH),
-                              (int)(gid & ((1u << lg) - 1)), 1 << lg);
+                              (int)(gid & ((1u << lg) - 1)), 1 << lg, duffy);
 }
 
 // One step (ASM_STEP) without compaction: one thread per pair (two for an 8-node
@@ -1564,7 +1606,8 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
                                            const float* __restrict__ geomf = nullptr,
                                            const float* __restrict__ coordf = nullptr,
                                            const ElemBox* __restrict__ ebox = nullptr,
-                                           float onem2nu_f = 0.f, float kscale_f = 0.f) {
+                                           float onem2nu_f = 0.f, float kscale_f = 0.f,
+                                           const double* __restrict__ duffy = nullptr) {
     const double xc[3] = {coords[c * 3], coords[c * 3 + 1], coords[c * 3 + 2]};
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float s32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, e32[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -1701,6 +1744,13 @@ __device__ __forceinline__ void cterm_node(const double* __restrict__ coords,
         for (int t = threadIdx.x; t < total * slots; t += blockDim.x) {
             const int code = s_sing[t / slots], qq = t % slots;
             const int es = code >> 3, sg = code & 7;
+            if (ENND == 4 && duffy) {  // the mesh's Duffy table
+                const double* g = duffy + (((size_t)es * 4 + sg) * slots + qq) * kGeomStride;
+                const double xq[3] = {__ldg(g), __ldg(g + 1), __ldg(g + 2)};
+                const double nv[3] = {__ldg(g + 3), __ldg(g + 4), __ldg(g + 5)};
+                kelvin64(xq, nv, __ldg(g + 6));
+                continue;
+            }
             int ids[2][4] = {{0, 1, 2, 3}, {0, 1, 2, 3}}, cid[2] = {sg, sg};
             int nsub = 1;
             if (ENND == 8) nsub = q8_subelements(sg, ids, cid);
@@ -1744,10 +1794,11 @@ __global__ void __launch_bounds__(256) k_cterm(const double* __restrict__ coords
                                                const float* __restrict__ geomf,
                                                const float* __restrict__ coordf,
                                                const ElemBox* __restrict__ ebox,
-                                               float onem2nu_f, float kscale_f) {
+                                               float onem2nu_f, float kscale_f,
+                                               const double* __restrict__ duffy) {
     cterm_node<ENND, FAST>(coords, ien, nel, node_lo + blockIdx.x, nq, gx, gw, geom, ph,
                            cbuf + (size_t)blockIdx.x * 9, geomf, coordf, ebox, onem2nu_f,
-                           kscale_f);
+                           kscale_f, duffy);
 }
 
 // Add C (+ the exterior free term 0.5 dt I, ElastoDynamicsT.cpp:212-225) to the
@@ -1852,6 +1903,20 @@ cudaError_t launch_gauss_geom(const double* coords, const int* ien, int nel, int
     return cudaGetLastError();
 }
 
+size_t duffy_table_elems(int nel, int nq) {
+    return (size_t)nel * 4 * 2 * nq * nq * kGeomStride;
+}
+
+cudaError_t launch_duffy_table(const double* coords, const int* ien, int nel, int nq,
+                               const double* gx, const double* gw, double* duffy,
+                               cudaStream_t s) {
+    const long long n = (long long)nel * 4 * 2 * nq * nq;
+    if (n == 0) return cudaSuccess;
+    k_duffy_table<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(coords, ien, nel, nq, gx, gw,
+                                                              duffy);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_element_box(const double* coords, const int* ien, int ennd, int nel,
                                ElemBox* ebox, cudaStream_t s) {
     if (nel == 0) return cudaSuccess;
@@ -1890,7 +1955,7 @@ static void launch_items_fp64(const double* coords, const int* ien, const int* e
                               const double* gw, const double* geom, const Phys& ph, int mode,
                               int level_last, int step_n, const PairInfo* pairs,
                               const unsigned* offsets, unsigned npairs, unsigned nitems,
-                              const AsmOut& out, cudaStream_t s) {
+                              const AsmOut& out, cudaStream_t s, const double* duffy) {
     const int bs = 128;
     // Lanes per item: a launch of few items (the near field of one colour: a few
     // thousand) would hold a handful of blocks, each thread summing 36-72 FP64 Gauss
@@ -1911,12 +1976,12 @@ static void launch_items_fp64(const double* coords, const int* ien, const int* e
     if (mode == ASM_LEVELS) {
         k_assemble_items<ASM_LEVELS, ENND><<<grid, bs, 0, s>>>(
             coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last, step_n, 0,
-            pairs, offsets, npairs, nitems, out, lg);
+            pairs, offsets, npairs, nitems, out, lg, duffy);
     } else {
         for (int part = 0; part < 2; part++)
             k_assemble_items<ASM_STEP, ENND><<<grid, bs, 0, s>>>(
                 coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, level_last,
-                step_n, part, pairs, offsets, npairs, nitems, out, lg);
+                step_n, part, pairs, offsets, npairs, nitems, out, lg, duffy);
     }
 }
 
@@ -1926,14 +1991,14 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
                                   const Phys& ph, int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  cudaStream_t s) {
+                                  cudaStream_t s, const double* duffy) {
     if (nitems == 0) return cudaSuccess;
     if (ennd == 8) {
         launch_items_fp64<8>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
-                             level_last, step_n, pairs, offsets, npairs, nitems, out, s);
+                             level_last, step_n, pairs, offsets, npairs, nitems, out, s, nullptr);
     } else {
         launch_items_fp64<4>(coords, ien, elems, nelem_color, node_lo, nq, gx, gw, geom, ph, mode,
-                             level_last, step_n, pairs, offsets, npairs, nitems, out, s);
+                             level_last, step_n, pairs, offsets, npairs, nitems, out, s, duffy);
     }
     return cudaGetLastError();
 }
@@ -2012,7 +2077,7 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
                          bool fast, const float* geomf, const float* coordf,
-                         const ElemBox* ebox) {
+                         const ElemBox* ebox, const double* duffy) {
     if (nnodes == 0) return cudaSuccess;
     // the FP32 path's constants, as cterm_node's FP64 ones rounded once
     const float onem2nu_f = (float)(1 - 2 * ph.nu);
@@ -2021,18 +2086,20 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel
         if (fast)
             k_cterm<8, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
                                                     cbuf, nullptr, nullptr, ebox, onem2nu_f,
-                                                    kscale_f);
+                                                    kscale_f, nullptr);
         else
             k_cterm<8, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f);
+                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f,
+                                                     nullptr);
     } else {
         if (fast)
             k_cterm<4, true><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom, ph,
                                                     cbuf, geomf, coordf, ebox, onem2nu_f,
-                                                    kscale_f);
+                                                    kscale_f, duffy);
         else
             k_cterm<4, false><<<nnodes, 256, 0, s>>>(coords, ien, nel, node_lo, nq, gx, gw, geom,
-                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f);
+                                                     ph, cbuf, nullptr, nullptr, ebox, 0.f, 0.f,
+                                                     duffy);
     }
     return cudaGetLastError();
 }

@@ -323,7 +323,7 @@ int assemble_color(tdbem_ctx* c, int color, int node_lo, int nnodes, int mode, i
         CUDA_TRY(launch_assemble_items(c->d_coords, c->d_ien, c->ennd, elems, ne, n0, c->nq,
                                        c->d_gx, c->d_gw, c->d_geom, c->ph, mode, level_last,
                                        step_n, c->d_pairs, c->d_offsets, npairs, nitems, out,
-                                       c->stream));
+                                       c->stream, c->d_duffy));
         if (nitems) c->launches += (mode == ASM_STEP ? 2 : 1);
         const double pts = (double)c->nq * c->nq;
         const double items = (double)nitems * (mode == ASM_STEP ? 2.0 : 1.0);
@@ -468,6 +468,13 @@ int tdbem_ctx_create(const tdbem_mesh* mesh, const tdbem_material* mat, double d
     CTX_TRY(launch_gauss_geom(c->d_coords, c->d_ien, c->nel, ennd, nq, c->d_gx, c->d_gw,
                               c->d_geom, c->d_geomf, c->stream));
     CTX_TRY(launch_element_box(c->d_coords, c->d_ien, ennd, c->nel, c->d_ebox, c->stream));
+    // 4-node meshes: the singular pairs' Duffy points, once (skipped above 512 MB: the
+    // kernels then map each point themselves)
+    if (ennd == 4 && duffy_table_elems(c->nel, nq) * sizeof(double) <= (size_t(512) << 20)) {
+        CTX_TRY(dalloc(&c->d_duffy, duffy_table_elems(c->nel, nq)));
+        CTX_TRY(launch_duffy_table(c->d_coords, c->d_ien, c->nel, nq, c->d_gx, c->d_gw,
+                                   c->d_duffy, c->stream));
+    }
     c->pair_cap = std::min<size_t>((size_t)c->nnd * max_color, (size_t)1 << 26);
     c->pair_cap = std::max<size_t>(c->pair_cap, (size_t)max_color);
     CTX_TRY(dalloc(&c->d_pairs, c->pair_cap));
@@ -500,6 +507,7 @@ int tdbem_ctx_destroy(tdbem_ctx* c) {
     dfree(c->d_geomf);
     dfree(c->d_coordf);
     dfree(c->d_ebox);
+    dfree(c->d_duffy);
     dfree(c->d_color_elems);
     dfree(c->d_color_start);
     dfree(c->d_far_items);
@@ -587,7 +595,7 @@ int tdbem_gh_driver(tdbem_ctx* c, int step, int node_lo, int node_hi, double* G_
     if (rc == TDBEM_OK && step == 1) {
         e = launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, node_lo, nn, c->nq, c->d_gx, c->d_gw,
                          c->d_geom, c->ph, c->d_cterm, c->stream, false, nullptr, nullptr,
-                         c->d_ebox);
+                         c->d_ebox, c->d_duffy);
         if (e == cudaSuccess)
             e = launch_cterm_apply(c->d_cterm, node_lo, nn, c->dt, c->if_ext, ASM_STEP, out,
                                    c->stream);
@@ -650,7 +658,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx, c->d_gw,
                               c->d_geom, c->ph, c->d_cterm, c->stream, false, nullptr, nullptr,
-                              c->d_ebox));
+                              c->d_ebox, c->d_duffy));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, out,
                                     c->stream));
         prof_end(c, pc, 0, 0);
@@ -714,7 +722,7 @@ int tdbem_assemble_levels(tdbem_ctx* c, int nsteps, int precision) {
         const int pc = prof_begin(c, TDBEM_K_AUX);
         CUDA_TRY(launch_cterm(c->d_coords, c->d_ien, c->ennd, c->nel, 0, c->nnd, c->nq, c->d_gx,
                               c->d_gw, c->d_geom, c->ph, c->d_cterm, c->stream, true,
-                              c->d_geomf, c->d_coordf, c->d_ebox));
+                              c->d_geomf, c->d_coordf, c->d_ebox, c->d_duffy));
         CUDA_TRY(launch_cterm_apply(c->d_cterm, 0, c->nnd, c->dt, c->if_ext, ASM_LEVELS, o64,
                                     c->stream));
         prof_end(c, pc, 0, 0);
@@ -971,6 +979,10 @@ int tdbem_footprint(const tdbem_mesh* mesh, const tdbem_material* mat, double dt
     size_t b = 24 * (size_t)mesh->nnd + 4 * (ennd + 1) * nel + q2 * nel * 16 * 8 +
                72 * (size_t)mesh->nnd +
                pair_cap * (sizeof(PairInfo) + 8) + pair_cap / 8 + ((size_t)1 << 16);  // + scan
+    // element boxes; the Duffy table of a 4-node mesh (when made: up to 512 MB)
+    b += sizeof(ElemBox) * nel;
+    if (ennd == 4 && duffy_table_elems((int)nel, nq) * sizeof(double) <= (size_t(512) << 20))
+        b += duffy_table_elems((int)nel, nq) * sizeof(double);
     // marching state common to both forms: maps, W vectors, partials, histories
     b += 8 * D * 8 + 3 * L * D * 8 + 2 * ((size_t)numstep + 1) * D * 8 + 4 * (D + 64);
     if (precision == TDBEM_FP64) {

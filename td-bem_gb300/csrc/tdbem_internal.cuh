@@ -89,7 +89,14 @@ cudaError_t launch_assemble_items(const double* coords, const int* ien, int ennd
                                   const Phys& ph, int mode, int level_last, int step_n,
                                   const PairInfo* pairs, const unsigned* offsets,
                                   unsigned npairs, unsigned nitems, const AsmOut& out,
-                                  cudaStream_t s);
+                                  cudaStream_t s, const double* duffy = nullptr);
+// The Duffy points of every (element, corner) of a 4-node mesh (kGeomStride doubles
+// each): duffy_table_elems doubles.  duffy (may be null) in the item and C-term
+// launches: the singular pairs read their points from it.
+size_t duffy_table_elems(int nel, int nq);
+cudaError_t launch_duffy_table(const double* coords, const int* ien, int nel, int nq,
+                               const double* gx, const double* gw, double* duffy,
+                               cudaStream_t s);
 // Element interface: n independent (collocation point, element) pairs, element
 // node coordinates ecoords[n][ennd][3], time times[n], singular local node sing[n]
 // (-1: FormGH_Regular); GE1/HE1 (I part), GE2/HE2 (J part) [n][3][3 ennd] and C1 / C2
@@ -124,7 +131,8 @@ cudaError_t launch_cterm(const double* coords, const int* ien, int ennd, int nel
                          int nnodes, int nq, const double* gx, const double* gw,
                          const double* geom, const Phys& ph, double* cbuf, cudaStream_t s,
                          bool fast = false, const float* geomf = nullptr,
-                         const float* coordf = nullptr, const ElemBox* ebox = nullptr);
+                         const float* coordf = nullptr, const ElemBox* ebox = nullptr,
+                         const double* duffy = nullptr);
 cudaError_t launch_cast_levels01(const double* G01, const double* H01, int D, int ldf, float* Gf,
                                  float* Hf, cudaStream_t s);
 cudaError_t launch_cterm_apply(const double* cbuf, int node_lo, int nnodes, double dt,
@@ -473,6 +481,7 @@ struct tdbem_ctx {
     float* d_geomf = nullptr;        // FP32 copy of the geometry (element-relative points)
     float* d_coordf = nullptr;       // node coordinates as FP32 pairs: hi[3], 0, lo[3], 0
     tdbem::ElemBox* d_ebox = nullptr;      // per element: node centroid, node radius (launch_element_box)
+    double* d_duffy = nullptr;       // 4-node meshes: the Duffy points of every (element, corner)
     // element colouring: elements of colour c are color_elems[color_start[c] .. color_start[c+1])
     std::vector<int> color_start;
     int* d_color_elems = nullptr;
