@@ -201,24 +201,25 @@ __global__ void k_reduce_cols(const double* __restrict__ partial, int nchunks, i
     if (v32 && i < D) v32[i] = (float)s;
 }
 
-// y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
-// row, pairs of columns per load when D is even.  v is FP32: converting an FP64
-// vector in every row would put D^2 conversions on GB300's narrow FP64 pipe.
 // A load of the step's FP32 inverse, with an L2 evict-last policy: every step's
 // solve reads the whole inverse (85 MB at D = 4614, under GB300's 129 MB L2), and
 // streaming loads (evict-first) would give its lines up first.  Measured on the
 // 4614-DOF march: 41.3 ms with streaming loads, 41.1 ms with these.
 __device__ __forceinline__ float2 ld_keep(const float2* p, unsigned long long pol) {
     float2 v;
-    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    asm volatile("ld.global.nc.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;"
+                 : "=f"(v.x), "=f"(v.y)
+                 : "l"(p), "l"(pol));
     return v;
 }
 
-// y = A v (accumulate: y += A v), a warp per row.  A row's loads go out in batches of
-// kGemvBatch 8-byte loads per lane, all in flight together: at D = 4614 (2307 pairs
-// a row) three batches, three round trips to memory per warp.  128-thread blocks of
-// at most 64 registers keep 32 warps on every SM: the 4614 rows' warps are resident
-// at once.
+// y = A32 v (+ y if accumulate): FP32 products, FP64 cross-lane sum; warp per
+// row, pairs of columns per load when D is even.  v is FP32: converting an FP64
+// vector in every row would put D^2 conversions on GB300's narrow FP64 pipe.
+// A row's loads go out in batches of kGemvBatch 8-byte loads per lane, all in flight
+// together: at D = 4614 (2307 pairs a row) three batches, three round trips to memory
+// per warp.  128-thread blocks of at most 64 registers keep 32 warps on every SM: the
+// 4614 rows' warps are resident at once.
 constexpr int kGemvBatch = 26;
 __global__ void __launch_bounds__(128, 8) k_gemv_f32(const float* __restrict__ A, int D,
                                                      const float* __restrict__ v,
