@@ -3,6 +3,8 @@
 // conditions and weights, the stepwise level placement, profiling counters.
 // The march engines are in capi_march.cu, the batched march in capi_batch.cu,
 // checkpoints in capi_ckpt.cu and the many-mesh calls in capi_group.cu.
+#include <system_error>
+
 #include "capi_common.cuh"
 
 using namespace tdbem;
@@ -130,8 +132,15 @@ int compute_max_step(const std::vector<double>& x, int nnd, double E, double nu,
         const long long want = pairs * (t + 1) / nt;
         while (hi < nnd && done < want) done += nnd - 1 - hi++;
         if (t == nt - 1) hi = nnd;
-        if (t == nt - 1) part[t] = rows(lo, hi);
-        else th.emplace_back([&, t, lo, hi] { part[t] = rows(lo, hi); });
+        bool started = false;
+        if (t < nt - 1) {
+            try {
+                th.emplace_back([&, t, lo, hi] { part[t] = rows(lo, hi); });
+                started = true;
+            } catch (const std::system_error&) {  // no thread to be had: this share here
+            }
+        }
+        if (!started) part[t] = rows(lo, hi);
         lo = hi;
     }
     for (auto& t : th) t.join();
