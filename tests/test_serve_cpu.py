@@ -48,6 +48,18 @@ def test_footprint_counts_the_level_store(tdlib):
     assert tdlib.footprint(m, tdlib.MIXED, numstep=400) > f32
 
 
+def test_footprint_of_the_bench_sphere(tdlib):
+    """The 1538-node sphere: the largest node distance is searched over 1.2 M pairs on
+    several host threads; the level store follows the mesh's max step (60)."""
+    m = meshes.cubed_sphere(16, numstep=400)
+    M = m.max_step()
+    D = 3 * m.nnd
+    assert M == 60
+    levels64 = 2 * (M + 1) * D * D * 8
+    f64 = tdlib.footprint(m, tdlib.FP64)
+    assert levels64 < f64 < 1.3 * levels64
+
+
 def test_halfspace_cavity_mesh():
     m = meshes.halfspace_cavity(n_sphere=4)
     assert m.nnd == 121 + 6 * 16 + 2 and m.nel == 100 + 6 * 16
